@@ -1,0 +1,197 @@
+/*
+ * nihu_gb300 -- C ABI of the GB300-native dense collocation BEM library.
+ *
+ * One library context drives one GPU (sm_103a) on one CUDA stream.  All
+ * entry points return a status code and never throw; a human-readable message
+ * for the last failure is available from nihu_gb_last_error().  Calls are
+ * synchronous: when a call returns, its results are complete (device or host).
+ *
+ * The entry points replace the following reference interfaces (paths inside
+ * the NiHu project):
+ *   - Res << test_space * Op[trial_space]
+ *       nihu/core/weighted_residual.hpp:197-206 -> integral_transform::test_on_into
+ *       nihu/core/integral_transform.hpp:181-192 -> assembly::eval_into
+ *       nihu/core/assembly.hpp:136-157 (hot loop :69-76, block "+=")
+ *     => nihu_gb_assemble()
+ *   - create_mesh(nodes, elements, tags...)  nihu/core/mesh.hpp:175-193,285-290
+ *     => nihu_gb_mesh_create()
+ *   - identity_integral_operator, (alpha * I)[space]
+ *       nihu/core/single_integral.hpp:146-180, nihu/core/integral_operator.hpp:215-238
+ *     => nihu_gb_add_identity()
+ *   - dense matvec inside Eigen::GMRES  nihu/fmm/GMRES.h:57-205
+ *     => nihu_gb_matvec(), nihu_gb_gmres()
+ *   - colPivHouseholderQr().solve()  nihu/applications/helmholtz/helmholtz_3d_coll.cpp:113
+ *     => nihu_gb_lu_solve()
+ *
+ * Matrices are column-major (Eigen's default), row = test DOF, column = trial
+ * DOF, leading dimension ld >= number of rows.  Complex numbers are stored as
+ * interleaved (re, im) pairs: complex64 = 2 x float, complex128 = 2 x double.
+ */
+#ifndef NIHU_GB300_H
+#define NIHU_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum nihu_gb_status {
+    NIHU_GB_OK = 0,
+    NIHU_GB_ERR_INVALID_ARGUMENT = 1, /* std::invalid_argument / logic errors */
+    NIHU_GB_ERR_OUT_OF_RANGE = 2,     /* std::out_of_range (e.g. quadrature degree > 14) */
+    NIHU_GB_ERR_RUNTIME = 3,          /* std::runtime_error (e.g. inverse mapping failed) */
+    NIHU_GB_ERR_CUDA = 4,             /* CUDA runtime failure */
+    NIHU_GB_ERR_OUT_OF_MEMORY = 5,    /* device memory budget exhausted */
+    NIHU_GB_ERR_NOT_CONVERGED = 6,    /* iterative solver hit its iteration limit */
+    NIHU_GB_ERR_NO_DEVICE = 7         /* no usable CUDA device */
+} nihu_gb_status;
+
+/* element type ids (nihu/core/element.hpp:112-118) */
+#define NIHU_GB_TRIA_1 32303
+#define NIHU_GB_QUAD_1 32404
+
+/* kernel families (nihu/library/helmholtz_kernel.hpp, laplace_kernel.hpp) */
+#define NIHU_GB_HELMHOLTZ_3D 0
+#define NIHU_GB_LAPLACE_3D 1
+
+/* operator bit mask: SLP = G, DLP = dG/dn_y (nihu/library/normal_derivative_kernel.hpp) */
+#define NIHU_GB_SLP 1
+#define NIHU_GB_DLP 2
+
+/* storage type of a matrix or vector */
+#define NIHU_GB_C64 0  /* complex64: 2 x float32 */
+#define NIHU_GB_C128 1 /* complex128: 2 x float64 */
+
+/* arithmetic of the regular (far-field) quadrature; singular and nearly
+ * singular integrals are always evaluated in FP64 */
+#define NIHU_GB_REGULAR_FP32 0
+#define NIHU_GB_REGULAR_FP64 1
+
+/* where a buffer lives */
+#define NIHU_GB_HOST 0
+#define NIHU_GB_DEVICE 1
+
+typedef struct nihu_gb_ctx nihu_gb_ctx;
+typedef struct nihu_gb_mesh nihu_gb_mesh;
+
+/* ------------------------------------------------------------------ context */
+
+/* Create a context on `device`.  `stream` is a cudaStream_t to run on, or NULL
+ * for a context-owned stream.  `hbm_budget_bytes` caps the device memory the
+ * context allocates (0 = no cap). */
+nihu_gb_status nihu_gb_ctx_create(int device, void *stream, size_t hbm_budget_bytes, nihu_gb_ctx **out);
+void nihu_gb_ctx_destroy(nihu_gb_ctx *ctx);
+/* message of the last failed call on this context ("" if none) */
+const char *nihu_gb_last_error(const nihu_gb_ctx *ctx);
+/* the cudaStream_t the context launches on */
+void *nihu_gb_ctx_stream(const nihu_gb_ctx *ctx);
+/* device bytes currently held by the context and its meshes */
+size_t nihu_gb_ctx_device_bytes(const nihu_gb_ctx *ctx);
+/* number of kernels this context has launched since creation */
+int64_t nihu_gb_ctx_launch_count(const nihu_gb_ctx *ctx);
+
+/* pinned host memory helpers for fast host<->device transfers */
+nihu_gb_status nihu_gb_host_alloc(nihu_gb_ctx *ctx, size_t bytes, void **out);
+void nihu_gb_host_free(void *ptr);
+/* device memory owned by the caller, charged to the context's budget */
+nihu_gb_status nihu_gb_device_alloc(nihu_gb_ctx *ctx, size_t bytes, void **out);
+void nihu_gb_device_free(nihu_gb_ctx *ctx, void *ptr);
+nihu_gb_status nihu_gb_memcpy(nihu_gb_ctx *ctx, void *dst, int dst_where, const void *src, int src_where, size_t bytes);
+
+/* --------------------------------------------------------------------- mesh */
+
+/* Build a mesh from host arrays (nihu/core/mesh.hpp:175-193):
+ *   nodes: n_nodes x 3 doubles, row-major (x, y, z)
+ *   elems: n_elems x elem_cols int32, row-major; column 0 is the element type
+ *          id (NIHU_GB_TRIA_1 / NIHU_GB_QUAD_1), columns 1.. the corner node
+ *          indices (unused trailing columns are ignored).
+ * Element ids, and so DOF numbers, follow the row order (nihu/core/mesh.hpp:155).
+ * Geometry (centres, sizes, normals, quadrature points) is computed on the GPU
+ * and kept on the device until nihu_gb_mesh_destroy(). */
+nihu_gb_status nihu_gb_mesh_create(nihu_gb_ctx *ctx, const double *nodes, int64_t n_nodes,
+                                   const int32_t *elems, int64_t n_elems, int64_t elem_cols,
+                                   nihu_gb_mesh **out);
+void nihu_gb_mesh_destroy(nihu_gb_mesh *mesh);
+int64_t nihu_gb_mesh_num_elements(const nihu_gb_mesh *mesh);
+
+/* ----------------------------------------------------------------- assembly */
+
+/* Assemble the collocational SLP and/or DLP matrices of a kernel family
+ * between a test mesh (rows, Dirac collocation at element centres) and a trial
+ * mesh (columns, constant elements):
+ *     out_op = alpha * Op            (accumulate == 0)
+ *     out_op = out_op + alpha * Op   (accumulate != 0, NiHu's "<<" semantics)
+ * `ops` is a bit mask of NIHU_GB_SLP / NIHU_GB_DLP; out_slp / out_dlp may be
+ * NULL for operators not requested.  test == trial (same handle) enables the
+ * singular self terms, as NiHu's same-mesh check does
+ * (nihu/core/integral_transform.hpp:156).  k is the real wave number (ignored
+ * for Laplace).  dtype is NIHU_GB_C64 or NIHU_GB_C128; where is NIHU_GB_HOST
+ * or NIHU_GB_DEVICE for both outputs.  Host outputs are assembled in column
+ * panels whose device-to-host copies overlap the next panel's assembly; pinned
+ * host memory (nihu_gb_host_alloc) makes those copies fastest.
+ * Replaces: nihu/core/weighted_residual.hpp:197-206, nihu/core/assembly.hpp:136-157,
+ * per-pair dispatch nihu/core/double_integral.hpp:543-673. */
+nihu_gb_status nihu_gb_assemble(nihu_gb_ctx *ctx, const nihu_gb_mesh *test, const nihu_gb_mesh *trial,
+                                int family, int ops, double k, double alpha_re, double alpha_im,
+                                int precision, int dtype, void *out_slp, void *out_dlp, int64_t ld,
+                                int accumulate, int where);
+
+/* out(i, i) += alpha for every element i (collocational identity operator on
+ * constant elements, nihu/core/single_integral.hpp:146-180).  The matrix is
+ * n x n with n = number of mesh elements. */
+nihu_gb_status nihu_gb_add_identity(nihu_gb_ctx *ctx, const nihu_gb_mesh *mesh, double alpha_re, double alpha_im,
+                                    int dtype, void *out, int64_t ld, int where);
+
+/* Per-pair quadrature statistics of an assembly (no matrix is written):
+ * counts[0] self pairs, counts[1] nearly singular pairs, counts[2 + 3*s + d]
+ * regular pairs whose SLP uses level s and DLP level d (levels 0, 1, 2 =
+ * 1 point / 3-4 points / 6-9 points). */
+nihu_gb_status nihu_gb_pair_statistics(nihu_gb_ctx *ctx, const nihu_gb_mesh *test, const nihu_gb_mesh *trial,
+                                       int64_t counts[11]);
+
+/* ------------------------------------------------------------- linear algebra */
+
+/* y = alpha * A x + beta * y; A is m x n (dtype_a, column-major, lda), x and
+ * y are complex128 vectors.  With dtype_a = NIHU_GB_C64 the products are
+ * formed in FP32 and the column-panel partial sums are added in FP64. */
+nihu_gb_status nihu_gb_matvec(nihu_gb_ctx *ctx, int dtype_a, const void *A, int64_t m, int64_t n, int64_t lda,
+                              const void *x, void *y, double alpha_re, double alpha_im,
+                              double beta_re, double beta_im, int where);
+
+/* Solve A x = b with restarted GMRES(restart) (nihu/fmm/GMRES.h:57-205
+ * semantics: stop when |residual estimate| / |b - A x0| < tol).  A is n x n
+ * (dtype_a) on the device; b and x are complex128 (x holds the initial guess
+ * on entry).  The Arnoldi basis and Givens rotations are FP64; the matvec is
+ * FP32 when dtype_a = NIHU_GB_C64.  iters / rel_residual may be NULL.
+ * Returns NIHU_GB_ERR_NOT_CONVERGED (with x set to the last iterate) when
+ * max_iters is reached first. */
+nihu_gb_status nihu_gb_gmres(nihu_gb_ctx *ctx, int dtype_a, const void *A, int64_t n, int64_t lda,
+                             const void *b, void *x, int restart, int max_iters, double tol,
+                             int *iters, double *rel_residual, int where);
+
+/* Solve A x = b by LU factorisation with partial pivoting in FP64 (complex128
+ * A, n x n, lda).  A is overwritten by its factors when where = DEVICE; a host
+ * A is copied to the device and left unchanged. */
+nihu_gb_status nihu_gb_lu_solve(nihu_gb_ctx *ctx, void *A, int64_t n, int64_t lda, const void *b, void *x,
+                                int where);
+
+/* ------------------------------------------------------- composite solve */
+
+/* Exterior collocation BEM solve of the Helmholtz/Laplace CBIE
+ *     (DLP - 1/2 I) p = SLP q
+ * on one mesh (nihu/applications/helmholtz/helmholtz_3d_coll.cpp:36-120 with
+ * the plain CBIE branch): assembles both matrices (dtype), forms the right-hand
+ * side on the device, and solves with GMRES (solver = 0) or LU (solver = 1,
+ * requires dtype = NIHU_GB_C128).  q and p are complex128 host vectors of
+ * length n.  iters / rel_residual may be NULL. */
+nihu_gb_status nihu_gb_solve_cbie(nihu_gb_ctx *ctx, const nihu_gb_mesh *mesh, int family, double k,
+                                  int precision, int dtype, const void *q, void *p, int solver,
+                                  int restart, int max_iters, double tol, int *iters, double *rel_residual);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* NIHU_GB300_H */

@@ -1,0 +1,21 @@
+"""GB300-native dense collocation BEM (NiHu's collocational SLP/DLP assembly
+and the GMRES matvec) on hand-written sm_103a CUDA kernels behind a C ABI.
+
+The C ABI is declared in ``include/nihu_gb300.h``; ``include/nihu_gb300/nihu.hpp``
+is the C++ front end shaped like NiHu's integral-operator API; this package
+is the Python front end with the same shape.
+"""
+from ._capi import (C64, C128, DEVICE, DLP, HELMHOLTZ_3D, HOST, LAPLACE_3D, QUAD_1, REGULAR_FP32, REGULAR_FP64, SLP,
+                    TRIA_1, InvalidArgumentError, NihuError, NotConvergedError, OutOfRangeError, lib)
+from .api import (Context, DeviceMesh, Mesh, constant_view, create_integral_operator, create_mesh, default_context,
+                  dirac, gmres, helmholtz_3d_DLP_kernel, helmholtz_3d_SLP_kernel, identity_integral_operator,
+                  laplace_3d_DLP_kernel, laplace_3d_SLP_kernel, lu_solve, matvec, pair_statistics, solve_cbie)
+from . import meshes
+
+__all__ = [
+    "C64", "C128", "DEVICE", "DLP", "HELMHOLTZ_3D", "HOST", "LAPLACE_3D", "QUAD_1", "REGULAR_FP32", "REGULAR_FP64",
+    "SLP", "TRIA_1", "InvalidArgumentError", "NihuError", "NotConvergedError", "OutOfRangeError", "lib", "Context",
+    "DeviceMesh", "Mesh", "constant_view", "create_integral_operator", "create_mesh", "default_context", "dirac",
+    "gmres", "helmholtz_3d_DLP_kernel", "helmholtz_3d_SLP_kernel", "identity_integral_operator",
+    "laplace_3d_DLP_kernel", "laplace_3d_SLP_kernel", "lu_solve", "matvec", "pair_statistics", "solve_cbie", "meshes",
+]

@@ -1,0 +1,392 @@
+"""NiHu-shaped Python front end of the GPU library.
+
+Mirrors the reference's user API for the collocation path
+(nihu/core/weighted_residual.hpp, integral_operator.hpp, function_space.hpp,
+mesh.hpp) so code reads like NiHu:
+
+    mesh = create_mesh(nodes, elements)
+    sp = constant_view(mesh)
+    Lop = create_integral_operator(helmholtz_3d_SLP_kernel(k))
+    Ls = np.zeros((n, n), complex, order="F")
+    Ls << dirac(sp) * Lop[sp]          # accumulates, like NiHu's operator<<
+
+Every evaluation runs on the GPU through the C ABI; results land in the
+caller's matrix with "+=" semantics (nihu/util/matrix_block.hpp).
+"""
+from __future__ import annotations
+
+import ctypes
+import weakref
+
+import numpy as np
+
+from . import _capi as C
+
+_default_ctx = None
+
+
+class Context:
+    """One GPU, one stream (nihu_gb_ctx)."""
+
+    def __init__(self, device: int = 0, hbm_budget_bytes: int = 0, stream=None):
+        L = C.lib()
+        h = ctypes.c_void_p()
+        st = L.nihu_gb_ctx_create(device, stream, hbm_budget_bytes, ctypes.byref(h))
+        if st != C.OK:
+            raise C._ERRORS.get(st, C.NihuError)(st, "nihu_gb_ctx_create failed (device %d)" % device)
+        self.handle = h
+        self._meshes = weakref.WeakValueDictionary()
+
+    def close(self):
+        if self.handle:
+            for dm in list(self._meshes.values()):
+                dm.close()
+            C.lib().nihu_gb_ctx_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def stream(self) -> int:
+        return C.lib().nihu_gb_ctx_stream(self.handle) or 0
+
+    @property
+    def device_bytes(self) -> int:
+        return C.lib().nihu_gb_ctx_device_bytes(self.handle)
+
+    @property
+    def launch_count(self) -> int:
+        return C.lib().nihu_gb_ctx_launch_count(self.handle)
+
+    def check(self, status):
+        C.check(self.handle, status)
+
+
+def default_context() -> Context:
+    global _default_ctx
+    if _default_ctx is None or _default_ctx.handle is None:
+        _default_ctx = Context(0)
+    return _default_ctx
+
+
+class DeviceMesh:
+    """A mesh uploaded to a context (nihu_gb_mesh)."""
+
+    def __init__(self, ctx: Context, nodes: np.ndarray, elems: np.ndarray):
+        nodes = np.ascontiguousarray(nodes, dtype=np.float64)
+        elems = np.ascontiguousarray(elems, dtype=np.int32)
+        if nodes.ndim != 2 or nodes.shape[1] != 3 or elems.ndim != 2:
+            raise ValueError("nodes must be (n, 3) and elements (m, cols)")
+        h = ctypes.c_void_p()
+        ctx.check(C.lib().nihu_gb_mesh_create(ctx.handle, nodes.ctypes.data, len(nodes), elems.ctypes.data,
+                                              len(elems), elems.shape[1], ctypes.byref(h)))
+        self.ctx = ctx
+        self.handle = h
+        self.n = len(elems)
+
+    def close(self):
+        if self.handle:
+            C.lib().nihu_gb_mesh_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            if self.ctx.handle:
+                self.close()
+        except Exception:
+            pass
+
+
+class Mesh:
+    """create_mesh(nodes, elements) (nihu/core/mesh.hpp:175-193,285-290).
+
+    ``elements`` rows are [type id, node indices...]; ids run in row order."""
+
+    def __init__(self, nodes, elements):
+        self.nodes = np.ascontiguousarray(nodes, dtype=np.float64)
+        el = np.asarray(elements)
+        if el.shape[1] < 5:
+            pad = np.full((el.shape[0], 5 - el.shape[1]), -1, dtype=np.int32)
+            el = np.hstack([el.astype(np.int32), pad])
+        self.elements = np.ascontiguousarray(el, dtype=np.int32)
+        self._dev = {}
+
+    @property
+    def num_elements(self) -> int:
+        return len(self.elements)
+
+    def device(self, ctx: Context) -> DeviceMesh:
+        key = id(ctx)
+        dm = self._dev.get(key)
+        if dm is None or dm.handle is None:
+            dm = DeviceMesh(ctx, self.nodes, self.elements)
+            self._dev[key] = dm
+            ctx._meshes[id(dm)] = dm
+        return dm
+
+
+def create_mesh(nodes, elements) -> Mesh:
+    return Mesh(nodes, elements)
+
+
+class FunctionSpace:
+    """constant_view(mesh): DOF = element id (nihu/core/function_space.hpp:263)."""
+
+    def __init__(self, mesh: Mesh):
+        self.mesh = mesh
+
+    def get_num_dofs(self) -> int:
+        return self.mesh.num_elements
+
+    def __mul__(self, transform):
+        return _make_wr(self, transform)
+
+
+class DiracSpace:
+    """dirac(space): collocation at element centres (nihu/core/function_space.hpp:355)."""
+
+    def __init__(self, space: FunctionSpace):
+        self.space = space
+        self.mesh = space.mesh
+
+    def get_num_dofs(self) -> int:
+        return self.space.get_num_dofs()
+
+    def __mul__(self, transform):
+        return _make_wr(self, transform)
+
+
+def constant_view(mesh: Mesh) -> FunctionSpace:
+    return FunctionSpace(mesh)
+
+
+def dirac(space: FunctionSpace) -> DiracSpace:
+    return DiracSpace(space)
+
+
+class Kernel:
+    def __init__(self, family: int, op: int, k: float = 0.0, name: str = ""):
+        self.family, self.op, self.k, self.name = family, op, float(k), name
+
+    def get_wave_number(self) -> float:
+        return self.k
+
+
+def helmholtz_3d_SLP_kernel(k: float) -> Kernel:
+    return Kernel(C.HELMHOLTZ_3D, C.SLP, k, "helmholtz_3d_SLP")
+
+
+def helmholtz_3d_DLP_kernel(k: float) -> Kernel:
+    return Kernel(C.HELMHOLTZ_3D, C.DLP, k, "helmholtz_3d_DLP")
+
+
+def laplace_3d_SLP_kernel() -> Kernel:
+    return Kernel(C.LAPLACE_3D, C.SLP, 0.0, "laplace_3d_SLP")
+
+
+def laplace_3d_DLP_kernel() -> Kernel:
+    return Kernel(C.LAPLACE_3D, C.DLP, 0.0, "laplace_3d_DLP")
+
+
+class IntegralOperator:
+    """create_integral_operator(kernel), with scalar scaling (nihu/core/integral_operator.hpp:131-194,324-329)."""
+
+    def __init__(self, kernel: Kernel, scale: complex = 1.0):
+        self.kernel, self.scale = kernel, complex(scale)
+
+    def __rmul__(self, alpha):
+        return IntegralOperator(self.kernel, self.scale * complex(alpha))
+
+    __mul__ = __rmul__
+
+    def __getitem__(self, trial_space):
+        return IntegralTransform(self, trial_space)
+
+
+class IdentityOperator:
+    """identity_integral_operator() (nihu/core/integral_operator.hpp:215-238)."""
+
+    def __init__(self, scale: complex = 1.0):
+        self.scale = complex(scale)
+
+    def __rmul__(self, alpha):
+        return IdentityOperator(self.scale * complex(alpha))
+
+    __mul__ = __rmul__
+
+    def __getitem__(self, trial_space):
+        return IntegralTransform(self, trial_space)
+
+
+def create_integral_operator(kernel: Kernel) -> IntegralOperator:
+    return IntegralOperator(kernel)
+
+
+def identity_integral_operator() -> IdentityOperator:
+    return IdentityOperator()
+
+
+class IntegralTransform:
+    """op[trial_space]; sums of transforms are evaluated term by term."""
+
+    def __init__(self, op, trial_space, terms=None):
+        self.terms = terms if terms is not None else [(op, trial_space)]
+
+    def __add__(self, other):
+        return IntegralTransform(None, None, self.terms + other.terms)
+
+
+def _make_wr(test, transform):
+    if not isinstance(transform, IntegralTransform):
+        return NotImplemented
+    return WeightedResidual(test, transform)
+
+
+def _space_mesh(space):
+    return space.mesh
+
+
+class WeightedResidual:
+    """test_space * Op[trial_space] (nihu/core/weighted_residual.hpp:176-186).
+
+    ``result << wr`` adds the operator matrix into ``result`` in place
+    (nihu/core/weighted_residual.hpp:197-206).  Options (``precision``:
+    "fp32" regular quadrature, the default, or "fp64") can be given with
+    ``wr.eval_into(result, precision=...)``."""
+
+    __array_ufunc__ = None  # make numpy defer ``ndarray << wr`` to __rlshift__
+
+    def __init__(self, test, transform: IntegralTransform):
+        self.test, self.transform = test, transform
+
+    def __rlshift__(self, result):
+        return self.eval_into(result)
+
+    def eval_into(self, result: np.ndarray, precision: str = "fp32", ctx: Context | None = None):
+        ctx = ctx or default_context()
+        if not isinstance(result, np.ndarray) or result.ndim != 2:
+            raise TypeError("result must be a 2D numpy array (a dynamic matrix, nihu/core/result_matrix.hpp)")
+        test_mesh = _space_mesh(self.test)
+        for op, trial_space in self.transform.terms:
+            trial_mesh = _space_mesh(trial_space)
+            m, n = test_mesh.num_elements, trial_mesh.num_elements
+            if result.shape != (m, n):
+                raise ValueError("result is %s, operator is %dx%d" % (result.shape, m, n))
+            if isinstance(op, IdentityOperator):
+                if test_mesh is not trial_mesh:
+                    continue  # the identity only couples coinciding elements of one mesh
+                idx = np.arange(m)
+                result[idx, idx] += op.scale
+                continue
+            _assemble_into(ctx, result, test_mesh, trial_mesh, op.kernel.family, op.kernel.op, op.kernel.k,
+                           op.scale, precision)
+        return result
+
+
+def _assemble_into(ctx, result, test_mesh, trial_mesh, family, op, k, alpha, precision):
+    L = C.lib()
+    if result.dtype == np.complex64:
+        dtype, target = C.C64, result
+    elif result.dtype == np.complex128:
+        dtype, target = C.C128, result
+    elif result.dtype in (np.float32, np.float64) and family == C.LAPLACE_3D and complex(alpha).imag == 0:
+        dtype = C.C64 if result.dtype == np.float32 else C.C128
+        target = None
+    else:
+        raise TypeError("result dtype %s not supported for this kernel" % result.dtype)
+    tdm, rdm = test_mesh.device(ctx), trial_mesh.device(ctx)
+    same = test_mesh is trial_mesh
+    rdm_handle = tdm.handle if same else rdm.handle
+    prec = C.REGULAR_FP64 if precision == "fp64" else C.REGULAR_FP32
+    if target is not None and target.flags.f_contiguous:
+        buf, accumulate = target, 1
+    else:
+        cdt = np.complex64 if dtype == C.C64 else np.complex128
+        buf, accumulate = np.zeros(result.shape, dtype=cdt, order="F"), 0
+    out_s = buf.ctypes.data if op == C.SLP else None
+    out_d = buf.ctypes.data if op == C.DLP else None
+    ctx.check(L.nihu_gb_assemble(ctx.handle, tdm.handle, rdm_handle, family, op, k, alpha.real, alpha.imag, prec,
+                                 dtype, out_s, out_d, max(result.shape[0], 1), accumulate, C.HOST))
+    if buf is not result:
+        if target is None:
+            result += buf.real.astype(result.dtype)
+        else:
+            result += buf
+
+
+# -------------------------------------------------------------- linear algebra
+
+def _c128(v):
+    return np.ascontiguousarray(v, dtype=np.complex128)
+
+
+def matvec(A: np.ndarray, x: np.ndarray, ctx: Context | None = None) -> np.ndarray:
+    """y = A x on the GPU (A complex64 or complex128, Fortran order)."""
+    ctx = ctx or default_context()
+    A = np.asfortranarray(A)
+    dtype = C.C64 if A.dtype == np.complex64 else C.C128
+    if A.dtype not in (np.complex64, np.complex128):
+        raise TypeError("A must be complex64 or complex128")
+    x = _c128(x)
+    y = np.zeros(A.shape[0], dtype=np.complex128)
+    ctx.check(C.lib().nihu_gb_matvec(ctx.handle, dtype, A.ctypes.data, A.shape[0], A.shape[1], max(A.shape[0], 1),
+                                     x.ctypes.data, y.ctypes.data, 1.0, 0.0, 0.0, 0.0, C.HOST))
+    return y
+
+
+def gmres(A: np.ndarray, b: np.ndarray, x0=None, restart: int = 50, max_iters: int = 1000, tol: float = 1e-6,
+          ctx: Context | None = None):
+    """Restarted GMRES on the GPU; returns (x, iterations, relative residual estimate)."""
+    ctx = ctx or default_context()
+    A = np.asfortranarray(A)
+    if A.dtype not in (np.complex64, np.complex128):
+        raise TypeError("A must be complex64 or complex128")
+    dtype = C.C64 if A.dtype == np.complex64 else C.C128
+    b = _c128(b)
+    x = _c128(np.zeros_like(b) if x0 is None else x0).copy()
+    it, res = ctypes.c_int(0), ctypes.c_double(0.0)
+    ctx.check(C.lib().nihu_gb_gmres(ctx.handle, dtype, A.ctypes.data, A.shape[0], max(A.shape[0], 1), b.ctypes.data,
+                                    x.ctypes.data, restart, max_iters, tol, ctypes.byref(it), ctypes.byref(res),
+                                    C.HOST))
+    return x, it.value, res.value
+
+
+def lu_solve(A: np.ndarray, b: np.ndarray, ctx: Context | None = None) -> np.ndarray:
+    """x = A^{-1} b by FP64 LU with partial pivoting on the GPU (A is not modified)."""
+    ctx = ctx or default_context()
+    A = np.asfortranarray(A, dtype=np.complex128)
+    b = _c128(b)
+    x = np.zeros_like(b)
+    ctx.check(C.lib().nihu_gb_lu_solve(ctx.handle, A.ctypes.data, A.shape[0], max(A.shape[0], 1), b.ctypes.data,
+                                       x.ctypes.data, C.HOST))
+    return x
+
+
+def solve_cbie(mesh: Mesh, k: float, q, family: int = C.HELMHOLTZ_3D, dtype: int = C.C64, solver: str = "gmres",
+               precision: str = "fp32", restart: int = 50, max_iters: int = 1000, tol: float = 1e-6,
+               ctx: Context | None = None):
+    """Exterior CBIE (DLP - I/2) p = SLP q on the GPU; returns (p, iterations, residual)."""
+    ctx = ctx or default_context()
+    q = _c128(q)
+    p = np.zeros_like(q)
+    it, res = ctypes.c_int(0), ctypes.c_double(0.0)
+    dm = mesh.device(ctx)
+    ctx.check(C.lib().nihu_gb_solve_cbie(ctx.handle, dm.handle, family, k,
+                                         C.REGULAR_FP64 if precision == "fp64" else C.REGULAR_FP32, dtype,
+                                         q.ctypes.data, p.ctypes.data, 0 if solver == "gmres" else 1, restart,
+                                         max_iters, tol, ctypes.byref(it), ctypes.byref(res)))
+    return p, it.value, res.value
+
+
+def pair_statistics(test: Mesh, trial: Mesh, ctx: Context | None = None) -> np.ndarray:
+    """[self, near, regular (SLP level, DLP level) 3x3] pair counts."""
+    ctx = ctx or default_context()
+    out = (ctypes.c_int64 * 11)()
+    tdm = test.device(ctx)
+    rdm = tdm if test is trial else trial.device(ctx)
+    ctx.check(C.lib().nihu_gb_pair_statistics(ctx.handle, tdm.handle, rdm.handle, out))
+    return np.array(list(out), dtype=np.int64)

@@ -1,0 +1,876 @@
+// C ABI of the GB300 collocation BEM library (declared in include/nihu_gb300.h).
+#include <algorithm>
+#include <cmath>
+#include <complex>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <string>
+#include <utility>
+#include <vector>
+
+#include "../../include/nihu_gb300.h"
+#include "kernels.h"
+#include "linalg.h"
+
+using namespace nihu;
+
+struct nihu_gb_ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    cudaStream_t copy_stream = nullptr;
+    bool own_stream = false;
+    size_t budget = 0;
+    size_t used = 0;
+    std::map<void *, size_t> allocs;
+    std::string err;
+    int64_t launches = 0;
+    int *d_flag = nullptr;       // device error flag / small scratch (4 ints)
+    void *h_small = nullptr;     // pinned host scratch (64 KB)
+    uint64_t next_uid = 1;
+    // nearly singular pair lists keyed by (test uid, trial uid)
+    std::map<std::pair<uint64_t, uint64_t>, NearList> near;
+    // reusable device scratch buffers
+    std::map<std::string, std::pair<void *, size_t>> scratch;
+};
+
+struct nihu_gb_mesh {
+    nihu_gb_ctx *ctx = nullptr;
+    uint64_t uid = 0;
+    int64_t n = 0;
+    DevMesh dm;
+    std::vector<void *> bufs;
+};
+
+namespace {
+
+nihu_gb_status fail(nihu_gb_ctx *ctx, nihu_gb_status st, const std::string &msg)
+{
+    if (ctx) ctx->err = msg;
+    return st;
+}
+
+nihu_gb_status cuda_fail(nihu_gb_ctx *ctx, cudaError_t e, const char *where)
+{
+    std::string msg = std::string(where) + ": " + cudaGetErrorString(e);
+    if (e == cudaErrorMemoryAllocation) return fail(ctx, NIHU_GB_ERR_OUT_OF_MEMORY, msg);
+    return fail(ctx, NIHU_GB_ERR_CUDA, msg);
+}
+
+#define CK(call)                                                 \
+    do {                                                         \
+        cudaError_t e_ = (call);                                 \
+        if (e_ != cudaSuccess) return cuda_fail(ctx, e_, #call); \
+    } while (0)
+
+nihu_gb_status dmalloc(nihu_gb_ctx *ctx, size_t bytes, void **out)
+{
+    *out = nullptr;
+    if (bytes == 0) bytes = 16;
+    if (ctx->budget && ctx->used + bytes > ctx->budget)
+        return fail(ctx, NIHU_GB_ERR_OUT_OF_MEMORY,
+                    "device memory budget exhausted (" + std::to_string(ctx->used + bytes) + " > " +
+                        std::to_string(ctx->budget) + " bytes)");
+    cudaError_t e = cudaMalloc(out, bytes);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return fail(ctx, NIHU_GB_ERR_OUT_OF_MEMORY, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+    }
+    ctx->allocs[*out] = bytes;
+    ctx->used += bytes;
+    return NIHU_GB_OK;
+}
+
+void dfree(nihu_gb_ctx *ctx, void *p)
+{
+    if (!p) return;
+    auto it = ctx->allocs.find(p);
+    if (it != ctx->allocs.end()) {
+        ctx->used -= it->second;
+        ctx->allocs.erase(it);
+    }
+    cudaFree(p);
+}
+
+// named scratch buffer of at least `bytes`, reused across calls
+nihu_gb_status scratch(nihu_gb_ctx *ctx, const char *name, size_t bytes, void **out)
+{
+    auto it = ctx->scratch.find(name);
+    if (it != ctx->scratch.end()) {
+        if (it->second.second >= bytes) { *out = it->second.first; return NIHU_GB_OK; }
+        dfree(ctx, it->second.first);
+        ctx->scratch.erase(it);
+    }
+    nihu_gb_status st = dmalloc(ctx, bytes, out);
+    if (st != NIHU_GB_OK) return st;
+    ctx->scratch[name] = {*out, bytes};
+    return NIHU_GB_OK;
+}
+
+void free_near(nihu_gb_ctx *ctx, NearList &nl)
+{
+    dfree(ctx, nl.col_ptr);
+    dfree(ctx, nl.rows);
+    nl = NearList();
+}
+
+nihu_gb_status sync(nihu_gb_ctx *ctx)
+{
+    cudaError_t e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaStreamSynchronize");
+    return NIHU_GB_OK;
+}
+
+// build (or fetch) the column-sorted nearly singular pair list of a mesh pair
+nihu_gb_status get_near(nihu_gb_ctx *ctx, const nihu_gb_mesh *test, const nihu_gb_mesh *trial, NearList **out)
+{
+    auto key = std::make_pair(test->uid, trial->uid);
+    auto it = ctx->near.find(key);
+    if (it != ctx->near.end()) { *out = &it->second; return NIHU_GB_OK; }
+    NearList nl;
+    nl.n_cols = (int)trial->n;
+    int same = test == trial;
+    void *counts = nullptr, *colptr = nullptr;
+    nihu_gb_status st = dmalloc(ctx, sizeof(int) * (trial->n + 1), &counts);
+    if (st) return st;
+    st = dmalloc(ctx, sizeof(int64_t) * (trial->n + 1), &colptr);
+    if (st) { dfree(ctx, counts); return st; }
+    nl.col_ptr = (int64_t *)colptr;
+    cudaError_t e = launch_near_count(test->dm, trial->dm, same, (int *)counts, ctx->stream);
+    if (e == cudaSuccess) e = launch_scan((int *)counts, (int)trial->n, nl.col_ptr, ctx->stream);
+    ctx->launches += 2;
+    int64_t nnz = 0;
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&nnz, nl.col_ptr + trial->n, sizeof(int64_t), cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    dfree(ctx, counts);
+    if (e != cudaSuccess) { free_near(ctx, nl); return cuda_fail(ctx, e, "nearly singular pair count"); }
+    nl.nnz = nnz;
+    void *rows = nullptr;
+    st = dmalloc(ctx, sizeof(int) * (nnz > 0 ? nnz : 1), &rows);
+    if (st) { free_near(ctx, nl); return st; }
+    nl.rows = (int *)rows;
+    e = launch_near_fill(test->dm, trial->dm, same, nl.col_ptr, nl.rows, ctx->stream);
+    ctx->launches += 1;
+    if (e != cudaSuccess) { free_near(ctx, nl); return cuda_fail(ctx, e, "nearly singular pair fill"); }
+    ctx->near[key] = nl;
+    *out = &ctx->near[key];
+    return NIHU_GB_OK;
+}
+
+size_t elem_bytes(int dtype) { return dtype == NIHU_GB_C64 ? 8 : 16; }
+
+bool valid_dtype(int d) { return d == NIHU_GB_C64 || d == NIHU_GB_C128; }
+bool valid_where(int w) { return w == NIHU_GB_HOST || w == NIHU_GB_DEVICE; }
+
+// regular + singular kernels for columns [j0, j1) into device buffers whose
+// column j starts at out + (j - j0) * ld
+nihu_gb_status assemble_panel(nihu_gb_ctx *ctx, RegularArgs a, NearList *nl)
+{
+    cudaError_t e = launch_assemble_regular(a, ctx->stream);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "assemble_regular launch");
+    e = launch_assemble_singular(a, *nl, ctx->d_flag, ctx->stream);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "assemble_singular launch");
+    ctx->launches += 2;
+    return NIHU_GB_OK;
+}
+
+nihu_gb_status check_flag(nihu_gb_ctx *ctx)
+{
+    int flag = 0;
+    CK(cudaMemcpyAsync(&flag, ctx->d_flag, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    if (flag) {
+        CK(cudaMemsetAsync(ctx->d_flag, 0, sizeof(int), ctx->stream));
+        return fail(ctx, NIHU_GB_ERR_RUNTIME, "Could not perform inverse mapping (nearly singular pair " +
+                                                  std::to_string(flag - 1) + ")");
+    }
+    return NIHU_GB_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+nihu_gb_status nihu_gb_ctx_create(int device, void *stream, size_t hbm_budget_bytes, nihu_gb_ctx **out)
+{
+    if (!out) return NIHU_GB_ERR_INVALID_ARGUMENT;
+    *out = nullptr;
+    int count = 0;
+    if (cudaGetDeviceCount(&count) != cudaSuccess || count == 0) {
+        cudaGetLastError();
+        return NIHU_GB_ERR_NO_DEVICE;
+    }
+    if (device < 0 || device >= count) return NIHU_GB_ERR_INVALID_ARGUMENT;
+    if (cudaSetDevice(device) != cudaSuccess) return NIHU_GB_ERR_NO_DEVICE;
+    nihu_gb_ctx *ctx = new nihu_gb_ctx();
+    ctx->device = device;
+    ctx->budget = hbm_budget_bytes;
+    if (stream) {
+        ctx->stream = (cudaStream_t)stream;
+    } else {
+        if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess) { delete ctx; return NIHU_GB_ERR_CUDA; }
+        ctx->own_stream = true;
+    }
+    if (cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking) != cudaSuccess) {
+        nihu_gb_ctx_destroy(ctx);
+        return NIHU_GB_ERR_CUDA;
+    }
+    void *flag = nullptr;
+    if (dmalloc(ctx, 4 * sizeof(int), &flag) != NIHU_GB_OK) { nihu_gb_ctx_destroy(ctx); return NIHU_GB_ERR_OUT_OF_MEMORY; }
+    ctx->d_flag = (int *)flag;
+    cudaMemset(ctx->d_flag, 0, 4 * sizeof(int));
+    if (cudaMallocHost(&ctx->h_small, 1 << 16) != cudaSuccess) { nihu_gb_ctx_destroy(ctx); return NIHU_GB_ERR_CUDA; }
+    *out = ctx;
+    return NIHU_GB_OK;
+}
+
+void nihu_gb_ctx_destroy(nihu_gb_ctx *ctx)
+{
+    if (!ctx) return;
+    cudaSetDevice(ctx->device);
+    if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    for (auto &kv : ctx->near) free_near(ctx, kv.second);
+    for (auto &kv : ctx->scratch) dfree(ctx, kv.second.first);
+    dfree(ctx, ctx->d_flag);
+    if (ctx->h_small) cudaFreeHost(ctx->h_small);
+    if (ctx->copy_stream) cudaStreamDestroy(ctx->copy_stream);
+    if (ctx->own_stream && ctx->stream) cudaStreamDestroy(ctx->stream);
+    delete ctx;
+}
+
+const char *nihu_gb_last_error(const nihu_gb_ctx *ctx) { return ctx ? ctx->err.c_str() : "null context"; }
+void *nihu_gb_ctx_stream(const nihu_gb_ctx *ctx) { return ctx ? (void *)ctx->stream : nullptr; }
+size_t nihu_gb_ctx_device_bytes(const nihu_gb_ctx *ctx) { return ctx ? ctx->used : 0; }
+int64_t nihu_gb_ctx_launch_count(const nihu_gb_ctx *ctx) { return ctx ? ctx->launches : 0; }
+
+nihu_gb_status nihu_gb_host_alloc(nihu_gb_ctx *ctx, size_t bytes, void **out)
+{
+    if (!ctx || !out) return NIHU_GB_ERR_INVALID_ARGUMENT;
+    cudaError_t e = cudaMallocHost(out, bytes ? bytes : 16);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaMallocHost");
+    return NIHU_GB_OK;
+}
+
+void nihu_gb_host_free(void *ptr)
+{
+    if (ptr) cudaFreeHost(ptr);
+}
+
+nihu_gb_status nihu_gb_device_alloc(nihu_gb_ctx *ctx, size_t bytes, void **out)
+{
+    if (!ctx || !out) return NIHU_GB_ERR_INVALID_ARGUMENT;
+    cudaSetDevice(ctx->device);
+    return dmalloc(ctx, bytes, out);
+}
+
+void nihu_gb_device_free(nihu_gb_ctx *ctx, void *ptr)
+{
+    if (!ctx || !ptr) return;
+    cudaSetDevice(ctx->device);
+    cudaStreamSynchronize(ctx->stream);
+    dfree(ctx, ptr);
+}
+
+nihu_gb_status nihu_gb_memcpy(nihu_gb_ctx *ctx, void *dst, int dst_where, const void *src, int src_where, size_t bytes)
+{
+    if (!ctx || (!dst && bytes) || (!src && bytes) || !valid_where(dst_where) || !valid_where(src_where))
+        return fail(ctx, NIHU_GB_ERR_INVALID_ARGUMENT, "nihu_gb_memcpy: bad argument");
+    cudaSetDevice(ctx->device);
+    cudaMemcpyKind kind = dst_where == NIHU_GB_DEVICE ? (src_where == NIHU_GB_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice)
+                                                      : (src_where == NIHU_GB_DEVICE ? cudaMemcpyDeviceToHost : cudaMemcpyHostToHost);
+    CK(cudaMemcpyAsync(dst, src, bytes, kind, ctx->stream));
+    return sync(ctx);
+}
+
+// ------------------------------------------------------------------ mesh
+
+nihu_gb_status nihu_gb_mesh_create(nihu_gb_ctx *ctx, const double *nodes, int64_t n_nodes, const int32_t *elems,
+                                   int64_t n_elems, int64_t elem_cols, nihu_gb_mesh **out)
+{
+    if (!ctx || !out) return NIHU_GB_ERR_INVALID_ARGUMENT;
+    *out = nullptr;
+    if (n_nodes < 0 || n_elems < 0 || (n_nodes && !nodes) || (n_elems && !elems) || elem_cols < 4 ||
+        elem_cols > 64 || n_elems > 0x3fffffff)
+        return fail(ctx, NIHU_GB_ERR_INVALID_ARGUMENT, "nihu_gb_mesh_create: bad mesh arrays");
+    cudaSetDevice(ctx->device);
+    nihu_gb_mesh *m = new nihu_gb_mesh();
+    m->ctx = ctx;
+    m->uid = ctx->next_uid++;
+    m->n = n_elems;
+    m->dm.n = (int)n_elems;
+    const int64_t n = std::max<int64_t>(n_elems, 1);
+    struct Req { void **p; size_t bytes; };
+    void *corners, *center, *size, *nc, *chi, *clo, *p0, *pts32, *pts64;
+    Req reqs[] = {{&corners, sizeof(double) * 12 * n}, {&center, sizeof(double) * 3 * n}, {&size, sizeof(double) * n},
+                  {&nc, sizeof(int8_t) * n}, {&chi, sizeof(float4) * n}, {&clo, sizeof(float4) * n},
+                  {&p0, sizeof(float4) * n}, {&pts32, sizeof(float4) * 2 * 2 * SLOTS * n},
+                  {&pts64, sizeof(double) * 8 * 2 * SLOTS * n}};
+    for (auto &r : reqs) {
+        nihu_gb_status st = dmalloc(ctx, r.bytes, r.p);
+        if (st) { nihu_gb_mesh_destroy(m); return st; }
+        m->bufs.push_back(*r.p);
+    }
+    m->dm.corners = (double *)corners;
+    m->dm.center = (double *)center;
+    m->dm.size = (double *)size;
+    m->dm.nc = (int8_t *)nc;
+    m->dm.chi = (float4 *)chi;
+    m->dm.clo = (float4 *)clo;
+    m->dm.p0 = (float4 *)p0;
+    m->dm.pts32 = (float4 *)pts32;
+    m->dm.pts64 = (double *)pts64;
+    for (int64_t e = 0; e < n_elems; ++e) {
+        int32_t t = elems[e * elem_cols];
+        if (t == NIHU_GB_TRIA_1) m->dm.has_tria = 1;
+        else if (t == NIHU_GB_QUAD_1) m->dm.has_quad = 1;
+        else {
+            nihu_gb_mesh_destroy(m);
+            return fail(ctx, NIHU_GB_ERR_INVALID_ARGUMENT,
+                        "nihu_gb_mesh_create: unknown element type id " + std::to_string(t) + " in row " + std::to_string(e));
+        }
+        int nc_e = t == NIHU_GB_TRIA_1 ? 3 : 4;
+        for (int a = 0; a < nc_e; ++a) {
+            int32_t nd = elems[e * elem_cols + 1 + a];
+            if (nd < 0 || nd >= n_nodes) {
+                nihu_gb_mesh_destroy(m);
+                return fail(ctx, NIHU_GB_ERR_OUT_OF_RANGE,
+                            "nihu_gb_mesh_create: node index out of range in element " + std::to_string(e));
+            }
+        }
+    }
+    if (n_elems > 0) {
+        void *dnodes = nullptr, *delems = nullptr;
+        nihu_gb_status st = dmalloc(ctx, sizeof(double) * 3 * std::max<int64_t>(n_nodes, 1), &dnodes);
+        if (st) { nihu_gb_mesh_destroy(m); return st; }
+        st = dmalloc(ctx, sizeof(int32_t) * n_elems * elem_cols, &delems);
+        if (st) { dfree(ctx, dnodes); nihu_gb_mesh_destroy(m); return st; }
+        cudaError_t e = cudaMemcpyAsync(dnodes, nodes, sizeof(double) * 3 * n_nodes, cudaMemcpyHostToDevice, ctx->stream);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(delems, elems, sizeof(int32_t) * n_elems * elem_cols, cudaMemcpyHostToDevice, ctx->stream);
+        if (e == cudaSuccess) e = cudaMemsetAsync(ctx->d_flag, 0, sizeof(int), ctx->stream);
+        if (e == cudaSuccess)
+            e = launch_mesh_geometry((const double *)dnodes, n_nodes, (const int32_t *)delems, (int)n_elems,
+                                     (int)elem_cols, m->dm, ctx->d_flag, ctx->stream);
+        ctx->launches += 1;
+        int bad = 0;
+        if (e == cudaSuccess) e = cudaMemcpyAsync(&bad, ctx->d_flag, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+        dfree(ctx, dnodes);
+        dfree(ctx, delems);
+        if (e != cudaSuccess) { nihu_gb_mesh_destroy(m); return cuda_fail(ctx, e, "mesh geometry"); }
+        if (bad) {
+            cudaMemsetAsync(ctx->d_flag, 0, sizeof(int), ctx->stream);
+            nihu_gb_mesh_destroy(m);
+            return fail(ctx, NIHU_GB_ERR_INVALID_ARGUMENT, "invalid element " + std::to_string(bad - 1));
+        }
+    }
+    *out = m;
+    return NIHU_GB_OK;
+}
+
+void nihu_gb_mesh_destroy(nihu_gb_mesh *m)
+{
+    if (!m) return;
+    nihu_gb_ctx *ctx = m->ctx;
+    cudaSetDevice(ctx->device);
+    cudaStreamSynchronize(ctx->stream);
+    for (auto it = ctx->near.begin(); it != ctx->near.end();) {
+        if (it->first.first == m->uid || it->first.second == m->uid) {
+            free_near(ctx, it->second);
+            it = ctx->near.erase(it);
+        } else {
+            ++it;
+        }
+    }
+    for (void *p : m->bufs) dfree(ctx, p);
+    delete m;
+}
+
+int64_t nihu_gb_mesh_num_elements(const nihu_gb_mesh *m) { return m ? m->n : -1; }
+
+// ---------------------------------------------------------------- assembly
+
+nihu_gb_status nihu_gb_assemble(nihu_gb_ctx *ctx, const nihu_gb_mesh *test, const nihu_gb_mesh *trial, int family,
+                                int ops, double k, double alpha_re, double alpha_im, int precision, int dtype,
+                                void *out_slp, void *out_dlp, int64_t ld, int accumulate, int where)
+{
+    if (!ctx) return NIHU_GB_ERR_INVALID_ARGUMENT;
+    if (!test || !trial || test->ctx != ctx || trial->ctx != ctx)
+        return fail(ctx, NIHU_GB_ERR_INVALID_ARGUMENT, "nihu_gb_assemble: meshes must belong to the context");
+    if (family != NIHU_GB_HELMHOLTZ_3D && family != NIHU_GB_LAPLACE_3D)
+        return fail(ctx, NIHU_GB_ERR_INVALID_ARGUMENT, "nihu_gb_assemble: unknown kernel family");
+    if (ops < 1 || ops > 3) return fail(ctx, NIHU_GB_ERR_INVALID_ARGUMENT, "nihu_gb_assemble: ops must be SLP, DLP or both");
+    if (((ops & NIHU_GB_SLP) && !out_slp) || ((ops & NIHU_GB_DLP) && !out_dlp))
+        return fail(ctx, NIHU_GB_ERR_INVALID_ARGUMENT, "nihu_gb_assemble: missing output buffer");
+    if (!valid_dtype(dtype) || !valid_where(where) || (precision != 0 && precision != 1))
+        return fail(ctx, NIHU_GB_ERR_INVALID_ARGUMENT, "nihu_gb_assemble: bad dtype, precision or location");
+    if (ld < std::max<int64_t>(test->n, 1)) return fail(ctx, NIHU_GB_ERR_INVALID_ARGUMENT, "nihu_gb_assemble: ld < rows");
+    if (!std::isfinite(k) || !std::isfinite(alpha_re) || !std::isfinite(alpha_im))
+        return fail(ctx, NIHU_GB_ERR_INVALID_ARGUMENT, "nihu_gb_assemble: non-finite wave number or scale");
+    if (test->n == 0 || trial->n == 0) return NIHU_GB_OK;
+    cudaSetDevice(ctx->device);
+    NearList *nl = nullptr;
+    nihu_gb_status st = get_near(ctx, test, trial, &nl);
+    if (st) return st;
+
+    RegularArgs a;
+    a.test = test->dm;
+    a.trial = trial->dm;
+    a.same_mesh = test == trial;
+    a.family = family;
+    a.ops = ops;
+    a.k = family == NIHU_GB_HELMHOLTZ_3D ? k : 0.0;
+    a.alpha_re = alpha_re;
+    a.alpha_im = alpha_im;
+    a.precision = precision;
+    a.dtype = dtype;
+    a.accumulate = accumulate ? 1 : 0;
+    const size_t es = elem_bytes(dtype);
+    const int64_t M = test->n, N = trial->n;
+
+    if (where == NIHU_GB_DEVICE) {
+        a.out_s = out_slp;
+        a.out_d = out_dlp;
+        a.ld = ld;
+        a.j0 = 0;
+        a.j1 = (int)N;
+        st = assemble_panel(ctx, a, nl);
+        if (st) return st;
+        return check_flag(ctx);
+    }
+
+    // host outputs: column panels, double-buffered; D2H copies on the copy
+    // stream overlap the next panel's kernels
+    const int nbuf_ops = (ops == 3) ? 2 : 1;
+    const size_t col_bytes = (size_t)M * es;
+    size_t panel_cap = (size_t)256 << 20;  // bytes per buffer
+    if (ctx->budget) {
+        size_t avail = ctx->budget > ctx->used ? ctx->budget - ctx->used : 0;
+        panel_cap = std::min(panel_cap, avail / (2 * nbuf_ops + 1));
+    }
+    int64_t P = std::max<int64_t>(1, (int64_t)(panel_cap / col_bytes));
+    P = std::min<int64_t>(P, N);
+    void *buf[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};
+    const char *names[2][2] = {{"panel_s0", "panel_d0"}, {"panel_s1", "panel_d1"}};
+    for (int b = 0; b < 2; ++b)
+        for (int o = 0; o < 2; ++o) {
+            if (!((o == 0 && (ops & 1)) || (o == 1 && (ops & 2)))) continue;
+            st = scratch(ctx, names[b][o], col_bytes * P, &buf[b][o]);
+            if (st) return st;
+        }
+    cudaEvent_t computed[2], copied[2];
+    for (int b = 0; b < 2; ++b) {
+        cudaEventCreateWithFlags(&computed[b], cudaEventDisableTiming);
+        cudaEventCreateWithFlags(&copied[b], cudaEventDisableTiming);
+    }
+    void *outs[2] = {out_slp, out_dlp};
+    cudaError_t e = cudaSuccess;
+    int b = 0;
+    bool used[2] = {false, false};
+    for (int64_t j0 = 0; j0 < N && e == cudaSuccess && st == NIHU_GB_OK; j0 += P, b ^= 1) {
+        const int64_t j1 = std::min(N, j0 + P);
+        if (used[b]) e = cudaStreamWaitEvent(ctx->stream, copied[b], 0);
+        for (int o = 0; o < 2 && e == cudaSuccess; ++o) {
+            if (!buf[b][o] || !accumulate) continue;
+            e = cudaMemcpy2DAsync(buf[b][o], col_bytes, (char *)outs[o] + j0 * ld * es, ld * es, col_bytes, j1 - j0,
+                                  cudaMemcpyHostToDevice, ctx->stream);
+        }
+        if (e != cudaSuccess) break;
+        a.out_s = buf[b][0];
+        a.out_d = buf[b][1];
+        a.ld = M;
+        a.j0 = (int)j0;
+        a.j1 = (int)j1;
+        st = assemble_panel(ctx, a, nl);
+        if (st) break;
+        e = cudaEventRecord(computed[b], ctx->stream);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(ctx->copy_stream, computed[b], 0);
+        for (int o = 0; o < 2 && e == cudaSuccess; ++o) {
+            if (!buf[b][o]) continue;
+            e = cudaMemcpy2DAsync((char *)outs[o] + j0 * ld * es, ld * es, buf[b][o], col_bytes, col_bytes, j1 - j0,
+                                  cudaMemcpyDeviceToHost, ctx->copy_stream);
+        }
+        if (e == cudaSuccess) e = cudaEventRecord(copied[b], ctx->copy_stream);
+        used[b] = true;
+    }
+    cudaError_t e2 = cudaStreamSynchronize(ctx->copy_stream);
+    cudaError_t e3 = cudaStreamSynchronize(ctx->stream);
+    for (int q = 0; q < 2; ++q) {
+        cudaEventDestroy(computed[q]);
+        cudaEventDestroy(copied[q]);
+    }
+    if (st) return st;
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "panel assembly");
+    if (e2 != cudaSuccess) return cuda_fail(ctx, e2, "panel copy");
+    if (e3 != cudaSuccess) return cuda_fail(ctx, e3, "panel compute");
+    return check_flag(ctx);
+}
+
+nihu_gb_status nihu_gb_add_identity(nihu_gb_ctx *ctx, const nihu_gb_mesh *mesh, double alpha_re, double alpha_im,
+                                    int dtype, void *out, int64_t ld, int where)
+{
+    if (!ctx) return NIHU_GB_ERR_INVALID_ARGUMENT;
+    if (!mesh || !out || !valid_dtype(dtype) || !valid_where(where) || ld < std::max<int64_t>(mesh->n, 1))
+        return fail(ctx, NIHU_GB_ERR_INVALID_ARGUMENT, "nihu_gb_add_identity: bad argument");
+    if (where == NIHU_GB_HOST) {
+        const int64_t n = mesh->n;
+        for (int64_t i = 0; i < n; ++i) {
+            if (dtype == NIHU_GB_C64) {
+                float *p = (float *)out + 2 * (i * ld + i);
+                p[0] += (float)alpha_re;
+                p[1] += (float)alpha_im;
+            } else {
+                double *p = (double *)out + 2 * (i * ld + i);
+                p[0] += alpha_re;
+                p[1] += alpha_im;
+            }
+        }
+        return NIHU_GB_OK;
+    }
+    cudaSetDevice(ctx->device);
+    CK(launch_add_identity((int)mesh->n, alpha_re, alpha_im, dtype, out, ld, ctx->stream));
+    ctx->launches += 1;
+    return sync(ctx);
+}
+
+nihu_gb_status nihu_gb_pair_statistics(nihu_gb_ctx *ctx, const nihu_gb_mesh *test, const nihu_gb_mesh *trial,
+                                       int64_t counts[11])
+{
+    if (!ctx) return NIHU_GB_ERR_INVALID_ARGUMENT;
+    if (!test || !trial || !counts) return fail(ctx, NIHU_GB_ERR_INVALID_ARGUMENT, "nihu_gb_pair_statistics: bad argument");
+    cudaSetDevice(ctx->device);
+    void *d = nullptr;
+    nihu_gb_status st = scratch(ctx, "stats", sizeof(unsigned long long) * 11, &d);
+    if (st) return st;
+    CK(cudaMemsetAsync(d, 0, sizeof(unsigned long long) * 11, ctx->stream));
+    CK(launch_pair_stats(test->dm, trial->dm, test == trial, (unsigned long long *)d, ctx->stream));
+    ctx->launches += 1;
+    unsigned long long h[11];
+    CK(cudaMemcpyAsync(h, d, sizeof(h), cudaMemcpyDeviceToHost, ctx->stream));
+    st = sync(ctx);
+    for (int q = 0; q < 11; ++q) counts[q] = (int64_t)h[q];
+    return st;
+}
+
+// ------------------------------------------------------------------ matvec
+
+nihu_gb_status nihu_gb_matvec(nihu_gb_ctx *ctx, int dtype_a, const void *A, int64_t m, int64_t n, int64_t lda,
+                              const void *x, void *y, double alpha_re, double alpha_im, double beta_re, double beta_im,
+                              int where)
+{
+    if (!ctx) return NIHU_GB_ERR_INVALID_ARGUMENT;
+    if (!valid_dtype(dtype_a) || !valid_where(where) || m < 0 || n < 0 || lda < std::max<int64_t>(m, 1) ||
+        (m && (!A || !y)) || (n && !x))
+        return fail(ctx, NIHU_GB_ERR_INVALID_ARGUMENT, "nihu_gb_matvec: bad argument");
+    if (m == 0) return NIHU_GB_OK;
+    cudaSetDevice(ctx->device);
+    const size_t es = elem_bytes(dtype_a);
+    const void *dA = A;
+    const double2 *dx = (const double2 *)x;
+    double2 *dy = (double2 *)y;
+    nihu_gb_status st;
+    if (where == NIHU_GB_HOST) {
+        void *pa, *px, *py;
+        if ((st = scratch(ctx, "mv_A", es * m * n, &pa))) return st;
+        if ((st = scratch(ctx, "mv_x", 16 * std::max<int64_t>(n, 1), &px))) return st;
+        if ((st = scratch(ctx, "mv_y", 16 * m, &py))) return st;
+        CK(cudaMemcpy2DAsync(pa, es * m, A, es * lda, es * m, n, cudaMemcpyHostToDevice, ctx->stream));
+        if (n) CK(cudaMemcpyAsync(px, x, 16 * n, cudaMemcpyHostToDevice, ctx->stream));
+        CK(cudaMemcpyAsync(py, y, 16 * m, cudaMemcpyHostToDevice, ctx->stream));
+        dA = pa;
+        dx = (const double2 *)px;
+        dy = (double2 *)py;
+        lda = m;
+    }
+    int splits = gemv_splits(m, n, dtype_a);
+    void *part;
+    if ((st = scratch(ctx, "mv_part", 16 * (size_t)splits * m, &part))) return st;
+    CK(launch_gemv(dtype_a, dA, m, n, lda, dx, dy, alpha_re, alpha_im, beta_re, beta_im, (double2 *)part, splits,
+                   ctx->stream));
+    ctx->launches += 2;
+    if (where == NIHU_GB_HOST) CK(cudaMemcpyAsync(y, dy, 16 * m, cudaMemcpyDeviceToHost, ctx->stream));
+    return sync(ctx);
+}
+
+// ------------------------------------------------------------------ GMRES
+
+namespace {
+
+struct Cplx {
+    double re, im;
+};
+
+nihu_gb_status gmres_device(nihu_gb_ctx *ctx, int dtype_a, const void *A, int64_t n, int64_t lda, const double2 *b,
+                            double2 *x, int restart, int max_iters, double tol, int *iters_out, double *res_out)
+{
+    typedef std::complex<double> C;
+    nihu_gb_status st;
+    const int m = restart;
+    void *pV, *pw, *pt, *ppart, *pdot, *ph;
+    if ((st = scratch(ctx, "gm_V", 16 * (size_t)n * (m + 1), &pV))) return st;
+    if ((st = scratch(ctx, "gm_w", 16 * (size_t)n, &pw))) return st;
+    if ((st = scratch(ctx, "gm_t", 16 * (size_t)n, &pt))) return st;
+    int splits = gemv_splits(n, n, dtype_a);
+    if ((st = scratch(ctx, "mv_part", 16 * (size_t)splits * n, &ppart))) return st;
+    const int dblocks = dot_blocks(n);
+    if ((st = scratch(ctx, "gm_dot", 16 * (size_t)dblocks * (m + 1), &pdot))) return st;
+    if ((st = scratch(ctx, "gm_h", 16 * (size_t)(m + 1), &ph))) return st;
+    double2 *V = (double2 *)pV, *w = (double2 *)pw, *t = (double2 *)pt, *part = (double2 *)ppart;
+    double2 *dot = (double2 *)pdot, *dh = (double2 *)ph;
+    Cplx *hsm = (Cplx *)ctx->h_small;  // pinned host scratch, (m + 1) * dblocks <= 4096 entries
+    if ((size_t)(m + 1) * dblocks * sizeof(Cplx) > (1 << 16)) return fail(ctx, NIHU_GB_ERR_INVALID_ARGUMENT, "GMRES restart too large");
+
+    auto norm_of = [&](const double2 *v, double *out) -> nihu_gb_status {
+        CK(launch_multidot(v, n, 1, v, dot, dblocks, ctx->stream));
+        ctx->launches += 1;
+        CK(cudaMemcpyAsync(hsm, dot, 16 * dblocks, cudaMemcpyDeviceToHost, ctx->stream));
+        if ((st = sync(ctx))) return st;
+        double s = 0;
+        for (int q = 0; q < dblocks; ++q) s += hsm[q].re;
+        *out = std::sqrt(s);
+        return NIHU_GB_OK;
+    };
+    auto project = [&](int nv, std::vector<C> &h) -> nihu_gb_status {
+        // h = V[0..nv)^H w ; w -= V h
+        CK(launch_multidot(V, n, nv, w, dot, dblocks, ctx->stream));
+        ctx->launches += 1;
+        CK(cudaMemcpyAsync(hsm, dot, 16 * (size_t)dblocks * nv, cudaMemcpyDeviceToHost, ctx->stream));
+        if ((st = sync(ctx))) return st;
+        std::vector<double2> hv(nv);
+        for (int v = 0; v < nv; ++v) {
+            double sr = 0, si = 0;
+            for (int q = 0; q < dblocks; ++q) { sr += hsm[v * dblocks + q].re; si += hsm[v * dblocks + q].im; }
+            h[v] += C(sr, si);
+            hv[v] = make_double2(sr, si);
+        }
+        CK(cudaMemcpyAsync(dh, hv.data(), 16 * nv, cudaMemcpyHostToDevice, ctx->stream));
+        CK(launch_subtract_combo(V, n, nv, dh, w, ctx->stream));
+        ctx->launches += 1;
+        return NIHU_GB_OK;
+    };
+
+    // r0 = b - A x ; reference normalises by the initial residual norm
+    CK(launch_gemv(dtype_a, A, n, n, lda, x, t, 1.0, 0.0, 0.0, 0.0, part, splits, ctx->stream));
+    CK(launch_sub(b, t, w, n, ctx->stream));
+    ctx->launches += 3;
+    double r0norm;
+    if ((st = norm_of(w, &r0norm))) return st;
+    int iters = 0;
+    double rel = 0.0;
+    if (r0norm == 0.0) {
+        if (iters_out) *iters_out = 0;
+        if (res_out) *res_out = 0.0;
+        return NIHU_GB_OK;
+    }
+    double beta = r0norm;
+    std::vector<std::vector<C>> H(m + 1, std::vector<C>(m, C(0)));
+    std::vector<C> g(m + 1), cs(m), sn(m);
+    bool converged = false;
+    while (true) {
+        CK(launch_scale_copy(w, V, n, 1.0 / beta, ctx->stream));
+        ctx->launches += 1;
+        std::fill(g.begin(), g.end(), C(0));
+        g[0] = beta;
+        int kdone = 0;
+        bool stop = false;
+        for (int k = 0; k < m; ++k) {
+            ++iters;
+            // w = A v_k
+            CK(launch_gemv(dtype_a, A, n, n, lda, V + (size_t)k * n, w, 1.0, 0.0, 0.0, 0.0, part, splits, ctx->stream));
+            ctx->launches += 2;
+            std::vector<C> h(k + 2, C(0));
+            if ((st = project(k + 1, h))) return st;
+            if ((st = project(k + 1, h))) return st;  // reorthogonalisation (CGS2)
+            double hn;
+            if ((st = norm_of(w, &hn))) return st;
+            h[k + 1] = hn;
+            if (hn > 0.0) {
+                CK(launch_scale_copy(w, V + (size_t)(k + 1) * n, n, 1.0 / hn, ctx->stream));
+                ctx->launches += 1;
+            }
+            // apply previous Givens rotations, then a new one
+            for (int i = 0; i < k; ++i) {
+                C a0 = h[i], a1 = h[i + 1];
+                h[i] = std::conj(cs[i]) * a0 + std::conj(sn[i]) * a1;
+                h[i + 1] = -sn[i] * a0 + cs[i] * a1;
+            }
+            double den = std::sqrt(std::norm(h[k]) + std::norm(h[k + 1]));
+            if (den == 0.0) { cs[k] = 1.0; sn[k] = 0.0; }
+            else { cs[k] = h[k] / den; sn[k] = h[k + 1] / den; }
+            C a0 = h[k], a1 = h[k + 1];
+            h[k] = std::conj(cs[k]) * a0 + std::conj(sn[k]) * a1;
+            h[k + 1] = 0.0;
+            C g0 = g[k], g1 = g[k + 1];
+            g[k] = std::conj(cs[k]) * g0 + std::conj(sn[k]) * g1;
+            g[k + 1] = -sn[k] * g0 + cs[k] * g1;
+            for (int i = 0; i <= k; ++i) H[i][k] = h[i];
+            kdone = k + 1;
+            rel = std::abs(g[k + 1]) / r0norm;
+            if (rel < tol || iters >= max_iters || hn == 0.0 || kdone == n) { stop = true; break; }
+        }
+        // y = H^{-1} g, x += V y
+        std::vector<C> yv(kdone);
+        for (int i = kdone - 1; i >= 0; --i) {
+            C s = g[i];
+            for (int j = i + 1; j < kdone; ++j) s -= H[i][j] * yv[j];
+            yv[i] = s / H[i][i];
+        }
+        std::vector<double2> yd(kdone);
+        for (int i = 0; i < kdone; ++i) yd[i] = make_double2(yv[i].real(), yv[i].imag());
+        CK(cudaMemcpyAsync(dh, yd.data(), 16 * kdone, cudaMemcpyHostToDevice, ctx->stream));
+        CK(launch_add_combo(V, n, kdone, dh, x, ctx->stream));
+        ctx->launches += 1;
+        if (rel < tol) converged = true;
+        if (stop) break;
+        // restart: w = b - A x
+        CK(launch_gemv(dtype_a, A, n, n, lda, x, t, 1.0, 0.0, 0.0, 0.0, part, splits, ctx->stream));
+        CK(launch_sub(b, t, w, n, ctx->stream));
+        ctx->launches += 3;
+        if ((st = norm_of(w, &beta))) return st;
+        if (beta == 0.0) { converged = true; rel = 0.0; break; }
+    }
+    if ((st = sync(ctx))) return st;
+    if (iters_out) *iters_out = iters;
+    if (res_out) *res_out = rel;
+    if (!converged) return fail(ctx, NIHU_GB_ERR_NOT_CONVERGED, "GMRES did not reach the tolerance");
+    return NIHU_GB_OK;
+}
+
+}  // namespace
+
+nihu_gb_status nihu_gb_gmres(nihu_gb_ctx *ctx, int dtype_a, const void *A, int64_t n, int64_t lda, const void *b,
+                             void *x, int restart, int max_iters, double tol, int *iters, double *rel_residual,
+                             int where)
+{
+    if (!ctx) return NIHU_GB_ERR_INVALID_ARGUMENT;
+    if (!valid_dtype(dtype_a) || !valid_where(where) || n < 0 || lda < std::max<int64_t>(n, 1) || restart < 1 ||
+        restart > 256 || max_iters < 1 || !(tol > 0.0) || (n && (!A || !b || !x)))
+        return fail(ctx, NIHU_GB_ERR_INVALID_ARGUMENT, "nihu_gb_gmres: bad argument");
+    if (n == 0) return NIHU_GB_OK;
+    cudaSetDevice(ctx->device);
+    restart = (int)std::min<int64_t>(restart, n);
+    nihu_gb_status st;
+    const void *dA = A;
+    const double2 *db = (const double2 *)b;
+    double2 *dx = (double2 *)x;
+    const size_t es = elem_bytes(dtype_a);
+    if (where == NIHU_GB_HOST) {
+        void *pa, *pb, *px;
+        if ((st = scratch(ctx, "mv_A", es * n * n, &pa))) return st;
+        if ((st = scratch(ctx, "gm_b", 16 * n, &pb))) return st;
+        if ((st = scratch(ctx, "gm_x", 16 * n, &px))) return st;
+        CK(cudaMemcpy2DAsync(pa, es * n, A, es * lda, es * n, n, cudaMemcpyHostToDevice, ctx->stream));
+        CK(cudaMemcpyAsync(pb, b, 16 * n, cudaMemcpyHostToDevice, ctx->stream));
+        CK(cudaMemcpyAsync(px, x, 16 * n, cudaMemcpyHostToDevice, ctx->stream));
+        dA = pa;
+        db = (const double2 *)pb;
+        dx = (double2 *)px;
+        lda = n;
+    }
+    st = gmres_device(ctx, dtype_a, dA, n, lda, db, dx, restart, max_iters, tol, iters, rel_residual);
+    if (where == NIHU_GB_HOST && (st == NIHU_GB_OK || st == NIHU_GB_ERR_NOT_CONVERGED)) {
+        std::string keep = ctx->err;
+        CK(cudaMemcpyAsync(x, dx, 16 * n, cudaMemcpyDeviceToHost, ctx->stream));
+        nihu_gb_status s2 = sync(ctx);
+        if (s2) return s2;
+        ctx->err = keep;
+    }
+    return st;
+}
+
+// ------------------------------------------------------------------ LU
+
+nihu_gb_status nihu_gb_lu_solve(nihu_gb_ctx *ctx, void *A, int64_t n, int64_t lda, const void *b, void *x, int where)
+{
+    if (!ctx) return NIHU_GB_ERR_INVALID_ARGUMENT;
+    if (!valid_where(where) || n < 0 || lda < std::max<int64_t>(n, 1) || (n && (!A || !b || !x)) || n > 0x7fffffff)
+        return fail(ctx, NIHU_GB_ERR_INVALID_ARGUMENT, "nihu_gb_lu_solve: bad argument");
+    if (n == 0) return NIHU_GB_OK;
+    cudaSetDevice(ctx->device);
+    nihu_gb_status st;
+    double2 *dA = (double2 *)A;
+    const double2 *db = (const double2 *)b;
+    double2 *dx = (double2 *)x;
+    if (where == NIHU_GB_HOST) {
+        void *pa, *pb, *px;
+        if ((st = scratch(ctx, "lu_A", 16 * n * n, &pa))) return st;
+        if ((st = scratch(ctx, "lu_b", 16 * n, &pb))) return st;
+        if ((st = scratch(ctx, "lu_x", 16 * n, &px))) return st;
+        CK(cudaMemcpy2DAsync(pa, 16 * n, A, 16 * lda, 16 * n, n, cudaMemcpyHostToDevice, ctx->stream));
+        CK(cudaMemcpyAsync(pb, b, 16 * n, cudaMemcpyHostToDevice, ctx->stream));
+        dA = (double2 *)pa;
+        db = (const double2 *)pb;
+        dx = (double2 *)px;
+        lda = n;
+    }
+    void *ppiv;
+    if ((st = scratch(ctx, "lu_piv", sizeof(int) * n, &ppiv))) return st;
+    CK(cudaMemsetAsync(ctx->d_flag + 1, 0, sizeof(int), ctx->stream));
+    CK(launch_lu_factor(dA, n, lda, (int *)ppiv, ctx->d_flag + 1, &ctx->launches, ctx->stream));
+    CK(launch_lu_solve(dA, n, lda, (const int *)ppiv, db, dx, ctx->stream));
+    ctx->launches += 1;
+    int info = 0;
+    CK(cudaMemcpyAsync(&info, ctx->d_flag + 1, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    if (where == NIHU_GB_HOST) CK(cudaMemcpyAsync(x, dx, 16 * n, cudaMemcpyDeviceToHost, ctx->stream));
+    if ((st = sync(ctx))) return st;
+    if (info) return fail(ctx, NIHU_GB_ERR_RUNTIME, "LU: exactly singular matrix (zero pivot in column " + std::to_string(info - 1) + ")");
+    return NIHU_GB_OK;
+}
+
+// --------------------------------------------------------- composite solve
+
+nihu_gb_status nihu_gb_solve_cbie(nihu_gb_ctx *ctx, const nihu_gb_mesh *mesh, int family, double k, int precision,
+                                  int dtype, const void *q, void *p, int solver, int restart, int max_iters,
+                                  double tol, int *iters, double *rel_residual)
+{
+    if (!ctx) return NIHU_GB_ERR_INVALID_ARGUMENT;
+    if (!mesh || !q || !p || (solver != 0 && solver != 1) || (solver == 1 && dtype != NIHU_GB_C128) || !valid_dtype(dtype))
+        return fail(ctx, NIHU_GB_ERR_INVALID_ARGUMENT, "nihu_gb_solve_cbie: bad argument");
+    const int64_t n = mesh->n;
+    if (n == 0) return NIHU_GB_OK;
+    cudaSetDevice(ctx->device);
+    const size_t es = elem_bytes(dtype);
+    nihu_gb_status st;
+    void *G, *Hm, *dq, *drhs, *dp;
+    if ((st = scratch(ctx, "cbie_G", es * n * n, &G))) return st;
+    if ((st = scratch(ctx, "cbie_H", es * n * n, &Hm))) return st;
+    if ((st = scratch(ctx, "cbie_q", 16 * n, &dq))) return st;
+    if ((st = scratch(ctx, "cbie_rhs", 16 * n, &drhs))) return st;
+    if ((st = scratch(ctx, "cbie_p", 16 * n, &dp))) return st;
+    CK(cudaMemcpyAsync(dq, q, 16 * n, cudaMemcpyHostToDevice, ctx->stream));
+    st = nihu_gb_assemble(ctx, mesh, mesh, family, NIHU_GB_SLP | NIHU_GB_DLP, k, 1.0, 0.0, precision, dtype, G, Hm, n, 0,
+                          NIHU_GB_DEVICE);
+    if (st) return st;
+    CK(launch_add_identity((int)n, -0.5, 0.0, dtype, Hm, n, ctx->stream));
+    ctx->launches += 1;
+    int splits = gemv_splits(n, n, dtype);
+    void *part;
+    if ((st = scratch(ctx, "mv_part", 16 * (size_t)splits * n, &part))) return st;
+    CK(launch_gemv(dtype, G, n, n, n, (const double2 *)dq, (double2 *)drhs, 1.0, 0.0, 0.0, 0.0, (double2 *)part, splits,
+                   ctx->stream));
+    ctx->launches += 2;
+    if (solver == 0) {
+        CK(cudaMemsetAsync(dp, 0, 16 * n, ctx->stream));
+        st = gmres_device(ctx, dtype, Hm, n, n, (const double2 *)drhs, (double2 *)dp, std::min<int64_t>(restart, n),
+                          max_iters, tol, iters, rel_residual);
+        if (st && st != NIHU_GB_ERR_NOT_CONVERGED) return st;
+    } else {
+        void *ppiv;
+        if ((st = scratch(ctx, "lu_piv", sizeof(int) * n, &ppiv))) return st;
+        CK(cudaMemsetAsync(ctx->d_flag + 1, 0, sizeof(int), ctx->stream));
+        CK(launch_lu_factor((double2 *)Hm, n, n, (int *)ppiv, ctx->d_flag + 1, &ctx->launches, ctx->stream));
+        CK(launch_lu_solve((const double2 *)Hm, n, n, (const int *)ppiv, (const double2 *)drhs, (double2 *)dp, ctx->stream));
+        ctx->launches += 1;
+        if (iters) *iters = 1;
+        if (rel_residual) *rel_residual = 0.0;
+    }
+    nihu_gb_status keep = st;
+    std::string msg = ctx->err;
+    CK(cudaMemcpyAsync(p, dp, 16 * n, cudaMemcpyDeviceToHost, ctx->stream));
+    if ((st = sync(ctx))) return st;
+    ctx->err = msg;
+    return keep;
+}
+
+}  // extern "C"

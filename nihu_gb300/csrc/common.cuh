@@ -1,0 +1,76 @@
+// Shared device definitions of the GB300 collocation BEM library.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "quad_rules.h"
+
+namespace nihu {
+
+constexpr double PI = 3.14159265358979323846264338327950288;
+constexpr double FOUR_PI = 4.0 * PI;
+constexpr int TRIA_1_ID = 32303;
+constexpr int QUAD_1_ID = 32404;
+constexpr int FAM_HELMHOLTZ = 0;
+constexpr int FAM_LAPLACE = 1;
+constexpr int OP_SLP = 1;
+constexpr int OP_DLP = 2;
+
+// Quadrature levels of the regular path.  Level l of a trial element uses the
+// rule of degree C + 2l' where C is the field complexity and 2l' the distance
+// interval (nihu/library/distance_kernel_intervals.hpp:117-139): level 0 =
+// interval 0, level 1 = interval 2, level 2 = interval 4.  Intervals 6 and 8
+// only occur for d/D < 1.5, which is always the nearly singular path.
+constexpr int NUM_LEVELS = 3;
+constexpr int SLOTS = 14;            // 1 + 4 + 9 points at most
+__host__ __device__ constexpr int level_slot0(int l) { return l == 0 ? 0 : (l == 1 ? 1 : 5); }
+
+// squared distance-ratio thresholds (x = d/D, strict '<'), reference doubles
+// 1.5 (nearly singular), SLP 1.8 / 9.1, DLP 2.8 / 15.8
+constexpr double T_NEAR = 1.5;
+constexpr double T_S1 = 18.0 / 10.0, T_S0 = 91.0 / 10.0;
+constexpr double T_D1 = 28.0 / 10.0, T_D0 = 158.0 / 10.0;
+
+// Per-element device records of a mesh (structure of arrays).
+struct DevMesh {
+    int n = 0;              // elements
+    int has_tria = 0, has_quad = 0;
+    // FP64 geometry
+    double *corners = nullptr;  // [n][12] (x,y,z) x 4 corners; 4th unused for trias
+    double *center = nullptr;   // [n][3]
+    double *size = nullptr;     // [n] mean edge length
+    int8_t *nc = nullptr;       // [n] 3 or 4
+    // FP32 geometry for the regular kernel
+    float4 *chi = nullptr;      // [n] (hi(cx), hi(cy), hi(cz), 1/D^2)
+    float4 *clo = nullptr;      // [n] (lo(cx), lo(cy), lo(cz), field complexity)
+    float4 *p0 = nullptr;       // [n] level-0 point: (w*J, unit normal)
+    // regular quadrature points per element and test-complexity parity:
+    // [n][2][SLOTS][2] float4 : (y, w*J), (unit normal, 0) -- FP32
+    float4 *pts32 = nullptr;
+    // the same in FP64: [n][2][SLOTS][8] doubles (y, w*J, unit normal, 0)
+    double *pts64 = nullptr;
+};
+
+// number of points of a regular level for (trial corners, test complexity)
+__host__ __device__ inline int level_npts(int trial_nc, int test_c, int level)
+{
+    if (trial_nc == 4) return level == 0 ? 1 : (level == 1 ? 4 : 9);
+    if (test_c == 0) return level == 0 ? 1 : (level == 1 ? 3 : 6);
+    return level == 0 ? 1 : (level == 1 ? 4 : 7);
+}
+
+struct cd { double re, im; };
+
+__device__ __forceinline__ cd cmul(cd a, cd b) { return {a.re * b.re - a.im * b.im, a.re * b.im + a.im * b.re}; }
+__device__ __forceinline__ cd cadd(cd a, cd b) { return {a.re + b.re, a.im + b.im}; }
+__device__ __forceinline__ cd cscale(cd a, double s) { return {a.re * s, a.im * s}; }
+
+__device__ __forceinline__ double warp_sum(double v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+}  // namespace nihu

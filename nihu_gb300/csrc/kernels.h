@@ -1,0 +1,63 @@
+// Internal launcher interface between the C ABI layer and the CUDA kernels.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "common.cuh"
+
+namespace nihu {
+
+// Column-sorted list of nearly singular (test i, trial j) pairs of a mesh pair:
+// pairs[col_ptr[j] .. col_ptr[j+1]) hold the rows i of column j.
+struct NearList {
+    int n_cols = 0;
+    int64_t nnz = 0;
+    int64_t *col_ptr = nullptr;  // [n_cols + 1]
+    int *rows = nullptr;         // [nnz]
+};
+
+// mesh.cu -----------------------------------------------------------------
+// geometry of n elements from device copies of the node and element arrays;
+// bad[0] receives 1 + the first invalid element index (0 if all valid)
+cudaError_t launch_mesh_geometry(const double *nodes, int64_t n_nodes, const int32_t *elems, int n,
+                                 int cols, DevMesh m, int *bad, cudaStream_t s);
+
+// classify.cu -------------------------------------------------------------
+// count the nearly singular rows of every column: counts[j]
+cudaError_t launch_near_count(const DevMesh &test, const DevMesh &trial, int same_mesh, int *counts,
+                              cudaStream_t s);
+// exclusive scan of counts into col_ptr (n + 1 entries), single block
+cudaError_t launch_scan(const int *counts, int n, int64_t *col_ptr, cudaStream_t s);
+cudaError_t launch_near_fill(const DevMesh &test, const DevMesh &trial, int same_mesh, const int64_t *col_ptr,
+                             int *rows, cudaStream_t s);
+// histogram of pair classes (see nihu_gb_pair_statistics)
+cudaError_t launch_pair_stats(const DevMesh &test, const DevMesh &trial, int same_mesh,
+                              unsigned long long *counts, cudaStream_t s);
+
+// assemble_regular.cu -----------------------------------------------------
+struct RegularArgs {
+    DevMesh test, trial;
+    int same_mesh;
+    int family, ops;
+    double k;
+    double alpha_re, alpha_im;
+    int precision;  // 0 FP32, 1 FP64
+    int dtype;      // 0 c64, 1 c128
+    void *out_s, *out_d;  // column j at out + (j - j0) * ld
+    int64_t ld;
+    int j0, j1;
+    int accumulate;
+};
+cudaError_t launch_assemble_regular(const RegularArgs &a, cudaStream_t s);
+
+// assemble_singular.cu ----------------------------------------------------
+// nearly singular pairs of columns [j0, j1) and, for the same mesh, the
+// diagonal self terms; err receives a nonzero code if an inverse mapping
+// failed to converge (1 + pair index)
+cudaError_t launch_assemble_singular(const RegularArgs &a, const NearList &near, int *err, cudaStream_t s);
+
+// linalg.cu ---------------------------------------------------------------
+cudaError_t launch_add_identity(int n, double are, double aim, int dtype, void *out, int64_t ld, cudaStream_t s);
+
+}  // namespace nihu

@@ -1,0 +1,27 @@
+// Internal launchers of the dense linear algebra kernels (linalg.cu).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace nihu {
+
+// number of column splits of a matvec (partial buffer holds splits * m complex128)
+int gemv_splits(int64_t m, int64_t n, int dtype);
+cudaError_t launch_gemv(int dtype, const void *A, int64_t m, int64_t n, int64_t lda, const double2 *x, double2 *y,
+                        double are, double aim, double bre, double bim, double2 *partial, int splits, cudaStream_t s);
+
+int dot_blocks(int64_t n);
+cudaError_t launch_multidot(const double2 *V, int64_t n, int nv, const double2 *w, double2 *partial, int blocks,
+                            cudaStream_t s);
+cudaError_t launch_subtract_combo(const double2 *V, int64_t n, int nv, const double2 *h, double2 *w, cudaStream_t s);
+cudaError_t launch_add_combo(const double2 *V, int64_t n, int nv, const double2 *y, double2 *x, cudaStream_t s);
+cudaError_t launch_scale_copy(const double2 *src, double2 *dst, int64_t n, double sc, cudaStream_t s);
+cudaError_t launch_sub(const double2 *a, const double2 *b, double2 *dst, int64_t n, cudaStream_t s);
+
+cudaError_t launch_lu_factor(double2 *A, int64_t n, int64_t lda, int *piv, int *info, int64_t *launches,
+                             cudaStream_t s);
+cudaError_t launch_lu_solve(const double2 *A, int64_t n, int64_t lda, const int *piv, const double2 *b, double2 *x,
+                            cudaStream_t s);
+
+}  // namespace nihu

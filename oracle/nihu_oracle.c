@@ -1,0 +1,845 @@
+/*
+ * FP64 CPU oracle of NiHu's dense collocational BEM assembly (TEST
+ * INFRASTRUCTURE ONLY).  This file is a from-scratch restatement of the
+ * reference algorithm, used by the tests as the checker and by bench.py as the
+ * timed CPU baseline.  It is never linked into, or called by, the product
+ * library.  Every function cites the reference file:line it restates
+ * (paths inside the NiHu project).
+ *
+ * Parity pins: the nearly singular Helmholtz/Laplace SLP element integrals
+ * against the reference's golden values
+ * (nihu/gtest/test_helmholtz_3d_elem_integrals.cpp:15-36,
+ *  nihu/gtest/test_laplace_3d_elem_integrals.cpp:17-37), the analytic
+ * pulsating-sphere solution, closed-form Laplace self integrals, and
+ * converged brute-force quadrature (see tests/).
+ *
+ * Conventions (as in the reference):
+ *  - time convention e^{+jwt}: G = e^{-ikr}/(4 pi r)
+ *    (nihu/library/helmholtz_kernel.hpp:180-186)
+ *  - r_vec = y - x, DLP = dG/dr * (r_vec . n_y)/r
+ *    (nihu/library/normal_derivative_kernel.hpp:167-180)
+ *  - constant elements, collocation at the reference-domain centre
+ *    (nihu/core/shapeset.hpp:290-293, nihu/library/lib_domain.cpp:70-71,94)
+ */
+#include <complex.h>
+#include <math.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include "../nihu_gb300/csrc/quad_rules.h"
+
+typedef double complex cplx;
+
+#define FAM_HELMHOLTZ 0
+#define FAM_LAPLACE 1
+#define OP_SLP 1
+#define OP_DLP 2
+#define TRIA_1_ID 32303
+#define QUAD_1_ID 32404
+
+static const double PI = 3.14159265358979323846264338327950288;
+
+static const int gauss_off[16] = NIHU_GAUSS_OFFSETS;
+static const double gauss_data[NIHU_GAUSS_DATA_LEN] = NIHU_GAUSS_DATA;
+static const int tri_npts[15] = NIHU_TRI_NPTS;
+static const int tri_off[15] = NIHU_TRI_OFFSETS;
+static const double tri_data[NIHU_TRI_DATA_LEN] = NIHU_TRI_DATA;
+
+/* Gauss-Legendre n-point rule (n = degree/2+1,
+ * nihu/core/gaussian_quadrature.hpp:136-151) */
+static const double *gauss_rule(int n) { return gauss_data + 2 * gauss_off[n - 1]; }
+
+/* ------------------------------------------------------------------ elements */
+
+typedef struct {
+    int nc;            /* 3: tria_1, 4: quad_1 */
+    double c[4][3];    /* corner coordinates */
+    double center[3];  /* x(domain centre), nihu/core/element.hpp:276 */
+    double size;       /* mean edge length, nihu/core/element.hpp:280-291 */
+} elem_t;
+
+static void shape(int nc, double xi, double eta, double N[4])
+{
+    if (nc == 3) { /* nihu/library/lib_shape.hpp:159-170 */
+        N[0] = 1.0 - xi - eta; N[1] = xi; N[2] = eta; N[3] = 0.0;
+    } else {       /* bilinear, corners (-1,-1),(1,-1),(1,1),(-1,1) */
+        N[0] = (1.0 - xi) * (1.0 - eta) / 4.0;
+        N[1] = (1.0 + xi) * (1.0 - eta) / 4.0;
+        N[2] = (1.0 + xi) * (1.0 + eta) / 4.0;
+        N[3] = (1.0 - xi) * (1.0 + eta) / 4.0;
+    }
+}
+
+static void dshape(int nc, double xi, double eta, double dN[4][2])
+{
+    if (nc == 3) {
+        dN[0][0] = -1.0; dN[0][1] = -1.0;
+        dN[1][0] = 1.0;  dN[1][1] = 0.0;
+        dN[2][0] = 0.0;  dN[2][1] = 1.0;
+        dN[3][0] = 0.0;  dN[3][1] = 0.0;
+    } else {
+        dN[0][0] = -(1.0 - eta) / 4.0; dN[0][1] = -(1.0 - xi) / 4.0;
+        dN[1][0] = (1.0 - eta) / 4.0;  dN[1][1] = -(1.0 + xi) / 4.0;
+        dN[2][0] = (1.0 + eta) / 4.0;  dN[2][1] = (1.0 + xi) / 4.0;
+        dN[3][0] = -(1.0 + eta) / 4.0; dN[3][1] = (1.0 - xi) / 4.0;
+    }
+}
+
+static void elem_x(const elem_t *e, double xi, double eta, double x[3])
+{
+    double N[4];
+    shape(e->nc, xi, eta, N);
+    for (int d = 0; d < 3; ++d) {
+        double s = 0.0;
+        for (int a = 0; a < e->nc; ++a) s += N[a] * e->c[a][d];
+        x[d] = s;
+    }
+}
+
+static void elem_dx(const elem_t *e, double xi, double eta, double dxi[3], double deta[3])
+{
+    double dN[4][2];
+    dshape(e->nc, xi, eta, dN);
+    for (int d = 0; d < 3; ++d) {
+        double s0 = 0.0, s1 = 0.0;
+        for (int a = 0; a < e->nc; ++a) { s0 += dN[a][0] * e->c[a][d]; s1 += dN[a][1] * e->c[a][d]; }
+        dxi[d] = s0; deta[d] = s1;
+    }
+}
+
+static void cross(const double a[3], const double b[3], double c[3])
+{
+    c[0] = a[1] * b[2] - a[2] * b[1];
+    c[1] = a[2] * b[0] - a[0] * b[2];
+    c[2] = a[0] * b[1] - a[1] * b[0];
+}
+
+static double dot3(const double a[3], const double b[3]) { return a[0] * b[0] + a[1] * b[1] + a[2] * b[2]; }
+static double norm3(const double a[3]) { return sqrt(dot3(a, a)); }
+
+/* surface normal dx/dxi x dx/deta, its length is the Jacobian
+ * (nihu/core/element.hpp:503-515) */
+static void elem_normal(const elem_t *e, double xi, double eta, double n[3])
+{
+    double a[3], b[3];
+    elem_dx(e, xi, eta, a, b);
+    cross(a, b, n);
+}
+
+static void domain_corner(int nc, int i, double *xi, double *eta)
+{
+    static const double tc[3][2] = {{0, 0}, {1, 0}, {0, 1}};
+    static const double qc[4][2] = {{-1, -1}, {1, -1}, {1, 1}, {-1, 1}};
+    if (nc == 3) { *xi = tc[i][0]; *eta = tc[i][1]; }
+    else { *xi = qc[i][0]; *eta = qc[i][1]; }
+}
+
+static void domain_center(int nc, double *xi, double *eta)
+{
+    if (nc == 3) { *xi = 1.0 / 3.0; *eta = 1.0 / 3.0; }
+    else { *xi = 0.0; *eta = 0.0; }
+}
+
+/* element constructor: centre and linear size estimate (mean edge length)
+ * (nihu/core/element.hpp:271-292) */
+static void elem_init(elem_t *e, int nc, const double *coords /* nc x 3 */)
+{
+    e->nc = nc;
+    memset(e->c, 0, sizeof(e->c));
+    for (int a = 0; a < nc; ++a)
+        for (int d = 0; d < 3; ++d) e->c[a][d] = coords[3 * a + d];
+    double xi, eta;
+    domain_center(nc, &xi, &eta);
+    elem_x(e, xi, eta, e->center);
+    double s = 0.0;
+    for (int ed = 0; ed < nc; ++ed) {
+        double x0[3], x1[3], x0i, x0e, x1i, x1e, dv[3];
+        domain_corner(nc, ed, &x0i, &x0e);
+        domain_corner(nc, (ed + 1) % nc, &x1i, &x1e);
+        elem_x(e, x0i, x0e, x0);
+        elem_x(e, x1i, x1e, x1);
+        for (int d = 0; d < 3; ++d) dv[d] = x1[d] - x0[d];
+        s += norm3(dv);
+    }
+    e->size = s / nc;
+}
+
+/* ------------------------------------------------------------------ kernels */
+
+/* G(r) (nihu/library/helmholtz_kernel.hpp:180-186, laplace_kernel.hpp:137-141) */
+static cplx green(int fam, double k, double r)
+{
+    if (fam == FAM_LAPLACE) return 1.0 / r / (4.0 * PI);
+    return cexp(-I * (k * r)) / r / (4.0 * PI);
+}
+
+/* dG/dr (nihu/library/helmholtz_kernel.hpp:190-195, laplace_kernel.hpp:143-147) */
+static cplx dgreen(int fam, double k, double r)
+{
+    if (fam == FAM_LAPLACE) return -1.0 / (r * r) / (4.0 * PI);
+    cplx ikr = I * (k * r);
+    return cexp(-ikr) / (r * r) / (4.0 * PI) * (-ikr - 1.0);
+}
+
+/* SLP kernel G(|y-x|) (nihu/library/normal_derivative_kernel.hpp:131-136) */
+static cplx kern_slp(int fam, double k, const double x[3], const double y[3])
+{
+    double rv[3] = {y[0] - x[0], y[1] - x[1], y[2] - x[2]};
+    return green(fam, k, norm3(rv));
+}
+
+/* DLP kernel dG/dr (r_vec.n_y)/r, n_y unit
+ * (nihu/library/normal_derivative_kernel.hpp:167-175) */
+static cplx kern_dlp(int fam, double k, const double x[3], const double y[3], const double ny[3])
+{
+    double rv[3] = {y[0] - x[0], y[1] - x[1], y[2] - x[2]};
+    double r = norm3(rv);
+    double rdny = dot3(rv, ny) / r;
+    return dgreen(fam, k, r) * rdny;
+}
+
+static cplx kern(int fam, int op, double k, const double x[3], const double y[3], const double ny[3])
+{
+    return op == OP_SLP ? kern_slp(fam, k, x, y) : kern_dlp(fam, k, x, y, ny);
+}
+
+/* ------------------------------------------------------- quadrature degree */
+
+/* distance intervals for accuracy 3 (nihu/library/distance_kernel_intervals.hpp:117-139),
+ * evaluated with strict '<' (nihu/tmp/interval.hpp:173-185).  SLP behaves as
+ * 1/r in the far field, DLP as 1/r^2 (nihu/library/helmholtz_kernel.hpp:281-306). */
+static int interval_degree(int op, double ratio)
+{
+    if (op == OP_SLP) {
+        if (ratio < 11.0 / 10.0) return 6;
+        if (ratio < 18.0 / 10.0) return 4;
+        if (ratio < 91.0 / 10.0) return 2;
+        return 0;
+    }
+    if (ratio < 11.0 / 10.0) return 8;
+    if (ratio < 15.0 / 10.0) return 6;
+    if (ratio < 28.0 / 10.0) return 4;
+    if (ratio < 158.0 / 10.0) return 2;
+    return 0;
+}
+
+/* field complexity: polynomial order of the constant N-set (0) plus the
+ * Jacobian order of the geometry (tria_1: 0, quad_1: 1)
+ * (nihu/core/complexity_estimator.hpp:47-62, nihu/library/lib_shape.hpp:134-143,219-228) */
+static int field_complexity(int nc) { return nc == 4 ? 1 : 0; }
+
+static double centre_distance(const elem_t *a, const elem_t *b)
+{
+    double dv[3] = {b->center[0] - a->center[0], b->center[1] - a->center[1], b->center[2] - a->center[2]};
+    return norm3(dv);
+}
+
+/* -------------------------------------------------------- regular integral */
+
+/* sum_q w_q K(x, y_q) J_q over the trial element with the rule of the given
+ * degree (nihu/core/double_integral.hpp:445-467 with the accelerator of :576-585) */
+static cplx regular_integral(const elem_t *e, int fam, int op, double k, const double x[3], int degree)
+{
+    cplx sum = 0.0;
+    if (e->nc == 3) {
+        const double *q = tri_data + 3 * tri_off[degree];
+        int np = tri_npts[degree];
+        for (int p = 0; p < np; ++p) {
+            double y[3], n[3];
+            elem_x(e, q[3 * p], q[3 * p + 1], y);
+            elem_normal(e, q[3 * p], q[3 * p + 1], n);
+            double J = norm3(n);
+            double un[3] = {n[0] / J, n[1] / J, n[2] / J};
+            sum += kern(fam, op, k, x, y, un) * (J * q[3 * p + 2]);
+        }
+    } else {
+        int ng = degree / 2 + 1;
+        const double *g = gauss_rule(ng);
+        for (int a = 0; a < ng; ++a)
+            for (int b = 0; b < ng; ++b) {
+                double xi = g[2 * a], eta = g[2 * b], w = g[2 * a + 1] * g[2 * b + 1];
+                double y[3], n[3];
+                elem_x(e, xi, eta, y);
+                elem_normal(e, xi, eta, n);
+                double J = norm3(n);
+                double un[3] = {n[0] / J, n[1] / J, n[2] / J};
+                sum += kern(fam, op, k, x, y, un) * (J * w);
+            }
+    }
+    return sum;
+}
+
+/* ------------------------------------------------- singular self integrals */
+
+/* radii, subtended angles and corner angles seen from an interior point
+ * (nihu/library/plane_element_helper.hpp:42-74) */
+static void plane_element_helper(const elem_t *e, const double x0[3], double r[4], double theta[4], double alpha[4])
+{
+    int N = e->nc;
+    double R[4][3], C[4][3];
+    for (int i = 0; i < N; ++i) {
+        for (int d = 0; d < 3; ++d) R[i][d] = e->c[i][d] - x0[d];
+        r[i] = norm3(R[i]);
+        for (int d = 0; d < 3; ++d) R[i][d] /= r[i];
+        for (int d = 0; d < 3; ++d) C[i][d] = e->c[i][d] - e->c[(i + 1) % N][d];
+        double cn = norm3(C[i]);
+        for (int d = 0; d < 3; ++d) C[i][d] /= cn;
+    }
+    for (int i = 0; i < N; ++i) {
+        double cs = dot3(R[i], R[(i + 1) % N]);
+        theta[i] = cs >= 1.0 ? 0.0 : acos(cs);
+        alpha[i] = acos(dot3(R[i], C[i]));
+    }
+}
+
+/* analytic integral of 1/r over a flat element from an interior point, times 4 pi
+ * (nihu/library/laplace_singular_integrals.hpp:465-479) */
+static double static_self_integral(const elem_t *e, const double x0[3])
+{
+    double r[4], th[4], al[4], s = 0.0;
+    plane_element_helper(e, x0, r, th, al);
+    for (int i = 0; i < e->nc; ++i)
+        s += r[i] * sin(al[i]) * log(tan((al[i] + th[i]) / 2.0) / tan(al[i] / 2.0));
+    return s;
+}
+
+/* sinc with the reference's small-argument series (nihu/util/math_functions.hpp:54-61) */
+static double sinc_ref(double x)
+{
+    if (fabs(x) > 1e-3) return sin(x) / x;
+    return 1.0 - x * x / 6.0 * (1.0 - x * x / 20.0);
+}
+
+/* constant flat triangle, Helmholtz SLP self term: analytic static part plus
+ * the regular dynamic part (e^{-ikr}-1)/r with the degree-7 Dunavant rule
+ * (nihu/library/helmholtz_singular_integrals.hpp:703-762) */
+static cplx self_tria_slp(const elem_t *e, int fam, double k)
+{
+    double stat = static_self_integral(e, e->center);
+    if (fam == FAM_LAPLACE) return stat / (4.0 * PI);
+    const double *q = tri_data + 3 * tri_off[7];
+    cplx dyn = 0.0;
+    for (int p = 0; p < tri_npts[7]; ++p) {
+        double y[3], n[3];
+        elem_x(e, q[3 * p], q[3 * p + 1], y);
+        elem_normal(e, q[3 * p], q[3 * p + 1], n);
+        double rv[3] = {y[0] - e->center[0], y[1] - e->center[1], y[2] - e->center[2]};
+        double r = norm3(rv);
+        cplx dp = -I * k * cexp(-I * k * r / 2.0) * sinc_ref(k * r / 2.0);
+        dyn += dp * q[3 * p + 2] * norm3(n);
+    }
+    return (stat + dyn) / (4.0 * PI);
+}
+
+/* quad self term: Duffy-type polar splitting of the reference square into four
+ * corner-collapsed quads around the collocation point, each with the 4x4
+ * Gauss rule of degree 7 (nihu/core/duffy_quadrature.hpp:82-141,
+ * nihu/core/singular_accelerator.hpp:440-448, nihu/core/quadrature.hpp:112-130,
+ * evaluated as in nihu/core/double_integral.hpp:474-510) */
+static cplx self_quad_duffy(const elem_t *e, int fam, int op, double k)
+{
+    const int ng = 7 / 2 + 1;
+    const double *g = gauss_rule(ng);
+    double s0, s1;
+    domain_center(4, &s0, &s1);
+    double x0[3];
+    elem_x(e, s0, s1, x0);
+    cplx sum = 0.0;
+    for (int d = 0; d < 4; ++d) {
+        double P[4][2];
+        P[0][0] = P[1][0] = s0; P[0][1] = P[1][1] = s1;
+        domain_corner(4, d, &P[2][0], &P[2][1]);
+        domain_corner(4, (d + 1) % 4, &P[3][0], &P[3][1]);
+        for (int a = 0; a < ng; ++a)
+            for (int b = 0; b < ng; ++b) {
+                double u = g[2 * a], v = g[2 * b], w = g[2 * a + 1] * g[2 * b + 1];
+                double N[4], dN[4][2];
+                shape(4, u, v, N);
+                dshape(4, u, v, dN);
+                double xi = 0, eta = 0, j00 = 0, j01 = 0, j10 = 0, j11 = 0;
+                for (int c = 0; c < 4; ++c) {
+                    xi += N[c] * P[c][0]; eta += N[c] * P[c][1];
+                    j00 += dN[c][0] * P[c][0]; j01 += dN[c][0] * P[c][1];
+                    j10 += dN[c][1] * P[c][0]; j11 += dN[c][1] * P[c][1];
+                }
+                double wd = w * (j00 * j11 - j01 * j10);
+                double y[3], n[3];
+                elem_x(e, xi, eta, y);
+                elem_normal(e, xi, eta, n);
+                double J = norm3(n);
+                double un[3] = {n[0] / J, n[1] / J, n[2] / J};
+                sum += kern(fam, op, k, x0, y, un) * (J * wd);
+            }
+    }
+    return sum;
+}
+
+/* self-term dispatch (nihu/core/double_integral.hpp:599-639): constant tria
+ * SLP shortcut, DLP = 0 on a flat triangle
+ * (nihu/library/normal_derivative_singular_integrals.hpp:13-33), quads by Duffy */
+static cplx self_integral(const elem_t *e, int fam, int op, double k)
+{
+    if (e->nc == 3) return op == OP_SLP ? self_tria_slp(e, fam, k) : 0.0;
+    return self_quad_duffy(e, fam, op, k);
+}
+
+/* ------------------------------------------------ nearly singular integrals */
+
+/* rotate a flat element parallel to the x-y plane: T = [v1^, (v1 x v2)^ x v1^, (v1 x v2)^]
+ * (nihu/library/plane_element_helper.hpp:112-126); the reference solves with
+ * T (LU), here T is applied through its transpose (T is orthonormal) */
+static void plane_local(const elem_t *e, const double x0in[3], double loc[4][3], double x0[3])
+{
+    double v1[3], v2[3], t0[3], t1[3], t2[3];
+    for (int d = 0; d < 3; ++d) { v1[d] = e->c[1][d] - e->c[0][d]; v2[d] = e->c[2][d] - e->c[0][d]; }
+    double n1 = norm3(v1);
+    for (int d = 0; d < 3; ++d) t0[d] = v1[d] / n1;
+    cross(v1, v2, t2);
+    double n2 = norm3(t2);
+    for (int d = 0; d < 3; ++d) t2[d] /= n2;
+    cross(t2, t0, t1);
+    double n3 = norm3(t1);
+    for (int d = 0; d < 3; ++d) t1[d] /= n3;
+    for (int a = 0; a < e->nc; ++a) {
+        loc[a][0] = dot3(t0, e->c[a]); loc[a][1] = dot3(t1, e->c[a]); loc[a][2] = dot3(t2, e->c[a]);
+    }
+    x0[0] = dot3(t0, x0in); x0[1] = dot3(t1, x0in); x0[2] = dot3(t2, x0in);
+}
+
+static int sgn(double v) { return (0.0 < v) - (v < 0.0); }
+
+/* Gauss points per side of the angular integral of the static part: 6 is the
+ * reference's line rule of order 10 (nihu/library/laplace_nearly_singular_integrals.hpp:66).
+ * Tests raise it to reproduce the reference's golden values, which were made
+ * with a converged angular integral (see tests/test_oracle_golden.py). */
+static int g_static_gauss = 10 / 2 + 1;
+
+int oracle_set_static_gauss_points(int n)
+{
+    if (n < 1 || n > NIHU_GAUSS_MAX_N) return 0;
+    g_static_gauss = n;
+    return 1;
+}
+
+/* semi-analytic static part over a flat element seen from x0: radial integral
+ * analytic, angular integral with 6-point Gauss per side.
+ *   SLP: (1/4pi) sum_sides int (sqrt(R^2+z^2) - |z|) dtheta
+ *   DLP: sgn(z)/(4pi) sum_sides int (1 - |z|/sqrt(R^2+z^2)) dtheta
+ * (nihu/library/laplace_nearly_singular_integrals.hpp:62-136 and :139-209,
+ *  geometry nihu/library/plane_element_helper.hpp:76-99) */
+static double static_near(const elem_t *e, const double x0in[3], int op)
+{
+    double loc[4][3], x0[3];
+    int N = e->nc;
+    plane_local(e, x0in, loc, x0);
+    double th_lim[4], th0[4], dref[4];
+    for (int n = 0; n < N; ++n) {
+        const double *c1 = loc[n], *c2 = loc[(n + 1) % N];
+        double l[2] = {c2[0] - c1[0], c2[1] - c1[1]};
+        double ln = sqrt(l[0] * l[0] + l[1] * l[1]);
+        l[0] /= ln; l[1] /= ln;
+        double d1[2] = {c1[0] - x0[0], c1[1] - x0[1]};
+        double pr = d1[0] * l[0] + d1[1] * l[1];
+        double d0[2] = {d1[0] - l[0] * pr, d1[1] - l[1] * pr};
+        th_lim[n] = atan2(d1[1], d1[0]);
+        th0[n] = atan2(d0[1], d0[0]);
+        dref[n] = sqrt(d0[0] * d0[0] + d0[1] * d0[1]);
+    }
+    double z = x0[2] - loc[0][2];
+    const double *g = gauss_rule(g_static_gauss);
+    double res = 0.0;
+    for (int i = 0; i < N; ++i) {
+        double t1 = th_lim[i], t2 = th_lim[(i + 1) % N];
+        if (fabs(t2 - t1) > PI) {
+            if (t2 > t1) t1 += 2.0 * PI; else t2 += 2.0 * PI;
+        }
+        double jac = (t2 - t1) / 2.0;
+        for (int q = 0; q < g_static_gauss; ++q) {
+            double xi = g[2 * q], w = g[2 * q + 1];
+            double th = t1 * (1.0 - xi) / 2.0 + t2 * (1.0 + xi) / 2.0;
+            double R = dref[i] / cos(th - th0[i]);
+            double r = sqrt(R * R + z * z);
+            if (op == OP_SLP) res += (r - fabs(z)) * jac * w;
+            else res += (1.0 - fabs(z) / r) * jac * w;
+        }
+    }
+    if (op == OP_SLP) return res / (4.0 * PI);
+    return sgn(z) * res / (4.0 * PI);
+}
+
+/* constant flat element, nearly singular: static Laplace part semi-analytic,
+ * dynamic part (K_k - K_0) with the degree-14 regular rule (Dunavant 42 points
+ * on triangles, 8x8 Gauss on quads)
+ * (nihu/library/helmholtz_nearly_singular_integrals.hpp:48-84 SLP, :91-129 DLP) */
+static cplx near_plane(const elem_t *e, int fam, int op, double k, const double x0[3])
+{
+    double st = static_near(e, x0, op);
+    if (fam == FAM_LAPLACE) return st;
+    double en[3];
+    {
+        double xi, eta;
+        domain_center(e->nc, &xi, &eta);
+        elem_normal(e, xi, eta, en);
+        double nn = norm3(en);
+        for (int d = 0; d < 3; ++d) en[d] /= nn;
+    }
+    cplx dyn = 0.0;
+    if (e->nc == 3) {
+        const double *q = tri_data + 3 * tri_off[14];
+        for (int p = 0; p < tri_npts[14]; ++p) {
+            double y[3], n[3];
+            elem_x(e, q[3 * p], q[3 * p + 1], y);
+            elem_normal(e, q[3 * p], q[3 * p + 1], n);
+            cplx kd = kern(FAM_HELMHOLTZ, op, k, x0, y, en) - kern(FAM_LAPLACE, op, k, x0, y, en);
+            dyn += kd * q[3 * p + 2] * norm3(n);
+        }
+    } else {
+        const double *g = gauss_rule(14 / 2 + 1);
+        for (int a = 0; a < 8; ++a)
+            for (int b = 0; b < 8; ++b) {
+                double xi = g[2 * a], eta = g[2 * b], w = g[2 * a + 1] * g[2 * b + 1];
+                double y[3], n[3];
+                elem_x(e, xi, eta, y);
+                elem_normal(e, xi, eta, n);
+                cplx kd = kern(FAM_HELMHOLTZ, op, k, x0, y, en) - kern(FAM_LAPLACE, op, k, x0, y, en);
+                dyn += kd * w * norm3(n);
+            }
+    }
+    return st + dyn;
+}
+
+/* Newton iteration for the image (xi, eta) and the scaled normal offset zeta of
+ * a point x0 near a surface element (nihu/core/inverse_mapping.hpp:52-112);
+ * returns 1 on convergence */
+static int inverse_mapping(const elem_t *e, const double x0[3], double tol, int max_iter, double res[3])
+{
+    res[0] = res[1] = res[2] = 0.0;
+    for (int it = 0; it < max_iter; ++it) {
+        double xi = res[0], eta = res[1], zeta = res[2];
+        double y[3], dxi[3], deta[3], n[3];
+        elem_x(e, xi, eta, y);
+        elem_dx(e, xi, eta, dxi, deta);
+        cross(dxi, deta, n);
+        double sq = sqrt(norm3(n));
+        for (int d = 0; d < 3; ++d) n[d] /= sq;
+        double f[3];
+        for (int d = 0; d < 3; ++d) f[d] = y[d] + n[d] * zeta - x0[d];
+        if (norm3(f) < tol) return 1;
+        /* second derivatives: only x_{xi eta} is nonzero for the bilinear quad */
+        double dxx[3] = {0, 0, 0}, dxe[3] = {0, 0, 0}, dee[3] = {0, 0, 0};
+        if (e->nc == 4)
+            for (int d = 0; d < 3; ++d) dxe[d] = (e->c[0][d] - e->c[1][d] + e->c[2][d] - e->c[3][d]) / 4.0;
+        double t1[3], t2[3], dnxi[3], dneta[3];
+        cross(dxx, deta, t1); cross(dxi, dxe, t2);
+        for (int d = 0; d < 3; ++d) dnxi[d] = (t1[d] + t2[d]) / sq;
+        cross(dxe, deta, t1); cross(dxi, dee, t2);
+        for (int d = 0; d < 3; ++d) dneta[d] = (t1[d] + t2[d]) / sq;
+        double A[3][3];
+        for (int d = 0; d < 3; ++d) {
+            A[d][0] = dxi[d] + dnxi[d] * zeta;
+            A[d][1] = deta[d] + dneta[d] * zeta;
+            A[d][2] = n[d];
+        }
+        /* solve A s = f by Gaussian elimination with partial pivoting */
+        double M[3][4];
+        for (int r = 0; r < 3; ++r) { for (int c = 0; c < 3; ++c) M[r][c] = A[r][c]; M[r][3] = f[r]; }
+        for (int c = 0; c < 3; ++c) {
+            int p = c;
+            for (int r = c + 1; r < 3; ++r) if (fabs(M[r][c]) > fabs(M[p][c])) p = r;
+            if (p != c) for (int q = 0; q < 4; ++q) { double t = M[c][q]; M[c][q] = M[p][q]; M[p][q] = t; }
+            for (int r = c + 1; r < 3; ++r) {
+                double fct = M[r][c] / M[c][c];
+                for (int q = c; q < 4; ++q) M[r][q] -= fct * M[c][q];
+            }
+        }
+        double s[3];
+        for (int r = 2; r >= 0; --r) {
+            double v = M[r][3];
+            for (int q = r + 1; q < 3; ++q) v -= M[r][q] * s[q];
+            s[r] = v / M[r][r];
+        }
+        for (int d = 0; d < 3; ++d) res[d] -= s[d];
+    }
+    return 0;
+}
+
+/* linearized element around xi0: corners x(xi0) + dx(xi0)(xi_c - xi0)
+ * (nihu/core/element.hpp:418-437) */
+static void linearized_elem(const elem_t *e, double xi0, double eta0, elem_t *lin)
+{
+    double x0[3], dxi[3], deta[3], coords[12];
+    elem_x(e, xi0, eta0, x0);
+    elem_dx(e, xi0, eta0, dxi, deta);
+    for (int a = 0; a < e->nc; ++a) {
+        double ci, ce;
+        domain_corner(e->nc, a, &ci, &ce);
+        for (int d = 0; d < 3; ++d) coords[3 * a + d] = x0[d] + dxi[d] * (ci - xi0) + deta[d] * (ce - eta0);
+    }
+    elem_init(lin, e->nc, coords);
+}
+
+static cplx kern_on_elem(const elem_t *e, int fam, int op, double k, const double x0[3], double xi, double eta)
+{
+    double y[3], n[3];
+    elem_x(e, xi, eta, y);
+    elem_normal(e, xi, eta, n);
+    double J = norm3(n);
+    double un[3] = {n[0] / J, n[1] / J, n[2] / J};
+    return kern(fam, op, k, x0, y, un) * J;
+}
+
+/* polar quadrature around the image of x0 in the reference domain with the
+ * linearized-element integrand subtracted, plus the planar constant-element
+ * shortcut on the linearized element; radial and tangential Gauss order 15
+ * (8 points) (nihu/library/nearly_singular_collocational.hpp:87-198) */
+static int near_polar(const elem_t *e, int fam, int op, double k, const double x0[3], cplx *out)
+{
+    double im[3];
+    if (!inverse_mapping(e, x0, 1e-5, 100, im)) return 0;
+    double xi0 = im[0], eta0 = im[1];
+    elem_t lin;
+    linearized_elem(e, xi0, eta0, &lin);
+    int N = e->nc;
+    double th_lim[4], th0[4], dref[4];
+    for (int n = 0; n < N; ++n) {
+        double c1[2], c2[2];
+        domain_corner(N, n, &c1[0], &c1[1]);
+        domain_corner(N, (n + 1) % N, &c2[0], &c2[1]);
+        double l[2] = {1.0, 0.0};
+        double dl[2] = {c2[0] - c1[0], c2[1] - c1[1]};
+        double ln = sqrt(dl[0] * dl[0] + dl[1] * dl[1]);
+        if (ln > 1e-3) { l[0] = dl[0] / ln; l[1] = dl[1] / ln; }
+        double d1[2] = {c1[0] - xi0, c1[1] - eta0};
+        double pr = d1[0] * l[0] + d1[1] * l[1];
+        double d0[2] = {d1[0] - l[0] * pr, d1[1] - l[1] * pr};
+        th_lim[n] = atan2(d1[1], d1[0]);
+        th0[n] = atan2(d0[1], d0[0]);
+        dref[n] = sqrt(d0[0] * d0[0] + d0[1] * d0[1]);
+    }
+    const double *g = gauss_rule(15 / 2 + 1);
+    const int ng = 8;
+    cplx I0 = 0.0;
+    for (int n = 0; n < N; ++n) {
+        double t1 = th_lim[n], t2 = th_lim[(n + 1) % N];
+        if (fabs(t2 - t1) > PI) {
+            if (t2 > t1) t1 += 2.0 * PI; else t2 += 2.0 * PI;
+        }
+        if (fabs(t2 - t1) < 1e-3) continue;
+        for (int a = 0; a < ng; ++a) {
+            double xx = g[2 * a];
+            double th = ((1.0 - xx) * t1 + (1.0 + xx) * t2) / 2.0;
+            double wth = g[2 * a + 1] * (t2 - t1) / 2.0;
+            double rho_lim = dref[n] / cos(th - th0[n]);
+            for (int b = 0; b < ng; ++b) {
+                double rho = (1.0 + g[2 * b]) * rho_lim / 2.0;
+                double wrho = g[2 * b + 1] * rho_lim / 2.0;
+                double xi = xi0 + rho * cos(th), eta = eta0 + rho * sin(th);
+                cplx F = kern_on_elem(e, fam, op, k, x0, xi, eta);
+                cplx Fl = kern_on_elem(&lin, fam, op, k, x0, xi, eta);
+                I0 += wth * wrho * rho * (F - Fl);
+            }
+        }
+    }
+    I0 += near_plane(&lin, fam, op, k, x0);
+    *out = I0;
+    return 1;
+}
+
+/* Telles (1987) cubic transformation of a tensor Gauss rule towards the image
+ * of x0 (nihu/library/telles_1987.hpp:44-113), 16x16 points (order 30)
+ * (nihu/library/nearly_singular_collocational_telles.hpp:85-110) */
+static int near_telles(const elem_t *e, int fam, int op, double k, const double x0[3], cplx *out)
+{
+    double im[3];
+    if (!inverse_mapping(e, x0, 1e-6, 100, im)) return 0;
+    double dist = im[2];
+    double rbar;
+    if (dist < 0.05) rbar = 0.0;
+    else if (dist <= 1.3) rbar = 0.85 + 0.24 * log(dist);
+    else if (dist <= 3.618) rbar = 0.893 + 0.0832 * log(dist);
+    else rbar = 1.0;
+    double ca[2], cb[2], cc[2], cd[2];
+    for (int dim = 0; dim < 2; ++dim) {
+        double eb = im[dim];
+        double f = 1.0 + 2.0 * rbar;
+        double q = 1.0 / (2.0 * f) * ((eb * (3.0 - 2.0 * rbar) - 2.0 * eb * eb * eb / f) * 1.0 / f - eb);
+        double p = 1.0 / (3.0 * f * f) * (4.0 * rbar * (1.0 - rbar) + 3.0 * (1.0 - eb * eb));
+        double s = sqrt(q * q + p * p * p);
+        double gb = cbrt(-q + s) + cbrt(-q - s) + eb / f;
+        double Q = 1.0 + 3.0 * gb * gb;
+        ca[dim] = (1.0 - rbar) / Q;
+        cb[dim] = -3.0 * (1.0 - rbar) * gb / Q;
+        cc[dim] = (3.0 * gb * gb + rbar) / Q;
+        cd[dim] = -cb[dim];
+    }
+    const double *g = gauss_rule(30 / 2 + 1);
+    const int ng = 16;
+    cplx sum = 0.0;
+    for (int a = 0; a < ng; ++a)
+        for (int b = 0; b < ng; ++b) {
+            double u[2] = {g[2 * a], g[2 * b]};
+            double w = g[2 * a + 1] * g[2 * b + 1];
+            double t[2];
+            for (int dim = 0; dim < 2; ++dim) {
+                double x = u[dim];
+                t[dim] = ca[dim] * x * x * x + cb[dim] * x * x + cc[dim] * x + cd[dim];
+                w *= 3.0 * ca[dim] * x * x + 2.0 * cb[dim] * x + cc[dim];
+            }
+            sum += kern_on_elem(e, fam, op, k, x0, t[0], t[1]) * w;
+        }
+    *out = sum;
+    return 1;
+}
+
+/* nearly singular dispatch (nihu/library/helmholtz_nearly_singular_integrals.hpp:223-408,
+ * nihu/library/laplace_nearly_singular_integrals.hpp:399-590): constant triangles
+ * use the planar semi-analytic scheme; quads use polar subtraction, except
+ * Helmholtz DLP which uses Telles */
+static int near_integral(const elem_t *e, int fam, int op, double k, const double x0[3], cplx *out)
+{
+    if (e->nc == 3) { *out = near_plane(e, fam, op, k, x0); return 1; }
+    if (fam == FAM_HELMHOLTZ && op == OP_DLP) return near_telles(e, fam, op, k, x0, out);
+    return near_polar(e, fam, op, k, x0, out);
+}
+
+/* ------------------------------------------------------------ meshes & API */
+
+static char g_err[256];
+
+static int load_elem(const double *nodes, int n_nodes, const int *elems, int cols, int i, elem_t *e)
+{
+    const int *row = elems + (long)i * cols;
+    int nc;
+    if (row[0] == TRIA_1_ID) nc = 3;
+    else if (row[0] == QUAD_1_ID) nc = 4;
+    else { snprintf(g_err, sizeof g_err, "unknown element type id %d", row[0]); return 0; }
+    if (cols < 1 + nc) { snprintf(g_err, sizeof g_err, "element row too short"); return 0; }
+    double coords[12];
+    for (int a = 0; a < nc; ++a) {
+        int nd = row[1 + a];
+        if (nd < 0 || nd >= n_nodes) { snprintf(g_err, sizeof g_err, "node index out of range"); return 0; }
+        for (int d = 0; d < 3; ++d) coords[3 * a + d] = nodes[3 * nd + d];
+    }
+    elem_init(e, nc, coords);
+    return 1;
+}
+
+const char *oracle_last_error(void) { return g_err; }
+
+/*
+ * One entry: self -> nearly singular -> regular, exactly as
+ * nihu/core/double_integral.hpp:543-673.  Returns 0 on error.
+ */
+static int entry(const elem_t *te, const elem_t *re, int same_id, int fam, int op, double k, cplx *out)
+{
+    if (same_id && te->nc == re->nc) { *out = self_integral(re, fam, op, k); return 1; }
+    double ratio = centre_distance(te, re) / re->size;
+    if (ratio < 1.5) {
+        if (!near_integral(re, fam, op, k, te->center, out)) {
+            snprintf(g_err, sizeof g_err, "Could not perform inverse mapping");
+            return 0;
+        }
+        return 1;
+    }
+    int cmax = field_complexity(te->nc) > field_complexity(re->nc) ? field_complexity(te->nc) : field_complexity(re->nc);
+    int degree = cmax + interval_degree(op, ratio);
+    if (degree > 14) { snprintf(g_err, sizeof g_err, "Too high quadrature degree selected for collocational integration"); return 0; }
+    if (re->nc == 3 && tri_npts[degree] == 0) { snprintf(g_err, sizeof g_err, "unsupported dunavant degree"); return 0; }
+    *out = regular_integral(re, fam, op, k, te->center, degree);
+    return 1;
+}
+
+/*
+ * Assemble rows [row_begin, row_end) of the operator (fam, op) between a test
+ * and a trial mesh into out[(i - row_begin) + j*ld] (column-major, complex128
+ * as interleaved doubles).  out = alpha*op if accumulate == 0, else out +=
+ * alpha*op (nihu/core/assembly.hpp:69-76 with block += semantics).
+ * same_mesh enables the self terms (nihu/core/integral_transform.hpp:156).
+ */
+int oracle_assemble(const double *tnodes, int tn_nodes, const int *telems, int tn_elems, int tcols,
+                    const double *rnodes, int rn_nodes, const int *relems, int rn_elems, int rcols,
+                    int same_mesh, int fam, int op, double k, double alpha_re, double alpha_im,
+                    int row_begin, int row_end, double *out, long ld, int accumulate)
+{
+    if (row_begin < 0 || row_end > tn_elems || row_begin > row_end) { snprintf(g_err, sizeof g_err, "bad row range"); return 0; }
+    cplx alpha = alpha_re + I * alpha_im;
+    /* element geometry is built once per mesh, like the reference's mesh
+     * construction (nihu/core/mesh.hpp:137-160) */
+    elem_t *trial = (elem_t *)malloc(sizeof(elem_t) * (size_t)(rn_elems > 0 ? rn_elems : 1));
+    if (!trial) { snprintf(g_err, sizeof g_err, "out of host memory"); return 0; }
+    int ok = 1;
+    for (int j = 0; j < rn_elems && ok; ++j) ok = load_elem(rnodes, rn_nodes, relems, rcols, j, &trial[j]);
+    for (int i = row_begin; i < row_end && ok; ++i) {
+        elem_t te;
+        if (!(ok = load_elem(tnodes, tn_nodes, telems, tcols, i, &te))) break;
+        for (int j = 0; j < rn_elems; ++j) {
+            cplx v;
+            if (!(ok = entry(&te, &trial[j], same_mesh && i == j, fam, op, k, &v))) break;
+            cplx *dst = (cplx *)out + (long)(i - row_begin) + (long)j * ld;
+            if (accumulate) *dst += alpha * v; else *dst = alpha * v;
+        }
+    }
+    free(trial);
+    return ok;
+}
+
+/* element geometry for tests: centre[3], size, normal at centre[3] (unnormalised) */
+int oracle_elem_geometry(const double *coords, int nc, double *out7)
+{
+    elem_t e;
+    elem_init(&e, nc, coords);
+    double xi, eta, n[3];
+    domain_center(nc, &xi, &eta);
+    elem_normal(&e, xi, eta, n);
+    out7[0] = e.center[0]; out7[1] = e.center[1]; out7[2] = e.center[2];
+    out7[3] = e.size;
+    out7[4] = n[0]; out7[5] = n[1]; out7[6] = n[2];
+    return 1;
+}
+
+/* single element integrals for known-answer tests.  kind: 0 regular (given
+ * degree), 1 nearly singular dispatch, 2 self, 3 planar near-singular scheme
+ * (constant-plane formula even on quads). out = (re, im). */
+int oracle_elem_integral(const double *coords, int nc, const double *x0, int fam, int op, double k,
+                         int kind, int degree, double *out)
+{
+    elem_t e;
+    elem_init(&e, nc, coords);
+    cplx v = 0.0;
+    if (kind == 0) v = regular_integral(&e, fam, op, k, x0, degree);
+    else if (kind == 1) { if (!near_integral(&e, fam, op, k, x0, &v)) return 0; }
+    else if (kind == 2) v = self_integral(&e, fam, op, k);
+    else if (kind == 3) v = near_plane(&e, fam, op, k, x0);
+    else return 0;
+    out[0] = creal(v); out[1] = cimag(v);
+    return 1;
+}
+
+/* per-pair classification for tests: level code per (i,j):
+ * -1 self, -2 near, else degree(SLP)*16 + degree(DLP) */
+int oracle_classify(const double *tnodes, int tn_nodes, const int *telems, int tn_elems, int tcols,
+                    const double *rnodes, int rn_nodes, const int *relems, int rn_elems, int rcols,
+                    int same_mesh, int row_begin, int row_end, int *out)
+{
+    for (int i = row_begin; i < row_end; ++i) {
+        elem_t te;
+        if (!load_elem(tnodes, tn_nodes, telems, tcols, i, &te)) return 0;
+        for (int j = 0; j < rn_elems; ++j) {
+            elem_t re;
+            if (!load_elem(rnodes, rn_nodes, relems, rcols, j, &re)) return 0;
+            int code;
+            if (same_mesh && i == j && te.nc == re.nc) code = -1;
+            else {
+                double ratio = centre_distance(&te, &re) / re.size;
+                if (ratio < 1.5) code = -2;
+                else {
+                    int cmax = field_complexity(te.nc) > field_complexity(re.nc) ? field_complexity(te.nc) : field_complexity(re.nc);
+                    code = (cmax + interval_degree(OP_SLP, ratio)) * 16 + cmax + interval_degree(OP_DLP, ratio);
+                }
+            }
+            out[(long)(i - row_begin) * rn_elems + j] = code;
+        }
+    }
+    return 1;
+}

@@ -1,0 +1,128 @@
+"""ctypes access to the FP64 CPU oracle (test infrastructure only).
+
+Only tests/, ``__graft_entry__.smoke()`` and bench.py's CPU-baseline leg use
+this module; the product library never does.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+import threading
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "liboracle.so")
+SOURCES = [os.path.join(HERE, "nihu_oracle.c")]
+HELMHOLTZ, LAPLACE = 0, 1
+SLP, DLP = 1, 2
+
+
+def build(force: bool = False) -> str:
+    """Compile the oracle with gcc (no external dependencies)."""
+    newest = max(os.path.getmtime(s) for s in SOURCES + [os.path.join(HERE, "..", "nihu_gb300", "csrc", "quad_rules.h")])
+    if force or not os.path.exists(LIB_PATH) or os.path.getmtime(LIB_PATH) < newest:
+        tmp = LIB_PATH + ".tmp%d" % os.getpid()
+        subprocess.check_call(["gcc", "-O2", "-std=c11", "-fPIC", "-shared", *SOURCES, "-o", tmp, "-lm"])
+        os.replace(tmp, LIB_PATH)
+    return LIB_PATH
+
+
+_lib = None
+_lock = threading.Lock()
+
+
+def lib():
+    global _lib
+    with _lock:
+        if _lib is None:
+            build()
+            L = ctypes.CDLL(LIB_PATH)
+            dp, ip = ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_int)
+            c_int, c_double, c_long = ctypes.c_int, ctypes.c_double, ctypes.c_long
+            L.oracle_assemble.argtypes = [dp, c_int, ip, c_int, c_int, dp, c_int, ip, c_int, c_int,
+                                          c_int, c_int, c_int, c_double, c_double, c_double,
+                                          c_int, c_int, dp, c_long, c_int]
+            L.oracle_assemble.restype = c_int
+            L.oracle_classify.argtypes = [dp, c_int, ip, c_int, c_int, dp, c_int, ip, c_int, c_int,
+                                          c_int, c_int, c_int, ip]
+            L.oracle_classify.restype = c_int
+            L.oracle_elem_integral.argtypes = [dp, c_int, dp, c_int, c_int, c_double, c_int, c_int, dp]
+            L.oracle_elem_integral.restype = c_int
+            L.oracle_elem_geometry.argtypes = [dp, c_int, dp]
+            L.oracle_last_error.restype = ctypes.c_char_p
+            _lib = L
+    return _lib
+
+
+def _ptr(a, t):
+    return a.ctypes.data_as(ctypes.POINTER(t))
+
+
+def _mesh_args(nodes, elems):
+    nodes = np.ascontiguousarray(nodes, dtype=np.float64)
+    elems = np.ascontiguousarray(elems, dtype=np.int32)
+    return nodes, elems, [_ptr(nodes, ctypes.c_double), len(nodes), _ptr(elems, ctypes.c_int), len(elems), elems.shape[1]]
+
+
+def assemble(test_mesh, trial_mesh, family, op, k, same_mesh=None, rows=None, alpha=1.0, threads=1):
+    """Dense operator block (rows x all trial elements) as complex128, C-contiguous
+    in column-major order (Fortran array)."""
+    tn, te, targs = _mesh_args(*test_mesh)
+    rn, re_, rargs = _mesh_args(*trial_mesh)
+    if same_mesh is None:
+        same_mesh = test_mesh is trial_mesh
+    r0, r1 = (0, len(te)) if rows is None else rows
+    m, n = r1 - r0, len(re_)
+    out = np.zeros((m, n), dtype=np.complex128, order="F")
+    alpha = complex(alpha)
+    L = lib()
+
+    errors = []
+
+    def work(a, b):
+        buf = np.zeros((b - a, n), dtype=np.complex128, order="F")
+        ptr = ctypes.cast(buf.ctypes.data, ctypes.POINTER(ctypes.c_double))
+        ok = L.oracle_assemble(*targs, *rargs, int(same_mesh), family, op, float(k), alpha.real, alpha.imag,
+                               a, b, ptr, b - a, 0)
+        if not ok:
+            errors.append(RuntimeError(L.oracle_last_error().decode()))
+            return
+        out[a - r0:b - r0] = buf
+
+    if threads <= 1 or m < 2:
+        work(r0, r1)
+    else:
+        bounds = np.linspace(r0, r1, threads + 1).astype(int)
+        ts = [threading.Thread(target=work, args=(int(bounds[i]), int(bounds[i + 1]))) for i in range(threads)]
+        for t in ts:
+            t.start()
+        for t in ts:
+            t.join()
+    if errors:
+        raise errors[0]
+    return out
+
+
+def classify(test_mesh, trial_mesh, same_mesh=None, rows=None):
+    tn, te, targs = _mesh_args(*test_mesh)
+    rn, re_, rargs = _mesh_args(*trial_mesh)
+    if same_mesh is None:
+        same_mesh = test_mesh is trial_mesh
+    r0, r1 = (0, len(te)) if rows is None else rows
+    out = np.zeros((r1 - r0, len(re_)), dtype=np.int32)
+    if not lib().oracle_classify(*targs, *rargs, int(same_mesh), r0, r1, _ptr(out, ctypes.c_int)):
+        raise RuntimeError(lib().oracle_last_error().decode())
+    return out
+
+
+def elem_integral(coords, x0, family, op, k, kind, degree=0):
+    """kind: 0 regular(degree), 1 nearly singular dispatch, 2 self, 3 planar near scheme."""
+    coords = np.ascontiguousarray(coords, dtype=np.float64)
+    x0 = np.ascontiguousarray(x0, dtype=np.float64)
+    out = np.zeros(2)
+    if not lib().oracle_elem_integral(_ptr(coords, ctypes.c_double), coords.shape[0], _ptr(x0, ctypes.c_double),
+                                      family, op, float(k), kind, degree, _ptr(out, ctypes.c_double)):
+        raise RuntimeError("element integral failed")
+    return complex(out[0], out[1])

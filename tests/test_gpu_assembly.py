@@ -1,0 +1,240 @@
+"""GPU assembly parity against the FP64 oracle, through the C ABI.
+
+Tolerances (written here, checked on every entry of the matrix):
+  * FP64 regular mode: max |A_gpu - A_oracle| / max |A_oracle| <= 1e-12
+  * FP32 regular mode (the default): normwise entry error <= 1e-5, and for
+    the SLP every entry within 1e-5 of its own magnitude
+Singular and nearly singular entries are FP64 in both modes.
+"""
+import ctypes
+
+import numpy as np
+import pytest
+
+import nihu_gb300 as g
+from nihu_gb300 import meshes
+
+pytestmark = pytest.mark.gpu
+
+
+def rel_norm(a, b):
+    return np.abs(a - b).max() / np.abs(b).max()
+
+
+def rel_entry(a, b):
+    return (np.abs(a - b) / np.abs(b)).max()
+
+
+def mixed_mesh():
+    nodes, elems = meshes.cylinder(12, 4, 1, radius=1.0, length=2.0)
+    rows = []
+    for e, row in enumerate(elems):
+        if e % 3 == 0:
+            a, b, c, d = row[1:5]
+            rows.append([g.TRIA_1, a, b, c, -1])
+            rows.append([g.TRIA_1, a, c, d, -1])
+        else:
+            rows.append(list(row))
+    return nodes, np.array(rows, dtype=np.int32)
+
+
+MESHES = {
+    "ico2": lambda: meshes.icosphere(2),
+    "ico3": lambda: meshes.icosphere(3),
+    "cyl": lambda: meshes.cylinder(16, 8, 2, radius=1.0, length=3.0),
+    "mixed": mixed_mesh,
+}
+_cache = {}
+
+
+def get_mesh(name):
+    if name not in _cache:
+        _cache[name] = MESHES[name]()
+    return _cache[name]
+
+
+_oracle_cache = {}
+
+
+def oracle_matrix(oracle, name, family, op, k):
+    key = (name, family, op, k)
+    if key not in _oracle_cache:
+        m = get_mesh(name)
+        _oracle_cache[key] = oracle.assemble(m, m, family, op, k, threads=8)
+    return _oracle_cache[key]
+
+
+def gpu_assemble(ctx, mesh, family, ops, k, precision, dtype, test_mesh=None, alpha=1.0, accumulate_into=None):
+    L = g.lib()
+    trial = g.api.DeviceMesh(ctx, *mesh)
+    test = trial if test_mesh is None else g.api.DeviceMesh(ctx, *test_mesh)
+    m, n = test.n, trial.n
+    cdt = np.complex64 if dtype == g.C64 else np.complex128
+    outs = {}
+    for op in (g.SLP, g.DLP):
+        if ops & op:
+            outs[op] = (np.array(accumulate_into[op], dtype=cdt, order="F") if accumulate_into
+                        else np.zeros((m, n), dtype=cdt, order="F"))
+    alpha = complex(alpha)
+    ctx.check(L.nihu_gb_assemble(ctx.handle, test.handle, trial.handle, family, ops, k, alpha.real, alpha.imag,
+                                 precision, dtype, outs[g.SLP].ctypes.data if g.SLP in outs else None,
+                                 outs[g.DLP].ctypes.data if g.DLP in outs else None, m,
+                                 1 if accumulate_into else 0, g.HOST))
+    test.close()
+    if test_mesh is not None:
+        trial.close()
+    return outs
+
+
+CASES = [("ico2", g.HELMHOLTZ_3D, 1.0), ("ico2", g.LAPLACE_3D, 0.0), ("ico3", g.HELMHOLTZ_3D, 5.0),
+         ("cyl", g.HELMHOLTZ_3D, 2.0), ("cyl", g.LAPLACE_3D, 0.0), ("mixed", g.HELMHOLTZ_3D, 1.5)]
+
+
+@pytest.mark.parametrize("name,family,k", CASES)
+def test_fp64_mode_matches_oracle(gpu_ctx, oracle, name, family, k):
+    mesh = get_mesh(name)
+    out = gpu_assemble(gpu_ctx, mesh, family, g.SLP | g.DLP, k, g.REGULAR_FP64, g.C128)
+    for op in (g.SLP, g.DLP):
+        ref = oracle_matrix(oracle, name, family, op, k)
+        assert np.all(np.isfinite(out[op]))
+        assert rel_norm(out[op], ref) < 1e-12, (op, rel_norm(out[op], ref))
+        if op == g.SLP:
+            assert rel_entry(out[op], ref) < 1e-11
+
+
+@pytest.mark.parametrize("name,family,k", CASES)
+def test_fp32_mode_matches_oracle(gpu_ctx, oracle, name, family, k):
+    mesh = get_mesh(name)
+    out = gpu_assemble(gpu_ctx, mesh, family, g.SLP | g.DLP, k, g.REGULAR_FP32, g.C64)
+    for op in (g.SLP, g.DLP):
+        ref = oracle_matrix(oracle, name, family, op, k)
+        assert rel_norm(out[op], ref) < 1e-5, (op, rel_norm(out[op], ref))
+        if op == g.SLP:
+            assert rel_entry(out[op], ref) < 1e-5
+
+
+@pytest.mark.parametrize("ops", [g.SLP, g.DLP])
+def test_single_operator_and_complex128_output(gpu_ctx, oracle, ops):
+    out = gpu_assemble(gpu_ctx, get_mesh("ico2"), g.HELMHOLTZ_3D, ops, 1.0, g.REGULAR_FP32, g.C128)
+    ref = oracle_matrix(oracle, "ico2", g.HELMHOLTZ_3D, ops, 1.0)
+    assert list(out) == [ops]
+    assert rel_norm(out[ops], ref) < 1e-5
+
+
+def test_accumulate_and_scale(gpu_ctx, oracle):
+    """NiHu's '<<' adds alpha * Op into the existing matrix (nihu/core/weighted_residual.hpp:197-206)."""
+    mesh = get_mesh("ico2")
+    rng = np.random.default_rng(7)
+    n = len(mesh[1])
+    base = {op: rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n)) for op in (g.SLP, g.DLP)}
+    alpha = -0.5 + 0.25j
+    out = gpu_assemble(gpu_ctx, mesh, g.HELMHOLTZ_3D, 3, 1.0, g.REGULAR_FP64, g.C128, alpha=alpha,
+                       accumulate_into=base)
+    for op in (g.SLP, g.DLP):
+        ref = base[op] + alpha * oracle_matrix(oracle, "ico2", g.HELMHOLTZ_3D, op, 1.0)
+        assert rel_norm(out[op], ref) < 1e-13
+
+
+def test_field_points_different_mesh(gpu_ctx, oracle):
+    """Test mesh != trial mesh: no self terms, nearly singular check still applies
+    (nihu/core/integral_transform.hpp:159-161)."""
+    trial = get_mesh("ico2")
+    nodes, elems = meshes.icosphere(2, radius=1.08)
+    test = (nodes, elems)
+    out = gpu_assemble(gpu_ctx, trial, g.HELMHOLTZ_3D, 3, 2.0, g.REGULAR_FP64, g.C128, test_mesh=test)
+    codes = oracle.classify(test, trial, same_mesh=False)
+    assert (codes == -2).sum() > 0 and (codes == -1).sum() == 0
+    for op in (g.SLP, g.DLP):
+        ref = oracle.assemble(test, trial, g.HELMHOLTZ_3D, op, 2.0, same_mesh=False, threads=8)
+        assert rel_norm(out[op], ref) < 1e-12
+
+
+def test_panel_pipeline_small_budget(oracle):
+    """A small HBM budget forces many column panels with overlapped copies."""
+    mesh = get_mesh("ico3")
+    ctx = g.Context(0, hbm_budget_bytes=48 << 20)
+    try:
+        out = gpu_assemble(ctx, mesh, g.HELMHOLTZ_3D, 3, 5.0, g.REGULAR_FP32, g.C64)
+    finally:
+        ctx.close()
+    for op in (g.SLP, g.DLP):
+        assert rel_norm(out[op], oracle_matrix(oracle, "ico3", g.HELMHOLTZ_3D, op, 5.0)) < 1e-5
+
+
+def test_device_output(gpu_ctx, oracle):
+    L = g.lib()
+    mesh = get_mesh("ico2")
+    dm = g.api.DeviceMesh(gpu_ctx, *mesh)
+    n = dm.n
+    bytes_ = n * n * 16
+    dptr = ctypes.c_void_p()
+    gpu_ctx.check(L.nihu_gb_device_alloc(gpu_ctx.handle, bytes_, ctypes.byref(dptr)))
+    try:
+        gpu_ctx.check(L.nihu_gb_assemble(gpu_ctx.handle, dm.handle, dm.handle, g.HELMHOLTZ_3D, g.SLP, 1.0, 1.0, 0.0,
+                                         g.REGULAR_FP64, g.C128, dptr, None, n, 0, g.DEVICE))
+        host = np.zeros((n, n), np.complex128, order="F")
+        gpu_ctx.check(L.nihu_gb_memcpy(gpu_ctx.handle, host.ctypes.data, g.HOST, dptr, g.DEVICE, bytes_))
+    finally:
+        L.nihu_gb_device_free(gpu_ctx.handle, dptr)
+        dm.close()
+    assert rel_norm(host, oracle_matrix(oracle, "ico2", g.HELMHOLTZ_3D, g.SLP, 1.0)) < 1e-12
+
+
+@pytest.mark.parametrize("name", ["ico3", "cyl", "mixed"])
+def test_pair_statistics_match_oracle(gpu_ctx, oracle, name):
+    mesh = get_mesh(name)
+    m = g.create_mesh(*mesh)
+    stats = g.pair_statistics(m, m, ctx=gpu_ctx)
+    codes = oracle.classify(mesh, mesh)
+    assert stats[0] == (codes == -1).sum()
+    assert stats[1] == (codes == -2).sum()
+    assert stats.sum() == codes.size
+
+
+def test_nihu_shaped_api(gpu_ctx, oracle):
+    """Ls << dirac(sp) * Lop[sp]; Ms << dirac(sp) * Mop[sp]; Ms << dirac(sp) * (-.5*I)[sp]
+    (nihu/test/matlab/acoustic_bem.mex.cpp:30-50)."""
+    nodes, elems = get_mesh("ico2")
+    mesh = g.create_mesh(nodes, elems)
+    sp = g.constant_view(mesh)
+    n = sp.get_num_dofs()
+    k = 1.0
+    I = g.identity_integral_operator()
+    Lop = g.create_integral_operator(g.helmholtz_3d_SLP_kernel(k))
+    Mop = g.create_integral_operator(g.helmholtz_3d_DLP_kernel(k))
+    Ls = np.zeros((n, n), np.complex128, order="F")
+    Ms = np.zeros((n, n), np.complex128, order="F")
+    Ls << g.dirac(sp) * Lop[sp]
+    Ms << g.dirac(sp) * Mop[sp]
+    Ms << g.dirac(sp) * (-.5 * I)[sp]
+    refL = oracle_matrix(oracle, "ico2", g.HELMHOLTZ_3D, g.SLP, k)
+    refM = oracle_matrix(oracle, "ico2", g.HELMHOLTZ_3D, g.DLP, k) - 0.5 * np.eye(n)
+    assert rel_norm(Ls, refL) < 1e-5
+    assert rel_norm(Ms, refM) < 1e-5
+    # C-ordered result and a scaled operator
+    Lc = np.zeros((n, n), np.complex128)
+    Lc << g.dirac(sp) * (2.0 * Lop)[sp]
+    assert rel_norm(Lc, 2 * refL) < 1e-5
+
+
+def test_invalid_arguments_raise(gpu_ctx):
+    nodes, elems = get_mesh("ico2")
+    bad = elems.copy()
+    bad[3, 0] = 12345
+    with pytest.raises(ValueError):
+        g.api.DeviceMesh(gpu_ctx, nodes, bad)
+    bad = elems.copy()
+    bad[5, 2] = len(nodes) + 3
+    with pytest.raises(IndexError):
+        g.api.DeviceMesh(gpu_ctx, nodes, bad)
+    dm = g.api.DeviceMesh(gpu_ctx, nodes, elems)
+    n = dm.n
+    out = np.zeros((n, n), np.complex64, order="F")
+    L = g.lib()
+    with pytest.raises(ValueError):  # ld < rows
+        gpu_ctx.check(L.nihu_gb_assemble(gpu_ctx.handle, dm.handle, dm.handle, 0, 1, 1.0, 1.0, 0.0, 0, 0,
+                                         out.ctypes.data, None, n - 1, 0, g.HOST))
+    with pytest.raises(ValueError):  # DLP requested without a buffer
+        gpu_ctx.check(L.nihu_gb_assemble(gpu_ctx.handle, dm.handle, dm.handle, 0, 3, 1.0, 1.0, 0.0, 0, 0,
+                                         out.ctypes.data, None, n, 0, g.HOST))
+    dm.close()
