@@ -1,0 +1,427 @@
+#!/usr/bin/env python3
+"""Headline benchmark of the dense collocation BEM hot path on one GB300.
+
+Workload (the large single instance): unit icosphere subdivided 5 times
+(20480 flat constant triangles), Helmholtz 3D, k = 5; one step assembles both
+the SLP and the DLP matrix (2 x 20480^2 complex64 entries, regular quadrature
+in FP32, singular and nearly singular entries in FP64) into device memory.
+Metric: BEM entries per second (SLP and DLP entries counted separately).
+
+Also reported, in the same JSON line:
+  e2e          the same metric through the C ABI with host buffers: mesh arrays
+               uploaded and both matrices copied to pinned host memory per step
+  roofline     achieved HBM bandwidth of the dominant kernel (assemble_regular)
+  solve        GMRES(50) to 1e-6 on (DLP - I/2) p = SLP q (pulsating sphere),
+               FP32 matvec / FP64 Arnoldi, with matvec bandwidth
+  cpu_baseline the FP64 CPU oracle on the host cores on a sample of rows
+
+--impl reference times the CPU restatement of NiHu's assembly (the oracle) on
+all host cores instead, on a bounded row sample per step.
+Multi-GPU: replicas only (every rank assembles the same instance on its GPU).
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+SUBDIV = 5
+K_WAVE = 5.0
+METRIC = "BEM entries/s"
+UNIT = "entries/s"
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=10)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    p.add_argument("--cpu-seconds", type=float, default=15.0, help="CPU baseline sample budget")
+    p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--no-solve", action="store_true")
+    p.add_argument("--no-cpu", action="store_true")
+    return p.parse_args()
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def workload_config(n):
+    return {
+        "workload": "icosphere s=5 (%d flat constant triangles), Helmholtz 3D SLP+DLP collocation, k=5" % n,
+        "n_elements": n,
+        "entries_per_step": 2 * n * n,
+        "storage": "complex64",
+        "regular_quadrature": "fp32, distance-adaptive 1/3/6-point Dunavant",
+        "singular_nearly_singular": "fp64",
+        "l2": "256 MB written between timed steps (L2 flushed); outputs 6.7 GB >> 129 MB L2",
+        "parallelism": "replicas only (1 GPU per instance)",
+    }
+
+
+# ------------------------------------------------------------ CPU baseline
+
+def cpu_sample(mesh, seconds, threads):
+    """Time the FP64 oracle on a sample of full rows (SLP and DLP) on `threads`
+    host threads; returns (entries/s, rows, elapsed)."""
+    from oracle import oracle
+    n = len(mesh[1])
+    t0 = time.perf_counter()
+    oracle.assemble(mesh, mesh, oracle.HELMHOLTZ, oracle.SLP, K_WAVE, rows=(0, 1))
+    oracle.assemble(mesh, mesh, oracle.HELMHOLTZ, oracle.DLP, K_WAVE, rows=(0, 1))
+    per_row = time.perf_counter() - t0
+    rows = int(max(threads, min(8192, seconds * threads / max(per_row, 1e-6))))
+    rows = max(threads, (rows // threads) * threads)
+    t0 = time.perf_counter()
+    # contiguous blocks spread over the sphere: row ranges of equal size
+    blocks = np.linspace(0, n, threads + 1).astype(int)
+    per = rows // threads
+    errs = []
+
+    def work(b):
+        try:
+            a = int(blocks[b])
+            for op in (oracle.SLP, oracle.DLP):
+                oracle.assemble(mesh, mesh, oracle.HELMHOLTZ, op, K_WAVE, rows=(a, min(n, a + per)))
+        except Exception as e:  # pragma: no cover
+            errs.append(e)
+
+    ts = [threading.Thread(target=work, args=(b,)) for b in range(threads)]
+    for t in ts:
+        t.start()
+    for t in ts:
+        t.join()
+    el = time.perf_counter() - t0
+    if errs:
+        raise errs[0]
+    return 2.0 * per * threads * n / el, per * threads, el
+
+
+def run_reference(args):
+    ws, rank, local = dist_env()
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo", init_method="env://")
+        dist.barrier()
+        if rank != 0:
+            dist.destroy_process_group()
+            return
+    from oracle import oracle
+    from nihu_gb300 import meshes
+    oracle.build()
+    mesh = meshes.icosphere(SUBDIV)
+    n = len(mesh[1])
+    threads = os.cpu_count() or 1
+    per_step = max(2.0, min(12.0, 150.0 / max(1, args.steps + args.warmup)))
+    for _ in range(args.warmup):
+        cpu_sample(mesh, 0.5, threads)
+    vals, rows_tot, el_tot = [], 0, 0.0
+    for _ in range(args.steps):
+        v, rows, el = cpu_sample(mesh, per_step, threads)
+        vals.append(v)
+        rows_tot += rows
+        el_tot += el
+    value = float(np.mean(vals))
+    ms_per_step = 1e3 * 2.0 * n * n / value
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "fp64", "data": "synthetic (icosphere mesh generated in-process)", "impl": "reference",
+        "config": workload_config(n),
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": "%d full rows x %d columns x (SLP, DLP) per step, FP64 restatement of NiHu's "
+                                   "collocational assembly (the reference needs Eigen/Boost, absent)" % (rows_tot // max(1, args.steps), n)},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+# ------------------------------------------------------------ clocks
+
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax = float(parts[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ------------------------------------------------------------ our arm
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def recorded_traffic():
+    """Per-launch DRAM bytes of assemble_regular from the committed ncu summary, if any."""
+    try:
+        with open(os.path.join(ROOT, "profiles", "roofline_traffic.json")) as f:
+            d = json.load(f)
+        return d
+    except (OSError, ValueError):
+        return None
+
+
+def run_ours(args):
+    import torch
+
+    import nihu_gb300 as g
+    from nihu_gb300 import meshes
+    from nihu_gb300 import _capi as C
+
+    ws, rank, local = dist_env()
+    dist = None
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo", init_method="env://")
+    torch.cuda.set_device(local)
+    L = g.lib()
+    mesh = meshes.icosphere(SUBDIV)
+    nodes, elems = mesh
+    n = len(elems)
+    ctx = g.Context(local)
+    stream = torch.cuda.ExternalStream(ctx.stream, device=torch.device("cuda", local))
+    dm = g.api.DeviceMesh(ctx, nodes, elems)
+    mat_bytes = n * n * 8
+    ps, pd = ctypes.c_void_p(), ctypes.c_void_p()
+    ctx.check(L.nihu_gb_device_alloc(ctx.handle, mat_bytes, ctypes.byref(ps)))
+    ctx.check(L.nihu_gb_device_alloc(ctx.handle, mat_bytes, ctypes.byref(pd)))
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+
+    def step():
+        ctx.check(L.nihu_gb_assemble(ctx.handle, dm.handle, dm.handle, C.HELMHOLTZ_3D, C.SLP | C.DLP, K_WAVE, 1.0, 0.0,
+                                     C.REGULAR_FP32, C.C64, ps, pd, n, 0, C.DEVICE))
+
+    for _ in range(args.warmup):
+        step()
+    counts = (ctypes.c_int64 * 11)()
+    ctx.check(L.nihu_gb_pair_statistics(ctx.handle, dm.handle, dm.handle, counts))
+    counts = np.array(list(counts))
+    n_regular = int(counts[2:].sum())
+
+    ctx.set_profiling(True)
+    ctx.profile_reset()
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    clocks = ClockSampler(local)
+    clocks.start()
+    launches0 = ctx.launch_count
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    torch.cuda.synchronize()
+    t_wall0 = time.perf_counter()
+    for s in range(args.steps):
+        flush.fill_(s & 0xFF)  # evict the previous step's lines from L2 (not timed)
+        torch.cuda.synchronize()
+        ev[s][0].record(stream)
+        step()
+        ev[s][1].record(stream)
+    torch.cuda.synchronize()
+    t_wall = time.perf_counter() - t_wall0
+    launches = ctx.launch_count - launches0
+    clk = clocks.stop()
+    prof = ctx.profile()
+    ctx.set_profiling(False)
+    step_ms = [a.elapsed_time(b) for a, b in ev]
+    ms_per_step = float(np.mean(step_ms))
+    if dist:
+        t = torch.tensor([ms_per_step], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms_per_step = float(t.item())
+    entries = 2.0 * n * n
+    value = entries * ws / (ms_per_step / 1e3)
+
+    reg_ms, reg_n = prof.get("assemble_regular", (0.0, 0))
+    sing_ms, sing_n = prof.get("assemble_singular", (0.0, 0))
+    reg_avg = reg_ms / max(reg_n, 1)
+    alg_bytes = 16.0 * n_regular  # one complex64 SLP + one complex64 DLP entry written per regular pair
+    peak, peak_kind = measured_peaks()
+    achieved = alg_bytes / (reg_avg / 1e3) / 1e9
+    tr = recorded_traffic()
+    traffic = None
+    if tr and tr.get("kernel") == "k_regular" and tr.get("n_elements") == n:
+        traffic = tr.get("dram_bytes_per_launch")
+    roofline = {"kernel": "k_regular (assemble_regular.cu)", "bound": "hbm", "achieved": achieved, "peak": peak,
+                "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,
+                "peak_source": "%s (MEASURED_PEAKS.json hbm_gbs)" % peak_kind if peak_kind == "measured" else "fallback 6.8 TB/s",
+                "algorithmic_bytes_per_launch": alg_bytes, "avg_launch_ms": reg_avg,
+                "regular_pairs": n_regular, "near_pairs": int(counts[1]), "self_pairs": int(counts[0]),
+                "level_histogram_slp_dlp": counts[2:].reshape(3, 3).tolist()}
+    phases = {k: {"ms_per_step": v[0] / args.steps, "launches": v[1]} for k, v in prof.items()}
+
+    out = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "fp32 regular quadrature, fp64 singular/nearly singular; complex64 storage",
+        "data": "synthetic (icosphere mesh generated in-process)",
+        "config": workload_config(n), "gpu_launches": int(launches), "clocks": clk, "roofline": roofline,
+        "phases": phases, "wall_s_timed_region": t_wall,
+    }
+
+    # ---- e2e through the C ABI with host buffers
+    if not args.no_e2e:
+        hs, hd = ctypes.c_void_p(), ctypes.c_void_p()
+        ctx.check(L.nihu_gb_host_alloc(ctx.handle, mat_bytes, ctypes.byref(hs)))
+        ctx.check(L.nihu_gb_host_alloc(ctx.handle, mat_bytes, ctypes.byref(hd)))
+        e2e_steps = max(1, min(args.steps, 5))
+
+        def e2e_step():
+            m = ctypes.c_void_p()
+            ctx.check(L.nihu_gb_mesh_create(ctx.handle, nodes.ctypes.data, len(nodes), elems.ctypes.data, n,
+                                            elems.shape[1], ctypes.byref(m)))
+            ctx.check(L.nihu_gb_assemble(ctx.handle, m, m, C.HELMHOLTZ_3D, C.SLP | C.DLP, K_WAVE, 1.0, 0.0,
+                                         C.REGULAR_FP32, C.C64, hs, hd, n, 0, C.HOST))
+            L.nihu_gb_mesh_destroy(m)
+
+        e2e_step()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(e2e_steps):
+            e2e_step()
+        torch.cuda.synchronize()
+        e2e_ms = (time.perf_counter() - t0) * 1e3 / e2e_steps
+        # spot check of the host copy against the device matrices (first column)
+        col = np.ctypeslib.as_array(ctypes.cast(hs, ctypes.POINTER(ctypes.c_float)), shape=(2 * n,)).copy()
+        dcol = np.zeros(2 * n, np.float32)
+        ctx.check(L.nihu_gb_memcpy(ctx.handle, dcol.ctypes.data, C.HOST, ps, C.DEVICE, 8 * n))
+        out["e2e"] = {"value": entries * ws / (e2e_ms / 1e3), "unit": UNIT,
+                      "h2d_bytes_per_step": int(nodes.nbytes + elems.nbytes), "d2h_bytes_per_step": int(2 * mat_bytes),
+                      "ms_per_step": e2e_ms, "steps": e2e_steps,
+                      "path": "nihu_gb_mesh_create + nihu_gb_assemble(where=HOST, pinned) + nihu_gb_mesh_destroy",
+                      "host_matches_device_first_column": bool(np.array_equal(col, dcol))}
+        L.nihu_gb_host_free(hs)
+        L.nihu_gb_host_free(hd)
+
+    # ---- GMRES solve on the assembled matrices
+    if not args.no_solve:
+        ctx.check(L.nihu_gb_add_identity(ctx.handle, dm.handle, -0.5, 0.0, C.C64, pd, n, C.DEVICE))
+        q = np.ones(n, np.complex128)
+        dq, drhs, dp = ctypes.c_void_p(), ctypes.c_void_p(), ctypes.c_void_p()
+        for p_ in (dq, drhs, dp):
+            ctx.check(L.nihu_gb_device_alloc(ctx.handle, 16 * n, ctypes.byref(p_)))
+        ctx.check(L.nihu_gb_memcpy(ctx.handle, dq, C.DEVICE, q.ctypes.data, C.HOST, 16 * n))
+        ctx.profile_reset()
+        ctx.set_profiling(True)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        ctx.check(L.nihu_gb_matvec(ctx.handle, C.C64, ps, n, n, n, dq, drhs, 1.0, 0.0, 0.0, 0.0, C.DEVICE))
+        ctx.check(L.nihu_gb_memcpy(ctx.handle, dp, C.DEVICE, np.zeros(n, np.complex128).ctypes.data, C.HOST, 16 * n))
+        it, res = ctypes.c_int(0), ctypes.c_double(0.0)
+        st = L.nihu_gb_gmres(ctx.handle, C.C64, pd, n, n, drhs, dp, 50, 1000, 1e-6, ctypes.byref(it),
+                             ctypes.byref(res), C.DEVICE)
+        torch.cuda.synchronize()
+        solve_ms = (time.perf_counter() - t0) * 1e3
+        prof = ctx.profile()
+        ctx.set_profiling(False)
+        p = np.zeros(n, np.complex128)
+        ctx.check(L.nihu_gb_memcpy(ctx.handle, p.ctypes.data, C.HOST, dp, C.DEVICE, 16 * n))
+        pa = -1.0 / (1 + 1j * K_WAVE)
+        gm_ms, gm_n = prof.get("gemv_c64", (0.0, 0))
+        gm_avg = gm_ms / max(gm_n, 1)
+        out["solve"] = {
+            "solver": "GMRES(50), FP32 matvec (complex64 matrix), FP64 CGS2 Arnoldi, tol 1e-6",
+            "status": int(st), "iterations": it.value, "rel_residual": res.value, "ms": solve_ms,
+            "matvecs": gm_n, "matvec_avg_ms": gm_avg,
+            "matvec_gbs": 8.0 * n * n / (gm_avg / 1e3) / 1e9 if gm_avg else None,
+            "matvec_frac_of_hbm": (8.0 * n * n / (gm_avg / 1e3) / 1e9) / peak if gm_avg else None,
+            "pressure_error_vs_analytic": float(np.abs(p - pa).max() / abs(pa)),
+        }
+        for p_ in (dq, drhs, dp):
+            L.nihu_gb_device_free(ctx.handle, p_)
+
+    L.nihu_gb_device_free(ctx.handle, ps)
+    L.nihu_gb_device_free(ctx.handle, pd)
+    dm.close()
+    ctx.close()
+
+    # ---- CPU baseline (rank 0, N = 1 only)
+    if not args.no_cpu and rank == 0 and ws == 1:
+        threads = os.cpu_count() or 1
+        v, rows, el = cpu_sample(mesh, args.cpu_seconds, threads)
+        out["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
+                               "sample": "%d full rows x %d columns x (SLP, DLP), FP64 oracle (restatement of NiHu's "
+                                         "collocational assembly), %.1f s" % (rows, n, el)}
+    if dist:
+        dist.barrier()
+        dist.destroy_process_group()
+    if rank == 0:
+        print(json.dumps(out), flush=True)
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

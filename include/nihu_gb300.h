@@ -92,6 +92,17 @@ size_t nihu_gb_ctx_device_bytes(const nihu_gb_ctx *ctx);
 /* number of kernels this context has launched since creation */
 int64_t nihu_gb_ctx_launch_count(const nihu_gb_ctx *ctx);
 
+/* Per-phase device timing: with profiling enabled, every kernel phase a call
+ * launches is bracketed by CUDA events on the context's stream and its device
+ * time is accumulated per phase name ("assemble_regular",
+ * "assemble_singular", "near_list", "gemv", ...).  Off by default. */
+nihu_gb_status nihu_gb_ctx_set_profiling(nihu_gb_ctx *ctx, int enable);
+/* Phase `index` (0-based): name, total device milliseconds and launches.
+ * Returns NIHU_GB_ERR_OUT_OF_RANGE past the last phase. */
+nihu_gb_status nihu_gb_ctx_profile(const nihu_gb_ctx *ctx, int index, const char **name, double *total_ms,
+                                   int64_t *launches);
+void nihu_gb_ctx_profile_reset(nihu_gb_ctx *ctx);
+
 /* pinned host memory helpers for fast host<->device transfers */
 nihu_gb_status nihu_gb_host_alloc(nihu_gb_ctx *ctx, size_t bytes, void **out);
 void nihu_gb_host_free(void *ptr);

@@ -34,6 +34,9 @@ SIGNATURES = {
     "nihu_gb_ctx_stream": (_vp, [_vp]),
     "nihu_gb_ctx_device_bytes": (_sz, [_vp]),
     "nihu_gb_ctx_launch_count": (_i64, [_vp]),
+    "nihu_gb_ctx_set_profiling": (_i, [_vp, _i]),
+    "nihu_gb_ctx_profile": (_i, [_vp, _i, ctypes.POINTER(ctypes.c_char_p), _dp, ctypes.POINTER(ctypes.c_int64)]),
+    "nihu_gb_ctx_profile_reset": (None, [_vp]),
     "nihu_gb_host_alloc": (_i, [_vp, _sz, ctypes.POINTER(_vp)]),
     "nihu_gb_host_free": (None, [_vp]),
     "nihu_gb_device_alloc": (_i, [_vp, _sz, ctypes.POINTER(_vp)]),

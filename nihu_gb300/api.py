@@ -65,6 +65,21 @@ class Context:
     def check(self, status):
         C.check(self.handle, status)
 
+    def set_profiling(self, enable: bool = True):
+        self.check(C.lib().nihu_gb_ctx_set_profiling(self.handle, int(enable)))
+
+    def profile(self) -> dict:
+        """{phase: (total device ms, launches)} accumulated while profiling."""
+        out, i = {}, 0
+        name, ms, n = ctypes.c_char_p(), ctypes.c_double(), ctypes.c_int64()
+        while C.lib().nihu_gb_ctx_profile(self.handle, i, ctypes.byref(name), ctypes.byref(ms), ctypes.byref(n)) == 0:
+            out[name.value.decode()] = (ms.value, n.value)
+            i += 1
+        return out
+
+    def profile_reset(self):
+        C.lib().nihu_gb_ctx_profile_reset(self.handle)
+
 
 def default_context() -> Context:
     global _default_ctx

@@ -33,6 +33,12 @@ struct nihu_gb_ctx {
     std::map<std::pair<uint64_t, uint64_t>, NearList> near;
     // reusable device scratch buffers
     std::map<std::string, std::pair<void *, size_t>> scratch;
+    // per-phase device timing
+    bool profiling = false;
+    std::vector<std::string> phase_names;
+    std::map<std::string, std::pair<double, int64_t>> phases;
+    std::vector<std::pair<std::string, std::pair<cudaEvent_t, cudaEvent_t>>> pending;
+    std::vector<cudaEvent_t> event_pool;
 };
 
 struct nihu_gb_mesh {
@@ -115,10 +121,67 @@ void free_near(nihu_gb_ctx *ctx, NearList &nl)
     nl = NearList();
 }
 
+cudaEvent_t pool_event(nihu_gb_ctx *ctx)
+{
+    if (!ctx->event_pool.empty()) {
+        cudaEvent_t e = ctx->event_pool.back();
+        ctx->event_pool.pop_back();
+        return e;
+    }
+    cudaEvent_t e;
+    cudaEventCreate(&e);
+    return e;
+}
+
+// bracket a phase with events on the context stream (no-op unless profiling)
+struct Phase {
+    nihu_gb_ctx *ctx;
+    const char *name;
+    cudaEvent_t a = nullptr;
+    Phase(nihu_gb_ctx *c, const char *n) : ctx(c), name(n)
+    {
+        if (ctx->profiling) {
+            a = pool_event(ctx);
+            cudaEventRecord(a, ctx->stream);
+        }
+    }
+    ~Phase()
+    {
+        if (a) {
+            cudaEvent_t b = pool_event(ctx);
+            cudaEventRecord(b, ctx->stream);
+            ctx->pending.push_back({name, {a, b}});
+        }
+    }
+};
+
+// fold completed phase events into the totals (after a stream sync)
+void collect_phases(nihu_gb_ctx *ctx)
+{
+    for (auto &p : ctx->pending) {
+        float ms = 0.f;
+        if (cudaEventSynchronize(p.second.second) == cudaSuccess &&
+            cudaEventElapsedTime(&ms, p.second.first, p.second.second) == cudaSuccess) {
+            auto it = ctx->phases.find(p.first);
+            if (it == ctx->phases.end()) {
+                ctx->phase_names.push_back(p.first);
+                ctx->phases[p.first] = {ms, 1};
+            } else {
+                it->second.first += ms;
+                it->second.second += 1;
+            }
+        }
+        ctx->event_pool.push_back(p.second.first);
+        ctx->event_pool.push_back(p.second.second);
+    }
+    ctx->pending.clear();
+}
+
 nihu_gb_status sync(nihu_gb_ctx *ctx)
 {
     cudaError_t e = cudaStreamSynchronize(ctx->stream);
     if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaStreamSynchronize");
+    if (!ctx->pending.empty()) collect_phases(ctx);
     return NIHU_GB_OK;
 }
 
@@ -137,8 +200,12 @@ nihu_gb_status get_near(nihu_gb_ctx *ctx, const nihu_gb_mesh *test, const nihu_g
     st = dmalloc(ctx, sizeof(int64_t) * (trial->n + 1), &colptr);
     if (st) { dfree(ctx, counts); return st; }
     nl.col_ptr = (int64_t *)colptr;
-    cudaError_t e = launch_near_count(test->dm, trial->dm, same, (int *)counts, ctx->stream);
-    if (e == cudaSuccess) e = launch_scan((int *)counts, (int)trial->n, nl.col_ptr, ctx->stream);
+    cudaError_t e;
+    {
+        Phase ph(ctx, "near_list");
+        e = launch_near_count(test->dm, trial->dm, same, (int *)counts, ctx->stream);
+        if (e == cudaSuccess) e = launch_scan((int *)counts, (int)trial->n, nl.col_ptr, ctx->stream);
+    }
     ctx->launches += 2;
     int64_t nnz = 0;
     if (e == cudaSuccess) e = cudaMemcpyAsync(&nnz, nl.col_ptr + trial->n, sizeof(int64_t), cudaMemcpyDeviceToHost, ctx->stream);
@@ -150,7 +217,10 @@ nihu_gb_status get_near(nihu_gb_ctx *ctx, const nihu_gb_mesh *test, const nihu_g
     st = dmalloc(ctx, sizeof(int) * (nnz > 0 ? nnz : 1), &rows);
     if (st) { free_near(ctx, nl); return st; }
     nl.rows = (int *)rows;
-    e = launch_near_fill(test->dm, trial->dm, same, nl.col_ptr, nl.rows, ctx->stream);
+    {
+        Phase ph(ctx, "near_list");
+        e = launch_near_fill(test->dm, trial->dm, same, nl.col_ptr, nl.rows, ctx->stream);
+    }
     ctx->launches += 1;
     if (e != cudaSuccess) { free_near(ctx, nl); return cuda_fail(ctx, e, "nearly singular pair fill"); }
     ctx->near[key] = nl;
@@ -160,6 +230,14 @@ nihu_gb_status get_near(nihu_gb_ctx *ctx, const nihu_gb_mesh *test, const nihu_g
 
 size_t elem_bytes(int dtype) { return dtype == NIHU_GB_C64 ? 8 : 16; }
 
+cudaError_t timed_gemv(nihu_gb_ctx *ctx, int dtype, const void *A, int64_t m, int64_t n, int64_t lda, const double2 *x,
+                       double2 *y, double are, double aim, double bre, double bim, double2 *partial, int splits)
+{
+    Phase ph(ctx, dtype == 0 ? "gemv_c64" : "gemv_c128");
+    ctx->launches += 2;
+    return launch_gemv(dtype, A, m, n, lda, x, y, are, aim, bre, bim, partial, splits, ctx->stream);
+}
+
 bool valid_dtype(int d) { return d == NIHU_GB_C64 || d == NIHU_GB_C128; }
 bool valid_where(int w) { return w == NIHU_GB_HOST || w == NIHU_GB_DEVICE; }
 
@@ -167,9 +245,16 @@ bool valid_where(int w) { return w == NIHU_GB_HOST || w == NIHU_GB_DEVICE; }
 // column j starts at out + (j - j0) * ld
 nihu_gb_status assemble_panel(nihu_gb_ctx *ctx, RegularArgs a, NearList *nl)
 {
-    cudaError_t e = launch_assemble_regular(a, ctx->stream);
+    cudaError_t e;
+    {
+        Phase ph(ctx, "assemble_regular");
+        e = launch_assemble_regular(a, ctx->stream);
+    }
     if (e != cudaSuccess) return cuda_fail(ctx, e, "assemble_regular launch");
-    e = launch_assemble_singular(a, *nl, ctx->d_flag, ctx->stream);
+    {
+        Phase ph(ctx, "assemble_singular");
+        e = launch_assemble_singular(a, *nl, ctx->d_flag, ctx->stream);
+    }
     if (e != cudaSuccess) return cuda_fail(ctx, e, "assemble_singular launch");
     ctx->launches += 2;
     return NIHU_GB_OK;
@@ -179,7 +264,8 @@ nihu_gb_status check_flag(nihu_gb_ctx *ctx)
 {
     int flag = 0;
     CK(cudaMemcpyAsync(&flag, ctx->d_flag, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
-    CK(cudaStreamSynchronize(ctx->stream));
+    nihu_gb_status st = sync(ctx);
+    if (st) return st;
     if (flag) {
         CK(cudaMemsetAsync(ctx->d_flag, 0, sizeof(int), ctx->stream));
         return fail(ctx, NIHU_GB_ERR_RUNTIME, "Could not perform inverse mapping (nearly singular pair " +
@@ -234,12 +320,41 @@ void nihu_gb_ctx_destroy(nihu_gb_ctx *ctx)
     for (auto &kv : ctx->scratch) dfree(ctx, kv.second.first);
     dfree(ctx, ctx->d_flag);
     if (ctx->h_small) cudaFreeHost(ctx->h_small);
+    collect_phases(ctx);
+    for (cudaEvent_t e : ctx->event_pool) cudaEventDestroy(e);
     if (ctx->copy_stream) cudaStreamDestroy(ctx->copy_stream);
     if (ctx->own_stream && ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
 }
 
 const char *nihu_gb_last_error(const nihu_gb_ctx *ctx) { return ctx ? ctx->err.c_str() : "null context"; }
+
+nihu_gb_status nihu_gb_ctx_set_profiling(nihu_gb_ctx *ctx, int enable)
+{
+    if (!ctx) return NIHU_GB_ERR_INVALID_ARGUMENT;
+    ctx->profiling = enable != 0;
+    return NIHU_GB_OK;
+}
+
+nihu_gb_status nihu_gb_ctx_profile(const nihu_gb_ctx *ctx, int index, const char **name, double *total_ms,
+                                   int64_t *launches)
+{
+    if (!ctx) return NIHU_GB_ERR_INVALID_ARGUMENT;
+    if (index < 0 || index >= (int)ctx->phase_names.size()) return NIHU_GB_ERR_OUT_OF_RANGE;
+    const std::string &nm = ctx->phase_names[index];
+    auto it = ctx->phases.find(nm);
+    if (name) *name = nm.c_str();
+    if (total_ms) *total_ms = it->second.first;
+    if (launches) *launches = it->second.second;
+    return NIHU_GB_OK;
+}
+
+void nihu_gb_ctx_profile_reset(nihu_gb_ctx *ctx)
+{
+    if (!ctx) return;
+    ctx->phases.clear();
+    ctx->phase_names.clear();
+}
 void *nihu_gb_ctx_stream(const nihu_gb_ctx *ctx) { return ctx ? (void *)ctx->stream : nullptr; }
 size_t nihu_gb_ctx_device_bytes(const nihu_gb_ctx *ctx) { return ctx ? ctx->used : 0; }
 int64_t nihu_gb_ctx_launch_count(const nihu_gb_ctx *ctx) { return ctx ? ctx->launches : 0; }
@@ -586,9 +701,7 @@ nihu_gb_status nihu_gb_matvec(nihu_gb_ctx *ctx, int dtype_a, const void *A, int6
     int splits = gemv_splits(m, n, dtype_a);
     void *part;
     if ((st = scratch(ctx, "mv_part", 16 * (size_t)splits * m, &part))) return st;
-    CK(launch_gemv(dtype_a, dA, m, n, lda, dx, dy, alpha_re, alpha_im, beta_re, beta_im, (double2 *)part, splits,
-                   ctx->stream));
-    ctx->launches += 2;
+    CK(timed_gemv(ctx, dtype_a, dA, m, n, lda, dx, dy, alpha_re, alpha_im, beta_re, beta_im, (double2 *)part, splits));
     if (where == NIHU_GB_HOST) CK(cudaMemcpyAsync(y, dy, 16 * m, cudaMemcpyDeviceToHost, ctx->stream));
     return sync(ctx);
 }
@@ -651,9 +764,9 @@ nihu_gb_status gmres_device(nihu_gb_ctx *ctx, int dtype_a, const void *A, int64_
     };
 
     // r0 = b - A x ; reference normalises by the initial residual norm
-    CK(launch_gemv(dtype_a, A, n, n, lda, x, t, 1.0, 0.0, 0.0, 0.0, part, splits, ctx->stream));
+    CK(timed_gemv(ctx, dtype_a, A, n, n, lda, x, t, 1.0, 0.0, 0.0, 0.0, part, splits));
     CK(launch_sub(b, t, w, n, ctx->stream));
-    ctx->launches += 3;
+    ctx->launches += 1;
     double r0norm;
     if ((st = norm_of(w, &r0norm))) return st;
     int iters = 0;
@@ -677,8 +790,7 @@ nihu_gb_status gmres_device(nihu_gb_ctx *ctx, int dtype_a, const void *A, int64_
         for (int k = 0; k < m; ++k) {
             ++iters;
             // w = A v_k
-            CK(launch_gemv(dtype_a, A, n, n, lda, V + (size_t)k * n, w, 1.0, 0.0, 0.0, 0.0, part, splits, ctx->stream));
-            ctx->launches += 2;
+            CK(timed_gemv(ctx, dtype_a, A, n, n, lda, V + (size_t)k * n, w, 1.0, 0.0, 0.0, 0.0, part, splits));
             std::vector<C> h(k + 2, C(0));
             if ((st = project(k + 1, h))) return st;
             if ((st = project(k + 1, h))) return st;  // reorthogonalisation (CGS2)
@@ -724,9 +836,9 @@ nihu_gb_status gmres_device(nihu_gb_ctx *ctx, int dtype_a, const void *A, int64_
         if (rel < tol) converged = true;
         if (stop) break;
         // restart: w = b - A x
-        CK(launch_gemv(dtype_a, A, n, n, lda, x, t, 1.0, 0.0, 0.0, 0.0, part, splits, ctx->stream));
+        CK(timed_gemv(ctx, dtype_a, A, n, n, lda, x, t, 1.0, 0.0, 0.0, 0.0, part, splits));
         CK(launch_sub(b, t, w, n, ctx->stream));
-        ctx->launches += 3;
+        ctx->launches += 1;
         if ((st = norm_of(w, &beta))) return st;
         if (beta == 0.0) { converged = true; rel = 0.0; break; }
     }
@@ -847,9 +959,7 @@ nihu_gb_status nihu_gb_solve_cbie(nihu_gb_ctx *ctx, const nihu_gb_mesh *mesh, in
     int splits = gemv_splits(n, n, dtype);
     void *part;
     if ((st = scratch(ctx, "mv_part", 16 * (size_t)splits * n, &part))) return st;
-    CK(launch_gemv(dtype, G, n, n, n, (const double2 *)dq, (double2 *)drhs, 1.0, 0.0, 0.0, 0.0, (double2 *)part, splits,
-                   ctx->stream));
-    ctx->launches += 2;
+    CK(timed_gemv(ctx, dtype, G, n, n, n, (const double2 *)dq, (double2 *)drhs, 1.0, 0.0, 0.0, 0.0, (double2 *)part, splits));
     if (solver == 0) {
         CK(cudaMemsetAsync(dp, 0, 16 * n, ctx->stream));
         st = gmres_device(ctx, dtype, Hm, n, n, (const double2 *)drhs, (double2 *)dp, std::min<int64_t>(restart, n),

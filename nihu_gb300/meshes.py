@@ -59,7 +59,7 @@ def icosphere(subdivisions: int, radius: float = 1.0):
     return _pack(nodes, faces, TRIA_1)
 
 
-def cylinder(n_theta: int, n_z: int, n_ring: int, radius: float = 1.0, length: float = 4.0):
+def cylinder(n_theta: int, n_z: int, n_ring: int, radius: float = 1.0, length: float = 4.0, smooth: int = 200):
     """Closed cylinder of flat quads: an ``n_theta x n_z`` side grid plus two
     O-grid caps.  Each cap is an ``m x m`` square core (m = n_theta/4) blended
     into the rim circle through ``n_ring`` rings of ``n_theta`` quads.
@@ -142,6 +142,24 @@ def cylinder(n_theta: int, n_z: int, n_ring: int, radius: float = 1.0, length: f
             quads = [q[::-1] for q in quads]
         faces += quads
     nodes = np.array(nodes, dtype=np.float64)
+    faces = np.asarray(faces, dtype=np.int64)
+    # Laplacian smoothing of the cap interiors (rim and side nodes fixed):
+    # rounds the square core so that no cap quad is kite-shaped; the
+    # nearly singular quad scheme's Newton inverse mapping (the reference's,
+    # nihu/core/inverse_mapping.hpp) converges for all neighbour pairs only on
+    # such near-parallelogram quads.
+    n_side = (n_z + 1) * n_theta
+    nbrs = [set() for _ in range(len(nodes))]
+    for f in faces[n_theta * n_z:]:
+        for a in range(4):
+            nbrs[f[a]].add(int(f[(a + 1) % 4]))
+            nbrs[f[(a + 1) % 4]].add(int(f[a]))
+    free = np.array([v for v in range(n_side, len(nodes))], dtype=np.int64)
+    if len(free):
+        lists = [np.fromiter(nbrs[v], dtype=np.int64) for v in free]
+        for _ in range(smooth):
+            new = np.array([nodes[l, :2].mean(axis=0) for l in lists])
+            nodes[free, :2] = new
     return _pack(nodes, faces, QUAD_1)
 
 

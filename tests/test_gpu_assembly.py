@@ -26,10 +26,11 @@ def rel_entry(a, b):
 
 
 def mixed_mesh():
-    nodes, elems = meshes.cylinder(12, 4, 1, radius=1.0, length=2.0)
+    """Closed cylinder with every third side quad split into two triangles."""
+    nodes, elems = meshes.cylinder(16, 6, 2, radius=1.0, length=4.0)
     rows = []
     for e, row in enumerate(elems):
-        if e % 3 == 0:
+        if e < 16 * 6 and e % 3 == 0:
             a, b, c, d = row[1:5]
             rows.append([g.TRIA_1, a, b, c, -1])
             rows.append([g.TRIA_1, a, c, d, -1])
