@@ -1,10 +1,12 @@
 // FP64 singular (self) and nearly singular collocational entries.
 //
-// One warp evaluates one (test, trial) pair: the quadrature points of every
-// scheme are spread over the 32 lanes and the partial sums are reduced with
-// warp shuffles, so a pair costs a few points per lane instead of dozens of
-// sequential kernel evaluations.  SLP and DLP of a pair share the geometry,
-// the inverse mapping and the e^{-ikr} evaluations.
+// One thread evaluates one (test, trial) pair.  GB300's FP64 pipe is narrow,
+// so the per-pair set-up (plane transform, side angles, inverse mapping) is
+// done exactly once per pair -- never replicated across lanes -- and every
+// quadrature point shares one sincos and one reciprocal square root between
+// the SLP and the DLP and between the Helmholtz and Laplace parts of the
+// kernel difference.  Threads of a warp take consecutive pairs of the
+// column-sorted list, so they share the trial element and the code path.
 //
 // Schemes (all restated from the reference, paths inside the NiHu project):
 //  self, constant tria, SLP: analytic static part + (e^{-ikr}-1)/r with the
@@ -28,94 +30,93 @@
 
 namespace nihu {
 
-constexpr int SING_WARPS = 4;
+constexpr int SING_THREADS = 128;
+constexpr double INV_FOUR_PI = 1.0 / FOUR_PI;
 
 struct Acc {
     double sr = 0, si = 0, dr = 0, di = 0;
 };
 
-__device__ __forceinline__ void reduce_acc(Acc &a)
+// G(r) and dG/dr of the Helmholtz kernel sharing one sincos and 1/r:
+//   G = e^{-ikr}/(4 pi r), dG/dr = -(1 + ikr) e^{-ikr}/(4 pi r^2)
+__device__ __forceinline__ void helm_g_dg(double k, double r, double rinv, cd &g, cd &dg)
 {
-    a.sr = warp_sum(a.sr);
-    a.si = warp_sum(a.si);
-    a.dr = warp_sum(a.dr);
-    a.di = warp_sum(a.di);
-}
-
-// G(r) and dG/dr of a family; g = e^{-ikr}/(4 pi r)
-__device__ __forceinline__ cd green(int fam, double k, double r)
-{
-    if (fam == FAM_LAPLACE) return {1.0 / r / FOUR_PI, 0.0};
     double s, c;
     sincos(k * r, &s, &c);
-    return {c / r / FOUR_PI, -s / r / FOUR_PI};
+    double a = rinv * INV_FOUR_PI;
+    g = {c * a, -s * a};
+    double b = a * rinv, kr = k * r;
+    dg = {-(c + kr * s) * b, -(kr * c - s) * b};
 }
 
-__device__ __forceinline__ cd dgreen(int fam, double k, double r)
+// kernel values times the Jacobian at a point y with (unnormalised) normal n:
+// SLP = G J, DLP = dG/dr (r.n)/r (n = N/J, so the J cancels)
+__device__ __forceinline__ void kern_point(int fam, double k, const double x0[3], const double y[3], const double n[3],
+                                           double J, bool do_s, bool do_d, cd &ks, cd &kd)
 {
-    if (fam == FAM_LAPLACE) return {-1.0 / (r * r) / FOUR_PI, 0.0};
-    double s, c;
-    sincos(k * r, &s, &c);
-    double kr = k * r;
-    double f = 1.0 / (r * r) / FOUR_PI;
-    // e^{-ikr} (-ikr - 1) = -(c + kr s) - i (kr c - s)
-    return {-(c + kr * s) * f, -(kr * c - s) * f};
+    double rv0 = y[0] - x0[0], rv1 = y[1] - x0[1], rv2 = y[2] - x0[2];
+    double r2 = rv0 * rv0 + rv1 * rv1 + rv2 * rv2;
+    double r = sqrt(r2);
+    double rinv = 1.0 / r;
+    double rn = (rv0 * n[0] + rv1 * n[1] + rv2 * n[2]) * rinv;  // (r.N)/r = J (r.n)/r
+    if (fam == FAM_LAPLACE) {
+        double a = rinv * INV_FOUR_PI;
+        if (do_s) ks = {a * J, 0.0};
+        if (do_d) kd = {-a * rinv * rn, 0.0};
+        return;
+    }
+    cd g, dg;
+    helm_g_dg(k, r, rinv, g, dg);
+    if (do_s) ks = cscale(g, J);
+    if (do_d) kd = cscale(dg, rn);
 }
 
-// kernel value times Jacobian at reference point (xi, eta) of element e seen from x0
 __device__ __forceinline__ void kern_on_elem(const Elem64 &e, int fam, double k, const double x0[3], double xi,
                                              double eta, bool do_s, bool do_d, cd &ks, cd &kd)
 {
     double y[3], n[3];
     ex(e, xi, eta, y);
     enormal(e, xi, eta, n);
-    double J = norm3(n);
-    double rv[3] = {y[0] - x0[0], y[1] - x0[1], y[2] - x0[2]};
-    double r = norm3(rv);
-    if (do_s) ks = cscale(green(fam, k, r), J);
-    if (do_d) {
-        double rdn = (rv[0] * n[0] + rv[1] * n[1] + rv[2] * n[2]) / J / r;
-        kd = cscale(dgreen(fam, k, r), rdn * J);
-    }
+    kern_point(fam, k, x0, y, n, norm3(n), do_s, do_d, ks, kd);
 }
 
 // ------------------------------------------------------------------ planar
 
 // rotate the element parallel to the x-y plane (nihu/library/plane_element_helper.hpp:112-126)
-__device__ void plane_local(const Elem64 &e, const double x0in[3], double loc[4][3], double x0[3])
+__device__ void plane_local(const Elem64 &e, const double x0in[3], double loc[4][2], double &z)
 {
     double v1[3], v2[3], t0[3], t1[3], t2[3];
     for (int d = 0; d < 3; ++d) { v1[d] = e.c[1][d] - e.c[0][d]; v2[d] = e.c[2][d] - e.c[0][d]; }
-    double n1 = norm3(v1);
-    for (int d = 0; d < 3; ++d) t0[d] = v1[d] / n1;
+    double n1 = 1.0 / norm3(v1);
+    for (int d = 0; d < 3; ++d) t0[d] = v1[d] * n1;
     cross3(v1, v2, t2);
-    double n2 = norm3(t2);
-    for (int d = 0; d < 3; ++d) t2[d] /= n2;
+    double n2 = 1.0 / norm3(t2);
+    for (int d = 0; d < 3; ++d) t2[d] *= n2;
     cross3(t2, t0, t1);
-    double n3 = norm3(t1);
-    for (int d = 0; d < 3; ++d) t1[d] /= n3;
+    double n3 = 1.0 / norm3(t1);
+    for (int d = 0; d < 3; ++d) t1[d] *= n3;
     for (int a = 0; a < e.nc; ++a) {
-        loc[a][0] = dot3(t0, e.c[a]);
-        loc[a][1] = dot3(t1, e.c[a]);
-        loc[a][2] = dot3(t2, e.c[a]);
+        double dv[3] = {e.c[a][0] - x0in[0], e.c[a][1] - x0in[1], e.c[a][2] - x0in[2]};
+        loc[a][0] = dot3(t0, dv);
+        loc[a][1] = dot3(t1, dv);
     }
-    x0[0] = dot3(t0, x0in);
-    x0[1] = dot3(t1, x0in);
-    x0[2] = dot3(t2, x0in);
+    // height of x0 above the element plane
+    double dv[3] = {x0in[0] - e.c[0][0], x0in[1] - e.c[0][1], x0in[2] - e.c[0][2]};
+    z = dot3(t2, dv);
 }
 
-// side data seen from the projected point: corner angle, foot angle, distance
-__device__ __forceinline__ void side_geometry(const double c1[2], const double c2[2], const double p[2], double &th_lim,
-                                              double &th0, double &dref, bool guard_short)
+// corner angle, foot angle and distance of a side (c1 -> c2) seen from the
+// origin of the local frame (nihu/library/plane_element_helper.hpp:76-99)
+__device__ __forceinline__ void side_geometry(const double c1[2], const double c2[2], double &th_lim, double &th0,
+                                              double &dref, bool guard_short)
 {
     double l0 = 1.0, l1 = 0.0;
     double d0 = c2[0] - c1[0], d1 = c2[1] - c1[1];
     double ln = sqrt(d0 * d0 + d1 * d1);
-    if (!guard_short || ln > 1e-3) { l0 = d0 / ln; l1 = d1 / ln; }
-    double a0 = c1[0] - p[0], a1 = c1[1] - p[1];
-    double pr = a0 * l0 + a1 * l1;
-    double f0 = a0 - l0 * pr, f1 = a1 - l1 * pr;
-    th_lim = atan2(a1, a0);
+    if (!guard_short || ln > 1e-3) { double il = 1.0 / ln; l0 = d0 * il; l1 = d1 * il; }
+    double pr = c1[0] * l0 + c1[1] * l1;
+    double f0 = c1[0] - l0 * pr, f1 = c1[1] - l1 * pr;
+    th_lim = atan2(c1[1], c1[0]);
     th0 = atan2(f1, f0);
     dref = sqrt(f0 * f0 + f1 * f1);
 }
@@ -128,99 +129,100 @@ __device__ __forceinline__ void wrap_limits(double &t1, double &t2)
     }
 }
 
-// static (Laplace) nearly singular part over a flat element, lanes 0 .. 6 nc - 1
-// (nihu/library/laplace_nearly_singular_integrals.hpp:62-209); adds SLP and DLP
-// (real) results to a.sr / a.dr after the warp reduction
-__device__ void near_static(const Elem64 &e, const double x0in[3], bool do_s, bool do_d, int lane, Acc &a)
+// static (Laplace) nearly singular part over a flat element: radial integral
+// analytic, angular integral with 6 Gauss points per side
+// (nihu/library/laplace_nearly_singular_integrals.hpp:62-209); adds the SLP and
+// DLP (real) results to a.sr / a.dr
+__device__ void near_static(const Elem64 &e, const double x0[3], bool do_s, bool do_d, Acc &a)
 {
-    double loc[4][3], x0[3];
-    plane_local(e, x0in, loc, x0);
-    const double z = x0[2] - loc[0][2];
-    double s_sum = 0.0, d_sum = 0.0;
+    double loc[4][2], z;
+    plane_local(e, x0, loc, z);
     const int N = e.nc;
-    if (lane < 6 * N) {
-        int side = lane / 6, q = lane % 6;
-        double p[2] = {x0[0], x0[1]};
-        double c1[2] = {loc[side][0], loc[side][1]};
-        double c2[2] = {loc[(side + 1) % N][0], loc[(side + 1) % N][1]};
-        double c3[2] = {loc[(side + 2) % N][0], loc[(side + 2) % N][1]};
-        double t1, th0, dref, t2, dummy0, dummy1;
-        side_geometry(c1, c2, p, t1, th0, dref, false);
-        side_geometry(c2, c3, p, t2, dummy0, dummy1, false);
+    double tl[4], t0[4], dr[4];
+    for (int s = 0; s < N; ++s) side_geometry(loc[s], loc[(s + 1) % N], tl[s], t0[s], dr[s], false);
+    const double az = fabs(z), z2 = z * z;
+    double s_sum = 0.0, d_sum = 0.0;
+    for (int s = 0; s < N; ++s) {
+        double t1 = tl[s], t2 = tl[(s + 1) % N];
         wrap_limits(t1, t2);
-        double jac = (t2 - t1) / 2.0;
-        double xi, w;
-        gauss_pt(6, q, xi, w);
-        double th = t1 * (1.0 - xi) / 2.0 + t2 * (1.0 + xi) / 2.0;
-        double R = dref / cos(th - th0);
-        double r = sqrt(R * R + z * z);
-        if (do_s) s_sum = (r - fabs(z)) * jac * w;
-        if (do_d) d_sum = (1.0 - fabs(z) / r) * jac * w;
+        const double jac = (t2 - t1) / 2.0;
+        for (int q = 0; q < 6; ++q) {
+            double xi, w;
+            gauss_pt(6, q, xi, w);
+            double th = t1 * (1.0 - xi) / 2.0 + t2 * (1.0 + xi) / 2.0;
+            double R = dr[s] / cos(th - t0[s]);
+            double r = sqrt(R * R + z2);
+            if (do_s) s_sum += (r - az) * jac * w;
+            if (do_d) d_sum += (1.0 - az / r) * jac * w;
+        }
     }
-    s_sum = warp_sum(s_sum);
-    d_sum = warp_sum(d_sum);
-    double sg = (0.0 < z) - (z < 0.0);
-    a.sr += s_sum / FOUR_PI;
-    a.dr += sg * d_sum / FOUR_PI;
+    const double sg = (0.0 < z) - (z < 0.0);
+    a.sr += s_sum * INV_FOUR_PI;
+    a.dr += sg * d_sum * INV_FOUR_PI;
 }
 
 // dynamic part (K_k - K_0) of the planar nearly singular scheme with the
-// degree-14 rule; per-lane partial sums (not reduced)
-__device__ void near_dynamic(const Elem64 &e, double k, const double x0[3], bool do_s, bool do_d, int lane, Acc &a)
+// degree-14 rule (42-point Dunavant on triangles, 8x8 Gauss on quads)
+__device__ void near_dynamic(const Elem64 &e, double k, const double x0[3], bool do_s, bool do_d, Acc &a)
 {
     double en[3];
     {
         double xi, eta;
         domain_center(e.nc, xi, eta);
         enormal(e, xi, eta, en);
-        double nn = norm3(en);
-        for (int d = 0; d < 3; ++d) en[d] /= nn;
+        double nn = 1.0 / norm3(en);
+        for (int d = 0; d < 3; ++d) en[d] *= nn;
+    }
+    // flat triangle: x(xi) affine, normal constant
+    double e1[3], e2[3], Jt = 0.0;
+    if (e.nc == 3) {
+        double nt[3];
+        for (int d = 0; d < 3; ++d) { e1[d] = e.c[1][d] - e.c[0][d]; e2[d] = e.c[2][d] - e.c[0][d]; }
+        cross3(e1, e2, nt);
+        Jt = norm3(nt);
     }
     const int np = e.nc == 3 ? 42 : 64;
-    for (int p = lane; p < np; p += 32) {
-        double xi, eta, w;
-        if (e.nc == 3) tri_pt(14, p, xi, eta, w);
-        else {
-            double w0, w1;
+    for (int p = 0; p < np; ++p) {
+        double xi, eta, w, J;
+        double y[3];
+        if (e.nc == 3) {
+            tri_pt(14, p, xi, eta, w);
+            for (int d = 0; d < 3; ++d) y[d] = e.c[0][d] + xi * e1[d] + eta * e2[d];
+            J = Jt;
+        } else {
+            double w0, w1, n[3];
             gauss_pt(8, p / 8, xi, w0);
             gauss_pt(8, p % 8, eta, w1);
             w = w0 * w1;
+            ex(e, xi, eta, y);
+            enormal(e, xi, eta, n);
+            J = norm3(n);
         }
-        double y[3], n[3];
-        ex(e, xi, eta, y);
-        enormal(e, xi, eta, n);
-        double J = norm3(n);
-        double rv[3] = {y[0] - x0[0], y[1] - x0[1], y[2] - x0[2]};
-        double r = norm3(rv);
+        double rv0 = y[0] - x0[0], rv1 = y[1] - x0[1], rv2 = y[2] - x0[2];
+        double r = sqrt(rv0 * rv0 + rv1 * rv1 + rv2 * rv2);
+        double rinv = 1.0 / r;
+        cd g, dg;
+        helm_g_dg(k, r, rinv, g, dg);
+        double g0 = rinv * INV_FOUR_PI;
+        double wj = w * J;
         if (do_s) {
-            cd gk = green(FAM_HELMHOLTZ, k, r), g0 = green(FAM_LAPLACE, k, r);
-            a.sr += (gk.re - g0.re) * w * J;
-            a.si += (gk.im - g0.im) * w * J;
+            a.sr += (g.re - g0) * wj;
+            a.si += g.im * wj;
         }
         if (do_d) {
-            double rdn = dot3(rv, en) / r;
-            cd gk = dgreen(FAM_HELMHOLTZ, k, r), g0 = dgreen(FAM_LAPLACE, k, r);
-            a.dr += (gk.re * rdn - g0.re * rdn) * w * J;
-            a.di += (gk.im * rdn - g0.im * rdn) * w * J;
+            double rdn = (rv0 * en[0] + rv1 * en[1] + rv2 * en[2]) * rinv;
+            double dg0 = -g0 * rinv;
+            a.dr += (dg.re * rdn - dg0 * rdn) * wj;
+            a.di += dg.im * rdn * wj;
         }
     }
 }
 
-// full planar constant-element nearly singular integral (reduced into a)
-__device__ void near_plane(const Elem64 &e, int fam, double k, const double x0[3], bool do_s, bool do_d, int lane,
-                           Acc &a)
+// full planar constant-element nearly singular integral
+__device__ void near_plane(const Elem64 &e, int fam, double k, const double x0[3], bool do_s, bool do_d, Acc &a)
 {
-    Acc dyn;
-    if (fam == FAM_HELMHOLTZ) {
-        near_dynamic(e, k, x0, do_s, do_d, lane, dyn);
-        reduce_acc(dyn);
-    }
-    Acc st;
-    near_static(e, x0, do_s, do_d, lane, st);
-    a.sr += st.sr + dyn.sr;
-    a.si += dyn.si;
-    a.dr += st.dr + dyn.dr;
-    a.di += dyn.di;
+    if (fam == FAM_HELMHOLTZ) near_dynamic(e, k, x0, do_s, do_d, a);
+    near_static(e, x0, do_s, do_d, a);
 }
 
 // ------------------------------------------------------------ inverse mapping
@@ -232,6 +234,9 @@ __device__ bool inverse_mapping(const Elem64 &e, const double x0[3], bool need6,
 {
     double res[3] = {0.0, 0.0, 0.0};
     bool got5 = false;
+    double dxe[3] = {0, 0, 0};
+    if (e.nc == 4)
+        for (int d = 0; d < 3; ++d) dxe[d] = (e.c[0][d] - e.c[1][d] + e.c[2][d] - e.c[3][d]) * 0.25;
     for (int it = 0; it < 100; ++it) {
         double dxi[3], deta[3], n[3], y[3];
         ex(e, res[0], res[1], y);
@@ -251,9 +256,6 @@ __device__ bool inverse_mapping(const Elem64 &e, const double x0[3], bool need6,
             for (int d = 0; d < 3; ++d) r6[d] = res[d];
             return got5;
         }
-        double dxe[3] = {0, 0, 0};
-        if (e.nc == 4)
-            for (int d = 0; d < 3; ++d) dxe[d] = (e.c[0][d] - e.c[1][d] + e.c[2][d] - e.c[3][d]) * 0.25;
         // d n / d xi = (x_xixi x x_eta + x_xi x x_xieta) / sq, x_xixi = x_etaeta = 0
         double t2[3], dnxi[3], dneta[3];
         cross3(dxi, dxe, t2);
@@ -302,47 +304,59 @@ __device__ void linearized(const Elem64 &e, double xi0, double eta0, Elem64 &lin
     }
 }
 
-// polar scheme around (xi0, eta0) with linearized-element subtraction;
-// per-lane partial sums of SLP (do_s) and DLP (do_d)
+// polar scheme around (xi0, eta0) with linearized-element subtraction
 __device__ void near_polar_sum(const Elem64 &e, const Elem64 &lin, int fam, double k, const double x0[3], double xi0,
-                               double eta0, bool do_s, bool do_d, int lane, Acc &a)
+                               double eta0, bool do_s, bool do_d, Acc &a)
 {
     const int N = e.nc;
     double tl[4], t0[4], dr[4];
     for (int n = 0; n < N; ++n) {
-        double c1[2], c2[2], p[2] = {xi0, eta0};
+        double c1[2], c2[2];
         domain_corner(N, n, c1[0], c1[1]);
         domain_corner(N, (n + 1) % N, c2[0], c2[1]);
-        side_geometry(c1, c2, p, tl[n], t0[n], dr[n], true);
+        c1[0] -= xi0; c1[1] -= eta0;
+        c2[0] -= xi0; c2[1] -= eta0;
+        side_geometry(c1, c2, tl[n], t0[n], dr[n], true);
     }
-    for (int p = lane; p < N * 64; p += 32) {
-        int n = p / 64, ia = (p / 8) % 8, ib = p % 8;
+    // the linearized element is affine: one normal for all points
+    double ln[3];
+    enormal(lin, xi0, eta0, ln);
+    const double lJ = norm3(ln);
+    for (int n = 0; n < N; ++n) {
         double t1 = tl[n], t2 = tl[(n + 1) % N];
         wrap_limits(t1, t2);
         if (fabs(t2 - t1) < 1e-3) continue;
-        double xx, wa, xr, wb;
-        gauss_pt(8, ia, xx, wa);
-        gauss_pt(8, ib, xr, wb);
-        double th = ((1.0 - xx) * t1 + (1.0 + xx) * t2) / 2.0;
-        double wth = wa * (t2 - t1) / 2.0;
-        double rho_lim = dr[n] / cos(th - t0[n]);
-        double rho = (1.0 + xr) * rho_lim / 2.0;
-        double wrho = wb * rho_lim / 2.0;
-        double xi = xi0 + rho * cos(th), eta = eta0 + rho * sin(th);
-        cd fs{0, 0}, fd{0, 0}, ls{0, 0}, ld{0, 0};
-        kern_on_elem(e, fam, k, x0, xi, eta, do_s, do_d, fs, fd);
-        kern_on_elem(lin, fam, k, x0, xi, eta, do_s, do_d, ls, ld);
-        double wt = wth * wrho * rho;
-        a.sr += wt * (fs.re - ls.re);
-        a.si += wt * (fs.im - ls.im);
-        a.dr += wt * (fd.re - ld.re);
-        a.di += wt * (fd.im - ld.im);
+        for (int ia = 0; ia < 8; ++ia) {
+            double xx, wa;
+            gauss_pt(8, ia, xx, wa);
+            double th = ((1.0 - xx) * t1 + (1.0 + xx) * t2) / 2.0;
+            double wth = wa * (t2 - t1) / 2.0;
+            double cth, sth;
+            sincos(th, &sth, &cth);
+            double rho_lim = dr[n] / cos(th - t0[n]);
+            for (int ib = 0; ib < 8; ++ib) {
+                double xr, wb;
+                gauss_pt(8, ib, xr, wb);
+                double rho = (1.0 + xr) * rho_lim / 2.0;
+                double wrho = wb * rho_lim / 2.0;
+                double xi = xi0 + rho * cth, eta = eta0 + rho * sth;
+                cd fs{0, 0}, fd{0, 0}, ls{0, 0}, ld{0, 0};
+                kern_on_elem(e, fam, k, x0, xi, eta, do_s, do_d, fs, fd);
+                double yl[3];
+                ex(lin, xi, eta, yl);
+                kern_point(fam, k, x0, yl, ln, lJ, do_s, do_d, ls, ld);
+                double wt = wth * wrho * rho;
+                a.sr += wt * (fs.re - ls.re);
+                a.si += wt * (fs.im - ls.im);
+                a.dr += wt * (fd.re - ld.re);
+                a.di += wt * (fd.im - ld.im);
+            }
+        }
     }
 }
 
-// Telles-transformed 16x16 Gauss rule (DLP only); per-lane partial sums
-__device__ void near_telles_sum(const Elem64 &e, int fam, double k, const double x0[3], const double im[3], int lane,
-                                Acc &a)
+// Telles-transformed 16x16 Gauss rule (DLP only)
+__device__ void near_telles_sum(const Elem64 &e, int fam, double k, const double x0[3], const double im[3], Acc &a)
 {
     double dist = im[2];
     double rb;
@@ -364,43 +378,54 @@ __device__ void near_telles_sum(const Elem64 &e, int fam, double k, const double
         cc[dim] = (3.0 * gb * gb + rb) / Q;
         cdd[dim] = -cb[dim];
     }
-    for (int p = lane; p < 256; p += 32) {
-        double u[2], wu[2];
-        gauss_pt(16, p / 16, u[0], wu[0]);
-        gauss_pt(16, p % 16, u[1], wu[1]);
-        double w = wu[0] * wu[1], t[2];
-        for (int dim = 0; dim < 2; ++dim) {
-            double x = u[dim];
-            t[dim] = ca[dim] * x * x * x + cb[dim] * x * x + cc[dim] * x + cdd[dim];
-            w *= 3.0 * ca[dim] * x * x + 2.0 * cb[dim] * x + cc[dim];
+    double tv[16], tw[16];  // transformed eta nodes and Jacobians (second dimension)
+    for (int b = 0; b < 16; ++b) {
+        double x, w;
+        gauss_pt(16, b, x, w);
+        tv[b] = ca[1] * x * x * x + cb[1] * x * x + cc[1] * x + cdd[1];
+        tw[b] = w * (3.0 * ca[1] * x * x + 2.0 * cb[1] * x + cc[1]);
+    }
+    for (int ia = 0; ia < 16; ++ia) {
+        double x, w;
+        gauss_pt(16, ia, x, w);
+        double t0 = ca[0] * x * x * x + cb[0] * x * x + cc[0] * x + cdd[0];
+        double w0 = w * (3.0 * ca[0] * x * x + 2.0 * cb[0] * x + cc[0]);
+        for (int ib = 0; ib < 16; ++ib) {
+            cd ks{0, 0}, kd{0, 0};
+            kern_on_elem(e, fam, k, x0, t0, tv[ib], false, true, ks, kd);
+            double wt = w0 * tw[ib];
+            a.dr += kd.re * wt;
+            a.di += kd.im * wt;
         }
-        cd ks{0, 0}, kd{0, 0};
-        kern_on_elem(e, fam, k, x0, t[0], t[1], false, true, ks, kd);
-        a.dr += kd.re * w;
-        a.di += kd.im * w;
     }
 }
 
 // -------------------------------------------------------------------- self
 
 // analytic static part of the flat-element 1/r integral from an interior point
-// (nihu/library/plane_element_helper.hpp:42-74), lanes 0 .. nc-1
-__device__ double self_static(const Elem64 &e, const double x0[3], int lane)
+// (nihu/library/plane_element_helper.hpp:42-74)
+__device__ double self_static(const Elem64 &e, const double x0[3])
 {
-    double v = 0.0;
     const int N = e.nc;
-    if (lane < N) {
-        int i = lane, i1 = (lane + 1) % N;
-        double R0[3], R1[3], C[3];
-        for (int d = 0; d < 3; ++d) { R0[d] = e.c[i][d] - x0[d]; R1[d] = e.c[i1][d] - x0[d]; C[d] = e.c[i][d] - e.c[i1][d]; }
-        double r0 = norm3(R0), r1 = norm3(R1), cn = norm3(C);
-        for (int d = 0; d < 3; ++d) { R0[d] /= r0; R1[d] /= r1; C[d] /= cn; }
-        double cs = dot3(R0, R1);
-        double theta = cs >= 1.0 ? 0.0 : acos(cs);
-        double alpha = acos(dot3(R0, C));
-        v = r0 * sin(alpha) * log(tan((alpha + theta) / 2.0) / tan(alpha / 2.0));
+    double R[4][3], r[4];
+    for (int i = 0; i < N; ++i) {
+        for (int d = 0; d < 3; ++d) R[i][d] = e.c[i][d] - x0[d];
+        r[i] = norm3(R[i]);
+        double ir = 1.0 / r[i];
+        for (int d = 0; d < 3; ++d) R[i][d] *= ir;
     }
-    return warp_sum(v);
+    double v = 0.0;
+    for (int i = 0; i < N; ++i) {
+        int i1 = (i + 1) % N;
+        double C[3] = {e.c[i][0] - e.c[i1][0], e.c[i][1] - e.c[i1][1], e.c[i][2] - e.c[i1][2]};
+        double ic = 1.0 / norm3(C);
+        for (int d = 0; d < 3; ++d) C[d] *= ic;
+        double cs = dot3(R[i], R[i1]);
+        double theta = cs >= 1.0 ? 0.0 : acos(cs);
+        double alpha = acos(dot3(R[i], C));
+        v += r[i] * sin(alpha) * log(tan((alpha + theta) / 2.0) / tan(alpha / 2.0));
+    }
+    return v;
 }
 
 __device__ __forceinline__ double sinc_ref(double x)
@@ -409,67 +434,65 @@ __device__ __forceinline__ double sinc_ref(double x)
     return 1.0 - x * x / 6.0 * (1.0 - x * x / 20.0);
 }
 
-__device__ void self_tria(const Elem64 &e, int fam, double k, const double x0[3], int lane, Acc &a)
+__device__ void self_tria(const Elem64 &e, int fam, double k, const double x0[3], Acc &a)
 {
-    double st = self_static(e, x0, lane);
+    double st = self_static(e, x0);
     double dr = 0.0, di = 0.0;
-    if (fam == FAM_HELMHOLTZ && lane < 13) {
-        double xi, eta, w;
-        tri_pt(7, lane, xi, eta, w);
-        double y[3], n[3];
-        ex(e, xi, eta, y);
-        enormal(e, xi, eta, n);
-        double rv[3] = {y[0] - x0[0], y[1] - x0[1], y[2] - x0[2]};
-        double r = norm3(rv);
-        // -ik e^{-ikr/2} sinc(kr/2)
-        double s, c;
-        sincos(k * r / 2.0, &s, &c);
-        double sc = sinc_ref(k * r / 2.0);
-        double wj = w * norm3(n);
-        dr = -k * s * sc * wj;
-        di = -k * c * sc * wj;
+    if (fam == FAM_HELMHOLTZ) {
+        double e1[3], e2[3], nt[3];
+        for (int d = 0; d < 3; ++d) { e1[d] = e.c[1][d] - e.c[0][d]; e2[d] = e.c[2][d] - e.c[0][d]; }
+        cross3(e1, e2, nt);
+        const double J = norm3(nt);
+        for (int p = 0; p < 13; ++p) {
+            double xi, eta, w;
+            tri_pt(7, p, xi, eta, w);
+            double rv[3];
+            for (int d = 0; d < 3; ++d) rv[d] = e.c[0][d] + xi * e1[d] + eta * e2[d] - x0[d];
+            double r = norm3(rv);
+            // (e^{-ikr} - 1)/r = -ik e^{-ikr/2} sinc(kr/2)
+            double s, c;
+            sincos(k * r / 2.0, &s, &c);
+            double sc = sinc_ref(k * r / 2.0);
+            double wj = w * J;
+            dr += -k * s * sc * wj;
+            di += -k * c * sc * wj;
+        }
     }
-    dr = warp_sum(dr);
-    di = warp_sum(di);
-    a.sr += (st + dr) / FOUR_PI;
-    a.si += di / FOUR_PI;
+    a.sr += (st + dr) * INV_FOUR_PI;
+    a.si += di * INV_FOUR_PI;
     // DLP of a flat triangle over itself is zero
 }
 
-__device__ void self_quad(const Elem64 &e, int fam, double k, const double x0[3], bool do_s, bool do_d, int lane,
-                          Acc &a)
+__device__ void self_quad(const Elem64 &e, int fam, double k, const double x0[3], bool do_s, bool do_d, Acc &a)
 {
-    for (int p = lane; p < 64; p += 32) {
-        int d = p / 16, ia = (p % 16) / 4, ib = p % 4;
-        double u, wu, v, wv;
-        gauss_pt(4, ia, u, wu);
-        gauss_pt(4, ib, v, wv);
-        double P[4][2];
-        P[0][0] = P[1][0] = 0.0;
-        P[0][1] = P[1][1] = 0.0;
-        domain_corner(4, d, P[2][0], P[2][1]);
-        domain_corner(4, (d + 1) % 4, P[3][0], P[3][1]);
-        double N[4], dN[4][2];
-        shape(4, u, v, N);
-        dshape(4, u, v, dN);
-        double xi = 0, eta = 0, j00 = 0, j01 = 0, j10 = 0, j11 = 0;
-        for (int c = 0; c < 4; ++c) {
-            xi += N[c] * P[c][0];
-            eta += N[c] * P[c][1];
-            j00 += dN[c][0] * P[c][0];
-            j01 += dN[c][0] * P[c][1];
-            j10 += dN[c][1] * P[c][0];
-            j11 += dN[c][1] * P[c][1];
-        }
-        double wd = wu * wv * (j00 * j11 - j01 * j10);
-        cd ks{0, 0}, kd{0, 0};
-        kern_on_elem(e, fam, k, x0, xi, eta, do_s, do_d, ks, kd);
-        a.sr += ks.re * wd;
-        a.si += ks.im * wd;
-        a.dr += kd.re * wd;
-        a.di += kd.im * wd;
+    for (int d = 0; d < 4; ++d) {
+        double P2[2], P3[2];
+        domain_corner(4, d, P2[0], P2[1]);
+        domain_corner(4, (d + 1) % 4, P3[0], P3[1]);
+        for (int ia = 0; ia < 4; ++ia)
+            for (int ib = 0; ib < 4; ++ib) {
+                double u, wu, v, wv;
+                gauss_pt(4, ia, u, wu);
+                gauss_pt(4, ib, v, wv);
+                // corners P0 = P1 = (0,0) (the collocation point), P2, P3
+                double N[4], dN[4][2];
+                shape(4, u, v, N);
+                dshape(4, u, v, dN);
+                double xi = N[2] * P2[0] + N[3] * P3[0];
+                double eta = N[2] * P2[1] + N[3] * P3[1];
+                double j00 = dN[2][0] * P2[0] + dN[3][0] * P3[0];
+                double j01 = dN[2][0] * P2[1] + dN[3][0] * P3[1];
+                double j10 = dN[2][1] * P2[0] + dN[3][1] * P3[0];
+                double j11 = dN[2][1] * P2[1] + dN[3][1] * P3[1];
+                double wd = wu * wv * (j00 * j11 - j01 * j10);
+                cd ks{0, 0}, kd{0, 0};
+                kern_on_elem(e, fam, k, x0, xi, eta, do_s, do_d, ks, kd);
+                a.sr += ks.re * wd;
+                a.si += ks.im * wd;
+                a.dr += kd.re * wd;
+                a.di += kd.im * wd;
+            }
     }
-    reduce_acc(a);
 }
 
 // ------------------------------------------------------------------ driver
@@ -491,9 +514,8 @@ __device__ __forceinline__ void store64(Out *p, double re, double im, double are
 }
 
 template <typename Out>
-__global__ void __launch_bounds__(32 * SING_WARPS) k_singular(RegularArgs a, NearList near, int *err)
+__global__ void __launch_bounds__(SING_THREADS) k_singular(RegularArgs a, NearList near, int *err)
 {
-    const int lane = threadIdx.x & 31;
     const int64_t p_begin = near.col_ptr ? near.col_ptr[a.j0] : 0;
     const int64_t p_end = near.col_ptr ? near.col_ptr[a.j1] : 0;
     const int64_t n_near = p_end - p_begin;
@@ -505,8 +527,8 @@ __global__ void __launch_bounds__(32 * SING_WARPS) k_singular(RegularArgs a, Nea
     const int fam = a.family;
     const double k = a.k;
 
-    for (int64_t item = (int64_t)blockIdx.x * SING_WARPS + (threadIdx.x >> 5); item < total;
-         item += (int64_t)gridDim.x * SING_WARPS) {
+    for (int64_t item = (int64_t)blockIdx.x * SING_THREADS + threadIdx.x; item < total;
+         item += (int64_t)gridDim.x * SING_THREADS) {
         int i, j;
         bool self;
         if (item < n_near) {
@@ -534,45 +556,34 @@ __global__ void __launch_bounds__(32 * SING_WARPS) k_singular(RegularArgs a, Nea
         bool ok = true;
         if (self) {
             if (e.nc == 3) {
-                if (do_s) self_tria(e, fam, k, x0, lane, acc);
+                if (do_s) self_tria(e, fam, k, x0, acc);
             } else {
-                self_quad(e, fam, k, x0, do_s, do_d, lane, acc);
+                self_quad(e, fam, k, x0, do_s, do_d, acc);
             }
         } else if (e.nc == 3) {
-            near_plane(e, fam, k, x0, do_s, do_d, lane, acc);
+            near_plane(e, fam, k, x0, do_s, do_d, acc);
         } else {
             const bool telles = fam == FAM_HELMHOLTZ && do_d;
             const bool polar_d = fam == FAM_LAPLACE && do_d;
             double r5[3] = {0, 0, 0}, r6[3] = {0, 0, 0};
             ok = inverse_mapping(e, x0, telles, r5, r6);
             if (ok) {
-                Acc part;
                 if (do_s || polar_d) {
                     Elem64 lin;
                     linearized(e, r5[0], r5[1], lin);
-                    near_polar_sum(e, lin, fam, k, x0, r5[0], r5[1], do_s, polar_d, lane, part);
-                    reduce_acc(part);
-                    near_plane(lin, fam, k, x0, do_s, polar_d, lane, part);
+                    near_polar_sum(e, lin, fam, k, x0, r5[0], r5[1], do_s, polar_d, acc);
+                    near_plane(lin, fam, k, x0, do_s, polar_d, acc);
                 }
-                if (telles) {
-                    Acc tp;
-                    near_telles_sum(e, fam, k, x0, r6, lane, tp);
-                    reduce_acc(tp);
-                    part.dr += tp.dr;
-                    part.di += tp.di;
-                }
-                acc = part;
+                if (telles) near_telles_sum(e, fam, k, x0, r6, acc);
             }
         }
-        if (lane == 0) {
-            if (!ok) {
-                atomicCAS(err, 0, (int)min(item + 1, (int64_t)0x7fffffff));
-                continue;
-            }
-            const int64_t off = (int64_t)(j - a.j0) * a.ld + i;
-            if (do_s) store64(out_s + off, acc.sr, acc.si, a.alpha_re, a.alpha_im, a.accumulate);
-            if (do_d) store64(out_d + off, acc.dr, acc.di, a.alpha_re, a.alpha_im, a.accumulate);
+        if (!ok) {
+            atomicCAS(err, 0, (int)min(item + 1, (int64_t)0x7fffffff));
+            continue;
         }
+        const int64_t off = (int64_t)(j - a.j0) * a.ld + i;
+        if (do_s) store64(out_s + off, acc.sr, acc.si, a.alpha_re, a.alpha_im, a.accumulate);
+        if (do_d) store64(out_d + off, acc.dr, acc.di, a.alpha_re, a.alpha_im, a.accumulate);
     }
 }
 
@@ -581,9 +592,11 @@ cudaError_t launch_assemble_singular(const RegularArgs &a, const NearList &near,
     int dev = 0, sms = 148;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    int blocks = sms * 16;
-    if (a.dtype == 0) k_singular<float2><<<blocks, 32 * SING_WARPS, 0, s>>>(a, near, err);
-    else k_singular<double2><<<blocks, 32 * SING_WARPS, 0, s>>>(a, near, err);
+    int64_t total = (near.col_ptr ? near.nnz : 0) + (a.same_mesh ? (a.j1 - a.j0) : 0);
+    int64_t want = (total + SING_THREADS - 1) / SING_THREADS;
+    int blocks = (int)max((int64_t)1, min(want, (int64_t)sms * 16));
+    if (a.dtype == 0) k_singular<float2><<<blocks, SING_THREADS, 0, s>>>(a, near, err);
+    else k_singular<double2><<<blocks, SING_THREADS, 0, s>>>(a, near, err);
     return cudaGetLastError();
 }
 
