@@ -22,9 +22,18 @@ namespace nihu {
 constexpr int REG_THREADS = 256;
 constexpr int REG_COLS = 32;
 
+// sin and cos of 2 pi t for any t: the period count is removed exactly
+// (t - rint(t) is exact in binary floating point), leaving |2 pi f| <= pi for
+// the hardware approximation (absolute error about 4e-7 there)
+__device__ __forceinline__ void sincos_2pi(float t, float &s, float &c)
+{
+    float f = t - rintf(t);
+    __sincosf(6.28318530717958647692f * f, &s, &c);
+}
+
 template <int FAM, typename R>
-__device__ __forceinline__ void eval_point(R rx, R ry, R rz, R wj, R nx, R ny, R nz, R k, bool do_s, bool do_d,
-                                           R &sr, R &si, R &dr, R &di)
+__device__ __forceinline__ void eval_point(R rx, R ry, R rz, R wj, R nx, R ny, R nz, R k, R ws, R wd, R &sr,
+                                           R &si, R &dr, R &di)
 {
     constexpr R INV4PI = R(1.0 / (4.0 * 3.14159265358979323846));
     R r2 = rx * rx + ry * ry + rz * rz;
@@ -32,47 +41,51 @@ __device__ __forceinline__ void eval_point(R rx, R ry, R rz, R wj, R nx, R ny, R
     if constexpr (sizeof(R) == 4) rinv = rsqrtf(r2);
     else rinv = rsqrt(r2);
     R g = wj * rinv * INV4PI;
+    R rdn = (rx * nx + ry * ny + rz * nz) * rinv;
     if constexpr (FAM == FAM_HELMHOLTZ) {
         R kr = k * (r2 * rinv);
         R s, c;
-        if constexpr (sizeof(R) == 4) sincosf(kr, &s, &c);
+        if constexpr (sizeof(R) == 4) sincos_2pi(kr * 0.159154943091895335769f, s, c);
         else sincos(kr, &s, &c);
-        // e^{-ikr} = c - i s
-        if (do_s) { sr += g * c; si -= g * s; }
-        if (do_d) {
-            // dG/dr (r.n)/r = -(1 + ikr) e^{-ikr} / (4 pi r^2) * (r.n)/r
-            R f = -g * rinv * ((rx * nx + ry * ny + rz * nz) * rinv);
-            dr += f * (c + kr * s);
-            di += f * (kr * c - s);
-        }
+        // SLP: G = e^{-ikr}/(4 pi r) = (c - i s)/(4 pi r)
+        R gs = g * ws;
+        sr += gs * c;
+        si -= gs * s;
+        // DLP: dG/dr (r.n)/r = -(1 + ikr) e^{-ikr} / (4 pi r^2) * (r.n)/r
+        R f = -g * rinv * rdn * wd;
+        dr += f * (c + kr * s);
+        di += f * (kr * c - s);
     } else {
-        if (do_s) sr += g;
-        if (do_d) dr -= g * rinv * ((rx * nx + ry * ny + rz * nz) * rinv);
+        sr += g * ws;
+        dr -= g * rinv * rdn * wd;
     }
 }
 
 template <typename Out, typename R>
-__device__ __forceinline__ void store_entry(Out *p, R re, R im, double are, double aim, int accumulate)
+__device__ __forceinline__ void store_entry(Out *p, R re, R im, R are, R aim, bool unit_alpha, int accumulate)
 {
-    R vr = R(are) * re - R(aim) * im;
-    R vi = R(are) * im + R(aim) * re;
+    R vr = re, vi = im;
+    if (!unit_alpha) {
+        vr = are * re - aim * im;
+        vi = are * im + aim * re;
+    }
+    Out o;
     if (accumulate) {
-        Out o = *p;
+        o = *p;
         o.x += vr;
         o.y += vi;
-        *p = o;
     } else {
-        Out o;
         o.x = vr;
         o.y = vi;
-        *p = o;
     }
+    *p = o;
 }
 
 template <typename R, typename Out, int FAM, int OPS>
 __global__ void __launch_bounds__(REG_THREADS) k_regular(RegularArgs a)
 {
-    __shared__ float4 s_hi[REG_COLS], s_lo[REG_COLS], s_p0[REG_COLS];
+    __shared__ float4 s_hi[REG_COLS], s_lo[REG_COLS];
+    __shared__ int s_nc[REG_COLS];
     constexpr bool DO_S = (OPS & OP_SLP) != 0;
     constexpr bool DO_D = (OPS & OP_DLP) != 0;
     const DevMesh &test = a.test;
@@ -83,7 +96,7 @@ __global__ void __launch_bounds__(REG_THREADS) k_regular(RegularArgs a)
     if (threadIdx.x < ncols) {
         s_hi[threadIdx.x] = trial.chi[jb + threadIdx.x];
         s_lo[threadIdx.x] = trial.clo[jb + threadIdx.x];
-        s_p0[threadIdx.x] = trial.p0[jb + threadIdx.x];
+        s_nc[threadIdx.x] = trial.nc[jb + threadIdx.x];
     }
     __syncthreads();
     if (i >= test.n) return;
@@ -91,11 +104,18 @@ __global__ void __launch_bounds__(REG_THREADS) k_regular(RegularArgs a)
     const float4 ih = test.chi[i], il = test.clo[i];
     const int par = il.w != 0.0f ? 1 : 0;
     const R k = R(a.k);
-    R xi0, xi1, xi2;
+    const R are = R(a.alpha_re), aim = R(a.alpha_im);
+    const bool unit_alpha = a.alpha_re == 1.0 && a.alpha_im == 0.0;
+    const int accumulate = a.accumulate;
+    R x0, x1, x2;
     if constexpr (sizeof(R) == 8) {
-        xi0 = test.center[3 * (int64_t)i];
-        xi1 = test.center[3 * (int64_t)i + 1];
-        xi2 = test.center[3 * (int64_t)i + 2];
+        x0 = test.center[3 * (int64_t)i];
+        x1 = test.center[3 * (int64_t)i + 1];
+        x2 = test.center[3 * (int64_t)i + 2];
+    } else {
+        x0 = ih.x + il.x;
+        x1 = ih.y + il.y;
+        x2 = ih.z + il.z;
     }
     Out *out_s = reinterpret_cast<Out *>(a.out_s);
     Out *out_d = reinterpret_cast<Out *>(a.out_d);
@@ -107,51 +127,38 @@ __global__ void __launch_bounds__(REG_THREADS) k_regular(RegularArgs a)
         int kind = classify_pair(ih, il, s_hi[c], s_lo[c], i, j, test.center, trial.center, trial.size,
                                  a.same_mesh, ls, ld, dx, dy, dz);
         if (kind != KIND_REGULAR) continue;
+        if (!DO_S) ls = ld;
+        if (!DO_D) ld = ls;
+        // one uniform loop over this lane's points: SLP and DLP at the same
+        // level share every point; otherwise the SLP points come first
+        const int tnc = s_nc[c];
+        const int nps = level_npts(tnc, par, ls);
+        const int npd = level_npts(tnc, par, ld);
+        const int n_eval = ls == ld ? nps : nps + npd;
+        const int64_t base = ((int64_t)j * 2 + par) * SLOTS;
         R sr = 0, si = 0, dr = 0, di = 0;
-        const int tnc = trial.nc[j];
-        if constexpr (sizeof(R) == 4) {
-            // FP32: level-0 point is the trial centre; r = c_j - c_i from the hi/lo split
-            auto eval_level = [&](int lev, bool es, bool ed) {
-                if (lev == 0) {
-                    float4 p = s_p0[c];
-                    eval_point<FAM, float>(dx, dy, dz, p.x, p.y, p.z, p.w, k, es, ed, sr, si, dr, di);
-                    return;
-                }
-                const int np = level_npts(tnc, par, lev);
-                const float4 *pp = trial.pts32 + 2 * (((int64_t)j * 2 + par) * SLOTS + level_slot0(lev));
-                const float xx = ih.x + il.x, xy = ih.y + il.y, xz = ih.z + il.z;
-                for (int q = 0; q < np; ++q) {
-                    float4 y = __ldg(pp + 2 * q), n = __ldg(pp + 2 * q + 1);
-                    eval_point<FAM, float>(y.x - xx, y.y - xy, y.z - xz, y.w, n.x, n.y, n.z, k, es, ed, sr, si, dr,
-                                           di);
-                }
-            };
-            if (!DO_S || !DO_D || ls == ld) {
-                eval_level(DO_S && DO_D ? ls : (DO_S ? ls : ld), DO_S, DO_D);
+        for (int q = 0; q < n_eval; ++q) {
+            int slot;
+            R ws, wd;
+            if (ls == ld) { slot = level_slot0(ls) + q; ws = R(DO_S); wd = R(DO_D); }
+            else if (q < nps) { slot = level_slot0(ls) + q; ws = R(1); wd = R(0); }
+            else { slot = level_slot0(ld) + q - nps; ws = R(0); wd = R(1); }
+            if constexpr (sizeof(R) == 4) {
+                const float4 y = __ldg(trial.pts32 + 2 * (base + slot));
+                const float4 n = __ldg(trial.pts32 + 2 * (base + slot) + 1);
+                // level-0 point: the trial centre; use the accurate hi/lo difference
+                const bool centre = slot == 0;
+                eval_point<FAM, float>(centre ? dx : y.x - x0, centre ? dy : y.y - x1, centre ? dz : y.z - x2, y.w,
+                                       n.x, n.y, n.z, k, ws, wd, sr, si, dr, di);
             } else {
-                eval_level(ls, true, false);
-                eval_level(ld, false, true);
-            }
-        } else {
-            auto eval_level = [&](int lev, bool es, bool ed) {
-                const int np = level_npts(tnc, par, lev);
-                const double *pp = trial.pts64 + 8 * (((int64_t)j * 2 + par) * SLOTS + level_slot0(lev));
-                for (int q = 0; q < np; ++q) {
-                    const double *y = pp + 8 * q;
-                    eval_point<FAM, double>(y[0] - xi0, y[1] - xi1, y[2] - xi2, y[3], y[4], y[5], y[6], k, es, ed, sr,
-                                            si, dr, di);
-                }
-            };
-            if (!DO_S || !DO_D || ls == ld) {
-                eval_level(DO_S && DO_D ? ls : (DO_S ? ls : ld), DO_S, DO_D);
-            } else {
-                eval_level(ls, true, false);
-                eval_level(ld, false, true);
+                const double *y = trial.pts64 + 8 * (base + slot);
+                eval_point<FAM, double>(y[0] - x0, y[1] - x1, y[2] - x2, y[3], y[4], y[5], y[6], k, ws, wd, sr, si,
+                                        dr, di);
             }
         }
         const int64_t off = (int64_t)(j - a.j0) * a.ld + i;
-        if (DO_S) store_entry(out_s + off, sr, si, a.alpha_re, a.alpha_im, a.accumulate);
-        if (DO_D) store_entry(out_d + off, dr, di, a.alpha_re, a.alpha_im, a.accumulate);
+        if (DO_S) store_entry(out_s + off, sr, si, are, aim, unit_alpha, accumulate);
+        if (DO_D) store_entry(out_d + off, dr, di, are, aim, unit_alpha, accumulate);
     }
 }
 

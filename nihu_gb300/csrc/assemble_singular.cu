@@ -37,12 +37,65 @@ struct Acc {
     double sr = 0, si = 0, dr = 0, di = 0;
 };
 
+// Maclaurin series of cos and sin truncated after x^22 / x^23: on
+// |x| <= pi/2 the first omitted terms are below 1e-19, so these agree with the
+// correctly rounded values to a few ulp at a fraction of the cost of the
+// general routines (which reduce arbitrary arguments).  Coefficients are
+// (-1)^n / (2n)! and (-1)^n / (2n+1)!.
+struct TaylorCoeffs {
+    double c[12], s[12];
+    constexpr TaylorCoeffs() : c(), s()
+    {
+        double fc = 1.0, fs = 1.0;  // (2n)! and (2n+1)!
+        for (int n = 0; n < 12; ++n) {
+            if (n > 0) {
+                fc *= (2.0 * n - 1.0) * (2.0 * n);
+                fs *= (2.0 * n) * (2.0 * n + 1.0);
+            }
+            c[n] = (n % 2 ? -1.0 : 1.0) / fc;
+            s[n] = (n % 2 ? -1.0 : 1.0) / fs;
+        }
+    }
+};
+__device__ constexpr TaylorCoeffs TAYLOR{};
+constexpr double HALF_PI = 1.57079632679489661923;
+
+__device__ __forceinline__ void sincos_bounded(double x, double *s, double *c)
+{
+    if (fabs(x) > HALF_PI) {
+        sincos(x, s, c);
+        return;
+    }
+    const double u = x * x;
+    double pc = TAYLOR.c[11], ps = TAYLOR.s[11];
+#pragma unroll
+    for (int n = 10; n >= 0; --n) {
+        pc = fma(pc, u, TAYLOR.c[n]);
+        ps = fma(ps, u, TAYLOR.s[n]);
+    }
+    *c = pc;
+    *s = ps * x;
+}
+
+// cos of an angle difference known to lie within pi/2 of 0 modulo 2 pi
+__device__ __forceinline__ double cos_angle(double x)
+{
+    if (x > PI) x -= 2.0 * PI;
+    else if (x < -PI) x += 2.0 * PI;
+    if (fabs(x) > HALF_PI) return cos(x);
+    const double u = x * x;
+    double pc = TAYLOR.c[11];
+#pragma unroll
+    for (int n = 10; n >= 0; --n) pc = fma(pc, u, TAYLOR.c[n]);
+    return pc;
+}
+
 // G(r) and dG/dr of the Helmholtz kernel sharing one sincos and 1/r:
 //   G = e^{-ikr}/(4 pi r), dG/dr = -(1 + ikr) e^{-ikr}/(4 pi r^2)
 __device__ __forceinline__ void helm_g_dg(double k, double r, double rinv, cd &g, cd &dg)
 {
     double s, c;
-    sincos(k * r, &s, &c);
+    sincos_bounded(k * r, &s, &c);
     double a = rinv * INV_FOUR_PI;
     g = {c * a, -s * a};
     double b = a * rinv, kr = k * r;
@@ -56,8 +109,8 @@ __device__ __forceinline__ void kern_point(int fam, double k, const double x0[3]
 {
     double rv0 = y[0] - x0[0], rv1 = y[1] - x0[1], rv2 = y[2] - x0[2];
     double r2 = rv0 * rv0 + rv1 * rv1 + rv2 * rv2;
-    double r = sqrt(r2);
-    double rinv = 1.0 / r;
+    double rinv = rsqrt(r2);
+    double r = r2 * rinv;
     double rn = (rv0 * n[0] + rv1 * n[1] + rv2 * n[2]) * rinv;  // (r.N)/r = J (r.n)/r
     if (fam == FAM_LAPLACE) {
         double a = rinv * INV_FOUR_PI;
@@ -150,7 +203,7 @@ __device__ void near_static(const Elem64 &e, const double x0[3], bool do_s, bool
             double xi, w;
             gauss_pt(6, q, xi, w);
             double th = t1 * (1.0 - xi) / 2.0 + t2 * (1.0 + xi) / 2.0;
-            double R = dr[s] / cos(th - t0[s]);
+            double R = dr[s] / cos_angle(th - t0[s]);
             double r = sqrt(R * R + z2);
             if (do_s) s_sum += (r - az) * jac * w;
             if (do_d) d_sum += (1.0 - az / r) * jac * w;
@@ -199,8 +252,9 @@ __device__ void near_dynamic(const Elem64 &e, double k, const double x0[3], bool
             J = norm3(n);
         }
         double rv0 = y[0] - x0[0], rv1 = y[1] - x0[1], rv2 = y[2] - x0[2];
-        double r = sqrt(rv0 * rv0 + rv1 * rv1 + rv2 * rv2);
-        double rinv = 1.0 / r;
+        double r2 = rv0 * rv0 + rv1 * rv1 + rv2 * rv2;
+        double rinv = rsqrt(r2);
+        double r = r2 * rinv;
         cd g, dg;
         helm_g_dg(k, r, rinv, g, dg);
         double g0 = rinv * INV_FOUR_PI;
@@ -333,7 +387,7 @@ __device__ void near_polar_sum(const Elem64 &e, const Elem64 &lin, int fam, doub
             double wth = wa * (t2 - t1) / 2.0;
             double cth, sth;
             sincos(th, &sth, &cth);
-            double rho_lim = dr[n] / cos(th - t0[n]);
+            double rho_lim = dr[n] / cos_angle(th - t0[n]);
             for (int ib = 0; ib < 8; ++ib) {
                 double xr, wb;
                 gauss_pt(8, ib, xr, wb);
@@ -451,7 +505,7 @@ __device__ void self_tria(const Elem64 &e, int fam, double k, const double x0[3]
             double r = norm3(rv);
             // (e^{-ikr} - 1)/r = -ik e^{-ikr/2} sinc(kr/2)
             double s, c;
-            sincos(k * r / 2.0, &s, &c);
+            sincos_bounded(k * r / 2.0, &s, &c);
             double sc = sinc_ref(k * r / 2.0);
             double wj = w * J;
             dr += -k * s * sc * wj;
@@ -592,9 +646,12 @@ cudaError_t launch_assemble_singular(const RegularArgs &a, const NearList &near,
     int dev = 0, sms = 148;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    // one 4-warp block per SM saturates the FP64 pipe (a warp-wide FP64
+    // instruction occupies it for many cycles) and leaves the rest of every SM
+    // to the concurrently running regular kernel
     int64_t total = (near.col_ptr ? near.nnz : 0) + (a.same_mesh ? (a.j1 - a.j0) : 0);
     int64_t want = (total + SING_THREADS - 1) / SING_THREADS;
-    int blocks = (int)max((int64_t)1, min(want, (int64_t)sms * 16));
+    int blocks = (int)max((int64_t)1, min(want, (int64_t)sms));
     if (a.dtype == 0) k_singular<float2><<<blocks, SING_THREADS, 0, s>>>(a, near, err);
     else k_singular<double2><<<blocks, SING_THREADS, 0, s>>>(a, near, err);
     return cudaGetLastError();

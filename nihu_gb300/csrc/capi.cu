@@ -20,6 +20,8 @@ struct nihu_gb_ctx {
     int device = 0;
     cudaStream_t stream = nullptr;
     cudaStream_t copy_stream = nullptr;
+    cudaStream_t aux_stream = nullptr;  // high priority: FP64 singular kernel beside the regular one
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     bool own_stream = false;
     size_t budget = 0;
     size_t used = 0;
@@ -133,23 +135,24 @@ cudaEvent_t pool_event(nihu_gb_ctx *ctx)
     return e;
 }
 
-// bracket a phase with events on the context stream (no-op unless profiling)
+// bracket a phase with events on a stream (no-op unless profiling)
 struct Phase {
     nihu_gb_ctx *ctx;
     const char *name;
+    cudaStream_t stream;
     cudaEvent_t a = nullptr;
-    Phase(nihu_gb_ctx *c, const char *n) : ctx(c), name(n)
+    Phase(nihu_gb_ctx *c, const char *n, cudaStream_t s = nullptr) : ctx(c), name(n), stream(s ? s : c->stream)
     {
         if (ctx->profiling) {
             a = pool_event(ctx);
-            cudaEventRecord(a, ctx->stream);
+            cudaEventRecord(a, stream);
         }
     }
     ~Phase()
     {
         if (a) {
             cudaEvent_t b = pool_event(ctx);
-            cudaEventRecord(b, ctx->stream);
+            cudaEventRecord(b, stream);
             ctx->pending.push_back({name, {a, b}});
         }
     }
@@ -243,19 +246,28 @@ bool valid_where(int w) { return w == NIHU_GB_HOST || w == NIHU_GB_DEVICE; }
 
 // regular + singular kernels for columns [j0, j1) into device buffers whose
 // column j starts at out + (j - j0) * ld
+// The FP64 singular/nearly singular kernel and the FP32 regular kernel write
+// disjoint entries and load different pipes (FP64 vs FMA/XU + HBM stores), so
+// they run concurrently: the singular kernel first, on the high-priority
+// auxiliary stream with one block per SM, the regular kernel on the main
+// stream filling the remaining SM resources; the main stream then joins.
 nihu_gb_status assemble_panel(nihu_gb_ctx *ctx, RegularArgs a, NearList *nl)
 {
-    cudaError_t e;
+    cudaError_t e = cudaEventRecord(ctx->ev_fork, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(ctx->aux_stream, ctx->ev_fork, 0);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "fork");
+    {
+        Phase ph(ctx, "assemble_singular", ctx->aux_stream);
+        e = launch_assemble_singular(a, *nl, ctx->d_flag, ctx->aux_stream);
+    }
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "assemble_singular launch");
+    if ((e = cudaEventRecord(ctx->ev_join, ctx->aux_stream)) != cudaSuccess) return cuda_fail(ctx, e, "join");
     {
         Phase ph(ctx, "assemble_regular");
         e = launch_assemble_regular(a, ctx->stream);
     }
     if (e != cudaSuccess) return cuda_fail(ctx, e, "assemble_regular launch");
-    {
-        Phase ph(ctx, "assemble_singular");
-        e = launch_assemble_singular(a, *nl, ctx->d_flag, ctx->stream);
-    }
-    if (e != cudaSuccess) return cuda_fail(ctx, e, "assemble_singular launch");
+    if ((e = cudaStreamWaitEvent(ctx->stream, ctx->ev_join, 0)) != cudaSuccess) return cuda_fail(ctx, e, "join");
     ctx->launches += 2;
     return NIHU_GB_OK;
 }
@@ -298,7 +310,12 @@ nihu_gb_status nihu_gb_ctx_create(int device, void *stream, size_t hbm_budget_by
         if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess) { delete ctx; return NIHU_GB_ERR_CUDA; }
         ctx->own_stream = true;
     }
-    if (cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking) != cudaSuccess) {
+    int prio_lo = 0, prio_hi = 0;
+    cudaDeviceGetStreamPriorityRange(&prio_lo, &prio_hi);
+    if (cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaStreamCreateWithPriority(&ctx->aux_stream, cudaStreamNonBlocking, prio_hi) != cudaSuccess ||
+        cudaEventCreateWithFlags(&ctx->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&ctx->ev_join, cudaEventDisableTiming) != cudaSuccess) {
         nihu_gb_ctx_destroy(ctx);
         return NIHU_GB_ERR_CUDA;
     }
@@ -322,7 +339,11 @@ void nihu_gb_ctx_destroy(nihu_gb_ctx *ctx)
     if (ctx->h_small) cudaFreeHost(ctx->h_small);
     collect_phases(ctx);
     for (cudaEvent_t e : ctx->event_pool) cudaEventDestroy(e);
+    if (ctx->aux_stream) cudaStreamSynchronize(ctx->aux_stream);
     if (ctx->copy_stream) cudaStreamDestroy(ctx->copy_stream);
+    if (ctx->aux_stream) cudaStreamDestroy(ctx->aux_stream);
+    if (ctx->ev_fork) cudaEventDestroy(ctx->ev_fork);
+    if (ctx->ev_join) cudaEventDestroy(ctx->ev_join);
     if (ctx->own_stream && ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
 }

@@ -100,7 +100,7 @@ def test_fp64_mode_matches_oracle(gpu_ctx, oracle, name, family, k):
         assert np.all(np.isfinite(out[op]))
         assert rel_norm(out[op], ref) < 1e-11, (op, rel_norm(out[op], ref))
         if op == g.SLP:
-            assert rel_entry(out[op], ref) < 1e-11
+            assert rel_entry(out[op], ref) < 1e-10
 
 
 @pytest.mark.parametrize("name,family,k", CASES)
