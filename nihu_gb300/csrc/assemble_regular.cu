@@ -81,10 +81,16 @@ __device__ __forceinline__ void store_entry(Out *p, R re, R im, R are, R aim, bo
     *p = o;
 }
 
+// Squared distance ratio above which a pair is certainly regular with the
+// 1-point rule for both SLP (x >= 9.1) and DLP (x >= 15.8): 15.8^2 with a
+// relative margin far larger than the FP32 error of the plain centre
+// difference of a far pair.
+constexpr float Q_FAR = 249.64f * (1.0f + 1e-4f);
+
 template <typename R, typename Out, int FAM, int OPS>
 __global__ void __launch_bounds__(REG_THREADS) k_regular(RegularArgs a)
 {
-    __shared__ float4 s_hi[REG_COLS], s_lo[REG_COLS];
+    __shared__ float4 s_hi[REG_COLS], s_lo[REG_COLS], s_p0[REG_COLS];
     __shared__ int s_nc[REG_COLS];
     constexpr bool DO_S = (OPS & OP_SLP) != 0;
     constexpr bool DO_D = (OPS & OP_DLP) != 0;
@@ -97,11 +103,17 @@ __global__ void __launch_bounds__(REG_THREADS) k_regular(RegularArgs a)
         s_hi[threadIdx.x] = trial.chi[jb + threadIdx.x];
         s_lo[threadIdx.x] = trial.clo[jb + threadIdx.x];
         s_nc[threadIdx.x] = trial.nc[jb + threadIdx.x];
+        s_p0[threadIdx.x] = trial.p0[jb + threadIdx.x];
     }
     __syncthreads();
-    if (i >= test.n) return;
+    // whole warps beyond the last row leave; a partial last warp keeps its
+    // out-of-range lanes (clamped to the last row, writes masked) so that
+    // warp votes see every lane
+    if ((i & ~31) >= test.n) return;
+    const bool row_ok = i < test.n;
+    const int ii = row_ok ? i : test.n - 1;
 
-    const float4 ih = test.chi[i], il = test.clo[i];
+    const float4 ih = test.chi[ii], il = test.clo[ii];
     const int par = il.w != 0.0f ? 1 : 0;
     const R k = R(a.k);
     const R are = R(a.alpha_re), aim = R(a.alpha_im);
@@ -109,9 +121,9 @@ __global__ void __launch_bounds__(REG_THREADS) k_regular(RegularArgs a)
     const int accumulate = a.accumulate;
     R x0, x1, x2;
     if constexpr (sizeof(R) == 8) {
-        x0 = test.center[3 * (int64_t)i];
-        x1 = test.center[3 * (int64_t)i + 1];
-        x2 = test.center[3 * (int64_t)i + 2];
+        x0 = test.center[3 * (int64_t)ii];
+        x1 = test.center[3 * (int64_t)ii + 1];
+        x2 = test.center[3 * (int64_t)ii + 2];
     } else {
         x0 = ih.x + il.x;
         x1 = ih.y + il.y;
@@ -122,11 +134,29 @@ __global__ void __launch_bounds__(REG_THREADS) k_regular(RegularArgs a)
 
     for (int c = 0; c < ncols; ++c) {
         const int j = jb + c;
+        if constexpr (sizeof(R) == 4) {
+            // far-field fast path, taken when every lane of the warp is a far
+            // pair: one centroid point for both operators
+            const float4 h = s_hi[c];
+            const float fx = h.x - x0, fy = h.y - x1, fz = h.z - x2;
+            const float q = (fx * fx + fy * fy + fz * fz) * h.w;
+            if (__all_sync(0xffffffffu, q > Q_FAR)) {
+                const float4 p = s_p0[c];
+                R sr = 0, si = 0, dr = 0, di = 0;
+                eval_point<FAM, float>(fx, fy, fz, p.x, p.y, p.z, p.w, k, R(DO_S), R(DO_D), sr, si, dr, di);
+                if (row_ok) {
+                    const int64_t off = (int64_t)(j - a.j0) * a.ld + i;
+                    if (DO_S) store_entry(out_s + off, sr, si, are, aim, unit_alpha, accumulate);
+                    if (DO_D) store_entry(out_d + off, dr, di, are, aim, unit_alpha, accumulate);
+                }
+                continue;
+            }
+        }
         int ls, ld;
         float dx, dy, dz;
-        int kind = classify_pair(ih, il, s_hi[c], s_lo[c], i, j, test.center, trial.center, trial.size,
+        int kind = classify_pair(ih, il, s_hi[c], s_lo[c], ii, j, test.center, trial.center, trial.size,
                                  a.same_mesh, ls, ld, dx, dy, dz);
-        if (kind != KIND_REGULAR) continue;
+        if (kind != KIND_REGULAR || !row_ok) continue;
         if (!DO_S) ls = ld;
         if (!DO_D) ld = ls;
         // one uniform loop over this lane's points: SLP and DLP at the same

@@ -62,16 +62,30 @@ constexpr double HALF_PI = 1.57079632679489661923;
 
 __device__ __forceinline__ void sincos_bounded(double x, double *s, double *c)
 {
-    if (fabs(x) > HALF_PI) {
+    const double ax = fabs(x);
+    if (ax > HALF_PI) {
         sincos(x, s, c);
         return;
     }
     const double u = x * x;
-    double pc = TAYLOR.c[11], ps = TAYLOR.s[11];
+    double pc, ps;
+    if (ax <= 0.5) {
+        // |x| <= 1/2: terms up to x^16 / x^17 (omitted < 2e-22)
+        pc = TAYLOR.c[8];
+        ps = TAYLOR.s[8];
 #pragma unroll
-    for (int n = 10; n >= 0; --n) {
-        pc = fma(pc, u, TAYLOR.c[n]);
-        ps = fma(ps, u, TAYLOR.s[n]);
+        for (int n = 7; n >= 0; --n) {
+            pc = fma(pc, u, TAYLOR.c[n]);
+            ps = fma(ps, u, TAYLOR.s[n]);
+        }
+    } else {
+        pc = TAYLOR.c[11];
+        ps = TAYLOR.s[11];
+#pragma unroll
+        for (int n = 10; n >= 0; --n) {
+            pc = fma(pc, u, TAYLOR.c[n]);
+            ps = fma(ps, u, TAYLOR.s[n]);
+        }
     }
     *c = pc;
     *s = ps * x;
@@ -204,9 +218,11 @@ __device__ void near_static(const Elem64 &e, const double x0[3], bool do_s, bool
             gauss_pt(6, q, xi, w);
             double th = t1 * (1.0 - xi) / 2.0 + t2 * (1.0 + xi) / 2.0;
             double R = dr[s] / cos_angle(th - t0[s]);
-            double r = sqrt(R * R + z2);
-            if (do_s) s_sum += (r - az) * jac * w;
-            if (do_d) d_sum += (1.0 - az / r) * jac * w;
+            double r2 = R * R + z2;
+            double rinv = rsqrt(r2);
+            double jw = jac * w;
+            if (do_s) s_sum += (r2 * rinv - az) * jw;  // r - |z|
+            if (do_d) d_sum += (1.0 - az * rinv) * jw;  // 1 - |z|/r
         }
     }
     const double sg = (0.0 < z) - (z < 0.0);
@@ -254,20 +270,21 @@ __device__ void near_dynamic(const Elem64 &e, double k, const double x0[3], bool
         double rv0 = y[0] - x0[0], rv1 = y[1] - x0[1], rv2 = y[2] - x0[2];
         double r2 = rv0 * rv0 + rv1 * rv1 + rv2 * rv2;
         double rinv = rsqrt(r2);
-        double r = r2 * rinv;
-        cd g, dg;
-        helm_g_dg(k, r, rinv, g, dg);
-        double g0 = rinv * INV_FOUR_PI;
-        double wj = w * J;
+        double kr = k * (r2 * rinv);
+        double sn, cs;
+        sincos_bounded(kr, &sn, &cs);
+        // t = w J / (4 pi r); e^{-ikr} = cs - i sn
+        //   SLP: (G_k - G_0) w J = t (cs - 1 - i sn)
+        //   DLP: (dG_k - dG_0)/dr (r.n)/r w J = -t/r (r.n)/r ((cs + kr sn - 1) + i (kr cs - sn))
+        const double t = w * J * rinv * INV_FOUR_PI;
         if (do_s) {
-            a.sr += (g.re - g0) * wj;
-            a.si += g.im * wj;
+            a.sr += t * (cs - 1.0);
+            a.si -= t * sn;
         }
         if (do_d) {
-            double rdn = (rv0 * en[0] + rv1 * en[1] + rv2 * en[2]) * rinv;
-            double dg0 = -g0 * rinv;
-            a.dr += (dg.re * rdn - dg0 * rdn) * wj;
-            a.di += dg.im * rdn * wj;
+            double u = t * rinv * ((rv0 * en[0] + rv1 * en[1] + rv2 * en[2]) * rinv);
+            a.dr -= u * (cs + kr * sn - 1.0);
+            a.di -= u * (kr * cs - sn);
         }
     }
 }
