@@ -60,32 +60,23 @@ struct TaylorCoeffs {
 __device__ constexpr TaylorCoeffs TAYLOR{};
 constexpr double HALF_PI = 1.57079632679489661923;
 
-__device__ __forceinline__ void sincos_bounded(double x, double *s, double *c)
+// sin and cos for |x| <= pi/2 (general routine beyond).  `short_series`
+// is a launch-wide promise that every argument has |x| <= 3/4 (nearly
+// singular pairs at small k D): the terms up to x^18 / x^19 then leave an
+// error below 2e-21.
+__device__ __forceinline__ void sincos_bounded(double x, double *s, double *c, bool short_series)
 {
     const double ax = fabs(x);
-    if (ax > HALF_PI) {
+    if (ax > HALF_PI || (short_series && ax > 0.75)) {
         sincos(x, s, c);
         return;
     }
     const double u = x * x;
-    double pc, ps;
-    if (ax <= 0.5) {
-        // |x| <= 1/2: terms up to x^16 / x^17 (omitted < 2e-22)
-        pc = TAYLOR.c[8];
-        ps = TAYLOR.s[8];
-#pragma unroll
-        for (int n = 7; n >= 0; --n) {
-            pc = fma(pc, u, TAYLOR.c[n]);
-            ps = fma(ps, u, TAYLOR.s[n]);
-        }
-    } else {
-        pc = TAYLOR.c[11];
-        ps = TAYLOR.s[11];
-#pragma unroll
-        for (int n = 10; n >= 0; --n) {
-            pc = fma(pc, u, TAYLOR.c[n]);
-            ps = fma(ps, u, TAYLOR.s[n]);
-        }
+    const int top = short_series ? 9 : 11;
+    double pc = TAYLOR.c[top], ps = TAYLOR.s[top];
+    for (int n = top - 1; n >= 0; --n) {
+        pc = fma(pc, u, TAYLOR.c[n]);
+        ps = fma(ps, u, TAYLOR.s[n]);
     }
     *c = pc;
     *s = ps * x;
@@ -94,8 +85,7 @@ __device__ __forceinline__ void sincos_bounded(double x, double *s, double *c)
 // cos of an angle difference known to lie within pi/2 of 0 modulo 2 pi
 __device__ __forceinline__ double cos_angle(double x)
 {
-    if (x > PI) x -= 2.0 * PI;
-    else if (x < -PI) x += 2.0 * PI;
+    x -= (2.0 * PI) * rint(x * (0.5 / PI));
     if (fabs(x) > HALF_PI) return cos(x);
     const double u = x * x;
     double pc = TAYLOR.c[11];
@@ -109,7 +99,7 @@ __device__ __forceinline__ double cos_angle(double x)
 __device__ __forceinline__ void helm_g_dg(double k, double r, double rinv, cd &g, cd &dg)
 {
     double s, c;
-    sincos_bounded(k * r, &s, &c);
+    sincos_bounded(k * r, &s, &c, false);
     double a = rinv * INV_FOUR_PI;
     g = {c * a, -s * a};
     double b = a * rinv, kr = k * r;
@@ -232,7 +222,8 @@ __device__ void near_static(const Elem64 &e, const double x0[3], bool do_s, bool
 
 // dynamic part (K_k - K_0) of the planar nearly singular scheme with the
 // degree-14 rule (42-point Dunavant on triangles, 8x8 Gauss on quads)
-__device__ void near_dynamic(const Elem64 &e, double k, const double x0[3], bool do_s, bool do_d, Acc &a)
+__device__ void near_dynamic(const Elem64 &e, double k, const double x0[3], bool do_s, bool do_d, Acc &a,
+                             const double4 *__restrict__ pts42, bool short_series)
 {
     double en[3];
     {
@@ -242,22 +233,23 @@ __device__ void near_dynamic(const Elem64 &e, double k, const double x0[3], bool
         double nn = 1.0 / norm3(en);
         for (int d = 0; d < 3; ++d) en[d] *= nn;
     }
-    // flat triangle: x(xi) affine, normal constant
-    double e1[3], e2[3], Jt = 0.0;
-    if (e.nc == 3) {
-        double nt[3];
-        for (int d = 0; d < 3; ++d) { e1[d] = e.c[1][d] - e.c[0][d]; e2[d] = e.c[2][d] - e.c[0][d]; }
-        cross3(e1, e2, nt);
-        Jt = norm3(nt);
-    }
     const int np = e.nc == 3 ? 42 : 64;
     for (int p = 0; p < np; ++p) {
         double xi, eta, w, J;
         double y[3];
-        if (e.nc == 3) {
+        if (pts42) {
+            // precomputed per triangle: (y, w J) of the 42-point rule
+            const double4 v = pts42[p];
+            y[0] = v.x; y[1] = v.y; y[2] = v.z;
+            w = v.w;
+            J = 1.0;
+        } else if (e.nc == 3) {
+            double e1[3], e2[3], nt[3];
+            for (int d = 0; d < 3; ++d) { e1[d] = e.c[1][d] - e.c[0][d]; e2[d] = e.c[2][d] - e.c[0][d]; }
+            cross3(e1, e2, nt);
             tri_pt(14, p, xi, eta, w);
             for (int d = 0; d < 3; ++d) y[d] = e.c[0][d] + xi * e1[d] + eta * e2[d];
-            J = Jt;
+            J = norm3(nt);
         } else {
             double w0, w1, n[3];
             gauss_pt(8, p / 8, xi, w0);
@@ -272,7 +264,7 @@ __device__ void near_dynamic(const Elem64 &e, double k, const double x0[3], bool
         double rinv = rsqrt(r2);
         double kr = k * (r2 * rinv);
         double sn, cs;
-        sincos_bounded(kr, &sn, &cs);
+        sincos_bounded(kr, &sn, &cs, short_series);
         // t = w J / (4 pi r); e^{-ikr} = cs - i sn
         //   SLP: (G_k - G_0) w J = t (cs - 1 - i sn)
         //   DLP: (dG_k - dG_0)/dr (r.n)/r w J = -t/r (r.n)/r ((cs + kr sn - 1) + i (kr cs - sn))
@@ -290,9 +282,10 @@ __device__ void near_dynamic(const Elem64 &e, double k, const double x0[3], bool
 }
 
 // full planar constant-element nearly singular integral
-__device__ void near_plane(const Elem64 &e, int fam, double k, const double x0[3], bool do_s, bool do_d, Acc &a)
+__device__ void near_plane(const Elem64 &e, int fam, double k, const double x0[3], bool do_s, bool do_d, Acc &a,
+                           const double4 *__restrict__ pts42 = nullptr, bool short_series = false)
 {
-    if (fam == FAM_HELMHOLTZ) near_dynamic(e, k, x0, do_s, do_d, a);
+    if (fam == FAM_HELMHOLTZ) near_dynamic(e, k, x0, do_s, do_d, a, pts42, short_series);
     near_static(e, x0, do_s, do_d, a);
 }
 
@@ -522,7 +515,7 @@ __device__ void self_tria(const Elem64 &e, int fam, double k, const double x0[3]
             double r = norm3(rv);
             // (e^{-ikr} - 1)/r = -ik e^{-ikr/2} sinc(kr/2)
             double s, c;
-            sincos_bounded(k * r / 2.0, &s, &c);
+            sincos_bounded(k * r / 2.0, &s, &c, false);
             double sc = sinc_ref(k * r / 2.0);
             double wj = w * J;
             dr += -k * s * sc * wj;
@@ -597,6 +590,8 @@ __global__ void __launch_bounds__(SING_THREADS) k_singular(RegularArgs a, NearLi
     Out *out_d = reinterpret_cast<Out *>(a.out_d);
     const int fam = a.family;
     const double k = a.k;
+    // nearly singular pairs have r < 1.5 D + (point to centre) <= 3 D_max
+    const bool short_series = k * 3.0 * a.trial_size_max <= 0.75;
 
     for (int64_t item = (int64_t)blockIdx.x * SING_THREADS + threadIdx.x; item < total;
          item += (int64_t)gridDim.x * SING_THREADS) {
@@ -632,7 +627,7 @@ __global__ void __launch_bounds__(SING_THREADS) k_singular(RegularArgs a, NearLi
                 self_quad(e, fam, k, x0, do_s, do_d, acc);
             }
         } else if (e.nc == 3) {
-            near_plane(e, fam, k, x0, do_s, do_d, acc);
+            near_plane(e, fam, k, x0, do_s, do_d, acc, a.trial.dyn42 + 42 * (int64_t)j, short_series);
         } else {
             const bool telles = fam == FAM_HELMHOLTZ && do_d;
             const bool polar_d = fam == FAM_LAPLACE && do_d;

@@ -47,6 +47,7 @@ struct nihu_gb_mesh {
     nihu_gb_ctx *ctx = nullptr;
     uint64_t uid = 0;
     int64_t n = 0;
+    double size_max = 0.0;  // largest element size (mean edge length)
     DevMesh dm;
     std::vector<void *> bufs;
 };
@@ -437,11 +438,11 @@ nihu_gb_status nihu_gb_mesh_create(nihu_gb_ctx *ctx, const double *nodes, int64_
     m->dm.n = (int)n_elems;
     const int64_t n = std::max<int64_t>(n_elems, 1);
     struct Req { void **p; size_t bytes; };
-    void *corners, *center, *size, *nc, *chi, *clo, *p0, *pts32, *pts64;
+    void *corners, *center, *size, *nc, *chi, *clo, *p0, *pts32, *pts64, *dyn42;
     Req reqs[] = {{&corners, sizeof(double) * 12 * n}, {&center, sizeof(double) * 3 * n}, {&size, sizeof(double) * n},
                   {&nc, sizeof(int8_t) * n}, {&chi, sizeof(float4) * n}, {&clo, sizeof(float4) * n},
                   {&p0, sizeof(float4) * n}, {&pts32, sizeof(float4) * 2 * 2 * SLOTS * n},
-                  {&pts64, sizeof(double) * 8 * 2 * SLOTS * n}};
+                  {&pts64, sizeof(double) * 8 * 2 * SLOTS * n}, {&dyn42, sizeof(double4) * 42 * n}};
     for (auto &r : reqs) {
         nihu_gb_status st = dmalloc(ctx, r.bytes, r.p);
         if (st) { nihu_gb_mesh_destroy(m); return st; }
@@ -456,6 +457,7 @@ nihu_gb_status nihu_gb_mesh_create(nihu_gb_ctx *ctx, const double *nodes, int64_
     m->dm.p0 = (float4 *)p0;
     m->dm.pts32 = (float4 *)pts32;
     m->dm.pts64 = (double *)pts64;
+    m->dm.dyn42 = (double4 *)dyn42;
     for (int64_t e = 0; e < n_elems; ++e) {
         int32_t t = elems[e * elem_cols];
         if (t == NIHU_GB_TRIA_1) m->dm.has_tria = 1;
@@ -484,19 +486,23 @@ nihu_gb_status nihu_gb_mesh_create(nihu_gb_ctx *ctx, const double *nodes, int64_
         cudaError_t e = cudaMemcpyAsync(dnodes, nodes, sizeof(double) * 3 * n_nodes, cudaMemcpyHostToDevice, ctx->stream);
         if (e == cudaSuccess)
             e = cudaMemcpyAsync(delems, elems, sizeof(int32_t) * n_elems * elem_cols, cudaMemcpyHostToDevice, ctx->stream);
-        if (e == cudaSuccess) e = cudaMemsetAsync(ctx->d_flag, 0, sizeof(int), ctx->stream);
+        if (e == cudaSuccess) e = cudaMemsetAsync(ctx->d_flag, 0, 4 * sizeof(int), ctx->stream);
+        unsigned long long *dmax = (unsigned long long *)(ctx->d_flag + 2);
         if (e == cudaSuccess)
             e = launch_mesh_geometry((const double *)dnodes, n_nodes, (const int32_t *)delems, (int)n_elems,
-                                     (int)elem_cols, m->dm, ctx->d_flag, ctx->stream);
+                                     (int)elem_cols, m->dm, ctx->d_flag, dmax, ctx->stream);
         ctx->launches += 1;
         int bad = 0;
+        unsigned long long smax = 0;
         if (e == cudaSuccess) e = cudaMemcpyAsync(&bad, ctx->d_flag, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(&smax, dmax, sizeof(smax), cudaMemcpyDeviceToHost, ctx->stream);
         if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
         dfree(ctx, dnodes);
         dfree(ctx, delems);
         if (e != cudaSuccess) { nihu_gb_mesh_destroy(m); return cuda_fail(ctx, e, "mesh geometry"); }
+        std::memcpy(&m->size_max, &smax, sizeof(double));
+        cudaMemsetAsync(ctx->d_flag, 0, 4 * sizeof(int), ctx->stream);
         if (bad) {
-            cudaMemsetAsync(ctx->d_flag, 0, sizeof(int), ctx->stream);
             nihu_gb_mesh_destroy(m);
             return fail(ctx, NIHU_GB_ERR_INVALID_ARGUMENT, "invalid element " + std::to_string(bad - 1));
         }
@@ -562,6 +568,7 @@ nihu_gb_status nihu_gb_assemble(nihu_gb_ctx *ctx, const nihu_gb_mesh *test, cons
     a.precision = precision;
     a.dtype = dtype;
     a.accumulate = accumulate ? 1 : 0;
+    a.trial_size_max = trial->size_max;
     const size_t es = elem_bytes(dtype);
     const int64_t M = test->n, N = trial->n;
 

@@ -50,6 +50,9 @@ struct DevMesh {
     float4 *pts32 = nullptr;
     // the same in FP64: [n][2][SLOTS][8] doubles (y, w*J, unit normal, 0)
     double *pts64 = nullptr;
+    // triangles: the 42 points of the degree-14 rule used by the nearly
+    // singular dynamic part, (y, w*J) in FP64; [n][42] (unused for quads)
+    double4 *dyn42 = nullptr;
 };
 
 // number of points of a regular level for (trial corners, test complexity)

@@ -20,8 +20,9 @@ struct NearList {
 // mesh.cu -----------------------------------------------------------------
 // geometry of n elements from device copies of the node and element arrays;
 // bad[0] receives 1 + the first invalid element index (0 if all valid)
+// size_max receives the largest element size (as the bits of a positive double)
 cudaError_t launch_mesh_geometry(const double *nodes, int64_t n_nodes, const int32_t *elems, int n,
-                                 int cols, DevMesh m, int *bad, cudaStream_t s);
+                                 int cols, DevMesh m, int *bad, unsigned long long *size_max, cudaStream_t s);
 
 // classify.cu -------------------------------------------------------------
 // count the nearly singular rows of every column: counts[j]
@@ -48,6 +49,7 @@ struct RegularArgs {
     int64_t ld;
     int j0, j1;
     int accumulate;
+    double trial_size_max;  // largest mean edge length of the trial mesh
 };
 cudaError_t launch_assemble_regular(const RegularArgs &a, cudaStream_t s);
 

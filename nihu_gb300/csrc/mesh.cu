@@ -7,7 +7,7 @@ namespace nihu {
 
 // one thread per element
 __global__ void k_mesh_geometry(const double *__restrict__ nodes, int64_t n_nodes, const int32_t *__restrict__ elems,
-                                int n, int cols, DevMesh m, int *bad)
+                                int n, int cols, DevMesh m, int *bad, unsigned long long *size_max)
 {
     int e = blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= n) return;
@@ -43,6 +43,7 @@ __global__ void k_mesh_geometry(const double *__restrict__ nodes, int64_t n_node
     double size = s / nc;
     for (int d = 0; d < 3; ++d) m.center[3 * (int64_t)e + d] = cen[d];
     m.size[e] = size;
+    atomicMax(size_max, (unsigned long long)__double_as_longlong(size));  // positive doubles order as integers
 
     // FP32 centre split into hi + lo parts so that centre differences keep
     // ~FP32 relative accuracy however close two elements are
@@ -50,6 +51,19 @@ __global__ void k_mesh_geometry(const double *__restrict__ nodes, int64_t n_node
     m.chi[e] = make_float4(hx, hy, hz, (float)(1.0 / (size * size)));
     m.clo[e] = make_float4((float)(cen[0] - (double)hx), (float)(cen[1] - (double)hy), (float)(cen[2] - (double)hz),
                            nc == 4 ? 1.0f : 0.0f);
+
+    // degree-14 points of the nearly singular dynamic part (triangles)
+    if (nc == 3) {
+        double nv[3];
+        enormal(el, 1.0 / 3.0, 1.0 / 3.0, nv);
+        const double J = norm3(nv);
+        for (int p = 0; p < 42; ++p) {
+            double qx, qe, w, y[3];
+            tri_pt(14, p, qx, qe, w);
+            ex(el, qx, qe, y);
+            m.dyn42[42 * (int64_t)e + p] = make_double4(y[0], y[1], y[2], w * J);
+        }
+    }
 
     // regular quadrature points for both test-complexity parities
     for (int par = 0; par < 2; ++par) {
@@ -86,11 +100,11 @@ __global__ void k_mesh_geometry(const double *__restrict__ nodes, int64_t n_node
 }
 
 cudaError_t launch_mesh_geometry(const double *nodes, int64_t n_nodes, const int32_t *elems, int n, int cols,
-                                 DevMesh m, int *bad, cudaStream_t s)
+                                 DevMesh m, int *bad, unsigned long long *size_max, cudaStream_t s)
 {
     if (n == 0) return cudaSuccess;
     int threads = 128;
-    k_mesh_geometry<<<(n + threads - 1) / threads, threads, 0, s>>>(nodes, n_nodes, elems, n, cols, m, bad);
+    k_mesh_geometry<<<(n + threads - 1) / threads, threads, 0, s>>>(nodes, n_nodes, elems, n, cols, m, bad, size_max);
     return cudaGetLastError();
 }
 
