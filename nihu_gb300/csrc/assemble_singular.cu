@@ -72,11 +72,23 @@ __device__ __forceinline__ void sincos_bounded(double x, double *s, double *c, b
         return;
     }
     const double u = x * x;
-    const int top = short_series ? 9 : 11;
-    double pc = TAYLOR.c[top], ps = TAYLOR.s[top];
-    for (int n = top - 1; n >= 0; --n) {
-        pc = fma(pc, u, TAYLOR.c[n]);
-        ps = fma(ps, u, TAYLOR.s[n]);
+    double pc, ps;
+    if (short_series) {
+        pc = TAYLOR.c[9];
+        ps = TAYLOR.s[9];
+#pragma unroll
+        for (int n = 8; n >= 0; --n) {
+            pc = fma(pc, u, TAYLOR.c[n]);
+            ps = fma(ps, u, TAYLOR.s[n]);
+        }
+    } else {
+        pc = TAYLOR.c[11];
+        ps = TAYLOR.s[11];
+#pragma unroll
+        for (int n = 10; n >= 0; --n) {
+            pc = fma(pc, u, TAYLOR.c[n]);
+            ps = fma(ps, u, TAYLOR.s[n]);
+        }
     }
     *c = pc;
     *s = ps * x;
@@ -658,12 +670,12 @@ cudaError_t launch_assemble_singular(const RegularArgs &a, const NearList &near,
     int dev = 0, sms = 148;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    // one 4-warp block per SM saturates the FP64 pipe (a warp-wide FP64
-    // instruction occupies it for many cycles) and leaves the rest of every SM
+    // two 4-warp blocks per SM keep the narrow FP64 pipe busy (a warp-wide
+    // FP64 instruction occupies it for many cycles) and leave most of every SM
     // to the concurrently running regular kernel
     int64_t total = (near.col_ptr ? near.nnz : 0) + (a.same_mesh ? (a.j1 - a.j0) : 0);
     int64_t want = (total + SING_THREADS - 1) / SING_THREADS;
-    int blocks = (int)max((int64_t)1, min(want, (int64_t)sms));
+    int blocks = (int)max((int64_t)1, min(want, (int64_t)sms * 2));
     if (a.dtype == 0) k_singular<float2><<<blocks, SING_THREADS, 0, s>>>(a, near, err);
     else k_singular<double2><<<blocks, SING_THREADS, 0, s>>>(a, near, err);
     return cudaGetLastError();
