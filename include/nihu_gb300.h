@@ -171,6 +171,27 @@ nihu_gb_status nihu_gb_matvec(nihu_gb_ctx *ctx, int dtype_a, const void *A, int6
                               const void *x, void *y, double alpha_re, double alpha_im,
                               double beta_re, double beta_im, int where);
 
+/* y = alpha * A x + beta * y like nihu_gb_matvec(), for callers that cannot
+ * allocate device memory (hosts that reserve all of it for their own pool,
+ * request loops that must never wait on the allocator, plug-in hosts whose
+ * memory manager forbids allocations behind their back).  No context is
+ * needed and nothing is allocated: the partial sums live in one static device
+ * array of NIHU_GB_NOALLOC_PARTIAL_ELEMS complex128 values (16 MiB) that every
+ * GPU which loads the library keeps until the process exits.  A, x, y are
+ * device pointers on the current device; the work is enqueued on `stream`
+ * (a cudaStream_t, NULL = the legacy default stream) and is complete when the
+ * stream reaches that point.  m above NIHU_GB_NOALLOC_PARTIAL_ELEMS returns
+ * NIHU_GB_ERR_OUT_OF_RANGE.  The first call on a device looks up the array's
+ * device address (cudaGetSymbolAddress), so make it before any stream
+ * capture.  All calls share the array and every call overwrites the part it
+ * reads, so nothing needs clearing -- but two calls that run on the GPU at the
+ * same time (different streams or host threads) race and corrupt each other.
+ * This entry point has no counterpart in the reference. */
+#define NIHU_GB_NOALLOC_PARTIAL_ELEMS (1 << 20)
+nihu_gb_status nihu_gb_matvec_noalloc(int dtype_a, const void *A, int64_t m, int64_t n, int64_t lda, const void *x,
+                                      void *y, double alpha_re, double alpha_im, double beta_re, double beta_im,
+                                      void *stream);
+
 /* Solve A x = b with restarted GMRES(restart) (nihu/fmm/GMRES.h:57-205
  * semantics: stop when |residual estimate| / |b - A x0| < tol).  A is n x n
  * (dtype_a) on the device; b and x are complex128 (x holds the initial guess

@@ -23,6 +23,7 @@ SLP, DLP = 1, 2
 C64, C128 = 0, 1
 REGULAR_FP32, REGULAR_FP64 = 0, 1
 HOST, DEVICE = 0, 1
+NOALLOC_PARTIAL_ELEMS = 1 << 20  # NIHU_GB_NOALLOC_PARTIAL_ELEMS
 
 # every symbol include/nihu_gb300.h declares, with (restype, argtypes)
 _vp, _i, _i64, _d, _sz = ctypes.c_void_p, ctypes.c_int, ctypes.c_int64, ctypes.c_double, ctypes.c_size_t
@@ -49,6 +50,7 @@ SIGNATURES = {
     "nihu_gb_add_identity": (_i, [_vp, _vp, _d, _d, _i, _vp, _i64, _i]),
     "nihu_gb_pair_statistics": (_i, [_vp, _vp, _vp, ctypes.POINTER(ctypes.c_int64)]),
     "nihu_gb_matvec": (_i, [_vp, _i, _vp, _i64, _i64, _i64, _vp, _vp, _d, _d, _d, _d, _i]),
+    "nihu_gb_matvec_noalloc": (_i, [_i, _vp, _i64, _i64, _i64, _vp, _vp, _d, _d, _d, _d, _vp]),
     "nihu_gb_gmres": (_i, [_vp, _i, _vp, _i64, _i64, _vp, _vp, _i, _i, _d, _ip, _dp, _i]),
     "nihu_gb_lu_solve": (_i, [_vp, _vp, _i64, _i64, _vp, _vp, _i]),
     "nihu_gb_solve_cbie": (_i, [_vp, _vp, _i, _d, _i, _i, _vp, _vp, _i, _i, _i, _d, _ip, _dp]),
