@@ -235,7 +235,7 @@ __device__ void near_static(const Elem64 &e, const double x0[3], bool do_s, bool
 // dynamic part (K_k - K_0) of the planar nearly singular scheme with the
 // degree-14 rule (42-point Dunavant on triangles, 8x8 Gauss on quads)
 __device__ void near_dynamic(const Elem64 &e, double k, const double x0[3], bool do_s, bool do_d, Acc &a,
-                             const double4 *__restrict__ pts42, bool short_series)
+                             const Pt4 *__restrict__ pts42, bool short_series)
 {
     double en[3];
     {
@@ -251,7 +251,7 @@ __device__ void near_dynamic(const Elem64 &e, double k, const double x0[3], bool
         double y[3];
         if (pts42) {
             // precomputed per triangle: (y, w J) of the 42-point rule
-            const double4 v = pts42[p];
+            const Pt4 v = pts42[p];
             y[0] = v.x; y[1] = v.y; y[2] = v.z;
             w = v.w;
             J = 1.0;
@@ -295,7 +295,7 @@ __device__ void near_dynamic(const Elem64 &e, double k, const double x0[3], bool
 
 // full planar constant-element nearly singular integral
 __device__ void near_plane(const Elem64 &e, int fam, double k, const double x0[3], bool do_s, bool do_d, Acc &a,
-                           const double4 *__restrict__ pts42 = nullptr, bool short_series = false)
+                           const Pt4 *__restrict__ pts42 = nullptr, bool short_series = false)
 {
     if (fam == FAM_HELMHOLTZ) near_dynamic(e, k, x0, do_s, do_d, a, pts42, short_series);
     near_static(e, x0, do_s, do_d, a);

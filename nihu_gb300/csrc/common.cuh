@@ -52,7 +52,7 @@ struct DevMesh {
     double *pts64 = nullptr;
     // triangles: the 42 points of the degree-14 rule used by the nearly
     // singular dynamic part, (y, w*J) in FP64; [n][42] (unused for quads)
-    double4 *dyn42 = nullptr;
+    struct Pt4 *dyn42 = nullptr;
 };
 
 // number of points of a regular level for (trial corners, test complexity)
@@ -64,6 +64,11 @@ __host__ __device__ inline int level_npts(int trial_nc, int test_c, int level)
 }
 
 struct cd { double re, im; };
+
+// four doubles in one 32-byte aligned record (point + weight)
+struct __align__(32) Pt4 {
+    double x, y, z, w;
+};
 
 __device__ __forceinline__ cd cmul(cd a, cd b) { return {a.re * b.re - a.im * b.im, a.re * b.im + a.im * b.re}; }
 __device__ __forceinline__ cd cadd(cd a, cd b) { return {a.re + b.re, a.im + b.im}; }

@@ -61,7 +61,7 @@ __global__ void k_mesh_geometry(const double *__restrict__ nodes, int64_t n_node
             double qx, qe, w, y[3];
             tri_pt(14, p, qx, qe, w);
             ex(el, qx, qe, y);
-            m.dyn42[42 * (int64_t)e + p] = make_double4(y[0], y[1], y[2], w * J);
+            m.dyn42[42 * (int64_t)e + p] = Pt4{y[0], y[1], y[2], w * J};
         }
     }
 
