@@ -670,12 +670,12 @@ cudaError_t launch_assemble_singular(const RegularArgs &a, const NearList &near,
     int dev = 0, sms = 148;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    // two 4-warp blocks per SM keep the narrow FP64 pipe busy (a warp-wide
+    // one 4-warp block per SM keeps the narrow FP64 pipe busy (a warp-wide
     // FP64 instruction occupies it for many cycles) and leave most of every SM
     // to the concurrently running regular kernel
     int64_t total = (near.col_ptr ? near.nnz : 0) + (a.same_mesh ? (a.j1 - a.j0) : 0);
     int64_t want = (total + SING_THREADS - 1) / SING_THREADS;
-    int blocks = (int)max((int64_t)1, min(want, (int64_t)sms * 2));
+    int blocks = (int)max((int64_t)1, min(want, (int64_t)sms));
     if (a.dtype == 0) k_singular<float2><<<blocks, SING_THREADS, 0, s>>>(a, near, err);
     else k_singular<double2><<<blocks, SING_THREADS, 0, s>>>(a, near, err);
     return cudaGetLastError();

@@ -1,0 +1,53 @@
+"""The C++ front end (include/nihu_gb300/nihu.hpp): NiHu-shaped user code
+compiled with g++ against the C ABI, run on the GPU, checked against the
+FP64 oracle and the analytic pulsating sphere."""
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+from nihu_gb300 import meshes
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def build_shim(tmp):
+    exe = os.path.join(tmp, "test_shim")
+    lib_dir = os.path.join(ROOT, "nihu_gb300")
+    subprocess.check_call(["g++", "-std=c++17", "-O2", "-Wall", "-Wextra", os.path.join(ROOT, "tests", "cpp", "test_shim.cpp"),
+                           "-I", os.path.join(ROOT, "include"), "-L", lib_dir, "-lnihu_gb300",
+                           "-Wl,-rpath," + lib_dir, "-o", exe])
+    return exe
+
+
+def test_shim_compiles(tmp_path):
+    """The header is plain C++17 and links against the library (no GPU needed)."""
+    build_shim(str(tmp_path))
+
+
+@pytest.mark.gpu
+def test_shim_acoustic_bem_sequence(tmp_path, oracle):
+    exe = build_shim(str(tmp_path))
+    nodes, elems = meshes.icosphere(2)
+    mesh_bin = tmp_path / "mesh.bin"
+    with open(mesh_bin, "wb") as f:
+        f.write(np.array([len(nodes), len(elems)], np.int64).tobytes())
+        f.write(np.ascontiguousarray(nodes, np.float64).tobytes())
+        f.write(np.ascontiguousarray(elems, np.int32).tobytes())
+    out_bin = tmp_path / "out.bin"
+    k = 1.0
+    r = subprocess.run([exe, str(mesh_bin), str(k), str(out_bin)], capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stdout + r.stderr
+    n = len(elems)
+    raw = np.fromfile(out_bin, dtype=np.complex128)
+    Ls = raw[:n * n].reshape(n, n, order="F")
+    Ms = raw[n * n:2 * n * n].reshape(n, n, order="F")
+    p = raw[2 * n * n:]
+    mesh = (nodes, elems)
+    L = oracle.assemble(mesh, mesh, oracle.HELMHOLTZ, oracle.SLP, k, threads=8)
+    M = oracle.assemble(mesh, mesh, oracle.HELMHOLTZ, oracle.DLP, k, threads=8) - 0.5 * np.eye(n)
+    assert np.abs(Ls - L).max() / np.abs(L).max() < 1e-5
+    assert np.abs(Ms - M).max() / np.abs(M).max() < 1e-5
+    p_ref = np.linalg.solve(M, L @ np.ones(n))
+    assert np.abs(p - p_ref).max() / np.abs(p_ref).max() < 1e-4
