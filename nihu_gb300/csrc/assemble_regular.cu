@@ -115,9 +115,17 @@ __global__ void __launch_bounds__(REG_THREADS) k_regular(RegularArgs a)
 
     const float4 ih = test.chi[ii], il = test.clo[ii];
     const int par = il.w != 0.0f ? 1 : 0;
-    const R k = R(a.k);
-    const R are = R(a.alpha_re), aim = R(a.alpha_im);
-    const bool unit_alpha = a.alpha_re == 1.0 && a.alpha_im == 0.0;
+    R k, are, aim;
+    if constexpr (sizeof(R) == 4) {
+        k = a.k32;
+        are = a.alpha_re32;
+        aim = a.alpha_im32;
+    } else {
+        k = a.k;
+        are = a.alpha_re;
+        aim = a.alpha_im;
+    }
+    const bool unit_alpha = a.unit_alpha != 0;
     const int accumulate = a.accumulate;
     R x0, x1, x2;
     if constexpr (sizeof(R) == 8) {

@@ -569,6 +569,10 @@ nihu_gb_status nihu_gb_assemble(nihu_gb_ctx *ctx, const nihu_gb_mesh *test, cons
     a.dtype = dtype;
     a.accumulate = accumulate ? 1 : 0;
     a.trial_size_max = trial->size_max;
+    a.k32 = (float)a.k;
+    a.alpha_re32 = (float)alpha_re;
+    a.alpha_im32 = (float)alpha_im;
+    a.unit_alpha = alpha_re == 1.0 && alpha_im == 0.0;
     const size_t es = elem_bytes(dtype);
     const int64_t M = test->n, N = trial->n;
 

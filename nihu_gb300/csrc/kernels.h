@@ -50,6 +50,10 @@ struct RegularArgs {
     int j0, j1;
     int accumulate;
     double trial_size_max;  // largest mean edge length of the trial mesh
+    // the same parameters pre-rounded on the host, so the FP32 kernel runs no
+    // FP64 instruction (the FP64 pipe belongs to the concurrent singular kernel)
+    float k32, alpha_re32, alpha_im32;
+    int unit_alpha;
 };
 cudaError_t launch_assemble_regular(const RegularArgs &a, cudaStream_t s);
 
