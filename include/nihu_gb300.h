@@ -192,6 +192,36 @@ nihu_gb_status nihu_gb_matvec_noalloc(int dtype_a, const void *A, int64_t m, int
                                       void *y, double alpha_re, double alpha_im, double beta_re, double beta_im,
                                       void *stream);
 
+/* arithmetic of a multi-right-hand-side product (nihu_gb_gemm) */
+#define NIHU_GB_GEMM_FP32 0   /* FP32 on the CUDA cores */
+#define NIHU_GB_GEMM_TF32 1   /* TF32 tensor cores, FP32 accumulation */
+#define NIHU_GB_GEMM_BF16X9 2 /* split BF16 (3 parts, 9 products) on the tensor cores: FP32-accurate */
+
+/* Y = alpha * A X + beta * Y for nrhs right-hand sides: A complex64 m x n
+ * (lda), X n x nrhs (ldx) and Y m x nrhs (ldy) complex128, column-major.
+ * One real GEMM on the float view of A (even rows Re A, odd rows Im A) times
+ * the planes [Re X | Im X] reads A once; the complex combination and alpha,
+ * beta are applied in FP64.  The multi-RHS product of the reference is
+ * Eigen's dense product (nihu/applications/helmholtz/helmholtz_3d_coll.cpp:68-74).
+ * All buffers on the device when where = NIHU_GB_DEVICE. */
+nihu_gb_status nihu_gb_gemm(nihu_gb_ctx *ctx, int mode, const void *A, int64_t m, int64_t n, int64_t lda,
+                            const void *X, int64_t ldx, int64_t nrhs, void *Y, int64_t ldy, double alpha_re,
+                            double alpha_im, double beta_re, double beta_im, int where);
+
+/* Solve A X = B for nrhs right-hand sides (A complex64 n x n, B and X
+ * complex128 n x nrhs, ld = n) by mixed-precision iterative refinement:
+ * each outer step runs one GMRES(restart) cycle on every right-hand side in
+ * lockstep (the products A [v_1 .. v_nrhs] are one tensor-core GEMM of mode
+ * inner_mode; FP64 Arnoldi), stops a column when its residual estimate falls
+ * by inner_tol, adds the correction to X in FP64 and recomputes the residual
+ * B - A X with BF16x9 (FP32-accurate) products accumulated in FP64.  Stops
+ * when every column has |B - A X| <= tol |B|.  X starts from zero.
+ * rel_residuals (nrhs doubles) receives the final relative residuals. */
+nihu_gb_status nihu_gb_solve_multi(nihu_gb_ctx *ctx, const void *A, int64_t n, int64_t lda, const void *B, void *X,
+                                   int64_t nrhs, int inner_mode, int restart, int max_outer, double tol,
+                                   double inner_tol, int *outer_iters, int *inner_iters, double *rel_residuals,
+                                   int where);
+
 /* Solve A x = b with restarted GMRES(restart) (nihu/fmm/GMRES.h:57-205
  * semantics: stop when |residual estimate| / |b - A x0| < tol).  A is n x n
  * (dtype_a) on the device; b and x are complex128 (x holds the initial guess

@@ -22,6 +22,7 @@ HELMHOLTZ_3D, LAPLACE_3D = 0, 1
 SLP, DLP = 1, 2
 C64, C128 = 0, 1
 REGULAR_FP32, REGULAR_FP64 = 0, 1
+GEMM_FP32, GEMM_TF32, GEMM_BF16X9 = 0, 1, 2
 HOST, DEVICE = 0, 1
 NOALLOC_PARTIAL_ELEMS = 1 << 20  # NIHU_GB_NOALLOC_PARTIAL_ELEMS
 
@@ -52,6 +53,8 @@ SIGNATURES = {
     "nihu_gb_matvec": (_i, [_vp, _i, _vp, _i64, _i64, _i64, _vp, _vp, _d, _d, _d, _d, _i]),
     "nihu_gb_matvec_noalloc": (_i, [_i, _vp, _i64, _i64, _i64, _vp, _vp, _d, _d, _d, _d, _vp]),
     "nihu_gb_gmres": (_i, [_vp, _i, _vp, _i64, _i64, _vp, _vp, _i, _i, _d, _ip, _dp, _i]),
+    "nihu_gb_gemm": (_i, [_vp, _i, _vp, _i64, _i64, _i64, _vp, _i64, _i64, _vp, _i64, _d, _d, _d, _d, _i]),
+    "nihu_gb_solve_multi": (_i, [_vp, _vp, _i64, _i64, _vp, _vp, _i64, _i, _i, _i, _d, _d, _ip, _ip, _dp, _i]),
     "nihu_gb_lu_solve": (_i, [_vp, _vp, _i64, _i64, _vp, _vp, _i]),
     "nihu_gb_solve_cbie": (_i, [_vp, _vp, _i, _d, _i, _i, _vp, _vp, _i, _i, _i, _d, _ip, _dp]),
 }

@@ -381,6 +381,38 @@ def lu_solve(A: np.ndarray, b: np.ndarray, ctx: Context | None = None) -> np.nda
     return x
 
 
+def gemm(A: np.ndarray, X: np.ndarray, mode: int = C.GEMM_FP32, ctx: Context | None = None) -> np.ndarray:
+    """Y = A X on the GPU for many right-hand sides (A complex64, X complex128 n x nrhs)."""
+    ctx = ctx or default_context()
+    A = np.asfortranarray(A, dtype=np.complex64)
+    X = np.asfortranarray(X, dtype=np.complex128)
+    m, n = A.shape
+    nrhs = X.shape[1]
+    Y = np.zeros((m, nrhs), np.complex128, order="F")
+    ctx.check(C.lib().nihu_gb_gemm(ctx.handle, mode, A.ctypes.data, m, n, max(m, 1), X.ctypes.data, max(n, 1), nrhs,
+                                   Y.ctypes.data, max(m, 1), 1.0, 0.0, 0.0, 0.0, C.HOST))
+    return Y
+
+
+def solve_multi(A: np.ndarray, B: np.ndarray, inner_mode: int = C.GEMM_TF32, restart: int = 30, max_outer: int = 20,
+                tol: float = 1e-6, inner_tol: float = 1e-3, ctx: Context | None = None):
+    """A X = B for many right-hand sides by mixed-precision iterative refinement
+    (tensor-core GMRES inner solves, FP64-accumulated residuals).
+    Returns (X, outer iterations, inner iterations, relative residual per column)."""
+    ctx = ctx or default_context()
+    A = np.asfortranarray(A, dtype=np.complex64)
+    B = np.asfortranarray(B, dtype=np.complex128)
+    n, nrhs = B.shape
+    X = np.zeros_like(B, order="F")
+    oi, ii = ctypes.c_int(0), ctypes.c_int(0)
+    res = np.zeros(nrhs)
+    ctx.check(C.lib().nihu_gb_solve_multi(ctx.handle, A.ctypes.data, n, max(n, 1), B.ctypes.data, X.ctypes.data, nrhs,
+                                          inner_mode, restart, max_outer, tol, inner_tol, ctypes.byref(oi),
+                                          ctypes.byref(ii), res.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
+                                          C.HOST))
+    return X, oi.value, ii.value, res
+
+
 def solve_cbie(mesh: Mesh, k: float, q, family: int = C.HELMHOLTZ_3D, dtype: int = C.C64, solver: str = "gmres",
                precision: str = "fp32", restart: int = 50, max_iters: int = 1000, tol: float = 1e-6,
                ctx: Context | None = None):

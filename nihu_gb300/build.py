@@ -16,7 +16,7 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libnihu_gb300.so")
 SOURCES = ["mesh.cu", "classify.cu", "assemble_regular.cu", "assemble_singular.cu", "linalg.cu", "capi.cu",
-           "noalloc.cu"]
+           "noalloc.cu", "multi.cu"]
 HEADERS = ["common.cuh", "geom.cuh", "classify.cuh", "kernels.h", "linalg.h", "quad_rules.h"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2"]
@@ -56,7 +56,9 @@ def build(force: bool = False, verbose: bool = False) -> str:
     objs = [os.path.join(BUILD, s.replace(".cu", ".o")) for s in SOURCES]
     if force or jobs or _stale(LIB, objs):
         tmp = LIB + ".tmp%d" % os.getpid()
-        cmd = [nvcc(), *ARCH, "-shared", "-cudart", "static", *objs, "-o", tmp]
+        cuda_lib = os.path.join(os.path.dirname(os.path.dirname(nvcc())), "lib64")
+        cmd = [nvcc(), *ARCH, "-shared", "-cudart", "static", *objs, "-o", tmp, "-lcublas",
+               "-Xlinker", "-rpath", "-Xlinker", cuda_lib]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode:
             sys.stderr.write(r.stdout + r.stderr)

@@ -10,6 +10,8 @@
 #include <utility>
 #include <vector>
 
+#include <cublas_v2.h>
+
 #include "../../include/nihu_gb300.h"
 #include "kernels.h"
 #include "linalg.h"
@@ -41,6 +43,7 @@ struct nihu_gb_ctx {
     std::map<std::string, std::pair<double, int64_t>> phases;
     std::vector<std::pair<std::string, std::pair<cudaEvent_t, cudaEvent_t>>> pending;
     std::vector<cudaEvent_t> event_pool;
+    cublasHandle_t cublas = nullptr;  // created on first multi-RHS product
 };
 
 struct nihu_gb_mesh {
@@ -338,6 +341,7 @@ void nihu_gb_ctx_destroy(nihu_gb_ctx *ctx)
     for (auto &kv : ctx->scratch) dfree(ctx, kv.second.first);
     dfree(ctx, ctx->d_flag);
     if (ctx->h_small) cudaFreeHost(ctx->h_small);
+    if (ctx->cublas) cublasDestroy(ctx->cublas);
     collect_phases(ctx);
     for (cudaEvent_t e : ctx->event_pool) cudaEventDestroy(e);
     if (ctx->aux_stream) cudaStreamSynchronize(ctx->aux_stream);
@@ -1016,3 +1020,289 @@ nihu_gb_status nihu_gb_solve_cbie(nihu_gb_ctx *ctx, const nihu_gb_mesh *mesh, in
 }
 
 }  // extern "C"
+
+// ------------------------------------------------------- multi-RHS
+
+namespace {
+
+nihu_gb_status ensure_cublas(nihu_gb_ctx *ctx)
+{
+    if (ctx->cublas) return NIHU_GB_OK;
+    if (cublasCreate(&ctx->cublas) != CUBLAS_STATUS_SUCCESS) {
+        ctx->cublas = nullptr;
+        return fail(ctx, NIHU_GB_ERR_CUDA, "cublasCreate failed");
+    }
+    return NIHU_GB_OK;
+}
+
+// Y = alpha A X + beta Y on the device (A complex64)
+nihu_gb_status gemm_device(nihu_gb_ctx *ctx, int mode, const void *A, int64_t m, int64_t n, int64_t lda,
+                           const double2 *X, int64_t ldx, int64_t nrhs, double2 *Y, int64_t ldy, double are, double aim,
+                           double bre, double bim)
+{
+    nihu_gb_status st;
+    if ((st = ensure_cublas(ctx))) return st;
+    void *xp, *z;
+    if ((st = scratch(ctx, "gemm_xp", sizeof(float) * 2 * std::max<int64_t>(n, 1) * nrhs, &xp))) return st;
+    if ((st = scratch(ctx, "gemm_z", sizeof(float) * 4 * m * nrhs, &z))) return st;
+    int cs = 0;
+    cudaError_t e;
+    {
+        Phase ph(ctx, mode == NIHU_GB_GEMM_TF32 ? "gemm_tf32" : (mode == NIHU_GB_GEMM_BF16X9 ? "gemm_bf16x9" : "gemm_fp32"));
+        e = launch_gemm_c64(ctx->cublas, mode, A, m, n, lda, X, ldx, (int)nrhs, Y, ldy, are, aim, bre, bim, (float *)xp,
+                            (float *)z, ctx->stream, &cs);
+    }
+    ctx->launches += 3;
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "gemm");
+    if (cs) return fail(ctx, NIHU_GB_ERR_CUDA, "cublasGemmEx failed with status " + std::to_string(cs));
+    return NIHU_GB_OK;
+}
+
+}  // namespace
+
+extern "C" nihu_gb_status nihu_gb_gemm(nihu_gb_ctx *ctx, int mode, const void *A, int64_t m, int64_t n, int64_t lda,
+                                       const void *X, int64_t ldx, int64_t nrhs, void *Y, int64_t ldy, double alpha_re,
+                                       double alpha_im, double beta_re, double beta_im, int where)
+{
+    if (!ctx) return NIHU_GB_ERR_INVALID_ARGUMENT;
+    if (mode < 0 || mode > 2 || !valid_where(where) || m < 0 || n < 0 || nrhs < 0 || lda < std::max<int64_t>(m, 1) ||
+        ldx < std::max<int64_t>(n, 1) || ldy < std::max<int64_t>(m, 1) || (m && nrhs && (!A || !Y)) ||
+        (n && nrhs && !X) || m > 0x3fffffff || n > 0x7fffffff || nrhs > 0x3fffffff)
+        return fail(ctx, NIHU_GB_ERR_INVALID_ARGUMENT, "nihu_gb_gemm: bad argument");
+    if (m == 0 || nrhs == 0) return NIHU_GB_OK;
+    cudaSetDevice(ctx->device);
+    nihu_gb_status st;
+    const void *dA = A;
+    const double2 *dX = (const double2 *)X;
+    double2 *dY = (double2 *)Y;
+    if (where == NIHU_GB_HOST) {
+        void *pa, *px, *py;
+        if ((st = scratch(ctx, "mv_A", 8 * m * n, &pa))) return st;
+        if ((st = scratch(ctx, "gm_X", 16 * std::max<int64_t>(n, 1) * nrhs, &px))) return st;
+        if ((st = scratch(ctx, "gm_Y", 16 * m * nrhs, &py))) return st;
+        CK(cudaMemcpy2DAsync(pa, 8 * m, A, 8 * lda, 8 * m, n, cudaMemcpyHostToDevice, ctx->stream));
+        if (n) CK(cudaMemcpy2DAsync(px, 16 * n, X, 16 * ldx, 16 * n, nrhs, cudaMemcpyHostToDevice, ctx->stream));
+        CK(cudaMemcpy2DAsync(py, 16 * m, Y, 16 * ldy, 16 * m, nrhs, cudaMemcpyHostToDevice, ctx->stream));
+        dA = pa;
+        dX = (const double2 *)px;
+        dY = (double2 *)py;
+        lda = m;
+        ldx = n;
+        ldy = m;
+    }
+    if ((st = gemm_device(ctx, mode, dA, m, n, lda, dX, ldx, nrhs, dY, ldy, alpha_re, alpha_im, beta_re, beta_im)))
+        return st;
+    if (where == NIHU_GB_HOST)
+        CK(cudaMemcpy2DAsync(Y, 16 * ldy, dY, 16 * m, 16 * m, nrhs, cudaMemcpyDeviceToHost, ctx->stream));
+    return sync(ctx);
+}
+
+namespace {
+
+// one GMRES(restart) cycle on all right-hand sides in lockstep: D = approx A^{-1} R
+// for the columns with active[r]; returns the iterations done
+nihu_gb_status gmres_cycle_multi(nihu_gb_ctx *ctx, int mode, const void *A, int64_t n, int64_t lda, const double2 *R,
+                                 double2 *D, int nrhs, const std::vector<char> &active, int restart, double inner_tol,
+                                 int *iters)
+{
+    typedef std::complex<double> C;
+    nihu_gb_status st;
+    const int m = restart;
+    void *pV, *pW, *ppart, *ph, *psc;
+    const int blocks = bdot_blocks(n);
+    if ((st = scratch(ctx, "mr_V", 16 * (size_t)n * nrhs * (m + 1), &pV))) return st;
+    if ((st = scratch(ctx, "mr_W", 16 * (size_t)n * nrhs, &pW))) return st;
+    if ((st = scratch(ctx, "mr_part", 16 * (size_t)(m + 1) * nrhs * blocks, &ppart))) return st;
+    if ((st = scratch(ctx, "mr_h", 16 * (size_t)(m + 1) * nrhs, &ph))) return st;
+    if ((st = scratch(ctx, "mr_sc", 8 * (size_t)nrhs, &psc))) return st;
+    double2 *V = (double2 *)pV, *W = (double2 *)pW, *part = (double2 *)ppart, *hd = (double2 *)ph;
+    double *scd = (double *)psc;
+    const size_t blk = (size_t)n * nrhs;
+    std::vector<double2> hh((size_t)(m + 1) * nrhs);
+    std::vector<double> sc(nrhs);
+
+    auto norms = [&](const double2 *X, std::vector<double> &out) -> nihu_gb_status {
+        CK(launch_bdot(X, 1, X, n, nrhs, part, hd, ctx->stream));
+        ctx->launches += 2;
+        CK(cudaMemcpyAsync(hh.data(), hd, 16 * (size_t)nrhs, cudaMemcpyDeviceToHost, ctx->stream));
+        if ((st = sync(ctx))) return st;
+        for (int r = 0; r < nrhs; ++r) out[r] = std::sqrt(std::max(hh[r].x, 0.0));
+        return NIHU_GB_OK;
+    };
+
+    std::vector<double> beta(nrhs);
+    if ((st = norms(R, beta))) return st;
+    std::vector<char> act(nrhs);
+    for (int r = 0; r < nrhs; ++r) {
+        act[r] = active[r] && beta[r] > 0.0;
+        sc[r] = act[r] ? 1.0 / beta[r] : 0.0;
+    }
+    CK(cudaMemcpyAsync(scd, sc.data(), 8 * (size_t)nrhs, cudaMemcpyHostToDevice, ctx->stream));
+    CK(launch_bscale(R, V, n, nrhs, scd, ctx->stream));
+    ctx->launches += 1;
+    std::vector<std::vector<C>> H(nrhs, std::vector<C>((size_t)(m + 1) * m, C(0)));
+    std::vector<std::vector<C>> g(nrhs, std::vector<C>(m + 1, C(0))), cs(nrhs, std::vector<C>(m)), sn(nrhs, std::vector<C>(m));
+    std::vector<int> kdone(nrhs, 0);
+    std::vector<char> run = act;
+    for (int r = 0; r < nrhs; ++r) g[r][0] = beta[r];
+    int k = 0;
+    for (; k < m; ++k) {
+        bool any = false;
+        for (int r = 0; r < nrhs; ++r) any = any || run[r];
+        if (!any) break;
+        // W = A V_k: one tensor-core GEMM over all right-hand sides
+        if ((st = gemm_device(ctx, mode, A, n, n, lda, V + (size_t)k * blk, n, nrhs, W, n, 1.0, 0.0, 0.0, 0.0)))
+            return st;
+        std::vector<std::vector<C>> h(nrhs, std::vector<C>(k + 2, C(0)));
+        for (int pass = 0; pass < 2; ++pass) {  // CGS2
+            CK(launch_bdot(V, k + 1, W, n, nrhs, part, hd, ctx->stream));
+            CK(cudaMemcpyAsync(hh.data(), hd, 16 * (size_t)(k + 1) * nrhs, cudaMemcpyDeviceToHost, ctx->stream));
+            if ((st = sync(ctx))) return st;
+            for (int v = 0; v <= k; ++v)
+                for (int r = 0; r < nrhs; ++r) h[r][v] += C(hh[(size_t)v * nrhs + r].x, hh[(size_t)v * nrhs + r].y);
+            CK(launch_bcombo(V, n, nrhs, k + 1, hd, -1.0, W, ctx->stream));
+            ctx->launches += 3;
+        }
+        std::vector<double> hn(nrhs);
+        if ((st = norms(W, hn))) return st;
+        for (int r = 0; r < nrhs; ++r) sc[r] = (run[r] && hn[r] > 0.0) ? 1.0 / hn[r] : 0.0;
+        CK(cudaMemcpyAsync(scd, sc.data(), 8 * (size_t)nrhs, cudaMemcpyHostToDevice, ctx->stream));
+        CK(launch_bscale(W, V + (size_t)(k + 1) * blk, n, nrhs, scd, ctx->stream));
+        ctx->launches += 1;
+        for (int r = 0; r < nrhs; ++r) {
+            if (!run[r]) continue;
+            std::vector<C> &hr = h[r];
+            hr[k + 1] = hn[r];
+            for (int i = 0; i < k; ++i) {
+                C a0 = hr[i], a1 = hr[i + 1];
+                hr[i] = std::conj(cs[r][i]) * a0 + std::conj(sn[r][i]) * a1;
+                hr[i + 1] = -sn[r][i] * a0 + cs[r][i] * a1;
+            }
+            double den = std::sqrt(std::norm(hr[k]) + std::norm(hr[k + 1]));
+            if (den == 0.0) { cs[r][k] = 1.0; sn[r][k] = 0.0; }
+            else { cs[r][k] = hr[k] / den; sn[r][k] = hr[k + 1] / den; }
+            C a0 = hr[k], a1 = hr[k + 1];
+            hr[k] = std::conj(cs[r][k]) * a0 + std::conj(sn[r][k]) * a1;
+            C g0 = g[r][k], g1 = g[r][k + 1];
+            g[r][k] = std::conj(cs[r][k]) * g0 + std::conj(sn[r][k]) * g1;
+            g[r][k + 1] = -sn[r][k] * g0 + cs[r][k] * g1;
+            for (int i = 0; i <= k; ++i) H[r][(size_t)i * m + k] = hr[i];
+            kdone[r] = k + 1;
+            if (std::abs(g[r][k + 1]) <= inner_tol * beta[r] || hn[r] == 0.0) run[r] = 0;
+        }
+    }
+    *iters = k;
+    // y = H^{-1} g per column, D += V y
+    std::vector<double2> yd((size_t)m * nrhs, make_double2(0.0, 0.0));
+    int kmax = 0;
+    for (int r = 0; r < nrhs; ++r) {
+        int kd = kdone[r];
+        kmax = std::max(kmax, kd);
+        std::vector<C> y(kd);
+        for (int i = kd - 1; i >= 0; --i) {
+            C sum = g[r][i];
+            for (int j = i + 1; j < kd; ++j) sum -= H[r][(size_t)i * m + j] * y[j];
+            y[i] = sum / H[r][(size_t)i * m + i];
+        }
+        for (int i = 0; i < kd; ++i) yd[(size_t)i * nrhs + r] = make_double2(y[i].real(), y[i].imag());
+    }
+    if (kmax > 0) {
+        CK(cudaMemcpyAsync(hd, yd.data(), 16 * (size_t)kmax * nrhs, cudaMemcpyHostToDevice, ctx->stream));
+        CK(launch_bcombo(V, n, nrhs, kmax, hd, 1.0, D, ctx->stream));
+        ctx->launches += 1;
+    }
+    return sync(ctx);
+}
+
+}  // namespace
+
+extern "C" nihu_gb_status nihu_gb_solve_multi(nihu_gb_ctx *ctx, const void *A, int64_t n, int64_t lda, const void *B,
+                                              void *X, int64_t nrhs, int inner_mode, int restart, int max_outer,
+                                              double tol, double inner_tol, int *outer_iters, int *inner_iters,
+                                              double *rel_residuals, int where)
+{
+    if (!ctx) return NIHU_GB_ERR_INVALID_ARGUMENT;
+    if (inner_mode < 0 || inner_mode > 2 || !valid_where(where) || n < 0 || nrhs < 0 || lda < std::max<int64_t>(n, 1) ||
+        restart < 1 || restart > 200 || max_outer < 1 || !(tol > 0.0) || !(inner_tol > 0.0) ||
+        (n && nrhs && (!A || !B || !X)) || n > 0x3fffffff || nrhs > 4096)
+        return fail(ctx, NIHU_GB_ERR_INVALID_ARGUMENT, "nihu_gb_solve_multi: bad argument");
+    if (n == 0 || nrhs == 0) return NIHU_GB_OK;
+    cudaSetDevice(ctx->device);
+    restart = (int)std::min<int64_t>(restart, n);
+    nihu_gb_status st;
+    const void *dA = A;
+    double2 *dB, *dX, *dR, *dD;
+    void *pb, *px, *pr, *pd, *pp, *ph;
+    const size_t blk = 16 * (size_t)n * nrhs;
+    if ((st = scratch(ctx, "ms_B", blk, &pb))) return st;
+    if ((st = scratch(ctx, "ms_X", blk, &px))) return st;
+    if ((st = scratch(ctx, "ms_R", blk, &pr))) return st;
+    if ((st = scratch(ctx, "ms_D", blk, &pd))) return st;
+    dB = (double2 *)pb;
+    dX = (double2 *)px;
+    dR = (double2 *)pr;
+    dD = (double2 *)pd;
+    if (where == NIHU_GB_HOST) {
+        void *pa;
+        if ((st = scratch(ctx, "mv_A", 8 * n * n, &pa))) return st;
+        CK(cudaMemcpy2DAsync(pa, 8 * n, A, 8 * lda, 8 * n, n, cudaMemcpyHostToDevice, ctx->stream));
+        dA = pa;
+        lda = n;
+        CK(cudaMemcpyAsync(dB, B, blk, cudaMemcpyHostToDevice, ctx->stream));
+    } else {
+        CK(cudaMemcpyAsync(dB, B, blk, cudaMemcpyDeviceToDevice, ctx->stream));
+    }
+    const int blocks = bdot_blocks(n);
+    if ((st = scratch(ctx, "mr_part", 16 * (size_t)(restart + 1) * nrhs * blocks, &pp))) return st;
+    if ((st = scratch(ctx, "mr_h", 16 * (size_t)(restart + 1) * nrhs, &ph))) return st;
+    std::vector<double2> hh((size_t)nrhs);
+    auto norms = [&](const double2 *Xv, std::vector<double> &out) -> nihu_gb_status {
+        CK(launch_bdot(Xv, 1, Xv, n, (int)nrhs, (double2 *)pp, (double2 *)ph, ctx->stream));
+        ctx->launches += 2;
+        CK(cudaMemcpyAsync(hh.data(), ph, 16 * (size_t)nrhs, cudaMemcpyDeviceToHost, ctx->stream));
+        if ((st = sync(ctx))) return st;
+        for (int64_t r = 0; r < nrhs; ++r) out[r] = std::sqrt(std::max(hh[r].x, 0.0));
+        return NIHU_GB_OK;
+    };
+    std::vector<double> bn(nrhs), rn(nrhs), rel(nrhs);
+    if ((st = norms(dB, bn))) return st;
+    CK(cudaMemsetAsync(dX, 0, blk, ctx->stream));
+    CK(cudaMemcpyAsync(dR, dB, blk, cudaMemcpyDeviceToDevice, ctx->stream));
+    int outer = 0, inner_total = 0;
+    bool converged = false;
+    while (true) {
+        if ((st = norms(dR, rn))) return st;
+        double worst = 0.0;
+        std::vector<char> active(nrhs);
+        for (int64_t r = 0; r < nrhs; ++r) {
+            rel[r] = bn[r] > 0.0 ? rn[r] / bn[r] : 0.0;
+            active[r] = rel[r] > tol;
+            worst = std::max(worst, rel[r]);
+        }
+        if (worst <= tol) { converged = true; break; }
+        if (outer >= max_outer) break;
+        ++outer;
+        CK(cudaMemsetAsync(dD, 0, blk, ctx->stream));
+        int it = 0;
+        if ((st = gmres_cycle_multi(ctx, inner_mode, dA, n, lda, dR, dD, (int)nrhs, active, restart, inner_tol, &it)))
+            return st;
+        inner_total += it;
+        // X += D (FP64); R = B - A X with FP32-accurate split-BF16 products, FP64 accumulation
+        std::vector<double2> ones((size_t)nrhs, make_double2(1.0, 0.0));
+        CK(cudaMemcpyAsync(ph, ones.data(), 16 * (size_t)nrhs, cudaMemcpyHostToDevice, ctx->stream));
+        CK(launch_bcombo(dD, n, (int)nrhs, 1, (const double2 *)ph, 1.0, dX, ctx->stream));
+        ctx->launches += 1;
+        CK(cudaMemcpyAsync(dR, dB, blk, cudaMemcpyDeviceToDevice, ctx->stream));
+        if ((st = gemm_device(ctx, NIHU_GB_GEMM_BF16X9, dA, n, n, lda, dX, n, nrhs, dR, n, -1.0, 0.0, 1.0, 0.0)))
+            return st;
+    }
+    if (where == NIHU_GB_HOST) CK(cudaMemcpyAsync(X, dX, blk, cudaMemcpyDeviceToHost, ctx->stream));
+    else CK(cudaMemcpyAsync(X, dX, blk, cudaMemcpyDeviceToDevice, ctx->stream));
+    if ((st = sync(ctx))) return st;
+    if (outer_iters) *outer_iters = outer;
+    if (inner_iters) *inner_iters = inner_total;
+    if (rel_residuals)
+        for (int64_t r = 0; r < nrhs; ++r) rel_residuals[r] = rel[r];
+    if (!converged) return fail(ctx, NIHU_GB_ERR_NOT_CONVERGED, "multi-RHS refinement did not reach the tolerance");
+    return NIHU_GB_OK;
+}

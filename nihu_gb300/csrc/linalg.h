@@ -24,4 +24,15 @@ cudaError_t launch_lu_factor(double2 *A, int64_t n, int64_t lda, int *piv, int *
 cudaError_t launch_lu_solve(const double2 *A, int64_t n, int64_t lda, const int *piv, const double2 *b, double2 *x,
                             cudaStream_t s);
 
+// multi.cu: complex GEMM on a real view of A (cuBLAS), batched vector kernels
+cudaError_t launch_gemm_c64(void *cublas, int mode, const void *A, int64_t m, int64_t n, int64_t lda, const double2 *X,
+                            int64_t ldx, int nrhs, double2 *Y, int64_t ldy, double are, double aim, double bre,
+                            double bim, float *Xp, float *Z, cudaStream_t s, int *cublas_status);
+int bdot_blocks(int64_t n);
+cudaError_t launch_bdot(const double2 *V, int nv, const double2 *W, int64_t n, int nrhs, double2 *part, double2 *out,
+                        cudaStream_t s);
+cudaError_t launch_bcombo(const double2 *V, int64_t n, int nrhs, int nv, const double2 *h, double sign, double2 *W,
+                          cudaStream_t s);
+cudaError_t launch_bscale(const double2 *src, double2 *dst, int64_t n, int nrhs, const double *sc, cudaStream_t s);
+
 }  // namespace nihu

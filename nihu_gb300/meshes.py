@@ -211,3 +211,21 @@ def read_off(path, tag=None):
         elems[e, 1:1 + k] = [int(t) for t in tokens[pos:pos + k]]
         pos += k
     return nodes, elems
+
+
+def plane_wave_neumann(nodes, elems, k: float, directions):
+    """Neumann data of the field scattered by a rigid body from plane waves
+    p_inc = exp(-i k d.x) (e^{-ikr} convention): q = -dp_inc/dn = i k (d.n) p_inc,
+    sampled at the element centres; returns (n_elems, n_directions) complex128."""
+    cen, nrm = centroids_and_normals(nodes, elems)
+    d = np.asarray(directions, dtype=np.float64)
+    d = d / np.linalg.norm(d, axis=1, keepdims=True)
+    p_inc = np.exp(-1j * k * (cen @ d.T))
+    return np.asfortranarray(1j * k * (nrm @ d.T) * p_inc)
+
+
+def sphere_directions(count: int, seed: int = 0):
+    """``count`` unit vectors uniform on the sphere (seeded)."""
+    rng = np.random.default_rng(seed)
+    v = rng.standard_normal((count, 3))
+    return v / np.linalg.norm(v, axis=1, keepdims=True)

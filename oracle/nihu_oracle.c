@@ -751,8 +751,9 @@ static int entry(const elem_t *te, const elem_t *re, int same_id, int fam, int o
 }
 
 /*
- * Assemble rows [row_begin, row_end) of the operator (fam, op) between a test
- * and a trial mesh into out[(i - row_begin) + j*ld] (column-major, complex128
+ * Assemble the block rows [row_begin, row_end) x columns [col_begin, col_end)
+ * of the operator (fam, op) between a test and a trial mesh into
+ * out[(i - row_begin) + (j - col_begin)*ld] (column-major, complex128
  * as interleaved doubles).  out = alpha*op if accumulate == 0, else out +=
  * alpha*op (nihu/core/assembly.hpp:69-76 with block += semantics).
  * same_mesh enables the self terms (nihu/core/integral_transform.hpp:156).
@@ -760,9 +761,10 @@ static int entry(const elem_t *te, const elem_t *re, int same_id, int fam, int o
 int oracle_assemble(const double *tnodes, int tn_nodes, const int *telems, int tn_elems, int tcols,
                     const double *rnodes, int rn_nodes, const int *relems, int rn_elems, int rcols,
                     int same_mesh, int fam, int op, double k, double alpha_re, double alpha_im,
-                    int row_begin, int row_end, double *out, long ld, int accumulate)
+                    int row_begin, int row_end, int col_begin, int col_end, double *out, long ld, int accumulate)
 {
     if (row_begin < 0 || row_end > tn_elems || row_begin > row_end) { snprintf(g_err, sizeof g_err, "bad row range"); return 0; }
+    if (col_begin < 0 || col_end > rn_elems || col_begin > col_end) { snprintf(g_err, sizeof g_err, "bad column range"); return 0; }
     cplx alpha = alpha_re + I * alpha_im;
     /* element geometry is built once per mesh, like the reference's mesh
      * construction (nihu/core/mesh.hpp:137-160) */
@@ -773,10 +775,10 @@ int oracle_assemble(const double *tnodes, int tn_nodes, const int *telems, int t
     for (int i = row_begin; i < row_end && ok; ++i) {
         elem_t te;
         if (!(ok = load_elem(tnodes, tn_nodes, telems, tcols, i, &te))) break;
-        for (int j = 0; j < rn_elems; ++j) {
+        for (int j = col_begin; j < col_end; ++j) {
             cplx v;
             if (!(ok = entry(&te, &trial[j], same_mesh && i == j, fam, op, k, &v))) break;
-            cplx *dst = (cplx *)out + (long)(i - row_begin) + (long)j * ld;
+            cplx *dst = (cplx *)out + (long)(i - row_begin) + (long)(j - col_begin) * ld;
             if (accumulate) *dst += alpha * v; else *dst = alpha * v;
         }
     }

@@ -43,7 +43,7 @@ def lib():
             c_int, c_double, c_long = ctypes.c_int, ctypes.c_double, ctypes.c_long
             L.oracle_assemble.argtypes = [dp, c_int, ip, c_int, c_int, dp, c_int, ip, c_int, c_int,
                                           c_int, c_int, c_int, c_double, c_double, c_double,
-                                          c_int, c_int, dp, c_long, c_int]
+                                          c_int, c_int, c_int, c_int, dp, c_long, c_int]
             L.oracle_assemble.restype = c_int
             L.oracle_classify.argtypes = [dp, c_int, ip, c_int, c_int, dp, c_int, ip, c_int, c_int,
                                           c_int, c_int, c_int, ip]
@@ -66,15 +66,16 @@ def _mesh_args(nodes, elems):
     return nodes, elems, [_ptr(nodes, ctypes.c_double), len(nodes), _ptr(elems, ctypes.c_int), len(elems), elems.shape[1]]
 
 
-def assemble(test_mesh, trial_mesh, family, op, k, same_mesh=None, rows=None, alpha=1.0, threads=1):
-    """Dense operator block (rows x all trial elements) as complex128, C-contiguous
-    in column-major order (Fortran array)."""
+def assemble(test_mesh, trial_mesh, family, op, k, same_mesh=None, rows=None, alpha=1.0, threads=1, cols=None):
+    """Dense operator block (rows x cols, default all) as complex128 in
+    column-major order (Fortran array)."""
     tn, te, targs = _mesh_args(*test_mesh)
     rn, re_, rargs = _mesh_args(*trial_mesh)
     if same_mesh is None:
         same_mesh = test_mesh is trial_mesh
     r0, r1 = (0, len(te)) if rows is None else rows
-    m, n = r1 - r0, len(re_)
+    c0, c1 = (0, len(re_)) if cols is None else cols
+    m, n = r1 - r0, c1 - c0
     out = np.zeros((m, n), dtype=np.complex128, order="F")
     alpha = complex(alpha)
     L = lib()
@@ -85,7 +86,7 @@ def assemble(test_mesh, trial_mesh, family, op, k, same_mesh=None, rows=None, al
         buf = np.zeros((b - a, n), dtype=np.complex128, order="F")
         ptr = ctypes.cast(buf.ctypes.data, ctypes.POINTER(ctypes.c_double))
         ok = L.oracle_assemble(*targs, *rargs, int(same_mesh), family, op, float(k), alpha.real, alpha.imag,
-                               a, b, ptr, b - a, 0)
+                               a, b, c0, c1, ptr, b - a, 0)
         if not ok:
             errors.append(RuntimeError(L.oracle_last_error().decode()))
             return

@@ -1,0 +1,62 @@
+"""Multi-right-hand-side GEMM (FP32 / TF32 / split BF16x9) and the
+mixed-precision refinement solver, against numpy and the FP64 oracle."""
+import numpy as np
+import pytest
+
+import nihu_gb300 as g
+from nihu_gb300 import meshes
+
+pytestmark = pytest.mark.gpu
+
+
+def rand_c(rng, *shape):
+    return rng.standard_normal(shape) + 1j * rng.standard_normal(shape)
+
+
+@pytest.mark.parametrize("mode,tol", [(g.GEMM_FP32, 1e-5), (g.GEMM_BF16X9, 1e-5), (g.GEMM_TF32, 3e-3)])
+@pytest.mark.parametrize("m,n,nrhs", [(1000, 700, 64), (333, 517, 5)])
+def test_gemm_modes(gpu_ctx, mode, tol, m, n, nrhs):
+    rng = np.random.default_rng(m + n + nrhs)
+    A = rand_c(rng, m, n).astype(np.complex64)
+    X = rand_c(rng, n, nrhs)
+    Y = g.gemm(A, X, mode=mode, ctx=gpu_ctx)
+    ref = A.astype(np.complex128) @ X
+    assert np.abs(Y - ref).max() / np.abs(ref).max() < tol
+
+
+@pytest.mark.parametrize("inner_mode", [g.GEMM_TF32, g.GEMM_BF16X9])
+def test_solve_multi_random(gpu_ctx, inner_mode):
+    rng = np.random.default_rng(1)
+    n, nrhs = 900, 12
+    A = (np.eye(n) + 0.4 * rand_c(rng, n, n) / np.sqrt(n)).astype(np.complex64)
+    B = rand_c(rng, n, nrhs)
+    X, outer, inner, res = g.solve_multi(A, B, inner_mode=inner_mode, tol=1e-8, ctx=gpu_ctx)
+    ref = np.linalg.solve(A.astype(np.complex128), B)
+    assert res.max() <= 1e-8
+    assert np.linalg.norm(X - ref, axis=0).max() / np.linalg.norm(ref, axis=0).min() < 1e-6
+    assert outer >= 1 and inner >= 1
+
+
+def test_solve_multi_cylinder_plane_waves(gpu_ctx, oracle):
+    """Rigid closed cylinder, 16 plane waves: (M - I/2) p = L q per direction;
+    surface pressure within 1e-4 of the FP64 oracle solution."""
+    mesh = meshes.cylinder(16, 8, 2, radius=1.0, length=3.0)
+    n = len(mesh[1])
+    k = 2.0
+    dirs = meshes.sphere_directions(16, seed=5)
+    Q = meshes.plane_wave_neumann(*mesh, k, dirs)
+    L = oracle.assemble(mesh, mesh, oracle.HELMHOLTZ, oracle.SLP, k, threads=8)
+    M = oracle.assemble(mesh, mesh, oracle.HELMHOLTZ, oracle.DLP, k, threads=8) - 0.5 * np.eye(n)
+    P_ref = np.linalg.solve(M, L @ Q)
+    m = g.create_mesh(*mesh)
+    sp = g.constant_view(m)
+    Lg = np.zeros((n, n), np.complex64, order="F")
+    Mg = np.zeros((n, n), np.complex64, order="F")
+    Lg << g.dirac(sp) * g.create_integral_operator(g.helmholtz_3d_SLP_kernel(k))[sp]
+    Mg << g.dirac(sp) * g.create_integral_operator(g.helmholtz_3d_DLP_kernel(k))[sp]
+    Mg << g.dirac(sp) * (-.5 * g.identity_integral_operator())[sp]
+    Bg = g.gemm(Lg, Q, mode=g.GEMM_BF16X9, ctx=gpu_ctx)
+    X, outer, inner, res = g.solve_multi(Mg, Bg, inner_mode=g.GEMM_TF32, tol=1e-6, ctx=gpu_ctx)
+    assert res.max() <= 1e-6
+    err = np.abs(X - P_ref).max(axis=0) / np.abs(P_ref).max(axis=0)
+    assert err.max() < 1e-4, err
