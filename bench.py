@@ -463,14 +463,25 @@ def run_multirhs(args):
     ctx.check(L.nihu_gb_add_identity(ctx.handle, dm.handle, -0.5, 0.0, C.C64, pd, n, C.DEVICE))
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    ctx.check(L.nihu_gb_gemm(ctx.handle, C.GEMM_BF16X9, ps, n, n, n, pq, n, nrhs, pb, n, 1.0, 0.0, 0.0, 0.0, C.DEVICE))
+    ctx.check(L.nihu_gb_gemm(ctx.handle, C.GEMM_FP32, ps, n, n, n, pq, n, nrhs, pb, n, 1.0, 0.0, 0.0, 0.0, C.DEVICE))
     torch.cuda.synchronize()
     rhs_ms = (time.perf_counter() - t0) * 1e3
+    # one product of each GEMM mode on the 40000 x 40000 matrix (64 right-hand sides)
+    mode_ms = {}
+    for mname, mode in (("fp32_cuda_cores", C.GEMM_FP32), ("tf32_tensor", C.GEMM_TF32), ("bf16x9_tensor", C.GEMM_BF16X9)):
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        ctx.check(L.nihu_gb_gemm(ctx.handle, mode, ps, n, n, n, pq, n, nrhs, px, n, 1.0, 0.0, 0.0, 0.0, C.DEVICE))
+        torch.cuda.synchronize()
+        ms_ = (time.perf_counter() - t1) * 1e3
+        mode_ms[mname] = {"ms": ms_, "hbm_gbs": 8.0 * n * n / (ms_ / 1e3) / 1e9,
+                          "complex_tflops": 8.0 * n * n * nrhs / (ms_ / 1e3) / 1e12}
     oi, ii = ctypes.c_int(0), ctypes.c_int(0)
     res = np.zeros(nrhs)
     t0 = time.perf_counter()
-    st = L.nihu_gb_solve_multi(ctx.handle, pd, n, n, pb, px, nrhs, C.GEMM_TF32, 30, 20, 1e-6, 1e-3, ctypes.byref(oi),
-                               ctypes.byref(ii), res.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), C.DEVICE)
+    st = L.nihu_gb_solve_multi(ctx.handle, pd, n, n, pb, px, nrhs, C.GEMM_TF32, C.GEMM_FP32, 30, 20, 1e-6, 1e-3,
+                               ctypes.byref(oi), ctypes.byref(ii), res.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
+                               C.DEVICE)
     torch.cuda.synchronize()
     solve_ms = (time.perf_counter() - t0) * 1e3
     prof_solve = ctx.profile()
@@ -496,13 +507,15 @@ def run_multirhs(args):
         if op == oracle.DLP:
             ref[np.arange(nc), np.arange(nc)] -= 0.5
         worst[name] = float(np.abs(got - ref).max() / np.abs(ref).max())
+        if os.environ.get("NIHU_GB_DUMP_COLUMNS"):
+            np.savez(os.environ["NIHU_GB_DUMP_COLUMNS"] + "_" + name + ".npz", got=got, ref=ref)
     out = {
         "metric": "multi-RHS solve (config 3)", "impl": "ours", "n_elements": n, "nrhs": nrhs, "k": k,
         "assembly_ms": asm_ms, "assembly_entries_per_s": 2.0 * n * n / (asm_ms / 1e3),
         "assembly_phases_ms": {kk: v[0] / steps for kk, v in prof_asm.items()},
         "near_pairs": int(counts[1]), "rhs_gemm_ms": rhs_ms, "solve_ms": solve_ms, "solve_status": int(st),
         "outer_iterations": oi.value, "inner_iterations": ii.value, "max_rel_residual": float(res.max()),
-        "gemm": gem, "solves_per_s": nrhs / ((rhs_ms + solve_ms) / 1e3),
+        "gemm": gem, "gemm_modes_one_product": mode_ms, "solves_per_s": nrhs / ((rhs_ms + solve_ms) / 1e3),
         "entry_error_vs_fp64_oracle_first_64_columns": worst,
         "note": "per-RHS accuracy is the FP64-accumulated residual |B - A X|/|B|; a dense FP64 oracle solve of "
                 "40000 unknowns is out of reach on the host, the oracle solution is compared on a smaller "

@@ -211,16 +211,17 @@ nihu_gb_status nihu_gb_gemm(nihu_gb_ctx *ctx, int mode, const void *A, int64_t m
 /* Solve A X = B for nrhs right-hand sides (A complex64 n x n, B and X
  * complex128 n x nrhs, ld = n) by mixed-precision iterative refinement:
  * each outer step runs one GMRES(restart) cycle on every right-hand side in
- * lockstep (the products A [v_1 .. v_nrhs] are one tensor-core GEMM of mode
- * inner_mode; FP64 Arnoldi), stops a column when its residual estimate falls
- * by inner_tol, adds the correction to X in FP64 and recomputes the residual
- * B - A X with BF16x9 (FP32-accurate) products accumulated in FP64.  Stops
- * when every column has |B - A X| <= tol |B|.  X starts from zero.
+ * lockstep (the products A [v_1 .. v_nrhs] are one GEMM of mode inner_mode,
+ * normally TF32 tensor cores; FP64 Arnoldi), stops a column when its residual
+ * estimate falls by inner_tol, adds the correction to X in FP64 and
+ * recomputes the residual B - A X with FP32-accurate products (residual_mode
+ * NIHU_GB_GEMM_FP32 or NIHU_GB_GEMM_BF16X9) combined in FP64.  Stops when
+ * every column has |B - A X| <= tol |B|.  X starts from zero.
  * rel_residuals (nrhs doubles) receives the final relative residuals. */
 nihu_gb_status nihu_gb_solve_multi(nihu_gb_ctx *ctx, const void *A, int64_t n, int64_t lda, const void *B, void *X,
-                                   int64_t nrhs, int inner_mode, int restart, int max_outer, double tol,
-                                   double inner_tol, int *outer_iters, int *inner_iters, double *rel_residuals,
-                                   int where);
+                                   int64_t nrhs, int inner_mode, int residual_mode, int restart, int max_outer,
+                                   double tol, double inner_tol, int *outer_iters, int *inner_iters,
+                                   double *rel_residuals, int where);
 
 /* Solve A x = b with restarted GMRES(restart) (nihu/fmm/GMRES.h:57-205
  * semantics: stop when |residual estimate| / |b - A x0| < tol).  A is n x n

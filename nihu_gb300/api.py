@@ -395,7 +395,8 @@ def gemm(A: np.ndarray, X: np.ndarray, mode: int = C.GEMM_FP32, ctx: Context | N
 
 
 def solve_multi(A: np.ndarray, B: np.ndarray, inner_mode: int = C.GEMM_TF32, restart: int = 30, max_outer: int = 20,
-                tol: float = 1e-6, inner_tol: float = 1e-3, ctx: Context | None = None):
+                tol: float = 1e-6, inner_tol: float = 1e-3, residual_mode: int = C.GEMM_FP32,
+                ctx: Context | None = None):
     """A X = B for many right-hand sides by mixed-precision iterative refinement
     (tensor-core GMRES inner solves, FP64-accumulated residuals).
     Returns (X, outer iterations, inner iterations, relative residual per column)."""
@@ -407,7 +408,8 @@ def solve_multi(A: np.ndarray, B: np.ndarray, inner_mode: int = C.GEMM_TF32, res
     oi, ii = ctypes.c_int(0), ctypes.c_int(0)
     res = np.zeros(nrhs)
     ctx.check(C.lib().nihu_gb_solve_multi(ctx.handle, A.ctypes.data, n, max(n, 1), B.ctypes.data, X.ctypes.data, nrhs,
-                                          inner_mode, restart, max_outer, tol, inner_tol, ctypes.byref(oi),
+                                          inner_mode, residual_mode, restart, max_outer, tol, inner_tol,
+                                          ctypes.byref(oi),
                                           ctypes.byref(ii), res.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
                                           C.HOST))
     return X, oi.value, ii.value, res

@@ -1217,12 +1217,12 @@ nihu_gb_status gmres_cycle_multi(nihu_gb_ctx *ctx, int mode, const void *A, int6
 }  // namespace
 
 extern "C" nihu_gb_status nihu_gb_solve_multi(nihu_gb_ctx *ctx, const void *A, int64_t n, int64_t lda, const void *B,
-                                              void *X, int64_t nrhs, int inner_mode, int restart, int max_outer,
-                                              double tol, double inner_tol, int *outer_iters, int *inner_iters,
-                                              double *rel_residuals, int where)
+                                              void *X, int64_t nrhs, int inner_mode, int residual_mode, int restart,
+                                              int max_outer, double tol, double inner_tol, int *outer_iters,
+                                              int *inner_iters, double *rel_residuals, int where)
 {
     if (!ctx) return NIHU_GB_ERR_INVALID_ARGUMENT;
-    if (inner_mode < 0 || inner_mode > 2 || !valid_where(where) || n < 0 || nrhs < 0 || lda < std::max<int64_t>(n, 1) ||
+    if (inner_mode < 0 || inner_mode > 2 || (residual_mode != NIHU_GB_GEMM_FP32 && residual_mode != NIHU_GB_GEMM_BF16X9) || !valid_where(where) || n < 0 || nrhs < 0 || lda < std::max<int64_t>(n, 1) ||
         restart < 1 || restart > 200 || max_outer < 1 || !(tol > 0.0) || !(inner_tol > 0.0) ||
         (n && nrhs && (!A || !B || !X)) || n > 0x3fffffff || nrhs > 4096)
         return fail(ctx, NIHU_GB_ERR_INVALID_ARGUMENT, "nihu_gb_solve_multi: bad argument");
@@ -1293,7 +1293,7 @@ extern "C" nihu_gb_status nihu_gb_solve_multi(nihu_gb_ctx *ctx, const void *A, i
         CK(launch_bcombo(dD, n, (int)nrhs, 1, (const double2 *)ph, 1.0, dX, ctx->stream));
         ctx->launches += 1;
         CK(cudaMemcpyAsync(dR, dB, blk, cudaMemcpyDeviceToDevice, ctx->stream));
-        if ((st = gemm_device(ctx, NIHU_GB_GEMM_BF16X9, dA, n, n, lda, dX, n, nrhs, dR, n, -1.0, 0.0, 1.0, 0.0)))
+        if ((st = gemm_device(ctx, residual_mode, dA, n, n, lda, dX, n, nrhs, dR, n, -1.0, 0.0, 1.0, 0.0)))
             return st;
     }
     if (where == NIHU_GB_HOST) CK(cudaMemcpyAsync(X, dX, blk, cudaMemcpyDeviceToHost, ctx->stream));
