@@ -503,7 +503,7 @@ def run_multirhs(args):
         got = np.zeros((n, nc), np.complex64, order="F")
         ctx.check(L.nihu_gb_memcpy(ctx.handle, got.ctypes.data, C.HOST, ptr, C.DEVICE, got.nbytes))
         ref = oracle.assemble((nodes, elems), (nodes, elems), oracle.HELMHOLTZ, op, k, cols=(0, nc),
-                              threads=os.cpu_count() or 1)
+                              same_mesh=True, threads=os.cpu_count() or 1)
         if op == oracle.DLP:
             ref[np.arange(nc), np.arange(nc)] -= 0.5
         worst[name] = float(np.abs(got - ref).max() / np.abs(ref).max())
