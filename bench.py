@@ -52,7 +52,7 @@ def parse():
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-solve", action="store_true")
     p.add_argument("--no-cpu", action="store_true")
-    p.add_argument("--config", default="large", choices=["large", "multirhs"],
+    p.add_argument("--config", default="large", choices=["large", "multirhs", "sweep"],
                    help="large: the headline line (20480-triangle icosphere); multirhs: the 40000-quad "
                         "cylinder with 64 plane waves (a separate line)")
     return p.parse_args()
@@ -528,10 +528,74 @@ def run_multirhs(args):
     print(json.dumps(out), flush=True)
 
 
+def run_sweep(args):
+    """Batched frequency sweep: icospheres of 320, 1280 and 5120 triangles,
+    256 wave numbers uniform in [0.1, 10] (seeded) dealt round-robin to the
+    meshes; pulsating-sphere Neumann data; every instance assembled (complex64,
+    FP64 singular terms) and solved to 1e-6 by GMRES.  The batched path
+    (nihu_gb_solve_sweep, one call per mesh) is timed against the plain
+    single-instance path (nihu_gb_solve_cbie per instance) on a sample."""
+    import torch
+
+    import nihu_gb300 as g
+
+    rng = np.random.default_rng(2026)
+    ks_all = rng.uniform(0.1, 10.0, 256)
+    meshes_ = {s_: g.create_mesh(*__import__("nihu_gb300").meshes.icosphere(s_)) for s_ in (2, 3, 4)}
+    groups = {s_: ks_all[i::3] for i, s_ in enumerate((2, 3, 4))}
+    ctx = g.Context(0)
+    for m in meshes_.values():
+        m.device(ctx)
+    # warm-up: one small sweep per mesh (near lists, code paths)
+    for s_, m in meshes_.items():
+        g.solve_sweep(m, groups[s_][:2], np.ones(m.num_elements), tol=1e-6, ctx=ctx)
+    out = {"metric": "BEM solves/s (batched frequency sweep, config 4)", "impl": "ours", "unit": "solves/s",
+           "instances": 256, "per_mesh": {}}
+    torch.cuda.synchronize()
+    t_all = time.perf_counter()
+    for s_, m in meshes_.items():
+        n = m.num_elements
+        t0 = time.perf_counter()
+        P, cyc, it, res = g.solve_sweep(m, groups[s_], np.ones(n), tol=1e-6, restart=40, max_cycles=60, ctx=ctx)
+        torch.cuda.synchronize()
+        dt = time.perf_counter() - t0
+        pa = -1.0 / (1 + 1j * groups[s_])
+        err = np.abs(P - pa[None, :]).max(axis=0) / np.abs(pa)
+        out["per_mesh"][n] = {"instances": len(groups[s_]), "seconds": dt, "lockstep_iterations": it, "cycles": cyc,
+                              "max_rel_residual": float(res.max()),
+                              "pressure_error_vs_analytic_median": float(np.median(err)),
+                              "pressure_error_vs_analytic_max": float(err.max())}
+    batched_s = time.perf_counter() - t_all
+    out["batched_seconds"] = batched_s
+    out["value"] = 256 / batched_s
+    # plain single-instance path on a sample of 6 instances per mesh, extrapolated
+    plain_s, agree = 0.0, 0.0
+    for s_, m in meshes_.items():
+        n = m.num_elements
+        sample = groups[s_][:6]
+        t0 = time.perf_counter()
+        ps = [g.solve_cbie(m, float(k), np.ones(n), tol=1e-6, ctx=ctx)[0] for k in sample]
+        torch.cuda.synchronize()
+        dt = (time.perf_counter() - t0) / len(sample)
+        plain_s += dt * len(groups[s_])
+        Pb = g.solve_sweep(m, sample, np.ones(n), tol=1e-6, ctx=ctx)[0]
+        for f, p1 in enumerate(ps):
+            agree = max(agree, float(np.abs(Pb[:, f] - p1).max() / np.abs(p1).max()))
+        out["per_mesh"][n]["plain_seconds_per_instance"] = dt
+    out["plain_solves_per_s"] = 256 / plain_s
+    out["speedup_vs_plain_gpu"] = out["value"] / out["plain_solves_per_s"]
+    out["batched_vs_plain_max_rel_difference"] = agree
+    ctx.close()
+    print(json.dumps(out), flush=True)
+
+
 def main():
     args = parse()
     if args.config == "multirhs":
         run_multirhs(args)
+        return
+    if args.config == "sweep":
+        run_sweep(args)
         return
     if args.impl == "reference":
         run_reference(args)

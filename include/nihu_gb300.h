@@ -223,6 +223,30 @@ nihu_gb_status nihu_gb_solve_multi(nihu_gb_ctx *ctx, const void *A, int64_t n, i
                                    double tol, double inner_tol, int *outer_iters, int *inner_iters,
                                    double *rel_residuals, int where);
 
+/* Frequency batch: assemble the operators of one mesh pair for nk wave
+ * numbers in one pass.  Every thread classifies its pairs once and evaluates
+ * them for all wave numbers; the k-independent static part of the nearly
+ * singular triangle integrals is computed once.  Matrix f starts at
+ * out + f * mat_stride elements (mat_stride >= ld * trial elements); outputs
+ * on the device, overwritten (alpha = 1).  Replaces nk calls of the
+ * reference's assembly (nihu/core/assembly.hpp:136-157), one per wave number. */
+nihu_gb_status nihu_gb_assemble_sweep(nihu_gb_ctx *ctx, const nihu_gb_mesh *test, const nihu_gb_mesh *trial,
+                                      int family, int ops, const double *ks, int nk, int precision, int dtype,
+                                      void *out_slp, void *out_dlp, int64_t ld, int64_t mat_stride);
+
+/* Frequency sweep of the exterior CBIE (DLP - I/2) p_f = SLP q_f on one mesh
+ * (the plain branch of nihu/applications/helmholtz/helmholtz_3d_coll.cpp:36-120
+ * for every wave number): batched assembly (complex64, FP64 singular terms),
+ * batched right-hand sides, and restarted GMRES on all wave numbers in
+ * lockstep (batched FP32 matvecs, FP64 Arnoldi).  q is n x q_cols complex128
+ * on the host (q_cols = 1 broadcasts one Neumann datum to every wave number,
+ * else q_cols = nk); p receives n x nk complex128.  cycles / iters (may be
+ * NULL) receive the restart cycles and the lockstep iterations;
+ * rel_residuals (nk doubles, may be NULL) the final relative residuals. */
+nihu_gb_status nihu_gb_solve_sweep(nihu_gb_ctx *ctx, const nihu_gb_mesh *mesh, int family, const double *ks, int nk,
+                                   int precision, const void *q, int q_cols, void *p, int restart, int max_cycles,
+                                   double tol, int *cycles, int *iters, double *rel_residuals);
+
 /* Solve A x = b with restarted GMRES(restart) (nihu/fmm/GMRES.h:57-205
  * semantics: stop when |residual estimate| / |b - A x0| < tol).  A is n x n
  * (dtype_a) on the device; b and x are complex128 (x holds the initial guess

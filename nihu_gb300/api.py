@@ -431,6 +431,30 @@ def solve_cbie(mesh: Mesh, k: float, q, family: int = C.HELMHOLTZ_3D, dtype: int
     return p, it.value, res.value
 
 
+def solve_sweep(mesh: Mesh, ks, q, family: int = C.HELMHOLTZ_3D, precision: str = "fp32", restart: int = 30,
+                max_cycles: int = 50, tol: float = 1e-6, ctx: Context | None = None):
+    """(DLP - I/2) p_f = SLP q_f for every wave number ks[f] on one mesh, batched on
+    the GPU.  q: (n,) broadcast or (n, nk).  Returns (P (n x nk), cycles,
+    lockstep iterations, relative residuals)."""
+    ctx = ctx or default_context()
+    ks = np.ascontiguousarray(ks, dtype=np.float64)
+    nk = len(ks)
+    q = np.asarray(q, dtype=np.complex128)
+    q_cols = 1 if q.ndim == 1 else q.shape[1]
+    q = np.asfortranarray(q.reshape(q.shape[0], q_cols))
+    n = mesh.num_elements
+    P = np.zeros((n, nk), np.complex128, order="F")
+    cyc, it = ctypes.c_int(0), ctypes.c_int(0)
+    res = np.zeros(nk)
+    dm = mesh.device(ctx)
+    ctx.check(C.lib().nihu_gb_solve_sweep(ctx.handle, dm.handle, family,
+                                          ks.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), nk,
+                                          C.REGULAR_FP64 if precision == "fp64" else C.REGULAR_FP32, q.ctypes.data,
+                                          q_cols, P.ctypes.data, restart, max_cycles, tol, ctypes.byref(cyc),
+                                          ctypes.byref(it), res.ctypes.data_as(ctypes.POINTER(ctypes.c_double))))
+    return P, cyc.value, it.value, res
+
+
 def pair_statistics(test: Mesh, trial: Mesh, ctx: Context | None = None) -> np.ndarray:
     """[self, near, regular (SLP level, DLP level) 3x3] pair counts."""
     ctx = ctx or default_context()

@@ -150,12 +150,16 @@ __global__ void __launch_bounds__(REG_THREADS) k_regular(RegularArgs a)
             const float q = (fx * fx + fy * fy + fz * fz) * h.w;
             if (__all_sync(0xffffffffu, q > Q_FAR)) {
                 const float4 p = s_p0[c];
-                R sr = 0, si = 0, dr = 0, di = 0;
-                eval_point<FAM, float>(fx, fy, fz, p.x, p.y, p.z, p.w, k, R(DO_S), R(DO_D), sr, si, dr, di);
-                if (row_ok) {
-                    const int64_t off = (int64_t)(j - a.j0) * a.ld + i;
-                    if (DO_S) store_entry(out_s + off, sr, si, are, aim, unit_alpha, accumulate);
-                    if (DO_D) store_entry(out_d + off, dr, di, are, aim, unit_alpha, accumulate);
+                const int64_t off = (int64_t)(j - a.j0) * a.ld + i;
+                for (int f = 0; f < a.nk; ++f) {
+                    const R kf = a.nk > 1 ? a.ks32[f] : k;
+                    R sr = 0, si = 0, dr = 0, di = 0;
+                    eval_point<FAM, float>(fx, fy, fz, p.x, p.y, p.z, p.w, kf, R(DO_S), R(DO_D), sr, si, dr, di);
+                    if (row_ok) {
+                        const int64_t fo = off + f * a.mat_stride;
+                        if (DO_S) store_entry(out_s + fo, sr, si, are, aim, unit_alpha, accumulate);
+                        if (DO_D) store_entry(out_d + fo, dr, di, are, aim, unit_alpha, accumulate);
+                    }
                 }
                 continue;
             }
@@ -174,6 +178,10 @@ __global__ void __launch_bounds__(REG_THREADS) k_regular(RegularArgs a)
         const int npd = level_npts(tnc, par, ld);
         const int n_eval = ls == ld ? nps : nps + npd;
         const int64_t base = ((int64_t)j * 2 + par) * SLOTS;
+        for (int f = 0; f < a.nk; ++f) {
+        R kf;
+        if constexpr (sizeof(R) == 4) kf = a.nk > 1 ? a.ks32[f] : k;
+        else kf = a.nk > 1 ? a.ks[f] : k;
         R sr = 0, si = 0, dr = 0, di = 0;
         for (int q = 0; q < n_eval; ++q) {
             int slot;
@@ -187,16 +195,17 @@ __global__ void __launch_bounds__(REG_THREADS) k_regular(RegularArgs a)
                 // level-0 point: the trial centre; use the accurate hi/lo difference
                 const bool centre = slot == 0;
                 eval_point<FAM, float>(centre ? dx : y.x - x0, centre ? dy : y.y - x1, centre ? dz : y.z - x2, y.w,
-                                       n.x, n.y, n.z, k, ws, wd, sr, si, dr, di);
+                                       n.x, n.y, n.z, kf, ws, wd, sr, si, dr, di);
             } else {
                 const double *y = trial.pts64 + 8 * (base + slot);
-                eval_point<FAM, double>(y[0] - x0, y[1] - x1, y[2] - x2, y[3], y[4], y[5], y[6], k, ws, wd, sr, si,
-                                        dr, di);
+                eval_point<FAM, double>(y[0] - x0, y[1] - x1, y[2] - x2, y[3], y[4], y[5], y[6], kf, ws, wd, sr,
+                                        si, dr, di);
             }
         }
-        const int64_t off = (int64_t)(j - a.j0) * a.ld + i;
+        const int64_t off = (int64_t)(j - a.j0) * a.ld + i + f * a.mat_stride;
         if (DO_S) store_entry(out_s + off, sr, si, are, aim, unit_alpha, accumulate);
         if (DO_D) store_entry(out_d + off, dr, di, are, aim, unit_alpha, accumulate);
+        }
     }
 }
 

@@ -630,38 +630,65 @@ __global__ void __launch_bounds__(SING_THREADS) k_singular(RegularArgs a, NearLi
                         a.test.center[3 * (int64_t)i + 2]};
         Elem64 e;
         load_elem(a.trial, j, e);
-        Acc acc;
-        bool ok = true;
-        if (self) {
-            if (e.nc == 3) {
-                if (do_s) self_tria(e, fam, k, x0, acc);
-            } else {
-                self_quad(e, fam, k, x0, do_s, do_d, acc);
-            }
-        } else if (e.nc == 3) {
-            near_plane(e, fam, k, x0, do_s, do_d, acc, a.trial.dyn42 + 42 * (int64_t)j, short_series);
-        } else {
-            const bool telles = fam == FAM_HELMHOLTZ && do_d;
-            const bool polar_d = fam == FAM_LAPLACE && do_d;
-            double r5[3] = {0, 0, 0}, r6[3] = {0, 0, 0};
-            ok = inverse_mapping(e, x0, telles, r5, r6);
-            if (ok) {
-                if (do_s || polar_d) {
-                    Elem64 lin;
-                    linearized(e, r5[0], r5[1], lin);
-                    near_polar_sum(e, lin, fam, k, x0, r5[0], r5[1], do_s, polar_d, acc);
-                    near_plane(lin, fam, k, x0, do_s, polar_d, acc);
+        const int64_t off = (int64_t)(j - a.j0) * a.ld + i;
+        if (a.nk > 1 && e.nc == 3) {
+            // frequency batch on a triangle: the k-independent static part once,
+            // the dynamic part (or the self term) per wave number
+            Acc st;
+            if (!self) near_static(e, x0, do_s, do_d, st);
+            for (int f = 0; f < a.nk; ++f) {
+                const double kf = a.ks[f];
+                Acc acc;
+                if (self) {
+                    if (do_s) self_tria(e, fam, kf, x0, acc);
+                } else {
+                    acc = st;
+                    if (fam == FAM_HELMHOLTZ)
+                        near_dynamic(e, kf, x0, do_s, do_d, acc, a.trial.dyn42 + 42 * (int64_t)j,
+                                     kf * 3.0 * a.trial_size_max <= 0.75);
                 }
-                if (telles) near_telles_sum(e, fam, k, x0, r6, acc);
+                const int64_t fo = off + f * a.mat_stride;
+                if (do_s) store64(out_s + fo, acc.sr, acc.si, a.alpha_re, a.alpha_im, a.accumulate);
+                if (do_d) store64(out_d + fo, acc.dr, acc.di, a.alpha_re, a.alpha_im, a.accumulate);
             }
-        }
-        if (!ok) {
-            atomicCAS(err, 0, (int)min(item + 1, (int64_t)0x7fffffff));
             continue;
         }
-        const int64_t off = (int64_t)(j - a.j0) * a.ld + i;
-        if (do_s) store64(out_s + off, acc.sr, acc.si, a.alpha_re, a.alpha_im, a.accumulate);
-        if (do_d) store64(out_d + off, acc.dr, acc.di, a.alpha_re, a.alpha_im, a.accumulate);
+        for (int f = 0; f < a.nk; ++f) {
+            const double kf = a.nk > 1 ? a.ks[f] : k;
+            const bool short_f = a.nk > 1 ? kf * 3.0 * a.trial_size_max <= 0.75 : short_series;
+            Acc acc;
+            bool ok = true;
+            if (self) {
+                if (e.nc == 3) {
+                    if (do_s) self_tria(e, fam, kf, x0, acc);
+                } else {
+                    self_quad(e, fam, kf, x0, do_s, do_d, acc);
+                }
+            } else if (e.nc == 3) {
+                near_plane(e, fam, kf, x0, do_s, do_d, acc, a.trial.dyn42 + 42 * (int64_t)j, short_f);
+            } else {
+                const bool telles = fam == FAM_HELMHOLTZ && do_d;
+                const bool polar_d = fam == FAM_LAPLACE && do_d;
+                double r5[3] = {0, 0, 0}, r6[3] = {0, 0, 0};
+                ok = inverse_mapping(e, x0, telles, r5, r6);
+                if (ok) {
+                    if (do_s || polar_d) {
+                        Elem64 lin;
+                        linearized(e, r5[0], r5[1], lin);
+                        near_polar_sum(e, lin, fam, kf, x0, r5[0], r5[1], do_s, polar_d, acc);
+                        near_plane(lin, fam, kf, x0, do_s, polar_d, acc);
+                    }
+                    if (telles) near_telles_sum(e, fam, kf, x0, r6, acc);
+                }
+            }
+            if (!ok) {
+                atomicCAS(err, 0, (int)min(item + 1, (int64_t)0x7fffffff));
+                break;
+            }
+            const int64_t fo = off + f * a.mat_stride;
+            if (do_s) store64(out_s + fo, acc.sr, acc.si, a.alpha_re, a.alpha_im, a.accumulate);
+            if (do_d) store64(out_d + fo, acc.dr, acc.di, a.alpha_re, a.alpha_im, a.accumulate);
+        }
     }
 }
 

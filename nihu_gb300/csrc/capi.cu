@@ -4,6 +4,7 @@
 #include <complex>
 #include <cstdio>
 #include <cstring>
+#include <functional>
 #include <map>
 #include <mutex>
 #include <string>
@@ -1101,9 +1102,13 @@ namespace {
 
 // one GMRES(restart) cycle on all right-hand sides in lockstep: D = approx A^{-1} R
 // for the columns with active[r]; returns the iterations done
-nihu_gb_status gmres_cycle_multi(nihu_gb_ctx *ctx, int mode, const void *A, int64_t n, int64_t lda, const double2 *R,
-                                 double2 *D, int nrhs, const std::vector<char> &active, int restart, double inner_tol,
-                                 int *iters)
+// Y = A X for nrhs columns of length n (leading dimension n); `active`
+// (device int per column, may be NULL) marks the columns that still iterate
+typedef std::function<nihu_gb_status(const double2 *X, double2 *Y, const int *active)> ApplyFn;
+
+nihu_gb_status gmres_cycle_multi(nihu_gb_ctx *ctx, const ApplyFn &apply, int64_t n, const double2 *R, double2 *D,
+                                 int nrhs, const std::vector<char> &active, int restart,
+                                 const std::vector<double> &target_rel, int *iters)
 {
     typedef std::complex<double> C;
     nihu_gb_status st;
@@ -1144,15 +1149,20 @@ nihu_gb_status gmres_cycle_multi(nihu_gb_ctx *ctx, int mode, const void *A, int6
     std::vector<std::vector<C>> g(nrhs, std::vector<C>(m + 1, C(0))), cs(nrhs, std::vector<C>(m)), sn(nrhs, std::vector<C>(m));
     std::vector<int> kdone(nrhs, 0);
     std::vector<char> run = act;
+    void *pact;
+    if ((st = scratch(ctx, "mr_active", sizeof(int) * (size_t)nrhs, &pact))) return st;
+    int *dact = (int *)pact;
+    std::vector<int> runi(nrhs);
     for (int r = 0; r < nrhs; ++r) g[r][0] = beta[r];
     int k = 0;
     for (; k < m; ++k) {
         bool any = false;
         for (int r = 0; r < nrhs; ++r) any = any || run[r];
         if (!any) break;
-        // W = A V_k: one tensor-core GEMM over all right-hand sides
-        if ((st = gemm_device(ctx, mode, A, n, n, lda, V + (size_t)k * blk, n, nrhs, W, n, 1.0, 0.0, 0.0, 0.0)))
-            return st;
+        // W = A V_k for every right-hand side still iterating, in one call
+        for (int r = 0; r < nrhs; ++r) runi[r] = run[r];
+        CK(cudaMemcpyAsync(dact, runi.data(), sizeof(int) * nrhs, cudaMemcpyHostToDevice, ctx->stream));
+        if ((st = apply(V + (size_t)k * blk, W, dact))) return st;
         std::vector<std::vector<C>> h(nrhs, std::vector<C>(k + 2, C(0)));
         for (int pass = 0; pass < 2; ++pass) {  // CGS2
             CK(launch_bdot(V, k + 1, W, n, nrhs, part, hd, ctx->stream));
@@ -1188,7 +1198,7 @@ nihu_gb_status gmres_cycle_multi(nihu_gb_ctx *ctx, int mode, const void *A, int6
             g[r][k + 1] = -sn[r][k] * g0 + cs[r][k] * g1;
             for (int i = 0; i <= k; ++i) H[r][(size_t)i * m + k] = hr[i];
             kdone[r] = k + 1;
-            if (std::abs(g[r][k + 1]) <= inner_tol * beta[r] || hn[r] == 0.0) run[r] = 0;
+            if (std::abs(g[r][k + 1]) <= target_rel[r] * beta[r] || hn[r] == 0.0) run[r] = 0;
         }
     }
     *iters = k;
@@ -1216,42 +1226,24 @@ nihu_gb_status gmres_cycle_multi(nihu_gb_ctx *ctx, int mode, const void *A, int6
 
 }  // namespace
 
-extern "C" nihu_gb_status nihu_gb_solve_multi(nihu_gb_ctx *ctx, const void *A, int64_t n, int64_t lda, const void *B,
-                                              void *X, int64_t nrhs, int inner_mode, int residual_mode, int restart,
-                                              int max_outer, double tol, double inner_tol, int *outer_iters,
-                                              int *inner_iters, double *rel_residuals, int where)
+namespace {
+
+// Restarted lockstep GMRES on nrhs columns with an iterative-refinement outer
+// loop: X = 0, R = B; per outer step one GMRES cycle of `inner` on R (columns
+// still above tol), X += D, R = B - residual(X).  With inner == residual this
+// is plain restarted GMRES; with a low-precision inner product and an accurate
+// residual it is mixed-precision iterative refinement.  inner_tol <= 0 runs
+// each cycle to the global tolerance.
+nihu_gb_status multi_solve_driver(nihu_gb_ctx *ctx, const ApplyFn &inner, const ApplyFn &residual, int64_t n,
+                                  const double2 *dB, double2 *dX, int64_t nrhs, int restart, int max_outer, double tol,
+                                  double inner_tol, int *outer_iters, int *inner_iters, std::vector<double> &rel)
 {
-    if (!ctx) return NIHU_GB_ERR_INVALID_ARGUMENT;
-    if (inner_mode < 0 || inner_mode > 2 || (residual_mode != NIHU_GB_GEMM_FP32 && residual_mode != NIHU_GB_GEMM_BF16X9) || !valid_where(where) || n < 0 || nrhs < 0 || lda < std::max<int64_t>(n, 1) ||
-        restart < 1 || restart > 200 || max_outer < 1 || !(tol > 0.0) || !(inner_tol > 0.0) ||
-        (n && nrhs && (!A || !B || !X)) || n > 0x3fffffff || nrhs > 4096)
-        return fail(ctx, NIHU_GB_ERR_INVALID_ARGUMENT, "nihu_gb_solve_multi: bad argument");
-    if (n == 0 || nrhs == 0) return NIHU_GB_OK;
-    cudaSetDevice(ctx->device);
-    restart = (int)std::min<int64_t>(restart, n);
     nihu_gb_status st;
-    const void *dA = A;
-    double2 *dB, *dX, *dR, *dD;
-    void *pb, *px, *pr, *pd, *pp, *ph;
+    void *pr, *pd, *pp, *ph;
     const size_t blk = 16 * (size_t)n * nrhs;
-    if ((st = scratch(ctx, "ms_B", blk, &pb))) return st;
-    if ((st = scratch(ctx, "ms_X", blk, &px))) return st;
     if ((st = scratch(ctx, "ms_R", blk, &pr))) return st;
     if ((st = scratch(ctx, "ms_D", blk, &pd))) return st;
-    dB = (double2 *)pb;
-    dX = (double2 *)px;
-    dR = (double2 *)pr;
-    dD = (double2 *)pd;
-    if (where == NIHU_GB_HOST) {
-        void *pa;
-        if ((st = scratch(ctx, "mv_A", 8 * n * n, &pa))) return st;
-        CK(cudaMemcpy2DAsync(pa, 8 * n, A, 8 * lda, 8 * n, n, cudaMemcpyHostToDevice, ctx->stream));
-        dA = pa;
-        lda = n;
-        CK(cudaMemcpyAsync(dB, B, blk, cudaMemcpyHostToDevice, ctx->stream));
-    } else {
-        CK(cudaMemcpyAsync(dB, B, blk, cudaMemcpyDeviceToDevice, ctx->stream));
-    }
+    double2 *dR = (double2 *)pr, *dD = (double2 *)pd;
     const int blocks = bdot_blocks(n);
     if ((st = scratch(ctx, "mr_part", 16 * (size_t)(restart + 1) * nrhs * blocks, &pp))) return st;
     if ((st = scratch(ctx, "mr_h", 16 * (size_t)(restart + 1) * nrhs, &ph))) return st;
@@ -1264,7 +1256,8 @@ extern "C" nihu_gb_status nihu_gb_solve_multi(nihu_gb_ctx *ctx, const void *A, i
         for (int64_t r = 0; r < nrhs; ++r) out[r] = std::sqrt(std::max(hh[r].x, 0.0));
         return NIHU_GB_OK;
     };
-    std::vector<double> bn(nrhs), rn(nrhs), rel(nrhs);
+    std::vector<double> bn(nrhs), rn(nrhs);
+    rel.assign(nrhs, 0.0);
     if ((st = norms(dB, bn))) return st;
     CK(cudaMemsetAsync(dX, 0, blk, ctx->stream));
     CK(cudaMemcpyAsync(dR, dB, blk, cudaMemcpyDeviceToDevice, ctx->stream));
@@ -1274,35 +1267,212 @@ extern "C" nihu_gb_status nihu_gb_solve_multi(nihu_gb_ctx *ctx, const void *A, i
         if ((st = norms(dR, rn))) return st;
         double worst = 0.0;
         std::vector<char> active(nrhs);
+        std::vector<double> target(nrhs);
         for (int64_t r = 0; r < nrhs; ++r) {
             rel[r] = bn[r] > 0.0 ? rn[r] / bn[r] : 0.0;
             active[r] = rel[r] > tol;
             worst = std::max(worst, rel[r]);
+            // stop a column's cycle at inner_tol of its current residual, or at the global tolerance
+            target[r] = inner_tol > 0.0 ? inner_tol : (rn[r] > 0.0 ? tol * bn[r] / rn[r] : 1.0);
         }
         if (worst <= tol) { converged = true; break; }
         if (outer >= max_outer) break;
         ++outer;
         CK(cudaMemsetAsync(dD, 0, blk, ctx->stream));
         int it = 0;
-        if ((st = gmres_cycle_multi(ctx, inner_mode, dA, n, lda, dR, dD, (int)nrhs, active, restart, inner_tol, &it)))
-            return st;
+        if ((st = gmres_cycle_multi(ctx, inner, n, dR, dD, (int)nrhs, active, restart, target, &it))) return st;
         inner_total += it;
-        // X += D (FP64); R = B - A X with FP32-accurate split-BF16 products, FP64 accumulation
         std::vector<double2> ones((size_t)nrhs, make_double2(1.0, 0.0));
         CK(cudaMemcpyAsync(ph, ones.data(), 16 * (size_t)nrhs, cudaMemcpyHostToDevice, ctx->stream));
         CK(launch_bcombo(dD, n, (int)nrhs, 1, (const double2 *)ph, 1.0, dX, ctx->stream));
         ctx->launches += 1;
-        CK(cudaMemcpyAsync(dR, dB, blk, cudaMemcpyDeviceToDevice, ctx->stream));
-        if ((st = gemm_device(ctx, residual_mode, dA, n, n, lda, dX, n, nrhs, dR, n, -1.0, 0.0, 1.0, 0.0)))
-            return st;
+        // R = B - A X
+        if ((st = residual(dX, dR, nullptr))) return st;
+        CK(launch_rsub(dB, dR, (size_t)n * nrhs, ctx->stream));
+        ctx->launches += 1;
     }
-    if (where == NIHU_GB_HOST) CK(cudaMemcpyAsync(X, dX, blk, cudaMemcpyDeviceToHost, ctx->stream));
-    else CK(cudaMemcpyAsync(X, dX, blk, cudaMemcpyDeviceToDevice, ctx->stream));
     if ((st = sync(ctx))) return st;
     if (outer_iters) *outer_iters = outer;
     if (inner_iters) *inner_iters = inner_total;
+    if (!converged) return fail(ctx, NIHU_GB_ERR_NOT_CONVERGED, "lockstep GMRES did not reach the tolerance");
+    return NIHU_GB_OK;
+}
+
+}  // namespace
+
+extern "C" nihu_gb_status nihu_gb_solve_multi(nihu_gb_ctx *ctx, const void *A, int64_t n, int64_t lda, const void *B,
+                                              void *X, int64_t nrhs, int inner_mode, int residual_mode, int restart,
+                                              int max_outer, double tol, double inner_tol, int *outer_iters,
+                                              int *inner_iters, double *rel_residuals, int where)
+{
+    if (!ctx) return NIHU_GB_ERR_INVALID_ARGUMENT;
+    if (inner_mode < 0 || inner_mode > 2 || (residual_mode != NIHU_GB_GEMM_FP32 && residual_mode != NIHU_GB_GEMM_BF16X9) ||
+        !valid_where(where) || n < 0 || nrhs < 0 || lda < std::max<int64_t>(n, 1) || restart < 1 || restart > 200 ||
+        max_outer < 1 || !(tol > 0.0) || !(inner_tol > 0.0) || (n && nrhs && (!A || !B || !X)) || n > 0x3fffffff ||
+        nrhs > 4096)
+        return fail(ctx, NIHU_GB_ERR_INVALID_ARGUMENT, "nihu_gb_solve_multi: bad argument");
+    if (n == 0 || nrhs == 0) return NIHU_GB_OK;
+    cudaSetDevice(ctx->device);
+    restart = (int)std::min<int64_t>(restart, n);
+    nihu_gb_status st;
+    const void *dA = A;
+    void *pb, *px;
+    const size_t blk = 16 * (size_t)n * nrhs;
+    if ((st = scratch(ctx, "ms_B", blk, &pb))) return st;
+    if ((st = scratch(ctx, "ms_X", blk, &px))) return st;
+    double2 *dB = (double2 *)pb, *dX = (double2 *)px;
+    if (where == NIHU_GB_HOST) {
+        void *pa;
+        if ((st = scratch(ctx, "mv_A", 8 * n * n, &pa))) return st;
+        CK(cudaMemcpy2DAsync(pa, 8 * n, A, 8 * lda, 8 * n, n, cudaMemcpyHostToDevice, ctx->stream));
+        dA = pa;
+        lda = n;
+        CK(cudaMemcpyAsync(dB, B, blk, cudaMemcpyHostToDevice, ctx->stream));
+    } else {
+        CK(cudaMemcpyAsync(dB, B, blk, cudaMemcpyDeviceToDevice, ctx->stream));
+    }
+    ApplyFn inner = [&](const double2 *Xv, double2 *Yv, const int *) {
+        return gemm_device(ctx, inner_mode, dA, n, n, lda, Xv, n, nrhs, Yv, n, 1.0, 0.0, 0.0, 0.0);
+    };
+    ApplyFn resid = [&](const double2 *Xv, double2 *Yv, const int *) {
+        return gemm_device(ctx, residual_mode, dA, n, n, lda, Xv, n, nrhs, Yv, n, 1.0, 0.0, 0.0, 0.0);
+    };
+    std::vector<double> rel;
+    nihu_gb_status sst = multi_solve_driver(ctx, inner, resid, n, dB, dX, nrhs, restart, max_outer, tol, inner_tol,
+                                            outer_iters, inner_iters, rel);
+    if (sst && sst != NIHU_GB_ERR_NOT_CONVERGED) return sst;
+    std::string msg = ctx->err;
+    if (where == NIHU_GB_HOST) CK(cudaMemcpyAsync(X, dX, blk, cudaMemcpyDeviceToHost, ctx->stream));
+    else CK(cudaMemcpyAsync(X, dX, blk, cudaMemcpyDeviceToDevice, ctx->stream));
+    if ((st = sync(ctx))) return st;
+    ctx->err = msg;
     if (rel_residuals)
         for (int64_t r = 0; r < nrhs; ++r) rel_residuals[r] = rel[r];
-    if (!converged) return fail(ctx, NIHU_GB_ERR_NOT_CONVERGED, "multi-RHS refinement did not reach the tolerance");
-    return NIHU_GB_OK;
+    return sst;
+}
+
+// ------------------------------------------------------- frequency sweep
+
+namespace {
+
+nihu_gb_status upload_ks(nihu_gb_ctx *ctx, const double *ks, int nk, const double **dks, const float **dks32)
+{
+    nihu_gb_status st;
+    void *p64, *p32;
+    if ((st = scratch(ctx, "sw_k64", 8 * (size_t)nk, &p64))) return st;
+    if ((st = scratch(ctx, "sw_k32", 4 * (size_t)nk, &p32))) return st;
+    std::vector<float> k32(ks, ks + nk);
+    CK(cudaMemcpyAsync(p64, ks, 8 * (size_t)nk, cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaMemcpyAsync(p32, k32.data(), 4 * (size_t)nk, cudaMemcpyHostToDevice, ctx->stream));
+    *dks = (const double *)p64;
+    *dks32 = (const float *)p32;
+    return sync(ctx);  // the host vector dies here
+}
+
+}  // namespace
+
+extern "C" nihu_gb_status nihu_gb_assemble_sweep(nihu_gb_ctx *ctx, const nihu_gb_mesh *test, const nihu_gb_mesh *trial,
+                                                 int family, int ops, const double *ks, int nk, int precision,
+                                                 int dtype, void *out_slp, void *out_dlp, int64_t ld,
+                                                 int64_t mat_stride)
+{
+    if (!ctx) return NIHU_GB_ERR_INVALID_ARGUMENT;
+    if (!test || !trial || test->ctx != ctx || trial->ctx != ctx || nk < 1 || !ks || ops < 1 || ops > 3 ||
+        ((ops & 1) && !out_slp) || ((ops & 2) && !out_dlp) || !valid_dtype(dtype) || (precision != 0 && precision != 1) ||
+        ld < std::max<int64_t>(test->n, 1) || mat_stride < ld * trial->n ||
+        (family != NIHU_GB_HELMHOLTZ_3D && family != NIHU_GB_LAPLACE_3D))
+        return fail(ctx, NIHU_GB_ERR_INVALID_ARGUMENT, "nihu_gb_assemble_sweep: bad argument");
+    for (int f = 0; f < nk; ++f)
+        if (!std::isfinite(ks[f])) return fail(ctx, NIHU_GB_ERR_INVALID_ARGUMENT, "nihu_gb_assemble_sweep: bad k");
+    if (test->n == 0 || trial->n == 0) return NIHU_GB_OK;
+    cudaSetDevice(ctx->device);
+    nihu_gb_status st;
+    NearList *nl = nullptr;
+    if ((st = get_near(ctx, test, trial, &nl))) return st;
+    RegularArgs a;
+    a.test = test->dm;
+    a.trial = trial->dm;
+    a.same_mesh = test == trial;
+    a.family = family;
+    a.ops = ops;
+    a.k = ks[0];
+    a.alpha_re = 1.0;
+    a.alpha_im = 0.0;
+    a.precision = precision;
+    a.dtype = dtype;
+    a.accumulate = 0;
+    a.trial_size_max = trial->size_max;
+    a.k32 = (float)ks[0];
+    a.alpha_re32 = 1.0f;
+    a.alpha_im32 = 0.0f;
+    a.unit_alpha = 1;
+    a.out_s = out_slp;
+    a.out_d = out_dlp;
+    a.ld = ld;
+    a.j0 = 0;
+    a.j1 = (int)trial->n;
+    a.nk = nk;
+    a.mat_stride = mat_stride;
+    if ((st = upload_ks(ctx, ks, nk, &a.ks, &a.ks32))) return st;
+    if ((st = assemble_panel(ctx, a, nl))) return st;
+    return check_flag(ctx);
+}
+
+extern "C" nihu_gb_status nihu_gb_solve_sweep(nihu_gb_ctx *ctx, const nihu_gb_mesh *mesh, int family, const double *ks,
+                                              int nk, int precision, const void *q, int q_cols, void *p, int restart,
+                                              int max_cycles, double tol, int *cycles, int *iters, double *rel_residuals)
+{
+    if (!ctx) return NIHU_GB_ERR_INVALID_ARGUMENT;
+    if (!mesh || nk < 1 || !ks || !q || !p || (q_cols != 1 && q_cols != nk) || restart < 1 || restart > 200 ||
+        max_cycles < 1 || !(tol > 0.0))
+        return fail(ctx, NIHU_GB_ERR_INVALID_ARGUMENT, "nihu_gb_solve_sweep: bad argument");
+    const int64_t n = mesh->n;
+    if (n == 0) return NIHU_GB_OK;
+    cudaSetDevice(ctx->device);
+    nihu_gb_status st;
+    const int64_t stride = n * n;
+    void *G, *H, *pq, *pb, *px, *part;
+    if ((st = scratch(ctx, "sw_G", 8 * (size_t)stride * nk, &G))) return st;
+    if ((st = scratch(ctx, "sw_H", 8 * (size_t)stride * nk, &H))) return st;
+    if ((st = scratch(ctx, "sw_q", 16 * (size_t)n * nk, &pq))) return st;
+    if ((st = scratch(ctx, "ms_B", 16 * (size_t)n * nk, &pb))) return st;
+    if ((st = scratch(ctx, "ms_X", 16 * (size_t)n * nk, &px))) return st;
+    const int splits = gemv_splits(n, n, NIHU_GB_C64);
+    if ((st = scratch(ctx, "sw_part", 16 * (size_t)splits * n * nk, &part))) return st;
+    // q: one column broadcast to every wave number, or one column each
+    for (int f = 0; f < nk; ++f) {
+        const char *src = (const char *)q + (q_cols == 1 ? 0 : 16 * (size_t)n * f);
+        CK(cudaMemcpyAsync((char *)pq + 16 * (size_t)n * f, src, 16 * (size_t)n, cudaMemcpyHostToDevice, ctx->stream));
+    }
+    if ((st = nihu_gb_assemble_sweep(ctx, mesh, mesh, family, NIHU_GB_SLP | NIHU_GB_DLP, ks, nk, precision, NIHU_GB_C64,
+                                     G, H, n, stride)))
+        return st;
+    CK(launch_add_identity_batched((int)n, -0.5, 0.0, NIHU_GB_C64, H, n, stride, nk, ctx->stream));
+    ctx->launches += 1;
+    {
+        Phase ph(ctx, "gemv_c64");
+        CK(launch_gemv_batched(NIHU_GB_C64, G, n, n, n, stride, nk, (const double2 *)pq, (double2 *)pb, 1.0, 0.0, 0.0,
+                               0.0, (double2 *)part, splits, ctx->stream, nullptr));
+    }
+    ctx->launches += 2;
+    ApplyFn apply = [&](const double2 *Xv, double2 *Yv, const int *active) -> nihu_gb_status {
+        Phase ph(ctx, "gemv_c64");
+        cudaError_t e = launch_gemv_batched(NIHU_GB_C64, H, n, n, n, stride, nk, Xv, Yv, 1.0, 0.0, 0.0, 0.0,
+                                            (double2 *)part, splits, ctx->stream, active);
+        ctx->launches += 2;
+        if (e != cudaSuccess) return cuda_fail(ctx, e, "batched matvec");
+        return NIHU_GB_OK;
+    };
+    std::vector<double> rel;
+    restart = (int)std::min<int64_t>(restart, n);
+    nihu_gb_status sst = multi_solve_driver(ctx, apply, apply, n, (const double2 *)pb, (double2 *)px, nk, restart,
+                                            max_cycles, tol, -1.0, cycles, iters, rel);
+    if (sst && sst != NIHU_GB_ERR_NOT_CONVERGED) return sst;
+    std::string msg = ctx->err;
+    CK(cudaMemcpyAsync(p, px, 16 * (size_t)n * nk, cudaMemcpyDeviceToHost, ctx->stream));
+    if ((st = sync(ctx))) return st;
+    ctx->err = msg;
+    if (rel_residuals)
+        for (int f = 0; f < nk; ++f) rel_residuals[f] = rel[f];
+    return sst;
 }

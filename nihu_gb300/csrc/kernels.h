@@ -54,6 +54,12 @@ struct RegularArgs {
     // FP64 instruction (the FP64 pipe belongs to the concurrent singular kernel)
     float k32, alpha_re32, alpha_im32;
     int unit_alpha;
+    // frequency batch: nk > 1 assembles one matrix per wave number ks[f]
+    // (FP64 and FP32 copies on the device) at out + f * mat_stride
+    int nk = 1;
+    const double *ks = nullptr;
+    const float *ks32 = nullptr;
+    int64_t mat_stride = 0;
 };
 cudaError_t launch_assemble_regular(const RegularArgs &a, cudaStream_t s);
 

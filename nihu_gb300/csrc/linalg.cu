@@ -42,9 +42,15 @@ constexpr int GEMV_XCHUNK = 1024;
 
 __global__ void __launch_bounds__(GEMV_THREADS) k_gemv_c64(const float2 *__restrict__ A, int64_t m, int64_t n,
                                                            int64_t lda, const double2 *__restrict__ x,
-                                                           double2 *__restrict__ partial, int cols_per_split)
+                                                           double2 *__restrict__ partial, int cols_per_split,
+                                                           int64_t a_stride, const int *__restrict__ active)
 {
     __shared__ float2 xs[GEMV_XCHUNK];
+    if (active && !active[blockIdx.z]) return;  // converged batch member: its matrix is not read
+    // batch member blockIdx.z: its matrix, vector and partial sums
+    A += blockIdx.z * a_stride;
+    x += blockIdx.z * n;
+    partial += (int64_t)blockIdx.z * gridDim.y * m;
     const int64_t row0 = ((int64_t)blockIdx.x * GEMV_THREADS + threadIdx.x) * 2;
     const int64_t j_begin = (int64_t)blockIdx.y * cols_per_split;
     const int64_t j_end = min(n, j_begin + cols_per_split);
@@ -106,9 +112,14 @@ __global__ void __launch_bounds__(GEMV_THREADS) k_gemv_c64(const float2 *__restr
 
 __global__ void __launch_bounds__(GEMV_THREADS) k_gemv_c128(const double2 *__restrict__ A, int64_t m, int64_t n,
                                                             int64_t lda, const double2 *__restrict__ x,
-                                                            double2 *__restrict__ partial, int cols_per_split)
+                                                            double2 *__restrict__ partial, int cols_per_split,
+                                                            int64_t a_stride, const int *__restrict__ active)
 {
     __shared__ double2 xs[GEMV_XCHUNK];
+    if (active && !active[blockIdx.z]) return;
+    A += blockIdx.z * a_stride;
+    x += blockIdx.z * n;
+    partial += (int64_t)blockIdx.z * gridDim.y * m;
     const int64_t row = (int64_t)blockIdx.x * GEMV_THREADS + threadIdx.x;
     const int64_t j_begin = (int64_t)blockIdx.y * cols_per_split;
     const int64_t j_end = min(n, j_begin + cols_per_split);
@@ -143,11 +154,14 @@ __global__ void __launch_bounds__(GEMV_THREADS) k_gemv_c128(const double2 *__res
     if (row < m) partial[(int64_t)blockIdx.y * m + row] = make_double2(ar, ai);
 }
 
-// y = alpha * sum_s partial[s] + beta * y
+// y = alpha * sum_s partial[s] + beta * y  (batch member blockIdx.y)
 __global__ void k_gemv_reduce(const double2 *__restrict__ partial, int splits, int64_t m, double2 *y, double are,
-                              double aim, double bre, double bim)
+                              double aim, double bre, double bim, const int *__restrict__ active)
 {
+    if (active && !active[blockIdx.y]) return;
     int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    partial += (int64_t)blockIdx.y * splits * m;
+    y += (int64_t)blockIdx.y * m;
     if (i >= m) return;
     double sr = 0.0, si = 0.0;
     for (int s = 0; s < splits; ++s) {
@@ -174,20 +188,53 @@ int gemv_splits(int64_t m, int64_t n, int dtype)
     return (int)max((int64_t)1, min(splits, (int64_t)1024));
 }
 
-cudaError_t launch_gemv(int dtype, const void *A, int64_t m, int64_t n, int64_t lda, const double2 *x, double2 *y,
-                        double are, double aim, double bre, double bim, double2 *partial, int splits, cudaStream_t s)
+cudaError_t launch_gemv_batched(int dtype, const void *A, int64_t m, int64_t n, int64_t lda, int64_t a_stride,
+                                int batch, const double2 *x, double2 *y, double are, double aim, double bre,
+                                double bim, double2 *partial, int splits, cudaStream_t s, const int *active)
 {
-    if (m == 0) return cudaSuccess;
+    if (m == 0 || batch == 0) return cudaSuccess;
     int cols_per_split = (int)((n + splits - 1) / splits);
     if (n == 0) cols_per_split = 0;
     if (dtype == 0) {
-        dim3 grid((unsigned)((m + 2 * GEMV_THREADS - 1) / (2 * GEMV_THREADS)), splits);
-        k_gemv_c64<<<grid, GEMV_THREADS, 0, s>>>((const float2 *)A, m, n, lda, x, partial, cols_per_split);
+        dim3 grid((unsigned)((m + 2 * GEMV_THREADS - 1) / (2 * GEMV_THREADS)), splits, batch);
+        k_gemv_c64<<<grid, GEMV_THREADS, 0, s>>>((const float2 *)A, m, n, lda, x, partial, cols_per_split, a_stride,
+                                                  active);
     } else {
-        dim3 grid((unsigned)((m + GEMV_THREADS - 1) / GEMV_THREADS), splits);
-        k_gemv_c128<<<grid, GEMV_THREADS, 0, s>>>((const double2 *)A, m, n, lda, x, partial, cols_per_split);
+        dim3 grid((unsigned)((m + GEMV_THREADS - 1) / GEMV_THREADS), splits, batch);
+        k_gemv_c128<<<grid, GEMV_THREADS, 0, s>>>((const double2 *)A, m, n, lda, x, partial, cols_per_split,
+                                                   a_stride, active);
     }
-    k_gemv_reduce<<<(unsigned)((m + 255) / 256), 256, 0, s>>>(partial, splits, m, y, are, aim, bre, bim);
+    dim3 rgrid((unsigned)((m + 255) / 256), batch);
+    k_gemv_reduce<<<rgrid, 256, 0, s>>>(partial, splits, m, y, are, aim, bre, bim, active);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_gemv(int dtype, const void *A, int64_t m, int64_t n, int64_t lda, const double2 *x, double2 *y,
+                        double are, double aim, double bre, double bim, double2 *partial, int splits, cudaStream_t s)
+{
+    return launch_gemv_batched(dtype, A, m, n, lda, 0, 1, x, y, are, aim, bre, bim, partial, splits, s, nullptr);
+}
+
+// out(i, i) += alpha on `batch` matrices spaced `stride` elements apart
+template <typename Out>
+__global__ void k_add_identity_batched(int n, double are, double aim, Out *out, int64_t ld, int64_t stride)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    Out *p = out + blockIdx.y * stride + (int64_t)i * ld + i;
+    Out v = *p;
+    v.x += are;
+    v.y += aim;
+    *p = v;
+}
+
+cudaError_t launch_add_identity_batched(int n, double are, double aim, int dtype, void *out, int64_t ld, int64_t stride,
+                                        int batch, cudaStream_t s)
+{
+    if (n == 0 || batch == 0) return cudaSuccess;
+    dim3 g((n + 255) / 256, batch);
+    if (dtype == 0) k_add_identity_batched<float2><<<g, 256, 0, s>>>(n, are, aim, (float2 *)out, ld, stride);
+    else k_add_identity_batched<double2><<<g, 256, 0, s>>>(n, are, aim, (double2 *)out, ld, stride);
     return cudaGetLastError();
 }
 

@@ -11,6 +11,16 @@ int gemv_splits(int64_t m, int64_t n, int dtype);
 cudaError_t launch_gemv(int dtype, const void *A, int64_t m, int64_t n, int64_t lda, const double2 *x, double2 *y,
                         double are, double aim, double bre, double bim, double2 *partial, int splits, cudaStream_t s);
 
+// batch members b = 0..batch-1: y_b = alpha A_b x_b + beta y_b with
+// A_b = A + b * a_stride (elements), x_b = x + b * n, y_b = y + b * m;
+// partial holds batch * splits * m complex128; active (device, may be NULL)
+// skips members whose flag is 0 (their y is left untouched)
+cudaError_t launch_gemv_batched(int dtype, const void *A, int64_t m, int64_t n, int64_t lda, int64_t a_stride,
+                                int batch, const double2 *x, double2 *y, double are, double aim, double bre,
+                                double bim, double2 *partial, int splits, cudaStream_t s, const int *active);
+cudaError_t launch_add_identity_batched(int n, double are, double aim, int dtype, void *out, int64_t ld, int64_t stride,
+                                        int batch, cudaStream_t s);
+
 int dot_blocks(int64_t n);
 cudaError_t launch_multidot(const double2 *V, int64_t n, int nv, const double2 *w, double2 *partial, int blocks,
                             cudaStream_t s);
@@ -34,5 +44,6 @@ cudaError_t launch_bdot(const double2 *V, int nv, const double2 *W, int64_t n, i
 cudaError_t launch_bcombo(const double2 *V, int64_t n, int nrhs, int nv, const double2 *h, double sign, double2 *W,
                           cudaStream_t s);
 cudaError_t launch_bscale(const double2 *src, double2 *dst, int64_t n, int nrhs, const double *sc, cudaStream_t s);
+cudaError_t launch_rsub(const double2 *B, double2 *R, size_t count, cudaStream_t s);
 
 }  // namespace nihu

@@ -154,6 +154,22 @@ __global__ void k_bscale(const double2 *__restrict__ src, double2 *dst, int64_t 
     dst[(int64_t)r * n + i] = make_double2(v.x * f, v.y * f);
 }
 
+// R = B - R (element-wise, count complex values)
+__global__ void k_rsub(const double2 *__restrict__ B, double2 *R, size_t count)
+{
+    size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= count) return;
+    double2 b = B[i], r = R[i];
+    R[i] = make_double2(b.x - r.x, b.y - r.y);
+}
+
+cudaError_t launch_rsub(const double2 *B, double2 *R, size_t count, cudaStream_t s)
+{
+    if (count == 0) return cudaSuccess;
+    k_rsub<<<(unsigned)((count + 255) / 256), 256, 0, s>>>(B, R, count);
+    return cudaGetLastError();
+}
+
 int bdot_blocks(int64_t n)
 {
     int64_t b = (n + BT * 8 - 1) / (BT * 8);

@@ -1,0 +1,62 @@
+"""Frequency sweep (batched assembly + lockstep GMRES) against the plain
+single-instance path and the FP64 oracle."""
+import numpy as np
+import pytest
+
+import nihu_gb300 as g
+from nihu_gb300 import meshes
+
+pytestmark = pytest.mark.gpu
+
+
+def test_assemble_sweep_matches_single_assembly(gpu_ctx):
+    import ctypes
+    L = g.lib()
+    mesh = meshes.icosphere(2)
+    dm = g.api.DeviceMesh(gpu_ctx, *mesh)
+    n = dm.n
+    ks = np.array([0.5, 1.7, 4.2, 9.0])
+    nk = len(ks)
+    S = np.zeros((n, n * nk), np.complex64, order="F")
+    D = np.zeros((n, n * nk), np.complex64, order="F")
+    dS, dD = ctypes.c_void_p(), ctypes.c_void_p()
+    gpu_ctx.check(L.nihu_gb_device_alloc(gpu_ctx.handle, S.nbytes, ctypes.byref(dS)))
+    gpu_ctx.check(L.nihu_gb_device_alloc(gpu_ctx.handle, D.nbytes, ctypes.byref(dD)))
+    try:
+        gpu_ctx.check(L.nihu_gb_assemble_sweep(gpu_ctx.handle, dm.handle, dm.handle, g.HELMHOLTZ_3D, 3,
+                                               ks.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), nk, 0, 0, dS, dD,
+                                               n, n * n))
+        gpu_ctx.check(L.nihu_gb_memcpy(gpu_ctx.handle, S.ctypes.data, g.HOST, dS, g.DEVICE, S.nbytes))
+        gpu_ctx.check(L.nihu_gb_memcpy(gpu_ctx.handle, D.ctypes.data, g.HOST, dD, g.DEVICE, D.nbytes))
+    finally:
+        L.nihu_gb_device_free(gpu_ctx.handle, dS)
+        L.nihu_gb_device_free(gpu_ctx.handle, dD)
+    for f, k in enumerate(ks):
+        s1 = np.zeros((n, n), np.complex64, order="F")
+        d1 = np.zeros((n, n), np.complex64, order="F")
+        gpu_ctx.check(L.nihu_gb_assemble(gpu_ctx.handle, dm.handle, dm.handle, g.HELMHOLTZ_3D, 3, float(k), 1.0, 0.0,
+                                         0, 0, s1.ctypes.data, d1.ctypes.data, n, 0, g.HOST))
+        for a, b in ((S[:, f * n:(f + 1) * n], s1), (D[:, f * n:(f + 1) * n], d1)):
+            assert np.abs(a - b).max() / np.abs(b).max() < 1e-6
+    dm.close()
+
+
+def test_solve_sweep_pulsating_sphere(gpu_ctx, oracle):
+    mesh_arr = meshes.icosphere(3)
+    mesh = g.create_mesh(*mesh_arr)
+    n = mesh.num_elements
+    rng = np.random.default_rng(4)
+    ks = np.sort(rng.uniform(0.1, 2.5, 9))
+    P, cycles, iters, res = g.solve_sweep(mesh, ks, np.ones(n), tol=1e-7, ctx=gpu_ctx)
+    assert res.max() <= 1e-7
+    for f, k in enumerate(ks):
+        p1, it1, res1 = g.solve_cbie(mesh, float(k), np.ones(n), tol=1e-7, ctx=gpu_ctx)
+        assert np.abs(P[:, f] - p1).max() / np.abs(p1).max() < 1e-5
+        pa = -1.0 / (1 + 1j * k)
+        assert np.abs(P[:, f] - pa).max() / abs(pa) < 0.03
+    # one wave number against the FP64 oracle
+    k = float(ks[4])
+    L = oracle.assemble(mesh_arr, mesh_arr, oracle.HELMHOLTZ, oracle.SLP, k, threads=8)
+    M = oracle.assemble(mesh_arr, mesh_arr, oracle.HELMHOLTZ, oracle.DLP, k, threads=8) - 0.5 * np.eye(n)
+    p_ref = np.linalg.solve(M, L @ np.ones(n))
+    assert np.abs(P[:, 4] - p_ref).max() / np.abs(p_ref).max() < 1e-4
