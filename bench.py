@@ -548,23 +548,30 @@ def run_sweep(args):
         m.device(ctx)
     # warm-up: one small sweep per mesh (near lists, code paths)
     for s_, m in meshes_.items():
-        g.solve_sweep(m, groups[s_][:2], np.ones(m.num_elements), tol=1e-6, ctx=ctx)
+        g.solve_sweep(m, groups[s_][:2], np.ones(m.num_elements), tol=1e-6, ctx=ctx, check=False)
     out = {"metric": "BEM solves/s (batched frequency sweep, config 4)", "impl": "ours", "unit": "solves/s",
-           "instances": 256, "per_mesh": {}}
+           "instances": 256, "per_mesh": {},
+           "note": "the plain CBIE (DLP - I/2) p = SLP q is singular at the sphere's interior Dirichlet "
+                   "eigenvalues (k = pi, 4.49, 5.76, ...); wave numbers close to them may not reach 1e-6 "
+                   "within 1000 iterations on either path"}
     torch.cuda.synchronize()
     t_all = time.perf_counter()
     for s_, m in meshes_.items():
         n = m.num_elements
         t0 = time.perf_counter()
-        P, cyc, it, res = g.solve_sweep(m, groups[s_], np.ones(n), tol=1e-6, restart=40, max_cycles=60, ctx=ctx)
+        # restart 40 x 25 cycles: at most 1000 iterations, as for the plain path below
+        P, cyc, it, res = g.solve_sweep(m, groups[s_], np.ones(n), tol=1e-6, restart=40, max_cycles=25, ctx=ctx,
+                                        check=False)
         torch.cuda.synchronize()
         dt = time.perf_counter() - t0
         pa = -1.0 / (1 + 1j * groups[s_])
         err = np.abs(P - pa[None, :]).max(axis=0) / np.abs(pa)
+        conv = res <= 1e-6
         out["per_mesh"][n] = {"instances": len(groups[s_]), "seconds": dt, "lockstep_iterations": it, "cycles": cyc,
-                              "max_rel_residual": float(res.max()),
-                              "pressure_error_vs_analytic_median": float(np.median(err)),
-                              "pressure_error_vs_analytic_max": float(err.max())}
+                              "converged": int(conv.sum()),
+                              "not_converged_k": [round(float(x), 4) for x in groups[s_][~conv]],
+                              "max_rel_residual_converged": float(res[conv].max()) if conv.any() else None,
+                              "pressure_error_vs_analytic_median": float(np.median(err[conv])) if conv.any() else None}
     batched_s = time.perf_counter() - t_all
     out["batched_seconds"] = batched_s
     out["value"] = 256 / batched_s
@@ -574,11 +581,12 @@ def run_sweep(args):
         n = m.num_elements
         sample = groups[s_][:6]
         t0 = time.perf_counter()
-        ps = [g.solve_cbie(m, float(k), np.ones(n), tol=1e-6, ctx=ctx)[0] for k in sample]
+        ps = [g.solve_cbie(m, float(k), np.ones(n), tol=1e-6, restart=40, max_iters=1000, ctx=ctx, check=False)[0]
+              for k in sample]
         torch.cuda.synchronize()
         dt = (time.perf_counter() - t0) / len(sample)
         plain_s += dt * len(groups[s_])
-        Pb = g.solve_sweep(m, sample, np.ones(n), tol=1e-6, ctx=ctx)[0]
+        Pb = g.solve_sweep(m, sample, np.ones(n), tol=1e-6, restart=40, max_cycles=25, ctx=ctx, check=False)[0]
         for f, p1 in enumerate(ps):
             agree = max(agree, float(np.abs(Pb[:, f] - p1).max() / np.abs(p1).max()))
         out["per_mesh"][n]["plain_seconds_per_instance"] = dt
