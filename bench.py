@@ -532,67 +532,100 @@ def run_sweep(args):
     """Batched frequency sweep: icospheres of 320, 1280 and 5120 triangles,
     256 wave numbers uniform in [0.1, 10] (seeded) dealt round-robin to the
     meshes; pulsating-sphere Neumann data; every instance assembled (complex64,
-    FP64 singular terms) and solved to 1e-6 by GMRES.  The batched path
-    (nihu_gb_solve_sweep, one call per mesh) is timed against the plain
-    single-instance path (nihu_gb_solve_cbie per instance) on a sample."""
+    FP64 singular terms) and solved by GMRES(50) to 1e-6 (at most 1000
+    iterations).  The batched path (nihu_gb_solve_sweep_batched: one call,
+    per-mesh frequency-batched assembly, one persistent GMRES launch over all
+    256 systems) is timed against the plain single-instance path
+    (nihu_gb_solve_cbie, one call per instance) on every instance."""
     import torch
 
     import nihu_gb300 as g
 
     rng = np.random.default_rng(2026)
     ks_all = rng.uniform(0.1, 10.0, 256)
-    meshes_ = {s_: g.create_mesh(*__import__("nihu_gb300").meshes.icosphere(s_)) for s_ in (2, 3, 4)}
-    groups = {s_: ks_all[i::3] for i, s_ in enumerate((2, 3, 4))}
+    subdivs = (2, 3, 4)
+    mesh_list = [g.create_mesh(*g.meshes.icosphere(s_)) for s_ in subdivs]
+    mesh_of = np.arange(256) % 3
+    sizes = [m.num_elements for m in mesh_list]
     ctx = g.Context(0)
-    for m in meshes_.values():
+    for m in mesh_list:
         m.device(ctx)
-    # warm-up: one small sweep per mesh (near lists, code paths)
-    for s_, m in meshes_.items():
-        g.solve_sweep(m, groups[s_][:2], np.ones(m.num_elements), tol=1e-6, ctx=ctx, check=False)
+    restart, max_iters, tol = 50, 1000, 1e-6
     out = {"metric": "BEM solves/s (batched frequency sweep, config 4)", "impl": "ours", "unit": "solves/s",
-           "instances": 256, "per_mesh": {},
+           "instances": 256, "meshes": sizes, "restart": restart, "max_iters": max_iters, "tol": tol,
            "note": "the plain CBIE (DLP - I/2) p = SLP q is singular at the sphere's interior Dirichlet "
-                   "eigenvalues (k = pi, 4.49, 5.76, ...); wave numbers close to them may not reach 1e-6 "
-                   "within 1000 iterations on either path"}
-    torch.cuda.synchronize()
-    t_all = time.perf_counter()
-    for s_, m in meshes_.items():
-        n = m.num_elements
+                   "eigenvalues (k = pi, 4.49, 5.76, ...); wave numbers close to them may stop at the "
+                   "iteration cap on either path"}
+    ctx.set_profiling(True)
+    for _ in range(max(1, args.warmup)):  # warm-up: near lists, scratch, code paths
+        g.solve_sweep_batched(mesh_list, ks_all, mesh_of, restart=restart, max_iters=max_iters, tol=tol, ctx=ctx,
+                              check=False)
+    times = []
+    for _ in range(max(1, args.steps)):
+        ctx.profile_reset()
+        torch.cuda.synchronize()
         t0 = time.perf_counter()
-        # restart 40 x 25 cycles: at most 1000 iterations, as for the plain path below
-        P, cyc, it, res = g.solve_sweep(m, groups[s_], np.ones(n), tol=1e-6, restart=40, max_cycles=25, ctx=ctx,
-                                        check=False)
+        P, it, rel, conv = g.solve_sweep_batched(mesh_list, ks_all, mesh_of, restart=restart, max_iters=max_iters,
+                                                 tol=tol, ctx=ctx, check=False)
+        torch.cuda.synchronize()
+        times.append(time.perf_counter() - t0)
+    prof = ctx.profile()
+    batched_s = float(np.median(times))
+    out["batched_seconds"] = batched_s
+    out["batched_seconds_all"] = times
+    out["value"] = 256 / batched_s
+    out["phases_ms"] = {k: round(v[0], 3) for k, v in prof.items()}
+    out["launches"] = {k: v[1] for k, v in prof.items()}
+    # plain single-instance path on every instance
+    ctx.set_profiling(False)
+    per_mesh = {}
+    plain_s, agree, it_diff = 0.0, 0.0, []
+    pa_err = []
+    for f in range(256):
+        m = mesh_list[mesh_of[f]]
+        n = m.num_elements
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        p1, it1, res1 = g.solve_cbie(m, float(ks_all[f]), np.ones(n), restart=restart, max_iters=max_iters, tol=tol,
+                                     ctx=ctx, check=False)
         torch.cuda.synchronize()
         dt = time.perf_counter() - t0
-        pa = -1.0 / (1 + 1j * groups[s_])
-        err = np.abs(P - pa[None, :]).max(axis=0) / np.abs(pa)
-        conv = res <= 1e-6
-        out["per_mesh"][n] = {"instances": len(groups[s_]), "seconds": dt, "lockstep_iterations": it, "cycles": cyc,
-                              "converged": int(conv.sum()),
-                              "not_converged_k": [round(float(x), 4) for x in groups[s_][~conv]],
-                              "max_rel_residual_converged": float(res[conv].max()) if conv.any() else None,
-                              "pressure_error_vs_analytic_median": float(np.median(err[conv])) if conv.any() else None}
-    batched_s = time.perf_counter() - t_all
-    out["batched_seconds"] = batched_s
-    out["value"] = 256 / batched_s
-    # plain single-instance path on a sample of 6 instances per mesh, extrapolated
-    plain_s, agree = 0.0, 0.0
-    for s_, m in meshes_.items():
-        n = m.num_elements
-        sample = groups[s_][:6]
-        t0 = time.perf_counter()
-        ps = [g.solve_cbie(m, float(k), np.ones(n), tol=1e-6, restart=40, max_iters=1000, ctx=ctx, check=False)[0]
-              for k in sample]
-        torch.cuda.synchronize()
-        dt = (time.perf_counter() - t0) / len(sample)
-        plain_s += dt * len(groups[s_])
-        Pb = g.solve_sweep(m, sample, np.ones(n), tol=1e-6, restart=40, max_cycles=25, ctx=ctx, check=False)[0]
-        for f, p1 in enumerate(ps):
-            agree = max(agree, float(np.abs(Pb[:, f] - p1).max() / np.abs(p1).max()))
-        out["per_mesh"][n]["plain_seconds_per_instance"] = dt
+        plain_s += dt
+        agree = max(agree, float(np.abs(P[f] - p1).max() / np.abs(p1).max()))
+        it_diff.append(int(it[f]) - it1)
+        pa = -1.0 / (1 + 1j * ks_all[f])
+        pa_err.append(float(np.abs(P[f] - pa).max() / abs(pa)))
+        d = per_mesh.setdefault(str(n), {"instances": 0, "plain_seconds": 0.0, "iterations": [], "converged": 0,
+                                         "not_converged_k": [], "pressure_error_vs_analytic": []})
+        d["instances"] += 1
+        d["plain_seconds"] += dt
+        d["iterations"].append(int(it[f]))
+        if conv[f]:
+            d["converged"] += 1
+            d["pressure_error_vs_analytic"].append(pa_err[-1])
+        else:
+            d["not_converged_k"].append(round(float(ks_all[f]), 4))
+    for d in per_mesh.values():
+        its = np.array(d.pop("iterations"))
+        errs = d.pop("pressure_error_vs_analytic")
+        d["iterations_median"] = float(np.median(its))
+        d["iterations_max"] = int(its.max())
+        d["iterations_total"] = int(its.sum())
+        d["pressure_error_vs_analytic_median"] = float(np.median(errs)) if errs else None
+    out["per_mesh"] = per_mesh
+    out["plain_seconds"] = plain_s
     out["plain_solves_per_s"] = 256 / plain_s
     out["speedup_vs_plain_gpu"] = out["value"] / out["plain_solves_per_s"]
     out["batched_vs_plain_max_rel_difference"] = agree
+    out["iteration_difference_batched_minus_plain"] = {"max_abs": int(np.abs(it_diff).max()),
+                                                       "equal": int(np.sum(np.array(it_diff) == 0))}
+    # matrix bytes the solves stream: iterations + restarts, one n^2 complex64 matrix read each
+    mat_bytes = sum(8.0 * sizes[mesh_of[f]] ** 2 * (int(it[f]) + int(it[f]) // restart) for f in range(256))
+    gm = [v for k, v in prof.items() if k.startswith("persistent_gmres")]
+    if gm:
+        ms_ = gm[0][0]
+        out["persistent_gmres"] = {"ms": ms_, "matrix_bytes": mat_bytes,
+                                   "achieved_GBs": mat_bytes / (ms_ * 1e-3) / 1e9}
     ctx.close()
     print(json.dumps(out), flush=True)
 

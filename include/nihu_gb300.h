@@ -237,15 +237,47 @@ nihu_gb_status nihu_gb_assemble_sweep(nihu_gb_ctx *ctx, const nihu_gb_mesh *test
 /* Frequency sweep of the exterior CBIE (DLP - I/2) p_f = SLP q_f on one mesh
  * (the plain branch of nihu/applications/helmholtz/helmholtz_3d_coll.cpp:36-120
  * for every wave number): batched assembly (complex64, FP64 singular terms),
- * batched right-hand sides, and restarted GMRES on all wave numbers in
- * lockstep (batched FP32 matvecs, FP64 Arnoldi).  q is n x q_cols complex128
- * on the host (q_cols = 1 broadcasts one Neumann datum to every wave number,
- * else q_cols = nk); p receives n x nk complex128.  cycles / iters (may be
- * NULL) receive the restart cycles and the lockstep iterations;
- * rel_residuals (nk doubles, may be NULL) the final relative residuals. */
+ * batched right-hand sides, and one persistent GMRES launch over all wave
+ * numbers (nihu_gb_solve_batched; at most restart * max_cycles iterations
+ * each).  q is n x q_cols complex128 on the host (q_cols = 1 broadcasts one
+ * Neumann datum to every wave number, else q_cols = nk); p receives n x nk
+ * complex128.  cycles / iters (may be NULL) receive the largest restart-cycle
+ * and iteration counts over the wave numbers; rel_residuals (nk doubles, may
+ * be NULL) the final relative residual estimates. */
 nihu_gb_status nihu_gb_solve_sweep(nihu_gb_ctx *ctx, const nihu_gb_mesh *mesh, int family, const double *ks, int nk,
                                    int precision, const void *q, int q_cols, void *p, int restart, int max_cycles,
                                    double tol, int *cycles, int *iters, double *rel_residuals);
+
+/* Solve `count` independent dense systems A_f x_f = b_f of any sizes with
+ * restarted GMRES(restart) in ONE persistent kernel launch: each
+ * thread-block cluster solves one system at a time (FP32 complex matvec on
+ * its share of the rows, FP64 Arnoldi with CGS2, cluster reductions through
+ * distributed shared memory) and takes the next system from a device
+ * counter, largest first, with no host round trip between Krylov steps.
+ * Per system the stopping rules of nihu_gb_gmres apply with x0 = 0
+ * (nihu/fmm/GMRES.h:57-205 semantics, one call per system in the reference).
+ * A[f] (complex64, column-major, leading dimension lda[f]), b[f] and x[f]
+ * (complex128, length n[f]) are device pointers held in host arrays.
+ * iters, rel_residuals and converged (count entries each, may be NULL)
+ * receive the per-system results; returns NIHU_GB_ERR_NOT_CONVERGED, with
+ * every x written, when some system stopped at max_iters. */
+nihu_gb_status nihu_gb_solve_batched(nihu_gb_ctx *ctx, int count, const void *const *A, const int64_t *n,
+                                     const int64_t *lda, const void *const *b, void *const *x, int restart,
+                                     int max_iters, double tol, int *iters, double *rel_residuals, int *converged);
+
+/* Frequency sweep over several meshes of uneven size in one call: instance f
+ * solves the CBIE (DLP - I/2) p = SLP q on meshes[mesh_of[f]] at wave number
+ * ks[f] (helmholtz_3d_coll.cpp:36-120 once per instance in the reference).
+ * Each mesh's instances are assembled in one frequency-batched pass
+ * (nihu_gb_assemble_sweep), and all instances are solved by one persistent
+ * launch (nihu_gb_solve_batched).  q and p are complex128 host arrays holding
+ * the instances' columns back to back in instance order (instance f has
+ * the element count of its mesh).  iters, rel_residuals and converged (nk
+ * entries, may be NULL) as for nihu_gb_solve_batched. */
+nihu_gb_status nihu_gb_solve_sweep_batched(nihu_gb_ctx *ctx, int n_meshes, const nihu_gb_mesh *const *meshes,
+                                           int family, int nk, const double *ks, const int *mesh_of, int precision,
+                                           const void *q, void *p, int restart, int max_iters, double tol, int *iters,
+                                           double *rel_residuals, int *converged);
 
 /* Solve A x = b with restarted GMRES(restart) (nihu/fmm/GMRES.h:57-205
  * semantics: stop when |residual estimate| / |b - A x0| < tol).  A is n x n

@@ -10,11 +10,11 @@ from ._capi import (C64, C128, DEVICE, DLP, GEMM_BF16X9, GEMM_FP32, GEMM_TF32, H
 from .api import (Context, DeviceMesh, Mesh, constant_view, create_integral_operator, create_mesh, default_context,
                   dirac, gemm, gmres, helmholtz_3d_DLP_kernel, helmholtz_3d_SLP_kernel, identity_integral_operator,
                   laplace_3d_DLP_kernel, laplace_3d_SLP_kernel, lu_solve, matvec, pair_statistics, solve_cbie,
-                  solve_multi, solve_sweep)
+                  solve_batched, solve_multi, solve_sweep, solve_sweep_batched)
 from . import meshes
 
 __all__ = [
-    "C64", "C128", "DEVICE", "DLP", "GEMM_BF16X9", "GEMM_FP32", "GEMM_TF32", "gemm", "solve_multi", "solve_sweep", "HELMHOLTZ_3D", "HOST", "LAPLACE_3D", "QUAD_1", "REGULAR_FP32", "REGULAR_FP64",
+    "C64", "C128", "DEVICE", "DLP", "GEMM_BF16X9", "GEMM_FP32", "GEMM_TF32", "gemm", "solve_batched", "solve_multi", "solve_sweep", "solve_sweep_batched", "HELMHOLTZ_3D", "HOST", "LAPLACE_3D", "QUAD_1", "REGULAR_FP32", "REGULAR_FP64",
     "SLP", "TRIA_1", "InvalidArgumentError", "NihuError", "NotConvergedError", "OutOfRangeError", "lib", "Context",
     "DeviceMesh", "Mesh", "constant_view", "create_integral_operator", "create_mesh", "default_context", "dirac",
     "gmres", "helmholtz_3d_DLP_kernel", "helmholtz_3d_SLP_kernel", "identity_integral_operator",

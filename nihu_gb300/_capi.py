@@ -57,6 +57,8 @@ SIGNATURES = {
     "nihu_gb_solve_multi": (_i, [_vp, _vp, _i64, _i64, _vp, _vp, _i64, _i, _i, _i, _i, _d, _d, _ip, _ip, _dp, _i]),
     "nihu_gb_assemble_sweep": (_i, [_vp, _vp, _vp, _i, _i, _dp, _i, _i, _i, _vp, _vp, _i64, _i64]),
     "nihu_gb_solve_sweep": (_i, [_vp, _vp, _i, _dp, _i, _i, _vp, _i, _vp, _i, _i, _d, _ip, _ip, _dp]),
+    "nihu_gb_solve_batched": (_i, [_vp, _i, _vp, _vp, _vp, _vp, _vp, _i, _i, _d, _vp, _vp, _vp]),
+    "nihu_gb_solve_sweep_batched": (_i, [_vp, _i, _vp, _i, _i, _vp, _vp, _i, _vp, _vp, _i, _i, _d, _vp, _vp, _vp]),
     "nihu_gb_lu_solve": (_i, [_vp, _vp, _i64, _i64, _vp, _vp, _i]),
     "nihu_gb_solve_cbie": (_i, [_vp, _vp, _i, _d, _i, _i, _vp, _vp, _i, _i, _i, _d, _ip, _dp]),
 }

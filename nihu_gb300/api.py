@@ -436,8 +436,9 @@ def solve_cbie(mesh: Mesh, k: float, q, family: int = C.HELMHOLTZ_3D, dtype: int
 def solve_sweep(mesh: Mesh, ks, q, family: int = C.HELMHOLTZ_3D, precision: str = "fp32", restart: int = 30,
                 max_cycles: int = 50, tol: float = 1e-6, ctx: Context | None = None, check: bool = True):
     """(DLP - I/2) p_f = SLP q_f for every wave number ks[f] on one mesh, batched on
-    the GPU.  q: (n,) broadcast or (n, nk).  Returns (P (n x nk), cycles,
-    lockstep iterations, relative residuals).  With check=False an iteration
+    the GPU (frequency-batched assembly, one persistent GMRES launch).  q: (n,)
+    broadcast or (n, nk).  Returns (P (n x nk), largest restart-cycle count,
+    largest iteration count, relative residual estimates).  With check=False an iteration
     limit is not an error: the residuals tell which columns converged."""
     ctx = ctx or default_context()
     ks = np.ascontiguousarray(ks, dtype=np.float64)
@@ -457,6 +458,98 @@ def solve_sweep(mesh: Mesh, ks, q, family: int = C.HELMHOLTZ_3D, precision: str 
     if st != C.OK and (check or st != 6):
         ctx.check(st)
     return P, cyc.value, it.value, res
+
+
+def solve_batched(As, bs, restart: int = 50, max_iters: int = 1000, tol: float = 1e-6, ctx: Context | None = None,
+                  check: bool = True):
+    """Solve the independent systems As[f] x = bs[f] (any sizes) with GMRES in one
+    persistent GPU launch (nihu_gb_solve_batched).  As: complex64 matrices;
+    bs: vectors.  Returns (xs, iterations, relative residual estimates,
+    converged flags).  With check=False an iteration limit is not an error."""
+    ctx = ctx or default_context()
+    L = C.lib()
+    count = len(As)
+    if len(bs) != count:
+        raise ValueError("one right-hand side per matrix")
+    mats = [np.asfortranarray(A, dtype=np.complex64) for A in As]
+    rhs = [_c128(b) for b in bs]
+    for A, b in zip(mats, rhs):
+        if A.ndim != 2 or A.shape[0] != A.shape[1] or b.shape != (A.shape[0],):
+            raise ValueError("square matrices with matching right-hand sides expected")
+    ptrs = []
+
+    def dev(nbytes):
+        p = ctypes.c_void_p()
+        ctx.check(L.nihu_gb_device_alloc(ctx.handle, max(nbytes, 16), ctypes.byref(p)))
+        ptrs.append(p)
+        return p
+
+    try:
+        dA, db, dx = [], [], []
+        for A, b in zip(mats, rhs):
+            pa, pb, px = dev(A.nbytes), dev(b.nbytes), dev(b.nbytes)
+            ctx.check(L.nihu_gb_memcpy(ctx.handle, pa, C.DEVICE, A.ctypes.data, C.HOST, A.nbytes))
+            ctx.check(L.nihu_gb_memcpy(ctx.handle, pb, C.DEVICE, b.ctypes.data, C.HOST, b.nbytes))
+            dA.append(pa.value)
+            db.append(pb.value)
+            dx.append(px.value)
+        arr = lambda v: (ctypes.c_void_p * max(count, 1))(*v)
+        n = np.array([A.shape[0] for A in mats] or [0], dtype=np.int64)
+        lda = np.maximum(n, 1)
+        it = np.zeros(max(count, 1), np.int32)
+        rel = np.zeros(max(count, 1))
+        conv = np.zeros(max(count, 1), np.int32)
+        st = L.nihu_gb_solve_batched(ctx.handle, count, arr(dA), n.ctypes.data, lda.ctypes.data, arr(db), arr(dx),
+                                     restart, max_iters, tol, it.ctypes.data, rel.ctypes.data, conv.ctypes.data)
+        if st != C.OK and (check or st != 6):
+            ctx.check(st)
+        xs = []
+        for f, b in enumerate(rhs):
+            x = np.zeros_like(b)
+            ctx.check(L.nihu_gb_memcpy(ctx.handle, x.ctypes.data, C.HOST, dx[f], C.DEVICE, x.nbytes))
+            xs.append(x)
+        return xs, it[:count], rel[:count], conv[:count].astype(bool)
+    finally:
+        for p in ptrs:
+            L.nihu_gb_device_free(ctx.handle, p)
+
+
+def solve_sweep_batched(meshes, ks, mesh_of, q=None, family: int = C.HELMHOLTZ_3D, precision: str = "fp32",
+                        restart: int = 50, max_iters: int = 1000, tol: float = 1e-6, ctx: Context | None = None,
+                        check: bool = True):
+    """(DLP - I/2) p_f = SLP q_f for instance f on meshes[mesh_of[f]] at wave number
+    ks[f], all instances assembled per mesh in frequency batches and solved in
+    one persistent launch.  q: None (q = 1, the pulsating sphere) or a list of
+    per-instance vectors.  Returns (list of p_f, iterations, relative residual
+    estimates, converged flags)."""
+    ctx = ctx or default_context()
+    ks = np.ascontiguousarray(ks, dtype=np.float64)
+    mesh_of = np.ascontiguousarray(mesh_of, dtype=np.int32)
+    nk = len(ks)
+    if mesh_of.shape != (nk,):
+        raise ValueError("one mesh index per wave number")
+    dms = [m.device(ctx) for m in meshes]
+    sizes = [m.num_elements for m in meshes]
+    ns = [sizes[i] for i in mesh_of]
+    if q is None:
+        qf = np.ones(sum(ns), np.complex128)
+    else:
+        qf = np.concatenate([_c128(v) for v in q]) if nk else np.zeros(0, np.complex128)
+        if qf.shape != (sum(ns),):
+            raise ValueError("q: one vector per instance with its mesh's element count")
+    pf = np.zeros_like(qf)
+    handles = (ctypes.c_void_p * len(dms))(*[d.handle.value if hasattr(d.handle, "value") else d.handle for d in dms])
+    it = np.zeros(nk, np.int32)
+    rel = np.zeros(nk)
+    conv = np.zeros(nk, np.int32)
+    st = C.lib().nihu_gb_solve_sweep_batched(
+        ctx.handle, len(dms), handles, family, nk, ks.ctypes.data, mesh_of.ctypes.data,
+        C.REGULAR_FP64 if precision == "fp64" else C.REGULAR_FP32, qf.ctypes.data, pf.ctypes.data, restart, max_iters,
+        tol, it.ctypes.data, rel.ctypes.data, conv.ctypes.data)
+    if st != C.OK and (check or st != 6):
+        ctx.check(st)
+    out = np.split(pf, np.cumsum(ns)[:-1]) if nk else []
+    return out, it, rel, conv.astype(bool)
 
 
 def pair_statistics(test: Mesh, trial: Mesh, ctx: Context | None = None) -> np.ndarray:

@@ -61,6 +61,48 @@ __device__ __forceinline__ void eval_point(R rx, R ry, R rz, R wj, R nx, R ny, R
     }
 }
 
+// k-independent part of one quadrature point (frequency batches): the
+// distance and the SLP and DLP factors of eval_point
+template <typename R>
+struct PointGeom {
+    R r, gs, fd;
+};
+
+template <typename R>
+__device__ __forceinline__ PointGeom<R> point_geom(R rx, R ry, R rz, R wj, R nx, R ny, R nz, R ws, R wd)
+{
+    constexpr R INV4PI = R(1.0 / (4.0 * 3.14159265358979323846));
+    R r2 = rx * rx + ry * ry + rz * rz;
+    R rinv;
+    if constexpr (sizeof(R) == 4) rinv = rsqrtf(r2);
+    else rinv = rsqrt(r2);
+    R g = wj * rinv * INV4PI;
+    R rdn = (rx * nx + ry * ny + rz * nz) * rinv;
+    return {r2 * rinv, g * ws, -g * rinv * rdn * wd};
+}
+
+// the k-dependent part: the same sums as eval_point
+template <int FAM, typename R>
+__device__ __forceinline__ void point_freq(const PointGeom<R> &p, R k, R &sr, R &si, R &dr, R &di)
+{
+    if constexpr (FAM == FAM_HELMHOLTZ) {
+        R kr = k * p.r;
+        R s, c;
+        if constexpr (sizeof(R) == 4) sincos_2pi(kr * 0.159154943091895335769f, s, c);
+        else sincos(kr, &s, &c);
+        sr += p.gs * c;
+        si -= p.gs * s;
+        dr += p.fd * (c + kr * s);
+        di += p.fd * (kr * c - s);
+    } else {
+        sr += p.gs;
+        dr += p.fd;
+    }
+}
+
+// wave numbers evaluated together per pass over a pair's points
+constexpr int FREQ_TILE = 4;
+
 template <typename Out, typename R>
 __device__ __forceinline__ void store_entry(Out *p, R re, R im, R are, R aim, bool unit_alpha, int accumulate)
 {
@@ -87,7 +129,9 @@ __device__ __forceinline__ void store_entry(Out *p, R re, R im, R are, R aim, bo
 // difference of a far pair.
 constexpr float Q_FAR = 249.64f * (1.0f + 1e-4f);
 
-template <typename R, typename Out, int FAM, int OPS>
+// BATCH: frequency batch (a.nk > 1), a separate instantiation so that the
+// single wave number kernel carries none of its code
+template <typename R, typename Out, int FAM, int OPS, bool BATCH>
 __global__ void __launch_bounds__(REG_THREADS) k_regular(RegularArgs a)
 {
     __shared__ float4 s_hi[REG_COLS], s_lo[REG_COLS], s_p0[REG_COLS];
@@ -151,14 +195,23 @@ __global__ void __launch_bounds__(REG_THREADS) k_regular(RegularArgs a)
             if (__all_sync(0xffffffffu, q > Q_FAR)) {
                 const float4 p = s_p0[c];
                 const int64_t off = (int64_t)(j - a.j0) * a.ld + i;
-                for (int f = 0; f < a.nk; ++f) {
-                    const R kf = a.nk > 1 ? a.ks32[f] : k;
+                if constexpr (BATCH) {
+                    const PointGeom<float> gm = point_geom<float>(fx, fy, fz, p.x, p.y, p.z, p.w, R(DO_S), R(DO_D));
+                    for (int f = 0; f < a.nk; ++f) {
+                        R sr = 0, si = 0, dr = 0, di = 0;
+                        point_freq<FAM, float>(gm, a.ks32[f], sr, si, dr, di);
+                        if (row_ok) {
+                            const int64_t fo = off + f * a.mat_stride;
+                            if (DO_S) store_entry(out_s + fo, sr, si, are, aim, unit_alpha, accumulate);
+                            if (DO_D) store_entry(out_d + fo, dr, di, are, aim, unit_alpha, accumulate);
+                        }
+                    }
+                } else {
                     R sr = 0, si = 0, dr = 0, di = 0;
-                    eval_point<FAM, float>(fx, fy, fz, p.x, p.y, p.z, p.w, kf, R(DO_S), R(DO_D), sr, si, dr, di);
+                    eval_point<FAM, float>(fx, fy, fz, p.x, p.y, p.z, p.w, k, R(DO_S), R(DO_D), sr, si, dr, di);
                     if (row_ok) {
-                        const int64_t fo = off + f * a.mat_stride;
-                        if (DO_S) store_entry(out_s + fo, sr, si, are, aim, unit_alpha, accumulate);
-                        if (DO_D) store_entry(out_d + fo, dr, di, are, aim, unit_alpha, accumulate);
+                        if (DO_S) store_entry(out_s + off, sr, si, are, aim, unit_alpha, accumulate);
+                        if (DO_D) store_entry(out_d + off, dr, di, are, aim, unit_alpha, accumulate);
                     }
                 }
                 continue;
@@ -178,50 +231,91 @@ __global__ void __launch_bounds__(REG_THREADS) k_regular(RegularArgs a)
         const int npd = level_npts(tnc, par, ld);
         const int n_eval = ls == ld ? nps : nps + npd;
         const int64_t base = ((int64_t)j * 2 + par) * SLOTS;
-        for (int f = 0; f < a.nk; ++f) {
-        R kf;
-        if constexpr (sizeof(R) == 4) kf = a.nk > 1 ? a.ks32[f] : k;
-        else kf = a.nk > 1 ? a.ks[f] : k;
-        R sr = 0, si = 0, dr = 0, di = 0;
-        for (int q = 0; q < n_eval; ++q) {
-            int slot;
-            R ws, wd;
-            if (ls == ld) { slot = level_slot0(ls) + q; ws = R(DO_S); wd = R(DO_D); }
-            else if (q < nps) { slot = level_slot0(ls) + q; ws = R(1); wd = R(0); }
-            else { slot = level_slot0(ld) + q - nps; ws = R(0); wd = R(1); }
-            if constexpr (sizeof(R) == 4) {
-                const float4 y = __ldg(trial.pts32 + 2 * (base + slot));
-                const float4 n = __ldg(trial.pts32 + 2 * (base + slot) + 1);
-                // level-0 point: the trial centre; use the accurate hi/lo difference
-                const bool centre = slot == 0;
-                eval_point<FAM, float>(centre ? dx : y.x - x0, centre ? dy : y.y - x1, centre ? dz : y.z - x2, y.w,
-                                       n.x, n.y, n.z, kf, ws, wd, sr, si, dr, di);
-            } else {
-                const double *y = trial.pts64 + 8 * (base + slot);
-                eval_point<FAM, double>(y[0] - x0, y[1] - x1, y[2] - x2, y[3], y[4], y[5], y[6], kf, ws, wd, sr,
-                                        si, dr, di);
+        if constexpr (BATCH) {
+            // frequency batch: each point's geometry once per tile of wave numbers
+            for (int f0 = 0; f0 < a.nk; f0 += FREQ_TILE) {
+                R kf[FREQ_TILE], sr[FREQ_TILE], si[FREQ_TILE], dr[FREQ_TILE], di[FREQ_TILE];
+#pragma unroll
+                for (int u = 0; u < FREQ_TILE; ++u) {
+                    if constexpr (sizeof(R) == 4) kf[u] = f0 + u < a.nk ? a.ks32[f0 + u] : 0.0f;
+                    else kf[u] = f0 + u < a.nk ? a.ks[f0 + u] : 0.0;
+                    sr[u] = si[u] = dr[u] = di[u] = 0;
+                }
+                for (int q = 0; q < n_eval; ++q) {
+                    int slot;
+                    R ws, wd;
+                    if (ls == ld) { slot = level_slot0(ls) + q; ws = R(DO_S); wd = R(DO_D); }
+                    else if (q < nps) { slot = level_slot0(ls) + q; ws = R(1); wd = R(0); }
+                    else { slot = level_slot0(ld) + q - nps; ws = R(0); wd = R(1); }
+                    PointGeom<R> gm;
+                    if constexpr (sizeof(R) == 4) {
+                        const float4 y = __ldg(trial.pts32 + 2 * (base + slot));
+                        const float4 n = __ldg(trial.pts32 + 2 * (base + slot) + 1);
+                        const bool centre = slot == 0;
+                        gm = point_geom<float>(centre ? dx : y.x - x0, centre ? dy : y.y - x1,
+                                               centre ? dz : y.z - x2, y.w, n.x, n.y, n.z, ws, wd);
+                    } else {
+                        const double *y = trial.pts64 + 8 * (base + slot);
+                        gm = point_geom<double>(y[0] - x0, y[1] - x1, y[2] - x2, y[3], y[4], y[5], y[6], ws, wd);
+                    }
+#pragma unroll
+                    for (int u = 0; u < FREQ_TILE; ++u) point_freq<FAM, R>(gm, kf[u], sr[u], si[u], dr[u], di[u]);
+                }
+#pragma unroll
+                for (int u = 0; u < FREQ_TILE; ++u) {
+                    if (f0 + u >= a.nk) break;
+                    const int64_t off = (int64_t)(j - a.j0) * a.ld + i + (f0 + u) * a.mat_stride;
+                    if (DO_S) store_entry(out_s + off, sr[u], si[u], are, aim, unit_alpha, accumulate);
+                    if (DO_D) store_entry(out_d + off, dr[u], di[u], are, aim, unit_alpha, accumulate);
+                }
             }
-        }
-        const int64_t off = (int64_t)(j - a.j0) * a.ld + i + f * a.mat_stride;
-        if (DO_S) store_entry(out_s + off, sr, si, are, aim, unit_alpha, accumulate);
-        if (DO_D) store_entry(out_d + off, dr, di, are, aim, unit_alpha, accumulate);
+        } else {
+            R sr = 0, si = 0, dr = 0, di = 0;
+            for (int q = 0; q < n_eval; ++q) {
+                int slot;
+                R ws, wd;
+                if (ls == ld) { slot = level_slot0(ls) + q; ws = R(DO_S); wd = R(DO_D); }
+                else if (q < nps) { slot = level_slot0(ls) + q; ws = R(1); wd = R(0); }
+                else { slot = level_slot0(ld) + q - nps; ws = R(0); wd = R(1); }
+                if constexpr (sizeof(R) == 4) {
+                    const float4 y = __ldg(trial.pts32 + 2 * (base + slot));
+                    const float4 n = __ldg(trial.pts32 + 2 * (base + slot) + 1);
+                    // level-0 point: the trial centre; use the accurate hi/lo difference
+                    const bool centre = slot == 0;
+                    eval_point<FAM, float>(centre ? dx : y.x - x0, centre ? dy : y.y - x1, centre ? dz : y.z - x2, y.w,
+                                           n.x, n.y, n.z, k, ws, wd, sr, si, dr, di);
+                } else {
+                    const double *y = trial.pts64 + 8 * (base + slot);
+                    eval_point<FAM, double>(y[0] - x0, y[1] - x1, y[2] - x2, y[3], y[4], y[5], y[6], k, ws, wd, sr,
+                                            si, dr, di);
+                }
+            }
+            const int64_t off = (int64_t)(j - a.j0) * a.ld + i;
+            if (DO_S) store_entry(out_s + off, sr, si, are, aim, unit_alpha, accumulate);
+            if (DO_D) store_entry(out_d + off, dr, di, are, aim, unit_alpha, accumulate);
         }
     }
 }
 
-template <typename R, typename Out, int FAM>
+template <typename R, typename Out, int FAM, bool BATCH>
 static void launch_ops(const RegularArgs &a, dim3 grid, cudaStream_t s)
 {
-    if (a.ops == OP_SLP) k_regular<R, Out, FAM, OP_SLP><<<grid, REG_THREADS, 0, s>>>(a);
-    else if (a.ops == OP_DLP) k_regular<R, Out, FAM, OP_DLP><<<grid, REG_THREADS, 0, s>>>(a);
-    else k_regular<R, Out, FAM, OP_SLP | OP_DLP><<<grid, REG_THREADS, 0, s>>>(a);
+    if (a.ops == OP_SLP) k_regular<R, Out, FAM, OP_SLP, BATCH><<<grid, REG_THREADS, 0, s>>>(a);
+    else if (a.ops == OP_DLP) k_regular<R, Out, FAM, OP_DLP, BATCH><<<grid, REG_THREADS, 0, s>>>(a);
+    else k_regular<R, Out, FAM, OP_SLP | OP_DLP, BATCH><<<grid, REG_THREADS, 0, s>>>(a);
 }
 
 template <typename R, typename Out>
 static void launch_fam(const RegularArgs &a, dim3 grid, cudaStream_t s)
 {
-    if (a.family == FAM_HELMHOLTZ) launch_ops<R, Out, FAM_HELMHOLTZ>(a, grid, s);
-    else launch_ops<R, Out, FAM_LAPLACE>(a, grid, s);
+    const bool batch = a.nk > 1;
+    if (a.family == FAM_HELMHOLTZ) {
+        if (batch) launch_ops<R, Out, FAM_HELMHOLTZ, true>(a, grid, s);
+        else launch_ops<R, Out, FAM_HELMHOLTZ, false>(a, grid, s);
+    } else {
+        if (batch) launch_ops<R, Out, FAM_LAPLACE, true>(a, grid, s);
+        else launch_ops<R, Out, FAM_LAPLACE, false>(a, grid, s);
+    }
 }
 
 cudaError_t launch_assemble_regular(const RegularArgs &a, cudaStream_t s)

@@ -25,6 +25,8 @@
 //      (nihu/library/nearly_singular_collocational.hpp:87-198, inverse_mapping.hpp:52-112)
 //  near, quad, Helmholtz DLP: Telles-transformed 16x16 Gauss
 //      (nihu/library/nearly_singular_collocational_telles.hpp:85-110, telles_1987.hpp:44-113)
+// A frequency batch on a triangle evaluates the same 42-point dynamic sums
+// through their power series in k (near_moments / near_series below).
 #include "geom.cuh"
 #include "kernels.h"
 
@@ -301,6 +303,143 @@ __device__ void near_plane(const Elem64 &e, int fam, double k, const double x0[3
     near_static(e, x0, do_s, do_d, a);
 }
 
+// ------------------------------------------------ frequency-batch moments
+//
+// With W_p = w_p J_p / (4 pi) and x = k r_p, the 42-point dynamic sums of a
+// triangle are power series in k with k-independent coefficients (term by
+// term expansions of e^{-ix} - 1 and 1 - (1 + ix) e^{-ix}):
+//   SLP(k) = sum_{j>=1} (-ik)^j / j!        S_j,  S_j = sum_p W_p r_p^{j-1}
+//   DLP(k) = sum_{j>=2} (-ik)^j (j - 1)/j!  T_j,  T_j = sum_p W_p (r_p.n) r_p^{j-3}
+// The moments are formed once per pair; each wave number then costs one
+// Horner evaluation in u = -k^2 ((-ik)^{2m} = u^m, (-ik)^{2m+1} = -ik u^m)
+// instead of 42 complex exponentials.  The series stops at the first J with
+// x^{J+1} / J! < 1e-15 for x = k_max max_p r_p, which bounds the truncation
+// of every point's term by 1e-15 times that point's static contribution.
+
+constexpr int MOM_J = 64;  // most series terms (shared memory per thread: 2 x MOM_J doubles)
+constexpr size_t MOM_SMEM = 2 * sizeof(double) * MOM_J * SING_THREADS;
+
+struct InvFactorials {
+    double v[MOM_J];
+    constexpr InvFactorials() : v()
+    {
+        double f = 1.0;
+        for (int j = 0; j < MOM_J; ++j) {
+            if (j > 0) f *= j;
+            v[j] = 1.0 / f;
+        }
+    }
+};
+__device__ constexpr InvFactorials INV_FACT{};
+
+__device__ __forceinline__ void unit_normal_center(const Elem64 &e, double en[3])
+{
+    double xi, eta;
+    domain_center(e.nc, xi, eta);
+    enormal(e, xi, eta, en);
+    const double nn = 1.0 / norm3(en);
+    for (int d = 0; d < 3; ++d) en[d] *= nn;
+}
+
+// coefficients c^S_j = S_j / j! at mS[j * SING_THREADS] and, when en is
+// given, c^T_j = (j-1) T_j / j! at mT[j * SING_THREADS], j = 0..J, over the np
+// points that pts(p, y, W) yields (W = w J / (4 pi)); returns J, or 0 when
+// MOM_J terms do not reach the bound (the caller then sums the points per
+// wave number)
+template <class PointFn>
+__device__ int series_moments(int np, PointFn pts, const double x0[3], const double *en, double kmax, double *mS,
+                              double *mT)
+{
+    double r2max = 0.0;
+    for (int p = 0; p < np; ++p) {
+        double y[3], W;
+        pts(p, y, W);
+        const double r0 = y[0] - x0[0], r1 = y[1] - x0[1], r2 = y[2] - x0[2];
+        r2max = fmax(r2max, r0 * r0 + r1 * r1 + r2 * r2);
+    }
+    const double x = kmax * sqrt(r2max);
+    int J = 1;
+    double t = x * x;  // x^{J+1} / J!
+    while (t >= 1e-15) {
+        if (J == MOM_J - 1) return 0;
+        ++J;
+        t *= x / J;
+    }
+    for (int j = 0; j <= J; ++j) {
+        mS[j * SING_THREADS] = 0.0;
+        if (en) mT[j * SING_THREADS] = 0.0;
+    }
+    for (int p = 0; p < np; ++p) {
+        double y[3], ws;
+        pts(p, y, ws);
+        const double r0 = y[0] - x0[0], r1 = y[1] - x0[1], r2 = y[2] - x0[2];
+        const double rr = r0 * r0 + r1 * r1 + r2 * r2;
+        double pw = 1.0;  // r^{j-1}
+        if (en) {
+            // nearly singular: the point never coincides with x0
+            const double rinv = rsqrt(rr), r = rr * rinv;
+            const double wd = ws * ((r0 * en[0] + r1 * en[1] + r2 * en[2]) * rinv);  // W (r.n) / r
+            for (int j = 1; j <= J; ++j) {
+                mS[j * SING_THREADS] += ws * pw;
+                if (j < J) mT[(j + 1) * SING_THREADS] += wd * pw;
+                pw *= r;
+            }
+        } else {
+            // self rules may hold the collocation point itself (r = 0, only r^0 survives)
+            const double r = sqrt(rr);
+            for (int j = 1; j <= J; ++j) {
+                mS[j * SING_THREADS] += ws * pw;
+                pw *= r;
+            }
+        }
+    }
+    for (int j = 1; j <= J; ++j) {
+        mS[j * SING_THREADS] *= INV_FACT.v[j];
+        if (en) mT[j * SING_THREADS] *= (j - 1) * INV_FACT.v[j];
+    }
+    return J;
+}
+
+// the moments of a triangle's 42-point dynamic rule (table of (y, w J))
+__device__ int near_moments(const Elem64 &e, const Pt4 *__restrict__ pts, const double x0[3], double kmax,
+                            double *mS, double *mT)
+{
+    double en[3];
+    unit_normal_center(e, en);
+    return series_moments(
+        42,
+        [&](int p, double y[3], double &W) {
+            const Pt4 v = pts[p];
+            y[0] = v.x;
+            y[1] = v.y;
+            y[2] = v.z;
+            W = v.w * INV_FOUR_PI;
+        },
+        x0, en, kmax, mS, mT);
+}
+
+// the dynamic sums at wave number k from the coefficients of near_moments
+__device__ __forceinline__ void near_series(int J, double k, const double *mS, const double *mT, bool do_s,
+                                            bool do_d, Acc &a)
+{
+    const double u = -k * k;
+    const int je = J & ~1, jo = (J & 1) ? J : J - 1;
+    if (do_s) {
+        double ev = 0.0, od = 0.0;
+        for (int j = je; j >= 2; j -= 2) ev = fma(ev, u, mS[j * SING_THREADS]);
+        for (int j = jo; j >= 1; j -= 2) od = fma(od, u, mS[j * SING_THREADS]);
+        a.sr += u * ev;
+        a.si -= k * od;
+    }
+    if (do_d) {
+        double ev = 0.0, od = 0.0;
+        for (int j = je; j >= 2; j -= 2) ev = fma(ev, u, mT[j * SING_THREADS]);
+        for (int j = jo; j >= 1; j -= 2) od = fma(od, u, mT[j * SING_THREADS]);
+        a.dr += u * ev;
+        a.di -= k * od;
+    }
+}
+
 // ------------------------------------------------------------ inverse mapping
 
 // Newton iteration (nihu/core/inverse_mapping.hpp:52-112).  Records the first
@@ -510,6 +649,50 @@ __device__ __forceinline__ double sinc_ref(double x)
     return 1.0 - x * x / 6.0 * (1.0 - x * x / 20.0);
 }
 
+// (e^{-ikr} - 1) / (4 pi r) over a flat triangle with the 13-point degree-7
+// rule, as -ik e^{-ikr/2} sinc(kr/2) / (4 pi)
+__device__ void self_tria_dynamic(const Elem64 &e, double k, const double x0[3], Acc &a)
+{
+    double e1[3], e2[3], nt[3];
+    for (int d = 0; d < 3; ++d) { e1[d] = e.c[1][d] - e.c[0][d]; e2[d] = e.c[2][d] - e.c[0][d]; }
+    cross3(e1, e2, nt);
+    const double J = norm3(nt);
+    double dr = 0.0, di = 0.0;
+    for (int p = 0; p < 13; ++p) {
+        double xi, eta, w;
+        tri_pt(7, p, xi, eta, w);
+        double rv[3];
+        for (int d = 0; d < 3; ++d) rv[d] = e.c[0][d] + xi * e1[d] + eta * e2[d] - x0[d];
+        double r = norm3(rv);
+        double s, c;
+        sincos_bounded(k * r / 2.0, &s, &c, false);
+        double sc = sinc_ref(k * r / 2.0);
+        double wj = w * J;
+        dr += -k * s * sc * wj;
+        di += -k * c * sc * wj;
+    }
+    a.sr += dr * INV_FOUR_PI;
+    a.si += di * INV_FOUR_PI;
+}
+
+// the moments of the same 13-point rule (SLP series only)
+__device__ int self_tria_moments(const Elem64 &e, const double x0[3], double kmax, double *mS)
+{
+    double e1[3], e2[3], nt[3];
+    for (int d = 0; d < 3; ++d) { e1[d] = e.c[1][d] - e.c[0][d]; e2[d] = e.c[2][d] - e.c[0][d]; }
+    cross3(e1, e2, nt);
+    const double J = norm3(nt) * INV_FOUR_PI;
+    return series_moments(
+        13,
+        [&](int p, double y[3], double &W) {
+            double xi, eta, w;
+            tri_pt(7, p, xi, eta, w);
+            for (int d = 0; d < 3; ++d) y[d] = e.c[0][d] + xi * e1[d] + eta * e2[d];
+            W = w * J;
+        },
+        x0, nullptr, kmax, mS, nullptr);
+}
+
 __device__ void self_tria(const Elem64 &e, int fam, double k, const double x0[3], Acc &a)
 {
     double st = self_static(e, x0);
@@ -589,9 +772,13 @@ __device__ __forceinline__ void store64(Out *p, double re, double im, double are
     *p = o;
 }
 
-template <typename Out>
-__global__ void __launch_bounds__(SING_THREADS) k_singular(RegularArgs a, NearList near, int *err)
+// BATCH: frequency batch (a.nk > 1), a separate kernel so that the single
+// wave number kernel carries none of its code.
+template <typename Out, bool BATCH>
+__device__ __forceinline__ void singular_pairs(const RegularArgs &a, const NearList &near, int *err)
 {
+    // frequency batches: per-thread series coefficients (MOM_SMEM bytes, launched only with nk > 1)
+    extern __shared__ double s_mom[];
     const int64_t p_begin = near.col_ptr ? near.col_ptr[a.j0] : 0;
     const int64_t p_end = near.col_ptr ? near.col_ptr[a.j1] : 0;
     const int64_t n_near = p_end - p_begin;
@@ -631,21 +818,38 @@ __global__ void __launch_bounds__(SING_THREADS) k_singular(RegularArgs a, NearLi
         Elem64 e;
         load_elem(a.trial, j, e);
         const int64_t off = (int64_t)(j - a.j0) * a.ld + i;
-        if (a.nk > 1 && e.nc == 3) {
-            // frequency batch on a triangle: the k-independent static part once,
-            // the dynamic part (or the self term) per wave number
+        if (BATCH && e.nc == 3) {
+            // frequency batch on a triangle: the k-independent static part and
+            // the moments of the dynamic part once, then per wave number the
+            // series (or the self term)
             Acc st;
-            if (!self) near_static(e, x0, do_s, do_d, st);
+            int J = 0;
+            double *mS = s_mom + threadIdx.x, *mT = s_mom + MOM_J * SING_THREADS + threadIdx.x;
+            const Pt4 *pts = a.trial.dyn42 + 42 * (int64_t)j;
+            if (!self) {
+                near_static(e, x0, do_s, do_d, st);
+                if (fam == FAM_HELMHOLTZ) J = near_moments(e, pts, x0, a.k_absmax, mS, mT);
+            } else if (do_s) {
+                st.sr = self_static(e, x0) * INV_FOUR_PI;
+                if (fam == FAM_HELMHOLTZ) J = self_tria_moments(e, x0, a.k_absmax, mS);
+            }
             for (int f = 0; f < a.nk; ++f) {
                 const double kf = a.ks[f];
                 Acc acc;
                 if (self) {
-                    if (do_s) self_tria(e, fam, kf, x0, acc);
+                    if (do_s) {
+                        acc = st;
+                        if (fam == FAM_HELMHOLTZ) {
+                            if (J) near_series(J, kf, mS, mT, true, false, acc);
+                            else self_tria_dynamic(e, kf, x0, acc);
+                        }
+                    }
                 } else {
                     acc = st;
-                    if (fam == FAM_HELMHOLTZ)
-                        near_dynamic(e, kf, x0, do_s, do_d, acc, a.trial.dyn42 + 42 * (int64_t)j,
-                                     kf * 3.0 * a.trial_size_max <= 0.75);
+                    if (fam == FAM_HELMHOLTZ) {
+                        if (J) near_series(J, kf, mS, mT, do_s, do_d, acc);
+                        else near_dynamic(e, kf, x0, do_s, do_d, acc, pts, kf * 3.0 * a.trial_size_max <= 0.75);
+                    }
                 }
                 const int64_t fo = off + f * a.mat_stride;
                 if (do_s) store64(out_s + fo, acc.sr, acc.si, a.alpha_re, a.alpha_im, a.accumulate);
@@ -692,6 +896,22 @@ __global__ void __launch_bounds__(SING_THREADS) k_singular(RegularArgs a, NearLi
     }
 }
 
+template <typename Out>
+__global__ void __launch_bounds__(SING_THREADS) k_singular(RegularArgs a, NearList near, int *err)
+{
+    singular_pairs<Out, false>(a, near, err);
+}
+
+// held to 128 registers (its code alone would take about 166), so that the
+// concurrent regular kernel keeps three of its blocks on every SM beside this
+// kernel's one; the single wave number kernel comes to 128 by itself, where
+// the occupancy hint would only change its schedule
+template <typename Out>
+__global__ void __launch_bounds__(SING_THREADS, 4) k_singular_batch(RegularArgs a, NearList near, int *err)
+{
+    singular_pairs<Out, true>(a, near, err);
+}
+
 cudaError_t launch_assemble_singular(const RegularArgs &a, const NearList &near, int *err, cudaStream_t s)
 {
     int dev = 0, sms = 148;
@@ -703,8 +923,21 @@ cudaError_t launch_assemble_singular(const RegularArgs &a, const NearList &near,
     int64_t total = (near.col_ptr ? near.nnz : 0) + (a.same_mesh ? (a.j1 - a.j0) : 0);
     int64_t want = (total + SING_THREADS - 1) / SING_THREADS;
     int blocks = (int)max((int64_t)1, min(want, (int64_t)sms));
-    if (a.dtype == 0) k_singular<float2><<<blocks, SING_THREADS, 0, s>>>(a, near, err);
-    else k_singular<double2><<<blocks, SING_THREADS, 0, s>>>(a, near, err);
+    size_t smem = 0;
+    if (a.nk > 1) {
+        smem = MOM_SMEM;
+        cudaError_t e = a.dtype == 0
+                            ? cudaFuncSetAttribute(k_singular_batch<float2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                   (int)MOM_SMEM)
+                            : cudaFuncSetAttribute(k_singular_batch<double2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                   (int)MOM_SMEM);
+        if (e != cudaSuccess) return e;
+        if (a.dtype == 0) k_singular_batch<float2><<<blocks, SING_THREADS, smem, s>>>(a, near, err);
+        else k_singular_batch<double2><<<blocks, SING_THREADS, smem, s>>>(a, near, err);
+    } else {
+        if (a.dtype == 0) k_singular<float2><<<blocks, SING_THREADS, 0, s>>>(a, near, err);
+        else k_singular<double2><<<blocks, SING_THREADS, 0, s>>>(a, near, err);
+    }
     return cudaGetLastError();
 }
 

@@ -7,6 +7,7 @@
 #include <functional>
 #include <map>
 #include <mutex>
+#include <queue>
 #include <string>
 #include <utility>
 #include <vector>
@@ -16,6 +17,7 @@
 #include "../../include/nihu_gb300.h"
 #include "kernels.h"
 #include "linalg.h"
+#include "solve_persistent.h"
 
 using namespace nihu;
 
@@ -1412,10 +1414,288 @@ extern "C" nihu_gb_status nihu_gb_assemble_sweep(nihu_gb_ctx *ctx, const nihu_gb
     a.j0 = 0;
     a.j1 = (int)trial->n;
     a.nk = nk;
+    for (int f = 0; f < nk; ++f) a.k_absmax = std::max(a.k_absmax, std::fabs(ks[f]));
     a.mat_stride = mat_stride;
     if ((st = upload_ks(ctx, ks, nk, &a.ks, &a.ks32))) return st;
     if ((st = assemble_panel(ctx, a, nl))) return st;
     return check_flag(ctx);
+}
+
+// ------------------------------------------------ persistent batched GMRES
+
+namespace {
+
+struct BatchSystem {
+    const void *A;  // complex64, column-major
+    int64_t n, lda;
+    const double2 *b;
+    double2 *x;
+    double work;  // processing order: larger first
+};
+
+// one persistent launch over all systems; per-system outputs on the host (may be NULL)
+nihu_gb_status solve_batched_device(nihu_gb_ctx *ctx, const std::vector<BatchSystem> &sys, int restart, int max_iters,
+                                    double tol, int *iters, double *rel, int *converged)
+{
+    const int count = (int)sys.size();
+    if (count == 0) return NIHU_GB_OK;
+    nihu_gb_status st;
+    int64_t n_max = 1;
+    for (const BatchSystem &s : sys) n_max = std::max(n_max, s.n);
+    const int m = (int)std::max<int64_t>(1, std::min<int64_t>(restart, n_max));
+    int smem_optin = 0, l2 = 0;
+    cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, ctx->device);
+    cudaDeviceGetAttribute(&l2, cudaDevAttrL2CacheSize, ctx->device);
+    // Cluster size from a launch model (results do not depend on it): the
+    // systems, largest first, go to the earliest free of the clusters that
+    // run at once; a system of nb 128-row blocks keeps min(C, nb) CTAs busy
+    // for n^2 / min(C, nb) time units, slowed in proportion when more CTAs
+    // stream at once than HBM feeds (about 60 GB/s per 512-thread CTA).
+    int mem_khz = 0, bus_bits = 0;
+    cudaDeviceGetAttribute(&mem_khz, cudaDevAttrMemoryClockRate, ctx->device);
+    cudaDeviceGetAttribute(&bus_bits, cudaDevAttrGlobalMemoryBusWidth, ctx->device);
+    const double hbm_gbs = 2.0 * mem_khz * 1e3 * bus_bits / 8.0 / 1e9;
+    const double feeding = std::max(8.0, 0.8 * hbm_gbs / 60.0);  // CTAs that saturate HBM
+    std::vector<int> by_work(count);
+    for (int f = 0; f < count; ++f) by_work[f] = f;
+    std::stable_sort(by_work.begin(), by_work.end(), [&](int x, int y) { return sys[x].work > sys[y].work; });
+    int cluster = 0, clusters = 0;
+    size_t smem = 0;
+    double best = 0.0;
+    for (int c : {2, 4, 8, 16, 1}) {
+        if (persistent_smem_layout((int)n_max, c, m).total > (size_t)smem_optin) continue;
+        int act = 0;
+        size_t sm_bytes = 0;
+        if (persistent_gmres_plan((int)n_max, m, c, count, &act, &sm_bytes) != cudaSuccess) {
+            cudaGetLastError();
+            continue;
+        }
+        const double rate = std::min(1.0, feeding / ((double)act * c));
+        std::priority_queue<double, std::vector<double>, std::greater<double>> free_at;
+        for (int q = 0; q < act; ++q) free_at.push(0.0);
+        double makespan = 0.0;
+        for (int f : by_work) {
+            const BatchSystem &s = sys[f];
+            const double nb = (double)((s.n + 127) / 128);
+            double t = free_at.top();
+            free_at.pop();
+            t += (double)s.n * (double)s.n / (std::max(1.0, std::min((double)c, nb)) * rate);
+            free_at.push(t);
+            makespan = std::max(makespan, t);
+        }
+        // within 3 %, the later candidate (larger clusters) loses to the earlier
+        if (!cluster || makespan < 0.97 * best) {
+            best = makespan;
+            cluster = c;
+        }
+    }
+    if (!cluster)
+        return fail(ctx, NIHU_GB_ERR_INVALID_ARGUMENT, "batched GMRES: system or restart too large for shared memory");
+    CK(persistent_gmres_plan((int)n_max, m, cluster, count, &clusters, &smem));
+    void *pitems, *porder, *pV, *pout;
+    if ((st = scratch(ctx, "pg_items", sizeof(PersistentItem) * (size_t)count, &pitems))) return st;
+    if ((st = scratch(ctx, "pg_order", sizeof(int) * (size_t)count, &porder))) return st;
+    if ((st = scratch(ctx, "pg_V", 16 * (size_t)clusters * (m + 1) * n_max, &pV))) return st;
+    // counter | iters[count] | converged[count] | (8-aligned) rel[count]
+    const size_t off_rel = ((sizeof(int) * (1 + 2 * (size_t)count)) + 7) & ~(size_t)7;
+    if ((st = scratch(ctx, "pg_out", off_rel + 8 * (size_t)count, &pout))) return st;
+    std::vector<PersistentItem> items(count);
+    std::vector<int> order(count);
+    for (int f = 0; f < count; ++f) {
+        const BatchSystem &s = sys[f];
+        PersistentItem &it = items[f];
+        it.A = (const float2 *)s.A;
+        it.lda = s.lda;
+        it.b = s.b;
+        it.x = s.x;
+        it.n = (int)s.n;
+        it.vec = (s.n % 2 == 0) && (s.lda % 2 == 0) && ((reinterpret_cast<uintptr_t>(s.A) & 15) == 0);
+        it.stream = 8.0 * (double)s.n * (double)s.n * std::min(count, clusters) > 0.5 * l2;
+        it.pad = 0;
+        order[f] = f;
+    }
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return sys[a].work > sys[b].work; });
+    int *dout = (int *)pout;
+    PersistentArgs a;
+    a.items = (const PersistentItem *)pitems;
+    a.order = (const int *)porder;
+    a.count = count;
+    a.n_max = (int)n_max;
+    a.restart = m;
+    a.max_iters = max_iters;
+    a.tol = tol;
+    a.V = (double2 *)pV;
+    a.counter = dout;
+    a.iters = dout + 1;
+    a.converged = dout + 1 + count;
+    a.rel = (double *)((char *)pout + off_rel);
+    CK(cudaMemcpyAsync(pitems, items.data(), sizeof(PersistentItem) * count, cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaMemcpyAsync(porder, order.data(), sizeof(int) * count, cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaMemsetAsync(dout, 0, sizeof(int), ctx->stream));
+    {
+        // the phase name records the launch shape: clusters x CTAs per cluster
+        const std::string name = "persistent_gmres[" + std::to_string(clusters) + "x" + std::to_string(cluster) + "]";
+        Phase ph(ctx, name.c_str());
+        CK(launch_persistent_gmres(a, cluster, clusters, smem, ctx->stream));
+    }
+    ctx->launches += 1;
+    std::vector<int> hi(2 * (size_t)count);
+    std::vector<double> hr(count);
+    CK(cudaMemcpyAsync(hi.data(), dout + 1, sizeof(int) * 2 * count, cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaMemcpyAsync(hr.data(), a.rel, 8 * (size_t)count, cudaMemcpyDeviceToHost, ctx->stream));
+    if ((st = sync(ctx))) return st;
+    bool all = true;
+    for (int f = 0; f < count; ++f) {
+        if (iters) iters[f] = hi[f];
+        if (converged) converged[f] = hi[count + f];
+        if (rel) rel[f] = hr[f];
+        all = all && hi[count + f];
+    }
+    if (!all) return fail(ctx, NIHU_GB_ERR_NOT_CONVERGED, "batched GMRES: some systems did not reach the tolerance");
+    return NIHU_GB_OK;
+}
+
+// CBIE sweep over several meshes: instance f on meshes[mesh_of[f]] at ks[f];
+// q_dev / p_dev hold the instances' columns grouped by mesh (offsets `off`)
+nihu_gb_status sweep_solve_impl(nihu_gb_ctx *ctx, int n_meshes, const nihu_gb_mesh *const *meshes, int family,
+                                int nk, const double *ks, const int *mesh_of, int precision, const double2 *q_dev,
+                                double2 *p_dev, const std::vector<int64_t> &off, int restart, int max_iters, double tol,
+                                int *iters, double *rel, int *converged)
+{
+    nihu_gb_status st;
+    std::vector<BatchSystem> sys(nk);
+    void *pb;
+    int64_t total = 0;
+    for (int f = 0; f < nk; ++f) total += meshes[mesh_of[f]]->n;
+    if ((st = scratch(ctx, "swb_b", 16 * (size_t)total, &pb))) return st;
+    double2 *b = (double2 *)pb;
+    for (int i = 0; i < n_meshes; ++i) {
+        const nihu_gb_mesh *mesh = meshes[i];
+        const int64_t n = mesh->n;
+        std::vector<int> fs;
+        std::vector<double> ki;
+        for (int f = 0; f < nk; ++f)
+            if (mesh_of[f] == i) {
+                fs.push_back(f);
+                ki.push_back(ks[f]);
+            }
+        if (fs.empty() || n == 0) {
+            for (int f : fs) sys[f] = BatchSystem{nullptr, 0, 1, nullptr, nullptr, 0.0};
+            continue;
+        }
+        const int cnt = (int)fs.size();
+        const int64_t stride = n * n;
+        void *G, *H, *part;
+        const std::string tag = std::to_string(i);
+        if ((st = scratch(ctx, ("swb_G" + tag).c_str(), 8 * (size_t)stride * cnt, &G))) return st;
+        if ((st = scratch(ctx, ("swb_H" + tag).c_str(), 8 * (size_t)stride * cnt, &H))) return st;
+        if ((st = nihu_gb_assemble_sweep(ctx, mesh, mesh, family, NIHU_GB_SLP | NIHU_GB_DLP, ki.data(), cnt, precision,
+                                         NIHU_GB_C64, G, H, n, stride)))
+            return st;
+        CK(launch_add_identity_batched((int)n, -0.5, 0.0, NIHU_GB_C64, H, n, stride, cnt, ctx->stream));
+        ctx->launches += 1;
+        // b_f = SLP_f q_f: the mesh's instances are contiguous in q_dev / b
+        const int splits = gemv_splits(n, n, NIHU_GB_C64);
+        if ((st = scratch(ctx, "swb_part", 16 * (size_t)splits * n * cnt, &part))) return st;
+        const int64_t o = off[fs[0]];
+        {
+            Phase ph(ctx, "gemv_c64");
+            CK(launch_gemv_batched(NIHU_GB_C64, G, n, n, n, stride, cnt, q_dev + o, b + o, 1.0, 0.0, 0.0, 0.0,
+                                   (double2 *)part, splits, ctx->stream, nullptr));
+        }
+        ctx->launches += 2;
+        for (int j = 0; j < cnt; ++j) {
+            const int f = fs[j];
+            sys[f] = BatchSystem{(const char *)H + 8 * (size_t)stride * j, n, n, b + off[f], p_dev + off[f],
+                                 (double)n * (double)n * (1.0 + ks[f])};
+        }
+    }
+    return solve_batched_device(ctx, sys, restart, max_iters, tol, iters, rel, converged);
+}
+
+// device offsets of the instances' columns, grouped by mesh in mesh order
+std::vector<int64_t> sweep_offsets(int n_meshes, const nihu_gb_mesh *const *meshes, int nk, const int *mesh_of)
+{
+    std::vector<int64_t> off(nk);
+    int64_t o = 0;
+    for (int i = 0; i < n_meshes; ++i)
+        for (int f = 0; f < nk; ++f)
+            if (mesh_of[f] == i) {
+                off[f] = o;
+                o += meshes[i]->n;
+            }
+    return off;
+}
+
+}  // namespace
+
+extern "C" nihu_gb_status nihu_gb_solve_batched(nihu_gb_ctx *ctx, int count, const void *const *A, const int64_t *n,
+                                                const int64_t *lda, const void *const *b, void *const *x, int restart,
+                                                int max_iters, double tol, int *iters, double *rel_residuals,
+                                                int *converged)
+{
+    if (!ctx) return NIHU_GB_ERR_INVALID_ARGUMENT;
+    if (count < 0 || (count > 0 && (!A || !n || !lda || !b || !x)) || restart < 1 || restart > 200 || max_iters < 1 ||
+        !(tol > 0.0))
+        return fail(ctx, NIHU_GB_ERR_INVALID_ARGUMENT, "nihu_gb_solve_batched: bad argument");
+    std::vector<BatchSystem> sys(count);
+    for (int f = 0; f < count; ++f) {
+        if (n[f] < 0 || n[f] > 0x3fffffff || lda[f] < std::max<int64_t>(n[f], 1) || (n[f] > 0 && (!A[f] || !b[f] || !x[f])))
+            return fail(ctx, NIHU_GB_ERR_INVALID_ARGUMENT, "nihu_gb_solve_batched: bad system " + std::to_string(f));
+        sys[f] = BatchSystem{A[f], n[f], lda[f], (const double2 *)b[f], (double2 *)x[f], (double)n[f] * (double)n[f]};
+    }
+    if (count == 0) return NIHU_GB_OK;
+    cudaSetDevice(ctx->device);
+    return solve_batched_device(ctx, sys, restart, max_iters, tol, iters, rel_residuals, converged);
+}
+
+extern "C" nihu_gb_status nihu_gb_solve_sweep_batched(nihu_gb_ctx *ctx, int n_meshes, const nihu_gb_mesh *const *meshes,
+                                                      int family, int nk, const double *ks, const int *mesh_of,
+                                                      int precision, const void *q, void *p, int restart, int max_iters,
+                                                      double tol, int *iters, double *rel_residuals, int *converged)
+{
+    if (!ctx) return NIHU_GB_ERR_INVALID_ARGUMENT;
+    if (n_meshes < 1 || !meshes || nk < 1 || !ks || !mesh_of || !q || !p || restart < 1 || restart > 200 ||
+        max_iters < 1 || !(tol > 0.0) || (precision != 0 && precision != 1) ||
+        (family != NIHU_GB_HELMHOLTZ_3D && family != NIHU_GB_LAPLACE_3D))
+        return fail(ctx, NIHU_GB_ERR_INVALID_ARGUMENT, "nihu_gb_solve_sweep_batched: bad argument");
+    for (int i = 0; i < n_meshes; ++i)
+        if (!meshes[i] || meshes[i]->ctx != ctx)
+            return fail(ctx, NIHU_GB_ERR_INVALID_ARGUMENT, "nihu_gb_solve_sweep_batched: bad mesh");
+    for (int f = 0; f < nk; ++f)
+        if (mesh_of[f] < 0 || mesh_of[f] >= n_meshes || !std::isfinite(ks[f]))
+            return fail(ctx, NIHU_GB_ERR_INVALID_ARGUMENT, "nihu_gb_solve_sweep_batched: bad instance");
+    cudaSetDevice(ctx->device);
+    nihu_gb_status st;
+    const std::vector<int64_t> off = sweep_offsets(n_meshes, meshes, nk, mesh_of);
+    // user layout: instance columns back to back in instance order; device layout: grouped by mesh
+    int64_t total = 0;
+    std::vector<int64_t> user(nk);
+    for (int f = 0; f < nk; ++f) {
+        user[f] = total;
+        total += meshes[mesh_of[f]]->n;
+    }
+    if (total == 0) return NIHU_GB_OK;
+    std::vector<double2> hq(total);
+    for (int f = 0; f < nk; ++f)
+        std::memcpy(hq.data() + off[f], (const double2 *)q + user[f], 16 * (size_t)meshes[mesh_of[f]]->n);
+    void *pq, *pp;
+    if ((st = scratch(ctx, "swb_q", 16 * (size_t)total, &pq))) return st;
+    if ((st = scratch(ctx, "swb_p", 16 * (size_t)total, &pp))) return st;
+    CK(cudaMemcpyAsync(pq, hq.data(), 16 * (size_t)total, cudaMemcpyHostToDevice, ctx->stream));
+    nihu_gb_status sst = sweep_solve_impl(ctx, n_meshes, meshes, family, nk, ks, mesh_of, precision, (const double2 *)pq,
+                                          (double2 *)pp, off, restart, max_iters, tol, iters, rel_residuals, converged);
+    if (sst && sst != NIHU_GB_ERR_NOT_CONVERGED) {
+        sync(ctx);
+        return sst;
+    }
+    std::string msg = ctx->err;
+    CK(cudaMemcpyAsync(hq.data(), pp, 16 * (size_t)total, cudaMemcpyDeviceToHost, ctx->stream));
+    if ((st = sync(ctx))) return st;
+    for (int f = 0; f < nk; ++f)
+        std::memcpy((double2 *)p + user[f], hq.data() + off[f], 16 * (size_t)meshes[mesh_of[f]]->n);
+    ctx->err = msg;
+    return sst;
 }
 
 extern "C" nihu_gb_status nihu_gb_solve_sweep(nihu_gb_ctx *ctx, const nihu_gb_mesh *mesh, int family, const double *ks,
@@ -1428,51 +1708,19 @@ extern "C" nihu_gb_status nihu_gb_solve_sweep(nihu_gb_ctx *ctx, const nihu_gb_me
         return fail(ctx, NIHU_GB_ERR_INVALID_ARGUMENT, "nihu_gb_solve_sweep: bad argument");
     const int64_t n = mesh->n;
     if (n == 0) return NIHU_GB_OK;
-    cudaSetDevice(ctx->device);
-    nihu_gb_status st;
-    const int64_t stride = n * n;
-    void *G, *H, *pq, *pb, *px, *part;
-    if ((st = scratch(ctx, "sw_G", 8 * (size_t)stride * nk, &G))) return st;
-    if ((st = scratch(ctx, "sw_H", 8 * (size_t)stride * nk, &H))) return st;
-    if ((st = scratch(ctx, "sw_q", 16 * (size_t)n * nk, &pq))) return st;
-    if ((st = scratch(ctx, "ms_B", 16 * (size_t)n * nk, &pb))) return st;
-    if ((st = scratch(ctx, "ms_X", 16 * (size_t)n * nk, &px))) return st;
-    const int splits = gemv_splits(n, n, NIHU_GB_C64);
-    if ((st = scratch(ctx, "sw_part", 16 * (size_t)splits * n * nk, &part))) return st;
-    // q: one column broadcast to every wave number, or one column each
-    for (int f = 0; f < nk; ++f) {
-        const char *src = (const char *)q + (q_cols == 1 ? 0 : 16 * (size_t)n * f);
-        CK(cudaMemcpyAsync((char *)pq + 16 * (size_t)n * f, src, 16 * (size_t)n, cudaMemcpyHostToDevice, ctx->stream));
-    }
-    if ((st = nihu_gb_assemble_sweep(ctx, mesh, mesh, family, NIHU_GB_SLP | NIHU_GB_DLP, ks, nk, precision, NIHU_GB_C64,
-                                     G, H, n, stride)))
-        return st;
-    CK(launch_add_identity_batched((int)n, -0.5, 0.0, NIHU_GB_C64, H, n, stride, nk, ctx->stream));
-    ctx->launches += 1;
-    {
-        Phase ph(ctx, "gemv_c64");
-        CK(launch_gemv_batched(NIHU_GB_C64, G, n, n, n, stride, nk, (const double2 *)pq, (double2 *)pb, 1.0, 0.0, 0.0,
-                               0.0, (double2 *)part, splits, ctx->stream, nullptr));
-    }
-    ctx->launches += 2;
-    ApplyFn apply = [&](const double2 *Xv, double2 *Yv, const int *active) -> nihu_gb_status {
-        Phase ph(ctx, "gemv_c64");
-        cudaError_t e = launch_gemv_batched(NIHU_GB_C64, H, n, n, n, stride, nk, Xv, Yv, 1.0, 0.0, 0.0, 0.0,
-                                            (double2 *)part, splits, ctx->stream, active);
-        ctx->launches += 2;
-        if (e != cudaSuccess) return cuda_fail(ctx, e, "batched matvec");
-        return NIHU_GB_OK;
-    };
-    std::vector<double> rel;
-    restart = (int)std::min<int64_t>(restart, n);
-    nihu_gb_status sst = multi_solve_driver(ctx, apply, apply, n, (const double2 *)pb, (double2 *)px, nk, restart,
-                                            max_cycles, tol, -1.0, cycles, iters, rel);
-    if (sst && sst != NIHU_GB_ERR_NOT_CONVERGED) return sst;
-    std::string msg = ctx->err;
-    CK(cudaMemcpyAsync(p, px, 16 * (size_t)n * nk, cudaMemcpyDeviceToHost, ctx->stream));
-    if ((st = sync(ctx))) return st;
-    ctx->err = msg;
-    if (rel_residuals)
-        for (int f = 0; f < nk; ++f) rel_residuals[f] = rel[f];
-    return sst;
+    std::vector<double2> qf((size_t)n * nk);
+    for (int f = 0; f < nk; ++f)
+        std::memcpy(qf.data() + (size_t)n * f, (const double2 *)q + (q_cols == 1 ? 0 : (size_t)n * f), 16 * (size_t)n);
+    std::vector<int> mesh_of(nk, 0), it(nk);
+    const nihu_gb_mesh *ms[1] = {mesh};
+    const int max_iters = (int)std::min<int64_t>((int64_t)restart * max_cycles, 1 << 30);
+    nihu_gb_status st = nihu_gb_solve_sweep_batched(ctx, 1, ms, family, nk, ks, mesh_of.data(), precision, qf.data(), p,
+                                                    restart, max_iters, tol, it.data(), rel_residuals, nullptr);
+    if (st && st != NIHU_GB_ERR_NOT_CONVERGED) return st;
+    int most = 0;
+    for (int f = 0; f < nk; ++f) most = std::max(most, it[f]);
+    const int r = (int)std::min<int64_t>(restart, n);
+    if (cycles) *cycles = (most + r - 1) / r;
+    if (iters) *iters = most;
+    return st;
 }

@@ -60,6 +60,7 @@ struct RegularArgs {
     const double *ks = nullptr;
     const float *ks32 = nullptr;
     int64_t mat_stride = 0;
+    double k_absmax = 0.0;  // largest |ks[f]| of a frequency batch
 };
 cudaError_t launch_assemble_regular(const RegularArgs &a, cudaStream_t s);
 

@@ -18,6 +18,18 @@ def test_header_and_binding_agree():
     assert declared_symbols() == sorted(_capi.SIGNATURES)
 
 
+def test_binding_argument_counts_match_header():
+    from nihu_gb300 import _capi
+    txt = open(os.path.join(ROOT, "include", "nihu_gb300.h")).read()
+    txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+    decls = dict(re.findall(r"\b(nihu_gb_\w+)\s*\(([^;{]*?)\)\s*;", txt))
+    assert sorted(decls) == sorted(_capi.SIGNATURES)
+    for name, params in decls.items():
+        params = params.strip()
+        count = 0 if params in ("", "void") else params.count(",") + 1
+        assert count == len(_capi.SIGNATURES[name][1]), name
+
+
 def test_library_exports_all_symbols():
     import nihu_gb300
     L = nihu_gb300.lib()
