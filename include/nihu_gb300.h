@@ -75,6 +75,7 @@ typedef enum nihu_gb_status {
 
 typedef struct nihu_gb_ctx nihu_gb_ctx;
 typedef struct nihu_gb_mesh nihu_gb_mesh;
+typedef struct nihu_gb_server nihu_gb_server;
 
 /* ------------------------------------------------------------------ context */
 
@@ -308,6 +309,40 @@ nihu_gb_status nihu_gb_lu_solve(nihu_gb_ctx *ctx, void *A, int64_t n, int64_t ld
 nihu_gb_status nihu_gb_solve_cbie(nihu_gb_ctx *ctx, const nihu_gb_mesh *mesh, int family, double k,
                                   int precision, int dtype, const void *q, void *p, int solver,
                                   int restart, int max_iters, double tol, int *iters, double *rel_residual);
+
+/* ------------------------------------------------------------ serving */
+
+/* A serving loop for CBIE solves (DLP - I/2) p = SLP q of requests arriving
+ * over time (the reference solves one problem per program run,
+ * helmholtz_3d_coll.cpp:36-120; it has no counterpart for the loop itself).
+ * Requests wait in a FIFO queue until hbm_budget_bytes holds their matrices
+ * (complex64; the SLP matrix is freed once the right-hand side is formed)
+ * and Krylov state, and at most max_active requests are admitted at once.
+ * Each nihu_gb_server_step admits what fits, assembles the new requests (one
+ * frequency batch per mesh), and advances every admitted system by at most
+ * `quantum` GMRES(restart) steps (0: to the end) in one persistent launch;
+ * matrices, Krylov state and iterates stay on the device between steps, and
+ * a request's result does not depend on what else is in flight.  The meshes
+ * must outlive the server.  Calls on one server are not thread safe. */
+nihu_gb_status nihu_gb_server_create(nihu_gb_ctx *ctx, int n_meshes, const nihu_gb_mesh *const *meshes, int family,
+                                     int precision, size_t hbm_budget_bytes, int max_active, int restart,
+                                     int max_iters, double tol, int quantum, nihu_gb_server **out);
+void nihu_gb_server_destroy(nihu_gb_server *server);
+
+/* Queue a request on meshes[mesh] at wave number k with Neumann data q
+ * (complex128 host vector of the mesh's element count, copied).  *id
+ * receives its number (0, 1, 2, ... in submission order).
+ * NIHU_GB_ERR_OUT_OF_MEMORY: the request alone exceeds the budget. */
+nihu_gb_status nihu_gb_server_submit(nihu_gb_server *server, int mesh, double k, const void *q, int64_t *id);
+
+/* One round (waits for its GPU work); the counts after it may be NULL. */
+nihu_gb_status nihu_gb_server_step(nihu_gb_server *server, int *n_queued, int *n_active, int *n_done);
+
+/* Take the oldest finished request: *id (-1 if none), p (complex128, at
+ * least the mesh's element count, `capacity`), GMRES iterations, relative
+ * residual estimate and convergence flag (each may be NULL). */
+nihu_gb_status nihu_gb_server_take(nihu_gb_server *server, int64_t *id, void *p, int64_t capacity, int *iters,
+                                   double *rel_residual, int *converged);
 
 #ifdef __cplusplus
 }

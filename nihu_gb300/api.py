@@ -552,6 +552,72 @@ def solve_sweep_batched(meshes, ks, mesh_of, q=None, family: int = C.HELMHOLTZ_3
     return out, it, rel, conv.astype(bool)
 
 
+class Server:
+    """Continuous-batching serving loop of CBIE solves (DLP - I/2) p = SLP q
+    (nihu_gb_server_*).  Requests wait in a FIFO queue until the HBM budget
+    holds them; each step() admits what fits, assembles the new requests (one
+    frequency batch per mesh), advances every admitted system by at most
+    `quantum` GMRES steps in one persistent launch and retires the finished
+    ones, whose results take() returns.  A request's result does not depend
+    on what else is in flight."""
+
+    def __init__(self, meshes, family: int = C.HELMHOLTZ_3D, precision: str = "fp32",
+                 hbm_budget_bytes: int = 150 << 30, max_active: int = 1024, restart: int = 50, max_iters: int = 1000,
+                 tol: float = 1e-6, quantum: int = 8, ctx: Context | None = None):
+        self.ctx = ctx or default_context()
+        self.meshes = list(meshes)
+        self._dms = [m.device(self.ctx) for m in self.meshes]
+        self.sizes = [m.num_elements for m in self.meshes]
+        handles = (ctypes.c_void_p * len(self._dms))(*[d.handle.value for d in self._dms])
+        h = ctypes.c_void_p()
+        self.ctx.check(C.lib().nihu_gb_server_create(
+            self.ctx.handle, len(self._dms), handles, family, C.REGULAR_FP64 if precision == "fp64" else C.REGULAR_FP32,
+            int(hbm_budget_bytes), max_active, restart, max_iters, tol, quantum, ctypes.byref(h)))
+        self.handle = h
+        self._mesh_of = {}
+
+    def submit(self, mesh: int, k: float, q) -> int:
+        q = _c128(q)
+        if q.shape != (self.sizes[mesh],):
+            raise ValueError("q must have the mesh's element count")
+        rid = ctypes.c_int64(-1)
+        self.ctx.check(C.lib().nihu_gb_server_submit(self.handle, mesh, float(k), q.ctypes.data, ctypes.byref(rid)))
+        self._mesh_of[rid.value] = mesh
+        return rid.value
+
+    def step(self):
+        """One round; returns (queued, active, finished-but-not-taken)."""
+        a, b, c = ctypes.c_int(0), ctypes.c_int(0), ctypes.c_int(0)
+        self.ctx.check(C.lib().nihu_gb_server_step(self.handle, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c)))
+        return a.value, b.value, c.value
+
+    def take(self):
+        """The oldest finished request as (id, p, iterations, relative residual,
+        converged), or None."""
+        cap = max(self.sizes)
+        p = np.zeros(cap, np.complex128)
+        rid, it, conv = ctypes.c_int64(-1), ctypes.c_int(0), ctypes.c_int(0)
+        rel = ctypes.c_double(0.0)
+        self.ctx.check(C.lib().nihu_gb_server_take(self.handle, ctypes.byref(rid), p.ctypes.data, cap, ctypes.byref(it),
+                                                   ctypes.byref(rel), ctypes.byref(conv)))
+        if rid.value < 0:
+            return None
+        n = self.sizes[self._mesh_of.pop(rid.value)]
+        return rid.value, p[:n].copy(), it.value, rel.value, bool(conv.value)
+
+    def close(self):
+        if getattr(self, "handle", None):
+            C.lib().nihu_gb_server_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            if self.ctx.handle:
+                self.close()
+        except Exception:
+            pass
+
+
 def pair_statistics(test: Mesh, trial: Mesh, ctx: Context | None = None) -> np.ndarray:
     """[self, near, regular (SLP level, DLP level) 3x3] pair counts."""
     ctx = ctx or default_context()

@@ -201,9 +201,8 @@ __global__ void __launch_bounds__(REG_THREADS) k_regular(RegularArgs a)
                         R sr = 0, si = 0, dr = 0, di = 0;
                         point_freq<FAM, float>(gm, a.ks32[f], sr, si, dr, di);
                         if (row_ok) {
-                            const int64_t fo = off + f * a.mat_stride;
-                            if (DO_S) store_entry(out_s + fo, sr, si, are, aim, unit_alpha, accumulate);
-                            if (DO_D) store_entry(out_d + fo, dr, di, are, aim, unit_alpha, accumulate);
+                            if (DO_S) store_entry(batch_matrix<Out>(a, false, f) + off, sr, si, are, aim, unit_alpha, accumulate);
+                            if (DO_D) store_entry(batch_matrix<Out>(a, true, f) + off, dr, di, are, aim, unit_alpha, accumulate);
                         }
                     }
                 } else {
@@ -264,9 +263,11 @@ __global__ void __launch_bounds__(REG_THREADS) k_regular(RegularArgs a)
 #pragma unroll
                 for (int u = 0; u < FREQ_TILE; ++u) {
                     if (f0 + u >= a.nk) break;
-                    const int64_t off = (int64_t)(j - a.j0) * a.ld + i + (f0 + u) * a.mat_stride;
-                    if (DO_S) store_entry(out_s + off, sr[u], si[u], are, aim, unit_alpha, accumulate);
-                    if (DO_D) store_entry(out_d + off, dr[u], di[u], are, aim, unit_alpha, accumulate);
+                    const int64_t off = (int64_t)(j - a.j0) * a.ld + i;
+                    if (DO_S)
+                        store_entry(batch_matrix<Out>(a, false, f0 + u) + off, sr[u], si[u], are, aim, unit_alpha, accumulate);
+                    if (DO_D)
+                        store_entry(batch_matrix<Out>(a, true, f0 + u) + off, dr[u], di[u], are, aim, unit_alpha, accumulate);
                 }
             }
         } else {
@@ -308,7 +309,7 @@ static void launch_ops(const RegularArgs &a, dim3 grid, cudaStream_t s)
 template <typename R, typename Out>
 static void launch_fam(const RegularArgs &a, dim3 grid, cudaStream_t s)
 {
-    const bool batch = a.nk > 1;
+    const bool batch = a.nk > 1 || a.force_batch;
     if (a.family == FAM_HELMHOLTZ) {
         if (batch) launch_ops<R, Out, FAM_HELMHOLTZ, true>(a, grid, s);
         else launch_ops<R, Out, FAM_HELMHOLTZ, false>(a, grid, s);

@@ -27,6 +27,8 @@
 //      (nihu/library/nearly_singular_collocational_telles.hpp:85-110, telles_1987.hpp:44-113)
 // A frequency batch on a triangle evaluates the same 42-point dynamic sums
 // through their power series in k (near_moments / near_series below).
+#include <cmath>
+
 #include "geom.cuh"
 #include "kernels.h"
 
@@ -312,12 +314,28 @@ __device__ void near_plane(const Elem64 &e, int fam, double k, const double x0[3
 //   DLP(k) = sum_{j>=2} (-ik)^j (j - 1)/j!  T_j,  T_j = sum_p W_p (r_p.n) r_p^{j-3}
 // The moments are formed once per pair; each wave number then costs one
 // Horner evaluation in u = -k^2 ((-ik)^{2m} = u^m, (-ik)^{2m+1} = -ik u^m)
-// instead of 42 complex exponentials.  The series stops at the first J with
-// x^{J+1} / J! < 1e-15 for x = k_max max_p r_p, which bounds the truncation
-// of every point's term by 1e-15 times that point's static contribution.
+// instead of 42 complex exponentials.  Wave number k uses the first J with
+// x^{J+1} / J! < 1e-15 for x = |k| max_p r_p, which bounds the truncation of
+// every point's term by 1e-15 times that point's static contribution; the
+// moments are formed up to the J of the batch's largest |k|.  J depends only
+// on the pair and k, so an entry does not depend on the other wave numbers
+// of its batch; where x is beyond the longest series the points are summed
+// directly for that wave number.
 
 constexpr int MOM_J = 64;  // most series terms (shared memory per thread: 2 x MOM_J doubles)
 constexpr size_t MOM_SMEM = 2 * sizeof(double) * MOM_J * SING_THREADS;
+
+// c_series_x[J] = (1e-15 J!)^{1/(J+1)} (1 - 1e-5): the largest x that J terms serve
+__constant__ float c_series_x[MOM_J];
+
+// terms for x = k max r: the smallest J >= 1 with x <= c_series_x[J], or
+// MOM_J when even MOM_J - 1 terms do not reach the bound
+__device__ __forceinline__ int series_terms(float x)
+{
+    int J = 1;
+    while (J < MOM_J - 1 && x > c_series_x[J]) ++J;
+    return x > c_series_x[J] ? MOM_J : J;
+}
 
 struct InvFactorials {
     double v[MOM_J];
@@ -343,12 +361,11 @@ __device__ __forceinline__ void unit_normal_center(const Elem64 &e, double en[3]
 
 // coefficients c^S_j = S_j / j! at mS[j * SING_THREADS] and, when en is
 // given, c^T_j = (j-1) T_j / j! at mT[j * SING_THREADS], j = 0..J, over the np
-// points that pts(p, y, W) yields (W = w J / (4 pi)); returns J, or 0 when
-// MOM_J terms do not reach the bound (the caller then sums the points per
-// wave number)
+// points that pts(p, y, W) yields (W = w J / (4 pi)), for J = the terms of
+// kmax; returns J (capped at MOM_J - 1) and *rmax = max_p r_p
 template <class PointFn>
 __device__ int series_moments(int np, PointFn pts, const double x0[3], const double *en, double kmax, double *mS,
-                              double *mT)
+                              double *mT, float *rmax)
 {
     double r2max = 0.0;
     for (int p = 0; p < np; ++p) {
@@ -357,14 +374,8 @@ __device__ int series_moments(int np, PointFn pts, const double x0[3], const dou
         const double r0 = y[0] - x0[0], r1 = y[1] - x0[1], r2 = y[2] - x0[2];
         r2max = fmax(r2max, r0 * r0 + r1 * r1 + r2 * r2);
     }
-    const double x = kmax * sqrt(r2max);
-    int J = 1;
-    double t = x * x;  // x^{J+1} / J!
-    while (t >= 1e-15) {
-        if (J == MOM_J - 1) return 0;
-        ++J;
-        t *= x / J;
-    }
+    *rmax = (float)sqrt(r2max);
+    const int J = min(series_terms((float)kmax * *rmax), MOM_J - 1);
     for (int j = 0; j <= J; ++j) {
         mS[j * SING_THREADS] = 0.0;
         if (en) mT[j * SING_THREADS] = 0.0;
@@ -402,7 +413,7 @@ __device__ int series_moments(int np, PointFn pts, const double x0[3], const dou
 
 // the moments of a triangle's 42-point dynamic rule (table of (y, w J))
 __device__ int near_moments(const Elem64 &e, const Pt4 *__restrict__ pts, const double x0[3], double kmax,
-                            double *mS, double *mT)
+                            double *mS, double *mT, float *rmax)
 {
     double en[3];
     unit_normal_center(e, en);
@@ -415,7 +426,7 @@ __device__ int near_moments(const Elem64 &e, const Pt4 *__restrict__ pts, const 
             y[2] = v.z;
             W = v.w * INV_FOUR_PI;
         },
-        x0, en, kmax, mS, mT);
+        x0, en, kmax, mS, mT, rmax);
 }
 
 // the dynamic sums at wave number k from the coefficients of near_moments
@@ -676,7 +687,7 @@ __device__ void self_tria_dynamic(const Elem64 &e, double k, const double x0[3],
 }
 
 // the moments of the same 13-point rule (SLP series only)
-__device__ int self_tria_moments(const Elem64 &e, const double x0[3], double kmax, double *mS)
+__device__ int self_tria_moments(const Elem64 &e, const double x0[3], double kmax, double *mS, float *rmax)
 {
     double e1[3], e2[3], nt[3];
     for (int d = 0; d < 3; ++d) { e1[d] = e.c[1][d] - e.c[0][d]; e2[d] = e.c[2][d] - e.c[0][d]; }
@@ -690,7 +701,7 @@ __device__ int self_tria_moments(const Elem64 &e, const double x0[3], double kma
             for (int d = 0; d < 3; ++d) y[d] = e.c[0][d] + xi * e1[d] + eta * e2[d];
             W = w * J;
         },
-        x0, nullptr, kmax, mS, nullptr);
+        x0, nullptr, kmax, mS, nullptr, rmax);
 }
 
 __device__ void self_tria(const Elem64 &e, int fam, double k, const double x0[3], Acc &a)
@@ -785,8 +796,6 @@ __device__ __forceinline__ void singular_pairs(const RegularArgs &a, const NearL
     const int64_t n_self = a.same_mesh ? (int64_t)(a.j1 - a.j0) : 0;
     const int64_t total = n_near + n_self;
     const bool do_s = (a.ops & OP_SLP) != 0, do_d = (a.ops & OP_DLP) != 0;
-    Out *out_s = reinterpret_cast<Out *>(a.out_s);
-    Out *out_d = reinterpret_cast<Out *>(a.out_d);
     const int fam = a.family;
     const double k = a.k;
     // nearly singular pairs have r < 1.5 D + (point to centre) <= 3 D_max
@@ -823,37 +832,38 @@ __device__ __forceinline__ void singular_pairs(const RegularArgs &a, const NearL
             // the moments of the dynamic part once, then per wave number the
             // series (or the self term)
             Acc st;
-            int J = 0;
+            float rmax = 0.0f;
             double *mS = s_mom + threadIdx.x, *mT = s_mom + MOM_J * SING_THREADS + threadIdx.x;
             const Pt4 *pts = a.trial.dyn42 + 42 * (int64_t)j;
             if (!self) {
                 near_static(e, x0, do_s, do_d, st);
-                if (fam == FAM_HELMHOLTZ) J = near_moments(e, pts, x0, a.k_absmax, mS, mT);
+                if (fam == FAM_HELMHOLTZ) near_moments(e, pts, x0, a.k_absmax, mS, mT, &rmax);
             } else if (do_s) {
                 st.sr = self_static(e, x0) * INV_FOUR_PI;
-                if (fam == FAM_HELMHOLTZ) J = self_tria_moments(e, x0, a.k_absmax, mS);
+                if (fam == FAM_HELMHOLTZ) self_tria_moments(e, x0, a.k_absmax, mS, &rmax);
             }
             for (int f = 0; f < a.nk; ++f) {
                 const double kf = a.ks[f];
+                // this wave number's series length (MOM_J: sum the points directly)
+                const int Jf = fam == FAM_HELMHOLTZ ? series_terms(fabsf((float)kf) * rmax) : 0;
                 Acc acc;
                 if (self) {
                     if (do_s) {
                         acc = st;
                         if (fam == FAM_HELMHOLTZ) {
-                            if (J) near_series(J, kf, mS, mT, true, false, acc);
+                            if (Jf < MOM_J) near_series(Jf, kf, mS, mT, true, false, acc);
                             else self_tria_dynamic(e, kf, x0, acc);
                         }
                     }
                 } else {
                     acc = st;
                     if (fam == FAM_HELMHOLTZ) {
-                        if (J) near_series(J, kf, mS, mT, do_s, do_d, acc);
+                        if (Jf < MOM_J) near_series(Jf, kf, mS, mT, do_s, do_d, acc);
                         else near_dynamic(e, kf, x0, do_s, do_d, acc, pts, kf * 3.0 * a.trial_size_max <= 0.75);
                     }
                 }
-                const int64_t fo = off + f * a.mat_stride;
-                if (do_s) store64(out_s + fo, acc.sr, acc.si, a.alpha_re, a.alpha_im, a.accumulate);
-                if (do_d) store64(out_d + fo, acc.dr, acc.di, a.alpha_re, a.alpha_im, a.accumulate);
+                if (do_s) store64(batch_matrix<Out>(a, false, f) + off, acc.sr, acc.si, a.alpha_re, a.alpha_im, a.accumulate);
+                if (do_d) store64(batch_matrix<Out>(a, true, f) + off, acc.dr, acc.di, a.alpha_re, a.alpha_im, a.accumulate);
             }
             continue;
         }
@@ -889,9 +899,8 @@ __device__ __forceinline__ void singular_pairs(const RegularArgs &a, const NearL
                 atomicCAS(err, 0, (int)min(item + 1, (int64_t)0x7fffffff));
                 break;
             }
-            const int64_t fo = off + f * a.mat_stride;
-            if (do_s) store64(out_s + fo, acc.sr, acc.si, a.alpha_re, a.alpha_im, a.accumulate);
-            if (do_d) store64(out_d + fo, acc.dr, acc.di, a.alpha_re, a.alpha_im, a.accumulate);
+            if (do_s) store64(batch_matrix<Out>(a, false, f) + off, acc.sr, acc.si, a.alpha_re, a.alpha_im, a.accumulate);
+            if (do_d) store64(batch_matrix<Out>(a, true, f) + off, acc.dr, acc.di, a.alpha_re, a.alpha_im, a.accumulate);
         }
     }
 }
@@ -912,6 +921,19 @@ __global__ void __launch_bounds__(SING_THREADS, 4) k_singular_batch(RegularArgs 
     singular_pairs<Out, true>(a, near, err);
 }
 
+// host values of c_series_x
+struct SeriesBounds {
+    float x[MOM_J];
+    SeriesBounds()
+    {
+        double lf = 0.0;  // log J!
+        for (int J = 0; J < MOM_J; ++J) {
+            if (J > 0) lf += std::log((double)J);
+            x[J] = J == 0 ? 0.0f : (float)(std::exp((std::log(1e-15) + lf) / (J + 1)) * (1.0 - 1e-5));
+        }
+    }
+};
+
 cudaError_t launch_assemble_singular(const RegularArgs &a, const NearList &near, int *err, cudaStream_t s)
 {
     int dev = 0, sms = 148;
@@ -924,7 +946,10 @@ cudaError_t launch_assemble_singular(const RegularArgs &a, const NearList &near,
     int64_t want = (total + SING_THREADS - 1) / SING_THREADS;
     int blocks = (int)max((int64_t)1, min(want, (int64_t)sms));
     size_t smem = 0;
-    if (a.nk > 1) {
+    if (a.nk > 1 || a.force_batch) {
+        static const SeriesBounds bounds;
+        cudaError_t e0 = cudaMemcpyToSymbolAsync(c_series_x, bounds.x, sizeof(bounds.x), 0, cudaMemcpyHostToDevice, s);
+        if (e0 != cudaSuccess) return e0;
         smem = MOM_SMEM;
         cudaError_t e = a.dtype == 0
                             ? cudaFuncSetAttribute(k_singular_batch<float2>, cudaFuncAttributeMaxDynamicSharedMemorySize,

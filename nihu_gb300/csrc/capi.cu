@@ -4,8 +4,10 @@
 #include <complex>
 #include <cstdio>
 #include <cstring>
+#include <deque>
 #include <functional>
 #include <map>
+#include <memory>
 #include <mutex>
 #include <queue>
 #include <string>
@@ -1373,21 +1375,14 @@ nihu_gb_status upload_ks(nihu_gb_ctx *ctx, const double *ks, int nk, const doubl
 
 }  // namespace
 
-extern "C" nihu_gb_status nihu_gb_assemble_sweep(nihu_gb_ctx *ctx, const nihu_gb_mesh *test, const nihu_gb_mesh *trial,
-                                                 int family, int ops, const double *ks, int nk, int precision,
-                                                 int dtype, void *out_slp, void *out_dlp, int64_t ld,
-                                                 int64_t mat_stride)
+namespace {
+
+// frequency batch of one mesh pair: matrices f at out + f * mat_stride, or
+// (outs_dev, nk > 1) at the device pointers outs_dev[f] / outs_dev[nk + f]
+nihu_gb_status assemble_batch(nihu_gb_ctx *ctx, const nihu_gb_mesh *test, const nihu_gb_mesh *trial, int family, int ops,
+                              const double *ks, int nk, int precision, int dtype, void *out_slp, void *out_dlp,
+                              int64_t ld, int64_t mat_stride, void *const *outs_dev, bool force_batch = false)
 {
-    if (!ctx) return NIHU_GB_ERR_INVALID_ARGUMENT;
-    if (!test || !trial || test->ctx != ctx || trial->ctx != ctx || nk < 1 || !ks || ops < 1 || ops > 3 ||
-        ((ops & 1) && !out_slp) || ((ops & 2) && !out_dlp) || !valid_dtype(dtype) || (precision != 0 && precision != 1) ||
-        ld < std::max<int64_t>(test->n, 1) || mat_stride < ld * trial->n ||
-        (family != NIHU_GB_HELMHOLTZ_3D && family != NIHU_GB_LAPLACE_3D))
-        return fail(ctx, NIHU_GB_ERR_INVALID_ARGUMENT, "nihu_gb_assemble_sweep: bad argument");
-    for (int f = 0; f < nk; ++f)
-        if (!std::isfinite(ks[f])) return fail(ctx, NIHU_GB_ERR_INVALID_ARGUMENT, "nihu_gb_assemble_sweep: bad k");
-    if (test->n == 0 || trial->n == 0) return NIHU_GB_OK;
-    cudaSetDevice(ctx->device);
     nihu_gb_status st;
     NearList *nl = nullptr;
     if ((st = get_near(ctx, test, trial, &nl))) return st;
@@ -1416,9 +1411,32 @@ extern "C" nihu_gb_status nihu_gb_assemble_sweep(nihu_gb_ctx *ctx, const nihu_gb
     a.nk = nk;
     for (int f = 0; f < nk; ++f) a.k_absmax = std::max(a.k_absmax, std::fabs(ks[f]));
     a.mat_stride = mat_stride;
+    a.force_batch = force_batch;
+    a.outs = (nk > 1 || force_batch) ? outs_dev : nullptr;
     if ((st = upload_ks(ctx, ks, nk, &a.ks, &a.ks32))) return st;
     if ((st = assemble_panel(ctx, a, nl))) return st;
     return check_flag(ctx);
+}
+
+}  // namespace
+
+extern "C" nihu_gb_status nihu_gb_assemble_sweep(nihu_gb_ctx *ctx, const nihu_gb_mesh *test, const nihu_gb_mesh *trial,
+                                                 int family, int ops, const double *ks, int nk, int precision,
+                                                 int dtype, void *out_slp, void *out_dlp, int64_t ld,
+                                                 int64_t mat_stride)
+{
+    if (!ctx) return NIHU_GB_ERR_INVALID_ARGUMENT;
+    if (!test || !trial || test->ctx != ctx || trial->ctx != ctx || nk < 1 || !ks || ops < 1 || ops > 3 ||
+        ((ops & 1) && !out_slp) || ((ops & 2) && !out_dlp) || !valid_dtype(dtype) || (precision != 0 && precision != 1) ||
+        ld < std::max<int64_t>(test->n, 1) || mat_stride < ld * trial->n ||
+        (family != NIHU_GB_HELMHOLTZ_3D && family != NIHU_GB_LAPLACE_3D))
+        return fail(ctx, NIHU_GB_ERR_INVALID_ARGUMENT, "nihu_gb_assemble_sweep: bad argument");
+    for (int f = 0; f < nk; ++f)
+        if (!std::isfinite(ks[f])) return fail(ctx, NIHU_GB_ERR_INVALID_ARGUMENT, "nihu_gb_assemble_sweep: bad k");
+    if (test->n == 0 || trial->n == 0) return NIHU_GB_OK;
+    cudaSetDevice(ctx->device);
+    return assemble_batch(ctx, test, trial, family, ops, ks, nk, precision, dtype, out_slp, out_dlp, ld, mat_stride,
+                          nullptr);
 }
 
 // ------------------------------------------------ persistent batched GMRES
@@ -1433,40 +1451,40 @@ struct BatchSystem {
     double work;  // processing order: larger first
 };
 
-// one persistent launch over all systems; per-system outputs on the host (may be NULL)
-nihu_gb_status solve_batched_device(nihu_gb_ctx *ctx, const std::vector<BatchSystem> &sys, int restart, int max_iters,
-                                    double tol, int *iters, double *rel, int *converged)
+struct PersistentPlan {
+    int cluster = 0, clusters = 0, vx_smem = 1;
+    size_t smem = 0;
+};
+
+// Launch shape of one persistent GMRES launch over systems of the given sizes
+// (results do not depend on it): the systems, largest first, go to the
+// earliest free of the clusters that run at once; a system of nb 128-row
+// blocks keeps min(C, nb) CTAs busy for n^2 / min(C, nb) time units, slowed
+// in proportion when more CTAs stream at once than HBM feeds (about 60 GB/s
+// per 512-thread CTA).  The matvec input moves from shared memory to a
+// global buffer when a cluster size's shared memory cannot hold it.
+nihu_gb_status plan_persistent(nihu_gb_ctx *ctx, const std::vector<int64_t> &ns, int m, PersistentPlan *out)
 {
-    const int count = (int)sys.size();
-    if (count == 0) return NIHU_GB_OK;
-    nihu_gb_status st;
-    int64_t n_max = 1;
-    for (const BatchSystem &s : sys) n_max = std::max(n_max, s.n);
-    const int m = (int)std::max<int64_t>(1, std::min<int64_t>(restart, n_max));
-    int smem_optin = 0, l2 = 0;
+    int smem_optin = 0, mem_khz = 0, bus_bits = 0;
     cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, ctx->device);
-    cudaDeviceGetAttribute(&l2, cudaDevAttrL2CacheSize, ctx->device);
-    // Cluster size from a launch model (results do not depend on it): the
-    // systems, largest first, go to the earliest free of the clusters that
-    // run at once; a system of nb 128-row blocks keeps min(C, nb) CTAs busy
-    // for n^2 / min(C, nb) time units, slowed in proportion when more CTAs
-    // stream at once than HBM feeds (about 60 GB/s per 512-thread CTA).
-    int mem_khz = 0, bus_bits = 0;
     cudaDeviceGetAttribute(&mem_khz, cudaDevAttrMemoryClockRate, ctx->device);
     cudaDeviceGetAttribute(&bus_bits, cudaDevAttrGlobalMemoryBusWidth, ctx->device);
     const double hbm_gbs = 2.0 * mem_khz * 1e3 * bus_bits / 8.0 / 1e9;
     const double feeding = std::max(8.0, 0.8 * hbm_gbs / 60.0);  // CTAs that saturate HBM
-    std::vector<int> by_work(count);
-    for (int f = 0; f < count; ++f) by_work[f] = f;
-    std::stable_sort(by_work.begin(), by_work.end(), [&](int x, int y) { return sys[x].work > sys[y].work; });
-    int cluster = 0, clusters = 0;
-    size_t smem = 0;
-    double best = 0.0;
+    const int count = (int)ns.size();
+    int64_t n_max = 1;
+    for (int64_t n : ns) n_max = std::max(n_max, n);
+    std::vector<int64_t> by_size(ns);
+    std::sort(by_size.begin(), by_size.end(), std::greater<int64_t>());
+    PersistentPlan best;
+    double best_t = 0.0;
     for (int c : {2, 4, 8, 16, 1}) {
-        if (persistent_smem_layout((int)n_max, c, m).total > (size_t)smem_optin) continue;
+        int vs = 1;
+        if (persistent_smem_layout((int)n_max, c, m, 1).total > (size_t)smem_optin) vs = 0;
+        if (persistent_smem_layout((int)n_max, c, m, vs).total > (size_t)smem_optin) continue;
         int act = 0;
         size_t sm_bytes = 0;
-        if (persistent_gmres_plan((int)n_max, m, c, count, &act, &sm_bytes) != cudaSuccess) {
+        if (persistent_gmres_plan((int)n_max, m, c, vs, count, &act, &sm_bytes) != cudaSuccess) {
             cudaGetLastError();
             continue;
         }
@@ -1474,48 +1492,60 @@ nihu_gb_status solve_batched_device(nihu_gb_ctx *ctx, const std::vector<BatchSys
         std::priority_queue<double, std::vector<double>, std::greater<double>> free_at;
         for (int q = 0; q < act; ++q) free_at.push(0.0);
         double makespan = 0.0;
-        for (int f : by_work) {
-            const BatchSystem &s = sys[f];
-            const double nb = (double)((s.n + 127) / 128);
+        for (int64_t n : by_size) {
+            const double nb = (double)((n + 127) / 128);
             double t = free_at.top();
             free_at.pop();
-            t += (double)s.n * (double)s.n / (std::max(1.0, std::min((double)c, nb)) * rate);
+            t += (double)n * (double)n / (std::max(1.0, std::min((double)c, nb)) * rate);
             free_at.push(t);
             makespan = std::max(makespan, t);
         }
         // within 3 %, the later candidate (larger clusters) loses to the earlier
-        if (!cluster || makespan < 0.97 * best) {
-            best = makespan;
-            cluster = c;
+        if (!best.cluster || makespan < 0.97 * best_t) {
+            best_t = makespan;
+            best.cluster = c;
+            best.clusters = act;
+            best.vx_smem = vs;
+            best.smem = sm_bytes;
         }
     }
-    if (!cluster)
+    if (!best.cluster)
         return fail(ctx, NIHU_GB_ERR_INVALID_ARGUMENT, "batched GMRES: system or restart too large for shared memory");
-    CK(persistent_gmres_plan((int)n_max, m, cluster, count, &clusters, &smem));
-    void *pitems, *porder, *pV, *pout;
+    CK(persistent_gmres_plan((int)n_max, m, best.cluster, best.vx_smem, count, &best.clusters, &best.smem));
+    *out = best;
+    return NIHU_GB_OK;
+}
+
+// one persistent launch over the items (states in device memory), in order
+// of decreasing `work`; asynchronous on the context stream
+nihu_gb_status launch_persistent(nihu_gb_ctx *ctx, std::vector<PersistentItem> &items, const std::vector<double> &work,
+                                 int m, int max_iters, int quantum, double tol)
+{
+    const int count = (int)items.size();
+    if (count == 0) return NIHU_GB_OK;
+    nihu_gb_status st;
+    std::vector<int64_t> ns(count);
+    int64_t n_max = 1;
+    for (int f = 0; f < count; ++f) {
+        ns[f] = items[f].n;
+        n_max = std::max<int64_t>(n_max, items[f].n);
+    }
+    PersistentPlan plan;
+    if ((st = plan_persistent(ctx, ns, m, &plan))) return st;
+    int l2 = 0;
+    cudaDeviceGetAttribute(&l2, cudaDevAttrL2CacheSize, ctx->device);
+    for (PersistentItem &it : items) {
+        it.vec = (it.n % 2 == 0) && (it.lda % 2 == 0) && ((reinterpret_cast<uintptr_t>(it.A) & 15) == 0);
+        it.stream = 8.0 * (double)it.n * (double)it.n * std::min(count, plan.clusters) > 0.5 * l2;
+    }
+    std::vector<int> order(count);
+    for (int f = 0; f < count; ++f) order[f] = f;
+    std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return work[x] > work[y]; });
+    void *pitems, *porder, *pcnt, *pvx = nullptr;
     if ((st = scratch(ctx, "pg_items", sizeof(PersistentItem) * (size_t)count, &pitems))) return st;
     if ((st = scratch(ctx, "pg_order", sizeof(int) * (size_t)count, &porder))) return st;
-    if ((st = scratch(ctx, "pg_V", 16 * (size_t)clusters * (m + 1) * n_max, &pV))) return st;
-    // counter | iters[count] | converged[count] | (8-aligned) rel[count]
-    const size_t off_rel = ((sizeof(int) * (1 + 2 * (size_t)count)) + 7) & ~(size_t)7;
-    if ((st = scratch(ctx, "pg_out", off_rel + 8 * (size_t)count, &pout))) return st;
-    std::vector<PersistentItem> items(count);
-    std::vector<int> order(count);
-    for (int f = 0; f < count; ++f) {
-        const BatchSystem &s = sys[f];
-        PersistentItem &it = items[f];
-        it.A = (const float2 *)s.A;
-        it.lda = s.lda;
-        it.b = s.b;
-        it.x = s.x;
-        it.n = (int)s.n;
-        it.vec = (s.n % 2 == 0) && (s.lda % 2 == 0) && ((reinterpret_cast<uintptr_t>(s.A) & 15) == 0);
-        it.stream = 8.0 * (double)s.n * (double)s.n * std::min(count, clusters) > 0.5 * l2;
-        it.pad = 0;
-        order[f] = f;
-    }
-    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return sys[a].work > sys[b].work; });
-    int *dout = (int *)pout;
+    if ((st = scratch(ctx, "pg_counter", sizeof(int), &pcnt))) return st;
+    if (!plan.vx_smem && (st = scratch(ctx, "pg_vx", 8 * (size_t)plan.clusters * n_max, &pvx))) return st;
     PersistentArgs a;
     a.items = (const PersistentItem *)pitems;
     a.order = (const int *)porder;
@@ -1523,33 +1553,73 @@ nihu_gb_status solve_batched_device(nihu_gb_ctx *ctx, const std::vector<BatchSys
     a.n_max = (int)n_max;
     a.restart = m;
     a.max_iters = max_iters;
+    a.quantum = quantum;
     a.tol = tol;
-    a.V = (double2 *)pV;
-    a.counter = dout;
-    a.iters = dout + 1;
-    a.converged = dout + 1 + count;
-    a.rel = (double *)((char *)pout + off_rel);
+    a.counter = (int *)pcnt;
+    a.vxg = (float2 *)pvx;
     CK(cudaMemcpyAsync(pitems, items.data(), sizeof(PersistentItem) * count, cudaMemcpyHostToDevice, ctx->stream));
     CK(cudaMemcpyAsync(porder, order.data(), sizeof(int) * count, cudaMemcpyHostToDevice, ctx->stream));
-    CK(cudaMemsetAsync(dout, 0, sizeof(int), ctx->stream));
+    CK(cudaMemsetAsync(pcnt, 0, sizeof(int), ctx->stream));
     {
         // the phase name records the launch shape: clusters x CTAs per cluster
-        const std::string name = "persistent_gmres[" + std::to_string(clusters) + "x" + std::to_string(cluster) + "]";
+        const std::string name = "persistent_gmres[" + std::to_string(plan.clusters) + "x" + std::to_string(plan.cluster) +
+                                 (plan.vx_smem ? "" : ",vx global") + "]";
         Phase ph(ctx, name.c_str());
-        CK(launch_persistent_gmres(a, cluster, clusters, smem, ctx->stream));
+        CK(launch_persistent_gmres(a, plan.cluster, plan.clusters, plan.smem, ctx->stream));
     }
     ctx->launches += 1;
-    std::vector<int> hi(2 * (size_t)count);
-    std::vector<double> hr(count);
-    CK(cudaMemcpyAsync(hi.data(), dout + 1, sizeof(int) * 2 * count, cudaMemcpyDeviceToHost, ctx->stream));
-    CK(cudaMemcpyAsync(hr.data(), a.rel, 8 * (size_t)count, cudaMemcpyDeviceToHost, ctx->stream));
+    // the host vectors above are read by the copies: wait for them before they go
+    return sync(ctx);
+}
+
+// one persistent launch solving every system to the end; per-system outputs
+// on the host (may be NULL)
+nihu_gb_status solve_batched_device(nihu_gb_ctx *ctx, const std::vector<BatchSystem> &sys, int restart, int max_iters,
+                                    double tol, int *iters, double *rel, int *converged)
+{
+    const int count = (int)sys.size();
+    if (count == 0) return NIHU_GB_OK;
+    nihu_gb_status st;
+    int64_t n_max = 1, vtotal = 0;
+    for (const BatchSystem &s : sys) {
+        n_max = std::max(n_max, s.n);
+        vtotal += s.n;
+    }
+    const int m = (int)std::max<int64_t>(1, std::min<int64_t>(restart, n_max));
+    const size_t ss = persistent_small_state(m);
+    void *pV, *pS, *pst;
+    if ((st = scratch(ctx, "pg_V", 16 * (size_t)vtotal * (m + 1), &pV))) return st;
+    if ((st = scratch(ctx, "pg_S", 16 * ss * count, &pS))) return st;
+    if ((st = scratch(ctx, "pg_st", sizeof(PersistentState) * (size_t)count, &pst))) return st;
+    CK(cudaMemsetAsync(pst, 0, sizeof(PersistentState) * (size_t)count, ctx->stream));  // PG_FRESH
+    std::vector<PersistentItem> items(count);
+    std::vector<double> work(count);
+    int64_t voff = 0;
+    for (int f = 0; f < count; ++f) {
+        const BatchSystem &s = sys[f];
+        PersistentItem &it = items[f];
+        it.A = (const float2 *)s.A;
+        it.lda = s.lda;
+        it.b = s.b;
+        it.x = s.x;
+        it.V = (double2 *)pV + voff * (m + 1);
+        it.S = (double2 *)pS + ss * f;
+        it.st = (PersistentState *)pst + f;
+        it.n = (int)s.n;
+        it.pad = 0;
+        voff += s.n;
+        work[f] = s.work;
+    }
+    if ((st = launch_persistent(ctx, items, work, m, max_iters, 0, tol))) return st;
+    std::vector<PersistentState> hs(count);
+    CK(cudaMemcpyAsync(hs.data(), pst, sizeof(PersistentState) * count, cudaMemcpyDeviceToHost, ctx->stream));
     if ((st = sync(ctx))) return st;
     bool all = true;
     for (int f = 0; f < count; ++f) {
-        if (iters) iters[f] = hi[f];
-        if (converged) converged[f] = hi[count + f];
-        if (rel) rel[f] = hr[f];
-        all = all && hi[count + f];
+        if (iters) iters[f] = hs[f].iters;
+        if (converged) converged[f] = hs[f].converged;
+        if (rel) rel[f] = hs[f].rel;
+        all = all && hs[f].converged;
     }
     if (!all) return fail(ctx, NIHU_GB_ERR_NOT_CONVERGED, "batched GMRES: some systems did not reach the tolerance");
     return NIHU_GB_OK;
@@ -1723,4 +1793,294 @@ extern "C" nihu_gb_status nihu_gb_solve_sweep(nihu_gb_ctx *ctx, const nihu_gb_me
     if (cycles) *cycles = (most + r - 1) / r;
     if (iters) *iters = most;
     return st;
+}
+
+// ------------------------------------------------------------ serving loop
+//
+// Continuous batching of CBIE solves (helmholtz_3d_coll.cpp:36-120 once per
+// request): requests wait in a FIFO queue until the HBM budget holds their
+// matrices and Krylov state; every round admits what fits, assembles the new
+// requests (one frequency batch per mesh), forms their right-hand sides,
+// advances every admitted system by at most `quantum` GMRES steps in one
+// persistent launch, and retires the finished ones.  Matrices, Krylov state
+// and iterates stay in device memory between rounds; memory comes from a
+// stream-ordered pool, so admission and retirement never synchronise the
+// device beyond the one wait per round.
+
+struct nihu_gb_server {
+    struct Request {
+        int64_t id = 0;
+        int mesh = 0;
+        double k = 0.0;
+        std::vector<double2> q;  // Neumann data until admission; then the result p
+        size_t held = 0;         // budget bytes held
+        void *G = nullptr, *H = nullptr, *blk = nullptr;
+        double2 *dq = nullptr, *b = nullptr, *x = nullptr, *V = nullptr, *S = nullptr;
+        int slot = -1;  // status word in the server's state array
+        PersistentState st{};
+    };
+    nihu_gb_ctx *ctx = nullptr;
+    std::vector<const nihu_gb_mesh *> meshes;
+    int family = 0, precision = 0, restart = 0, max_iters = 0, quantum = 0;
+    double tol = 0.0;
+    size_t budget = 0, held = 0;
+    cudaMemPool_t pool = nullptr;
+    PersistentState *d_states = nullptr;  // one slot per admitted request
+    int n_slots = 0;
+    std::vector<int> free_slots;
+    std::deque<Request *> queue;
+    std::vector<Request *> active;
+    std::deque<Request *> done;
+    int64_t next_id = 0;
+};
+
+namespace {
+
+typedef nihu_gb_server::Request SrvReq;
+
+size_t srv_align(size_t x) { return (x + 255) & ~(size_t)255; }
+
+// device bytes of one request's vectors, basis, small state: [q b x | V | S]
+size_t srv_block_bytes(int64_t n, int m)
+{
+    return srv_align(3 * 16 * (size_t)n) + srv_align(16 * (size_t)n * (m + 1)) + srv_align(16 * persistent_small_state(m));
+}
+
+void srv_release(nihu_gb_server *sv, SrvReq *r)
+{
+    cudaStream_t s = sv->ctx->stream;
+    if (r->G) cudaFreeAsync(r->G, s);
+    if (r->H) cudaFreeAsync(r->H, s);
+    if (r->blk) cudaFreeAsync(r->blk, s);
+    r->G = r->H = r->blk = nullptr;
+    if (r->slot >= 0) sv->free_slots.push_back(r->slot);
+    r->slot = -1;
+    sv->held -= r->held;
+    r->held = 0;
+}
+
+}  // namespace
+
+extern "C" nihu_gb_status nihu_gb_server_create(nihu_gb_ctx *ctx, int n_meshes, const nihu_gb_mesh *const *meshes,
+                                                int family, int precision, size_t hbm_budget_bytes, int max_active,
+                                                int restart, int max_iters, double tol, int quantum,
+                                                nihu_gb_server **out)
+{
+    if (!ctx || !out) return NIHU_GB_ERR_INVALID_ARGUMENT;
+    *out = nullptr;
+    if (n_meshes < 1 || !meshes || (precision != 0 && precision != 1) ||
+        (family != NIHU_GB_HELMHOLTZ_3D && family != NIHU_GB_LAPLACE_3D) || hbm_budget_bytes == 0 || max_active < 1 ||
+        restart < 1 || restart > 200 || max_iters < 1 || !(tol > 0.0) || quantum < 0)
+        return fail(ctx, NIHU_GB_ERR_INVALID_ARGUMENT, "nihu_gb_server_create: bad argument");
+    for (int i = 0; i < n_meshes; ++i)
+        if (!meshes[i] || meshes[i]->ctx != ctx || meshes[i]->n < 1)
+            return fail(ctx, NIHU_GB_ERR_INVALID_ARGUMENT, "nihu_gb_server_create: bad mesh");
+    cudaSetDevice(ctx->device);
+    std::unique_ptr<nihu_gb_server> sv(new nihu_gb_server);
+    sv->ctx = ctx;
+    sv->meshes.assign(meshes, meshes + n_meshes);
+    sv->family = family;
+    sv->precision = precision;
+    sv->budget = hbm_budget_bytes;
+    sv->restart = restart;
+    sv->max_iters = max_iters;
+    sv->tol = tol;
+    sv->quantum = quantum;
+    cudaMemPoolProps props = {};
+    props.allocType = cudaMemAllocationTypePinned;
+    props.location.type = cudaMemLocationTypeDevice;
+    props.location.id = ctx->device;
+    CK(cudaMemPoolCreate(&sv->pool, &props));
+    uint64_t keep = UINT64_MAX;  // freed blocks stay in the pool for the next requests
+    CK(cudaMemPoolSetAttribute(sv->pool, cudaMemPoolAttrReleaseThreshold, &keep));
+    sv->n_slots = max_active;
+    void *p;
+    nihu_gb_status st;
+    if ((st = dmalloc(ctx, sizeof(PersistentState) * (size_t)max_active, &p))) {
+        cudaMemPoolDestroy(sv->pool);
+        return st;
+    }
+    sv->d_states = (PersistentState *)p;
+    for (int i = max_active - 1; i >= 0; --i) sv->free_slots.push_back(i);
+    *out = sv.release();
+    return NIHU_GB_OK;
+}
+
+extern "C" void nihu_gb_server_destroy(nihu_gb_server *sv)
+{
+    if (!sv) return;
+    cudaSetDevice(sv->ctx->device);
+    for (SrvReq *r : sv->active) srv_release(sv, r);
+    cudaStreamSynchronize(sv->ctx->stream);
+    for (SrvReq *r : sv->queue) delete r;
+    for (SrvReq *r : sv->active) delete r;
+    for (SrvReq *r : sv->done) delete r;
+    dfree(sv->ctx, sv->d_states);
+    cudaMemPoolDestroy(sv->pool);
+    delete sv;
+}
+
+extern "C" nihu_gb_status nihu_gb_server_submit(nihu_gb_server *sv, int mesh, double k, const void *q, int64_t *id)
+{
+    if (!sv) return NIHU_GB_ERR_INVALID_ARGUMENT;
+    nihu_gb_ctx *ctx = sv->ctx;
+    if (mesh < 0 || mesh >= (int)sv->meshes.size() || !std::isfinite(k) || !q)
+        return fail(ctx, NIHU_GB_ERR_INVALID_ARGUMENT, "nihu_gb_server_submit: bad argument");
+    const int64_t n = sv->meshes[mesh]->n;
+    const size_t need = 16 * (size_t)n * n + srv_block_bytes(n, sv->restart);
+    if (need > sv->budget)
+        return fail(ctx, NIHU_GB_ERR_OUT_OF_MEMORY, "nihu_gb_server_submit: request larger than the HBM budget");
+    SrvReq *r = new SrvReq;
+    r->id = sv->next_id++;
+    r->mesh = mesh;
+    r->k = k;
+    r->q.assign((const double2 *)q, (const double2 *)q + n);
+    sv->queue.push_back(r);
+    if (id) *id = r->id;
+    return NIHU_GB_OK;
+}
+
+extern "C" nihu_gb_status nihu_gb_server_step(nihu_gb_server *sv, int *n_queued, int *n_active, int *n_done)
+{
+    if (!sv) return NIHU_GB_ERR_INVALID_ARGUMENT;
+    nihu_gb_ctx *ctx = sv->ctx;
+    cudaSetDevice(ctx->device);
+    cudaStream_t s = ctx->stream;
+    nihu_gb_status st;
+    const int m = sv->restart;
+    // 1. admission, first come first served, while the budget and the state slots hold
+    std::vector<SrvReq *> fresh;
+    while (!sv->queue.empty() && !sv->free_slots.empty()) {
+        SrvReq *r = sv->queue.front();
+        const int64_t n = sv->meshes[r->mesh]->n;
+        const size_t mat = 8 * (size_t)n * n, blk = srv_block_bytes(n, m);
+        if (sv->held + 2 * mat + blk > sv->budget) break;
+        CK(cudaMallocFromPoolAsync(&r->G, mat, sv->pool, s));
+        CK(cudaMallocFromPoolAsync(&r->H, mat, sv->pool, s));
+        CK(cudaMallocFromPoolAsync(&r->blk, blk, sv->pool, s));
+        r->held = 2 * mat + blk;
+        sv->held += r->held;
+        char *p = (char *)r->blk;
+        r->dq = (double2 *)p;
+        r->b = r->dq + n;
+        r->x = r->b + n;
+        p += srv_align(3 * 16 * (size_t)n);
+        r->V = (double2 *)p;
+        p += srv_align(16 * (size_t)n * (m + 1));
+        r->S = (double2 *)p;
+        r->slot = sv->free_slots.back();
+        sv->free_slots.pop_back();
+        CK(cudaMemcpyAsync(r->dq, r->q.data(), 16 * (size_t)n, cudaMemcpyHostToDevice, s));
+        CK(cudaMemsetAsync(sv->d_states + r->slot, 0, sizeof(PersistentState), s));  // PG_FRESH
+        sv->queue.pop_front();
+        fresh.push_back(r);
+    }
+    // 2. assembly of the new requests, one frequency batch per mesh; right-hand sides
+    std::vector<std::vector<void *>> tables;  // host sources of the pointer uploads, alive until the round's wait
+    for (int i = 0; i < (int)sv->meshes.size(); ++i) {
+        std::vector<SrvReq *> grp;
+        for (SrvReq *r : fresh)
+            if (r->mesh == i) grp.push_back(r);
+        if (grp.empty()) continue;
+        const nihu_gb_mesh *mesh = sv->meshes[i];
+        const int64_t n = mesh->n;
+        const int nk = (int)grp.size();
+        std::vector<double> ks(nk);
+        tables.emplace_back(2 * (size_t)nk);
+        std::vector<void *> &tab = tables.back();
+        for (int f = 0; f < nk; ++f) {
+            ks[f] = grp[f]->k;
+            tab[f] = grp[f]->G;
+            tab[nk + f] = grp[f]->H;
+        }
+        // always the frequency-batch kernels: an entry is then the same whatever else arrived with it
+        void *douts = nullptr;
+        const std::string name = "srv_outs" + std::to_string(i);
+        if ((st = scratch(ctx, name.c_str(), sizeof(void *) * 2 * (size_t)nk, &douts))) return st;
+        CK(cudaMemcpyAsync(douts, tab.data(), sizeof(void *) * 2 * (size_t)nk, cudaMemcpyHostToDevice, s));
+        if ((st = assemble_batch(ctx, mesh, mesh, sv->family, NIHU_GB_SLP | NIHU_GB_DLP, ks.data(), nk, sv->precision,
+                                 NIHU_GB_C64, grp[0]->G, grp[0]->H, n, n * n, (void *const *)douts, true)))
+            return st;
+        const int splits = gemv_splits(n, n, NIHU_GB_C64);
+        void *part;
+        if ((st = scratch(ctx, "srv_part", 16 * (size_t)splits * n, &part))) return st;
+        for (SrvReq *r : grp) {
+            CK(launch_add_identity((int)n, -0.5, 0.0, NIHU_GB_C64, r->H, n, s));
+            CK(timed_gemv(ctx, NIHU_GB_C64, r->G, n, n, n, r->dq, r->b, 1.0, 0.0, 0.0, 0.0, (double2 *)part, splits));
+            ctx->launches += 1;
+            // the single-layer matrix is only needed for the right-hand side
+            CK(cudaFreeAsync(r->G, s));
+            r->G = nullptr;
+            r->held -= 8 * (size_t)n * n;
+            sv->held -= 8 * (size_t)n * n;
+        }
+        sv->active.insert(sv->active.end(), grp.begin(), grp.end());
+    }
+    // 3. every admitted system advances by at most `quantum` steps
+    if (!sv->active.empty()) {
+        std::vector<PersistentItem> items(sv->active.size());
+        std::vector<double> work(sv->active.size());
+        for (size_t t = 0; t < sv->active.size(); ++t) {
+            SrvReq *r = sv->active[t];
+            const int64_t n = sv->meshes[r->mesh]->n;
+            PersistentItem &it = items[t];
+            it.A = (const float2 *)r->H;
+            it.lda = n;
+            it.b = r->b;
+            it.x = r->x;
+            it.V = r->V;
+            it.S = r->S;
+            it.st = sv->d_states + r->slot;
+            it.n = (int)n;
+            it.pad = 0;
+            work[t] = (double)n * (double)n;
+        }
+        if ((st = launch_persistent(ctx, items, work, m, sv->max_iters, sv->quantum, sv->tol))) return st;
+    }
+    // 4. retire the finished systems
+    std::vector<PersistentState> hs(sv->n_slots);
+    CK(cudaMemcpyAsync(hs.data(), sv->d_states, sizeof(PersistentState) * sv->n_slots, cudaMemcpyDeviceToHost, s));
+    if ((st = sync(ctx))) return st;
+    std::vector<SrvReq *> still;
+    std::vector<SrvReq *> finished;
+    for (SrvReq *r : sv->active) {
+        r->st = hs[r->slot];
+        if (r->st.status == PG_DONE) finished.push_back(r);
+        else still.push_back(r);
+    }
+    for (SrvReq *r : finished) {
+        const int64_t n = sv->meshes[r->mesh]->n;
+        r->q.resize(n);
+        CK(cudaMemcpyAsync(r->q.data(), r->x, 16 * (size_t)n, cudaMemcpyDeviceToHost, s));
+    }
+    if (!finished.empty() && (st = sync(ctx))) return st;
+    for (SrvReq *r : finished) {
+        srv_release(sv, r);
+        sv->done.push_back(r);
+    }
+    sv->active.swap(still);
+    if (n_queued) *n_queued = (int)sv->queue.size();
+    if (n_active) *n_active = (int)sv->active.size();
+    if (n_done) *n_done = (int)sv->done.size();
+    return NIHU_GB_OK;
+}
+
+extern "C" nihu_gb_status nihu_gb_server_take(nihu_gb_server *sv, int64_t *id, void *p, int64_t capacity, int *iters,
+                                              double *rel_residual, int *converged)
+{
+    if (!sv || !id) return NIHU_GB_ERR_INVALID_ARGUMENT;
+    *id = -1;
+    if (sv->done.empty()) return NIHU_GB_OK;
+    SrvReq *r = sv->done.front();
+    const int64_t n = (int64_t)r->q.size();
+    if (!p || capacity < n)
+        return fail(sv->ctx, NIHU_GB_ERR_INVALID_ARGUMENT, "nihu_gb_server_take: result buffer too small");
+    std::memcpy(p, r->q.data(), 16 * (size_t)n);
+    *id = r->id;
+    if (iters) *iters = r->st.iters;
+    if (rel_residual) *rel_residual = r->st.rel;
+    if (converged) *converged = r->st.converged;
+    sv->done.pop_front();
+    delete r;
+    return NIHU_GB_OK;
 }

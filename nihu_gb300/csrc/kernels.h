@@ -61,7 +61,21 @@ struct RegularArgs {
     const float *ks32 = nullptr;
     int64_t mat_stride = 0;
     double k_absmax = 0.0;  // largest |ks[f]| of a frequency batch
+    // frequency batch into separate matrices (mat_stride unused): SLP matrix
+    // f at outs[f], DLP matrix f at outs[nk + f] (device array of pointers)
+    void *const *outs = nullptr;
+    // 1: the frequency-batch kernels even for nk = 1, so that an entry is the
+    // same whatever the batch it is assembled in
+    int force_batch = 0;
 };
+
+// matrix f of a frequency batch (dlp: the DLP output)
+template <typename Out>
+__device__ __forceinline__ Out *batch_matrix(const RegularArgs &a, bool dlp, int f)
+{
+    if (a.outs) return reinterpret_cast<Out *>(a.outs[(dlp ? a.nk : 0) + f]);
+    return reinterpret_cast<Out *>(dlp ? a.out_d : a.out_s) + (int64_t)f * a.mat_stride;
+}
 cudaError_t launch_assemble_regular(const RegularArgs &a, cudaStream_t s);
 
 // assemble_singular.cu ----------------------------------------------------

@@ -15,12 +15,20 @@
 // after a cluster barrier, so all CTAs of a cluster pass the same sequence of
 // barriers.
 //
+// Every system keeps its whole Krylov state in device memory (basis V, the
+// Hessenberg matrix, Givens rotations, g, the iterate x and a status word),
+// so a launch may advance each system by at most `quantum` Arnoldi steps and
+// a later launch resumes it exactly where it stopped: the result is bitwise
+// the same however the steps are split over launches and whatever else
+// shares them.  This is what a serving loop needs to admit new systems
+// between launches.
+//
 // The stopping rules are those of the single-system solver (capi.cu,
 // gmres_device): a relative residual estimate |g_{k+1}| / |b| below tol, the
 // iteration cap, a zero Krylov vector or k = n end the solve; a cycle that
 // reaches the restart length restarts from the true residual b - A x.
-// Every loop is bounded by the iteration cap; the only waits are hardware
-// cluster barriers, which all CTAs of the cluster reach.
+// Every loop is bounded by the iteration cap or the quantum; the only waits
+// are hardware cluster barriers, which all CTAs of the cluster reach.
 
 #include <cooperative_groups.h>
 
@@ -64,8 +72,10 @@ __device__ __forceinline__ float4 load_a(const float4 *p)
     return __ldg(p);
 }
 
-// wl[row - ra] = sum_j A[row, j] vx[j] for the rows of pairs [pa, pb)
-template <bool STREAM>
+// wl[row - ra] = sum_j A[row, j] vx[j] for the rows of pairs [pa, pb); the
+// input vector vx is in shared memory, or (VXG) in a global buffer that the
+// cluster rewrites every step (read around L1)
+template <bool STREAM, bool VXG>
 __device__ void matvec_rows(const float2 *__restrict__ A, int64_t lda, int n, int pa, int pb, int ra, bool vec,
                             const float2 *vx, double2 *wl, float4 *red)
 {
@@ -84,15 +94,21 @@ __device__ void matvec_rows(const float2 *__restrict__ A, int64_t lda, int n, in
                 int j = js;
                 for (; j + 8 <= je; j += 8) {
                     float4 v[8];
+                    float2 xv[8];
 #pragma unroll
-                    for (int u = 0; u < 8; ++u) v[u] = load_a<STREAM>(col + (int64_t)(j - js + u) * stride);
+                    for (int u = 0; u < 8; ++u) {
+                        v[u] = load_a<STREAM>(col + (int64_t)(j - js + u) * stride);
+                        xv[u] = VXG ? __ldcg(vx + j + u) : vx[j + u];
+                    }
 #pragma unroll
-                    for (int u = 0; u < 8; ++u) fma_pair(v[u], vx[j + u], ar0, ai0, ar1, ai1);
+                    for (int u = 0; u < 8; ++u) fma_pair(v[u], xv[u], ar0, ai0, ar1, ai1);
                 }
-                for (; j < je; ++j) fma_pair(load_a<STREAM>(col + (int64_t)(j - js) * stride), vx[j], ar0, ai0, ar1, ai1);
+                for (; j < je; ++j)
+                    fma_pair(load_a<STREAM>(col + (int64_t)(j - js) * stride), VXG ? __ldcg(vx + j) : vx[j], ar0, ai0,
+                             ar1, ai1);
             } else {
                 for (int j = js; j < je; ++j) {
-                    const float2 xv = vx[j];
+                    const float2 xv = VXG ? __ldcg(vx + j) : vx[j];
                     fma_one(A[(int64_t)j * lda + row], xv, ar0, ai0);
                     if (row + 1 < n) fma_one(A[(int64_t)j * lda + row + 1], xv, ar1, ai1);
                 }
@@ -138,9 +154,10 @@ __global__ void __launch_bounds__(PT, 1) k_persistent_gmres(PersistentArgs a)
     const int cid = blockIdx.x / C;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int m = a.restart;
-    const PersistentSmem L = persistent_smem_layout(a.n_max, C, m);
+    const bool vxg = a.vxg != nullptr;
+    const PersistentSmem L = persistent_smem_layout(a.n_max, C, m, !vxg);
     extern __shared__ __align__(16) unsigned char sm[];
-    float2 *vx = reinterpret_cast<float2 *>(sm + L.vx);
+    float2 *vx = vxg ? a.vxg + (int64_t)cid * a.n_max : reinterpret_cast<float2 *>(sm + L.vx);
     double2 *wl = reinterpret_cast<double2 *>(sm + L.wl);
     float4 *red = reinterpret_cast<float4 *>(sm + L.red);
     double2 *hp = reinterpret_cast<double2 *>(sm + L.hp);
@@ -153,8 +170,8 @@ __global__ void __launch_bounds__(PT, 1) k_persistent_gmres(PersistentArgs a)
     double2 *y = reinterpret_cast<double2 *>(sm + L.y);
     __shared__ int ctl[4];
     __shared__ double2 scal[1];
-    double2 *V = a.V + (int64_t)cid * (m + 1) * a.n_max;  // this cluster's basis, vector v at V + v * n_max
-    const int hstride = L.blocks * (m + 2);                // one partial buffer: [local block][entry]
+    const int hstride = L.blocks * (m + 2);  // one partial buffer: [local block][entry]
+    const int budget = a.quantum > 0 ? a.quantum : 0x7fffffff;
     int buf = 0, slot = 1;
     int nb = 0;  // row blocks of the current system
 
@@ -190,13 +207,6 @@ __global__ void __launch_bounds__(PT, 1) k_persistent_gmres(PersistentArgs a)
         slot = slot == 3 ? 1 : slot + 1;
         return d;
     };
-    auto load_vx = [&](const double2 *src, int n) {
-        for (int j = tid; j < n; j += PT) {
-            const double2 v = __ldcg(src + j);
-            vx[j] = make_float2((float)v.x, (float)v.y);
-        }
-        __syncthreads();
-    };
 
     for (;;) {
         if (rank == 0 && tid == 0) ctl[0] = atomicAdd(a.counter, 1);
@@ -212,6 +222,9 @@ __global__ void __launch_bounds__(PT, 1) k_persistent_gmres(PersistentArgs a)
         const int b0 = (int)((int64_t)rank * nb / C), b1 = (int)((int64_t)(rank + 1) * nb / C), nlb = b1 - b0;
         const int pa = min(P, b0 * TILE), pb = min(P, b1 * TILE);
         const int ra = min(n, 2 * pa), rb = min(n, 2 * pb);
+        double2 *V = it.V;  // basis vector v at V + v * n
+        const bool vec = it.vec != 0;
+
         // |w|^2 of the cluster's rows: per-block partials, then the block-ordered sum
         auto cluster_norm2 = [&]() -> double {
             double2 *mine = hp + buf * hstride;
@@ -225,115 +238,53 @@ __global__ void __launch_bounds__(PT, 1) k_persistent_gmres(PersistentArgs a)
             cluster_sum(1, scal);
             return scal[0].x;
         };
-        const bool vec = it.vec != 0;
-        auto matvec = [&]() {
-            if (it.stream) matvec_rows<true>(it.A, it.lda, n, pa, pb, ra, vec, vx, wl, red);
-            else matvec_rows<false>(it.A, it.lda, n, pa, pb, ra, vec, vx, wl, red);
-        };
-
-        // x = 0, r = b
-        for (int i = ra + tid; i < rb; i += PT) {
-            it.x[i] = make_double2(0.0, 0.0);
-            wl[i - ra] = it.b[i];
-        }
-        __syncthreads();
-        const double r0 = sqrt(cluster_norm2());
-        int iters = 0;
-        double rel = 0.0;  // meaningful in thread 0
-        if (decide(!(r0 == 0.0)) == 0) {
-            if (rank == 0 && tid == 0) {
-                a.iters[f] = 0;
-                a.rel[f] = 0.0;
-                a.converged[f] = 1;
-            }
-            continue;
-        }
-        double beta = r0;
-        for (;;) {  // restart cycles
-            {
-                const double ib = 1.0 / beta;
+        // the matvec input: src (complete across the cluster) as complex64
+        auto load_vx = [&](const double2 *src) {
+            if (vxg) {
                 for (int i = ra + tid; i < rb; i += PT) {
-                    const double2 w = wl[i - ra];
-                    V[i] = make_double2(w.x * ib, w.y * ib);
+                    const double2 v = __ldcg(src + i);
+                    vx[i] = make_float2((float)v.x, (float)v.y);
                 }
+                cl.sync();
+            } else {
+                for (int j = tid; j < n; j += PT) {
+                    const double2 v = __ldcg(src + j);
+                    vx[j] = make_float2((float)v.x, (float)v.y);
+                }
+                __syncthreads();
+            }
+        };
+        auto matvec = [&]() {
+            if (it.stream) {
+                if (vxg) matvec_rows<true, true>(it.A, it.lda, n, pa, pb, ra, vec, vx, wl, red);
+                else matvec_rows<true, false>(it.A, it.lda, n, pa, pb, ra, vec, vx, wl, red);
+            } else {
+                if (vxg) matvec_rows<false, true>(it.A, it.lda, n, pa, pb, ra, vec, vx, wl, red);
+                else matvec_rows<false, false>(it.A, it.lda, n, pa, pb, ra, vec, vx, wl, red);
+            }
+        };
+        // a new cycle from the residual in wl with norm beta: V_0 and g = beta e_1
+        auto begin_cycle = [&](double beta) {
+            const double ib = 1.0 / beta;
+            for (int i = ra + tid; i < rb; i += PT) {
+                const double2 w = wl[i - ra];
+                V[i] = make_double2(w.x * ib, w.y * ib);
             }
             if (tid == 0) {
                 g[0] = make_double2(beta, 0.0);
                 for (int i = 1; i <= m; ++i) g[i] = make_double2(0.0, 0.0);
             }
-            cl.sync();  // V_0 complete across the cluster
-            load_vx(V, n);
-            int kdone = 0, d = 0;
-            for (int k = 0; k < m; ++k) {
-                ++iters;
-                matvec();
-                if (tid <= k) hk[tid] = make_double2(0.0, 0.0);
-                for (int pass = 0; pass < 2; ++pass) {  // CGS2
-                    double2 *mine = hp + buf * hstride;
-                    for (int task = warp; task < nlb * (k + 1); task += PW) {
-                        const int lb = task / (k + 1), v = task - lb * (k + 1);
-                        const double2 *Vv = V + (int64_t)v * a.n_max;
-                        const int i0 = ra + lb * 2 * TILE, i1 = min(rb, i0 + 2 * TILE);
-                        double sr = 0.0, si = 0.0;
-                        for (int i = i0 + lane; i < i1; i += 32) {
-                            const double2 t = zconjmul(__ldcg(Vv + i), wl[i - ra]);
-                            sr += t.x;
-                            si += t.y;
-                        }
-                        sr = warp_sum(sr);
-                        si = warp_sum(si);
-                        if (lane == 0) mine[lb * (m + 2) + v] = make_double2(sr, si);
-                    }
-                    cluster_sum(k + 1, hc);
-                    if (tid <= k) hk[tid] = zadd(hk[tid], hc[tid]);
-                    for (int i = ra + tid; i < rb; i += PT) {
-                        double2 acc = wl[i - ra];
-                        for (int v = 0; v <= k; ++v) acc = zsub(acc, zmul(__ldcg(V + (int64_t)v * a.n_max + i), hc[v]));
-                        wl[i - ra] = acc;
-                    }
-                    __syncthreads();
-                }
-                const double hn = sqrt(cluster_norm2());
-                if (hn > 0.0) {
-                    const double s = 1.0 / hn;
-                    double2 *Vn = V + (int64_t)(k + 1) * a.n_max;
-                    for (int i = ra + tid; i < rb; i += PT) {
-                        const double2 w = wl[i - ra];
-                        Vn[i] = make_double2(w.x * s, w.y * s);
-                    }
-                }
-                int local = 0;
-                if (tid == 0) {
-                    // previous rotations, then a new one zeroing the subdiagonal
-                    double2 *Hk = H + (int64_t)k * (m + 1);
-                    for (int i = 0; i <= k; ++i) Hk[i] = hk[i];
-                    Hk[k + 1] = make_double2(hn, 0.0);
-                    for (int i = 0; i < k; ++i) {
-                        const double2 a0 = Hk[i], a1 = Hk[i + 1];
-                        Hk[i] = zadd(zconjmul(cs[i], a0), zconjmul(sn[i], a1));
-                        Hk[i + 1] = zsub(zmul(cs[i], a1), zmul(sn[i], a0));
-                    }
-                    const double2 a0 = Hk[k], a1 = Hk[k + 1];
-                    const double den = sqrt(zabs2(a0) + zabs2(a1));
-                    const double2 c = den == 0.0 ? make_double2(1.0, 0.0) : make_double2(a0.x / den, a0.y / den);
-                    const double2 sv = den == 0.0 ? make_double2(0.0, 0.0) : make_double2(a1.x / den, a1.y / den);
-                    cs[k] = c;
-                    sn[k] = sv;
-                    Hk[k] = zadd(zconjmul(c, a0), zconjmul(sv, a1));
-                    Hk[k + 1] = make_double2(0.0, 0.0);
-                    const double2 g0 = g[k], g1 = g[k + 1];
-                    g[k] = zadd(zconjmul(c, g0), zconjmul(sv, g1));
-                    g[k + 1] = zsub(zmul(c, g1), zmul(sv, g0));
-                    rel = sqrt(zabs2(g[k + 1])) / r0;
-                    const bool stop = rel < a.tol || iters >= a.max_iters || hn == 0.0 || k + 1 == n;
-                    local = stop ? 2 : (k + 1 == m ? 1 : 0);
-                }
-                kdone = k + 1;
-                d = decide(local);  // also completes V_{k+1} across the cluster
-                if (d) break;
-                load_vx(V + (int64_t)(k + 1) * a.n_max, n);
-            }
-            // y = H^{-1} g (upper triangular after the rotations), x += V y on the own rows
+        };
+        // wl = b - A x on the own rows
+        auto residual = [&]() {
+            cl.sync();  // x complete across the cluster
+            load_vx(it.x);
+            matvec();
+            for (int i = ra + tid; i < rb; i += PT) wl[i - ra] = zsub(it.b[i], wl[i - ra]);
+            __syncthreads();
+        };
+        // y = H^{-1} g over kdone steps (upper triangular after the rotations), x += V y on the own rows
+        auto update_x = [&](int kdone) {
             if (tid == 0) {
                 for (int i = kdone - 1; i >= 0; --i) {
                     double2 s = g[i];
@@ -346,35 +297,182 @@ __global__ void __launch_bounds__(PT, 1) k_persistent_gmres(PersistentArgs a)
             __syncthreads();
             for (int i = ra + tid; i < rb; i += PT) {
                 double2 acc = it.x[i];
-                for (int v = 0; v < kdone; ++v) acc = zadd(acc, zmul(__ldcg(V + (int64_t)v * a.n_max + i), y[v]));
+                for (int v = 0; v < kdone; ++v) acc = zadd(acc, zmul(__ldcg(V + (int64_t)v * n + i), y[v]));
                 it.x[i] = acc;
             }
-            if (d == 2) break;
-            // restart from the true residual r = b - A x
-            cl.sync();  // x complete across the cluster
-            load_vx(it.x, n);
-            matvec();
-            for (int i = ra + tid; i < rb; i += PT) wl[i - ra] = zsub(it.b[i], wl[i - ra]);
+        };
+
+        // the state left by earlier launches (the same for every CTA of the cluster)
+        const PersistentState st = *it.st;
+        int status = st.status, k = st.k, iters = st.iters;
+        double r0 = st.r0;
+        double rel = st.rel;  // meaningful in thread 0
+        int steps = 0;
+        int finished = 0;  // 1: done in this launch; 2: done with a zero residual
+        if (status == PG_FRESH) {
+            // x = 0, r = b
+            for (int i = ra + tid; i < rb; i += PT) {
+                it.x[i] = make_double2(0.0, 0.0);
+                wl[i - ra] = it.b[i];
+            }
             __syncthreads();
-            beta = sqrt(cluster_norm2());
+            r0 = sqrt(cluster_norm2());
+            if (decide(!(r0 == 0.0)) == 0) {
+                finished = 2;
+            } else {
+                begin_cycle(r0);
+                k = 0;
+            }
+        } else if (status == PG_RESTART) {
+            residual();
+            const double beta = sqrt(cluster_norm2());
             if (decide(!(beta == 0.0)) == 0) {
-                if (tid == 0) rel = 0.0;
+                finished = 2;
+            } else {
+                begin_cycle(beta);
+                k = 0;
+            }
+        } else if (status == PG_IN_CYCLE) {
+            const double2 *S = it.S;
+            const int hs = (m + 1) * m;
+            for (int t = tid; t < hs; t += PT) H[t] = S[t];
+            for (int t = tid; t < m; t += PT) {
+                cs[t] = S[hs + t];
+                sn[t] = S[hs + m + t];
+            }
+            for (int t = tid; t <= m; t += PT) g[t] = S[hs + 2 * m + t];
+            __syncthreads();
+        } else {
+            finished = 3;  // already done: left as it is
+        }
+
+        while (finished == 0) {
+            cl.sync();  // V_k complete across the cluster
+            load_vx(V + (int64_t)k * n);
+            ++iters;
+            ++steps;
+            matvec();
+            if (tid <= k) hk[tid] = make_double2(0.0, 0.0);
+            for (int pass = 0; pass < 2; ++pass) {  // CGS2
+                double2 *mine = hp + buf * hstride;
+                for (int task = warp; task < nlb * (k + 1); task += PW) {
+                    const int lb = task / (k + 1), v = task - lb * (k + 1);
+                    const double2 *Vv = V + (int64_t)v * n;
+                    const int i0 = ra + lb * 2 * TILE, i1 = min(rb, i0 + 2 * TILE);
+                    double sr = 0.0, si = 0.0;
+                    for (int i = i0 + lane; i < i1; i += 32) {
+                        const double2 t = zconjmul(__ldcg(Vv + i), wl[i - ra]);
+                        sr += t.x;
+                        si += t.y;
+                    }
+                    sr = warp_sum(sr);
+                    si = warp_sum(si);
+                    if (lane == 0) mine[lb * (m + 2) + v] = make_double2(sr, si);
+                }
+                cluster_sum(k + 1, hc);
+                if (tid <= k) hk[tid] = zadd(hk[tid], hc[tid]);
+                for (int i = ra + tid; i < rb; i += PT) {
+                    double2 acc = wl[i - ra];
+                    for (int v = 0; v <= k; ++v) acc = zsub(acc, zmul(__ldcg(V + (int64_t)v * n + i), hc[v]));
+                    wl[i - ra] = acc;
+                }
+                __syncthreads();
+            }
+            const double hn = sqrt(cluster_norm2());
+            if (hn > 0.0) {
+                const double s = 1.0 / hn;
+                double2 *Vn = V + (int64_t)(k + 1) * n;
+                for (int i = ra + tid; i < rb; i += PT) {
+                    const double2 w = wl[i - ra];
+                    Vn[i] = make_double2(w.x * s, w.y * s);
+                }
+            }
+            int local = 0;
+            if (tid == 0) {
+                // previous rotations, then a new one zeroing the subdiagonal
+                double2 *Hk = H + (int64_t)k * (m + 1);
+                for (int i = 0; i <= k; ++i) Hk[i] = hk[i];
+                Hk[k + 1] = make_double2(hn, 0.0);
+                for (int i = 0; i < k; ++i) {
+                    const double2 a0 = Hk[i], a1 = Hk[i + 1];
+                    Hk[i] = zadd(zconjmul(cs[i], a0), zconjmul(sn[i], a1));
+                    Hk[i + 1] = zsub(zmul(cs[i], a1), zmul(sn[i], a0));
+                }
+                const double2 a0 = Hk[k], a1 = Hk[k + 1];
+                const double den = sqrt(zabs2(a0) + zabs2(a1));
+                const double2 c = den == 0.0 ? make_double2(1.0, 0.0) : make_double2(a0.x / den, a0.y / den);
+                const double2 sv = den == 0.0 ? make_double2(0.0, 0.0) : make_double2(a1.x / den, a1.y / den);
+                cs[k] = c;
+                sn[k] = sv;
+                Hk[k] = zadd(zconjmul(c, a0), zconjmul(sv, a1));
+                Hk[k + 1] = make_double2(0.0, 0.0);
+                const double2 g0 = g[k], g1 = g[k + 1];
+                g[k] = zadd(zconjmul(c, g0), zconjmul(sv, g1));
+                g[k + 1] = zsub(zmul(c, g1), zmul(sv, g0));
+                rel = sqrt(zabs2(g[k + 1])) / r0;
+                const bool stop = rel < a.tol || iters >= a.max_iters || hn == 0.0 || k + 1 == n;
+                // 2: stop, 1: end of the cycle, 3: quantum used up inside the cycle, 0: next step
+                local = stop ? 2 : (k + 1 == m ? 1 : (steps >= budget ? 3 : 0));
+            }
+            const int d = decide(local);  // also completes V_{k+1} across the cluster
+            if (d == 0) {
+                ++k;
+                continue;
+            }
+            if (d == 3) {
+                // pause inside the cycle: the small state goes to memory for the next launch
+                if (rank == 0) {
+                    double2 *S = it.S;
+                    const int hs = (m + 1) * m;
+                    for (int t = tid; t < (k + 1) * (m + 1); t += PT) S[t] = H[t];
+                    for (int t = tid; t <= k; t += PT) {
+                        S[hs + t] = cs[t];
+                        S[hs + m + t] = sn[t];
+                    }
+                    for (int t = tid; t <= m; t += PT) S[hs + 2 * m + t] = g[t];
+                }
+                status = PG_IN_CYCLE;
+                ++k;
                 break;
             }
+            update_x(k + 1);
+            if (d == 2) {
+                finished = 1;
+                break;
+            }
+            // end of a cycle: restart from the true residual, or leave that to the next launch
+            k = 0;
+            if (steps >= budget) {
+                status = PG_RESTART;
+                break;
+            }
+            residual();
+            const double beta = sqrt(cluster_norm2());
+            if (decide(!(beta == 0.0)) == 0) {
+                finished = 2;
+                break;
+            }
+            begin_cycle(beta);
         }
-        if (rank == 0 && tid == 0) {
-            a.iters[f] = iters;
-            a.rel[f] = rel;
-            a.converged[f] = rel < a.tol;
+        if (rank == 0 && tid == 0 && finished != 3) {
+            PersistentState o;
+            o.status = finished ? PG_DONE : status;
+            o.k = k;
+            o.iters = iters;
+            o.r0 = r0;
+            o.rel = finished == 2 ? 0.0 : rel;
+            o.converged = finished == 2 ? 1 : (finished == 1 ? (rel < a.tol) : 0);
+            *it.st = o;
         }
     }
 }
 
 }  // namespace
 
-cudaError_t persistent_gmres_plan(int n_max, int restart, int cluster, int count, int *clusters, size_t *smem)
+cudaError_t persistent_gmres_plan(int n_max, int restart, int cluster, int vx_smem, int count, int *clusters,
+                                  size_t *smem)
 {
-    const PersistentSmem L = persistent_smem_layout(n_max, cluster, restart);
+    const PersistentSmem L = persistent_smem_layout(n_max, cluster, restart, vx_smem);
     cudaError_t e = cudaFuncSetAttribute(k_persistent_gmres, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L.total);
     if (e != cudaSuccess) return e;
     if (cluster > 8) {

@@ -1,5 +1,8 @@
 // Persistent batched GMRES (solve_persistent.cu): many independent dense
-// complex64 systems in one launch, one thread-block cluster per system.
+// complex64 systems in one launch, one thread-block cluster per system at a
+// time, with the whole Krylov state of every system in device memory so that
+// a launch may advance each system by a bounded number of steps and a later
+// launch resumes it exactly.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -10,16 +13,34 @@ namespace nihu {
 
 constexpr int PERSISTENT_THREADS = 512;
 
+// progress of one system between launches
+enum PersistentStatus { PG_FRESH = 0, PG_IN_CYCLE = 1, PG_RESTART = 2, PG_DONE = 3 };
+
+struct PersistentState {
+    int status;     // PersistentStatus
+    int k;          // PG_IN_CYCLE: Arnoldi steps done in the current cycle
+    int iters;      // Arnoldi steps done in total
+    int converged;  // PG_DONE: relative residual estimate below tol
+    double r0;      // |b|, the reference of the relative residual
+    double rel;     // latest relative residual estimate
+};
+
 struct PersistentItem {
     const float2 *A;   // n x n, column-major, leading dimension lda
     int64_t lda;
     const double2 *b;  // right-hand side, n
     double2 *x;        // solution, n
+    double2 *V;        // Arnoldi basis, (restart + 1) vectors of n
+    double2 *S;        // small Krylov state, persistent_small_state(restart) complex128
+    PersistentState *st;
     int n;
     int vec;     // 1: n and lda even and A 16-byte aligned (two rows per 16-byte load)
     int stream;  // 1: matrix read with evict-first loads (larger than a share of L2)
     int pad;
 };
+
+// H ((m + 1) x m, column-major) | cs (m) | sn (m) | g (m + 1)
+__host__ __device__ inline size_t persistent_small_state(int m) { return (size_t)(m + 1) * m + 3 * (size_t)m + 1; }
 
 struct PersistentArgs {
     const PersistentItem *items;
@@ -28,12 +49,10 @@ struct PersistentArgs {
     int n_max;
     int restart;
     int max_iters;
+    int quantum;   // most Arnoldi steps per system in this launch (<= 0: no bound)
     double tol;
-    double2 *V;    // clusters * (restart + 1) * n_max basis vectors
     int *counter;  // zero before the launch
-    int *iters;    // per item
-    double *rel;   // per item: final relative residual estimate
-    int *converged;
+    float2 *vxg;   // NULL: matvec input in shared memory; else clusters * n_max complex64
 };
 
 // dynamic shared memory of one CTA, byte offsets
@@ -44,7 +63,8 @@ struct PersistentSmem {
 
 __host__ __device__ inline size_t persistent_align16(size_t x) { return (x + 15) & ~(size_t)15; }
 
-__host__ __device__ inline PersistentSmem persistent_smem_layout(int n_max, int cluster, int m)
+// vx_smem = 0: the matvec input lives in global memory (vxg) instead
+__host__ __device__ inline PersistentSmem persistent_smem_layout(int n_max, int cluster, int m, int vx_smem)
 {
     PersistentSmem s;
     size_t o = 0;
@@ -53,7 +73,7 @@ __host__ __device__ inline PersistentSmem persistent_smem_layout(int n_max, int 
     s.blocks = (nb + cluster - 1) / cluster;
     const size_t rows = 128 * (size_t)s.blocks;
     s.vx = o;   // matvec input, n_max complex64
-    o = persistent_align16(o + 8 * (size_t)n_max);
+    o = persistent_align16(o + (vx_smem ? 8 * (size_t)n_max : 0));
     s.wl = o;   // own rows of the Krylov vector, complex128
     o = persistent_align16(o + 16 * rows);
     s.red = o;  // slice partials of one matvec tile
@@ -79,7 +99,8 @@ __host__ __device__ inline PersistentSmem persistent_smem_layout(int n_max, int 
 }
 
 // clusters that can run at once (at most count) and the dynamic shared memory per CTA
-cudaError_t persistent_gmres_plan(int n_max, int restart, int cluster, int count, int *clusters, size_t *smem);
+cudaError_t persistent_gmres_plan(int n_max, int restart, int cluster, int vx_smem, int count, int *clusters,
+                                  size_t *smem);
 cudaError_t launch_persistent_gmres(const PersistentArgs &a, int cluster, int clusters, size_t smem, cudaStream_t s);
 
 }  // namespace nihu

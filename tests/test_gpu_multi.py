@@ -61,3 +61,30 @@ def test_solve_multi_cylinder_plane_waves(gpu_ctx, oracle):
     assert res.max() <= 1e-6
     err = np.abs(X - P_ref).max(axis=0) / np.abs(P_ref).max(axis=0)
     assert err.max() < 1e-4, err
+
+
+def test_cylinder_40k_entries_match_oracle(gpu_ctx, oracle):
+    """The full-size 40000-quad cylinder (k = 4): both matrices assembled on the
+    device, their first 64 columns (every row) against the FP64 oracle."""
+    import ctypes
+    nodes, elems = meshes.cylinder_40k()
+    n = len(elems)
+    k, nc = 4.0, 64
+    L = g.lib()
+    dm = g.api.DeviceMesh(gpu_ctx, nodes, elems)
+    ps, pd = ctypes.c_void_p(), ctypes.c_void_p()
+    gpu_ctx.check(L.nihu_gb_device_alloc(gpu_ctx.handle, 8 * n * n, ctypes.byref(ps)))
+    gpu_ctx.check(L.nihu_gb_device_alloc(gpu_ctx.handle, 8 * n * n, ctypes.byref(pd)))
+    try:
+        gpu_ctx.check(L.nihu_gb_assemble(gpu_ctx.handle, dm.handle, dm.handle, g.HELMHOLTZ_3D, 3, k, 1.0, 0.0,
+                                         g.REGULAR_FP32, g.C64, ps, pd, n, 0, g.DEVICE))
+        for ptr, op in ((ps, oracle.SLP), (pd, oracle.DLP)):
+            got = np.zeros((n, nc), np.complex64, order="F")
+            gpu_ctx.check(L.nihu_gb_memcpy(gpu_ctx.handle, got.ctypes.data, g.HOST, ptr, g.DEVICE, got.nbytes))
+            ref = oracle.assemble((nodes, elems), (nodes, elems), oracle.HELMHOLTZ, op, k, cols=(0, nc),
+                                  same_mesh=True, threads=16)
+            assert np.abs(got - ref).max() / np.abs(ref).max() < 1e-5
+    finally:
+        L.nihu_gb_device_free(gpu_ctx.handle, ps)
+        L.nihu_gb_device_free(gpu_ctx.handle, pd)
+    dm.close()
