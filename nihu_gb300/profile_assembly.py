@@ -2,7 +2,16 @@
 
     python -m nihu_gb300.profile_assembly --subdiv 5 --k 5 --budget-mb 1536
 
-assembles the Helmholtz SLP and DLP matrices of an icosphere.  With
+assembles the Helmholtz SLP and DLP matrices of an icosphere.
+
+    python -m nihu_gb300.profile_assembly --sweep 16 --subdiv 4
+    python -m nihu_gb300.profile_assembly --sweep-config4
+
+run a frequency sweep instead (nihu_gb_solve_sweep_batched: the frequency-batch
+assembly kernels and one persistent GMRES launch): `--sweep N` solves N wave
+numbers uniform in [0.1, 10] on one icosphere, `--sweep-config4` the
+256 wave numbers on icospheres of 320 / 1280 / 5120 triangles.  Both run the
+sweep twice (the first call builds the near-pair lists).  With
 ``--budget-mb`` the context's HBM budget forces host output in column panels,
 so every kernel launch covers one panel of the full-size problem while the
 device holds only about the budget -- small enough for an ``ncu`` capture of
@@ -32,7 +41,11 @@ def main(argv=None):
     ap.add_argument("--budget-mb", type=int, default=0, help="HBM budget: host output in column panels")
     ap.add_argument("--reps", type=int, default=2)
     ap.add_argument("--fp64", action="store_true", help="FP64 regular quadrature")
+    ap.add_argument("--sweep", type=int, default=0, metavar="N", help="frequency sweep of N wave numbers")
+    ap.add_argument("--sweep-config4", action="store_true", help="the 256-instance sweep on three icospheres")
     a = ap.parse_args(argv)
+    if a.sweep or a.sweep_config4:
+        return sweep(a)
 
     if a.cylinder:
         nt = a.cylinder
@@ -61,6 +74,30 @@ def main(argv=None):
                                      ps, pd, n, 0, where))
     prof = ctx.profile()
     print(json.dumps({"n_elements": n, "where": "host panels" if a.budget_mb else "device",
+                      "phases_ms": {k: round(v[0], 4) for k, v in prof.items()},
+                      "launches": {k: v[1] for k, v in prof.items()}}))
+    ctx.close()
+
+
+def sweep(a):
+    rng = np.random.default_rng(2026)
+    if a.sweep_config4:
+        mesh_list = [api.create_mesh(*meshes.icosphere(s_)) for s_ in (2, 3, 4)]
+        ks = rng.uniform(0.1, 10.0, 256)
+        mesh_of = np.arange(256) % 3
+    else:
+        mesh_list = [api.create_mesh(*meshes.icosphere(a.subdiv))]
+        ks = rng.uniform(0.1, 10.0, a.sweep)
+        mesh_of = np.zeros(a.sweep, np.int32)
+    ctx = api.Context(0)
+    ctx.set_profiling(True)
+    for _ in range(2):
+        ctx.profile_reset()
+        P, it, rel, conv = api.solve_sweep_batched(mesh_list, ks, mesh_of, restart=50, max_iters=1000, tol=1e-6,
+                                                   ctx=ctx, check=False)
+    prof = ctx.profile()
+    print(json.dumps({"instances": len(ks), "meshes": [m.num_elements for m in mesh_list],
+                      "iterations_total": int(np.sum(it)), "converged": int(np.sum(conv)),
                       "phases_ms": {k: round(v[0], 4) for k, v in prof.items()},
                       "launches": {k: v[1] for k, v in prof.items()}}))
     ctx.close()
