@@ -524,7 +524,10 @@ def run_sweep(args):
     iterations).  The batched path (nihu_gb_solve_sweep_batched: one call,
     per-mesh frequency-batched assembly, one persistent GMRES launch over all
     256 systems) is timed against the plain single-instance path
-    (nihu_gb_solve_cbie, one call per instance) on every instance."""
+    (nihu_gb_solve_cbie, one call per instance) on every instance.  The
+    timed batched path is the sweep plan (nihu_gb_sweep_plan_*: the same work
+    captured once as a CUDA graph and replayed); the eager single call is
+    reported beside it."""
     import torch
 
     import nihu_gb300 as g
@@ -544,26 +547,44 @@ def run_sweep(args):
            "note": "the plain CBIE (DLP - I/2) p = SLP q is singular at the sphere's interior Dirichlet "
                    "eigenvalues (k = pi, 4.49, 5.76, ...); wave numbers close to them may stop at the "
                    "iteration cap on either path"}
+    # eager path: one nihu_gb_solve_sweep_batched call (phases timed with CUDA events)
     ctx.set_profiling(True)
     for _ in range(max(1, args.warmup)):  # warm-up: near lists, scratch, code paths
         g.solve_sweep_batched(mesh_list, ks_all, mesh_of, restart=restart, max_iters=max_iters, tol=tol, ctx=ctx,
                               check=False)
-    times = []
+    eager = []
     for _ in range(max(1, args.steps)):
         ctx.profile_reset()
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        P, it, rel, conv = g.solve_sweep_batched(mesh_list, ks_all, mesh_of, restart=restart, max_iters=max_iters,
-                                                 tol=tol, ctx=ctx, check=False)
+        g.solve_sweep_batched(mesh_list, ks_all, mesh_of, restart=restart, max_iters=max_iters, tol=tol, ctx=ctx,
+                              check=False)
         torch.cuda.synchronize()
-        times.append(time.perf_counter() - t0)
+        eager.append(time.perf_counter() - t0)
     prof = ctx.profile()
+    out["phases_ms"] = {k: round(v[0], 3) for k, v in prof.items()}
+    out["launches"] = {k: v[1] for k, v in prof.items()}
+    out["eager_seconds"] = float(np.median(eager))
+    ctx.set_profiling(False)
+    # the timed path: the sweep captured once as a CUDA graph, replayed per run
+    # (host Neumann data in, host pressures out, every run)
+    t0 = time.perf_counter()
+    plan = g.SweepPlan(mesh_list, mesh_of, k_max=10.0, restart=restart, max_iters=max_iters, tol=tol, ctx=ctx)
+    out["plan_create_seconds"] = time.perf_counter() - t0
+    q1 = [np.ones(sizes[i]) for i in mesh_of]
+    for _ in range(max(1, args.warmup)):
+        plan.run(ks_all, q1, check=False)
+    times = []
+    for _ in range(max(1, args.steps)):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        P, it, rel, conv = plan.run(ks_all, q1, check=False)
+        times.append(time.perf_counter() - t0)
+    plan.close()
     batched_s = float(np.median(times))
     out["batched_seconds"] = batched_s
     out["batched_seconds_all"] = times
     out["value"] = 256 / batched_s
-    out["phases_ms"] = {k: round(v[0], 3) for k, v in prof.items()}
-    out["launches"] = {k: v[1] for k, v in prof.items()}
     # plain single-instance path on every instance
     ctx.set_profiling(False)
     per_mesh = {}

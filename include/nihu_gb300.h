@@ -76,6 +76,7 @@ typedef enum nihu_gb_status {
 typedef struct nihu_gb_ctx nihu_gb_ctx;
 typedef struct nihu_gb_mesh nihu_gb_mesh;
 typedef struct nihu_gb_server nihu_gb_server;
+typedef struct nihu_gb_sweep_plan nihu_gb_sweep_plan;
 
 /* ------------------------------------------------------------------ context */
 
@@ -309,6 +310,28 @@ nihu_gb_status nihu_gb_lu_solve(nihu_gb_ctx *ctx, void *A, int64_t n, int64_t ld
 nihu_gb_status nihu_gb_solve_cbie(nihu_gb_ctx *ctx, const nihu_gb_mesh *mesh, int family, double k,
                                   int precision, int dtype, const void *q, void *p, int solver,
                                   int restart, int max_iters, double tol, int *iters, double *rel_residual);
+
+/* A frequency sweep over fixed meshes captured once as a CUDA graph and
+ * replayed per set of wave numbers (the batched counterpart of running
+ * helmholtz_3d_coll.cpp:36-120 once per instance).  nk instances, instance f
+ * on meshes[mesh_of[f]]; every run's wave numbers satisfy |k| <= k_max (the
+ * series of the nearly singular terms are sized for it).  Creation builds
+ * the near-pair lists, allocates every buffer (matrices of all instances,
+ * Krylov state, pinned staging) and records: the uploads, each mesh's
+ * frequency-batch assembly, identities and right-hand sides, one persistent
+ * GMRES(restart) launch over all instances, and the downloads. */
+nihu_gb_status nihu_gb_sweep_plan_create(nihu_gb_ctx *ctx, int n_meshes, const nihu_gb_mesh *const *meshes, int family,
+                                         int nk, const int *mesh_of, double k_max, int precision, int restart,
+                                         int max_iters, double tol, nihu_gb_sweep_plan **out);
+
+/* One replay: ks (nk), q and p (complex128 host arrays, the instances'
+ * columns back to back in instance order) as for nihu_gb_solve_sweep_batched;
+ * iters, rel_residuals, converged (nk entries each) may be NULL.  Returns
+ * NIHU_GB_ERR_NOT_CONVERGED, with every p written, when some instance stopped
+ * at max_iters. */
+nihu_gb_status nihu_gb_sweep_plan_run(nihu_gb_sweep_plan *plan, const double *ks, const void *q, void *p, int *iters,
+                                      double *rel_residuals, int *converged);
+void nihu_gb_sweep_plan_destroy(nihu_gb_sweep_plan *plan);
 
 /* ------------------------------------------------------------ serving */
 

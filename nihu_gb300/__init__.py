@@ -7,7 +7,7 @@ is the Python front end with the same shape.
 """
 from ._capi import (C64, C128, DEVICE, DLP, GEMM_BF16X9, GEMM_FP32, GEMM_TF32, HELMHOLTZ_3D, HOST, LAPLACE_3D, QUAD_1, REGULAR_FP32, REGULAR_FP64, SLP,
                     TRIA_1, InvalidArgumentError, NihuError, NotConvergedError, OutOfRangeError, lib)
-from .api import (Context, DeviceMesh, Mesh, Server, constant_view, create_integral_operator, create_mesh, default_context,
+from .api import (Context, DeviceMesh, Mesh, Server, SweepPlan, constant_view, create_integral_operator, create_mesh, default_context,
                   dirac, gemm, gmres, helmholtz_3d_DLP_kernel, helmholtz_3d_SLP_kernel, identity_integral_operator,
                   laplace_3d_DLP_kernel, laplace_3d_SLP_kernel, lu_solve, matvec, pair_statistics, solve_cbie,
                   solve_batched, solve_multi, solve_sweep, solve_sweep_batched)
@@ -15,7 +15,7 @@ from . import meshes
 
 __all__ = [
     "C64", "C128", "DEVICE", "DLP", "GEMM_BF16X9", "GEMM_FP32", "GEMM_TF32", "gemm", "solve_batched", "solve_multi", "solve_sweep", "solve_sweep_batched", "HELMHOLTZ_3D", "HOST", "LAPLACE_3D", "QUAD_1", "REGULAR_FP32", "REGULAR_FP64",
-    "SLP", "TRIA_1", "InvalidArgumentError", "NihuError", "NotConvergedError", "OutOfRangeError", "lib", "Context", "Server",
+    "SLP", "TRIA_1", "InvalidArgumentError", "NihuError", "NotConvergedError", "OutOfRangeError", "lib", "Context", "Server", "SweepPlan",
     "DeviceMesh", "Mesh", "constant_view", "create_integral_operator", "create_mesh", "default_context", "dirac",
     "gmres", "helmholtz_3d_DLP_kernel", "helmholtz_3d_SLP_kernel", "identity_integral_operator",
     "laplace_3d_DLP_kernel", "laplace_3d_SLP_kernel", "lu_solve", "matvec", "pair_statistics", "solve_cbie", "meshes",

@@ -552,6 +552,59 @@ def solve_sweep_batched(meshes, ks, mesh_of, q=None, family: int = C.HELMHOLTZ_3
     return out, it, rel, conv.astype(bool)
 
 
+class SweepPlan:
+    """A frequency sweep over fixed meshes captured once as a CUDA graph
+    (nihu_gb_sweep_plan_*): instance f on meshes[mesh_of[f]]; run(ks, q)
+    replays assembly, right-hand sides and one persistent GMRES launch for a
+    new set of wave numbers (|k| <= k_max) and Neumann data."""
+
+    def __init__(self, meshes, mesh_of, k_max: float, family: int = C.HELMHOLTZ_3D, precision: str = "fp32",
+                 restart: int = 50, max_iters: int = 1000, tol: float = 1e-6, ctx: Context | None = None):
+        self.ctx = ctx or default_context()
+        self.meshes = list(meshes)
+        self._dms = [m.device(self.ctx) for m in self.meshes]
+        self.mesh_of = np.ascontiguousarray(mesh_of, dtype=np.int32)
+        self.nk = len(self.mesh_of)
+        self.sizes = [self.meshes[i].num_elements for i in self.mesh_of]
+        handles = (ctypes.c_void_p * len(self._dms))(*[d.handle.value for d in self._dms])
+        h = ctypes.c_void_p()
+        self.ctx.check(C.lib().nihu_gb_sweep_plan_create(
+            self.ctx.handle, len(self._dms), handles, family, self.nk, self.mesh_of.ctypes.data, float(k_max),
+            C.REGULAR_FP64 if precision == "fp64" else C.REGULAR_FP32, restart, max_iters, tol, ctypes.byref(h)))
+        self.handle = h
+
+    def run(self, ks, q=None, check: bool = True):
+        """Returns (list of p_f, iterations, relative residual estimates, converged)."""
+        ks = np.ascontiguousarray(ks, dtype=np.float64)
+        if ks.shape != (self.nk,):
+            raise ValueError("one wave number per instance")
+        total = sum(self.sizes)
+        qf = np.ones(total, np.complex128) if q is None else np.concatenate([_c128(v) for v in q])
+        if qf.shape != (total,):
+            raise ValueError("q: one vector per instance with its mesh's element count")
+        pf = np.zeros_like(qf)
+        it = np.zeros(self.nk, np.int32)
+        rel = np.zeros(self.nk)
+        conv = np.zeros(self.nk, np.int32)
+        st = C.lib().nihu_gb_sweep_plan_run(self.handle, ks.ctypes.data, qf.ctypes.data, pf.ctypes.data,
+                                            it.ctypes.data, rel.ctypes.data, conv.ctypes.data)
+        if st != C.OK and (check or st != 6):
+            self.ctx.check(st)
+        return np.split(pf, np.cumsum(self.sizes)[:-1]), it, rel, conv.astype(bool)
+
+    def close(self):
+        if getattr(self, "handle", None):
+            C.lib().nihu_gb_sweep_plan_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            if self.ctx.handle:
+                self.close()
+        except Exception:
+            pass
+
+
 class Server:
     """Continuous-batching serving loop of CBIE solves (DLP - I/2) p = SLP q
     (nihu_gb_server_*).  Requests wait in a FIFO queue until the HBM budget

@@ -14,6 +14,8 @@
 // cost -- storing 2 x 8 bytes per pair -- streams at full HBM width.
 // Self and nearly singular pairs are skipped (assemble_singular.cu writes
 // them), so every entry is written exactly once.
+#include <algorithm>
+
 #include "classify.cuh"
 #include "kernels.h"
 
@@ -183,6 +185,9 @@ __global__ void __launch_bounds__(REG_THREADS) k_regular(RegularArgs a)
     }
     Out *out_s = reinterpret_cast<Out *>(a.out_s);
     Out *out_d = reinterpret_cast<Out *>(a.out_d);
+    // frequency batch: this block's wave numbers [f_lo, f_hi) (gridDim.z chunks)
+    const int f_per = (a.nk + gridDim.z - 1) / gridDim.z;
+    const int f_lo = min(a.nk, (int)blockIdx.z * f_per), f_hi = min(a.nk, f_lo + f_per);
 
     for (int c = 0; c < ncols; ++c) {
         const int j = jb + c;
@@ -197,7 +202,7 @@ __global__ void __launch_bounds__(REG_THREADS) k_regular(RegularArgs a)
                 const int64_t off = (int64_t)(j - a.j0) * a.ld + i;
                 if constexpr (BATCH) {
                     const PointGeom<float> gm = point_geom<float>(fx, fy, fz, p.x, p.y, p.z, p.w, R(DO_S), R(DO_D));
-                    for (int f = 0; f < a.nk; ++f) {
+                    for (int f = f_lo; f < f_hi; ++f) {
                         R sr = 0, si = 0, dr = 0, di = 0;
                         point_freq<FAM, float>(gm, a.ks32[f], sr, si, dr, di);
                         if (row_ok) {
@@ -232,12 +237,12 @@ __global__ void __launch_bounds__(REG_THREADS) k_regular(RegularArgs a)
         const int64_t base = ((int64_t)j * 2 + par) * SLOTS;
         if constexpr (BATCH) {
             // frequency batch: each point's geometry once per tile of wave numbers
-            for (int f0 = 0; f0 < a.nk; f0 += FREQ_TILE) {
+            for (int f0 = f_lo; f0 < f_hi; f0 += FREQ_TILE) {
                 R kf[FREQ_TILE], sr[FREQ_TILE], si[FREQ_TILE], dr[FREQ_TILE], di[FREQ_TILE];
 #pragma unroll
                 for (int u = 0; u < FREQ_TILE; ++u) {
-                    if constexpr (sizeof(R) == 4) kf[u] = f0 + u < a.nk ? a.ks32[f0 + u] : 0.0f;
-                    else kf[u] = f0 + u < a.nk ? a.ks[f0 + u] : 0.0;
+                    if constexpr (sizeof(R) == 4) kf[u] = f0 + u < f_hi ? a.ks32[f0 + u] : 0.0f;
+                    else kf[u] = f0 + u < f_hi ? a.ks[f0 + u] : 0.0;
                     sr[u] = si[u] = dr[u] = di[u] = 0;
                 }
                 for (int q = 0; q < n_eval; ++q) {
@@ -262,7 +267,7 @@ __global__ void __launch_bounds__(REG_THREADS) k_regular(RegularArgs a)
                 }
 #pragma unroll
                 for (int u = 0; u < FREQ_TILE; ++u) {
-                    if (f0 + u >= a.nk) break;
+                    if (f0 + u >= f_hi) break;
                     const int64_t off = (int64_t)(j - a.j0) * a.ld + i;
                     if (DO_S)
                         store_entry(batch_matrix<Out>(a, false, f0 + u) + off, sr[u], si[u], are, aim, unit_alpha, accumulate);
@@ -324,6 +329,17 @@ cudaError_t launch_assemble_regular(const RegularArgs &a, cudaStream_t s)
     int ncols = a.j1 - a.j0;
     if (a.test.n == 0 || ncols <= 0) return cudaSuccess;
     dim3 grid((a.test.n + REG_THREADS - 1) / REG_THREADS, (ncols + REG_COLS - 1) / REG_COLS);
+    if (a.nk > 1 || a.force_batch) {
+        // small meshes: split the wave numbers over gridDim.z (at least one tile of
+        // FREQ_TILE each) until the grid holds about four blocks per SM
+        int dev = 0, sms = 148;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        const int64_t xy = (int64_t)grid.x * grid.y;
+        const int64_t want = (4 * (int64_t)sms + xy - 1) / xy;
+        const int most = (a.nk + FREQ_TILE - 1) / FREQ_TILE;
+        grid.z = (unsigned)std::max<int64_t>(1, std::min<int64_t>(want, most));
+    }
     if (a.precision == 0) {
         if (a.dtype == 0) launch_fam<float, float2>(a, grid, s);
         else launch_fam<float, double2>(a, grid, s);

@@ -801,6 +801,9 @@ __device__ __forceinline__ void singular_pairs(const RegularArgs &a, const NearL
     // nearly singular pairs have r < 1.5 D + (point to centre) <= 3 D_max
     const bool short_series = k * 3.0 * a.trial_size_max <= 0.75;
 
+    // this block's wave numbers [f_lo, f_hi) (gridDim.y chunks of a frequency batch)
+    const int f_per = (a.nk + gridDim.y - 1) / gridDim.y;
+    const int f_lo = min(a.nk, (int)blockIdx.y * f_per), f_hi = min(a.nk, f_lo + f_per);
     for (int64_t item = (int64_t)blockIdx.x * SING_THREADS + threadIdx.x; item < total;
          item += (int64_t)gridDim.x * SING_THREADS) {
         int i, j;
@@ -842,7 +845,7 @@ __device__ __forceinline__ void singular_pairs(const RegularArgs &a, const NearL
                 st.sr = self_static(e, x0) * INV_FOUR_PI;
                 if (fam == FAM_HELMHOLTZ) self_tria_moments(e, x0, a.k_absmax, mS, &rmax);
             }
-            for (int f = 0; f < a.nk; ++f) {
+            for (int f = f_lo; f < f_hi; ++f) {
                 const double kf = a.ks[f];
                 // this wave number's series length (MOM_J: sum the points directly)
                 const int Jf = fam == FAM_HELMHOLTZ ? series_terms(fabsf((float)kf) * rmax) : 0;
@@ -867,7 +870,7 @@ __device__ __forceinline__ void singular_pairs(const RegularArgs &a, const NearL
             }
             continue;
         }
-        for (int f = 0; f < a.nk; ++f) {
+        for (int f = f_lo; f < f_hi; ++f) {
             const double kf = a.nk > 1 ? a.ks[f] : k;
             const bool short_f = a.nk > 1 ? kf * 3.0 * a.trial_size_max <= 0.75 : short_series;
             Acc acc;
@@ -934,6 +937,17 @@ struct SeriesBounds {
     }
 };
 
+cudaError_t prepare_singular_batch(cudaStream_t s)
+{
+    static const SeriesBounds bounds;
+    cudaError_t e = cudaMemcpyToSymbolAsync(c_series_x, bounds.x, sizeof(bounds.x), 0, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_singular_batch<float2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)MOM_SMEM);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_singular_batch<double2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)MOM_SMEM);
+    return e;
+}
+
 cudaError_t launch_assemble_singular(const RegularArgs &a, const NearList &near, int *err, cudaStream_t s)
 {
     int dev = 0, sms = 148;
@@ -945,20 +959,21 @@ cudaError_t launch_assemble_singular(const RegularArgs &a, const NearList &near,
     int64_t total = (near.col_ptr ? near.nnz : 0) + (a.same_mesh ? (a.j1 - a.j0) : 0);
     int64_t want = (total + SING_THREADS - 1) / SING_THREADS;
     int blocks = (int)max((int64_t)1, min(want, (int64_t)sms));
+    // a frequency batch of few pairs: split the wave numbers over gridDim.y so
+    // that about one block per SM runs
+    dim3 grid(blocks, 1);
+    if (a.nk > 1 || a.force_batch) grid.y = (unsigned)max(1, min(a.nk, sms / blocks));
     size_t smem = 0;
     if (a.nk > 1 || a.force_batch) {
-        static const SeriesBounds bounds;
-        cudaError_t e0 = cudaMemcpyToSymbolAsync(c_series_x, bounds.x, sizeof(bounds.x), 0, cudaMemcpyHostToDevice, s);
-        if (e0 != cudaSuccess) return e0;
-        smem = MOM_SMEM;
-        cudaError_t e = a.dtype == 0
-                            ? cudaFuncSetAttribute(k_singular_batch<float2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                   (int)MOM_SMEM)
-                            : cudaFuncSetAttribute(k_singular_batch<double2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                   (int)MOM_SMEM);
+        // inside a stream capture the table and the attributes were set beforehand
+        // (prepare_singular_batch): a capture records no host-memory copy
+        cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+        cudaError_t e = cudaStreamIsCapturing(s, &cap);
         if (e != cudaSuccess) return e;
-        if (a.dtype == 0) k_singular_batch<float2><<<blocks, SING_THREADS, smem, s>>>(a, near, err);
-        else k_singular_batch<double2><<<blocks, SING_THREADS, smem, s>>>(a, near, err);
+        if (cap == cudaStreamCaptureStatusNone && (e = prepare_singular_batch(s)) != cudaSuccess) return e;
+        smem = MOM_SMEM;
+        if (a.dtype == 0) k_singular_batch<float2><<<grid, SING_THREADS, smem, s>>>(a, near, err);
+        else k_singular_batch<double2><<<grid, SING_THREADS, smem, s>>>(a, near, err);
     } else {
         if (a.dtype == 0) k_singular<float2><<<blocks, SING_THREADS, 0, s>>>(a, near, err);
         else k_singular<double2><<<blocks, SING_THREADS, 0, s>>>(a, near, err);

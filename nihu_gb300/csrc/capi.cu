@@ -2084,3 +2084,331 @@ extern "C" nihu_gb_status nihu_gb_server_take(nihu_gb_server *sv, int64_t *id, v
     delete r;
     return NIHU_GB_OK;
 }
+
+// ------------------------------------------------------ sweep plan (graph)
+//
+// A frequency sweep over fixed meshes, captured once as a CUDA graph: the
+// wave-number and Neumann-data uploads, every mesh's frequency-batch
+// assembly (the FP64 kernel on the auxiliary stream beside the regular one),
+// the identities and right-hand sides, the persistent GMRES launch over all
+// systems, and the downloads of the solutions, states and error flag.  Each
+// run refills pinned staging buffers and replays the graph: no host work,
+// allocation or synchronisation inside.
+
+struct nihu_gb_sweep_plan {
+    struct Group {
+        int mesh = 0;
+        std::vector<int> fs;       // instances, in instance order
+        int64_t n = 0, first = 0;  // elements; position of the group's first instance
+        void *G = nullptr, *H = nullptr;
+        double2 *part = nullptr;
+        int splits = 1;
+        NearList *nl = nullptr;
+    };
+    nihu_gb_ctx *ctx = nullptr;
+    std::vector<const nihu_gb_mesh *> meshes;
+    std::vector<int> mesh_of;
+    std::vector<Group> groups;
+    std::vector<int> order_of;       // instance f -> position (groups in mesh order)
+    std::vector<int64_t> off, user;  // device (position order) and user (instance order) column offsets
+    int family = 0, precision = 0, nk = 0, restart = 0, max_iters = 0;
+    double tol = 0.0, kmax = 0.0;
+    int64_t total = 0;
+    std::vector<void *> dbufs;  // device allocations of the plan
+    double *d_ks = nullptr;
+    float *d_ks32 = nullptr;
+    double2 *d_q = nullptr, *d_b = nullptr, *d_x = nullptr;
+    PersistentState *d_st = nullptr;
+    // pinned host staging
+    double *h_ks = nullptr;
+    float *h_ks32 = nullptr;
+    double2 *h_q = nullptr, *h_p = nullptr;
+    PersistentState *h_st = nullptr;
+    int *h_flag = nullptr;
+    PersistentArgs pargs{};
+    PersistentPlan pplan;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+};
+
+namespace {
+
+void plan_free(nihu_gb_sweep_plan *pl)
+{
+    if (!pl) return;
+    nihu_gb_ctx *ctx = pl->ctx;
+    cudaSetDevice(ctx->device);
+    cudaStreamSynchronize(ctx->stream);
+    if (pl->exec) cudaGraphExecDestroy(pl->exec);
+    if (pl->graph) cudaGraphDestroy(pl->graph);
+    for (void *p : pl->dbufs) dfree(ctx, p);
+    for (void *h : {(void *)pl->h_ks, (void *)pl->h_ks32, (void *)pl->h_q, (void *)pl->h_p, (void *)pl->h_st,
+                    (void *)pl->h_flag})
+        if (h) cudaFreeHost(h);
+    delete pl;
+}
+
+nihu_gb_status plan_alloc(nihu_gb_sweep_plan *pl, size_t bytes, void **out)
+{
+    nihu_gb_status st = dmalloc(pl->ctx, std::max<size_t>(bytes, 16), out);
+    if (st == NIHU_GB_OK) pl->dbufs.push_back(*out);
+    return st;
+}
+
+// record the whole sweep on the context stream into pl->graph and instantiate it
+nihu_gb_status plan_capture(nihu_gb_sweep_plan *pl)
+{
+    nihu_gb_ctx *ctx = pl->ctx;
+    cudaStream_t s = ctx->stream;
+    const bool prof = ctx->profiling;
+    ctx->profiling = false;  // no timing events inside the graph
+    cudaError_t e = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal);
+    nihu_gb_status st = NIHU_GB_OK;
+    auto chk = [&](cudaError_t r) {
+        if (r != cudaSuccess && e == cudaSuccess) e = r;
+    };
+    if (e == cudaSuccess) {
+        chk(cudaMemcpyAsync(pl->d_ks, pl->h_ks, 8 * (size_t)pl->nk, cudaMemcpyHostToDevice, s));
+        chk(cudaMemcpyAsync(pl->d_ks32, pl->h_ks32, 4 * (size_t)pl->nk, cudaMemcpyHostToDevice, s));
+        chk(cudaMemcpyAsync(pl->d_q, pl->h_q, 16 * (size_t)pl->total, cudaMemcpyHostToDevice, s));
+        for (auto &g : pl->groups) {
+            if (e != cudaSuccess || st) break;
+            const int cnt = (int)g.fs.size();
+            const nihu_gb_mesh *mesh = pl->meshes[g.mesh];
+            RegularArgs a;
+            a.test = mesh->dm;
+            a.trial = mesh->dm;
+            a.same_mesh = 1;
+            a.family = pl->family;
+            a.ops = NIHU_GB_SLP | NIHU_GB_DLP;
+            a.k = pl->kmax;
+            a.alpha_re = 1.0;
+            a.alpha_im = 0.0;
+            a.precision = pl->precision;
+            a.dtype = NIHU_GB_C64;
+            a.accumulate = 0;
+            a.trial_size_max = mesh->size_max;
+            a.k32 = (float)pl->kmax;
+            a.alpha_re32 = 1.0f;
+            a.alpha_im32 = 0.0f;
+            a.unit_alpha = 1;
+            a.out_s = g.G;
+            a.out_d = g.H;
+            a.ld = g.n;
+            a.j0 = 0;
+            a.j1 = (int)g.n;
+            a.nk = cnt;
+            a.ks = pl->d_ks + g.first;
+            a.ks32 = pl->d_ks32 + g.first;
+            a.mat_stride = g.n * g.n;
+            a.k_absmax = pl->kmax;
+            a.force_batch = 1;
+            st = assemble_panel(ctx, a, g.nl);
+            if (st) break;
+            const int64_t o = pl->off[g.fs[0]];
+            chk(launch_add_identity_batched((int)g.n, -0.5, 0.0, NIHU_GB_C64, g.H, g.n, g.n * g.n, cnt, s));
+            chk(launch_gemv_batched(NIHU_GB_C64, g.G, g.n, g.n, g.n, g.n * g.n, cnt, pl->d_q + o, pl->d_b + o, 1.0, 0.0,
+                                    0.0, 0.0, g.part, g.splits, s, nullptr));
+        }
+        chk(cudaMemsetAsync(pl->d_st, 0, sizeof(PersistentState) * (size_t)pl->nk, s));
+        chk(cudaMemsetAsync(pl->pargs.counter, 0, sizeof(int), s));
+        chk(launch_persistent_gmres(pl->pargs, pl->pplan.cluster, pl->pplan.clusters, pl->pplan.smem, s));
+        chk(cudaMemcpyAsync(pl->h_p, pl->d_x, 16 * (size_t)pl->total, cudaMemcpyDeviceToHost, s));
+        chk(cudaMemcpyAsync(pl->h_st, pl->d_st, sizeof(PersistentState) * (size_t)pl->nk, cudaMemcpyDeviceToHost, s));
+        chk(cudaMemcpyAsync(pl->h_flag, ctx->d_flag, sizeof(int), cudaMemcpyDeviceToHost, s));
+        chk(cudaMemsetAsync(ctx->d_flag, 0, sizeof(int), s));
+        cudaGraph_t graph = nullptr;
+        chk(cudaStreamEndCapture(s, &graph));  // ends the capture even after an error
+        pl->graph = graph;
+    }
+    ctx->profiling = prof;
+    if (st) return st;
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "sweep plan capture");
+    CK(cudaGraphInstantiate(&pl->exec, pl->graph, 0));
+    return NIHU_GB_OK;
+}
+
+}  // namespace
+
+extern "C" nihu_gb_status nihu_gb_sweep_plan_create(nihu_gb_ctx *ctx, int n_meshes, const nihu_gb_mesh *const *meshes,
+                                                    int family, int nk, const int *mesh_of, double k_max,
+                                                    int precision, int restart, int max_iters, double tol,
+                                                    nihu_gb_sweep_plan **out)
+{
+    if (!ctx || !out) return NIHU_GB_ERR_INVALID_ARGUMENT;
+    *out = nullptr;
+    if (n_meshes < 1 || !meshes || nk < 1 || !mesh_of || !(k_max > 0.0) || !std::isfinite(k_max) ||
+        (precision != 0 && precision != 1) || (family != NIHU_GB_HELMHOLTZ_3D && family != NIHU_GB_LAPLACE_3D) ||
+        restart < 1 || restart > 200 || max_iters < 1 || !(tol > 0.0))
+        return fail(ctx, NIHU_GB_ERR_INVALID_ARGUMENT, "nihu_gb_sweep_plan_create: bad argument");
+    for (int i = 0; i < n_meshes; ++i)
+        if (!meshes[i] || meshes[i]->ctx != ctx || meshes[i]->n < 1)
+            return fail(ctx, NIHU_GB_ERR_INVALID_ARGUMENT, "nihu_gb_sweep_plan_create: bad mesh");
+    for (int f = 0; f < nk; ++f)
+        if (mesh_of[f] < 0 || mesh_of[f] >= n_meshes)
+            return fail(ctx, NIHU_GB_ERR_INVALID_ARGUMENT, "nihu_gb_sweep_plan_create: bad mesh index");
+    cudaSetDevice(ctx->device);
+    nihu_gb_status st;
+    std::unique_ptr<nihu_gb_sweep_plan, void (*)(nihu_gb_sweep_plan *)> pl(new nihu_gb_sweep_plan, plan_free);
+    pl->ctx = ctx;
+    pl->meshes.assign(meshes, meshes + n_meshes);
+    pl->mesh_of.assign(mesh_of, mesh_of + nk);
+    pl->family = family;
+    pl->precision = precision;
+    pl->nk = nk;
+    pl->max_iters = max_iters;
+    pl->tol = tol;
+    pl->kmax = k_max;
+    pl->off = sweep_offsets(n_meshes, meshes, nk, mesh_of);
+    pl->user.resize(nk);
+    pl->order_of.resize(nk);
+    int64_t n_max = 1;
+    for (int f = 0; f < nk; ++f) {
+        pl->user[f] = pl->total;
+        pl->total += meshes[mesh_of[f]]->n;
+        n_max = std::max<int64_t>(n_max, meshes[mesh_of[f]]->n);
+    }
+    const int m = (int)std::min<int64_t>(restart, n_max);
+    pl->restart = m;
+    int pos = 0;
+    for (int i = 0; i < n_meshes; ++i) {
+        nihu_gb_sweep_plan::Group g;
+        g.mesh = i;
+        g.n = meshes[i]->n;
+        g.first = pos;
+        for (int f = 0; f < nk; ++f)
+            if (mesh_of[f] == i) {
+                g.fs.push_back(f);
+                pl->order_of[f] = pos++;
+            }
+        if (!g.fs.empty()) pl->groups.push_back(g);
+    }
+    // device buffers
+    void *p;
+    const size_t ss = persistent_small_state(m);
+    if ((st = plan_alloc(pl.get(), 8 * (size_t)nk, &p))) return st;
+    pl->d_ks = (double *)p;
+    if ((st = plan_alloc(pl.get(), 4 * (size_t)nk, &p))) return st;
+    pl->d_ks32 = (float *)p;
+    double2 *bufs[3];
+    for (int t = 0; t < 3; ++t) {
+        if ((st = plan_alloc(pl.get(), 16 * (size_t)pl->total, &p))) return st;
+        bufs[t] = (double2 *)p;
+    }
+    pl->d_q = bufs[0];
+    pl->d_b = bufs[1];
+    pl->d_x = bufs[2];
+    void *dV, *dS, *dst, *ditems, *dorder, *dcnt, *dvx = nullptr;
+    if ((st = plan_alloc(pl.get(), 16 * (size_t)pl->total * (m + 1), &dV))) return st;
+    if ((st = plan_alloc(pl.get(), 16 * ss * nk, &dS))) return st;
+    if ((st = plan_alloc(pl.get(), sizeof(PersistentState) * (size_t)nk, &dst))) return st;
+    pl->d_st = (PersistentState *)dst;
+    for (auto &g : pl->groups) {
+        const size_t mat = 8 * (size_t)g.n * g.n * g.fs.size();
+        if ((st = plan_alloc(pl.get(), mat, &g.G))) return st;
+        if ((st = plan_alloc(pl.get(), mat, &g.H))) return st;
+        g.splits = gemv_splits(g.n, g.n, NIHU_GB_C64);
+        if ((st = plan_alloc(pl.get(), 16 * (size_t)g.splits * g.n * g.fs.size(), &p))) return st;
+        g.part = (double2 *)p;
+        if ((st = get_near(ctx, meshes[g.mesh], meshes[g.mesh], &g.nl))) return st;
+    }
+    // the persistent launch: items, order and launch shape fixed by the plan
+    std::vector<PersistentItem> items(nk);
+    std::vector<int64_t> ns(nk);
+    int l2 = 0;
+    cudaDeviceGetAttribute(&l2, cudaDevAttrL2CacheSize, ctx->device);
+    for (auto &g : pl->groups)
+        for (size_t j = 0; j < g.fs.size(); ++j) {
+            const int f = g.fs[j], q = pl->order_of[f];
+            PersistentItem &it = items[q];
+            it.A = (const float2 *)g.H + (size_t)g.n * g.n * j;
+            it.lda = g.n;
+            it.b = pl->d_b + pl->off[f];
+            it.x = pl->d_x + pl->off[f];
+            it.V = (double2 *)dV + pl->off[f] * (m + 1);
+            it.S = (double2 *)dS + ss * q;
+            it.st = pl->d_st + q;
+            it.n = (int)g.n;
+            it.pad = 0;
+            ns[q] = g.n;
+        }
+    if ((st = plan_persistent(ctx, ns, m, &pl->pplan))) return st;
+    std::vector<int> order(nk);
+    for (int q = 0; q < nk; ++q) {
+        PersistentItem &it = items[q];
+        it.vec = (it.n % 2 == 0) && (it.lda % 2 == 0) && ((reinterpret_cast<uintptr_t>(it.A) & 15) == 0);
+        it.stream = 8.0 * (double)it.n * (double)it.n * std::min(nk, pl->pplan.clusters) > 0.5 * l2;
+        order[q] = q;
+    }
+    std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return ns[x] > ns[y]; });
+    if ((st = plan_alloc(pl.get(), sizeof(PersistentItem) * (size_t)nk, &ditems))) return st;
+    if ((st = plan_alloc(pl.get(), sizeof(int) * (size_t)nk, &dorder))) return st;
+    if ((st = plan_alloc(pl.get(), sizeof(int), &dcnt))) return st;
+    if (!pl->pplan.vx_smem && (st = plan_alloc(pl.get(), 8 * (size_t)pl->pplan.clusters * n_max, &dvx))) return st;
+    CK(cudaMemcpy(ditems, items.data(), sizeof(PersistentItem) * nk, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(dorder, order.data(), sizeof(int) * nk, cudaMemcpyHostToDevice));
+    PersistentArgs &a = pl->pargs;
+    a.items = (const PersistentItem *)ditems;
+    a.order = (const int *)dorder;
+    a.count = nk;
+    a.n_max = (int)n_max;
+    a.restart = m;
+    a.max_iters = max_iters;
+    a.quantum = 0;
+    a.tol = tol;
+    a.counter = (int *)dcnt;
+    a.vxg = (float2 *)dvx;
+    // pinned staging
+    CK(cudaMallocHost((void **)&pl->h_ks, 8 * (size_t)nk));
+    CK(cudaMallocHost((void **)&pl->h_ks32, 4 * (size_t)nk));
+    CK(cudaMallocHost((void **)&pl->h_q, 16 * (size_t)pl->total));
+    CK(cudaMallocHost((void **)&pl->h_p, 16 * (size_t)pl->total));
+    CK(cudaMallocHost((void **)&pl->h_st, sizeof(PersistentState) * (size_t)nk));
+    CK(cudaMallocHost((void **)&pl->h_flag, sizeof(int)));
+    CK(prepare_singular_batch(ctx->stream));
+    if ((st = sync(ctx))) return st;
+    if ((st = plan_capture(pl.get()))) return st;
+    *out = pl.release();
+    return NIHU_GB_OK;
+}
+
+extern "C" nihu_gb_status nihu_gb_sweep_plan_run(nihu_gb_sweep_plan *pl, const double *ks, const void *q, void *p,
+                                                 int *iters, double *rel_residuals, int *converged)
+{
+    if (!pl) return NIHU_GB_ERR_INVALID_ARGUMENT;
+    nihu_gb_ctx *ctx = pl->ctx;
+    if (!ks || !q || !p) return fail(ctx, NIHU_GB_ERR_INVALID_ARGUMENT, "nihu_gb_sweep_plan_run: bad argument");
+    for (int f = 0; f < pl->nk; ++f)
+        if (!std::isfinite(ks[f]) || std::fabs(ks[f]) > pl->kmax)
+            return fail(ctx, NIHU_GB_ERR_INVALID_ARGUMENT, "nihu_gb_sweep_plan_run: wave number beyond the plan's k_max");
+    cudaSetDevice(ctx->device);
+    for (int f = 0; f < pl->nk; ++f) {
+        const int q_ = pl->order_of[f];
+        pl->h_ks[q_] = ks[f];
+        pl->h_ks32[q_] = (float)ks[f];
+        std::memcpy(pl->h_q + pl->off[f], (const double2 *)q + pl->user[f], 16 * (size_t)pl->meshes[pl->mesh_of[f]]->n);
+    }
+    {
+        Phase ph(ctx, "sweep_graph");
+        CK(cudaGraphLaunch(pl->exec, ctx->stream));
+    }
+    ctx->launches += 1;
+    nihu_gb_status st;
+    if ((st = sync(ctx))) return st;
+    if (*pl->h_flag)
+        return fail(ctx, NIHU_GB_ERR_RUNTIME, "Could not perform inverse mapping (nearly singular pair " +
+                                                  std::to_string(*pl->h_flag - 1) + ")");
+    bool all = true;
+    for (int f = 0; f < pl->nk; ++f) {
+        std::memcpy((double2 *)p + pl->user[f], pl->h_p + pl->off[f], 16 * (size_t)pl->meshes[pl->mesh_of[f]]->n);
+        const PersistentState &s = pl->h_st[pl->order_of[f]];
+        if (iters) iters[f] = s.iters;
+        if (rel_residuals) rel_residuals[f] = s.rel;
+        if (converged) converged[f] = s.converged;
+        all = all && s.converged;
+    }
+    if (!all) return fail(ctx, NIHU_GB_ERR_NOT_CONVERGED, "sweep plan: some systems did not reach the tolerance");
+    return NIHU_GB_OK;
+}
+
+extern "C" void nihu_gb_sweep_plan_destroy(nihu_gb_sweep_plan *pl) { plan_free(pl); }

@@ -83,6 +83,9 @@ cudaError_t launch_assemble_regular(const RegularArgs &a, cudaStream_t s);
 // diagonal self terms; err receives a nonzero code if an inverse mapping
 // failed to converge (1 + pair index)
 cudaError_t launch_assemble_singular(const RegularArgs &a, const NearList &near, int *err, cudaStream_t s);
+// the frequency-batch kernel's series table and shared-memory attribute (done
+// by launch_assemble_singular itself, except inside a stream capture)
+cudaError_t prepare_singular_batch(cudaStream_t s);
 
 // linalg.cu ---------------------------------------------------------------
 cudaError_t launch_add_identity(int n, double are, double aim, int dtype, void *out, int64_t ld, cudaStream_t s);

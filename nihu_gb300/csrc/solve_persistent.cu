@@ -44,6 +44,7 @@ constexpr int PT = PERSISTENT_THREADS;
 constexpr int PW = PT / 32;
 constexpr int TILE = 64;            // row pairs per matvec tile (two warps)
 constexpr int SLICES = PT / TILE;   // column slices per tile
+constexpr int MV_UNROLL = 16;       // matrix loads in flight per thread
 
 __device__ __forceinline__ void fma_pair(float4 a, float2 x, float &ar0, float &ai0, float &ar1, float &ai1)
 {
@@ -92,16 +93,13 @@ __device__ void matvec_rows(const float2 *__restrict__ A, int64_t lda, int n, in
                 const float4 *col = reinterpret_cast<const float4 *>(A + (int64_t)js * lda + row);
                 const int64_t stride = lda / 2;
                 int j = js;
-                for (; j + 8 <= je; j += 8) {
-                    float4 v[8];
-                    float2 xv[8];
+                for (; j + MV_UNROLL <= je; j += MV_UNROLL) {
+                    float4 v[MV_UNROLL];
 #pragma unroll
-                    for (int u = 0; u < 8; ++u) {
-                        v[u] = load_a<STREAM>(col + (int64_t)(j - js + u) * stride);
-                        xv[u] = VXG ? __ldcg(vx + j + u) : vx[j + u];
-                    }
+                    for (int u = 0; u < MV_UNROLL; ++u) v[u] = load_a<STREAM>(col + (int64_t)(j - js + u) * stride);
 #pragma unroll
-                    for (int u = 0; u < 8; ++u) fma_pair(v[u], xv[u], ar0, ai0, ar1, ai1);
+                    for (int u = 0; u < MV_UNROLL; ++u)
+                        fma_pair(v[u], VXG ? __ldcg(vx + j + u) : vx[j + u], ar0, ai0, ar1, ai1);
                 }
                 for (; j < je; ++j)
                     fma_pair(load_a<STREAM>(col + (int64_t)(j - js) * stride), VXG ? __ldcg(vx + j) : vx[j], ar0, ai0,

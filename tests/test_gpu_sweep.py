@@ -96,3 +96,24 @@ def test_assemble_sweep_fp64_series_matches_direct(gpu_ctx, subdiv):
         for a, b in ((S[:, f * n:(f + 1) * n], s1), (D[:, f * n:(f + 1) * n], d1)):
             assert np.abs(a - b).max() / np.abs(b).max() < 1e-12
     dm.close()
+
+
+def test_sweep_plan_graph_matches_eager_sweep(gpu_ctx):
+    """The captured sweep gives the eager batched sweep's results, and replays
+    with new wave numbers and data."""
+    ms = [g.create_mesh(*meshes.icosphere(s)) for s in (1, 2, 3)]
+    rng = np.random.default_rng(31)
+    nk = 10
+    mesh_of = np.arange(nk) % 3
+    plan = g.SweepPlan(ms, mesh_of, k_max=6.0, tol=1e-7, ctx=gpu_ctx)
+    for rep in range(2):
+        ks = rng.uniform(0.2, 6.0, nk)
+        q = [rng.standard_normal(ms[i].num_elements) + 1j * rng.standard_normal(ms[i].num_elements) for i in mesh_of]
+        P, it, rel, conv = plan.run(ks, q, check=False)
+        P2, it2, rel2, conv2 = g.solve_sweep_batched(ms, ks, mesh_of, q=q, tol=1e-7, ctx=gpu_ctx, check=False)
+        assert list(it) == list(it2)
+        for a, b in zip(P, P2):
+            assert np.abs(a - b).max() <= 1e-6 * np.abs(b).max()
+    with pytest.raises(g.InvalidArgumentError):
+        plan.run(np.full(nk, 7.0))
+    plan.close()
