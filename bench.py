@@ -52,7 +52,7 @@ def parse():
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-solve", action="store_true")
     p.add_argument("--no-cpu", action="store_true")
-    p.add_argument("--config", default="large", choices=["large", "multirhs", "sweep", "serve"],
+    p.add_argument("--config", default="large", choices=["large", "small", "multirhs", "sweep", "serve"],
                    help="large: the headline line (20480-triangle icosphere); multirhs: the 40000-quad "
                         "cylinder with 64 plane waves; sweep: 256 wave numbers on three icospheres; serve: "
                         "the served stream (each a separate line)")
@@ -422,6 +422,96 @@ def run_ours(args):
         print(json.dumps(out), flush=True)
 
 
+def run_small(args):
+    """Plain small case: icosphere of 1280 triangles, k = 1, complex128 SLP and
+    DLP assembled in FP64 (nihu_gb_assemble), pulsating-sphere data q = 1, the
+    right-hand side on the GPU and a dense FP64 LU solve (nihu_gb_lu_solve);
+    surface pressure against the analytic -R/(1+ikR).  Timed device-resident
+    (CUDA events) and end to end through nihu_gb_solve_cbie with host data; the
+    CPU baseline is the FP64 oracle's assembly plus numpy's LU on the host
+    cores, whose pressure also checks the GPU's."""
+    import torch
+
+    import nihu_gb300 as g
+    from nihu_gb300 import _capi as C
+
+    k = 1.0
+    nodes, elems = g.meshes.icosphere(3)
+    n = len(elems)
+    mesh = g.create_mesh(nodes, elems)
+    ctx = g.Context(0)
+    L = g.lib()
+    dm = mesh.device(ctx)
+    ps, pd, pb, px = (ctypes.c_void_p() for _ in range(4))
+    for p_, size in ((ps, 16 * n * n), (pd, 16 * n * n), (pb, 16 * n), (px, 16 * n)):
+        ctx.check(L.nihu_gb_device_alloc(ctx.handle, size, ctypes.byref(p_)))
+    q = np.ones(n, np.complex128)
+    pq = ctypes.c_void_p()
+    ctx.check(L.nihu_gb_device_alloc(ctx.handle, 16 * n, ctypes.byref(pq)))
+    ctx.check(L.nihu_gb_memcpy(ctx.handle, pq, C.DEVICE, q.ctypes.data, C.HOST, 16 * n))
+    stream = torch.cuda.ExternalStream(ctx.stream)
+
+    def step():
+        ctx.check(L.nihu_gb_assemble(ctx.handle, dm.handle, dm.handle, C.HELMHOLTZ_3D, C.SLP | C.DLP, k, 1.0, 0.0,
+                                     C.REGULAR_FP64, C.C128, ps, pd, n, 0, C.DEVICE))
+        ctx.check(L.nihu_gb_add_identity(ctx.handle, dm.handle, -0.5, 0.0, C.C128, pd, n, C.DEVICE))
+        ctx.check(L.nihu_gb_matvec(ctx.handle, C.C128, ps, n, n, n, pq, pb, 1.0, 0.0, 0.0, 0.0, C.DEVICE))
+        ctx.check(L.nihu_gb_lu_solve(ctx.handle, pd, n, n, pb, px, C.DEVICE))
+
+    for _ in range(max(3, args.warmup)):
+        step()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    torch.cuda.synchronize()
+    for s_ in range(args.steps):
+        ev[s_][0].record(stream)
+        step()
+        ev[s_][1].record(stream)
+    torch.cuda.synchronize()
+    ms = float(np.mean([a.elapsed_time(b) for a, b in ev]))
+    p = np.zeros(n, np.complex128)
+    ctx.check(L.nihu_gb_memcpy(ctx.handle, p.ctypes.data, C.HOST, px, C.DEVICE, 16 * n))
+    ctx.set_profiling(True)
+    ctx.profile_reset()
+    step()
+    phases = {kk: round(v[0], 3) for kk, v in ctx.profile().items()}
+    ctx.set_profiling(False)
+    # end to end: host data in, host pressure out, through the composite call
+    e2e = []
+    for _ in range(max(1, args.steps)):
+        t0 = time.perf_counter()
+        p_e2e, _, _ = g.solve_cbie(mesh, k, q, dtype=g.C128, solver="lu", precision="fp64", ctx=ctx)
+        e2e.append(time.perf_counter() - t0)
+    pa = -1.0 / (1.0 + 1j * k)
+    out = {"metric": "plain small solve (config 1)", "impl": "ours", "value": ms, "unit": "ms",
+           "higher_is_better": False, "n_elements": n, "k": k, "dtype": "complex128, FP64 assembly and LU",
+           "data": "synthetic (icosphere generated in-process), pulsating sphere q = 1",
+           "steps": args.steps, "ms_per_step": ms,
+           "e2e": {"value": 1e3 * float(np.median(e2e)), "unit": "ms", "h2d_bytes_per_step": 16 * n + 20 * len(nodes),
+                   "d2h_bytes_per_step": 16 * n, "path": "nihu_gb_solve_cbie(dtype=C128, solver=LU, FP64)"},
+           "phases_ms": phases,
+           "pressure_error_vs_analytic": float(np.abs(p - pa).max() / abs(pa)),
+           "device_vs_e2e_max_rel_difference": float(np.abs(p - p_e2e).max() / np.abs(p).max())}
+    if not args.no_cpu:
+        from oracle import oracle
+        oracle.build()
+        threads = os.cpu_count() or 1
+        t0 = time.perf_counter()
+        Ls = oracle.assemble((nodes, elems), (nodes, elems), oracle.HELMHOLTZ, oracle.SLP, k, same_mesh=True,
+                             threads=threads)
+        Ms = oracle.assemble((nodes, elems), (nodes, elems), oracle.HELMHOLTZ, oracle.DLP, k, same_mesh=True,
+                             threads=threads) - 0.5 * np.eye(n)
+        p_cpu = np.linalg.solve(Ms, Ls @ q)
+        t_cpu = time.perf_counter() - t0
+        out["cpu_baseline"] = {"value": 1e3 * t_cpu, "unit": "ms", "cores": threads, "kind": "port",
+                               "sample": "the whole solve: FP64 oracle assembly of both matrices on all host cores "
+                                         "+ numpy LU"}
+        out["pressure_gpu_vs_cpu_oracle"] = float(np.abs(p - p_cpu).max() / np.abs(p_cpu).max())
+    for p_ in (ps, pd, pb, px, pq):
+        L.nihu_gb_device_free(ctx.handle, p_)
+    ctx.close()
+    print(json.dumps(out), flush=True)
+
+
 def run_multirhs(args):
     """Multi-RHS precision path: closed cylinder R=1, L=4, 40000 flat quads,
     k=4, 64 plane waves with seeded uniform directions.  Times the assembly of
@@ -758,6 +848,9 @@ def main():
     args = parse()
     if args.config == "multirhs":
         run_multirhs(args)
+        return
+    if args.config == "small":
+        run_small(args)
         return
     if args.config == "sweep":
         run_sweep(args)

@@ -960,8 +960,14 @@ nihu_gb_status nihu_gb_lu_solve(nihu_gb_ctx *ctx, void *A, int64_t n, int64_t ld
     void *ppiv;
     if ((st = scratch(ctx, "lu_piv", sizeof(int) * n, &ppiv))) return st;
     CK(cudaMemsetAsync(ctx->d_flag + 1, 0, sizeof(int), ctx->stream));
-    CK(launch_lu_factor(dA, n, lda, (int *)ppiv, ctx->d_flag + 1, &ctx->launches, ctx->stream));
-    CK(launch_lu_solve(dA, n, lda, (const int *)ppiv, db, dx, ctx->stream));
+    {
+        Phase ph(ctx, "lu_factor");
+        CK(launch_lu_factor(dA, n, lda, (int *)ppiv, ctx->d_flag + 1, &ctx->launches, ctx->stream));
+    }
+    {
+        Phase ph(ctx, "lu_solve");
+        CK(launch_lu_solve(dA, n, lda, (const int *)ppiv, db, dx, ctx->stream));
+    }
     ctx->launches += 1;
     int info = 0;
     CK(cudaMemcpyAsync(&info, ctx->d_flag + 1, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));

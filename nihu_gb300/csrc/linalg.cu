@@ -366,10 +366,15 @@ cudaError_t launch_sub(const double2 *a, const double2 *b, double2 *dst, int64_t
 
 __device__ __forceinline__ double cabs2(double2 v) { return v.x * v.x + v.y * v.y; }
 
-__global__ void __launch_bounds__(1024) k_lu_pivot(double2 *A, int64_t n, int64_t lda, int k, int *piv, int *info)
+// step k of the factorisation, one block: the pivot (largest |A[i][k]|, i >= k,
+// lowest index on ties), the swap of rows k and piv[k] across all columns, and
+// column k below the diagonal divided by the pivot
+__global__ void __launch_bounds__(1024) k_lu_pivot_swap_scale(double2 *A, int64_t n, int64_t lda, int k, int *piv,
+                                                              int *info)
 {
     __shared__ double best[32];
     __shared__ int besti[32];
+    __shared__ int pk;
     double bv = -1.0;
     int bi = k;
     for (int64_t i = k + threadIdx.x; i < n; i += blockDim.x) {
@@ -391,30 +396,23 @@ __global__ void __launch_bounds__(1024) k_lu_pivot(double2 *A, int64_t n, int64_
         for (int w = 1; w < nw; ++w)
             if (best[w] > bv || (best[w] == bv && besti[w] < bi)) { bv = best[w]; bi = besti[w]; }
         piv[k] = bi;
+        pk = bi;
         if (bv == 0.0 && *info == 0) *info = k + 1;
     }
-}
-
-// swap rows k and piv[k] across all columns, then scale column k below the diagonal
-__global__ void k_lu_swap_scale(double2 *A, int64_t n, int64_t lda, int k, const int *piv)
-{
-    int p = piv[k];
-    for (int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; j < n; j += (int64_t)gridDim.x * blockDim.x) {
-        if (p != k) {
+    __syncthreads();
+    const int p = pk;
+    if (p != k)
+        for (int64_t j = threadIdx.x; j < n; j += blockDim.x) {
             double2 t = A[j * lda + k];
             A[j * lda + k] = A[j * lda + p];
             A[j * lda + p] = t;
         }
-    }
-}
-
-__global__ void k_lu_scale(double2 *A, int64_t n, int64_t lda, int k)
-{
+    __syncthreads();
     double2 d = A[(int64_t)k * lda + k];
     double den = d.x * d.x + d.y * d.y;
     if (den == 0.0) return;
     double2 inv = make_double2(d.x / den, -d.y / den);
-    for (int64_t i = k + 1 + (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    for (int64_t i = k + 1 + threadIdx.x; i < n; i += blockDim.x) {
         double2 v = A[(int64_t)k * lda + i];
         A[(int64_t)k * lda + i] = make_double2(v.x * inv.x - v.y * inv.y, v.x * inv.y + v.y * inv.x);
     }
@@ -479,16 +477,13 @@ cudaError_t launch_lu_factor(double2 *A, int64_t n, int64_t lda, int *piv, int *
                              cudaStream_t s)
 {
     for (int k = 0; k < n; ++k) {
-        k_lu_pivot<<<1, 1024, 0, s>>>(A, n, lda, k, piv, info);
-        int sb = (int)min((int64_t)64, (n + 255) / 256);
-        k_lu_swap_scale<<<sb, 256, 0, s>>>(A, n, lda, k, piv);
-        k_lu_scale<<<sb, 256, 0, s>>>(A, n, lda, k);
+        k_lu_pivot_swap_scale<<<1, 1024, 0, s>>>(A, n, lda, k, piv, info);
         int64_t rem = n - k - 1;
         if (rem > 0) {
             dim3 grid((unsigned)((rem + 15) / 16), (unsigned)((rem + 15) / 16));
             k_lu_update<<<grid, dim3(16, 16), 0, s>>>(A, n, lda, k);
         }
-        *launches += rem > 0 ? 4 : 3;
+        *launches += rem > 0 ? 2 : 1;
     }
     return cudaGetLastError();
 }
