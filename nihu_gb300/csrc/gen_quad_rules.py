@@ -3,7 +3,7 @@
 
 Two families are produced, both to full double precision:
 
-* Gauss-Legendre rules on [-1, 1] with n = 1..16 nodes.  Nodes are the roots of
+* Gauss-Legendre rules on [-1, 1] with n = 1..21 nodes.  Nodes are the roots of
   the Legendre polynomial P_n found by Newton iteration in 40-digit arithmetic;
   weights are 2 / ((1 - x^2) P_n'(x)^2).  These are the same rules the
   reference obtains from the Golub-Welsch eigenproblem
@@ -174,15 +174,15 @@ def main(out_path):
         "#ifndef NIHU_GB300_QUAD_RULES_H",
         "#define NIHU_GB300_QUAD_RULES_H",
         "",
-        "#define NIHU_GAUSS_MAX_N 16",
+        "#define NIHU_GAUSS_MAX_N 21",
     ]
     offs, data = [], []
-    for n in range(1, 17):
+    for n in range(1, 22):
         x, w = gauss_legendre(n)
         offs.append(len(data) // 2)
         for xi, wi in zip(x, w):
             data.extend([xi, wi])
-    lines.append("/* offset (in points) of the n-point rule, n = 1..16, index n-1 */")
+    lines.append("/* offset (in points) of the n-point rule, n = 1..21, index n-1 */")
     lines.append("#define NIHU_GAUSS_OFFSETS { " + ", ".join(str(o) for o in offs) + " }")
     lines.append("/* (node, weight) pairs on [-1, 1] */")
     lines.append("#define NIHU_GAUSS_DATA { \\")

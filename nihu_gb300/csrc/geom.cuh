@@ -8,7 +8,7 @@ namespace nihu {
 // Quadrature tables in global memory (lanes of a warp read different points,
 // which constant memory would serialise).  One copy per translation unit.
 static __device__ const double g_gauss[NIHU_GAUSS_DATA_LEN] = NIHU_GAUSS_DATA;
-static __device__ const int g_gauss_off[16] = NIHU_GAUSS_OFFSETS;
+static __device__ const int g_gauss_off[NIHU_GAUSS_MAX_N] = NIHU_GAUSS_OFFSETS;
 static __device__ const double g_tri[NIHU_TRI_DATA_LEN] = NIHU_TRI_DATA;
 static __device__ const int g_tri_npts[15] = NIHU_TRI_NPTS;
 static __device__ const int g_tri_off[15] = NIHU_TRI_OFFSETS;

@@ -35,12 +35,14 @@ typedef double complex cplx;
 #define FAM_LAPLACE 1
 #define OP_SLP 1
 #define OP_DLP 2
+#define OP_DLPT 4
+#define OP_HSP 8
 #define TRIA_1_ID 32303
 #define QUAD_1_ID 32404
 
 static const double PI = 3.14159265358979323846264338327950288;
 
-static const int gauss_off[16] = NIHU_GAUSS_OFFSETS;
+static const int gauss_off[NIHU_GAUSS_MAX_N] = NIHU_GAUSS_OFFSETS;
 static const double gauss_data[NIHU_GAUSS_DATA_LEN] = NIHU_GAUSS_DATA;
 static const int tri_npts[15] = NIHU_TRI_NPTS;
 static const int tri_off[15] = NIHU_TRI_OFFSETS;
@@ -199,18 +201,65 @@ static cplx kern_dlp(int fam, double k, const double x[3], const double y[3], co
     return dgreen(fam, k, r) * rdny;
 }
 
-static cplx kern(int fam, int op, double k, const double x[3], const double y[3], const double ny[3])
+/* DLPt kernel dG/dr (-r_vec.n_x)/r, n_x the unit normal at the collocation point
+ * (nihu/library/normal_derivative_kernel.hpp:199-206) */
+static cplx kern_dlpt(int fam, double k, const double x[3], const double nx[3], const double y[3])
 {
-    return op == OP_SLP ? kern_slp(fam, k, x, y) : kern_dlp(fam, k, x, y, ny);
+    double rv[3] = {y[0] - x[0], y[1] - x[1], y[2] - x[2]};
+    double r = norm3(rv);
+    double rdnx = -dot3(rv, nx) / r;
+    return dgreen(fam, k, r) * rdnx;
+}
+
+/* f[0] = G'' - G'/r, f[1] = G'/r (nihu/library/helmholtz_kernel.hpp:198-205,
+ * the Laplace kernel being its k = 0 case) */
+static void ddgreen(int fam, double k, double r, cplx f[2])
+{
+    cplx ikr = fam == FAM_LAPLACE ? 0.0 : I * (k * r);
+    cplx g = cexp(-ikr) / (r * r * r) / (4.0 * PI);
+    f[1] = -g * (1.0 + ikr);
+    f[0] = g * (3.0 + ikr * (3.0 + ikr));
+}
+
+/* HSP kernel f0 (r.n_x)(r.n_y)-terms - f1 n_x.n_y
+ * (nihu/library/normal_derivative_kernel.hpp:242-251) */
+static cplx kern_hsp(int fam, double k, const double x[3], const double nx[3], const double y[3], const double ny[3])
+{
+    double rv[3] = {y[0] - x[0], y[1] - x[1], y[2] - x[2]};
+    double r = norm3(rv);
+    double rdny = dot3(rv, ny) / r;
+    double rdnx = -dot3(rv, nx) / r;
+    cplx f[2];
+    ddgreen(fam, k, r, f);
+    return f[0] * rdnx * rdny - f[1] * dot3(nx, ny);
+}
+
+/* nx: unit normal at the collocation point (used by DLPt and HSP only) */
+static cplx kern(int fam, int op, double k, const double x[3], const double *nx, const double y[3], const double ny[3])
+{
+    if (op == OP_SLP) return kern_slp(fam, k, x, y);
+    if (op == OP_DLP) return kern_dlp(fam, k, x, y, ny);
+    if (op == OP_DLPT) return kern_dlpt(fam, k, x, nx, y);
+    return kern_hsp(fam, k, x, nx, y, ny);
 }
 
 /* ------------------------------------------------------- quadrature degree */
 
-/* distance intervals for accuracy 3 (nihu/library/distance_kernel_intervals.hpp:117-139),
+/* distance intervals for accuracy 3 (nihu/library/distance_kernel_intervals.hpp:117-154),
  * evaluated with strict '<' (nihu/tmp/interval.hpp:173-185).  SLP behaves as
- * 1/r in the far field, DLP as 1/r^2 (nihu/library/helmholtz_kernel.hpp:281-306). */
+ * 1/r in the far field, DLP and DLPt as 1/r^2, HSP as 1/r^3
+ * (nihu/library/helmholtz_kernel.hpp:281-306). */
 static int interval_degree(int op, double ratio)
 {
+    if (op == OP_HSP) {
+        if (ratio < 10.0 / 10.0) return 9;
+        if (ratio < 11.0 / 10.0) return 9;
+        if (ratio < 14.0 / 10.0) return 8;
+        if (ratio < 19.0 / 10.0) return 6;
+        if (ratio < 36.0 / 10.0) return 4;
+        if (ratio < 223.0 / 10.0) return 2;
+        return 0;
+    }
     if (op == OP_SLP) {
         if (ratio < 11.0 / 10.0) return 6;
         if (ratio < 18.0 / 10.0) return 4;
@@ -239,7 +288,8 @@ static double centre_distance(const elem_t *a, const elem_t *b)
 
 /* sum_q w_q K(x, y_q) J_q over the trial element with the rule of the given
  * degree (nihu/core/double_integral.hpp:445-467 with the accelerator of :576-585) */
-static cplx regular_integral(const elem_t *e, int fam, int op, double k, const double x[3], int degree)
+static cplx regular_integral(const elem_t *e, int fam, int op, double k, const double x[3], const double *nx,
+                             int degree)
 {
     cplx sum = 0.0;
     if (e->nc == 3) {
@@ -251,7 +301,7 @@ static cplx regular_integral(const elem_t *e, int fam, int op, double k, const d
             elem_normal(e, q[3 * p], q[3 * p + 1], n);
             double J = norm3(n);
             double un[3] = {n[0] / J, n[1] / J, n[2] / J};
-            sum += kern(fam, op, k, x, y, un) * (J * q[3 * p + 2]);
+            sum += kern(fam, op, k, x, nx, y, un) * (J * q[3 * p + 2]);
         }
     } else {
         int ng = degree / 2 + 1;
@@ -264,7 +314,7 @@ static cplx regular_integral(const elem_t *e, int fam, int op, double k, const d
                 elem_normal(e, xi, eta, n);
                 double J = norm3(n);
                 double un[3] = {n[0] / J, n[1] / J, n[2] / J};
-                sum += kern(fam, op, k, x, y, un) * (J * w);
+                sum += kern(fam, op, k, x, nx, y, un) * (J * w);
             }
     }
     return sum;
@@ -369,18 +419,62 @@ static cplx self_quad_duffy(const elem_t *e, int fam, int op, double k)
                 elem_normal(e, xi, eta, n);
                 double J = norm3(n);
                 double un[3] = {n[0] / J, n[1] / J, n[2] / J};
-                sum += kern(fam, op, k, x0, y, un) * (J * wd);
+                sum += kern(fam, op, k, x0, NULL, y, un) * (J * wd);
             }
     }
     return sum;
 }
 
+/* the regular remainder (e^{-ikr}(1+ikr) - 1 + (ikr)^2/2) / r^3 of the HSP
+ * kernel's expansion, with the reference's series below r = 1e-3
+ * (nihu/library/helmholtz_singular_integrals.hpp:768-777) */
+static cplx hsp_dynamic(double r, double k)
+{
+    cplx ikr = I * (k * r);
+    if (fabs(r) > 1e-3) return (cexp(-ikr) * (1.0 + ikr) - 1.0 + ikr * ikr / 2.0) / r / r / r;
+    return -I * k * k * k *
+           (1.0 / 3.0 - ikr * (1.0 / 8.0 - ikr * (1.0 / 30.0 - ikr * (1.0 / 144.0 - ikr * (1.0 / 840.0 - ikr / 5760.0)))));
+}
+
+/* constant flat triangle, HSP self term: the finite-part static integrals
+ * IddG0 = sum (cos(alpha+theta) - cos(alpha)) / (r sin(alpha)) and
+ * IG0 (the 1/r integral), sides with theta < 1e-3 skipped, plus the dynamic
+ * remainder with the degree-7 Dunavant rule; (IddG0 + k^2/2 IG0 + I_dyn)/(4 pi)
+ * (nihu/library/helmholtz_singular_integrals.hpp:764-839) */
+static cplx self_tria_hsp(const elem_t *e, int fam, double k)
+{
+    double r[4], th[4], al[4];
+    plane_element_helper(e, e->center, r, th, al);
+    double IG0 = 0.0, IddG0 = 0.0;
+    for (int i = 0; i < e->nc; ++i) {
+        if (th[i] < 1e-3) continue;
+        IG0 += r[i] * sin(al[i]) * log(tan((al[i] + th[i]) / 2.0) / tan(al[i] / 2.0));
+        IddG0 += (cos(al[i] + th[i]) - cos(al[i])) / (r[i] * sin(al[i]));
+    }
+    if (fam == FAM_LAPLACE) return IddG0 / (4.0 * PI);
+    const double *q = tri_data + 3 * tri_off[7];
+    cplx dyn = 0.0;
+    for (int p = 0; p < tri_npts[7]; ++p) {
+        double y[3], n[3];
+        elem_x(e, q[3 * p], q[3 * p + 1], y);
+        elem_normal(e, q[3 * p], q[3 * p + 1], n);
+        double rv[3] = {y[0] - e->center[0], y[1] - e->center[1], y[2] - e->center[2]};
+        dyn += hsp_dynamic(norm3(rv), k) * q[3 * p + 2] * norm3(n);
+    }
+    return (IddG0 + k * k / 2.0 * IG0 + dyn) / (4.0 * PI);
+}
+
 /* self-term dispatch (nihu/core/double_integral.hpp:599-639): constant tria
- * SLP shortcut, DLP = 0 on a flat triangle
- * (nihu/library/normal_derivative_singular_integrals.hpp:13-33), quads by Duffy */
+ * SLP and HSP shortcuts, DLP and DLPt = 0 on a flat triangle
+ * (nihu/library/normal_derivative_singular_integrals.hpp:13-56), quads by Duffy
+ * (SLP and DLP only) */
 static cplx self_integral(const elem_t *e, int fam, int op, double k)
 {
-    if (e->nc == 3) return op == OP_SLP ? self_tria_slp(e, fam, k) : 0.0;
+    if (e->nc == 3) {
+        if (op == OP_SLP) return self_tria_slp(e, fam, k);
+        if (op == OP_HSP) return self_tria_hsp(e, fam, k);
+        return 0.0;
+    }
     return self_quad_duffy(e, fam, op, k);
 }
 
@@ -468,13 +562,71 @@ static double static_near(const elem_t *e, const double x0in[3], int op)
     return sgn(z) * res / (4.0 * PI);
 }
 
+/* static parts of DLPt and HSP over a flat element seen from x0 with unit
+ * normal nx (both expressed in the element's plane frame), per side
+ *   DLPt: 6-point Gauss: -nx.r_vec/r + (nx_0 cos t + nx_1 sin t) ln(R + r) - nx_2 sgn(z)
+ *   HSP: 21-point Gauss: -R^2/(r^2 z) (-r_vec.nx/r), or -nx_2/R when |z| <= 1e-12
+ * with r_vec = (R cos t, R sin t, -z), all over 4 pi
+ * (nihu/library/laplace_nearly_singular_integrals.hpp:212-298 and :301-380) */
+static double static_near_bm(const elem_t *e, const double x0in[3], const double nxin[3], int op)
+{
+    double loc[4][3], x0[3], nx[3];
+    int N = e->nc;
+    plane_local(e, x0in, loc, x0);
+    {
+        /* the same rotation applied to the normal (plane_local does not translate) */
+        double unused[4][3];
+        plane_local(e, nxin, unused, nx);
+    }
+    double th_lim[4], th0[4], dref[4];
+    for (int n = 0; n < N; ++n) {
+        const double *c1 = loc[n], *c2 = loc[(n + 1) % N];
+        double l[2] = {c2[0] - c1[0], c2[1] - c1[1]};
+        double ln = sqrt(l[0] * l[0] + l[1] * l[1]);
+        l[0] /= ln; l[1] /= ln;
+        double d1[2] = {c1[0] - x0[0], c1[1] - x0[1]};
+        double pr = d1[0] * l[0] + d1[1] * l[1];
+        double d0[2] = {d1[0] - l[0] * pr, d1[1] - l[1] * pr};
+        th_lim[n] = atan2(d1[1], d1[0]);
+        th0[n] = atan2(d0[1], d0[0]);
+        dref[n] = sqrt(d0[0] * d0[0] + d0[1] * d0[1]);
+    }
+    double z = x0[2] - loc[0][2];
+    const int ng = op == OP_HSP ? 40 / 2 + 1 : g_static_gauss;
+    const double *g = gauss_rule(ng);
+    double res = 0.0;
+    for (int i = 0; i < N; ++i) {
+        double t1 = th_lim[i], t2 = th_lim[(i + 1) % N];
+        if (fabs(t2 - t1) > PI) {
+            if (t2 > t1) t1 += 2.0 * PI; else t2 += 2.0 * PI;
+        }
+        double jac = (t2 - t1) / 2.0;
+        for (int q = 0; q < ng; ++q) {
+            double xi = g[2 * q], w = g[2 * q + 1];
+            double th = t1 * (1.0 - xi) / 2.0 + t2 * (1.0 + xi) / 2.0;
+            double R = dref[i] / cos(th - th0[i]);
+            double r = sqrt(R * R + z * z);
+            double rv[3] = {R * cos(th), R * sin(th), -z};
+            double f;
+            if (op == OP_DLPT) {
+                f = -dot3(nx, rv) / r + (nx[0] * cos(th) + nx[1] * sin(th)) * log(R + r) - nx[2] * sgn(z);
+            } else {
+                double rdnx = -dot3(rv, nx) / r;
+                f = fabs(z) > 1e-12 ? -R * R / (r * r) / z * rdnx : -nx[2] / R;
+            }
+            res += f * jac * w;
+        }
+    }
+    return res / (4.0 * PI);
+}
+
 /* constant flat element, nearly singular: static Laplace part semi-analytic,
  * dynamic part (K_k - K_0) with the degree-14 regular rule (Dunavant 42 points
  * on triangles, 8x8 Gauss on quads)
  * (nihu/library/helmholtz_nearly_singular_integrals.hpp:48-84 SLP, :91-129 DLP) */
-static cplx near_plane(const elem_t *e, int fam, int op, double k, const double x0[3])
+static cplx near_plane(const elem_t *e, int fam, int op, double k, const double x0[3], const double *nx)
 {
-    double st = static_near(e, x0, op);
+    double st = (op == OP_DLPT || op == OP_HSP) ? static_near_bm(e, x0, nx, op) : static_near(e, x0, op);
     if (fam == FAM_LAPLACE) return st;
     double en[3];
     {
@@ -491,7 +643,7 @@ static cplx near_plane(const elem_t *e, int fam, int op, double k, const double 
             double y[3], n[3];
             elem_x(e, q[3 * p], q[3 * p + 1], y);
             elem_normal(e, q[3 * p], q[3 * p + 1], n);
-            cplx kd = kern(FAM_HELMHOLTZ, op, k, x0, y, en) - kern(FAM_LAPLACE, op, k, x0, y, en);
+            cplx kd = kern(FAM_HELMHOLTZ, op, k, x0, nx, y, en) - kern(FAM_LAPLACE, op, k, x0, nx, y, en);
             dyn += kd * q[3 * p + 2] * norm3(n);
         }
     } else {
@@ -502,7 +654,7 @@ static cplx near_plane(const elem_t *e, int fam, int op, double k, const double 
                 double y[3], n[3];
                 elem_x(e, xi, eta, y);
                 elem_normal(e, xi, eta, n);
-                cplx kd = kern(FAM_HELMHOLTZ, op, k, x0, y, en) - kern(FAM_LAPLACE, op, k, x0, y, en);
+                cplx kd = kern(FAM_HELMHOLTZ, op, k, x0, nx, y, en) - kern(FAM_LAPLACE, op, k, x0, nx, y, en);
                 dyn += kd * w * norm3(n);
             }
     }
@@ -586,7 +738,7 @@ static cplx kern_on_elem(const elem_t *e, int fam, int op, double k, const doubl
     elem_normal(e, xi, eta, n);
     double J = norm3(n);
     double un[3] = {n[0] / J, n[1] / J, n[2] / J};
-    return kern(fam, op, k, x0, y, un) * J;
+    return kern(fam, op, k, x0, NULL, y, un) * J;
 }
 
 /* polar quadrature around the image of x0 in the reference domain with the
@@ -641,7 +793,7 @@ static int near_polar(const elem_t *e, int fam, int op, double k, const double x
             }
         }
     }
-    I0 += near_plane(&lin, fam, op, k, x0);
+    I0 += near_plane(&lin, fam, op, k, x0, NULL);
     *out = I0;
     return 1;
 }
@@ -696,9 +848,9 @@ static int near_telles(const elem_t *e, int fam, int op, double k, const double 
  * nihu/library/laplace_nearly_singular_integrals.hpp:399-590): constant triangles
  * use the planar semi-analytic scheme; quads use polar subtraction, except
  * Helmholtz DLP which uses Telles */
-static int near_integral(const elem_t *e, int fam, int op, double k, const double x0[3], cplx *out)
+static int near_integral(const elem_t *e, int fam, int op, double k, const double x0[3], const double *nx, cplx *out)
 {
-    if (e->nc == 3) { *out = near_plane(e, fam, op, k, x0); return 1; }
+    if (e->nc == 3) { *out = near_plane(e, fam, op, k, x0, nx); return 1; }
     if (fam == FAM_HELMHOLTZ && op == OP_DLP) return near_telles(e, fam, op, k, x0, out);
     return near_polar(e, fam, op, k, x0, out);
 }
@@ -731,12 +883,29 @@ const char *oracle_last_error(void) { return g_err; }
  * One entry: self -> nearly singular -> regular, exactly as
  * nihu/core/double_integral.hpp:543-673.  Returns 0 on error.
  */
+static void unit_normal_center(const elem_t *e, double n[3])
+{
+    double xi, eta;
+    domain_center(e->nc, &xi, &eta);
+    elem_normal(e, xi, eta, n);
+    double nn = norm3(n);
+    for (int d = 0; d < 3; ++d) n[d] /= nn;
+}
+
 static int entry(const elem_t *te, const elem_t *re, int same_id, int fam, int op, double k, cplx *out)
 {
+    double nx[3];
+    if (op == OP_DLPT || op == OP_HSP) {
+        if (re->nc != 3) {
+            snprintf(g_err, sizeof g_err, "DLPt / HSP: constant triangle trial elements only");
+            return 0;
+        }
+        unit_normal_center(te, nx);
+    }
     if (same_id && te->nc == re->nc) { *out = self_integral(re, fam, op, k); return 1; }
     double ratio = centre_distance(te, re) / re->size;
     if (ratio < 1.5) {
-        if (!near_integral(re, fam, op, k, te->center, out)) {
+        if (!near_integral(re, fam, op, k, te->center, nx, out)) {
             snprintf(g_err, sizeof g_err, "Could not perform inverse mapping");
             return 0;
         }
@@ -746,7 +915,7 @@ static int entry(const elem_t *te, const elem_t *re, int same_id, int fam, int o
     int degree = cmax + interval_degree(op, ratio);
     if (degree > 14) { snprintf(g_err, sizeof g_err, "Too high quadrature degree selected for collocational integration"); return 0; }
     if (re->nc == 3 && tri_npts[degree] == 0) { snprintf(g_err, sizeof g_err, "unsupported dunavant degree"); return 0; }
-    *out = regular_integral(re, fam, op, k, te->center, degree);
+    *out = regular_integral(re, fam, op, k, te->center, nx, degree);
     return 1;
 }
 
@@ -803,18 +972,54 @@ int oracle_elem_geometry(const double *coords, int nc, double *out7)
 /* single element integrals for known-answer tests.  kind: 0 regular (given
  * degree), 1 nearly singular dispatch, 2 self, 3 planar near-singular scheme
  * (constant-plane formula even on quads). out = (re, im). */
-int oracle_elem_integral(const double *coords, int nc, const double *x0, int fam, int op, double k,
-                         int kind, int degree, double *out)
+int oracle_elem_integral_nx(const double *coords, int nc, const double *x0, const double *nx, int fam, int op,
+                            double k, int kind, int degree, double *out)
 {
     elem_t e;
     elem_init(&e, nc, coords);
     cplx v = 0.0;
-    if (kind == 0) v = regular_integral(&e, fam, op, k, x0, degree);
-    else if (kind == 1) { if (!near_integral(&e, fam, op, k, x0, &v)) return 0; }
+    if ((op == OP_DLPT || op == OP_HSP) && (!nx || nc != 3)) return 0;
+    if (kind == 0) v = regular_integral(&e, fam, op, k, x0, nx, degree);
+    else if (kind == 1) { if (!near_integral(&e, fam, op, k, x0, nx, &v)) return 0; }
     else if (kind == 2) v = self_integral(&e, fam, op, k);
-    else if (kind == 3) v = near_plane(&e, fam, op, k, x0);
+    else if (kind == 3) v = near_plane(&e, fam, op, k, x0, nx);
     else return 0;
     out[0] = creal(v); out[1] = cimag(v);
+    return 1;
+}
+
+/* the same for SLP and DLP (no normal at the collocation point) */
+int oracle_elem_integral(const double *coords, int nc, const double *x0, int fam, int op, double k,
+                         int kind, int degree, double *out)
+{
+    if (op != OP_SLP && op != OP_DLP) return 0;
+    return oracle_elem_integral_nx(coords, nc, x0, NULL, fam, op, k, kind, degree, out);
+}
+
+/* per-pair quadrature degree of one operator for tests: -1 self, -2 near */
+int oracle_degree(const double *tnodes, int tn_nodes, const int *telems, int tn_elems, int tcols,
+                  const double *rnodes, int rn_nodes, const int *relems, int rn_elems, int rcols,
+                  int same_mesh, int op, int row_begin, int row_end, int *out)
+{
+    for (int i = row_begin; i < row_end; ++i) {
+        elem_t te;
+        if (!load_elem(tnodes, tn_nodes, telems, tcols, i, &te)) return 0;
+        for (int j = 0; j < rn_elems; ++j) {
+            elem_t re;
+            if (!load_elem(rnodes, rn_nodes, relems, rcols, j, &re)) return 0;
+            int code;
+            if (same_mesh && i == j && te.nc == re.nc) code = -1;
+            else {
+                double ratio = centre_distance(&te, &re) / re.size;
+                if (ratio < 1.5) code = -2;
+                else {
+                    int cmax = field_complexity(te.nc) > field_complexity(re.nc) ? field_complexity(te.nc) : field_complexity(re.nc);
+                    code = cmax + interval_degree(op, ratio);
+                }
+            }
+            out[(long)(i - row_begin) * rn_elems + j] = code;
+        }
+    }
     return 1;
 }
 

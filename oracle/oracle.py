@@ -16,7 +16,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "liboracle.so")
 SOURCES = [os.path.join(HERE, "nihu_oracle.c")]
 HELMHOLTZ, LAPLACE = 0, 1
-SLP, DLP = 1, 2
+SLP, DLP, DLPT, HSP = 1, 2, 4, 8
 
 
 def build(force: bool = False) -> str:
@@ -50,6 +50,11 @@ def lib():
             L.oracle_classify.restype = c_int
             L.oracle_elem_integral.argtypes = [dp, c_int, dp, c_int, c_int, c_double, c_int, c_int, dp]
             L.oracle_elem_integral.restype = c_int
+            L.oracle_elem_integral_nx.argtypes = [dp, c_int, dp, dp, c_int, c_int, c_double, c_int, c_int, dp]
+            L.oracle_elem_integral_nx.restype = c_int
+            L.oracle_degree.argtypes = [dp, c_int, ip, c_int, c_int, dp, c_int, ip, c_int, c_int,
+                                        c_int, c_int, c_int, c_int, ip]
+            L.oracle_degree.restype = c_int
             L.oracle_elem_geometry.argtypes = [dp, c_int, dp]
             L.oracle_last_error.restype = ctypes.c_char_p
             _lib = L
@@ -118,12 +123,33 @@ def classify(test_mesh, trial_mesh, same_mesh=None, rows=None):
     return out
 
 
-def elem_integral(coords, x0, family, op, k, kind, degree=0):
-    """kind: 0 regular(degree), 1 nearly singular dispatch, 2 self, 3 planar near scheme."""
+def elem_integral(coords, x0, family, op, k, kind, degree=0, nx=None):
+    """kind: 0 regular(degree), 1 nearly singular dispatch, 2 self, 3 planar near scheme.
+    nx: unit normal at the collocation point (DLPT and HSP)."""
     coords = np.ascontiguousarray(coords, dtype=np.float64)
     x0 = np.ascontiguousarray(x0, dtype=np.float64)
     out = np.zeros(2)
-    if not lib().oracle_elem_integral(_ptr(coords, ctypes.c_double), coords.shape[0], _ptr(x0, ctypes.c_double),
-                                      family, op, float(k), kind, degree, _ptr(out, ctypes.c_double)):
+    if nx is None:
+        ok = lib().oracle_elem_integral(_ptr(coords, ctypes.c_double), coords.shape[0], _ptr(x0, ctypes.c_double),
+                                        family, op, float(k), kind, degree, _ptr(out, ctypes.c_double))
+    else:
+        nx = np.ascontiguousarray(nx, dtype=np.float64)
+        ok = lib().oracle_elem_integral_nx(_ptr(coords, ctypes.c_double), coords.shape[0],
+                                           _ptr(x0, ctypes.c_double), _ptr(nx, ctypes.c_double), family, op,
+                                           float(k), kind, degree, _ptr(out, ctypes.c_double))
+    if not ok:
         raise RuntimeError("element integral failed")
     return complex(out[0], out[1])
+
+
+def degree(test_mesh, trial_mesh, op, same_mesh=None, rows=None):
+    """Quadrature degree of operator op per pair: -1 self, -2 nearly singular."""
+    tn, te, targs = _mesh_args(*test_mesh)
+    rn, re_, rargs = _mesh_args(*trial_mesh)
+    if same_mesh is None:
+        same_mesh = test_mesh is trial_mesh
+    r0, r1 = (0, len(te)) if rows is None else rows
+    out = np.zeros((r1 - r0, len(re_)), dtype=np.int32)
+    if not lib().oracle_degree(*targs, *rargs, int(same_mesh), op, r0, r1, _ptr(out, ctypes.c_int)):
+        raise RuntimeError(lib().oracle_last_error().decode())
+    return out

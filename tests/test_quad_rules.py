@@ -28,7 +28,7 @@ def tri(degree):
     return data[offs[degree]:offs[degree] + npts[degree]]
 
 
-@pytest.mark.parametrize("n", range(1, 17))
+@pytest.mark.parametrize("n", range(1, 22))
 def test_gauss_legendre_exact(n):
     r = gauss(n)
     assert np.all(np.diff(r[:, 0]) > 0)
