@@ -59,6 +59,11 @@ typedef enum nihu_gb_status {
 /* operator bit mask: SLP = G, DLP = dG/dn_y (nihu/library/normal_derivative_kernel.hpp) */
 #define NIHU_GB_SLP 1
 #define NIHU_GB_DLP 2
+/* Burton-Miller operators: DLPt = dG/dn_x, HSP = d2G/dn_x dn_y
+ * (helmholtz_3d_DLPt_kernel / helmholtz_3d_HSP_kernel,
+ * nihu/library/helmholtz_kernel.hpp:326-334, laplace_kernel.hpp likewise) */
+#define NIHU_GB_DLPT 4
+#define NIHU_GB_HSP 8
 
 /* storage type of a matrix or vector */
 #define NIHU_GB_C64 0  /* complex64: 2 x float32 */
@@ -156,6 +161,39 @@ nihu_gb_status nihu_gb_assemble(nihu_gb_ctx *ctx, const nihu_gb_mesh *test, cons
  * n x n with n = number of mesh elements. */
 nihu_gb_status nihu_gb_add_identity(nihu_gb_ctx *ctx, const nihu_gb_mesh *mesh, double alpha_re, double alpha_im,
                                     int dtype, void *out, int64_t ld, int where);
+
+/* The Burton-Miller operators DLPt (transposed double layer, kernel
+ * dG/dr (-r.n_x)/r) and HSP (hypersingular, d2G/dn_x dn_y) with the same
+ * conventions as nihu_gb_assemble: `ops` is a bit mask of NIHU_GB_DLPT /
+ * NIHU_GB_HSP, out = alpha * Op (or += with accumulate).  n_x is the unit
+ * normal at the collocation point (test element centre).  The trial mesh must
+ * hold constant triangles only (the reference's constant-plane singular and
+ * nearly singular schemes for these kernels are triangle schemes); quad
+ * trial elements give NIHU_GB_ERR_INVALID_ARGUMENT.  Regular pairs take the
+ * distance-adaptive rule of each kernel (HSP: 1/r^3 intervals 1.9 / 3.6 /
+ * 22.3); nearly singular pairs the semi-analytic static part plus the
+ * 42-point dynamic part; self terms DLPt = 0 and the finite-part HSP integral.
+ * Replaces: test_space * (alpha * Htop)[trial_space] and
+ * test_space * (alpha * Dop)[trial_space] of
+ * nihu/applications/helmholtz/helmholtz_3d_coll.cpp:53-56,71,87, dispatched by
+ * nihu/core/double_integral.hpp:543-673 to
+ * nihu/library/helmholtz_singular_integrals.hpp:764-839 and
+ * nihu/library/helmholtz_nearly_singular_integrals.hpp:131-220. */
+nihu_gb_status nihu_gb_assemble_bm(nihu_gb_ctx *ctx, const nihu_gb_mesh *test, const nihu_gb_mesh *trial,
+                                   int family, int ops, double k, double alpha_re, double alpha_im,
+                                   int precision, int dtype, void *out_dlpt, void *out_hsp, int64_t ld,
+                                   int accumulate, int where);
+
+/* The two Burton-Miller system matrices of one mesh with coupling c
+ * (the reference application uses c = -i/k):
+ *     A = DLP - 1/2 I + c HSP,   B = SLP + c DLPt + c/2 I
+ * assembled in one pass over the element pairs (all four kernels share each
+ * quadrature point).  The solve is then A p = B q.
+ * Replaces: nihu/applications/helmholtz/helmholtz_3d_coll.cpp:60-100 (BM
+ * branch, matrices Gs and Hs). */
+nihu_gb_status nihu_gb_assemble_burton_miller(nihu_gb_ctx *ctx, const nihu_gb_mesh *mesh, int family, double k,
+                                              double coupling_re, double coupling_im, int precision, int dtype,
+                                              void *out_a, void *out_b, int64_t ld, int where);
 
 /* Per-pair quadrature statistics of an assembly (no matrix is written):
  * counts[0] self pairs, counts[1] nearly singular pairs, counts[2 + 3*s + d]
@@ -310,6 +348,17 @@ nihu_gb_status nihu_gb_lu_solve(nihu_gb_ctx *ctx, void *A, int64_t n, int64_t ld
 nihu_gb_status nihu_gb_solve_cbie(nihu_gb_ctx *ctx, const nihu_gb_mesh *mesh, int family, double k,
                                   int precision, int dtype, const void *q, void *p, int solver,
                                   int restart, int max_iters, double tol, int *iters, double *rel_residual);
+
+/* Burton-Miller exterior solve A p = B q (matrices of
+ * nihu_gb_assemble_burton_miller) by GMRES (solver 0) or LU (solver 1,
+ * dtype = NIHU_GB_C128); arguments as nihu_gb_solve_cbie.  Free of the
+ * fictitious interior resonances of the plain CBIE.
+ * Replaces: nihu/applications/helmholtz/helmholtz_3d_coll.cpp:36-120 with BM
+ * (KHIE + HSIE) defined. */
+nihu_gb_status nihu_gb_solve_burton_miller(nihu_gb_ctx *ctx, const nihu_gb_mesh *mesh, int family, double k,
+                                           double coupling_re, double coupling_im, int precision, int dtype,
+                                           const void *q, void *p, int solver, int restart, int max_iters, double tol,
+                                           int *iters, double *rel_residual);
 
 /* A frequency sweep over fixed meshes captured once as a CUDA graph and
  * replayed per set of wave numbers (the batched counterpart of running

@@ -20,6 +20,7 @@ STATUS_NAMES = {
 TRIA_1, QUAD_1 = 32303, 32404
 HELMHOLTZ_3D, LAPLACE_3D = 0, 1
 SLP, DLP = 1, 2
+DLPT, HSP = 4, 8  # Burton-Miller operators
 C64, C128 = 0, 1
 REGULAR_FP32, REGULAR_FP64 = 0, 1
 GEMM_FP32, GEMM_TF32, GEMM_BF16X9 = 0, 1, 2
@@ -69,6 +70,9 @@ SIGNATURES = {
     "nihu_gb_server_step": (_i, [_vp, _ip, _ip, _ip]),
     "nihu_gb_server_take": (_i, [_vp, ctypes.POINTER(ctypes.c_int64), _vp, _i64, _ip, _dp, _ip]),
     "nihu_gb_solve_cbie": (_i, [_vp, _vp, _i, _d, _i, _i, _vp, _vp, _i, _i, _i, _d, _ip, _dp]),
+    "nihu_gb_assemble_bm": (_i, [_vp, _vp, _vp, _i, _i, _d, _d, _d, _i, _i, _vp, _vp, _i64, _i, _i]),
+    "nihu_gb_assemble_burton_miller": (_i, [_vp, _vp, _i, _d, _d, _d, _i, _i, _vp, _vp, _i64, _i]),
+    "nihu_gb_solve_burton_miller": (_i, [_vp, _vp, _i, _d, _d, _d, _i, _i, _vp, _vp, _i, _i, _i, _d, _ip, _dp]),
 }
 
 _lib = None

@@ -207,6 +207,24 @@ def laplace_3d_DLP_kernel() -> Kernel:
     return Kernel(C.LAPLACE_3D, C.DLP, 0.0, "laplace_3d_DLP")
 
 
+def helmholtz_3d_DLPt_kernel(k: float) -> Kernel:
+    """dG/dn_x (nihu/library/helmholtz_kernel.hpp:326-328); constant triangle trial elements."""
+    return Kernel(C.HELMHOLTZ_3D, C.DLPT, k, "helmholtz_3d_DLPt")
+
+
+def helmholtz_3d_HSP_kernel(k: float) -> Kernel:
+    """d2G/dn_x dn_y (nihu/library/helmholtz_kernel.hpp:332-334); constant triangle trial elements."""
+    return Kernel(C.HELMHOLTZ_3D, C.HSP, k, "helmholtz_3d_HSP")
+
+
+def laplace_3d_DLPt_kernel() -> Kernel:
+    return Kernel(C.LAPLACE_3D, C.DLPT, 0.0, "laplace_3d_DLPt")
+
+
+def laplace_3d_HSP_kernel() -> Kernel:
+    return Kernel(C.LAPLACE_3D, C.HSP, 0.0, "laplace_3d_HSP")
+
+
 class IntegralOperator:
     """create_integral_operator(kernel), with scalar scaling (nihu/core/integral_operator.hpp:131-194,324-329)."""
 
@@ -322,10 +340,16 @@ def _assemble_into(ctx, result, test_mesh, trial_mesh, family, op, k, alpha, pre
     else:
         cdt = np.complex64 if dtype == C.C64 else np.complex128
         buf, accumulate = np.zeros(result.shape, dtype=cdt, order="F"), 0
-    out_s = buf.ctypes.data if op == C.SLP else None
-    out_d = buf.ctypes.data if op == C.DLP else None
-    ctx.check(L.nihu_gb_assemble(ctx.handle, tdm.handle, rdm_handle, family, op, k, alpha.real, alpha.imag, prec,
-                                 dtype, out_s, out_d, max(result.shape[0], 1), accumulate, C.HOST))
+    if op in (C.SLP, C.DLP):
+        out_s = buf.ctypes.data if op == C.SLP else None
+        out_d = buf.ctypes.data if op == C.DLP else None
+        ctx.check(L.nihu_gb_assemble(ctx.handle, tdm.handle, rdm_handle, family, op, k, alpha.real, alpha.imag, prec,
+                                     dtype, out_s, out_d, max(result.shape[0], 1), accumulate, C.HOST))
+    else:
+        out_t = buf.ctypes.data if op == C.DLPT else None
+        out_h = buf.ctypes.data if op == C.HSP else None
+        ctx.check(L.nihu_gb_assemble_bm(ctx.handle, tdm.handle, rdm_handle, family, op, k, alpha.real, alpha.imag,
+                                        prec, dtype, out_t, out_h, max(result.shape[0], 1), accumulate, C.HOST))
     if buf is not result:
         if target is None:
             result += buf.real.astype(result.dtype)
@@ -428,6 +452,49 @@ def solve_cbie(mesh: Mesh, k: float, q, family: int = C.HELMHOLTZ_3D, dtype: int
                                     C.REGULAR_FP64 if precision == "fp64" else C.REGULAR_FP32, dtype,
                                     q.ctypes.data, p.ctypes.data, 0 if solver == "gmres" else 1, restart,
                                     max_iters, tol, ctypes.byref(it), ctypes.byref(res))
+    if st != C.OK and (check or st != 6):
+        ctx.check(st)
+    return p, it.value, res.value
+
+
+def burton_miller_coupling(k: float) -> complex:
+    """The reference application's coupling constant -i/k
+    (nihu/applications/helmholtz/helmholtz_3d_coll.cpp:44)."""
+    return complex(0.0, -1.0 / k)
+
+
+def assemble_burton_miller(mesh: Mesh, k: float, coupling=None, family: int = C.HELMHOLTZ_3D, dtype: int = C.C64,
+                           precision: str = "fp32", ctx: Context | None = None):
+    """The Burton-Miller system matrices A = DLP - I/2 + c HSP and B = SLP + c DLPt + c/2 I
+    (c = -i/k by default), assembled on the GPU in one pass; returns (A, B)."""
+    ctx = ctx or default_context()
+    c = burton_miller_coupling(k) if coupling is None else complex(coupling)
+    n = mesh.num_elements
+    cdt = np.complex64 if dtype == C.C64 else np.complex128
+    A = np.zeros((n, n), cdt, order="F")
+    B = np.zeros((n, n), cdt, order="F")
+    dm = mesh.device(ctx)
+    ctx.check(C.lib().nihu_gb_assemble_burton_miller(ctx.handle, dm.handle, family, k, c.real, c.imag,
+                                                     C.REGULAR_FP64 if precision == "fp64" else C.REGULAR_FP32,
+                                                     dtype, A.ctypes.data, B.ctypes.data, max(n, 1), C.HOST))
+    return A, B
+
+
+def solve_burton_miller(mesh: Mesh, k: float, q, coupling=None, family: int = C.HELMHOLTZ_3D, dtype: int = C.C64,
+                        solver: str = "gmres", precision: str = "fp32", restart: int = 50, max_iters: int = 1000,
+                        tol: float = 1e-6, ctx: Context | None = None, check: bool = True):
+    """Burton-Miller exterior solve A p = B q on the GPU (c = -i/k by default);
+    returns (p, iterations, residual)."""
+    ctx = ctx or default_context()
+    c = burton_miller_coupling(k) if coupling is None else complex(coupling)
+    q = _c128(q)
+    p = np.zeros_like(q)
+    it, res = ctypes.c_int(0), ctypes.c_double(0.0)
+    dm = mesh.device(ctx)
+    st = C.lib().nihu_gb_solve_burton_miller(ctx.handle, dm.handle, family, k, c.real, c.imag,
+                                             C.REGULAR_FP64 if precision == "fp64" else C.REGULAR_FP32, dtype,
+                                             q.ctypes.data, p.ctypes.data, 0 if solver == "gmres" else 1, restart,
+                                             max_iters, tol, ctypes.byref(it), ctypes.byref(res))
     if st != C.OK and (check or st != 6):
         ctx.check(st)
     return p, it.value, res.value

@@ -24,15 +24,6 @@ namespace nihu {
 constexpr int REG_THREADS = 256;
 constexpr int REG_COLS = 32;
 
-// sin and cos of 2 pi t for any t: the period count is removed exactly
-// (t - rint(t) is exact in binary floating point), leaving |2 pi f| <= pi for
-// the hardware approximation (absolute error about 4e-7 there)
-__device__ __forceinline__ void sincos_2pi(float t, float &s, float &c)
-{
-    float f = t - rintf(t);
-    __sincosf(6.28318530717958647692f * f, &s, &c);
-}
-
 template <int FAM, typename R>
 __device__ __forceinline__ void eval_point(R rx, R ry, R rz, R wj, R nx, R ny, R nz, R k, R ws, R wd, R &sr,
                                            R &si, R &dr, R &di)

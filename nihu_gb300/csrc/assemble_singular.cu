@@ -29,87 +29,12 @@
 // through their power series in k (near_moments / near_series below).
 #include <cmath>
 
-#include "geom.cuh"
 #include "kernels.h"
+#include "planar.cuh"
 
 namespace nihu {
 
 constexpr int SING_THREADS = 128;
-constexpr double INV_FOUR_PI = 1.0 / FOUR_PI;
-
-struct Acc {
-    double sr = 0, si = 0, dr = 0, di = 0;
-};
-
-// Maclaurin series of cos and sin truncated after x^22 / x^23: on
-// |x| <= pi/2 the first omitted terms are below 1e-19, so these agree with the
-// correctly rounded values to a few ulp at a fraction of the cost of the
-// general routines (which reduce arbitrary arguments).  Coefficients are
-// (-1)^n / (2n)! and (-1)^n / (2n+1)!.
-struct TaylorCoeffs {
-    double c[12], s[12];
-    constexpr TaylorCoeffs() : c(), s()
-    {
-        double fc = 1.0, fs = 1.0;  // (2n)! and (2n+1)!
-        for (int n = 0; n < 12; ++n) {
-            if (n > 0) {
-                fc *= (2.0 * n - 1.0) * (2.0 * n);
-                fs *= (2.0 * n) * (2.0 * n + 1.0);
-            }
-            c[n] = (n % 2 ? -1.0 : 1.0) / fc;
-            s[n] = (n % 2 ? -1.0 : 1.0) / fs;
-        }
-    }
-};
-__device__ constexpr TaylorCoeffs TAYLOR{};
-constexpr double HALF_PI = 1.57079632679489661923;
-
-// sin and cos for |x| <= pi/2 (general routine beyond).  `short_series`
-// is a launch-wide promise that every argument has |x| <= 3/4 (nearly
-// singular pairs at small k D): the terms up to x^18 / x^19 then leave an
-// error below 2e-21.
-__device__ __forceinline__ void sincos_bounded(double x, double *s, double *c, bool short_series)
-{
-    const double ax = fabs(x);
-    if (ax > HALF_PI || (short_series && ax > 0.75)) {
-        sincos(x, s, c);
-        return;
-    }
-    const double u = x * x;
-    double pc, ps;
-    if (short_series) {
-        pc = TAYLOR.c[9];
-        ps = TAYLOR.s[9];
-#pragma unroll
-        for (int n = 8; n >= 0; --n) {
-            pc = fma(pc, u, TAYLOR.c[n]);
-            ps = fma(ps, u, TAYLOR.s[n]);
-        }
-    } else {
-        pc = TAYLOR.c[11];
-        ps = TAYLOR.s[11];
-#pragma unroll
-        for (int n = 10; n >= 0; --n) {
-            pc = fma(pc, u, TAYLOR.c[n]);
-            ps = fma(ps, u, TAYLOR.s[n]);
-        }
-    }
-    *c = pc;
-    *s = ps * x;
-}
-
-// cos of an angle difference known to lie within pi/2 of 0 modulo 2 pi
-__device__ __forceinline__ double cos_angle(double x)
-{
-    x -= (2.0 * PI) * rint(x * (0.5 / PI));
-    if (fabs(x) > HALF_PI) return cos(x);
-    const double u = x * x;
-    double pc = TAYLOR.c[11];
-#pragma unroll
-    for (int n = 10; n >= 0; --n) pc = fma(pc, u, TAYLOR.c[n]);
-    return pc;
-}
-
 // G(r) and dG/dr of the Helmholtz kernel sharing one sincos and 1/r:
 //   G = e^{-ikr}/(4 pi r), dG/dr = -(1 + ikr) e^{-ikr}/(4 pi r^2)
 __device__ __forceinline__ void helm_g_dg(double k, double r, double rinv, cd &g, cd &dg)
@@ -154,53 +79,6 @@ __device__ __forceinline__ void kern_on_elem(const Elem64 &e, int fam, double k,
 }
 
 // ------------------------------------------------------------------ planar
-
-// rotate the element parallel to the x-y plane (nihu/library/plane_element_helper.hpp:112-126)
-__device__ void plane_local(const Elem64 &e, const double x0in[3], double loc[4][2], double &z)
-{
-    double v1[3], v2[3], t0[3], t1[3], t2[3];
-    for (int d = 0; d < 3; ++d) { v1[d] = e.c[1][d] - e.c[0][d]; v2[d] = e.c[2][d] - e.c[0][d]; }
-    double n1 = 1.0 / norm3(v1);
-    for (int d = 0; d < 3; ++d) t0[d] = v1[d] * n1;
-    cross3(v1, v2, t2);
-    double n2 = 1.0 / norm3(t2);
-    for (int d = 0; d < 3; ++d) t2[d] *= n2;
-    cross3(t2, t0, t1);
-    double n3 = 1.0 / norm3(t1);
-    for (int d = 0; d < 3; ++d) t1[d] *= n3;
-    for (int a = 0; a < e.nc; ++a) {
-        double dv[3] = {e.c[a][0] - x0in[0], e.c[a][1] - x0in[1], e.c[a][2] - x0in[2]};
-        loc[a][0] = dot3(t0, dv);
-        loc[a][1] = dot3(t1, dv);
-    }
-    // height of x0 above the element plane
-    double dv[3] = {x0in[0] - e.c[0][0], x0in[1] - e.c[0][1], x0in[2] - e.c[0][2]};
-    z = dot3(t2, dv);
-}
-
-// corner angle, foot angle and distance of a side (c1 -> c2) seen from the
-// origin of the local frame (nihu/library/plane_element_helper.hpp:76-99)
-__device__ __forceinline__ void side_geometry(const double c1[2], const double c2[2], double &th_lim, double &th0,
-                                              double &dref, bool guard_short)
-{
-    double l0 = 1.0, l1 = 0.0;
-    double d0 = c2[0] - c1[0], d1 = c2[1] - c1[1];
-    double ln = sqrt(d0 * d0 + d1 * d1);
-    if (!guard_short || ln > 1e-3) { double il = 1.0 / ln; l0 = d0 * il; l1 = d1 * il; }
-    double pr = c1[0] * l0 + c1[1] * l1;
-    double f0 = c1[0] - l0 * pr, f1 = c1[1] - l1 * pr;
-    th_lim = atan2(c1[1], c1[0]);
-    th0 = atan2(f1, f0);
-    dref = sqrt(f0 * f0 + f1 * f1);
-}
-
-__device__ __forceinline__ void wrap_limits(double &t1, double &t2)
-{
-    if (fabs(t2 - t1) > PI) {
-        if (t2 > t1) t1 += 2.0 * PI;
-        else t2 += 2.0 * PI;
-    }
-}
 
 // static (Laplace) nearly singular part over a flat element: radial integral
 // analytic, angular integral with 6 Gauss points per side
@@ -628,38 +506,6 @@ __device__ void near_telles_sum(const Elem64 &e, int fam, double k, const double
 
 // -------------------------------------------------------------------- self
 
-// analytic static part of the flat-element 1/r integral from an interior point
-// (nihu/library/plane_element_helper.hpp:42-74)
-__device__ double self_static(const Elem64 &e, const double x0[3])
-{
-    const int N = e.nc;
-    double R[4][3], r[4];
-    for (int i = 0; i < N; ++i) {
-        for (int d = 0; d < 3; ++d) R[i][d] = e.c[i][d] - x0[d];
-        r[i] = norm3(R[i]);
-        double ir = 1.0 / r[i];
-        for (int d = 0; d < 3; ++d) R[i][d] *= ir;
-    }
-    double v = 0.0;
-    for (int i = 0; i < N; ++i) {
-        int i1 = (i + 1) % N;
-        double C[3] = {e.c[i][0] - e.c[i1][0], e.c[i][1] - e.c[i1][1], e.c[i][2] - e.c[i1][2]};
-        double ic = 1.0 / norm3(C);
-        for (int d = 0; d < 3; ++d) C[d] *= ic;
-        double cs = dot3(R[i], R[i1]);
-        double theta = cs >= 1.0 ? 0.0 : acos(cs);
-        double alpha = acos(dot3(R[i], C));
-        v += r[i] * sin(alpha) * log(tan((alpha + theta) / 2.0) / tan(alpha / 2.0));
-    }
-    return v;
-}
-
-__device__ __forceinline__ double sinc_ref(double x)
-{
-    if (fabs(x) > 1e-3) return sin(x) / x;
-    return 1.0 - x * x / 6.0 * (1.0 - x * x / 20.0);
-}
-
 // (e^{-ikr} - 1) / (4 pi r) over a flat triangle with the 13-point degree-7
 // rule, as -ik e^{-ikr/2} sinc(kr/2) / (4 pi)
 __device__ void self_tria_dynamic(const Elem64 &e, double k, const double x0[3], Acc &a)
@@ -767,22 +613,6 @@ __device__ void self_quad(const Elem64 &e, int fam, double k, const double x0[3]
 
 // ------------------------------------------------------------------ driver
 
-template <typename Out>
-__device__ __forceinline__ void store64(Out *p, double re, double im, double are, double aim, int accumulate)
-{
-    double vr = are * re - aim * im, vi = are * im + aim * re;
-    Out o;
-    if (accumulate) {
-        o = *p;
-        o.x += vr;
-        o.y += vi;
-    } else {
-        o.x = vr;
-        o.y = vi;
-    }
-    *p = o;
-}
-
 // BATCH: frequency batch (a.nk > 1), a separate kernel so that the single
 // wave number kernel carries none of its code.
 template <typename Out, bool BATCH>
@@ -811,13 +641,7 @@ __device__ __forceinline__ void singular_pairs(const RegularArgs &a, const NearL
         if (item < n_near) {
             int64_t p = p_begin + item;
             i = near.rows[p];
-            int lo = a.j0, hi = a.j1 - 1;  // largest j with col_ptr[j] <= p
-            while (lo < hi) {
-                int mid = (lo + hi + 1) >> 1;
-                if (near.col_ptr[mid] <= p) lo = mid;
-                else hi = mid - 1;
-            }
-            j = lo;
+            j = near_column(near.col_ptr, a.j0, a.j1, p);
             self = false;
         } else {
             j = a.j0 + (int)(item - n_near);

@@ -295,6 +295,77 @@ nihu_gb_status check_flag(nihu_gb_ctx *ctx)
     return NIHU_GB_OK;
 }
 
+// columns [j0, j1) of up to two outputs into device buffers whose column j
+// starts at out + (j - j0) * ld
+using PanelFn = std::function<nihu_gb_status(void *o0, void *o1, int64_t ld, int j0, int j1)>;
+
+// host outputs: column panels, double-buffered; the D2H copies on the copy
+// stream overlap the next panel's kernels (out0 / out1 may be NULL)
+nihu_gb_status assemble_host_panels(nihu_gb_ctx *ctx, int64_t M, int64_t N, int dtype, void *out0, void *out1, int64_t ld,
+                                    int accumulate, const PanelFn &fn)
+{
+    const size_t es = elem_bytes(dtype);
+    nihu_gb_status st = NIHU_GB_OK;
+    const int nbuf_ops = (out0 ? 1 : 0) + (out1 ? 1 : 0);
+    const size_t col_bytes = (size_t)M * es;
+    size_t panel_cap = (size_t)256 << 20;  // bytes per buffer
+    if (ctx->budget) {
+        size_t avail = ctx->budget > ctx->used ? ctx->budget - ctx->used : 0;
+        panel_cap = std::min(panel_cap, avail / (2 * nbuf_ops + 1));
+    }
+    int64_t P = std::max<int64_t>(1, (int64_t)(panel_cap / col_bytes));
+    P = std::min<int64_t>(P, N);
+    void *buf[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};
+    const char *names[2][2] = {{"panel_s0", "panel_d0"}, {"panel_s1", "panel_d1"}};
+    for (int b = 0; b < 2; ++b)
+        for (int o = 0; o < 2; ++o) {
+            if (!(o == 0 ? out0 : out1)) continue;
+            st = scratch(ctx, names[b][o], col_bytes * P, &buf[b][o]);
+            if (st) return st;
+        }
+    cudaEvent_t computed[2], copied[2];
+    for (int b = 0; b < 2; ++b) {
+        cudaEventCreateWithFlags(&computed[b], cudaEventDisableTiming);
+        cudaEventCreateWithFlags(&copied[b], cudaEventDisableTiming);
+    }
+    void *outs[2] = {out0, out1};
+    cudaError_t e = cudaSuccess;
+    int b = 0;
+    bool used[2] = {false, false};
+    for (int64_t j0 = 0; j0 < N && e == cudaSuccess && st == NIHU_GB_OK; j0 += P, b ^= 1) {
+        const int64_t j1 = std::min(N, j0 + P);
+        if (used[b]) e = cudaStreamWaitEvent(ctx->stream, copied[b], 0);
+        for (int o = 0; o < 2 && e == cudaSuccess; ++o) {
+            if (!buf[b][o] || !accumulate) continue;
+            e = cudaMemcpy2DAsync(buf[b][o], col_bytes, (char *)outs[o] + j0 * ld * es, ld * es, col_bytes, j1 - j0,
+                                  cudaMemcpyHostToDevice, ctx->stream);
+        }
+        if (e != cudaSuccess) break;
+        st = fn(buf[b][0], buf[b][1], M, (int)j0, (int)j1);
+        if (st) break;
+        e = cudaEventRecord(computed[b], ctx->stream);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(ctx->copy_stream, computed[b], 0);
+        for (int o = 0; o < 2 && e == cudaSuccess; ++o) {
+            if (!buf[b][o]) continue;
+            e = cudaMemcpy2DAsync((char *)outs[o] + j0 * ld * es, ld * es, buf[b][o], col_bytes, col_bytes, j1 - j0,
+                                  cudaMemcpyDeviceToHost, ctx->copy_stream);
+        }
+        if (e == cudaSuccess) e = cudaEventRecord(copied[b], ctx->copy_stream);
+        used[b] = true;
+    }
+    cudaError_t e2 = cudaStreamSynchronize(ctx->copy_stream);
+    cudaError_t e3 = cudaStreamSynchronize(ctx->stream);
+    for (int q = 0; q < 2; ++q) {
+        cudaEventDestroy(computed[q]);
+        cudaEventDestroy(copied[q]);
+    }
+    if (st) return st;
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "panel assembly");
+    if (e2 != cudaSuccess) return cuda_fail(ctx, e2, "panel copy");
+    if (e3 != cudaSuccess) return cuda_fail(ctx, e3, "panel compute");
+    return check_flag(ctx);
+}
+
 }  // namespace
 
 extern "C" {
@@ -582,7 +653,6 @@ nihu_gb_status nihu_gb_assemble(nihu_gb_ctx *ctx, const nihu_gb_mesh *test, cons
     a.alpha_re32 = (float)alpha_re;
     a.alpha_im32 = (float)alpha_im;
     a.unit_alpha = alpha_re == 1.0 && alpha_im == 0.0;
-    const size_t es = elem_bytes(dtype);
     const int64_t M = test->n, N = trial->n;
 
     if (where == NIHU_GB_DEVICE) {
@@ -596,71 +666,203 @@ nihu_gb_status nihu_gb_assemble(nihu_gb_ctx *ctx, const nihu_gb_mesh *test, cons
         return check_flag(ctx);
     }
 
-    // host outputs: column panels, double-buffered; D2H copies on the copy
-    // stream overlap the next panel's kernels
-    const int nbuf_ops = (ops == 3) ? 2 : 1;
-    const size_t col_bytes = (size_t)M * es;
-    size_t panel_cap = (size_t)256 << 20;  // bytes per buffer
-    if (ctx->budget) {
-        size_t avail = ctx->budget > ctx->used ? ctx->budget - ctx->used : 0;
-        panel_cap = std::min(panel_cap, avail / (2 * nbuf_ops + 1));
-    }
-    int64_t P = std::max<int64_t>(1, (int64_t)(panel_cap / col_bytes));
-    P = std::min<int64_t>(P, N);
-    void *buf[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};
-    const char *names[2][2] = {{"panel_s0", "panel_d0"}, {"panel_s1", "panel_d1"}};
-    for (int b = 0; b < 2; ++b)
-        for (int o = 0; o < 2; ++o) {
-            if (!((o == 0 && (ops & 1)) || (o == 1 && (ops & 2)))) continue;
-            st = scratch(ctx, names[b][o], col_bytes * P, &buf[b][o]);
-            if (st) return st;
+    return assemble_host_panels(ctx, M, N, dtype, (ops & NIHU_GB_SLP) ? out_slp : nullptr,
+                                (ops & NIHU_GB_DLP) ? out_dlp : nullptr, ld, accumulate,
+                                [&](void *o0, void *o1, int64_t pld, int j0, int j1) {
+                                    a.out_s = o0;
+                                    a.out_d = o1;
+                                    a.ld = pld;
+                                    a.j0 = j0;
+                                    a.j1 = j1;
+                                    return assemble_panel(ctx, a, nl);
+                                });
+}
+
+}  // extern "C"
+
+namespace {
+
+constexpr int BM_ALL = NIHU_GB_SLP | NIHU_GB_DLP | NIHU_GB_DLPT | NIHU_GB_HSP;
+
+// Burton-Miller operators on one column panel: the FP64 nearly singular and
+// self kernels on the auxiliary stream beside the regular kernel (as
+// assemble_panel); the fused system takes its SLP and DLP near and self
+// entries from the plain singular kernel, then adds the DLPt and HSP ones
+nihu_gb_status assemble_panel_bm(nihu_gb_ctx *ctx, const BmArgs &b, NearList *nl)
+{
+    const bool all4 = b.ops == BM_ALL;
+    cudaError_t e = cudaEventRecord(ctx->ev_fork, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(ctx->aux_stream, ctx->ev_fork, 0);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "fork");
+    {
+        Phase ph(ctx, "assemble_singular_bm", ctx->aux_stream);
+        if (all4) {
+            RegularArgs r;
+            r.test = b.test;
+            r.trial = b.trial;
+            r.same_mesh = b.same_mesh;
+            r.family = b.family;
+            r.ops = NIHU_GB_SLP | NIHU_GB_DLP;
+            r.k = b.k;
+            r.k32 = b.k32;
+            r.alpha_re = 1.0;
+            r.alpha_im = 0.0;
+            r.alpha_re32 = 1.0f;
+            r.alpha_im32 = 0.0f;
+            r.unit_alpha = 1;
+            r.precision = b.precision;
+            r.dtype = b.dtype;
+            r.out_s = b.out_b;
+            r.out_d = b.out_a;
+            r.ld = b.ld;
+            r.j0 = b.j0;
+            r.j1 = b.j1;
+            r.accumulate = b.accumulate;
+            r.trial_size_max = b.trial_size_max;
+            e = launch_assemble_singular(r, *nl, ctx->d_flag, ctx->aux_stream);
+            BmArgs b2 = b;
+            b2.ops = NIHU_GB_DLPT | NIHU_GB_HSP;
+            b2.accumulate = 1;
+            if (e == cudaSuccess) e = launch_assemble_singular_bm(b2, *nl, ctx->aux_stream);
+        } else {
+            e = launch_assemble_singular_bm(b, *nl, ctx->aux_stream);
         }
-    cudaEvent_t computed[2], copied[2];
-    for (int b = 0; b < 2; ++b) {
-        cudaEventCreateWithFlags(&computed[b], cudaEventDisableTiming);
-        cudaEventCreateWithFlags(&copied[b], cudaEventDisableTiming);
     }
-    void *outs[2] = {out_slp, out_dlp};
-    cudaError_t e = cudaSuccess;
-    int b = 0;
-    bool used[2] = {false, false};
-    for (int64_t j0 = 0; j0 < N && e == cudaSuccess && st == NIHU_GB_OK; j0 += P, b ^= 1) {
-        const int64_t j1 = std::min(N, j0 + P);
-        if (used[b]) e = cudaStreamWaitEvent(ctx->stream, copied[b], 0);
-        for (int o = 0; o < 2 && e == cudaSuccess; ++o) {
-            if (!buf[b][o] || !accumulate) continue;
-            e = cudaMemcpy2DAsync(buf[b][o], col_bytes, (char *)outs[o] + j0 * ld * es, ld * es, col_bytes, j1 - j0,
-                                  cudaMemcpyHostToDevice, ctx->stream);
-        }
-        if (e != cudaSuccess) break;
-        a.out_s = buf[b][0];
-        a.out_d = buf[b][1];
-        a.ld = M;
-        a.j0 = (int)j0;
-        a.j1 = (int)j1;
-        st = assemble_panel(ctx, a, nl);
-        if (st) break;
-        e = cudaEventRecord(computed[b], ctx->stream);
-        if (e == cudaSuccess) e = cudaStreamWaitEvent(ctx->copy_stream, computed[b], 0);
-        for (int o = 0; o < 2 && e == cudaSuccess; ++o) {
-            if (!buf[b][o]) continue;
-            e = cudaMemcpy2DAsync((char *)outs[o] + j0 * ld * es, ld * es, buf[b][o], col_bytes, col_bytes, j1 - j0,
-                                  cudaMemcpyDeviceToHost, ctx->copy_stream);
-        }
-        if (e == cudaSuccess) e = cudaEventRecord(copied[b], ctx->copy_stream);
-        used[b] = true;
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "assemble_singular_bm launch");
+    if ((e = cudaEventRecord(ctx->ev_join, ctx->aux_stream)) != cudaSuccess) return cuda_fail(ctx, e, "join");
+    {
+        Phase ph(ctx, "assemble_regular_bm");
+        e = launch_assemble_regular_bm(b, ctx->stream);
     }
-    cudaError_t e2 = cudaStreamSynchronize(ctx->copy_stream);
-    cudaError_t e3 = cudaStreamSynchronize(ctx->stream);
-    for (int q = 0; q < 2; ++q) {
-        cudaEventDestroy(computed[q]);
-        cudaEventDestroy(copied[q]);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "assemble_regular_bm launch");
+    if ((e = cudaStreamWaitEvent(ctx->stream, ctx->ev_join, 0)) != cudaSuccess) return cuda_fail(ctx, e, "join");
+    ctx->launches += all4 ? 3 : 2;
+    return NIHU_GB_OK;
+}
+
+// checks shared by the Burton-Miller entry points
+nihu_gb_status bm_check(nihu_gb_ctx *ctx, const char *fn, const nihu_gb_mesh *test, const nihu_gb_mesh *trial,
+                        int family, double k, int precision, int dtype, int where, int64_t ld)
+{
+    const std::string f(fn);
+    if (!test || !trial || test->ctx != ctx || trial->ctx != ctx)
+        return fail(ctx, NIHU_GB_ERR_INVALID_ARGUMENT, f + ": meshes must belong to the context");
+    if (family != NIHU_GB_HELMHOLTZ_3D && family != NIHU_GB_LAPLACE_3D)
+        return fail(ctx, NIHU_GB_ERR_INVALID_ARGUMENT, f + ": unknown kernel family");
+    if (!valid_dtype(dtype) || !valid_where(where) || (precision != 0 && precision != 1))
+        return fail(ctx, NIHU_GB_ERR_INVALID_ARGUMENT, f + ": bad dtype, precision or location");
+    if (ld < std::max<int64_t>(test->n, 1)) return fail(ctx, NIHU_GB_ERR_INVALID_ARGUMENT, f + ": ld < rows");
+    if (!std::isfinite(k)) return fail(ctx, NIHU_GB_ERR_INVALID_ARGUMENT, f + ": non-finite wave number");
+    if (trial->dm.has_quad)
+        return fail(ctx, NIHU_GB_ERR_INVALID_ARGUMENT, f + ": DLPt / HSP: constant triangle trial elements only");
+    return NIHU_GB_OK;
+}
+
+BmArgs bm_args(const nihu_gb_mesh *test, const nihu_gb_mesh *trial, int family, int ops, double k, const double c[8],
+               int precision, int dtype, int accumulate)
+{
+    BmArgs b;
+    b.test = test->dm;
+    b.trial = trial->dm;
+    b.same_mesh = test == trial;
+    b.family = family;
+    b.ops = ops;
+    b.k = family == NIHU_GB_HELMHOLTZ_3D ? k : 0.0;
+    b.k32 = (float)b.k;
+    for (int o = 0; o < 4; ++o) {
+        b.cre[o] = c[2 * o];
+        b.cim[o] = c[2 * o + 1];
+        b.cre32[o] = (float)c[2 * o];
+        b.cim32[o] = (float)c[2 * o + 1];
     }
+    b.precision = precision;
+    b.dtype = dtype;
+    b.accumulate = accumulate ? 1 : 0;
+    b.trial_size_max = trial->size_max;
+    return b;
+}
+
+// all columns of the operators in b.ops into out_a / out_b (device or host)
+nihu_gb_status assemble_bm_all(nihu_gb_ctx *ctx, BmArgs b, NearList *nl, void *out_a, void *out_b, int64_t ld,
+                               int where, int64_t M, int64_t N)
+{
+    if (where == NIHU_GB_DEVICE) {
+        b.out_a = out_a;
+        b.out_b = out_b;
+        b.ld = ld;
+        b.j0 = 0;
+        b.j1 = (int)N;
+        nihu_gb_status st = assemble_panel_bm(ctx, b, nl);
+        if (st) return st;
+        return check_flag(ctx);
+    }
+    return assemble_host_panels(ctx, M, N, b.dtype, out_a, out_b, ld, b.accumulate,
+                                [&](void *o0, void *o1, int64_t pld, int j0, int j1) {
+                                    b.out_a = o0;
+                                    b.out_b = o1;
+                                    b.ld = pld;
+                                    b.j0 = j0;
+                                    b.j1 = j1;
+                                    return assemble_panel_bm(ctx, b, nl);
+                                });
+}
+
+}  // namespace
+
+extern "C" {
+
+nihu_gb_status nihu_gb_assemble_bm(nihu_gb_ctx *ctx, const nihu_gb_mesh *test, const nihu_gb_mesh *trial, int family,
+                                   int ops, double k, double alpha_re, double alpha_im, int precision, int dtype,
+                                   void *out_dlpt, void *out_hsp, int64_t ld, int accumulate, int where)
+{
+    if (!ctx) return NIHU_GB_ERR_INVALID_ARGUMENT;
+    nihu_gb_status st = bm_check(ctx, "nihu_gb_assemble_bm", test, trial, family, k, precision, dtype, where, ld);
     if (st) return st;
-    if (e != cudaSuccess) return cuda_fail(ctx, e, "panel assembly");
-    if (e2 != cudaSuccess) return cuda_fail(ctx, e2, "panel copy");
-    if (e3 != cudaSuccess) return cuda_fail(ctx, e3, "panel compute");
-    return check_flag(ctx);
+    if (ops < NIHU_GB_DLPT || (ops & ~(NIHU_GB_DLPT | NIHU_GB_HSP)))
+        return fail(ctx, NIHU_GB_ERR_INVALID_ARGUMENT, "nihu_gb_assemble_bm: ops must be DLPt, HSP or both");
+    if (((ops & NIHU_GB_DLPT) && !out_dlpt) || ((ops & NIHU_GB_HSP) && !out_hsp))
+        return fail(ctx, NIHU_GB_ERR_INVALID_ARGUMENT, "nihu_gb_assemble_bm: missing output buffer");
+    if (!std::isfinite(alpha_re) || !std::isfinite(alpha_im))
+        return fail(ctx, NIHU_GB_ERR_INVALID_ARGUMENT, "nihu_gb_assemble_bm: non-finite scale");
+    if (test->n == 0 || trial->n == 0) return NIHU_GB_OK;
+    cudaSetDevice(ctx->device);
+    NearList *nl = nullptr;
+    if ((st = get_near(ctx, test, trial, &nl))) return st;
+    const double c[8] = {0, 0, 0, 0, alpha_re, alpha_im, alpha_re, alpha_im};
+    BmArgs b = bm_args(test, trial, family, ops, k, c, precision, dtype, accumulate);
+    return assemble_bm_all(ctx, b, nl, (ops & NIHU_GB_HSP) ? out_hsp : nullptr,
+                           (ops & NIHU_GB_DLPT) ? out_dlpt : nullptr, ld, where, test->n, trial->n);
+}
+
+nihu_gb_status nihu_gb_assemble_burton_miller(nihu_gb_ctx *ctx, const nihu_gb_mesh *mesh, int family, double k,
+                                              double coupling_re, double coupling_im, int precision, int dtype,
+                                              void *out_a, void *out_b, int64_t ld, int where)
+{
+    if (!ctx) return NIHU_GB_ERR_INVALID_ARGUMENT;
+    nihu_gb_status st =
+        bm_check(ctx, "nihu_gb_assemble_burton_miller", mesh, mesh, family, k, precision, dtype, where, ld);
+    if (st) return st;
+    if (!out_a || !out_b) return fail(ctx, NIHU_GB_ERR_INVALID_ARGUMENT, "nihu_gb_assemble_burton_miller: missing output buffer");
+    if (!std::isfinite(coupling_re) || !std::isfinite(coupling_im))
+        return fail(ctx, NIHU_GB_ERR_INVALID_ARGUMENT, "nihu_gb_assemble_burton_miller: non-finite coupling");
+    const int64_t n = mesh->n;
+    if (n == 0) return NIHU_GB_OK;
+    cudaSetDevice(ctx->device);
+    NearList *nl = nullptr;
+    if ((st = get_near(ctx, mesh, mesh, &nl))) return st;
+    const double c[8] = {1, 0, 1, 0, coupling_re, coupling_im, coupling_re, coupling_im};
+    BmArgs b = bm_args(mesh, mesh, family, BM_ALL, k, c, precision, dtype, 0);
+    if (where == NIHU_GB_DEVICE) {
+        if ((st = assemble_bm_all(ctx, b, nl, out_a, out_b, ld, where, n, n))) return st;
+        // A -= I/2, B += c/2 I (helmholtz_3d_coll.cpp:71-72, 91)
+        CK(launch_add_identity((int)n, -0.5, 0.0, dtype, out_a, ld, ctx->stream));
+        CK(launch_add_identity((int)n, coupling_re / 2.0, coupling_im / 2.0, dtype, out_b, ld, ctx->stream));
+        ctx->launches += 2;
+        return sync(ctx);
+    }
+    if ((st = assemble_bm_all(ctx, b, nl, out_a, out_b, ld, where, n, n))) return st;
+    if ((st = nihu_gb_add_identity(ctx, mesh, -0.5, 0.0, dtype, out_a, ld, NIHU_GB_HOST))) return st;
+    return nihu_gb_add_identity(ctx, mesh, coupling_re / 2.0, coupling_im / 2.0, dtype, out_b, ld, NIHU_GB_HOST);
 }
 
 nihu_gb_status nihu_gb_add_identity(nihu_gb_ctx *ctx, const nihu_gb_mesh *mesh, double alpha_re, double alpha_im,
@@ -979,6 +1181,48 @@ nihu_gb_status nihu_gb_lu_solve(nihu_gb_ctx *ctx, void *A, int64_t n, int64_t ld
 
 // --------------------------------------------------------- composite solve
 
+}  // extern "C"
+
+namespace {
+
+// rhs = G q, then solve Hm p = rhs by GMRES (solver 0) or LU (solver 1) and
+// copy p to the host (the common tail of the composite solves)
+nihu_gb_status solve_tail(nihu_gb_ctx *ctx, int64_t n, int dtype, void *G, void *Hm, void *dq, void *drhs, void *dp,
+                          void *p, int solver, int restart, int max_iters, double tol, int *iters, double *rel_residual)
+{
+    nihu_gb_status st;
+    int splits = gemv_splits(n, n, dtype);
+    void *part;
+    if ((st = scratch(ctx, "mv_part", 16 * (size_t)splits * n, &part))) return st;
+    CK(timed_gemv(ctx, dtype, G, n, n, n, (const double2 *)dq, (double2 *)drhs, 1.0, 0.0, 0.0, 0.0, (double2 *)part, splits));
+    if (solver == 0) {
+        CK(cudaMemsetAsync(dp, 0, 16 * n, ctx->stream));
+        st = gmres_device(ctx, dtype, Hm, n, n, (const double2 *)drhs, (double2 *)dp, std::min<int64_t>(restart, n),
+                          max_iters, tol, iters, rel_residual);
+        if (st && st != NIHU_GB_ERR_NOT_CONVERGED) return st;
+    } else {
+        void *ppiv;
+        if ((st = scratch(ctx, "lu_piv", sizeof(int) * n, &ppiv))) return st;
+        CK(cudaMemsetAsync(ctx->d_flag + 1, 0, sizeof(int), ctx->stream));
+        CK(launch_lu_factor((double2 *)Hm, n, n, (int *)ppiv, ctx->d_flag + 1, &ctx->launches, ctx->stream));
+        CK(launch_lu_solve((const double2 *)Hm, n, n, (const int *)ppiv, (const double2 *)drhs, (double2 *)dp, ctx->stream));
+        ctx->launches += 1;
+        if (iters) *iters = 1;
+        if (rel_residual) *rel_residual = 0.0;
+        st = NIHU_GB_OK;
+    }
+    nihu_gb_status keep = st;
+    std::string msg = ctx->err;
+    CK(cudaMemcpyAsync(p, dp, 16 * n, cudaMemcpyDeviceToHost, ctx->stream));
+    if ((st = sync(ctx))) return st;
+    ctx->err = msg;
+    return keep;
+}
+
+}  // namespace
+
+extern "C" {
+
 nihu_gb_status nihu_gb_solve_cbie(nihu_gb_ctx *ctx, const nihu_gb_mesh *mesh, int family, double k, int precision,
                                   int dtype, const void *q, void *p, int solver, int restart, int max_iters,
                                   double tol, int *iters, double *rel_residual)
@@ -1003,31 +1247,33 @@ nihu_gb_status nihu_gb_solve_cbie(nihu_gb_ctx *ctx, const nihu_gb_mesh *mesh, in
     if (st) return st;
     CK(launch_add_identity((int)n, -0.5, 0.0, dtype, Hm, n, ctx->stream));
     ctx->launches += 1;
-    int splits = gemv_splits(n, n, dtype);
-    void *part;
-    if ((st = scratch(ctx, "mv_part", 16 * (size_t)splits * n, &part))) return st;
-    CK(timed_gemv(ctx, dtype, G, n, n, n, (const double2 *)dq, (double2 *)drhs, 1.0, 0.0, 0.0, 0.0, (double2 *)part, splits));
-    if (solver == 0) {
-        CK(cudaMemsetAsync(dp, 0, 16 * n, ctx->stream));
-        st = gmres_device(ctx, dtype, Hm, n, n, (const double2 *)drhs, (double2 *)dp, std::min<int64_t>(restart, n),
-                          max_iters, tol, iters, rel_residual);
-        if (st && st != NIHU_GB_ERR_NOT_CONVERGED) return st;
-    } else {
-        void *ppiv;
-        if ((st = scratch(ctx, "lu_piv", sizeof(int) * n, &ppiv))) return st;
-        CK(cudaMemsetAsync(ctx->d_flag + 1, 0, sizeof(int), ctx->stream));
-        CK(launch_lu_factor((double2 *)Hm, n, n, (int *)ppiv, ctx->d_flag + 1, &ctx->launches, ctx->stream));
-        CK(launch_lu_solve((const double2 *)Hm, n, n, (const int *)ppiv, (const double2 *)drhs, (double2 *)dp, ctx->stream));
-        ctx->launches += 1;
-        if (iters) *iters = 1;
-        if (rel_residual) *rel_residual = 0.0;
-    }
-    nihu_gb_status keep = st;
-    std::string msg = ctx->err;
-    CK(cudaMemcpyAsync(p, dp, 16 * n, cudaMemcpyDeviceToHost, ctx->stream));
-    if ((st = sync(ctx))) return st;
-    ctx->err = msg;
-    return keep;
+    return solve_tail(ctx, n, dtype, G, Hm, dq, drhs, dp, p, solver, restart, max_iters, tol, iters, rel_residual);
+}
+
+nihu_gb_status nihu_gb_solve_burton_miller(nihu_gb_ctx *ctx, const nihu_gb_mesh *mesh, int family, double k,
+                                           double coupling_re, double coupling_im, int precision, int dtype,
+                                           const void *q, void *p, int solver, int restart, int max_iters, double tol,
+                                           int *iters, double *rel_residual)
+{
+    if (!ctx) return NIHU_GB_ERR_INVALID_ARGUMENT;
+    if (!mesh || !q || !p || (solver != 0 && solver != 1) || (solver == 1 && dtype != NIHU_GB_C128) || !valid_dtype(dtype))
+        return fail(ctx, NIHU_GB_ERR_INVALID_ARGUMENT, "nihu_gb_solve_burton_miller: bad argument");
+    const int64_t n = mesh->n;
+    if (n == 0) return NIHU_GB_OK;
+    cudaSetDevice(ctx->device);
+    const size_t es = elem_bytes(dtype);
+    nihu_gb_status st;
+    void *A, *B, *dq, *drhs, *dp;
+    if ((st = scratch(ctx, "cbie_G", es * n * n, &B))) return st;
+    if ((st = scratch(ctx, "cbie_H", es * n * n, &A))) return st;
+    if ((st = scratch(ctx, "cbie_q", 16 * n, &dq))) return st;
+    if ((st = scratch(ctx, "cbie_rhs", 16 * n, &drhs))) return st;
+    if ((st = scratch(ctx, "cbie_p", 16 * n, &dp))) return st;
+    CK(cudaMemcpyAsync(dq, q, 16 * n, cudaMemcpyHostToDevice, ctx->stream));
+    st = nihu_gb_assemble_burton_miller(ctx, mesh, family, k, coupling_re, coupling_im, precision, dtype, A, B, n,
+                                        NIHU_GB_DEVICE);
+    if (st) return st;
+    return solve_tail(ctx, n, dtype, B, A, dq, drhs, dp, p, solver, restart, max_iters, tol, iters, rel_residual);
 }
 
 }  // extern "C"

@@ -16,6 +16,8 @@ constexpr int FAM_HELMHOLTZ = 0;
 constexpr int FAM_LAPLACE = 1;
 constexpr int OP_SLP = 1;
 constexpr int OP_DLP = 2;
+constexpr int OP_DLPT = 4;  // transposed DLP (normal derivative at the collocation point)
+constexpr int OP_HSP = 8;   // hypersingular operator
 
 // Quadrature levels of the regular path.  Level l of a trial element uses the
 // rule of degree C + 2l' where C is the field complexity and 2l' the distance
@@ -31,6 +33,9 @@ __host__ __device__ constexpr int level_slot0(int l) { return l == 0 ? 0 : (l ==
 constexpr double T_NEAR = 1.5;
 constexpr double T_S1 = 18.0 / 10.0, T_S0 = 91.0 / 10.0;
 constexpr double T_D1 = 28.0 / 10.0, T_D0 = 158.0 / 10.0;
+// HSP (1/r^3 far field): degree 6 / 4 / 2 below 1.9 / 3.6 / 22.3, else 0
+// (nihu/library/distance_kernel_intervals.hpp:117-154 for the 1/r^3 kernels)
+constexpr double T_H2 = 19.0 / 10.0, T_H1 = 36.0 / 10.0, T_H0 = 223.0 / 10.0;
 
 // Per-element device records of a mesh (structure of arrays).
 struct DevMesh {
@@ -61,6 +66,15 @@ __host__ __device__ inline int level_npts(int trial_nc, int test_c, int level)
     if (trial_nc == 4) return level == 0 ? 1 : (level == 1 ? 4 : 9);
     if (test_c == 0) return level == 0 ? 1 : (level == 1 ? 3 : 6);
     return level == 0 ? 1 : (level == 1 ? 4 : 7);
+}
+
+// sin and cos of 2 pi t for any t: the period count is removed exactly
+// (t - rint(t) is exact in binary floating point), leaving |2 pi f| <= pi for
+// the hardware approximation (absolute error about 4e-7 there)
+__device__ __forceinline__ void sincos_2pi(float t, float &s, float &c)
+{
+    float f = t - rintf(t);
+    __sincosf(6.28318530717958647692f * f, &s, &c);
 }
 
 struct cd { double re, im; };

@@ -87,6 +87,33 @@ cudaError_t launch_assemble_singular(const RegularArgs &a, const NearList &near,
 // by launch_assemble_singular itself, except inside a stream capture)
 cudaError_t prepare_singular_batch(cudaStream_t s);
 
+// assemble_bm.cu ----------------------------------------------------------
+// Burton-Miller operators on constant triangle trial elements.  `ops` is
+// OP_DLPT and/or OP_HSP, or all four operators (the fused system):
+//   out_a = c[1] DLP + c[3] HSP,  out_b = c[0] SLP + c[2] DLPt
+// restricted to the operators in ops (complex coefficients c = cre + i cim).
+struct BmArgs {
+    DevMesh test, trial;
+    int same_mesh = 0;
+    int family = 0, ops = 0;
+    double k = 0.0;
+    float k32 = 0.0f;
+    double cre[4] = {0, 0, 0, 0}, cim[4] = {0, 0, 0, 0};
+    float cre32[4] = {0, 0, 0, 0}, cim32[4] = {0, 0, 0, 0};
+    int precision = 0;  // regular entries: 0 FP32, 1 FP64
+    int dtype = 0;      // 0 c64, 1 c128
+    void *out_a = nullptr, *out_b = nullptr;  // column j at out + (j - j0) * ld
+    int64_t ld = 0;
+    int j0 = 0, j1 = 0;
+    int accumulate = 0;
+    double trial_size_max = 0.0;
+};
+// regular pairs of columns [j0, j1) (all operators in ops)
+cudaError_t launch_assemble_regular_bm(const BmArgs &a, cudaStream_t s);
+// nearly singular pairs and self terms of the DLPt and HSP operators only
+// (the SLP and DLP ones of the fused system come from launch_assemble_singular)
+cudaError_t launch_assemble_singular_bm(const BmArgs &a, const NearList &near, cudaStream_t s);
+
 // linalg.cu ---------------------------------------------------------------
 cudaError_t launch_add_identity(int n, double are, double aim, int dtype, void *out, int64_t ld, cudaStream_t s);
 
