@@ -52,10 +52,11 @@ def parse():
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-solve", action="store_true")
     p.add_argument("--no-cpu", action="store_true")
-    p.add_argument("--config", default="large", choices=["large", "small", "multirhs", "sweep", "serve"],
+    p.add_argument("--config", default="large", choices=["large", "small", "multirhs", "sweep", "serve", "bm"],
                    help="large: the headline line (20480-triangle icosphere); multirhs: the 40000-quad "
                         "cylinder with 64 plane waves; sweep: 256 wave numbers on three icospheres; serve: "
-                        "the served stream (each a separate line)")
+                        "the served stream; bm: the Burton-Miller system on the 20480-triangle icosphere "
+                        "(each a separate line)")
     p.add_argument("--requests", type=int, default=1000, help="serve: requests in the stream")
     p.add_argument("--quantum", type=int, default=8, help="serve: GMRES steps per system per round")
     p.add_argument("--plain-sample", type=int, default=4, help="serve: requests per mesh timed on the plain path")
@@ -844,6 +845,176 @@ def run_serve(args):
     print(json.dumps(out), flush=True)
 
 
+def run_bm(args):
+    """Burton-Miller system on the headline mesh (icosphere s=5, 20480
+    triangles, Helmholtz, k = 5, coupling -i/k): one step assembles
+    A = DLP - I/2 + c HSP and B = SLP + c DLPt + c/2 I (complex64, all four
+    kernels per quadrature point, FP64 nearly singular and self terms) into
+    device memory.  Metric: system entries per second (A and B counted
+    separately).  Also the GMRES solve A p = B q (pulsating sphere), the end to
+    end call with host buffers, and the FP64 oracle on a row sample of the
+    four operators as the CPU baseline."""
+    import torch
+
+    import nihu_gb300 as g
+    from nihu_gb300 import meshes
+    from nihu_gb300 import _capi as C
+
+    mesh = meshes.icosphere(SUBDIV)
+    nodes, elems = mesh
+    n = len(elems)
+    k = K_WAVE
+    c = g.burton_miller_coupling(k)
+    ctx = g.Context(0)
+    L = g.lib()
+    stream = torch.cuda.ExternalStream(ctx.stream)
+    dm = g.api.DeviceMesh(ctx, nodes, elems)
+    mat_bytes = n * n * 8
+    pa_, pb_ = ctypes.c_void_p(), ctypes.c_void_p()
+    ctx.check(L.nihu_gb_device_alloc(ctx.handle, mat_bytes, ctypes.byref(pa_)))
+    ctx.check(L.nihu_gb_device_alloc(ctx.handle, mat_bytes, ctypes.byref(pb_)))
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+
+    def step():
+        ctx.check(L.nihu_gb_assemble_burton_miller(ctx.handle, dm.handle, C.HELMHOLTZ_3D, k, c.real, c.imag,
+                                                   C.REGULAR_FP32, C.C64, pa_, pb_, n, C.DEVICE))
+
+    for _ in range(max(3, args.warmup)):
+        step()
+    counts = (ctypes.c_int64 * 11)()
+    ctx.check(L.nihu_gb_pair_statistics(ctx.handle, dm.handle, dm.handle, counts))
+    counts = np.array(list(counts))
+    n_regular = int(counts[2:].sum())
+    ctx.set_profiling(True)
+    ctx.profile_reset()
+    clocks = ClockSampler(0)
+    clocks.start()
+    launches0 = ctx.launch_count
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    torch.cuda.synchronize()
+    for s_ in range(args.steps):
+        flush.fill_(s_ & 0xFF)  # evict the previous step's lines from L2 (not timed)
+        torch.cuda.synchronize()
+        ev[s_][0].record(stream)
+        step()
+        ev[s_][1].record(stream)
+    torch.cuda.synchronize()
+    launches = ctx.launch_count - launches0
+    clk = clocks.stop()
+    prof = ctx.profile()
+    ctx.set_profiling(False)
+    ms = float(np.mean([a.elapsed_time(b) for a, b in ev]))
+    entries = 2.0 * n * n
+    reg_ms, reg_n = prof.get("assemble_regular_bm", (0.0, 0))
+    reg_avg = reg_ms / max(reg_n, 1)
+    alg_bytes = 16.0 * n_regular  # one complex64 entry of A and one of B written per regular pair
+    peak, peak_kind = measured_peaks()
+    achieved = alg_bytes / (reg_avg / 1e3) / 1e9
+    out = {
+        "metric": "Burton-Miller system entries/s", "impl": "ours", "value": entries / (ms / 1e3),
+        "unit": "entries/s", "n_gpus": 1, "steps": args.steps, "warmup": max(3, args.warmup), "ms_per_step": ms,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "fp32 regular quadrature and nearly singular dynamic parts, fp64 self terms and nearly singular static parts; complex64 storage",
+        "data": "synthetic (icosphere mesh generated in-process)",
+        "config": {"workload": "icosphere s=5 (%d flat constant triangles), Helmholtz 3D Burton-Miller system "
+                               "A = DLP - I/2 + c HSP, B = SLP + c DLPt + c/2 I, c = -i/k, k=5" % n,
+                   "n_elements": n, "entries_per_step": int(entries), "operator_entries_per_step": int(4 * n * n),
+                   "l2": "256 MB written between timed steps (L2 flushed); outputs 6.7 GB >> 129 MB L2"},
+        "gpu_launches": int(launches), "clocks": clk,
+        "roofline": {"kernel": "k_regular_bm (assemble_bm.cu)", "bound": "hbm", "achieved": achieved, "peak": peak,
+                     "unit": "GB/s", "frac": achieved / peak, "traffic": None,
+                     "peak_source": "%s (MEASURED_PEAKS.json hbm_gbs)" % peak_kind,
+                     "algorithmic_bytes_per_launch": alg_bytes, "avg_launch_ms": reg_avg,
+                     "regular_pairs": n_regular, "near_pairs": int(counts[1]), "self_pairs": int(counts[0])},
+        "phases": {kk: {"ms_per_step": v[0] / args.steps, "launches": v[1]} for kk, v in prof.items()},
+    }
+    # GMRES solve of A p = B q on the assembled matrices
+    q = np.ones(n, np.complex128)
+    dq, drhs, dp = ctypes.c_void_p(), ctypes.c_void_p(), ctypes.c_void_p()
+    for p_ in (dq, drhs, dp):
+        ctx.check(L.nihu_gb_device_alloc(ctx.handle, 16 * n, ctypes.byref(p_)))
+    ctx.check(L.nihu_gb_memcpy(ctx.handle, dq, C.DEVICE, q.ctypes.data, C.HOST, 16 * n))
+    ctx.check(L.nihu_gb_memcpy(ctx.handle, dp, C.DEVICE, np.zeros(n, np.complex128).ctypes.data, C.HOST, 16 * n))
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    ctx.check(L.nihu_gb_matvec(ctx.handle, C.C64, pb_, n, n, n, dq, drhs, 1.0, 0.0, 0.0, 0.0, C.DEVICE))
+    it, res = ctypes.c_int(0), ctypes.c_double(0.0)
+    st = L.nihu_gb_gmres(ctx.handle, C.C64, pa_, n, n, drhs, dp, 50, 1000, 1e-6, ctypes.byref(it), ctypes.byref(res),
+                         C.DEVICE)
+    torch.cuda.synchronize()
+    solve_ms = (time.perf_counter() - t0) * 1e3
+    p = np.zeros(n, np.complex128)
+    ctx.check(L.nihu_gb_memcpy(ctx.handle, p.ctypes.data, C.HOST, dp, C.DEVICE, 16 * n))
+    pa = -1.0 / (1 + 1j * k)
+    out["solve"] = {"solver": "GMRES(50), FP32 matvec, FP64 Arnoldi, tol 1e-6", "status": int(st),
+                    "iterations": it.value, "rel_residual": res.value, "ms": solve_ms,
+                    "pressure_error_vs_analytic": float(np.abs(p - pa).max() / abs(pa))}
+    for p_ in (dq, drhs, dp):
+        L.nihu_gb_device_free(ctx.handle, p_)
+    # end to end: mesh arrays in, both matrices out to pinned host memory
+    if not args.no_e2e:
+        ha, hb = ctypes.c_void_p(), ctypes.c_void_p()
+        ctx.check(L.nihu_gb_host_alloc(ctx.handle, mat_bytes, ctypes.byref(ha)))
+        ctx.check(L.nihu_gb_host_alloc(ctx.handle, mat_bytes, ctypes.byref(hb)))
+        e2e_steps = max(1, min(args.steps, 3))
+
+        def e2e_step():
+            m = ctypes.c_void_p()
+            ctx.check(L.nihu_gb_mesh_create(ctx.handle, nodes.ctypes.data, len(nodes), elems.ctypes.data, n,
+                                            elems.shape[1], ctypes.byref(m)))
+            ctx.check(L.nihu_gb_assemble_burton_miller(ctx.handle, m, C.HELMHOLTZ_3D, k, c.real, c.imag,
+                                                       C.REGULAR_FP32, C.C64, ha, hb, n, C.HOST))
+            L.nihu_gb_mesh_destroy(m)
+
+        e2e_step()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(e2e_steps):
+            e2e_step()
+        torch.cuda.synchronize()
+        e2e_ms = (time.perf_counter() - t0) * 1e3 / e2e_steps
+        out["e2e"] = {"value": entries / (e2e_ms / 1e3), "unit": "entries/s",
+                      "h2d_bytes_per_step": int(nodes.nbytes + elems.nbytes), "d2h_bytes_per_step": int(2 * mat_bytes),
+                      "ms_per_step": e2e_ms, "steps": e2e_steps,
+                      "path": "nihu_gb_mesh_create + nihu_gb_assemble_burton_miller(where=HOST, pinned)"}
+        L.nihu_gb_host_free(ha)
+        L.nihu_gb_host_free(hb)
+    L.nihu_gb_device_free(ctx.handle, pa_)
+    L.nihu_gb_device_free(ctx.handle, pb_)
+    dm.close()
+    ctx.close()
+    if not args.no_cpu:
+        # the FP64 oracle on a row sample of the four operators, all host cores
+        from oracle import oracle
+        oracle.build()
+        threads = os.cpu_count() or 1
+        t0 = time.perf_counter()
+        for op in (oracle.SLP, oracle.DLP, oracle.DLPT, oracle.HSP):
+            oracle.assemble(mesh, mesh, oracle.HELMHOLTZ, op, k, rows=(0, 1))
+        per_row = time.perf_counter() - t0
+        rows = int(max(threads, min(8192, args.cpu_seconds * threads / max(per_row, 1e-6))))
+        rows = max(threads, (rows // threads) * threads)
+        blocks = np.linspace(0, n, threads + 1).astype(int)
+        per = rows // threads
+
+        def work(b):
+            a = int(blocks[b])
+            for op in (oracle.SLP, oracle.DLP, oracle.DLPT, oracle.HSP):
+                oracle.assemble(mesh, mesh, oracle.HELMHOLTZ, op, k, rows=(a, min(n, a + per)))
+
+        t0 = time.perf_counter()
+        ts = [threading.Thread(target=work, args=(b,)) for b in range(threads)]
+        for t in ts:
+            t.start()
+        for t in ts:
+            t.join()
+        el = time.perf_counter() - t0
+        out["cpu_baseline"] = {"value": 2.0 * rows * n / el, "unit": "entries/s", "cores": threads, "kind": "port",
+                               "sample": "%d full rows x %d columns x (SLP, DLP, DLPt, HSP), FP64 oracle, %.1f s "
+                                         "(system entries: two operators per entry of A and of B)" % (rows, n, el)}
+    print(json.dumps(out), flush=True)
+
+
 def main():
     args = parse()
     if args.config == "multirhs":
@@ -857,6 +1028,9 @@ def main():
         return
     if args.config == "serve":
         run_serve(args)
+        return
+    if args.config == "bm":
+        run_bm(args)
         return
     if args.impl == "reference":
         run_reference(args)

@@ -685,48 +685,16 @@ namespace {
 constexpr int BM_ALL = NIHU_GB_SLP | NIHU_GB_DLP | NIHU_GB_DLPT | NIHU_GB_HSP;
 
 // Burton-Miller operators on one column panel: the FP64 nearly singular and
-// self kernels on the auxiliary stream beside the regular kernel (as
-// assemble_panel); the fused system takes its SLP and DLP near and self
-// entries from the plain singular kernel, then adds the DLPt and HSP ones
+// self kernel on the auxiliary stream beside the regular kernel (as
+// assemble_panel), each evaluating every operator of b.ops
 nihu_gb_status assemble_panel_bm(nihu_gb_ctx *ctx, const BmArgs &b, NearList *nl)
 {
-    const bool all4 = b.ops == BM_ALL;
     cudaError_t e = cudaEventRecord(ctx->ev_fork, ctx->stream);
     if (e == cudaSuccess) e = cudaStreamWaitEvent(ctx->aux_stream, ctx->ev_fork, 0);
     if (e != cudaSuccess) return cuda_fail(ctx, e, "fork");
     {
         Phase ph(ctx, "assemble_singular_bm", ctx->aux_stream);
-        if (all4) {
-            RegularArgs r;
-            r.test = b.test;
-            r.trial = b.trial;
-            r.same_mesh = b.same_mesh;
-            r.family = b.family;
-            r.ops = NIHU_GB_SLP | NIHU_GB_DLP;
-            r.k = b.k;
-            r.k32 = b.k32;
-            r.alpha_re = 1.0;
-            r.alpha_im = 0.0;
-            r.alpha_re32 = 1.0f;
-            r.alpha_im32 = 0.0f;
-            r.unit_alpha = 1;
-            r.precision = b.precision;
-            r.dtype = b.dtype;
-            r.out_s = b.out_b;
-            r.out_d = b.out_a;
-            r.ld = b.ld;
-            r.j0 = b.j0;
-            r.j1 = b.j1;
-            r.accumulate = b.accumulate;
-            r.trial_size_max = b.trial_size_max;
-            e = launch_assemble_singular(r, *nl, ctx->d_flag, ctx->aux_stream);
-            BmArgs b2 = b;
-            b2.ops = NIHU_GB_DLPT | NIHU_GB_HSP;
-            b2.accumulate = 1;
-            if (e == cudaSuccess) e = launch_assemble_singular_bm(b2, *nl, ctx->aux_stream);
-        } else {
-            e = launch_assemble_singular_bm(b, *nl, ctx->aux_stream);
-        }
+        e = launch_assemble_singular_bm(b, *nl, ctx->aux_stream);
     }
     if (e != cudaSuccess) return cuda_fail(ctx, e, "assemble_singular_bm launch");
     if ((e = cudaEventRecord(ctx->ev_join, ctx->aux_stream)) != cudaSuccess) return cuda_fail(ctx, e, "join");
@@ -736,7 +704,7 @@ nihu_gb_status assemble_panel_bm(nihu_gb_ctx *ctx, const BmArgs &b, NearList *nl
     }
     if (e != cudaSuccess) return cuda_fail(ctx, e, "assemble_regular_bm launch");
     if ((e = cudaStreamWaitEvent(ctx->stream, ctx->ev_join, 0)) != cudaSuccess) return cuda_fail(ctx, e, "join");
-    ctx->launches += all4 ? 3 : 2;
+    ctx->launches += 2;
     return NIHU_GB_OK;
 }
 

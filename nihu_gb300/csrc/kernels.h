@@ -110,8 +110,7 @@ struct BmArgs {
 };
 // regular pairs of columns [j0, j1) (all operators in ops)
 cudaError_t launch_assemble_regular_bm(const BmArgs &a, cudaStream_t s);
-// nearly singular pairs and self terms of the DLPt and HSP operators only
-// (the SLP and DLP ones of the fused system come from launch_assemble_singular)
+// nearly singular pairs and self terms of the operators in ops (FP64)
 cudaError_t launch_assemble_singular_bm(const BmArgs &a, const NearList &near, cudaStream_t s);
 
 // linalg.cu ---------------------------------------------------------------

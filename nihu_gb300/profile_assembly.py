@@ -2,7 +2,8 @@
 
     python -m nihu_gb300.profile_assembly --subdiv 5 --k 5 --budget-mb 1536
 
-assembles the Helmholtz SLP and DLP matrices of an icosphere.
+assembles the Helmholtz SLP and DLP matrices of an icosphere (with ``--bm``
+the two Burton-Miller system matrices instead).
 
     python -m nihu_gb300.profile_assembly --sweep 16 --subdiv 4
     python -m nihu_gb300.profile_assembly --sweep-config4
@@ -41,6 +42,8 @@ def main(argv=None):
     ap.add_argument("--budget-mb", type=int, default=0, help="HBM budget: host output in column panels")
     ap.add_argument("--reps", type=int, default=2)
     ap.add_argument("--fp64", action="store_true", help="FP64 regular quadrature")
+    ap.add_argument("--bm", action="store_true", help="the Burton-Miller system (nihu_gb_assemble_burton_miller, "
+                                                     "coupling -i/k) instead of SLP and DLP")
     ap.add_argument("--sweep", type=int, default=0, metavar="N", help="frequency sweep of N wave numbers")
     ap.add_argument("--sweep-config4", action="store_true", help="the 256-instance sweep on three icospheres")
     a = ap.parse_args(argv)
@@ -70,8 +73,13 @@ def main(argv=None):
     ctx.set_profiling(True)
     for r in range(a.reps):
         ctx.profile_reset()
-        ctx.check(L.nihu_gb_assemble(ctx.handle, dm.handle, dm.handle, fam, C.SLP | C.DLP, a.k, 1.0, 0.0, prec, C.C64,
-                                     ps, pd, n, 0, where))
+        if a.bm:
+            c = api.burton_miller_coupling(a.k) if fam == C.HELMHOLTZ_3D else 1.0 + 0.0j
+            ctx.check(L.nihu_gb_assemble_burton_miller(ctx.handle, dm.handle, fam, a.k, c.real, c.imag, prec, C.C64,
+                                                       pd, ps, n, where))
+        else:
+            ctx.check(L.nihu_gb_assemble(ctx.handle, dm.handle, dm.handle, fam, C.SLP | C.DLP, a.k, 1.0, 0.0, prec,
+                                         C.C64, ps, pd, n, 0, where))
     prof = ctx.profile()
     print(json.dumps({"n_elements": n, "where": "host panels" if a.budget_mb else "device",
                       "phases_ms": {k: round(v[0], 4) for k, v in prof.items()},

@@ -6,7 +6,9 @@ Tolerances (written here, on every entry of the matrix):
   * FP32 regular mode: the same ratio <= 1e-5
   * surface pressure of the Burton-Miller solve: <= 1e-4 of the FP64 oracle's
     dense solve of the same system
-Nearly singular and self entries are FP64 in both modes.
+Self entries and the static parts of nearly singular entries are FP64 in both
+modes; the dynamic part K_k - K_0 of a nearly singular entry is summed in FP32
+in FP32 mode (its size is (kr)^2 of the entry's).
 """
 import numpy as np
 import pytest
