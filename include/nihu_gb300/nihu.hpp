@@ -185,6 +185,14 @@ template <class WaveNumber = double>
 inline kernel_desc helmholtz_3d_DLP_kernel(WaveNumber k) { return {NIHU_GB_HELMHOLTZ_3D, NIHU_GB_DLP, (double)k}; }
 inline kernel_desc laplace_3d_SLP_kernel() { return {NIHU_GB_LAPLACE_3D, NIHU_GB_SLP, 0.0}; }
 inline kernel_desc laplace_3d_DLP_kernel() { return {NIHU_GB_LAPLACE_3D, NIHU_GB_DLP, 0.0}; }
+// Burton-Miller kernels (nihu/library/helmholtz_kernel.hpp:326-334): constant
+// triangle trial elements only
+template <class WaveNumber = double>
+inline kernel_desc helmholtz_3d_DLPt_kernel(WaveNumber k) { return {NIHU_GB_HELMHOLTZ_3D, NIHU_GB_DLPT, (double)k}; }
+template <class WaveNumber = double>
+inline kernel_desc helmholtz_3d_HSP_kernel(WaveNumber k) { return {NIHU_GB_HELMHOLTZ_3D, NIHU_GB_HSP, (double)k}; }
+inline kernel_desc laplace_3d_DLPt_kernel() { return {NIHU_GB_LAPLACE_3D, NIHU_GB_DLPT, 0.0}; }
+inline kernel_desc laplace_3d_HSP_kernel() { return {NIHU_GB_LAPLACE_3D, NIHU_GB_HSP, 0.0}; }
 
 // ------------------------------------------------------------- operators
 
@@ -276,11 +284,20 @@ Res &operator<<(Res &result, weighted_residual<TS> const &wr)
     context &ctx = *wr.ctx;
     nihu_gb_mesh *tmh = tm.on(ctx);
     nihu_gb_mesh *rmh = (&tm == &rm) ? tmh : rm.on(ctx);
-    void *out_s = op.kernel.op == NIHU_GB_SLP ? (void *)result.data() : nullptr;
-    void *out_d = op.kernel.op == NIHU_GB_DLP ? (void *)result.data() : nullptr;
-    check(ctx.handle(), nihu_gb_assemble(ctx.handle(), tmh, rmh, op.kernel.family, op.kernel.op, op.kernel.k,
-                                         op.scale.real(), op.scale.imag(), wr.precision, detail::storage<T>::dtype,
-                                         out_s, out_d, m, 1, NIHU_GB_HOST));
+    const int kop = op.kernel.op;
+    if (kop == NIHU_GB_SLP || kop == NIHU_GB_DLP) {
+        void *out_s = kop == NIHU_GB_SLP ? (void *)result.data() : nullptr;
+        void *out_d = kop == NIHU_GB_DLP ? (void *)result.data() : nullptr;
+        check(ctx.handle(), nihu_gb_assemble(ctx.handle(), tmh, rmh, op.kernel.family, kop, op.kernel.k,
+                                             op.scale.real(), op.scale.imag(), wr.precision, detail::storage<T>::dtype,
+                                             out_s, out_d, m, 1, NIHU_GB_HOST));
+    } else {
+        void *out_t = kop == NIHU_GB_DLPT ? (void *)result.data() : nullptr;
+        void *out_h = kop == NIHU_GB_HSP ? (void *)result.data() : nullptr;
+        check(ctx.handle(), nihu_gb_assemble_bm(ctx.handle(), tmh, rmh, op.kernel.family, kop, op.kernel.k,
+                                                op.scale.real(), op.scale.imag(), wr.precision,
+                                                detail::storage<T>::dtype, out_t, out_h, m, 1, NIHU_GB_HOST));
+    }
     return result;
 }
 

@@ -5,7 +5,9 @@
 //
 // usage: test_shim <mesh.bin> <k> <out.bin>
 //   mesh.bin: int64 n_nodes, int64 n_elems, n_nodes*3 doubles, n_elems*5 int32
-//   out.bin : Ls, Ms (n*n complex128 each, column-major), p (n complex128)
+//   out.bin : Ls, Ms (n*n complex128 each, column-major), p (n complex128),
+//             then the Burton-Miller matrices Gs, Hs and pressure p_bm of
+//             nihu/applications/helmholtz/helmholtz_3d_coll.cpp:36-120 (BM defined)
 #include <cstdio>
 #include <cstdlib>
 #include <fstream>
@@ -76,10 +78,29 @@ int main(int argc, char **argv)
             return 1;
         }
 
+        // Burton-Miller: Gs << G + alpha Ht + alpha/2 I, Hs << alpha D - I/2 + H, alpha = -i/k
+        const C alpha(0.0, -1.0 / k);
+        auto Htop = create_integral_operator(helmholtz_3d_DLPt_kernel<double>(k));
+        auto Dop = create_integral_operator(helmholtz_3d_HSP_kernel<double>(k));
+        dense_matrix<C> Gs(n, n), Hs(n, n);
+        Gs << dirac(surf_sp) * Lop[surf_sp];
+        Gs << dirac(surf_sp) * (alpha * Htop)[surf_sp];
+        Gs << dirac(surf_sp) * (alpha / 2. * I)[surf_sp];
+        Hs << dirac(surf_sp) * (alpha * Dop)[surf_sp];
+        Hs << dirac(surf_sp) * (-.5 * I)[surf_sp];
+        Hs << dirac(surf_sp) * Mop[surf_sp];
+        std::vector<C> rhs_bm((size_t)n, 0.0);
+        for (int64_t j = 0; j < n; ++j)
+            for (int64_t i = 0; i < n; ++i) rhs_bm[(size_t)i] += Gs(i, j) * q[(size_t)j];
+        std::vector<C> p_bm = gmres(Hs, rhs_bm, 1e-10, 50, 1000);
+
         std::ofstream out(argv[3], std::ios::binary);
         out.write((const char *)Ls.data(), n * n * 16);
         out.write((const char *)Ms.data(), n * n * 16);
         out.write((const char *)p.data(), n * 16);
+        out.write((const char *)Gs.data(), n * n * 16);
+        out.write((const char *)Hs.data(), n * n * 16);
+        out.write((const char *)p_bm.data(), n * 16);
         C pa = -1.0 / (1.0 + C(0.0, k));
         double err = 0.0;
         for (auto v : p) err = std::max(err, std::abs(v - pa) / std::abs(pa));

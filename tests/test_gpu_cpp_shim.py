@@ -43,7 +43,11 @@ def test_shim_acoustic_bem_sequence(tmp_path, oracle):
     raw = np.fromfile(out_bin, dtype=np.complex128)
     Ls = raw[:n * n].reshape(n, n, order="F")
     Ms = raw[n * n:2 * n * n].reshape(n, n, order="F")
-    p = raw[2 * n * n:]
+    p = raw[2 * n * n:2 * n * n + n]
+    o = 2 * n * n + n
+    Gs = raw[o:o + n * n].reshape(n, n, order="F")
+    Hs = raw[o + n * n:o + 2 * n * n].reshape(n, n, order="F")
+    p_bm = raw[o + 2 * n * n:]
     mesh = (nodes, elems)
     L = oracle.assemble(mesh, mesh, oracle.HELMHOLTZ, oracle.SLP, k, threads=8)
     M = oracle.assemble(mesh, mesh, oracle.HELMHOLTZ, oracle.DLP, k, threads=8) - 0.5 * np.eye(n)
@@ -51,3 +55,13 @@ def test_shim_acoustic_bem_sequence(tmp_path, oracle):
     assert np.abs(Ms - M).max() / np.abs(M).max() < 1e-5
     p_ref = np.linalg.solve(M, L @ np.ones(n))
     assert np.abs(p - p_ref).max() / np.abs(p_ref).max() < 1e-4
+    # the Burton-Miller branch of the same application
+    c = -1j / k
+    D = oracle.assemble(mesh, mesh, oracle.HELMHOLTZ, oracle.HSP, k, threads=8)
+    Ht = oracle.assemble(mesh, mesh, oracle.HELMHOLTZ, oracle.DLPT, k, threads=8)
+    G_ref = L + c * Ht + 0.5 * c * np.eye(n)
+    H_ref = M + c * D
+    assert np.abs(Gs - G_ref).max() / np.abs(G_ref).max() < 1e-5
+    assert np.abs(Hs - H_ref).max() / np.abs(H_ref).max() < 1e-5
+    p_bm_ref = np.linalg.solve(H_ref, G_ref @ np.ones(n))
+    assert np.abs(p_bm - p_bm_ref).max() / np.abs(p_bm_ref).max() < 1e-4
