@@ -195,6 +195,28 @@ nihu_gb_status nihu_gb_assemble_burton_miller(nihu_gb_ctx *ctx, const nihu_gb_me
                                               double coupling_re, double coupling_im, int precision, int dtype,
                                               void *out_a, void *out_b, int64_t ld, int where);
 
+/* Entries of an explicit list of element pairs (test rows[p], trial cols[p]),
+ * each with the full singular check of the dense path (self, nearly singular
+ * d/D < 1.5, regular by the interval tables): the near-field (P2P) matrix of
+ * a fast multipole or hierarchical solver, in sparse triplet form.  For every
+ * p (row / column indices int32):
+ *     out_a[p] = c_DLP DLP + c_HSP HSP (+ ident_a if test == trial and rows[p] == cols[p])
+ *     out_b[p] = c_SLP SLP + c_DLPt DLPt (+ ident_b likewise)
+ * over the operators in `ops` (mask of NIHU_GB_SLP / DLP / DLPT / HSP).
+ * coef = {re, im} x (SLP, DLP, DLPt, HSP) (NULL: all 1); ident = {re, im} x
+ * (a, b) (NULL: no identity).  out_a is needed when ops has DLP or HSP, out_b
+ * when it has SLP or DLPt (dtype complex64 / complex128, n_pairs values).
+ * where: NIHU_GB_HOST (pairs and outputs in host memory) or NIHU_GB_DEVICE.
+ * DLPt / HSP need constant triangle trial elements.  An index out of range
+ * gives NIHU_GB_ERR_INVALID_ARGUMENT.
+ * Replaces: nihu/fmm/p2p_integral.hpp:87-99 evaluated over the P2P list by
+ * nihu/fmm/p2p_precompute.hpp:110-180 (the Burton-Miller FMM solver's
+ * lhs/rhs near fields, nihu/fmm/helmholtz_burton_miller_solver.hpp:170-190). */
+nihu_gb_status nihu_gb_assemble_pairs(nihu_gb_ctx *ctx, const nihu_gb_mesh *test, const nihu_gb_mesh *trial,
+                                      int family, int ops, double k, const double *coef, const double *ident,
+                                      int precision, int dtype, int64_t n_pairs, const int32_t *rows,
+                                      const int32_t *cols, void *out_a, void *out_b, int where);
+
 /* Per-pair quadrature statistics of an assembly (no matrix is written):
  * counts[0] self pairs, counts[1] nearly singular pairs, counts[2 + 3*s + d]
  * regular pairs whose SLP uses level s and DLP level d (levels 0, 1, 2 =

@@ -7,7 +7,7 @@ is the Python front end with the same shape.
 """
 from ._capi import (C64, C128, DEVICE, DLP, DLPT, HSP, GEMM_BF16X9, GEMM_FP32, GEMM_TF32, HELMHOLTZ_3D, HOST, LAPLACE_3D, QUAD_1, REGULAR_FP32, REGULAR_FP64, SLP,
                     TRIA_1, InvalidArgumentError, NihuError, NotConvergedError, OutOfRangeError, lib)
-from .api import (Context, DeviceMesh, Mesh, Server, SweepPlan, assemble_burton_miller, burton_miller_coupling,
+from .api import (Context, DeviceMesh, Mesh, Server, SweepPlan, assemble_burton_miller, assemble_pairs, burton_miller_coupling,
                   constant_view, create_integral_operator, create_mesh, default_context,
                   dirac, gemm, gmres, helmholtz_3d_DLP_kernel, helmholtz_3d_DLPt_kernel, helmholtz_3d_HSP_kernel,
                   helmholtz_3d_SLP_kernel, identity_integral_operator, laplace_3d_DLP_kernel, laplace_3d_DLPt_kernel,
@@ -22,5 +22,5 @@ __all__ = [
     "gmres", "helmholtz_3d_DLP_kernel", "helmholtz_3d_SLP_kernel", "identity_integral_operator",
     "laplace_3d_DLP_kernel", "laplace_3d_SLP_kernel", "lu_solve", "matvec", "pair_statistics", "solve_cbie", "meshes",
     "DLPT", "HSP", "helmholtz_3d_DLPt_kernel", "helmholtz_3d_HSP_kernel", "laplace_3d_DLPt_kernel", "laplace_3d_HSP_kernel",
-    "assemble_burton_miller", "burton_miller_coupling", "solve_burton_miller",
+    "assemble_burton_miller", "assemble_pairs", "burton_miller_coupling", "solve_burton_miller",
 ]

@@ -457,6 +457,39 @@ def solve_cbie(mesh: Mesh, k: float, q, family: int = C.HELMHOLTZ_3D, dtype: int
     return p, it.value, res.value
 
 
+def assemble_pairs(test: Mesh, trial: Mesh, rows, cols, ops: int, k: float = 0.0, family: int = C.HELMHOLTZ_3D,
+                   coef=None, ident=None, dtype: int = C.C128, precision: str = "fp32", ctx: Context | None = None):
+    """Entries of the element pairs (rows[p], cols[p]) with the full singular
+    check, as the FMM near field (nihu/fmm/p2p_precompute.hpp):
+    a[p] = c_DLP DLP + c_HSP HSP (+ ident[0] on self pairs),
+    b[p] = c_SLP SLP + c_DLPt DLPt (+ ident[1]).  coef: dict or 4-sequence of
+    complex scales for (SLP, DLP, DLPt, HSP) (default 1).  Returns (a, b), None
+    for an output the operators do not touch."""
+    ctx = ctx or default_context()
+    rows = np.ascontiguousarray(rows, dtype=np.int32)
+    cols = np.ascontiguousarray(cols, dtype=np.int32)
+    if rows.shape != cols.shape or rows.ndim != 1:
+        raise ValueError("rows and cols must be 1D arrays of one length")
+    if isinstance(coef, dict):
+        coef = [coef.get(op, 1.0) for op in (C.SLP, C.DLP, C.DLPT, C.HSP)]
+    c = None if coef is None else np.array([[complex(v).real, complex(v).imag] for v in coef], np.float64).ravel()
+    idn = None if ident is None else np.array([[complex(v).real, complex(v).imag] for v in ident], np.float64).ravel()
+    n = len(rows)
+    cdt = np.complex64 if dtype == C.C64 else np.complex128
+    need_a = bool(ops & (C.DLP | C.HSP))
+    need_b = bool(ops & (C.SLP | C.DLPT))
+    a = np.zeros(n, cdt) if need_a else None
+    b = np.zeros(n, cdt) if need_b else None
+    tdm = test.device(ctx)
+    rdm = tdm if trial is test else trial.device(ctx)
+    ctx.check(C.lib().nihu_gb_assemble_pairs(
+        ctx.handle, tdm.handle, rdm.handle, family, ops, k, None if c is None else c.ctypes.data,
+        None if idn is None else idn.ctypes.data, C.REGULAR_FP64 if precision == "fp64" else C.REGULAR_FP32, dtype,
+        n, rows.ctypes.data, cols.ctypes.data, None if a is None else a.ctypes.data,
+        None if b is None else b.ctypes.data, C.HOST))
+    return a, b
+
+
 def burton_miller_coupling(k: float) -> complex:
     """The reference application's coupling constant -i/k
     (nihu/applications/helmholtz/helmholtz_3d_coll.cpp:44)."""

@@ -16,9 +16,10 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libnihu_gb300.so")
 SOURCES = ["mesh.cu", "classify.cu", "assemble_regular.cu", "assemble_singular.cu", "linalg.cu", "capi.cu",
-           "noalloc.cu", "multi.cu", "solve_persistent.cu", "assemble_bm.cu"]
+           "noalloc.cu", "multi.cu", "solve_persistent.cu", "assemble_bm.cu",
+           "assemble_pairs.cu"]
 HEADERS = ["common.cuh", "geom.cuh", "classify.cuh", "kernels.h", "linalg.h", "quad_rules.h", "solve_persistent.h",
-           "planar.cuh"]
+           "planar.cuh", "singular_schemes.cuh", "bm_schemes.cuh"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2"]
 

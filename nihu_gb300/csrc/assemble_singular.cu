@@ -30,159 +30,11 @@
 #include <cmath>
 
 #include "kernels.h"
-#include "planar.cuh"
+#include "singular_schemes.cuh"
 
 namespace nihu {
 
 constexpr int SING_THREADS = 128;
-// G(r) and dG/dr of the Helmholtz kernel sharing one sincos and 1/r:
-//   G = e^{-ikr}/(4 pi r), dG/dr = -(1 + ikr) e^{-ikr}/(4 pi r^2)
-__device__ __forceinline__ void helm_g_dg(double k, double r, double rinv, cd &g, cd &dg)
-{
-    double s, c;
-    sincos_bounded(k * r, &s, &c, false);
-    double a = rinv * INV_FOUR_PI;
-    g = {c * a, -s * a};
-    double b = a * rinv, kr = k * r;
-    dg = {-(c + kr * s) * b, -(kr * c - s) * b};
-}
-
-// kernel values times the Jacobian at a point y with (unnormalised) normal n:
-// SLP = G J, DLP = dG/dr (r.n)/r (n = N/J, so the J cancels)
-__device__ __forceinline__ void kern_point(int fam, double k, const double x0[3], const double y[3], const double n[3],
-                                           double J, bool do_s, bool do_d, cd &ks, cd &kd)
-{
-    double rv0 = y[0] - x0[0], rv1 = y[1] - x0[1], rv2 = y[2] - x0[2];
-    double r2 = rv0 * rv0 + rv1 * rv1 + rv2 * rv2;
-    double rinv = rsqrt(r2);
-    double r = r2 * rinv;
-    double rn = (rv0 * n[0] + rv1 * n[1] + rv2 * n[2]) * rinv;  // (r.N)/r = J (r.n)/r
-    if (fam == FAM_LAPLACE) {
-        double a = rinv * INV_FOUR_PI;
-        if (do_s) ks = {a * J, 0.0};
-        if (do_d) kd = {-a * rinv * rn, 0.0};
-        return;
-    }
-    cd g, dg;
-    helm_g_dg(k, r, rinv, g, dg);
-    if (do_s) ks = cscale(g, J);
-    if (do_d) kd = cscale(dg, rn);
-}
-
-__device__ __forceinline__ void kern_on_elem(const Elem64 &e, int fam, double k, const double x0[3], double xi,
-                                             double eta, bool do_s, bool do_d, cd &ks, cd &kd)
-{
-    double y[3], n[3];
-    ex(e, xi, eta, y);
-    enormal(e, xi, eta, n);
-    kern_point(fam, k, x0, y, n, norm3(n), do_s, do_d, ks, kd);
-}
-
-// ------------------------------------------------------------------ planar
-
-// static (Laplace) nearly singular part over a flat element: radial integral
-// analytic, angular integral with 6 Gauss points per side
-// (nihu/library/laplace_nearly_singular_integrals.hpp:62-209); adds the SLP and
-// DLP (real) results to a.sr / a.dr
-__device__ void near_static(const Elem64 &e, const double x0[3], bool do_s, bool do_d, Acc &a)
-{
-    double loc[4][2], z;
-    plane_local(e, x0, loc, z);
-    const int N = e.nc;
-    double tl[4], t0[4], dr[4];
-    for (int s = 0; s < N; ++s) side_geometry(loc[s], loc[(s + 1) % N], tl[s], t0[s], dr[s], false);
-    const double az = fabs(z), z2 = z * z;
-    double s_sum = 0.0, d_sum = 0.0;
-    for (int s = 0; s < N; ++s) {
-        double t1 = tl[s], t2 = tl[(s + 1) % N];
-        wrap_limits(t1, t2);
-        const double jac = (t2 - t1) / 2.0;
-        for (int q = 0; q < 6; ++q) {
-            double xi, w;
-            gauss_pt(6, q, xi, w);
-            double th = t1 * (1.0 - xi) / 2.0 + t2 * (1.0 + xi) / 2.0;
-            double R = dr[s] / cos_angle(th - t0[s]);
-            double r2 = R * R + z2;
-            double rinv = rsqrt(r2);
-            double jw = jac * w;
-            if (do_s) s_sum += (r2 * rinv - az) * jw;  // r - |z|
-            if (do_d) d_sum += (1.0 - az * rinv) * jw;  // 1 - |z|/r
-        }
-    }
-    const double sg = (0.0 < z) - (z < 0.0);
-    a.sr += s_sum * INV_FOUR_PI;
-    a.dr += sg * d_sum * INV_FOUR_PI;
-}
-
-// dynamic part (K_k - K_0) of the planar nearly singular scheme with the
-// degree-14 rule (42-point Dunavant on triangles, 8x8 Gauss on quads)
-__device__ void near_dynamic(const Elem64 &e, double k, const double x0[3], bool do_s, bool do_d, Acc &a,
-                             const Pt4 *__restrict__ pts42, bool short_series)
-{
-    double en[3];
-    {
-        double xi, eta;
-        domain_center(e.nc, xi, eta);
-        enormal(e, xi, eta, en);
-        double nn = 1.0 / norm3(en);
-        for (int d = 0; d < 3; ++d) en[d] *= nn;
-    }
-    const int np = e.nc == 3 ? 42 : 64;
-    for (int p = 0; p < np; ++p) {
-        double xi, eta, w, J;
-        double y[3];
-        if (pts42) {
-            // precomputed per triangle: (y, w J) of the 42-point rule
-            const Pt4 v = pts42[p];
-            y[0] = v.x; y[1] = v.y; y[2] = v.z;
-            w = v.w;
-            J = 1.0;
-        } else if (e.nc == 3) {
-            double e1[3], e2[3], nt[3];
-            for (int d = 0; d < 3; ++d) { e1[d] = e.c[1][d] - e.c[0][d]; e2[d] = e.c[2][d] - e.c[0][d]; }
-            cross3(e1, e2, nt);
-            tri_pt(14, p, xi, eta, w);
-            for (int d = 0; d < 3; ++d) y[d] = e.c[0][d] + xi * e1[d] + eta * e2[d];
-            J = norm3(nt);
-        } else {
-            double w0, w1, n[3];
-            gauss_pt(8, p / 8, xi, w0);
-            gauss_pt(8, p % 8, eta, w1);
-            w = w0 * w1;
-            ex(e, xi, eta, y);
-            enormal(e, xi, eta, n);
-            J = norm3(n);
-        }
-        double rv0 = y[0] - x0[0], rv1 = y[1] - x0[1], rv2 = y[2] - x0[2];
-        double r2 = rv0 * rv0 + rv1 * rv1 + rv2 * rv2;
-        double rinv = rsqrt(r2);
-        double kr = k * (r2 * rinv);
-        double sn, cs;
-        sincos_bounded(kr, &sn, &cs, short_series);
-        // t = w J / (4 pi r); e^{-ikr} = cs - i sn
-        //   SLP: (G_k - G_0) w J = t (cs - 1 - i sn)
-        //   DLP: (dG_k - dG_0)/dr (r.n)/r w J = -t/r (r.n)/r ((cs + kr sn - 1) + i (kr cs - sn))
-        const double t = w * J * rinv * INV_FOUR_PI;
-        if (do_s) {
-            a.sr += t * (cs - 1.0);
-            a.si -= t * sn;
-        }
-        if (do_d) {
-            double u = t * rinv * ((rv0 * en[0] + rv1 * en[1] + rv2 * en[2]) * rinv);
-            a.dr -= u * (cs + kr * sn - 1.0);
-            a.di -= u * (kr * cs - sn);
-        }
-    }
-}
-
-// full planar constant-element nearly singular integral
-__device__ void near_plane(const Elem64 &e, int fam, double k, const double x0[3], bool do_s, bool do_d, Acc &a,
-                           const Pt4 *__restrict__ pts42 = nullptr, bool short_series = false)
-{
-    if (fam == FAM_HELMHOLTZ) near_dynamic(e, k, x0, do_s, do_d, a, pts42, short_series);
-    near_static(e, x0, do_s, do_d, a);
-}
-
 // ------------------------------------------------ frequency-batch moments
 //
 // With W_p = w_p J_p / (4 pi) and x = k r_p, the 42-point dynamic sums of a
@@ -329,181 +181,6 @@ __device__ __forceinline__ void near_series(int J, double k, const double *mS, c
     }
 }
 
-// ------------------------------------------------------------ inverse mapping
-
-// Newton iteration (nihu/core/inverse_mapping.hpp:52-112).  Records the first
-// iterate with |f| < 1e-5 (polar scheme) and with |f| < 1e-6 (Telles); both
-// come from the same iteration sequence the reference runs separately.
-__device__ bool inverse_mapping(const Elem64 &e, const double x0[3], bool need6, double r5[3], double r6[3])
-{
-    double res[3] = {0.0, 0.0, 0.0};
-    bool got5 = false;
-    double dxe[3] = {0, 0, 0};
-    if (e.nc == 4)
-        for (int d = 0; d < 3; ++d) dxe[d] = (e.c[0][d] - e.c[1][d] + e.c[2][d] - e.c[3][d]) * 0.25;
-    for (int it = 0; it < 100; ++it) {
-        double dxi[3], deta[3], n[3], y[3];
-        ex(e, res[0], res[1], y);
-        edx(e, res[0], res[1], dxi, deta);
-        cross3(dxi, deta, n);
-        double sq = sqrt(norm3(n));
-        for (int d = 0; d < 3; ++d) n[d] /= sq;
-        double f[3];
-        for (int d = 0; d < 3; ++d) f[d] = y[d] + n[d] * res[2] - x0[d];
-        double err = norm3(f);
-        if (!got5 && err < 1e-5) {
-            got5 = true;
-            for (int d = 0; d < 3; ++d) r5[d] = res[d];
-            if (!need6) return true;
-        }
-        if (need6 && err < 1e-6) {
-            for (int d = 0; d < 3; ++d) r6[d] = res[d];
-            return got5;
-        }
-        // d n / d xi = (x_xixi x x_eta + x_xi x x_xieta) / sq, x_xixi = x_etaeta = 0
-        double t2[3], dnxi[3], dneta[3];
-        cross3(dxi, dxe, t2);
-        for (int d = 0; d < 3; ++d) dnxi[d] = t2[d] / sq;
-        cross3(dxe, deta, t2);
-        for (int d = 0; d < 3; ++d) dneta[d] = t2[d] / sq;
-        double M[3][4];
-        for (int d = 0; d < 3; ++d) {
-            M[d][0] = dxi[d] + dnxi[d] * res[2];
-            M[d][1] = deta[d] + dneta[d] * res[2];
-            M[d][2] = n[d];
-            M[d][3] = f[d];
-        }
-        for (int c = 0; c < 3; ++c) {
-            int p = c;
-            for (int r = c + 1; r < 3; ++r)
-                if (fabs(M[r][c]) > fabs(M[p][c])) p = r;
-            if (p != c)
-                for (int q = 0; q < 4; ++q) { double t = M[c][q]; M[c][q] = M[p][q]; M[p][q] = t; }
-            for (int r = c + 1; r < 3; ++r) {
-                double fct = M[r][c] / M[c][c];
-                for (int q = c; q < 4; ++q) M[r][q] -= fct * M[c][q];
-            }
-        }
-        double s[3];
-        for (int r = 2; r >= 0; --r) {
-            double v = M[r][3];
-            for (int q = r + 1; q < 3; ++q) v -= M[r][q] * s[q];
-            s[r] = v / M[r][r];
-        }
-        for (int d = 0; d < 3; ++d) res[d] -= s[d];
-    }
-    return false;
-}
-
-__device__ void linearized(const Elem64 &e, double xi0, double eta0, Elem64 &lin)
-{
-    double x0[3], dxi[3], deta[3];
-    ex(e, xi0, eta0, x0);
-    edx(e, xi0, eta0, dxi, deta);
-    lin.nc = e.nc;
-    for (int a = 0; a < 4; ++a) {
-        double ci, ce;
-        domain_corner(e.nc, a < e.nc ? a : e.nc - 1, ci, ce);
-        for (int d = 0; d < 3; ++d) lin.c[a][d] = x0[d] + dxi[d] * (ci - xi0) + deta[d] * (ce - eta0);
-    }
-}
-
-// polar scheme around (xi0, eta0) with linearized-element subtraction
-__device__ void near_polar_sum(const Elem64 &e, const Elem64 &lin, int fam, double k, const double x0[3], double xi0,
-                               double eta0, bool do_s, bool do_d, Acc &a)
-{
-    const int N = e.nc;
-    double tl[4], t0[4], dr[4];
-    for (int n = 0; n < N; ++n) {
-        double c1[2], c2[2];
-        domain_corner(N, n, c1[0], c1[1]);
-        domain_corner(N, (n + 1) % N, c2[0], c2[1]);
-        c1[0] -= xi0; c1[1] -= eta0;
-        c2[0] -= xi0; c2[1] -= eta0;
-        side_geometry(c1, c2, tl[n], t0[n], dr[n], true);
-    }
-    // the linearized element is affine: one normal for all points
-    double ln[3];
-    enormal(lin, xi0, eta0, ln);
-    const double lJ = norm3(ln);
-    for (int n = 0; n < N; ++n) {
-        double t1 = tl[n], t2 = tl[(n + 1) % N];
-        wrap_limits(t1, t2);
-        if (fabs(t2 - t1) < 1e-3) continue;
-        for (int ia = 0; ia < 8; ++ia) {
-            double xx, wa;
-            gauss_pt(8, ia, xx, wa);
-            double th = ((1.0 - xx) * t1 + (1.0 + xx) * t2) / 2.0;
-            double wth = wa * (t2 - t1) / 2.0;
-            double cth, sth;
-            sincos(th, &sth, &cth);
-            double rho_lim = dr[n] / cos_angle(th - t0[n]);
-            for (int ib = 0; ib < 8; ++ib) {
-                double xr, wb;
-                gauss_pt(8, ib, xr, wb);
-                double rho = (1.0 + xr) * rho_lim / 2.0;
-                double wrho = wb * rho_lim / 2.0;
-                double xi = xi0 + rho * cth, eta = eta0 + rho * sth;
-                cd fs{0, 0}, fd{0, 0}, ls{0, 0}, ld{0, 0};
-                kern_on_elem(e, fam, k, x0, xi, eta, do_s, do_d, fs, fd);
-                double yl[3];
-                ex(lin, xi, eta, yl);
-                kern_point(fam, k, x0, yl, ln, lJ, do_s, do_d, ls, ld);
-                double wt = wth * wrho * rho;
-                a.sr += wt * (fs.re - ls.re);
-                a.si += wt * (fs.im - ls.im);
-                a.dr += wt * (fd.re - ld.re);
-                a.di += wt * (fd.im - ld.im);
-            }
-        }
-    }
-}
-
-// Telles-transformed 16x16 Gauss rule (DLP only)
-__device__ void near_telles_sum(const Elem64 &e, int fam, double k, const double x0[3], const double im[3], Acc &a)
-{
-    double dist = im[2];
-    double rb;
-    if (dist < 0.05) rb = 0.0;
-    else if (dist <= 1.3) rb = 0.85 + 0.24 * log(dist);
-    else if (dist <= 3.618) rb = 0.893 + 0.0832 * log(dist);
-    else rb = 1.0;
-    double ca[2], cb[2], cc[2], cdd[2];
-    for (int dim = 0; dim < 2; ++dim) {
-        double eb = im[dim];
-        double f = 1.0 + 2.0 * rb;
-        double q = 1.0 / (2.0 * f) * ((eb * (3.0 - 2.0 * rb) - 2.0 * eb * eb * eb / f) * 1.0 / f - eb);
-        double p = 1.0 / (3.0 * f * f) * (4.0 * rb * (1.0 - rb) + 3.0 * (1.0 - eb * eb));
-        double s = sqrt(q * q + p * p * p);
-        double gb = cbrt(-q + s) + cbrt(-q - s) + eb / f;
-        double Q = 1.0 + 3.0 * gb * gb;
-        ca[dim] = (1.0 - rb) / Q;
-        cb[dim] = -3.0 * (1.0 - rb) * gb / Q;
-        cc[dim] = (3.0 * gb * gb + rb) / Q;
-        cdd[dim] = -cb[dim];
-    }
-    double tv[16], tw[16];  // transformed eta nodes and Jacobians (second dimension)
-    for (int b = 0; b < 16; ++b) {
-        double x, w;
-        gauss_pt(16, b, x, w);
-        tv[b] = ca[1] * x * x * x + cb[1] * x * x + cc[1] * x + cdd[1];
-        tw[b] = w * (3.0 * ca[1] * x * x + 2.0 * cb[1] * x + cc[1]);
-    }
-    for (int ia = 0; ia < 16; ++ia) {
-        double x, w;
-        gauss_pt(16, ia, x, w);
-        double t0 = ca[0] * x * x * x + cb[0] * x * x + cc[0] * x + cdd[0];
-        double w0 = w * (3.0 * ca[0] * x * x + 2.0 * cb[0] * x + cc[0]);
-        for (int ib = 0; ib < 16; ++ib) {
-            cd ks{0, 0}, kd{0, 0};
-            kern_on_elem(e, fam, k, x0, t0, tv[ib], false, true, ks, kd);
-            double wt = w0 * tw[ib];
-            a.dr += kd.re * wt;
-            a.di += kd.im * wt;
-        }
-    }
-}
-
 // -------------------------------------------------------------------- self
 
 // (e^{-ikr} - 1) / (4 pi r) over a flat triangle with the 13-point degree-7
@@ -577,38 +254,6 @@ __device__ void self_tria(const Elem64 &e, int fam, double k, const double x0[3]
     a.sr += (st + dr) * INV_FOUR_PI;
     a.si += di * INV_FOUR_PI;
     // DLP of a flat triangle over itself is zero
-}
-
-__device__ void self_quad(const Elem64 &e, int fam, double k, const double x0[3], bool do_s, bool do_d, Acc &a)
-{
-    for (int d = 0; d < 4; ++d) {
-        double P2[2], P3[2];
-        domain_corner(4, d, P2[0], P2[1]);
-        domain_corner(4, (d + 1) % 4, P3[0], P3[1]);
-        for (int ia = 0; ia < 4; ++ia)
-            for (int ib = 0; ib < 4; ++ib) {
-                double u, wu, v, wv;
-                gauss_pt(4, ia, u, wu);
-                gauss_pt(4, ib, v, wv);
-                // corners P0 = P1 = (0,0) (the collocation point), P2, P3
-                double N[4], dN[4][2];
-                shape(4, u, v, N);
-                dshape(4, u, v, dN);
-                double xi = N[2] * P2[0] + N[3] * P3[0];
-                double eta = N[2] * P2[1] + N[3] * P3[1];
-                double j00 = dN[2][0] * P2[0] + dN[3][0] * P3[0];
-                double j01 = dN[2][0] * P2[1] + dN[3][0] * P3[1];
-                double j10 = dN[2][1] * P2[0] + dN[3][1] * P3[0];
-                double j11 = dN[2][1] * P2[1] + dN[3][1] * P3[1];
-                double wd = wu * wv * (j00 * j11 - j01 * j10);
-                cd ks{0, 0}, kd{0, 0};
-                kern_on_elem(e, fam, k, x0, xi, eta, do_s, do_d, ks, kd);
-                a.sr += ks.re * wd;
-                a.si += ks.im * wd;
-                a.dr += kd.re * wd;
-                a.di += kd.im * wd;
-            }
-    }
 }
 
 // ------------------------------------------------------------------ driver

@@ -833,6 +833,100 @@ nihu_gb_status nihu_gb_assemble_burton_miller(nihu_gb_ctx *ctx, const nihu_gb_me
     return nihu_gb_add_identity(ctx, mesh, coupling_re / 2.0, coupling_im / 2.0, dtype, out_b, ld, NIHU_GB_HOST);
 }
 
+nihu_gb_status nihu_gb_assemble_pairs(nihu_gb_ctx *ctx, const nihu_gb_mesh *test, const nihu_gb_mesh *trial, int family,
+                                      int ops, double k, const double *coef, const double *ident, int precision,
+                                      int dtype, int64_t n_pairs, const int32_t *rows, const int32_t *cols,
+                                      void *out_a, void *out_b, int where)
+{
+    if (!ctx) return NIHU_GB_ERR_INVALID_ARGUMENT;
+    const char *fn = "nihu_gb_assemble_pairs";
+    if (!test || !trial || test->ctx != ctx || trial->ctx != ctx)
+        return fail(ctx, NIHU_GB_ERR_INVALID_ARGUMENT, std::string(fn) + ": meshes must belong to the context");
+    if (family != NIHU_GB_HELMHOLTZ_3D && family != NIHU_GB_LAPLACE_3D)
+        return fail(ctx, NIHU_GB_ERR_INVALID_ARGUMENT, std::string(fn) + ": unknown kernel family");
+    if (ops < 1 || ops > BM_ALL)
+        return fail(ctx, NIHU_GB_ERR_INVALID_ARGUMENT, std::string(fn) + ": ops must be a mask of SLP, DLP, DLPt, HSP");
+    const bool need_a = (ops & (NIHU_GB_DLP | NIHU_GB_HSP)) != 0, need_b = (ops & (NIHU_GB_SLP | NIHU_GB_DLPT)) != 0;
+    if (n_pairs < 0 || (n_pairs > 0 && (!rows || !cols || (need_a && !out_a) || (need_b && !out_b))))
+        return fail(ctx, NIHU_GB_ERR_INVALID_ARGUMENT, std::string(fn) + ": missing pair or output array");
+    if (!valid_dtype(dtype) || !valid_where(where) || (precision != 0 && precision != 1) || !std::isfinite(k))
+        return fail(ctx, NIHU_GB_ERR_INVALID_ARGUMENT, std::string(fn) + ": bad dtype, precision, location or wave number");
+    if ((ops & (NIHU_GB_DLPT | NIHU_GB_HSP)) && trial->dm.has_quad)
+        return fail(ctx, NIHU_GB_ERR_INVALID_ARGUMENT, std::string(fn) + ": DLPt / HSP: constant triangle trial elements only");
+    if (n_pairs == 0) return NIHU_GB_OK;
+    if (where == NIHU_GB_HOST) {
+        for (int64_t p = 0; p < n_pairs; ++p)
+            if (rows[p] < 0 || rows[p] >= test->n || cols[p] < 0 || cols[p] >= trial->n)
+                return fail(ctx, NIHU_GB_ERR_INVALID_ARGUMENT,
+                            std::string(fn) + ": pair " + std::to_string(p) + " has an index out of range");
+    }
+    cudaSetDevice(ctx->device);
+    nihu_gb_status st;
+    PairArgs a;
+    a.test = test->dm;
+    a.trial = trial->dm;
+    a.same_mesh = test == trial;
+    a.family = family;
+    a.ops = ops;
+    a.k = family == NIHU_GB_HELMHOLTZ_3D ? k : 0.0;
+    a.k32 = (float)a.k;
+    for (int o = 0; o < 4; ++o) {
+        a.cre[o] = coef ? coef[2 * o] : 1.0;
+        a.cim[o] = coef ? coef[2 * o + 1] : 0.0;
+    }
+    for (int o = 0; o < 2; ++o) {
+        a.id_re[o] = ident ? ident[2 * o] : 0.0;
+        a.id_im[o] = ident ? ident[2 * o + 1] : 0.0;
+    }
+    a.precision = precision;
+    a.dtype = dtype;
+    a.n = n_pairs;
+    a.trial_size_max = trial->size_max;
+    const size_t es = elem_bytes(dtype);
+    void *sing, *flags;
+    if ((st = scratch(ctx, "pairs_sing", sizeof(int64_t) * n_pairs, &sing))) return st;
+    if ((st = scratch(ctx, "pairs_flags", 16, &flags))) return st;
+    a.sing = (int64_t *)sing;
+    a.n_sing = (unsigned long long *)flags;
+    a.bad = (int *)((char *)flags + 8);
+    a.err = ctx->d_flag;
+    CK(cudaMemsetAsync(a.bad, 0, sizeof(int), ctx->stream));
+    if (where == NIHU_GB_DEVICE) {
+        a.rows = rows;
+        a.cols = cols;
+        a.out_a = need_a ? out_a : nullptr;
+        a.out_b = need_b ? out_b : nullptr;
+    } else {
+        void *dr, *dc, *da = nullptr, *db = nullptr;
+        if ((st = scratch(ctx, "pairs_rows", sizeof(int32_t) * n_pairs, &dr))) return st;
+        if ((st = scratch(ctx, "pairs_cols", sizeof(int32_t) * n_pairs, &dc))) return st;
+        if (need_a && (st = scratch(ctx, "pairs_out_a", es * n_pairs, &da))) return st;
+        if (need_b && (st = scratch(ctx, "pairs_out_b", es * n_pairs, &db))) return st;
+        CK(cudaMemcpyAsync(dr, rows, sizeof(int32_t) * n_pairs, cudaMemcpyHostToDevice, ctx->stream));
+        CK(cudaMemcpyAsync(dc, cols, sizeof(int32_t) * n_pairs, cudaMemcpyHostToDevice, ctx->stream));
+        a.rows = (const int32_t *)dr;
+        a.cols = (const int32_t *)dc;
+        a.out_a = da;
+        a.out_b = db;
+    }
+    {
+        Phase ph(ctx, "assemble_pairs");
+        CK(launch_assemble_pairs(a, ctx->stream));
+    }
+    ctx->launches += 2;
+    if (where == NIHU_GB_HOST) {
+        if (need_a) CK(cudaMemcpyAsync(out_a, a.out_a, es * n_pairs, cudaMemcpyDeviceToHost, ctx->stream));
+        if (need_b) CK(cudaMemcpyAsync(out_b, a.out_b, es * n_pairs, cudaMemcpyDeviceToHost, ctx->stream));
+    }
+    int bad = 0;
+    CK(cudaMemcpyAsync(&bad, a.bad, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    if ((st = check_flag(ctx))) return st;  // synchronises; inverse-mapping failures
+    if (bad)
+        return fail(ctx, NIHU_GB_ERR_INVALID_ARGUMENT,
+                    std::string(fn) + ": pair " + std::to_string(bad - 1) + " has an index out of range");
+    return NIHU_GB_OK;
+}
+
 nihu_gb_status nihu_gb_add_identity(nihu_gb_ctx *ctx, const nihu_gb_mesh *mesh, double alpha_re, double alpha_im,
                                     int dtype, void *out, int64_t ld, int where)
 {

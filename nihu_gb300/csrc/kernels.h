@@ -113,6 +113,33 @@ cudaError_t launch_assemble_regular_bm(const BmArgs &a, cudaStream_t s);
 // nearly singular pairs and self terms of the operators in ops (FP64)
 cudaError_t launch_assemble_singular_bm(const BmArgs &a, const NearList &near, cudaStream_t s);
 
+// assemble_pairs.cu -------------------------------------------------------
+// Entries of an explicit pair list (rows[p], cols[p]), p < n, each with the
+// full self / nearly singular / regular dispatch:
+//   out_a[p] = c[1] DLP + c[3] HSP (+ id[0] on a self pair)
+//   out_b[p] = c[0] SLP + c[2] DLPt (+ id[1] on a self pair)
+// for the operators in ops.  sing / n_sing: device scratch for the compacted
+// self and nearly singular pairs (n entries); bad receives 1 + the first pair
+// with an index out of range, err 1 + the first failed inverse mapping.
+struct PairArgs {
+    DevMesh test, trial;
+    int same_mesh = 0;
+    int family = 0, ops = 0;
+    double k = 0.0;
+    float k32 = 0.0f;
+    double cre[4] = {0, 0, 0, 0}, cim[4] = {0, 0, 0, 0};
+    double id_re[2] = {0, 0}, id_im[2] = {0, 0};
+    int precision = 0, dtype = 0;
+    int64_t n = 0;
+    const int32_t *rows = nullptr, *cols = nullptr;
+    void *out_a = nullptr, *out_b = nullptr;
+    int64_t *sing = nullptr;
+    unsigned long long *n_sing = nullptr;
+    int *bad = nullptr, *err = nullptr;
+    double trial_size_max = 0.0;
+};
+cudaError_t launch_assemble_pairs(const PairArgs &a, cudaStream_t s);
+
 // linalg.cu ---------------------------------------------------------------
 cudaError_t launch_add_identity(int n, double are, double aim, int dtype, void *out, int64_t ld, cudaStream_t s);
 
