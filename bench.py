@@ -52,10 +52,11 @@ def parse():
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-solve", action="store_true")
     p.add_argument("--no-cpu", action="store_true")
-    p.add_argument("--config", default="large", choices=["large", "small", "multirhs", "sweep", "serve", "bm"],
+    p.add_argument("--config", default="large", choices=["large", "small", "multirhs", "sweep", "serve", "bm", "p2p"],
                    help="large: the headline line (20480-triangle icosphere); multirhs: the 40000-quad "
                         "cylinder with 64 plane waves; sweep: 256 wave numbers on three icospheres; serve: "
-                        "the served stream; bm: the Burton-Miller system on the 20480-triangle icosphere "
+                        "the served stream; bm: the Burton-Miller system on the 20480-triangle icosphere; "
+                        "p2p: the Burton-Miller near field of a box partition of the same mesh "
                         "(each a separate line)")
     p.add_argument("--requests", type=int, default=1000, help="serve: requests in the stream")
     p.add_argument("--quantum", type=int, default=8, help="serve: GMRES steps per system per round")
@@ -1015,6 +1016,173 @@ def run_bm(args):
     print(json.dumps(out), flush=True)
 
 
+def box_near_field(centres, h):
+    """P2P list of a uniform box partition with leaf size h: every pair of
+    elements in the same or a neighbouring leaf box (as an FMM's leaf-level
+    near field); rows sorted by box."""
+    key = np.floor((centres + 1.0001) / h).astype(np.int64)
+    nb = int(key.max()) + 2
+    code = (key[:, 0] * nb + key[:, 1]) * nb + key[:, 2]
+    order = np.argsort(code, kind="stable")
+    codes, starts, counts = np.unique(code[order], return_index=True, return_counts=True)
+    where = {int(c): (int(s0), int(cn)) for c, s0, cn in zip(codes, starts, counts)}
+    rows, cols = [], []
+    offs = [(dx * nb + dy) * nb + dz for dx in (-1, 0, 1) for dy in (-1, 0, 1) for dz in (-1, 0, 1)]
+    for c, (s0, cn) in where.items():
+        mine = order[s0:s0 + cn]
+        for o in offs:
+            hit = where.get(c + o)
+            if hit is None:
+                continue
+            other = order[hit[0]:hit[0] + hit[1]]
+            rows.append(np.repeat(mine, len(other)))
+            cols.append(np.tile(other, len(mine)))
+    return np.concatenate(rows).astype(np.int32), np.concatenate(cols).astype(np.int32)
+
+
+def run_p2p(args):
+    """Near field of a box partition (the P2P part of NiHu's Burton-Miller FMM
+    solver, nihu/fmm/helmholtz_burton_miller_solver.hpp:170-190) on the
+    20480-triangle icosphere, k = 5: leaf boxes of 0.125, every pair of
+    elements in the same or a neighbouring box, each evaluated with the full
+    singular check into the two near-field operators
+    a = DLP + alpha HSP - I/2 and b = SLP + alpha DLPt + alpha/2 I
+    (complex64, FP32 regular quadrature).  Metric: near-field entries per
+    second (a and b counted separately), pairs and outputs resident in HBM;
+    e2e with the pair list uploaded and both value arrays read back per step."""
+    import torch
+
+    import nihu_gb300 as g
+    from nihu_gb300 import meshes
+    from nihu_gb300 import _capi as C
+
+    mesh = meshes.icosphere(SUBDIV)
+    nodes, elems = mesh
+    n = len(elems)
+    k = K_WAVE
+    alpha = g.burton_miller_coupling(k)
+    cen = meshes.centroids_and_normals(nodes, elems)[0]
+    rows, cols = box_near_field(cen, 0.125)
+    npairs = len(rows)
+    coef = np.array([1.0, 0.0, 1.0, 0.0, alpha.real, alpha.imag, alpha.real, alpha.imag])
+    ident = np.array([-0.5, 0.0, alpha.real / 2, alpha.imag / 2])
+    ops = C.SLP | C.DLP | C.DLPT | C.HSP
+    ctx = g.Context(0)
+    L = g.lib()
+    stream = torch.cuda.ExternalStream(ctx.stream)
+    dm = g.api.DeviceMesh(ctx, nodes, elems)
+    ptr = {nm: ctypes.c_void_p() for nm in ("r", "c", "a", "b")}
+    for nm, size in (("r", 4 * npairs), ("c", 4 * npairs), ("a", 8 * npairs), ("b", 8 * npairs)):
+        ctx.check(L.nihu_gb_device_alloc(ctx.handle, size, ctypes.byref(ptr[nm])))
+    ctx.check(L.nihu_gb_memcpy(ctx.handle, ptr["r"], C.DEVICE, rows.ctypes.data, C.HOST, 4 * npairs))
+    ctx.check(L.nihu_gb_memcpy(ctx.handle, ptr["c"], C.DEVICE, cols.ctypes.data, C.HOST, 4 * npairs))
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+
+    def step():
+        ctx.check(L.nihu_gb_assemble_pairs(ctx.handle, dm.handle, dm.handle, C.HELMHOLTZ_3D, ops, k,
+                                           coef.ctypes.data, ident.ctypes.data, C.REGULAR_FP32, C.C64, npairs,
+                                           ptr["r"], ptr["c"], ptr["a"], ptr["b"], C.DEVICE))
+
+    for _ in range(max(3, args.warmup)):
+        step()
+    ctx.set_profiling(True)
+    ctx.profile_reset()
+    clocks = ClockSampler(0)
+    clocks.start()
+    launches0 = ctx.launch_count
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    torch.cuda.synchronize()
+    for s_ in range(args.steps):
+        flush.fill_(s_ & 0xFF)
+        torch.cuda.synchronize()
+        ev[s_][0].record(stream)
+        step()
+        ev[s_][1].record(stream)
+    torch.cuda.synchronize()
+    launches = ctx.launch_count - launches0
+    clk = clocks.stop()
+    prof = ctx.profile()
+    ctx.set_profiling(False)
+    ms = float(np.mean([a_.elapsed_time(b_) for a_, b_ in ev]))
+    entries = 2.0 * npairs
+    ph_ms, ph_n = prof.get("assemble_pairs", (0.0, 0))
+    avg = ph_ms / max(ph_n, 1)
+    alg_bytes = 24.0 * npairs  # int32 row + column read, two complex64 values written
+    peak, peak_kind = measured_peaks()
+    achieved = alg_bytes / (avg / 1e3) / 1e9
+    n_self = int(np.sum(rows == cols))
+    out = {
+        "metric": "near-field (P2P) entries/s", "impl": "ours", "value": entries / (ms / 1e3), "unit": "entries/s",
+        "n_gpus": 1, "steps": args.steps, "warmup": max(3, args.warmup), "ms_per_step": ms,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "fp32 regular quadrature and nearly singular dynamic parts, fp64 self terms and nearly singular "
+                 "static parts; complex64 values",
+        "data": "synthetic (icosphere mesh generated in-process, uniform leaf boxes)",
+        "config": {"workload": "Burton-Miller near field (P2P) of icosphere s=5 (%d triangles), k=5, leaf boxes "
+                               "0.125, same and neighbouring boxes: %d pairs" % (n, npairs),
+                   "n_elements": n, "pairs": npairs, "self_pairs": n_self, "entries_per_step": int(entries),
+                   "l2": "256 MB written between timed steps (L2 flushed)"},
+        "gpu_launches": int(launches), "clocks": clk,
+        "roofline": {"kernel": "k_pairs_regular + k_pairs_singular (assemble_pairs.cu)", "bound": "hbm",
+                     "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak, "traffic": None,
+                     "peak_source": "%s (MEASURED_PEAKS.json hbm_gbs)" % peak_kind,
+                     "algorithmic_bytes_per_launch": alg_bytes, "avg_launch_ms": avg,
+                     "note": "compute-bound: near-field pairs take 3-12 regular points per operator or the FP64 "
+                             "nearly singular schemes"},
+        "phases": {kk: {"ms_per_step": v[0] / args.steps, "launches": v[1]} for kk, v in prof.items()},
+    }
+    a_dev = np.zeros(npairs, np.complex64)
+    ctx.check(L.nihu_gb_memcpy(ctx.handle, a_dev.ctypes.data, C.HOST, ptr["a"], C.DEVICE, 8 * npairs))
+    for p_ in ptr.values():
+        L.nihu_gb_device_free(ctx.handle, p_)
+    if not args.no_e2e:
+        ha, hb = np.zeros(npairs, np.complex64), np.zeros(npairs, np.complex64)
+
+        def e2e_step():
+            ctx.check(L.nihu_gb_assemble_pairs(ctx.handle, dm.handle, dm.handle, C.HELMHOLTZ_3D, ops, k,
+                                               coef.ctypes.data, ident.ctypes.data, C.REGULAR_FP32, C.C64, npairs,
+                                               rows.ctypes.data, cols.ctypes.data, ha.ctypes.data, hb.ctypes.data,
+                                               C.HOST))
+
+        e2e_step()
+        t0 = time.perf_counter()
+        e2e_steps = max(1, min(args.steps, 5))
+        for _ in range(e2e_steps):
+            e2e_step()
+        e2e_ms = (time.perf_counter() - t0) * 1e3 / e2e_steps
+        out["e2e"] = {"value": entries / (e2e_ms / 1e3), "unit": "entries/s",
+                      "h2d_bytes_per_step": int(8 * npairs), "d2h_bytes_per_step": int(16 * npairs),
+                      "ms_per_step": e2e_ms, "steps": e2e_steps,
+                      "path": "nihu_gb_assemble_pairs(where=HOST): pair list in, both value arrays out",
+                      "host_matches_device": bool(np.array_equal(ha, a_dev))}
+    dm.close()
+    ctx.close()
+    if not args.no_cpu:
+        from oracle import oracle
+        oracle.build()
+        threads = os.cpu_count() or 1
+        rng = np.random.default_rng(7)
+        probe = rng.choice(npairs, size=min(npairs, 1 << 14), replace=False)
+        t0 = time.perf_counter()
+        for op in (oracle.SLP, oracle.DLP, oracle.DLPT, oracle.HSP):
+            oracle.assemble_pairs(mesh, mesh, oracle.HELMHOLTZ, op, k, rows[probe], cols[probe], same_mesh=True,
+                                  threads=threads)
+        per_pair = (time.perf_counter() - t0) / len(probe)
+        size = int(min(npairs, max(len(probe), args.cpu_seconds / max(per_pair, 1e-12))))
+        sample = rng.choice(npairs, size=size, replace=False)
+        t0 = time.perf_counter()
+        for op in (oracle.SLP, oracle.DLP, oracle.DLPT, oracle.HSP):
+            oracle.assemble_pairs(mesh, mesh, oracle.HELMHOLTZ, op, k, rows[sample], cols[sample], same_mesh=True,
+                                  threads=threads)
+        el = time.perf_counter() - t0
+        out["cpu_baseline"] = {"value": 2.0 * len(sample) / el, "unit": "entries/s", "cores": threads,
+                               "kind": "port",
+                               "sample": "%d random pairs of the list x (SLP, DLP, DLPt, HSP), FP64 oracle, %.1f s "
+                                         "(near-field entries: two operators per entry of a and of b)"
+                                         % (len(sample), el)}
+    print(json.dumps(out), flush=True)
+
+
 def main():
     args = parse()
     if args.config == "multirhs":
@@ -1031,6 +1199,9 @@ def main():
         return
     if args.config == "bm":
         run_bm(args)
+        return
+    if args.config == "p2p":
+        run_p2p(args)
         return
     if args.impl == "reference":
         run_reference(args)

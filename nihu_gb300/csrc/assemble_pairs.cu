@@ -10,9 +10,11 @@
 // combines the operators as DLP + alpha HSP - I/2 and SLP + alpha DLPt +
 // alpha/2 I (nihu/fmm/helmholtz_burton_miller_solver.hpp:170-190).
 //
-// Two kernels: k_pairs_regular (one thread per pair) classifies every pair in
-// FP64 exactly as the reference, evaluates the regular ones (FP32 or FP64
-// quadrature) and compacts the self and nearly singular ones into a list;
+// Two kernels: k_pairs_regular (one thread per pair) classifies every pair
+// with the reference's decision (FP32 hi/lo centres, FP64 near a threshold),
+// evaluates the regular ones (FP32 or FP64 quadrature) and compacts the
+// nearly singular ones (from the front) and the self ones (from the back) of
+// a list;
 // k_pairs_singular (one FP64 thread per listed pair) evaluates those with the
 // schemes of the dense kernels.  Entries go to out_a[p] / out_b[p], p the
 // pair's position in the list.
@@ -33,8 +35,8 @@ __device__ __forceinline__ bool pair_valid(const PairArgs &a, int i, int j)
     return i >= 0 && i < a.test.n && j >= 0 && j < a.trial.n;
 }
 
-template <typename Out>
-__device__ __forceinline__ void store_pair(Out *p, double vr, double vi)
+template <typename Out, typename V>
+__device__ __forceinline__ void store_pair(Out *p, V vr, V vi)
 {
     Out o;
     o.x = vr;
@@ -57,24 +59,26 @@ __global__ void __launch_bounds__(PAIR_THREADS) k_pairs_regular(PairArgs a)
             atomicCAS(a.bad, 0, (int)min(p + 1, (int64_t)0x7fffffff));
             continue;
         }
-        // the reference's FP64 decision (nihu/core/double_integral.hpp:543-639)
-        const double ex = trial.center[3 * (int64_t)j] - test.center[3 * (int64_t)i];
-        const double ey = trial.center[3 * (int64_t)j + 1] - test.center[3 * (int64_t)i + 1];
-        const double ez = trial.center[3 * (int64_t)j + 2] - test.center[3 * (int64_t)i + 2];
-        const int code = (a.same_mesh && i == j) ? -1 : bm_code64(sqrt(ex * ex + ey * ey + ez * ez) / trial.size[j]);
-        if (code < 0) {
-            const unsigned long long slot = atomicAdd(a.n_sing, 1ULL);
-            a.sing[slot] = p;
-            continue;
-        }
-        const int lh = code % 4, ls = code / 12, ld = (code / 4) % 3;
+        // the reference's decision (nihu/core/double_integral.hpp:543-639):
+        // FP32 from the hi/lo centres, FP64 within 1e-5 of a threshold
         const float4 ih = test.chi[i], il = test.clo[i];
         const float4 jh = trial.chi[j], jl = trial.clo[j];
+        int ls, ld, lh;
+        float dx, dy, dz;
+        const int kind = classify_bm(ih, il, jh, jl, i, j, test.center, trial.center, trial.size, a.same_mesh, ls,
+                                     ld, lh, dx, dy, dz);
+        if (kind != KIND_REGULAR) {
+            // nearly singular pairs from the front, self pairs from the back,
+            // so that the FP64 kernel's warps run one scheme
+            if (kind == KIND_SELF) a.sing[a.n - 1 - (int64_t)atomicAdd(a.n_sing + 1, 1ULL)] = p;
+            else a.sing[atomicAdd(a.n_sing, 1ULL)] = p;
+            continue;
+        }
         const int par = il.w != 0.0f ? 1 : 0;
         const int tnc = trial.nc[j];
         const bool S = (a.ops & OP_SLP) != 0, D = (a.ops & OP_DLP) != 0;
         const bool T = (a.ops & OP_DLPT) != 0, H = (a.ops & OP_HSP) != 0;
-        R k, x0, x1, x2, nx0, nx1, nx2;
+        R k, x0, x1, x2, nx0, nx1, nx2, cr[4], ci[4];
         if constexpr (sizeof(R) == 4) {
             k = a.k32;
             x0 = ih.x + il.x;
@@ -84,6 +88,8 @@ __global__ void __launch_bounds__(PAIR_THREADS) k_pairs_regular(PairArgs a)
             nx0 = q.y;
             nx1 = q.z;
             nx2 = q.w;
+#pragma unroll
+            for (int o = 0; o < 4; ++o) { cr[o] = a.cre32[o]; ci[o] = a.cim32[o]; }
         } else {
             k = a.k;
             x0 = test.center[3 * (int64_t)i];
@@ -93,11 +99,9 @@ __global__ void __launch_bounds__(PAIR_THREADS) k_pairs_regular(PairArgs a)
             nx0 = n[0];
             nx1 = n[1];
             nx2 = n[2];
+#pragma unroll
+            for (int o = 0; o < 4; ++o) { cr[o] = a.cre[o]; ci[o] = a.cim[o]; }
         }
-        // hi/lo-accurate centre difference for the level-0 point
-        const float dx = (jh.x - ih.x) + (jl.x - il.x);
-        const float dy = (jh.y - ih.y) + (jl.y - il.y);
-        const float dz = (jh.z - ih.z) + (jl.z - il.z);
         const int64_t base = ((int64_t)j * 2 + par) * SLOTS;
         BmSum<R> o;
         for (int L = 0; L < 3; ++L) {
@@ -129,31 +133,44 @@ __global__ void __launch_bounds__(PAIR_THREADS) k_pairs_regular(PairArgs a)
             cross3(e1, e2, nt);
             const double J = norm3(nt);
             const int np = par ? 13 : 12;
-            for (int q = 0; q < np; ++q) {
-                double xi, eta, w;
-                tri_pt(par ? 7 : 6, q, xi, eta, w);
-                double y[3];
-                for (int d = 0; d < 3; ++d) y[d] = cc[d] + xi * e1[d] + eta * e2[d];
-                if constexpr (sizeof(R) == 4) {
-                    const double *cen = trial.center + 3 * (int64_t)j;
-                    eval_h<FAM, float>(dx + (float)(y[0] - cen[0]), dy + (float)(y[1] - cen[1]),
-                                       dz + (float)(y[2] - cen[2]), (float)(w * J), (float)n64[0], (float)n64[1],
-                                       (float)n64[2], nx0, nx1, nx2, k, o);
-                } else {
-                    eval_h<FAM, double>(y[0] - x0, y[1] - x1, y[2] - x2, w * J, n64[0], n64[1], n64[2], nx0, nx1, nx2,
-                                        k, o);
+            if constexpr (sizeof(R) == 4) {
+                // y - x = (c_j - x) + (y - c_j) as in the dense kernel
+                const double *cen = trial.center + 3 * (int64_t)j;
+                float b[3], f1[3], f2[3];
+                for (int d = 0; d < 3; ++d) {
+                    b[d] = (float)(cc[d] - cen[d]);
+                    f1[d] = (float)e1[d];
+                    f2[d] = (float)e2[d];
+                }
+                const float Jf = (float)J;
+                const float4 pj = trial.p0[j];
+                for (int q = 0; q < np; ++q) {
+                    const float *t = par ? TRI67.p7[q] : TRI67.p6[q];
+                    eval_h<FAM, float>(dx + (b[0] + t[0] * f1[0] + t[1] * f2[0]),
+                                       dy + (b[1] + t[0] * f1[1] + t[1] * f2[1]),
+                                       dz + (b[2] + t[0] * f1[2] + t[1] * f2[2]), t[2] * Jf, pj.y, pj.z, pj.w, nx0,
+                                       nx1, nx2, k, o);
+                }
+            } else {
+                for (int q = 0; q < np; ++q) {
+                    double xi, eta, w;
+                    tri_pt(par ? 7 : 6, q, xi, eta, w);
+                    double y[3];
+                    for (int d = 0; d < 3; ++d) y[d] = cc[d] + xi * e1[d] + eta * e2[d];
+                    eval_h<FAM, double>(y[0] - x0, y[1] - x1, y[2] - x2, w * J, n64[0], n64[1], n64[2], nx0, nx1,
+                                        nx2, k, o);
                 }
             }
         }
-        // out_a = c1 DLP + c3 HSP, out_b = c0 SLP + c2 DLPt (FP64 scaling of the sums)
+        // out_a = c1 DLP + c3 HSP, out_b = c0 SLP + c2 DLPt
         if (do_a) {
-            const double vr = a.cre[1] * o.dr - a.cim[1] * o.di + a.cre[3] * o.hr - a.cim[3] * o.hi;
-            const double vi = a.cre[1] * o.di + a.cim[1] * o.dr + a.cre[3] * o.hi + a.cim[3] * o.hr;
+            const R vr = cr[1] * o.dr - ci[1] * o.di + cr[3] * o.hr - ci[3] * o.hi;
+            const R vi = cr[1] * o.di + ci[1] * o.dr + cr[3] * o.hi + ci[3] * o.hr;
             store_pair(out_a + p, vr, vi);
         }
         if (do_b) {
-            const double vr = a.cre[0] * o.sr - a.cim[0] * o.si + a.cre[2] * o.tr - a.cim[2] * o.ti;
-            const double vi = a.cre[0] * o.si + a.cim[0] * o.sr + a.cre[2] * o.ti + a.cim[2] * o.tr;
+            const R vr = cr[0] * o.sr - ci[0] * o.si + cr[2] * o.tr - ci[2] * o.ti;
+            const R vi = cr[0] * o.si + ci[0] * o.sr + cr[2] * o.ti + ci[2] * o.tr;
             store_pair(out_b + p, vr, vi);
         }
     }
@@ -162,7 +179,7 @@ __global__ void __launch_bounds__(PAIR_THREADS) k_pairs_regular(PairArgs a)
 template <typename Out>
 __global__ void __launch_bounds__(PAIR_SING_THREADS) k_pairs_singular(PairArgs a)
 {
-    const unsigned long long count = *a.n_sing;
+    const unsigned long long n_near = a.n_sing[0], count = n_near + a.n_sing[1];
     const bool S = (a.ops & OP_SLP) != 0, D = (a.ops & OP_DLP) != 0;
     const bool T = (a.ops & OP_DLPT) != 0, H = (a.ops & OP_HSP) != 0;
     const bool bm_ops = T || H;
@@ -174,7 +191,7 @@ __global__ void __launch_bounds__(PAIR_SING_THREADS) k_pairs_singular(PairArgs a
     Out *out_b = reinterpret_cast<Out *>(a.out_b);
     for (unsigned long long t = (unsigned long long)blockIdx.x * PAIR_SING_THREADS + threadIdx.x; t < count;
          t += (unsigned long long)gridDim.x * PAIR_SING_THREADS) {
-        const int64_t p = a.sing[t];
+        const int64_t p = t < n_near ? a.sing[t] : a.sing[a.n - 1 - (int64_t)(t - n_near)];
         const int i = a.rows[p], j = a.cols[p];
         const bool self = a.same_mesh && i == j;
         const double x0[3] = {a.test.center[3 * (int64_t)i], a.test.center[3 * (int64_t)i + 1],
@@ -252,7 +269,7 @@ cudaError_t launch_assemble_pairs(const PairArgs &a, cudaStream_t s)
     int dev = 0, sms = 148;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaError_t e = cudaMemsetAsync(a.n_sing, 0, sizeof(unsigned long long), s);
+    cudaError_t e = cudaMemsetAsync(a.n_sing, 0, 2 * sizeof(unsigned long long), s);
     if (e != cudaSuccess) return e;
     const int64_t want = (a.n + PAIR_THREADS - 1) / PAIR_THREADS;
     const int blocks = (int)std::max<int64_t>(1, std::min<int64_t>(want, 8 * (int64_t)sms));

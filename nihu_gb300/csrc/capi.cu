@@ -873,6 +873,8 @@ nihu_gb_status nihu_gb_assemble_pairs(nihu_gb_ctx *ctx, const nihu_gb_mesh *test
     for (int o = 0; o < 4; ++o) {
         a.cre[o] = coef ? coef[2 * o] : 1.0;
         a.cim[o] = coef ? coef[2 * o + 1] : 0.0;
+        a.cre32[o] = (float)a.cre[o];
+        a.cim32[o] = (float)a.cim[o];
     }
     for (int o = 0; o < 2; ++o) {
         a.id_re[o] = ident ? ident[2 * o] : 0.0;
@@ -885,10 +887,10 @@ nihu_gb_status nihu_gb_assemble_pairs(nihu_gb_ctx *ctx, const nihu_gb_mesh *test
     const size_t es = elem_bytes(dtype);
     void *sing, *flags;
     if ((st = scratch(ctx, "pairs_sing", sizeof(int64_t) * n_pairs, &sing))) return st;
-    if ((st = scratch(ctx, "pairs_flags", 16, &flags))) return st;
+    if ((st = scratch(ctx, "pairs_flags", 32, &flags))) return st;
     a.sing = (int64_t *)sing;
     a.n_sing = (unsigned long long *)flags;
-    a.bad = (int *)((char *)flags + 8);
+    a.bad = (int *)((char *)flags + 16);
     a.err = ctx->d_flag;
     CK(cudaMemsetAsync(a.bad, 0, sizeof(int), ctx->stream));
     if (where == NIHU_GB_DEVICE) {

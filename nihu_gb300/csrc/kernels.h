@@ -119,8 +119,10 @@ cudaError_t launch_assemble_singular_bm(const BmArgs &a, const NearList &near, c
 //   out_a[p] = c[1] DLP + c[3] HSP (+ id[0] on a self pair)
 //   out_b[p] = c[0] SLP + c[2] DLPt (+ id[1] on a self pair)
 // for the operators in ops.  sing / n_sing: device scratch for the compacted
-// self and nearly singular pairs (n entries); bad receives 1 + the first pair
-// with an index out of range, err 1 + the first failed inverse mapping.
+// nearly singular pairs (from the front, count n_sing[0]) and self pairs
+// (from the back, count n_sing[1]) of the n entries; bad receives 1 + the
+// first pair with an index out of range, err 1 + the first failed inverse
+// mapping.
 struct PairArgs {
     DevMesh test, trial;
     int same_mesh = 0;
@@ -128,6 +130,7 @@ struct PairArgs {
     double k = 0.0;
     float k32 = 0.0f;
     double cre[4] = {0, 0, 0, 0}, cim[4] = {0, 0, 0, 0};
+    float cre32[4] = {0, 0, 0, 0}, cim32[4] = {0, 0, 0, 0};
     double id_re[2] = {0, 0}, id_im[2] = {0, 0};
     int precision = 0, dtype = 0;
     int64_t n = 0;

@@ -955,6 +955,35 @@ int oracle_assemble(const double *tnodes, int tn_nodes, const int *telems, int t
     return ok;
 }
 
+/*
+ * Entries of an explicit pair list (test rows[p], trial cols[p]), p < n,
+ * each with the full singular check, as NiHu's FMM near field evaluates them
+ * (nihu/fmm/p2p_integral.hpp:87-99 over the index pairs of
+ * nihu/fmm/p2p_precompute.hpp:110-180).  out[2p], out[2p+1] = (re, im).
+ * Returns 0 on error.
+ */
+int oracle_assemble_pairs(const double *tnodes, int tn_nodes, const int *telems, int tn_elems, int tcols,
+                          const double *rnodes, int rn_nodes, const int *relems, int rn_elems, int rcols,
+                          int same_mesh, int fam, int op, double k, long n, const int *rows, const int *cols,
+                          double *out)
+{
+    for (long p = 0; p < n; ++p) {
+        int i = rows[p], j = cols[p];
+        if (i < 0 || i >= tn_elems || j < 0 || j >= rn_elems) {
+            snprintf(g_err, sizeof g_err, "pair %ld: index out of range", p);
+            return 0;
+        }
+        elem_t te, re;
+        if (!load_elem(tnodes, tn_nodes, telems, tcols, i, &te)) return 0;
+        if (!load_elem(rnodes, rn_nodes, relems, rcols, j, &re)) return 0;
+        cplx v;
+        if (!entry(&te, &re, same_mesh && i == j, fam, op, k, &v)) return 0;
+        out[2 * p] = creal(v);
+        out[2 * p + 1] = cimag(v);
+    }
+    return 1;
+}
+
 /* element geometry for tests: centre[3], size, normal at centre[3] (unnormalised) */
 int oracle_elem_geometry(const double *coords, int nc, double *out7)
 {

@@ -45,6 +45,9 @@ def lib():
                                           c_int, c_int, c_int, c_double, c_double, c_double,
                                           c_int, c_int, c_int, c_int, dp, c_long, c_int]
             L.oracle_assemble.restype = c_int
+            L.oracle_assemble_pairs.argtypes = [dp, c_int, ip, c_int, c_int, dp, c_int, ip, c_int, c_int,
+                                                c_int, c_int, c_int, c_double, ctypes.c_long, ip, ip, dp]
+            L.oracle_assemble_pairs.restype = c_int
             L.oracle_classify.argtypes = [dp, c_int, ip, c_int, c_int, dp, c_int, ip, c_int, c_int,
                                           c_int, c_int, c_int, ip]
             L.oracle_classify.restype = c_int
@@ -101,6 +104,44 @@ def assemble(test_mesh, trial_mesh, family, op, k, same_mesh=None, rows=None, al
         work(r0, r1)
     else:
         bounds = np.linspace(r0, r1, threads + 1).astype(int)
+        ts = [threading.Thread(target=work, args=(int(bounds[i]), int(bounds[i + 1]))) for i in range(threads)]
+        for t in ts:
+            t.start()
+        for t in ts:
+            t.join()
+    if errors:
+        raise errors[0]
+    return out
+
+
+def assemble_pairs(test_mesh, trial_mesh, family, op, k, rows, cols, same_mesh=None, threads=1):
+    """Entries of the pair list (rows[p], cols[p]) with the full singular
+    check (complex128, one per pair): the FMM near-field evaluation."""
+    tn, te, targs = _mesh_args(*test_mesh)
+    rn, re_, rargs = _mesh_args(*trial_mesh)
+    if same_mesh is None:
+        same_mesh = test_mesh is trial_mesh
+    rows = np.ascontiguousarray(rows, dtype=np.int32)
+    cols = np.ascontiguousarray(cols, dtype=np.int32)
+    n = len(rows)
+    out = np.zeros(n, dtype=np.complex128)
+    L = lib()
+    errors = []
+
+    def work(a, b):
+        buf = np.zeros(b - a, dtype=np.complex128)
+        ok = L.oracle_assemble_pairs(*targs, *rargs, int(same_mesh), family, op, float(k), b - a,
+                                     _ptr(rows[a:b], ctypes.c_int), _ptr(cols[a:b], ctypes.c_int),
+                                     ctypes.cast(buf.ctypes.data, ctypes.POINTER(ctypes.c_double)))
+        if not ok:
+            errors.append(RuntimeError(L.oracle_last_error().decode()))
+            return
+        out[a:b] = buf
+
+    if threads <= 1 or n < 2:
+        work(0, n)
+    else:
+        bounds = np.linspace(0, n, threads + 1).astype(int)
         ts = [threading.Thread(target=work, args=(int(bounds[i]), int(bounds[i + 1]))) for i in range(threads)]
         for t in ts:
             t.start()

@@ -154,3 +154,21 @@ def test_hsp_degrees_follow_the_one_over_r_cubed_table():
     assert (d == -1).sum() == len(m[1])
     dd = oracle.degree(m, m, oracle.DLPT)
     assert (dd == oracle.degree(m, m, oracle.DLP)).all()
+
+
+def test_pair_list_matches_dense_entries():
+    """oracle.assemble_pairs (the FMM near-field loop) equals the dense
+    assembly at the listed pairs, self and nearly singular pairs included."""
+    from nihu_gb300 import meshes
+    m = meshes.icosphere(2)
+    kind = oracle.classify(m, m)
+    ii, jj = np.nonzero(kind < 0)
+    rng = np.random.default_rng(5)
+    rows = np.concatenate([ii, rng.integers(0, 320, 200)])
+    cols = np.concatenate([jj, rng.integers(0, 320, 200)])
+    for op in (oracle.SLP, oracle.DLP, oracle.DLPT, oracle.HSP):
+        M = oracle.assemble(m, m, oracle.HELMHOLTZ, op, 1.9)
+        v = oracle.assemble_pairs(m, m, oracle.HELMHOLTZ, op, 1.9, rows, cols, threads=2)
+        assert np.array_equal(v, M[rows, cols])
+    with pytest.raises(RuntimeError):
+        oracle.assemble_pairs(m, m, oracle.HELMHOLTZ, oracle.SLP, 1.0, [0], [320])
