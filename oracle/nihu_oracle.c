@@ -984,6 +984,273 @@ int oracle_assemble_pairs(const double *tnodes, int tn_nodes, const int *telems,
     return 1;
 }
 
+/* ------------------------------------------------------------ Galerkin */
+
+/* Regular Galerkin double integral: the rule of the given degree on both
+ * elements, every test point against every trial point, constant shape
+ * functions (nihu/core/double_integral.hpp:175-202 with the diadic dual
+ * accelerator of :300-312) */
+static cplx galerkin_regular(const elem_t *te, const elem_t *re, int fam, int op, double k, int degree)
+{
+    double tx[64][3], tw[64], ty[64][3], tn[64][3], rw[64];
+    int nt = 0, nr = 0;
+    for (int side = 0; side < 2; ++side) {
+        const elem_t *e = side == 0 ? te : re;
+        int cnt = 0;
+        double (*pts)[3] = side == 0 ? tx : ty;
+        double *ws = side == 0 ? tw : rw;
+        if (e->nc == 3) {
+            const double *q = tri_data + 3 * tri_off[degree];
+            for (int p = 0; p < tri_npts[degree]; ++p, ++cnt) {
+                double n[3];
+                elem_x(e, q[3 * p], q[3 * p + 1], pts[cnt]);
+                elem_normal(e, q[3 * p], q[3 * p + 1], n);
+                double J = norm3(n);
+                ws[cnt] = q[3 * p + 2] * J;
+                if (side == 1) for (int d = 0; d < 3; ++d) tn[cnt][d] = n[d] / J;
+            }
+        } else {
+            int ng = degree / 2 + 1;
+            const double *g = gauss_rule(ng);
+            for (int a = 0; a < ng; ++a)
+                for (int b = 0; b < ng; ++b, ++cnt) {
+                    double n[3];
+                    elem_x(e, g[2 * a], g[2 * b], pts[cnt]);
+                    elem_normal(e, g[2 * a], g[2 * b], n);
+                    double J = norm3(n);
+                    ws[cnt] = g[2 * a + 1] * g[2 * b + 1] * J;
+                    if (side == 1) for (int d = 0; d < 3; ++d) tn[cnt][d] = n[d] / J;
+                }
+        }
+        if (side == 0) nt = cnt; else nr = cnt;
+    }
+    cplx sum = 0.0;
+    for (int a = 0; a < nt; ++a)
+        for (int b = 0; b < nr; ++b) sum += tw[a] * kern(fam, op, k, tx[a], NULL, ty[b], tn[b]) * rw[b];
+    return sum;
+}
+
+/* Singular Galerkin quadrature on a pair of triangles with a common face
+ * (match 2), edge (1) or corner (0): the 4D Gauss product on (0,1)^4 with
+ * n = 7/2 + 1 = 4 points per direction (the kernels' singular quadrature
+ * order 7, nihu/library/helmholtz_kernel.hpp:69-71), split into Duffy-type
+ * subdomains in coordinate differences -- 3 (face, symmetric), 6 (edge), 1
+ * (corner, symmetric) -- and mapped back to the reference triangle
+ * (nihu/core/singular_galerkin_quadrature.hpp:200-420).  Points are stored as
+ * (test xi, eta, trial xi, eta, w); a symmetric rule also holds the swapped
+ * copy of every point. */
+#define GAL_N 4
+#define GAL_MAX (6 * GAL_N * GAL_N * GAL_N * GAL_N)
+static int g_gal_count[3];
+static double g_gal[3][GAL_MAX][5];
+
+static void gal_map(int match, int sub, const double u[4], double *w, double out[4])
+{
+    double a1, a2, b1, b2, jac;  /* test point (a1, a2), difference (b1, b2) */
+    if (match == 2) {
+        if (sub == 0) {
+            b1 = u[0]; b2 = u[0] * u[1];
+            a1 = (1.0 - b1) * u[2]; a2 = a1 * u[3];
+            jac = (1.0 - b1) * a1;
+        } else if (sub == 1) {
+            b1 = u[0] * u[1]; b2 = u[0] * (u[1] - 1.0);
+            a1 = (1.0 - b1 + b2) * u[2] - b2; a2 = (a1 + b2) * u[3] - b2;
+            jac = (1.0 - b1 + b2) * (a1 + b2);
+        } else {
+            b1 = u[0] * u[1]; b2 = u[0];
+            a1 = (1.0 - b2) * u[2] + b2 - b1; a2 = (a1 - b2 + b1) * u[3];
+            jac = (1.0 - b2) * (a1 - b2 + b1);
+        }
+        *w *= jac * u[0];
+    } else if (match == 1) {
+        const double p = u[0], q = u[1], r = u[2], s = u[3];
+        switch (sub) {
+        case 0: b1 = -p * q; b2 = -p * q * r; a1 = (1.0 - p) * s + p; a2 = p * (1.0 - q + q * r); break;
+        case 1: b1 = p * q; b2 = p * q * r; a1 = (1.0 - p) * s + p * (1.0 - q); a2 = p * (1.0 - q); break;
+        case 2: b1 = -p * q * r; b2 = p * q * (1.0 - r); a1 = (1.0 - p) * s + p; a2 = p * (1.0 - q); break;
+        case 3: b1 = p * q * r; b2 = p * q * (r - 1.0); a1 = (1.0 - p) * s + p * (1.0 - q * r); a2 = p * (1.0 - q * r); break;
+        case 4: b1 = -p * q * r; b2 = -p * q; a1 = (1.0 - p) * s + p; a2 = p; break;
+        default: b1 = p * q * r; b2 = p * q; a1 = (1.0 - p) * s + p * (1.0 - q * r); a2 = p * (1.0 - q); break;
+        }
+        *w *= q * p * p * (1.0 - p);
+    } else {
+        a1 = u[0]; a2 = a1 * u[1];
+        double e1 = a1 * u[2], e2 = e1 * u[3];
+        *w *= u[2] * u[0] * u[0] * u[0];
+        b1 = e1 - a1; b2 = e2 - a2;
+    }
+    /* (a1, a2) and (a1 + b1, a2 + b2) live on 0 <= x2 <= x1 <= 1: shift to the simplex */
+    out[0] = a1 - a2; out[1] = a2;
+    out[2] = (a1 + b1) - (a2 + b2); out[3] = a2 + b2;
+}
+
+static void gal_build(int match)
+{
+    const double *g = gauss_rule(GAL_N);
+    double x[GAL_N], w[GAL_N];
+    for (int i = 0; i < GAL_N; ++i) { x[i] = (1.0 + g[2 * i]) / 2.0; w[i] = g[2 * i + 1] / 2.0; }
+    const int subs = match == 2 ? 3 : (match == 1 ? 6 : 1);
+    const int sym = match != 1;
+    int n = 0;
+    for (int i1 = 0; i1 < GAL_N; ++i1)
+        for (int i2 = 0; i2 < GAL_N; ++i2)
+            for (int i3 = 0; i3 < GAL_N; ++i3)
+                for (int i4 = 0; i4 < GAL_N; ++i4)
+                    for (int sub = 0; sub < subs; ++sub) {
+                        double u[4] = {x[i1], x[i2], x[i3], x[i4]}, ww = w[i1] * w[i2] * w[i3] * w[i4], o[4];
+                        gal_map(match, sub, u, &ww, o);
+                        double *d = g_gal[match][n++];
+                        d[0] = o[0]; d[1] = o[1]; d[2] = o[2]; d[3] = o[3]; d[4] = ww;
+                        if (sym) {
+                            d = g_gal[match][n++];
+                            d[0] = o[2]; d[1] = o[3]; d[2] = o[0]; d[3] = o[1]; d[4] = ww;
+                        }
+                    }
+    g_gal_count[match] = n;
+}
+
+/* first common node of two triangles in each (cyclic order: the one the
+ * common edge starts from), as nihu/core/element.hpp:376-413 */
+static int common_nodes(const int *ta, const int *tb, int *ind1, int *ind2)
+{
+    int num = 0, s1 = 0, s2 = 0;
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) {
+            if (ta[i] != tb[j]) continue;
+            if (num == 0) { s1 = i; s2 = j; }
+            else {
+                if (i < s1 || (i == 2 && s1 == 0 && num == 1)) s1 = i;
+                if (j < s2 || (j == 2 && s2 == 0 && num == 1)) s2 = j;
+            }
+            ++num;
+        }
+    *ind1 = s1; *ind2 = s2;
+    return num;
+}
+
+/* reference-triangle point under a corner rotation: corner k of the rotated
+ * triangle is corner perm[k] of the reference one */
+static void tri_rotate(const int perm[3], double xi, double eta, double *oxi, double *oeta)
+{
+    static const double C[3][2] = {{0.0, 0.0}, {1.0, 0.0}, {0.0, 1.0}};
+    double N[3] = {1.0 - xi - eta, xi, eta};
+    *oxi = N[0] * C[perm[0]][0] + N[1] * C[perm[1]][0] + N[2] * C[perm[2]][0];
+    *oeta = N[0] * C[perm[0]][1] + N[1] * C[perm[1]][1] + N[2] * C[perm[2]][1];
+}
+
+/* singular Galerkin integral of a matched triangle pair: the test rule is
+ * rotated so that its first common node sits at corner 0, the trial rule so
+ * that the common edge runs the opposite way (edge) or its common node sits
+ * at corner 0 (corner) (nihu/core/singular_accelerator.hpp:270-310) */
+static cplx galerkin_singular(const elem_t *te, const elem_t *re, int fam, int op, double k, int match, int ind1,
+                              int ind2)
+{
+    if (!g_gal_count[match]) gal_build(match);
+    int pt[3], pr[3];
+    for (int q = 0; q < 3; ++q) {
+        pt[q] = match == 2 ? q : (ind1 + q) % 3;
+        pr[q] = match == 2 ? q : (match == 1 ? (ind2 + 1 + 3 - q) % 3 : (ind2 + q) % 3);
+    }
+    double nt[3], nr[3];
+    elem_normal(te, 0.25, 0.25, nt);
+    elem_normal(re, 0.25, 0.25, nr);
+    const double Jt = norm3(nt), Jr = norm3(nr);
+    double un[3] = {nr[0] / Jr, nr[1] / Jr, nr[2] / Jr};
+    cplx sum = 0.0;
+    for (int p = 0; p < g_gal_count[match]; ++p) {
+        const double *d = g_gal[match][p];
+        double a, b, x[3], y[3];
+        tri_rotate(pt, d[0], d[1], &a, &b);
+        elem_x(te, a, b, x);
+        tri_rotate(pr, d[2], d[3], &a, &b);
+        elem_x(re, a, b, y);
+        sum += d[4] * Jt * kern(fam, op, k, x, NULL, y, un) * Jr;
+    }
+    return sum;
+}
+
+/* One Galerkin entry (nihu/core/double_integral.hpp:318-384): face match for
+ * the same element of one mesh, edge / corner match for triangles of one mesh
+ * sharing 2 / 1 nodes, otherwise the regular rule of degree C + interval(d/D) */
+static int galerkin_entry(const elem_t *te, const elem_t *re, const int *tn, const int *rn, int same_mesh, int same_id,
+                          int fam, int op, double k, cplx *out)
+{
+    if (op != OP_SLP && op != OP_DLP) {
+        snprintf(g_err, sizeof g_err, "Galerkin: SLP and DLP only");
+        return 0;
+    }
+    int match = -1, ind1 = 0, ind2 = 0;
+    if (same_mesh) {
+        if (same_id) match = 2;
+        else if (te->nc == 3 && re->nc == 3) {
+            int num = common_nodes(tn, rn, &ind1, &ind2);
+            match = num > 1 ? 1 : (num == 1 ? 0 : -1);
+        } else {
+            int num = 0;
+            for (int i = 0; i < te->nc; ++i)
+                for (int j = 0; j < re->nc; ++j) num += tn[i] == rn[j];
+            if (num > 0) match = 0;
+        }
+    }
+    if (match >= 0) {
+        if (te->nc != 3 || re->nc != 3) {
+            snprintf(g_err, sizeof g_err, "Galerkin singular quadrature: constant triangles only");
+            return 0;
+        }
+        *out = galerkin_singular(te, re, fam, op, k, match, ind1, ind2);
+        return 1;
+    }
+    double ratio = centre_distance(te, re) / re->size;
+    int cmax = field_complexity(te->nc) > field_complexity(re->nc) ? field_complexity(te->nc) : field_complexity(re->nc);
+    int degree = cmax + interval_degree(op, ratio);
+    if (degree > 14 || (te->nc == 3 && tri_npts[degree] == 0)) {
+        snprintf(g_err, sizeof g_err, "unsupported quadrature degree %d", degree);
+        return 0;
+    }
+    *out = galerkin_regular(te, re, fam, op, k, degree);
+    return 1;
+}
+
+/* Galerkin assembly of rows [row_begin, row_end) x columns [col_begin, col_end)
+ * with the conventions of oracle_assemble (nihu/core/assembly.hpp:69-76) */
+int oracle_assemble_galerkin(const double *tnodes, int tn_nodes, const int *telems, int tn_elems, int tcols,
+                             const double *rnodes, int rn_nodes, const int *relems, int rn_elems, int rcols,
+                             int same_mesh, int fam, int op, double k, double alpha_re, double alpha_im,
+                             int row_begin, int row_end, int col_begin, int col_end, double *out, long ld,
+                             int accumulate)
+{
+    if (row_begin < 0 || row_end > tn_elems || row_begin > row_end) { snprintf(g_err, sizeof g_err, "bad row range"); return 0; }
+    if (col_begin < 0 || col_end > rn_elems || col_begin > col_end) { snprintf(g_err, sizeof g_err, "bad column range"); return 0; }
+    cplx alpha = alpha_re + I * alpha_im;
+    for (int i = row_begin; i < row_end; ++i) {
+        elem_t te;
+        if (!load_elem(tnodes, tn_nodes, telems, tcols, i, &te)) return 0;
+        const int *tn = telems + (long)i * tcols + 1;
+        for (int j = col_begin; j < col_end; ++j) {
+            elem_t re;
+            if (!load_elem(rnodes, rn_nodes, relems, rcols, j, &re)) return 0;
+            const int *rn = relems + (long)j * rcols + 1;
+            cplx v;
+            if (!galerkin_entry(&te, &re, tn, rn, same_mesh, same_mesh && i == j, fam, op, k, &v)) return 0;
+            cplx *dst = (cplx *)out + (long)(i - row_begin) + (long)(j - col_begin) * ld;
+            if (accumulate) *dst += alpha * v; else *dst = alpha * v;
+        }
+    }
+    return 1;
+}
+
+/* the singular Galerkin rule of a match type for tests: count, then points
+ * (test xi, eta, trial xi, eta, w) */
+int oracle_galerkin_rule(int match, double *out)
+{
+    if (match < 0 || match > 2) return 0;
+    if (!g_gal_count[match]) gal_build(match);
+    if (out)
+        for (int p = 0; p < g_gal_count[match]; ++p)
+            for (int c = 0; c < 5; ++c) out[5 * p + c] = g_gal[match][p][c];
+    return g_gal_count[match];
+}
+
 /* element geometry for tests: centre[3], size, normal at centre[3] (unnormalised) */
 int oracle_elem_geometry(const double *coords, int nc, double *out7)
 {

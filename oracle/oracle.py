@@ -48,6 +48,12 @@ def lib():
             L.oracle_assemble_pairs.argtypes = [dp, c_int, ip, c_int, c_int, dp, c_int, ip, c_int, c_int,
                                                 c_int, c_int, c_int, c_double, ctypes.c_long, ip, ip, dp]
             L.oracle_assemble_pairs.restype = c_int
+            L.oracle_assemble_galerkin.argtypes = [dp, c_int, ip, c_int, c_int, dp, c_int, ip, c_int, c_int, c_int,
+                                                   c_int, c_int, c_double, c_double, c_double, c_int, c_int, c_int,
+                                                   c_int, dp, ctypes.c_long, c_int]
+            L.oracle_assemble_galerkin.restype = c_int
+            L.oracle_galerkin_rule.argtypes = [c_int, dp]
+            L.oracle_galerkin_rule.restype = c_int
             L.oracle_classify.argtypes = [dp, c_int, ip, c_int, c_int, dp, c_int, ip, c_int, c_int,
                                           c_int, c_int, c_int, ip]
             L.oracle_classify.restype = c_int
@@ -111,6 +117,54 @@ def assemble(test_mesh, trial_mesh, family, op, k, same_mesh=None, rows=None, al
             t.join()
     if errors:
         raise errors[0]
+    return out
+
+
+def assemble_galerkin(test_mesh, trial_mesh, family, op, k, same_mesh=None, rows=None, alpha=1.0, threads=1):
+    """Dense Galerkin operator block (SLP or DLP, constant elements; singular
+    quadrature for matched triangles of one mesh) as complex128, Fortran order."""
+    tn, te, targs = _mesh_args(*test_mesh)
+    rn, re_, rargs = _mesh_args(*trial_mesh)
+    if same_mesh is None:
+        same_mesh = test_mesh is trial_mesh
+    r0, r1 = (0, len(te)) if rows is None else rows
+    m, n = r1 - r0, len(re_)
+    out = np.zeros((m, n), dtype=np.complex128, order="F")
+    alpha = complex(alpha)
+    L = lib()
+    errors = []
+
+    def work(a, b):
+        buf = np.zeros((b - a, n), dtype=np.complex128, order="F")
+        ok = L.oracle_assemble_galerkin(*targs, *rargs, int(same_mesh), family, op, float(k), alpha.real, alpha.imag,
+                                        a, b, 0, n, ctypes.cast(buf.ctypes.data, ctypes.POINTER(ctypes.c_double)),
+                                        b - a, 0)
+        if not ok:
+            errors.append(RuntimeError(L.oracle_last_error().decode()))
+            return
+        out[a - r0:b - r0] = buf
+
+    if threads <= 1 or m < 2:
+        work(r0, r1)
+    else:
+        bounds = np.linspace(r0, r1, threads + 1).astype(int)
+        ts = [threading.Thread(target=work, args=(int(bounds[i]), int(bounds[i + 1]))) for i in range(threads)]
+        for t in ts:
+            t.start()
+        for t in ts:
+            t.join()
+    if errors:
+        raise errors[0]
+    return out
+
+
+def galerkin_rule(match):
+    """The singular Galerkin rule of a triangle pair for match 2 (face), 1
+    (edge), 0 (corner): array of (test xi, eta, trial xi, eta, w)."""
+    L = lib()
+    n = L.oracle_galerkin_rule(match, None)
+    out = np.zeros((n, 5))
+    L.oracle_galerkin_rule(match, ctypes.cast(out.ctypes.data, ctypes.POINTER(ctypes.c_double)))
     return out
 
 
