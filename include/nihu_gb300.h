@@ -162,6 +162,29 @@ nihu_gb_status nihu_gb_assemble(nihu_gb_ctx *ctx, const nihu_gb_mesh *test, cons
 nihu_gb_status nihu_gb_add_identity(nihu_gb_ctx *ctx, const nihu_gb_mesh *mesh, double alpha_re, double alpha_im,
                                     int dtype, void *out, int64_t ld, int where);
 
+/* The Galerkin formalism of the SLP / DLP operators on constant elements,
+ * A(i, j) = int_{E_i} int_{E_j} K(x, y), with the conventions of
+ * nihu_gb_assemble (test == trial handle = one mesh).  On one mesh, pairs
+ * that share the element, an edge or a corner take the singular Galerkin
+ * rules of their match type (4 Gauss points per direction of a 4D Duffy-type
+ * split: 1536 / 1536 / 512 points); all other pairs the product of the
+ * regular rule of degree C + interval(d/D) on both elements.  Elements of one
+ * mesh must be constant triangles (quads: NIHU_GB_ERR_INVALID_ARGUMENT; the
+ * reference's quad rules are not built); a separate test mesh may hold quads.
+ * Replaces: test_space * Op[trial_space] with a function-space test space
+ * (nihu/core/double_integral.hpp:143-384, element_match.hpp:60-90,
+ * singular_accelerator.hpp:142-330, singular_galerkin_quadrature.hpp:200-420),
+ * e.g. nihu/test/stallone_unit/helmholtz_3d_pulsating_sphere_test.cpp:55-57. */
+nihu_gb_status nihu_gb_assemble_galerkin(nihu_gb_ctx *ctx, const nihu_gb_mesh *test, const nihu_gb_mesh *trial,
+                                         int family, int ops, double k, double alpha_re, double alpha_im,
+                                         int precision, int dtype, void *out_slp, void *out_dlp, int64_t ld,
+                                         int accumulate, int where);
+
+/* out(i, i) += alpha * area_i: the Galerkin identity operator of constant
+ * elements (test_space * I[trial_space], nihu/core/single_integral.hpp:97-140). */
+nihu_gb_status nihu_gb_add_mass(nihu_gb_ctx *ctx, const nihu_gb_mesh *mesh, double alpha_re, double alpha_im,
+                                int dtype, void *out, int64_t ld, int where);
+
 /* The Burton-Miller operators DLPt (transposed double layer, kernel
  * dG/dr (-r.n_x)/r) and HSP (hypersingular, d2G/dn_x dn_y) with the same
  * conventions as nihu_gb_assemble: `ops` is a bit mask of NIHU_GB_DLPT /

@@ -134,6 +134,17 @@ class Mesh:
     def num_elements(self) -> int:
         return len(self.elements)
 
+    def areas(self, ctx: Context | None = None) -> np.ndarray:
+        """Element areas with the one-point rule of the Galerkin identity
+        (nihu/core/single_integral.hpp:97-140): |e1 x e2| / 2 on triangles,
+        4 |x_xi x x_eta| at the centre on quads (nihu_gb_add_mass's weights)."""
+        el = self.elements
+        c = self.nodes[np.where(el[:, 1:5] >= 0, el[:, 1:5], el[:, 1:2])]
+        quad = el[:, 0] == C.QUAD_1
+        t1 = np.where(quad[:, None], (c[:, 1] + c[:, 2] - c[:, 0] - c[:, 3]) / 4, c[:, 1] - c[:, 0])
+        t2 = np.where(quad[:, None], (c[:, 2] + c[:, 3] - c[:, 0] - c[:, 1]) / 4, c[:, 2] - c[:, 0])
+        return np.linalg.norm(np.cross(t1, t2), axis=1) * np.where(quad, 4.0, 0.5)
+
     def device(self, ctx: Context) -> DeviceMesh:
         key = id(ctx)
         dm = self._dev.get(key)
@@ -304,6 +315,9 @@ class WeightedResidual:
         if not isinstance(result, np.ndarray) or result.ndim != 2:
             raise TypeError("result must be a 2D numpy array (a dynamic matrix, nihu/core/result_matrix.hpp)")
         test_mesh = _space_mesh(self.test)
+        # a function-space test space is the Galerkin formalism, dirac(...) collocation
+        # (nihu/core/formalism.hpp)
+        galerkin = not isinstance(self.test, DiracSpace)
         for op, trial_space in self.transform.terms:
             trial_mesh = _space_mesh(trial_space)
             m, n = test_mesh.num_elements, trial_mesh.num_elements
@@ -313,14 +327,14 @@ class WeightedResidual:
                 if test_mesh is not trial_mesh:
                     continue  # the identity only couples coinciding elements of one mesh
                 idx = np.arange(m)
-                result[idx, idx] += op.scale
+                result[idx, idx] += op.scale * (test_mesh.areas(ctx) if galerkin else 1.0)
                 continue
             _assemble_into(ctx, result, test_mesh, trial_mesh, op.kernel.family, op.kernel.op, op.kernel.k,
-                           op.scale, precision)
+                           op.scale, precision, galerkin)
         return result
 
 
-def _assemble_into(ctx, result, test_mesh, trial_mesh, family, op, k, alpha, precision):
+def _assemble_into(ctx, result, test_mesh, trial_mesh, family, op, k, alpha, precision, galerkin=False):
     L = C.lib()
     if result.dtype == np.complex64:
         dtype, target = C.C64, result
@@ -343,8 +357,11 @@ def _assemble_into(ctx, result, test_mesh, trial_mesh, family, op, k, alpha, pre
     if op in (C.SLP, C.DLP):
         out_s = buf.ctypes.data if op == C.SLP else None
         out_d = buf.ctypes.data if op == C.DLP else None
-        ctx.check(L.nihu_gb_assemble(ctx.handle, tdm.handle, rdm_handle, family, op, k, alpha.real, alpha.imag, prec,
-                                     dtype, out_s, out_d, max(result.shape[0], 1), accumulate, C.HOST))
+        fn = L.nihu_gb_assemble_galerkin if galerkin else L.nihu_gb_assemble
+        ctx.check(fn(ctx.handle, tdm.handle, rdm_handle, family, op, k, alpha.real, alpha.imag, prec,
+                     dtype, out_s, out_d, max(result.shape[0], 1), accumulate, C.HOST))
+    elif galerkin:
+        raise NotImplementedError("Galerkin formalism: SLP and DLP kernels only")
     else:
         out_t = buf.ctypes.data if op == C.DLPT else None
         out_h = buf.ctypes.data if op == C.HSP else None

@@ -1,0 +1,562 @@
+// Galerkin formalism of the SLP and DLP operators on constant elements:
+//   A(i, j) = int_{E_i} int_{E_j} K(x, y) dS_y dS_x
+// (nihu/core/double_integral.hpp:143-384, the "general" formalism).
+//
+// Dispatch, as the reference: on one mesh an element pair that shares the
+// element (face), two nodes (edge) or one node (corner) takes the singular
+// Galerkin rule of its match type (nihu/core/element_match.hpp:60-90,
+// nihu/core/singular_accelerator.hpp:220-310); every other pair takes the
+// product of the regular rule of degree C + interval(d/D) on both elements
+// (complexity_estimator.hpp:69-75, the dual accelerator of
+// double_integral.hpp:300-312).  The singular rules are the 4D Gauss products
+// (4 points per direction: the kernels' singular quadrature order 7) split
+// into Duffy-type subdomains in coordinate differences
+// (nihu/core/singular_galerkin_quadrature.hpp:200-420): face 3 subdomains
+// (symmetric, 1536 points), edge 6 (1536), corner 1 (symmetric, 512).
+//
+// Work layout: k_galerkin_regular (FP32 default / FP64) owns the pairs at
+// d/D >= 1.5 exactly as the collocation kernel does, with the test element's
+// points in the same rule as the trial element's (a far pair is the
+// collocation entry times the test element's area); k_galerkin_near (FP64,
+// one warp per pair, lanes over the rule's points) owns the self pairs, the
+// nearly singular list (d/D < 1.5: matched pairs, and unmatched ones with the
+// degree-6/8 product rules) and the rare pairs beyond 1.5 D that still share
+// a node (collected by the regular kernel).
+#include <algorithm>
+#include <mutex>
+#include <vector>
+
+#include "classify.cuh"
+#include "kernels.h"
+#include "singular_schemes.cuh"
+
+namespace nihu {
+
+constexpr int GAL_THREADS = 256;
+constexpr int GAL_COLS = 32;
+constexpr int GAL_WARPS = 4;
+constexpr int GAL_GAUSS = 4;  // points per direction of the singular rules
+constexpr int GAL_PER_DIM4 = GAL_GAUSS * GAL_GAUSS * GAL_GAUSS * GAL_GAUSS;
+// points of the corner (0), edge (1) and face (2) rules
+__host__ __device__ constexpr int gal_npts(int match) { return (match == 0 ? 2 : 6) * GAL_PER_DIM4; }
+constexpr int GAL_TOTAL = gal_npts(0) + gal_npts(1) + gal_npts(2);
+
+// the singular rules, (test xi, eta, trial xi, eta, w) per point: corner
+// points first, then edge, then face
+__device__ double g_gal_rule[GAL_TOTAL * 5];
+
+__host__ __device__ constexpr int gal_offset(int match)
+{
+    return match == 0 ? 0 : (match == 1 ? gal_npts(0) : gal_npts(0) + gal_npts(1));
+}
+
+// one point of the 4D cube mapped into a subdomain of the match type: test
+// point (a1, a2) and trial point (a1 + b1, a2 + b2) on 0 <= x2 <= x1 <= 1,
+// weight times the subdomain Jacobian
+static void gal_subdomain(int match, int sub, const double u[4], double &w, double out[4])
+{
+    double a1, a2, b1, b2;
+    if (match == 2) {
+        double jac;
+        if (sub == 0) {
+            b1 = u[0];
+            b2 = u[0] * u[1];
+            a1 = (1.0 - b1) * u[2];
+            a2 = a1 * u[3];
+            jac = (1.0 - b1) * a1;
+        } else if (sub == 1) {
+            b1 = u[0] * u[1];
+            b2 = u[0] * (u[1] - 1.0);
+            a1 = (1.0 - b1 + b2) * u[2] - b2;
+            a2 = (a1 + b2) * u[3] - b2;
+            jac = (1.0 - b1 + b2) * (a1 + b2);
+        } else {
+            b1 = u[0] * u[1];
+            b2 = u[0];
+            a1 = (1.0 - b2) * u[2] + b2 - b1;
+            a2 = (a1 - b2 + b1) * u[3];
+            jac = (1.0 - b2) * (a1 - b2 + b1);
+        }
+        w *= jac * u[0];
+    } else if (match == 1) {
+        const double p = u[0], q = u[1], r = u[2], s = u[3];
+        switch (sub) {
+        case 0: b1 = -p * q; b2 = -p * q * r; a1 = (1.0 - p) * s + p; a2 = p * (1.0 - q + q * r); break;
+        case 1: b1 = p * q; b2 = p * q * r; a1 = (1.0 - p) * s + p * (1.0 - q); a2 = p * (1.0 - q); break;
+        case 2: b1 = -p * q * r; b2 = p * q * (1.0 - r); a1 = (1.0 - p) * s + p; a2 = p * (1.0 - q); break;
+        case 3: b1 = p * q * r; b2 = p * q * (r - 1.0); a1 = (1.0 - p) * s + p * (1.0 - q * r); a2 = p * (1.0 - q * r); break;
+        case 4: b1 = -p * q * r; b2 = -p * q; a1 = (1.0 - p) * s + p; a2 = p; break;
+        default: b1 = p * q * r; b2 = p * q; a1 = (1.0 - p) * s + p * (1.0 - q * r); a2 = p * (1.0 - q); break;
+        }
+        w *= q * p * p * (1.0 - p);
+    } else {
+        a1 = u[0];
+        a2 = a1 * u[1];
+        const double e1 = a1 * u[2], e2 = e1 * u[3];
+        w *= u[2] * u[0] * u[0] * u[0];
+        b1 = e1 - a1;
+        b2 = e2 - a2;
+    }
+    out[0] = a1 - a2;
+    out[1] = a2;
+    out[2] = (a1 + b1) - (a2 + b2);
+    out[3] = a2 + b2;
+}
+
+// host generation of the three rules (the Gauss nodes come from the device
+// tables' source, quad_rules.h)
+static std::vector<double> gal_rules()
+{
+    static const double gdata[NIHU_GAUSS_DATA_LEN] = NIHU_GAUSS_DATA;
+    static const int goff[NIHU_GAUSS_MAX_N] = NIHU_GAUSS_OFFSETS;
+    double x[GAL_GAUSS], wt[GAL_GAUSS];
+    for (int i = 0; i < GAL_GAUSS; ++i) {
+        x[i] = (1.0 + gdata[2 * (goff[GAL_GAUSS - 1] + i)]) / 2.0;
+        wt[i] = gdata[2 * (goff[GAL_GAUSS - 1] + i) + 1] / 2.0;
+    }
+    std::vector<double> out((size_t)GAL_TOTAL * 5);
+    for (int match = 0; match < 3; ++match) {
+        const int subs = match == 2 ? 3 : (match == 1 ? 6 : 1);
+        const bool sym = match != 1;
+        double *d = out.data() + 5 * (size_t)gal_offset(match);
+        for (int i1 = 0; i1 < GAL_GAUSS; ++i1)
+            for (int i2 = 0; i2 < GAL_GAUSS; ++i2)
+                for (int i3 = 0; i3 < GAL_GAUSS; ++i3)
+                    for (int i4 = 0; i4 < GAL_GAUSS; ++i4)
+                        for (int sub = 0; sub < subs; ++sub) {
+                            const double u[4] = {x[i1], x[i2], x[i3], x[i4]};
+                            double w = wt[i1] * wt[i2] * wt[i3] * wt[i4], o[4];
+                            gal_subdomain(match, sub, u, w, o);
+                            d[0] = o[0]; d[1] = o[1]; d[2] = o[2]; d[3] = o[3]; d[4] = w;
+                            d += 5;
+                            if (sym) {
+                                d[0] = o[2]; d[1] = o[3]; d[2] = o[0]; d[3] = o[1]; d[4] = w;
+                                d += 5;
+                            }
+                        }
+    }
+    return out;
+}
+
+cudaError_t prepare_galerkin(cudaStream_t s)
+{
+    static std::mutex mu;
+    static std::vector<int> done;
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    std::lock_guard<std::mutex> lock(mu);
+    if ((int)done.size() > dev && done[dev]) return cudaSuccess;
+    static const std::vector<double> rules = gal_rules();
+    e = cudaMemcpyToSymbolAsync(g_gal_rule, rules.data(), rules.size() * sizeof(double), 0, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return e;
+    if ((int)done.size() <= dev) done.resize(dev + 1, 0);
+    done[dev] = 1;
+    return cudaSuccess;
+}
+
+// number of common corner nodes of two elements and, for triangles, the first
+// common node of each in cyclic order (nihu/core/element.hpp:376-413)
+__device__ __forceinline__ int common_nodes(int4 a, int na, int4 b, int nb, int &ind1, int &ind2)
+{
+    const int A[4] = {a.x, a.y, a.z, a.w}, B[4] = {b.x, b.y, b.z, b.w};
+    int num = 0, s1 = 0, s2 = 0;
+    for (int i = 0; i < na; ++i)
+        for (int j = 0; j < nb; ++j) {
+            if (A[i] != B[j]) continue;
+            if (num == 0) {
+                s1 = i;
+                s2 = j;
+            } else {
+                if (i < s1 || (i == na - 1 && s1 == 0 && num == 1)) s1 = i;
+                if (j < s2 || (j == nb - 1 && s2 == 0 && num == 1)) s2 = j;
+            }
+            ++num;
+        }
+    ind1 = s1;
+    ind2 = s2;
+    return num;
+}
+
+template <typename R, typename Out, int FAM, int OPS>
+__global__ void __launch_bounds__(GAL_THREADS) k_galerkin_regular(GalArgs a)
+{
+    __shared__ float4 s_hi[GAL_COLS], s_lo[GAL_COLS], s_p0[GAL_COLS];
+    __shared__ int4 s_nid[GAL_COLS];
+    __shared__ int s_nc[GAL_COLS];
+    constexpr bool DO_S = (OPS & OP_SLP) != 0;
+    constexpr bool DO_D = (OPS & OP_DLP) != 0;
+    const DevMesh &test = a.test;
+    const DevMesh &trial = a.trial;
+    const int i = blockIdx.x * GAL_THREADS + threadIdx.x;
+    const int jb = a.j0 + blockIdx.y * GAL_COLS;
+    const int ncols = min(GAL_COLS, a.j1 - jb);
+    if (threadIdx.x < ncols) {
+        const int j = jb + threadIdx.x;
+        s_hi[threadIdx.x] = trial.chi[j];
+        s_lo[threadIdx.x] = trial.clo[j];
+        s_p0[threadIdx.x] = trial.p0[j];
+        s_nid[threadIdx.x] = trial.nid[j];
+        s_nc[threadIdx.x] = trial.nc[j];
+    }
+    __syncthreads();
+    if ((i & ~31) >= test.n) return;
+    const bool row_ok = i < test.n;
+    const int ii = row_ok ? i : test.n - 1;
+    const float4 ih = test.chi[ii], il = test.clo[ii];
+    const int4 inid = test.nid[ii];
+    const int inc = test.nc[ii];
+    const float area_i = test.p0[ii].x;  // w J of the one-point rule: the element's area
+    R k, are, aim, x0, x1, x2;
+    if constexpr (sizeof(R) == 4) {
+        k = a.k32;
+        are = a.alpha_re32;
+        aim = a.alpha_im32;
+        x0 = ih.x + il.x;
+        x1 = ih.y + il.y;
+        x2 = ih.z + il.z;
+    } else {
+        k = a.k;
+        are = a.alpha_re;
+        aim = a.alpha_im;
+        x0 = test.center[3 * (int64_t)ii];
+        x1 = test.center[3 * (int64_t)ii + 1];
+        x2 = test.center[3 * (int64_t)ii + 2];
+    }
+    Out *out_s = reinterpret_cast<Out *>(a.out_s);
+    Out *out_d = reinterpret_cast<Out *>(a.out_d);
+    for (int c = 0; c < ncols; ++c) {
+        const int j = jb + c;
+        int ind1, ind2;
+        const int shared = a.same_mesh ? common_nodes(inid, inc, s_nid[c], s_nc[c], ind1, ind2) : 0;
+        R sr = 0, si = 0, dr = 0, di = 0;
+        bool done = false;
+        if constexpr (sizeof(R) == 4) {
+            // far field: both one-point rules, the centroid kernel times both areas
+            const float4 h = s_hi[c];
+            const float fx = h.x - x0, fy = h.y - x1, fz = h.z - x2;
+            const float q = (fx * fx + fy * fy + fz * fz) * h.w;
+            if (__all_sync(0xffffffffu, q > 249.64f * (1.0f + 1e-4f) && shared == 0)) {
+                const float4 p = s_p0[c];
+                eval_point<FAM, float>(fx, fy, fz, p.x, p.y, p.z, p.w, k, DO_S ? area_i : 0.0f, DO_D ? area_i : 0.0f,
+                                       sr, si, dr, di);
+                done = true;
+            }
+        }
+        if (!done) {
+            int ls, ld;
+            float dx, dy, dz;
+            const int kind = classify_pair(ih, il, s_hi[c], s_lo[c], ii, j, test.center, trial.center, trial.size,
+                                           a.same_mesh, ls, ld, dx, dy, dz);
+            if (kind != KIND_REGULAR || !row_ok) continue;  // self and d/D < 1.5: the FP64 kernel
+            if (shared > 0) {
+                // a node shared beyond 1.5 D (strongly graded mesh): singular rule
+                const unsigned slot = atomicAdd(a.n_extra, 1u);
+                if (slot < (unsigned)a.extra_cap) a.extra[slot] = make_int2(i, j);
+                else atomicCAS(a.err, 0, -1);
+                continue;
+            }
+            if (!DO_S) ls = ld;
+            if (!DO_D) ld = ls;
+            // the rule of degree C + 2 l on both elements: C = max complexity
+            const int cmax = (il.w != 0.0f || s_lo[c].w != 0.0f) ? 1 : 0;
+            const int64_t bi = ((int64_t)ii * 2 + cmax) * SLOTS, bj = ((int64_t)j * 2 + cmax) * SLOTS;
+            for (int pass = 0; pass < 2; ++pass) {
+                const int L = pass == 0 ? ls : ld;
+                if (pass == 1 && ld == ls) break;
+                const R ws = (DO_S && ls == L) ? R(1) : R(0), wd = (DO_D && ld == L) ? R(1) : R(0);
+                const int npi = level_npts(inc, cmax, L), npj = level_npts(s_nc[c], cmax, L);
+                for (int p = 0; p < npi; ++p) {
+                    const int sp = level_slot0(L) + p;
+                    R xp0, xp1, xp2, wp;
+                    if constexpr (sizeof(R) == 4) {
+                        const float4 y = __ldg(test.pts32 + 2 * (bi + sp));
+                        xp0 = y.x;
+                        xp1 = y.y;
+                        xp2 = y.z;
+                        wp = y.w;
+                    } else {
+                        const double *y = test.pts64 + 8 * (bi + sp);
+                        xp0 = y[0];
+                        xp1 = y[1];
+                        xp2 = y[2];
+                        wp = y[3];
+                    }
+                    for (int q = 0; q < npj; ++q) {
+                        const int sq = level_slot0(L) + q;
+                        if constexpr (sizeof(R) == 4) {
+                            const float4 y = __ldg(trial.pts32 + 2 * (bj + sq));
+                            const float4 n = __ldg(trial.pts32 + 2 * (bj + sq) + 1);
+                            // centroid pair: the accurate hi/lo difference
+                            const bool centre = sp == 0 && sq == 0;
+                            eval_point<FAM, float>(centre ? dx : y.x - xp0, centre ? dy : y.y - xp1,
+                                                   centre ? dz : y.z - xp2, y.w, n.x, n.y, n.z, k, ws * wp, wd * wp,
+                                                   sr, si, dr, di);
+                        } else {
+                            const double *y = trial.pts64 + 8 * (bj + sq);
+                            eval_point<FAM, double>(y[0] - xp0, y[1] - xp1, y[2] - xp2, y[3], y[4], y[5], y[6], k,
+                                                    ws * wp, wd * wp, sr, si, dr, di);
+                        }
+                    }
+                }
+            }
+        }
+        if (!row_ok) continue;
+        const int64_t off = (int64_t)(j - a.j0) * a.ld + i;
+        auto store = [&](Out *p, R re, R im) {
+            const R vr = are * re - aim * im, vi = are * im + aim * re;
+            Out o;
+            if (a.accumulate) {
+                o = *p;
+                o.x += vr;
+                o.y += vi;
+            } else {
+                o.x = vr;
+                o.y = vi;
+            }
+            *p = o;
+        };
+        if (DO_S) store(out_s + off, sr, si);
+        if (DO_D) store(out_d + off, dr, di);
+    }
+}
+
+// point p of the product rule of a given degree on an element: reference
+// coordinates and weight (Dunavant on triangles, Gauss tensor on quads)
+__device__ __forceinline__ void product_point(int nc, int degree, int p, double &xi, double &eta, double &w)
+{
+    if (nc == 3) {
+        tri_pt(degree, p, xi, eta, w);
+    } else {
+        const int ng = degree / 2 + 1;
+        double w0, w1;
+        gauss_pt(ng, p / ng, xi, w0);
+        gauss_pt(ng, p % ng, eta, w1);
+        w = w0 * w1;
+    }
+}
+
+__device__ __forceinline__ int product_npts(int nc, int degree)
+{
+    if (nc == 3) return g_tri_npts[degree];
+    const int ng = degree / 2 + 1;
+    return ng * ng;
+}
+
+// reference point under a corner rotation of the triangle: corner k of the
+// rotated triangle is corner perm[k] of (0,0), (1,0), (0,1)
+__device__ __forceinline__ void tri_rotate(const int perm[3], double xi, double eta, double &oxi, double &oeta)
+{
+    const double N[3] = {1.0 - xi - eta, xi, eta};
+    oxi = 0.0;
+    oeta = 0.0;
+#pragma unroll
+    for (int q = 0; q < 3; ++q) {
+        oxi += perm[q] == 1 ? N[q] : 0.0;
+        oeta += perm[q] == 2 ? N[q] : 0.0;
+    }
+}
+
+// The self pairs, the nearly singular list of columns [j0, j1) (extra = 0)
+// or the extra list (extra = 1): one warp per pair
+template <typename Out>
+__global__ void __launch_bounds__(GAL_WARPS * 32) k_galerkin_near(GalArgs a, NearList near, int extra)
+{
+    const int lane = threadIdx.x & 31;
+    const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    int64_t n_near = 0, p_begin = 0, total = 0;
+    if (extra) {
+        total = min((int64_t)*a.n_extra, (int64_t)a.extra_cap);
+    } else {
+        p_begin = near.col_ptr ? near.col_ptr[a.j0] : 0;
+        n_near = (near.col_ptr ? near.col_ptr[a.j1] : 0) - p_begin;
+        total = n_near + (a.same_mesh ? (int64_t)(a.j1 - a.j0) : 0);
+    }
+    const bool do_s = (a.ops & OP_SLP) != 0, do_d = (a.ops & OP_DLP) != 0;
+    const int fam = a.family;
+    const double k = a.k;
+    Out *out_s = reinterpret_cast<Out *>(a.out_s);
+    Out *out_d = reinterpret_cast<Out *>(a.out_d);
+    for (int64_t item = warp; item < total; item += nwarps) {
+        int i, j;
+        if (extra) {
+            const int2 e = a.extra[item];
+            i = e.x;
+            j = e.y;
+        } else if (item < n_near) {
+            const int64_t p = p_begin + item;
+            i = near.rows[p];
+            j = near_column(near.col_ptr, a.j0, a.j1, p);
+        } else {
+            j = a.j0 + (int)(item - n_near);
+            i = j;
+            if (i >= a.test.n) continue;
+        }
+        Elem64 te, re;
+        load_elem(a.test, i, te);
+        load_elem(a.trial, j, re);
+        int match = -1, ind1 = 0, ind2 = 0;
+        if (a.same_mesh) {
+            if (i == j) match = 2;
+            else {
+                const int num = common_nodes(a.test.nid[i], te.nc, a.trial.nid[j], re.nc, ind1, ind2);
+                match = num > 1 ? 1 : (num == 1 ? 0 : -1);
+            }
+        }
+        double sr = 0, si = 0, dr = 0, di = 0;
+        if (match >= 0) {
+            // matched triangles (quads were refused by the host): flat elements
+            int pt[3], pr[3];
+#pragma unroll
+            for (int q = 0; q < 3; ++q) {
+                pt[q] = match == 2 ? q : (ind1 + q) % 3;
+                pr[q] = match == 2 ? q : (match == 1 ? (ind2 + 1 + 3 - q) % 3 : (ind2 + q) % 3);
+            }
+            double t1[3], t2[3], r1[3], r2[3], nt[3], nr[3];
+            for (int d = 0; d < 3; ++d) {
+                t1[d] = te.c[1][d] - te.c[0][d];
+                t2[d] = te.c[2][d] - te.c[0][d];
+                r1[d] = re.c[1][d] - re.c[0][d];
+                r2[d] = re.c[2][d] - re.c[0][d];
+            }
+            cross3(t1, t2, nt);
+            cross3(r1, r2, nr);
+            const double Jt = norm3(nt), Jr = norm3(nr);
+            const double *rule = g_gal_rule + 5 * (size_t)gal_offset(match);
+            const int np = gal_npts(match);
+            for (int p = lane; p < np; p += 32) {
+                const double *q = rule + 5 * p;
+                double u, v, x[3], y[3];
+                tri_rotate(pt, q[0], q[1], u, v);
+                for (int d = 0; d < 3; ++d) x[d] = te.c[0][d] + u * t1[d] + v * t2[d];
+                tri_rotate(pr, q[2], q[3], u, v);
+                for (int d = 0; d < 3; ++d) y[d] = re.c[0][d] + u * r1[d] + v * r2[d];
+                cd ks{0, 0}, kd{0, 0};
+                kern_point(fam, k, x, y, nr, Jr, do_s, do_d, ks, kd);
+                const double w = q[4] * Jt;
+                sr += ks.re * w;
+                si += ks.im * w;
+                dr += kd.re * w;
+                di += kd.im * w;
+            }
+        } else {
+            // unmatched close pair: product of the degree C + interval(d/D)
+            // rules (up to degree 8 + 1), the SLP and DLP degrees apart
+            double dc[3];
+            for (int d = 0; d < 3; ++d) dc[d] = a.trial.center[3 * (int64_t)j + d] - a.test.center[3 * (int64_t)i + d];
+            const double ratio = norm3(dc) / a.trial.size[j];
+            const int cmax = (te.nc == 4 || re.nc == 4) ? 1 : 0;
+            const int deg_s = cmax + (ratio < 11.0 / 10.0 ? 6 : (ratio < T_S1 ? 4 : (ratio < T_S0 ? 2 : 0)));
+            const int deg_d =
+                cmax + (ratio < 11.0 / 10.0 ? 8 : (ratio < T_NEAR ? 6 : (ratio < T_D1 ? 4 : (ratio < T_D0 ? 2 : 0))));
+            const bool shared_pass = !do_s || !do_d || deg_s == deg_d;
+            for (int pass = 0; pass < (shared_pass ? 1 : 2); ++pass) {
+                const bool use_s = shared_pass ? do_s : pass == 0;
+                const bool use_d = shared_pass ? do_d : pass == 1;
+                const int deg = use_s ? deg_s : deg_d;
+                const int npt = product_npts(te.nc, deg), npr = product_npts(re.nc, deg);
+                for (int p = lane; p < npt * npr; p += 32) {
+                    double xi, eta, wt, xr, er, wr;
+                    product_point(te.nc, deg, p / npr, xi, eta, wt);
+                    product_point(re.nc, deg, p % npr, xr, er, wr);
+                    double x[3], y[3], n[3], nx[3];
+                    ex(te, xi, eta, x);
+                    enormal(te, xi, eta, nx);
+                    ex(re, xr, er, y);
+                    enormal(re, xr, er, n);
+                    cd ks{0, 0}, kd{0, 0};
+                    kern_point(fam, k, x, y, n, norm3(n), use_s, use_d, ks, kd);
+                    const double w = wt * norm3(nx) * wr;
+                    if (use_s) {
+                        sr += ks.re * w;
+                        si += ks.im * w;
+                    }
+                    if (use_d) {
+                        dr += kd.re * w;
+                        di += kd.im * w;
+                    }
+                }
+            }
+        }
+        sr = warp_sum(sr);
+        si = warp_sum(si);
+        dr = warp_sum(dr);
+        di = warp_sum(di);
+        if (lane == 0) {
+            const int64_t off = (int64_t)(j - a.j0) * a.ld + i;
+            if (do_s) store64(out_s + off, sr, si, a.alpha_re, a.alpha_im, a.accumulate);
+            if (do_d) store64(out_d + off, dr, di, a.alpha_re, a.alpha_im, a.accumulate);
+        }
+    }
+}
+
+template <typename R, typename Out, int FAM>
+static void launch_gal_ops(const GalArgs &a, dim3 grid, cudaStream_t s)
+{
+    if (a.ops == OP_SLP) k_galerkin_regular<R, Out, FAM, OP_SLP><<<grid, GAL_THREADS, 0, s>>>(a);
+    else if (a.ops == OP_DLP) k_galerkin_regular<R, Out, FAM, OP_DLP><<<grid, GAL_THREADS, 0, s>>>(a);
+    else k_galerkin_regular<R, Out, FAM, OP_SLP | OP_DLP><<<grid, GAL_THREADS, 0, s>>>(a);
+}
+
+template <typename R, typename Out>
+static void launch_gal_fam(const GalArgs &a, dim3 grid, cudaStream_t s)
+{
+    if (a.family == FAM_HELMHOLTZ) launch_gal_ops<R, Out, FAM_HELMHOLTZ>(a, grid, s);
+    else launch_gal_ops<R, Out, FAM_LAPLACE>(a, grid, s);
+}
+
+cudaError_t launch_galerkin_regular(const GalArgs &a, cudaStream_t s)
+{
+    const int ncols = a.j1 - a.j0;
+    if (a.test.n == 0 || ncols <= 0) return cudaSuccess;
+    dim3 grid((a.test.n + GAL_THREADS - 1) / GAL_THREADS, (ncols + GAL_COLS - 1) / GAL_COLS);
+    if (a.precision == 0) {
+        if (a.dtype == 0) launch_gal_fam<float, float2>(a, grid, s);
+        else launch_gal_fam<float, double2>(a, grid, s);
+    } else {
+        if (a.dtype == 0) launch_gal_fam<double, float2>(a, grid, s);
+        else launch_gal_fam<double, double2>(a, grid, s);
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_galerkin_near(const GalArgs &a, const NearList &near, int extra, int64_t max_items, cudaStream_t s)
+{
+    if (max_items <= 0) return cudaSuccess;
+    int dev = 0, sms = 148;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const int64_t want = (max_items + GAL_WARPS - 1) / GAL_WARPS;
+    const int blocks = (int)std::max<int64_t>(1, std::min<int64_t>(want, 8 * (int64_t)sms));
+    if (a.dtype == 0) k_galerkin_near<float2><<<blocks, GAL_WARPS * 32, 0, s>>>(a, near, extra);
+    else k_galerkin_near<double2><<<blocks, GAL_WARPS * 32, 0, s>>>(a, near, extra);
+    return cudaGetLastError();
+}
+
+template <typename Out>
+__global__ void k_add_mass(int n, const double *pts64, double are, double aim, Out *out, int64_t ld)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    // w J of the element's one-point rule (parity 0, level 0): its area,
+    // exact for flat triangles and bilinear quads
+    const double area = pts64[8 * ((int64_t)i * 2 * SLOTS) + 3];
+    Out o = out[(int64_t)i * ld + i];
+    o.x += are * area;
+    o.y += aim * area;
+    out[(int64_t)i * ld + i] = o;
+}
+
+cudaError_t launch_add_mass(int n, const double *pts64, double are, double aim, int dtype, void *out, int64_t ld,
+                            cudaStream_t s)
+{
+    if (n == 0) return cudaSuccess;
+    const int t = 256, b = (n + t - 1) / t;
+    if (dtype == 0) k_add_mass<float2><<<b, t, 0, s>>>(n, pts64, are, aim, (float2 *)out, ld);
+    else k_add_mass<double2><<<b, t, 0, s>>>(n, pts64, are, aim, (double2 *)out, ld);
+    return cudaGetLastError();
+}
+
+}  // namespace nihu

@@ -24,36 +24,6 @@ namespace nihu {
 constexpr int REG_THREADS = 256;
 constexpr int REG_COLS = 32;
 
-template <int FAM, typename R>
-__device__ __forceinline__ void eval_point(R rx, R ry, R rz, R wj, R nx, R ny, R nz, R k, R ws, R wd, R &sr,
-                                           R &si, R &dr, R &di)
-{
-    constexpr R INV4PI = R(1.0 / (4.0 * 3.14159265358979323846));
-    R r2 = rx * rx + ry * ry + rz * rz;
-    R rinv;
-    if constexpr (sizeof(R) == 4) rinv = rsqrtf(r2);
-    else rinv = rsqrt(r2);
-    R g = wj * rinv * INV4PI;
-    R rdn = (rx * nx + ry * ny + rz * nz) * rinv;
-    if constexpr (FAM == FAM_HELMHOLTZ) {
-        R kr = k * (r2 * rinv);
-        R s, c;
-        if constexpr (sizeof(R) == 4) sincos_2pi(kr * 0.159154943091895335769f, s, c);
-        else sincos(kr, &s, &c);
-        // SLP: G = e^{-ikr}/(4 pi r) = (c - i s)/(4 pi r)
-        R gs = g * ws;
-        sr += gs * c;
-        si -= gs * s;
-        // DLP: dG/dr (r.n)/r = -(1 + ikr) e^{-ikr} / (4 pi r^2) * (r.n)/r
-        R f = -g * rinv * rdn * wd;
-        dr += f * (c + kr * s);
-        di += f * (kr * c - s);
-    } else {
-        sr += g * ws;
-        dr -= g * rinv * rdn * wd;
-    }
-}
-
 // k-independent part of one quadrature point (frequency batches): the
 // distance and the SLP and DLP factors of eval_point
 template <typename R>

@@ -518,11 +518,12 @@ nihu_gb_status nihu_gb_mesh_create(nihu_gb_ctx *ctx, const double *nodes, int64_
     m->dm.n = (int)n_elems;
     const int64_t n = std::max<int64_t>(n_elems, 1);
     struct Req { void **p; size_t bytes; };
-    void *corners, *center, *size, *nc, *chi, *clo, *p0, *pts32, *pts64, *dyn42;
+    void *corners, *center, *size, *nc, *chi, *clo, *p0, *pts32, *pts64, *dyn42, *nid;
     Req reqs[] = {{&corners, sizeof(double) * 12 * n}, {&center, sizeof(double) * 3 * n}, {&size, sizeof(double) * n},
                   {&nc, sizeof(int8_t) * n}, {&chi, sizeof(float4) * n}, {&clo, sizeof(float4) * n},
                   {&p0, sizeof(float4) * n}, {&pts32, sizeof(float4) * 2 * 2 * SLOTS * n},
-                  {&pts64, sizeof(double) * 8 * 2 * SLOTS * n}, {&dyn42, sizeof(Pt4) * 42 * n}};
+                  {&pts64, sizeof(double) * 8 * 2 * SLOTS * n}, {&dyn42, sizeof(Pt4) * 42 * n},
+                  {&nid, sizeof(int4) * n}};
     for (auto &r : reqs) {
         nihu_gb_status st = dmalloc(ctx, r.bytes, r.p);
         if (st) { nihu_gb_mesh_destroy(m); return st; }
@@ -538,6 +539,7 @@ nihu_gb_status nihu_gb_mesh_create(nihu_gb_ctx *ctx, const double *nodes, int64_
     m->dm.pts32 = (float4 *)pts32;
     m->dm.pts64 = (double *)pts64;
     m->dm.dyn42 = (Pt4 *)dyn42;
+    m->dm.nid = (int4 *)nid;
     for (int64_t e = 0; e < n_elems; ++e) {
         int32_t t = elems[e * elem_cols];
         if (t == NIHU_GB_TRIA_1) m->dm.has_tria = 1;
@@ -926,6 +928,139 @@ nihu_gb_status nihu_gb_assemble_pairs(nihu_gb_ctx *ctx, const nihu_gb_mesh *test
     if (bad)
         return fail(ctx, NIHU_GB_ERR_INVALID_ARGUMENT,
                     std::string(fn) + ": pair " + std::to_string(bad - 1) + " has an index out of range");
+    return NIHU_GB_OK;
+}
+
+nihu_gb_status nihu_gb_assemble_galerkin(nihu_gb_ctx *ctx, const nihu_gb_mesh *test, const nihu_gb_mesh *trial,
+                                         int family, int ops, double k, double alpha_re, double alpha_im, int precision,
+                                         int dtype, void *out_slp, void *out_dlp, int64_t ld, int accumulate, int where)
+{
+    if (!ctx) return NIHU_GB_ERR_INVALID_ARGUMENT;
+    const std::string fn = "nihu_gb_assemble_galerkin";
+    if (!test || !trial || test->ctx != ctx || trial->ctx != ctx)
+        return fail(ctx, NIHU_GB_ERR_INVALID_ARGUMENT, fn + ": meshes must belong to the context");
+    if (family != NIHU_GB_HELMHOLTZ_3D && family != NIHU_GB_LAPLACE_3D)
+        return fail(ctx, NIHU_GB_ERR_INVALID_ARGUMENT, fn + ": unknown kernel family");
+    if (ops < 1 || ops > 3) return fail(ctx, NIHU_GB_ERR_INVALID_ARGUMENT, fn + ": ops must be SLP, DLP or both");
+    if (((ops & NIHU_GB_SLP) && !out_slp) || ((ops & NIHU_GB_DLP) && !out_dlp))
+        return fail(ctx, NIHU_GB_ERR_INVALID_ARGUMENT, fn + ": missing output buffer");
+    if (!valid_dtype(dtype) || !valid_where(where) || (precision != 0 && precision != 1))
+        return fail(ctx, NIHU_GB_ERR_INVALID_ARGUMENT, fn + ": bad dtype, precision or location");
+    if (ld < std::max<int64_t>(test->n, 1)) return fail(ctx, NIHU_GB_ERR_INVALID_ARGUMENT, fn + ": ld < rows");
+    if (!std::isfinite(k) || !std::isfinite(alpha_re) || !std::isfinite(alpha_im))
+        return fail(ctx, NIHU_GB_ERR_INVALID_ARGUMENT, fn + ": non-finite wave number or scale");
+    const bool same = test == trial;
+    if (same && test->dm.has_quad)
+        return fail(ctx, NIHU_GB_ERR_INVALID_ARGUMENT,
+                    fn + ": Galerkin singular quadrature: constant triangles only (elements of one mesh share nodes)");
+    if (test->n == 0 || trial->n == 0) return NIHU_GB_OK;
+    cudaSetDevice(ctx->device);
+    NearList *nl = nullptr;
+    nihu_gb_status st = get_near(ctx, test, trial, &nl);
+    if (st) return st;
+    CK(prepare_galerkin(ctx->stream));
+    GalArgs g;
+    g.test = test->dm;
+    g.trial = trial->dm;
+    g.same_mesh = same;
+    g.family = family;
+    g.ops = ops;
+    g.k = family == NIHU_GB_HELMHOLTZ_3D ? k : 0.0;
+    g.k32 = (float)g.k;
+    g.alpha_re = alpha_re;
+    g.alpha_im = alpha_im;
+    g.alpha_re32 = (float)alpha_re;
+    g.alpha_im32 = (float)alpha_im;
+    g.precision = precision;
+    g.dtype = dtype;
+    g.accumulate = accumulate ? 1 : 0;
+    g.extra_cap = (int)std::min<int64_t>(std::max<int64_t>(1024, 8 * trial->n), 1 << 26);
+    void *extra, *flags;
+    if ((st = scratch(ctx, "gal_extra", sizeof(int2) * g.extra_cap, &extra))) return st;
+    if ((st = scratch(ctx, "gal_flags", 16, &flags))) return st;
+    g.extra = (int2 *)extra;
+    g.n_extra = (unsigned int *)flags;
+    g.err = (int *)flags + 1;
+    CK(cudaMemsetAsync(g.err, 0, sizeof(int), ctx->stream));
+    const int64_t M = test->n, N = trial->n;
+    auto panel = [&](void *o0, void *o1, int64_t pld, int j0, int j1) -> nihu_gb_status {
+        g.out_s = o0;
+        g.out_d = o1;
+        g.ld = pld;
+        g.j0 = j0;
+        g.j1 = j1;
+        cudaError_t e = cudaMemsetAsync(g.n_extra, 0, sizeof(unsigned int), ctx->stream);
+        if (e == cudaSuccess) e = cudaEventRecord(ctx->ev_fork, ctx->stream);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(ctx->aux_stream, ctx->ev_fork, 0);
+        if (e != cudaSuccess) return cuda_fail(ctx, e, "fork");
+        {
+            Phase ph(ctx, "galerkin_near", ctx->aux_stream);
+            e = launch_galerkin_near(g, *nl, 0, nl->nnz + (j1 - j0), ctx->aux_stream);
+        }
+        if (e != cudaSuccess) return cuda_fail(ctx, e, "galerkin_near launch");
+        if ((e = cudaEventRecord(ctx->ev_join, ctx->aux_stream)) != cudaSuccess) return cuda_fail(ctx, e, "join");
+        {
+            Phase ph(ctx, "galerkin_regular");
+            e = launch_galerkin_regular(g, ctx->stream);
+        }
+        if (e != cudaSuccess) return cuda_fail(ctx, e, "galerkin_regular launch");
+        if ((e = cudaStreamWaitEvent(ctx->stream, ctx->ev_join, 0)) != cudaSuccess) return cuda_fail(ctx, e, "join");
+        {
+            // pairs beyond 1.5 D sharing a node (none on regular meshes)
+            Phase ph(ctx, "galerkin_extra");
+            e = launch_galerkin_near(g, *nl, 1, std::min<int64_t>(g.extra_cap, 4 * 1024), ctx->stream);
+        }
+        if (e != cudaSuccess) return cuda_fail(ctx, e, "galerkin_extra launch");
+        ctx->launches += 3;
+        return NIHU_GB_OK;
+    };
+    if (where == NIHU_GB_DEVICE) {
+        if ((st = panel(out_slp, out_dlp, ld, 0, (int)N))) return st;
+    } else {
+        st = assemble_host_panels(ctx, M, N, dtype, (ops & NIHU_GB_SLP) ? out_slp : nullptr,
+                                  (ops & NIHU_GB_DLP) ? out_dlp : nullptr, ld, accumulate, panel);
+        if (st) return st;
+    }
+    int err = 0;
+    CK(cudaMemcpyAsync(&err, g.err, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    if ((st = check_flag(ctx))) return st;
+    if (err)
+        return fail(ctx, NIHU_GB_ERR_RUNTIME, fn + ": more node-sharing pairs beyond 1.5 D than the list holds");
+    return NIHU_GB_OK;
+}
+
+nihu_gb_status nihu_gb_add_mass(nihu_gb_ctx *ctx, const nihu_gb_mesh *mesh, double alpha_re, double alpha_im, int dtype,
+                                void *out, int64_t ld, int where)
+{
+    if (!ctx) return NIHU_GB_ERR_INVALID_ARGUMENT;
+    if (!mesh || mesh->ctx != ctx || !out || !valid_dtype(dtype) || !valid_where(where) ||
+        ld < std::max<int64_t>(mesh->n, 1))
+        return fail(ctx, NIHU_GB_ERR_INVALID_ARGUMENT, "nihu_gb_add_mass: bad argument");
+    const int64_t n = mesh->n;
+    if (n == 0) return NIHU_GB_OK;
+    cudaSetDevice(ctx->device);
+    if (where == NIHU_GB_DEVICE) {
+        CK(launch_add_mass((int)n, mesh->dm.pts64, alpha_re, alpha_im, dtype, out, ld, ctx->stream));
+        ctx->launches += 1;
+        return sync(ctx);
+    }
+    std::vector<double> w((size_t)n);
+    // strided copy of the one-point weights (w J of slot 0, parity 0)
+    CK(cudaMemcpy2DAsync(w.data(), sizeof(double), mesh->dm.pts64 + 3, 8 * 2 * SLOTS * sizeof(double), sizeof(double),
+                         n, cudaMemcpyDeviceToHost, ctx->stream));
+    nihu_gb_status st = sync(ctx);
+    if (st) return st;
+    for (int64_t i = 0; i < n; ++i) {
+        if (dtype == NIHU_GB_C64) {
+            float *p = (float *)out + 2 * (i * ld + i);
+            p[0] += (float)(alpha_re * w[i]);
+            p[1] += (float)(alpha_im * w[i]);
+        } else {
+            double *p = (double *)out + 2 * (i * ld + i);
+            p[0] += alpha_re * w[i];
+            p[1] += alpha_im * w[i];
+        }
+    }
     return NIHU_GB_OK;
 }
 

@@ -58,6 +58,9 @@ struct DevMesh {
     // triangles: the 42 points of the degree-14 rule used by the nearly
     // singular dynamic part, (y, w*J) in FP64; [n][42] (unused for quads)
     struct Pt4 *dyn42 = nullptr;
+    // corner node indices (-1 for the 4th of a triangle): element adjacency
+    // of the Galerkin singular quadratures
+    int4 *nid = nullptr;
 };
 
 // number of points of a regular level for (trial corners, test complexity)
@@ -75,6 +78,39 @@ __device__ __forceinline__ void sincos_2pi(float t, float &s, float &c)
 {
     float f = t - rintf(t);
     __sincosf(6.28318530717958647692f * f, &s, &c);
+}
+
+// one quadrature point of the SLP (weight ws) and DLP (weight wd) kernels at
+// r_vec = (rx, ry, rz) with trial weight w J and unit normal n, sharing 1/r and
+// one sincos (Helmholtz: e^{-ikr} convention)
+template <int FAM, typename R>
+__device__ __forceinline__ void eval_point(R rx, R ry, R rz, R wj, R nx, R ny, R nz, R k, R ws, R wd, R &sr,
+                                           R &si, R &dr, R &di)
+{
+    constexpr R INV4PI = R(1.0 / (4.0 * 3.14159265358979323846));
+    R r2 = rx * rx + ry * ry + rz * rz;
+    R rinv;
+    if constexpr (sizeof(R) == 4) rinv = rsqrtf(r2);
+    else rinv = rsqrt(r2);
+    R g = wj * rinv * INV4PI;
+    R rdn = (rx * nx + ry * ny + rz * nz) * rinv;
+    if constexpr (FAM == FAM_HELMHOLTZ) {
+        R kr = k * (r2 * rinv);
+        R s, c;
+        if constexpr (sizeof(R) == 4) sincos_2pi(kr * 0.159154943091895335769f, s, c);
+        else sincos(kr, &s, &c);
+        // SLP: G = e^{-ikr}/(4 pi r) = (c - i s)/(4 pi r)
+        R gs = g * ws;
+        sr += gs * c;
+        si -= gs * s;
+        // DLP: dG/dr (r.n)/r = -(1 + ikr) e^{-ikr} / (4 pi r^2) * (r.n)/r
+        R f = -g * rinv * rdn * wd;
+        dr += f * (c + kr * s);
+        di += f * (kr * c - s);
+    } else {
+        sr += g * ws;
+        dr -= g * rinv * rdn * wd;
+    }
 }
 
 struct cd { double re, im; };

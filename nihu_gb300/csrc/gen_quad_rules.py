@@ -11,8 +11,8 @@ Two families are produced, both to full double precision:
   (:136-151 line, :186-202 quad tensor product).
 
 * Dunavant (1985) symmetric rules on the reference triangle (0,0),(1,0),(0,1)
-  for polynomial degrees 0..8 and 14 (nihu/core/gaussian_quadrature.hpp:209-513
-  uses the same published rules; point counts 1,1,3,4,6,7,12,13,16 and 42).  Each
+  for polynomial degrees 0..9 and 14 (nihu/core/gaussian_quadrature.hpp:209-513
+  uses the same published rules; point counts 1,1,3,4,6,7,12,13,16,19 and 42).  Each
   rule is described by its orbit structure (centroid S3, S21 orbits
   (a, a, 1-2a), S111 orbits (a, b, 1-a-b)).  The orbit parameters are seeded
   with 4-6 significant digits of the published 1985 values and refined by
@@ -76,6 +76,8 @@ DUNAVANT_SEEDS = {
         ("S111", 0.048690, 0.312865, 0.077114)],
     8: [("S3", 0.144316), ("S21", 0.459293, 0.0950916), ("S21", 0.170569, 0.103217),
         ("S21", 0.0505472, 0.0324585), ("S111", 0.00839478, 0.263113, 0.0272303)],
+    9: [("S3", 0.0971358), ("S21", 0.489682, 0.0313347), ("S21", 0.437090, 0.0778275),
+        ("S21", 0.188204, 0.0796477), ("S21", 0.0447295, 0.0255777), ("S111", 0.0368384, 0.221963, 0.0432835)],
     14: [("S21", 0.488964, 0.0218836), ("S21", 0.417645, 0.0327884),
          ("S21", 0.273478, 0.0517741), ("S21", 0.177206, 0.0421626),
          ("S21", 0.0617999, 0.0144337), ("S21", 0.0193910, 0.00492340),

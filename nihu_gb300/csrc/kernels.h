@@ -143,6 +143,38 @@ struct PairArgs {
 };
 cudaError_t launch_assemble_pairs(const PairArgs &a, cudaStream_t s);
 
+// assemble_galerkin.cu ----------------------------------------------------
+// Galerkin SLP / DLP (constant elements) of columns [j0, j1), conventions of
+// RegularArgs; extra / n_extra / extra_cap: device list of the pairs beyond
+// 1.5 D that share a node, err receives -1 if it overflows
+struct GalArgs {
+    DevMesh test, trial;
+    int same_mesh = 0;
+    int family = 0, ops = 0;
+    double k = 0.0;
+    float k32 = 0.0f;
+    double alpha_re = 1.0, alpha_im = 0.0;
+    float alpha_re32 = 1.0f, alpha_im32 = 0.0f;
+    int precision = 0, dtype = 0;
+    void *out_s = nullptr, *out_d = nullptr;
+    int64_t ld = 0;
+    int j0 = 0, j1 = 0;
+    int accumulate = 0;
+    int2 *extra = nullptr;
+    unsigned int *n_extra = nullptr;
+    int extra_cap = 0;
+    int *err = nullptr;
+};
+// the singular Galerkin rules into device memory (once per device)
+cudaError_t prepare_galerkin(cudaStream_t s);
+cudaError_t launch_galerkin_regular(const GalArgs &a, cudaStream_t s);
+// self pairs and the nearly singular list (extra = 0) or the extra list
+// (extra = 1, at most max_items entries)
+cudaError_t launch_galerkin_near(const GalArgs &a, const NearList &near, int extra, int64_t max_items, cudaStream_t s);
+// out(i, i) += alpha * area_i (the Galerkin identity of constant elements)
+cudaError_t launch_add_mass(int n, const double *pts64, double are, double aim, int dtype, void *out, int64_t ld,
+                            cudaStream_t s);
+
 // linalg.cu ---------------------------------------------------------------
 cudaError_t launch_add_identity(int n, double are, double aim, int dtype, void *out, int64_t ld, cudaStream_t s);
 

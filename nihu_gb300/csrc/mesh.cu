@@ -22,6 +22,7 @@ __global__ void k_mesh_geometry(const double *__restrict__ nodes, int64_t n_node
         for (int d = 0; d < 3; ++d) el.c[a][d] = nodes[3 * (int64_t)nd + d];
     }
     m.nc[e] = (int8_t)nc;
+    m.nid[e] = make_int4(row[1], row[2], row[3], nc == 4 ? row[4] : -1);
     double *cdst = m.corners + 12 * (int64_t)e;
     for (int a = 0; a < 4; ++a)
         for (int d = 0; d < 3; ++d) cdst[3 * a + d] = el.c[a][d];

@@ -1,0 +1,160 @@
+"""Galerkin formalism on the GPU (nihu_gb_assemble_galerkin) against the FP64
+oracle's Galerkin restatement, through the C ABI and the NiHu-shaped Python
+front end.
+
+Tolerances (every entry, normwise max |A_gpu - A_oracle| / max |A_oracle|):
+FP64 regular quadrature 1e-11, FP32 1e-5.  Matched (face / edge / corner)
+and nearly singular pairs are FP64 in both modes.
+"""
+import numpy as np
+import pytest
+
+import nihu_gb300 as g
+from nihu_gb300 import meshes
+
+pytestmark = pytest.mark.gpu
+
+TRIA = g.TRIA_1
+
+
+def rel_norm(a, b):
+    return np.abs(a - b).max() / np.abs(b).max()
+
+
+def two_spheres():
+    """Concentric spheres of radius 1 and 1.08 in one mesh: unmatched pairs at
+    d/D < 1.5 between them (the degree-6 / 8 product rules) beside the
+    matched pairs within each."""
+    n1, e1 = meshes.icosphere(2)
+    n2, e2 = meshes.icosphere(2)
+    e2 = e2.copy()
+    e2[:, 1:4] += len(n1)
+    return np.vstack([n1, 1.08 * n2]), np.vstack([e1, e2])
+
+
+def graded_fan():
+    """A large triangle and small ones sharing its corner node 0: node-sharing
+    pairs beyond 1.5 D (by the small trial element's size) and within it."""
+    nodes = np.array([[0, 0, 0], [4.0, 0, 0], [0, 4.0, 0.3], [-0.1, 0, 0.02], [0, -0.1, 0.03], [-0.08, 0.06, -0.01]])
+    elems = np.array([[TRIA, 0, 1, 2, -1], [TRIA, 0, 3, 4, -1], [TRIA, 0, 5, 3, -1], [TRIA, 3, 1, 4, -1]])
+    return nodes, elems.astype(np.int32)
+
+
+MESHES = {"ico2": lambda: meshes.icosphere(2), "ico3": lambda: meshes.icosphere(3), "two": two_spheres,
+          "fan": graded_fan}
+_cache, _ocache = {}, {}
+
+
+def get_mesh(name):
+    if name not in _cache:
+        _cache[name] = MESHES[name]()
+    return _cache[name]
+
+
+def oracle_g(oracle, name, family, op, k):
+    key = (name, family, op, k)
+    if key not in _ocache:
+        m = get_mesh(name)
+        _ocache[key] = oracle.assemble_galerkin(m, m, family, op, k, threads=8)
+    return _ocache[key]
+
+
+def gpu_galerkin(ctx, mesh, family, ops, k, precision, dtype, alpha=1.0, test_mesh=None):
+    L = g.lib()
+    trial = g.api.DeviceMesh(ctx, *mesh)
+    test = trial if test_mesh is None else g.api.DeviceMesh(ctx, *test_mesh)
+    cdt = np.complex64 if dtype == g.C64 else np.complex128
+    outs = {op: np.zeros((test.n, trial.n), cdt, order="F") for op in (g.SLP, g.DLP) if ops & op}
+    alpha = complex(alpha)
+    ctx.check(L.nihu_gb_assemble_galerkin(ctx.handle, test.handle, trial.handle, family, ops, k, alpha.real,
+                                          alpha.imag, precision, dtype,
+                                          outs[g.SLP].ctypes.data if g.SLP in outs else None,
+                                          outs[g.DLP].ctypes.data if g.DLP in outs else None, test.n, 0, g.HOST))
+    return outs
+
+
+@pytest.mark.parametrize("name", ["ico2", "ico3", "two", "fan"])
+@pytest.mark.parametrize("family,k", [(g.HELMHOLTZ_3D, 1.3), (g.HELMHOLTZ_3D, 4.0), (g.LAPLACE_3D, 0.0)])
+@pytest.mark.parametrize("precision,tol", [(g.REGULAR_FP64, 1e-11), (g.REGULAR_FP32, 1e-5)])
+def test_galerkin_against_oracle(gpu_ctx, oracle, name, family, k, precision, tol):
+    outs = gpu_galerkin(gpu_ctx, get_mesh(name), family, g.SLP | g.DLP, k, precision,
+                        g.C128 if precision == g.REGULAR_FP64 else g.C64)
+    for op, oop in ((g.SLP, oracle.SLP), (g.DLP, oracle.DLP)):
+        ref = oracle_g(oracle, name, family, oop, k)
+        err = rel_norm(outs[op].astype(np.complex128), ref)
+        assert err <= tol, (name, op, err)
+
+
+def test_pair_classes_are_all_exercised(oracle):
+    """The meshes above hold every Galerkin pair class."""
+    n, e = get_mesh("two")
+    kind = oracle.classify((n, e), (n, e))
+    # unmatched nearly singular pairs exist between the two spheres
+    between = kind[:320, 320:]
+    assert (between == -2).any()
+    fn, fe = get_mesh("fan")
+    cen = np.array([fn[r[1:4]].mean(0) for r in fe])
+    size = np.array([np.mean([np.linalg.norm(fn[r[1 + a]] - fn[r[1 + (a + 1) % 3]]) for a in range(3)]) for r in fe])
+    # element 0 (large) as test against element 1 (small) as trial: shares node 0, d/D > 1.5
+    assert np.linalg.norm(cen[1] - cen[0]) / size[1] > 1.5
+
+
+def test_field_mesh_with_quads(gpu_ctx, oracle):
+    """A separate test mesh (quads of a cylinder around the sphere): no
+    singular rules, the product rules with the mixed complexity."""
+    surf = get_mesh("ico2")
+    field = meshes.cylinder(8, 4, 2, radius=1.4, length=3.0)
+    k = 2.0
+    outs = gpu_galerkin(gpu_ctx, surf, g.HELMHOLTZ_3D, g.SLP | g.DLP, k, g.REGULAR_FP64, g.C128, test_mesh=field)
+    for op, oop in ((g.SLP, oracle.SLP), (g.DLP, oracle.DLP)):
+        ref = oracle.assemble_galerkin(field, surf, oracle.HELMHOLTZ, oop, k, same_mesh=False, threads=8)
+        assert rel_norm(outs[op], ref) <= 1e-11
+
+
+def test_scale_and_accumulate(gpu_ctx, oracle):
+    mesh = get_mesh("ico2")
+    alpha = -0.5 + 1.5j
+    outs = gpu_galerkin(gpu_ctx, mesh, g.HELMHOLTZ_3D, g.DLP, 1.3, g.REGULAR_FP64, g.C128, alpha=alpha)
+    ref = alpha * oracle_g(oracle, "ico2", g.HELMHOLTZ_3D, oracle.DLP, 1.3)
+    assert rel_norm(outs[g.DLP], ref) <= 1e-11
+
+
+def test_pulsating_sphere_through_the_operator_algebra(gpu_ctx, oracle):
+    """nihu/test/stallone_unit/helmholtz_3d_pulsating_sphere_test.cpp:40-70 with
+    the Python front end: I, L, M << test_space * Op[trial_space] (Galerkin),
+    (M - I/2) p = L q."""
+    nodes, elems = get_mesh("ico3")
+    mesh = g.create_mesh(nodes, elems)
+    sp = g.constant_view(mesh)
+    n = sp.get_num_dofs()
+    k = 1.0
+    I = np.zeros((n, n), np.complex128)
+    L = np.zeros((n, n), np.complex128)
+    M = np.zeros((n, n), np.complex128)
+    (sp * g.identity_integral_operator()[sp]).eval_into(I, ctx=gpu_ctx)
+    (sp * g.create_integral_operator(g.helmholtz_3d_SLP_kernel(k))[sp]).eval_into(L, precision="fp64", ctx=gpu_ctx)
+    (sp * g.create_integral_operator(g.helmholtz_3d_DLP_kernel(k))[sp]).eval_into(M, precision="fp64", ctx=gpu_ctx)
+    p = np.linalg.solve(M - 0.5 * I, L @ np.ones(n))
+    pa = -1.0 / (1.0 + 1j * k)
+    assert np.abs(p - pa).max() / abs(pa) < 5e-3
+    Lr = oracle_g(oracle, "ico3", oracle.HELMHOLTZ, oracle.SLP, k)
+    Mr = oracle_g(oracle, "ico3", oracle.HELMHOLTZ, oracle.DLP, k)
+    pr = np.linalg.solve(Mr - 0.5 * np.diag(mesh.areas()), Lr @ np.ones(n))
+    assert np.abs(p - pr).max() / np.abs(pr).max() <= 1e-9
+    assert np.allclose(np.diag(I).real, mesh.areas(), rtol=1e-12)
+
+
+def test_mass_matrix_entry_point(gpu_ctx):
+    L = g.lib()
+    mesh = g.create_mesh(*get_mesh("ico2"))
+    dm = mesh.device(gpu_ctx)
+    n = mesh.num_elements
+    out = np.zeros((n, n), np.complex64, order="F")
+    gpu_ctx.check(L.nihu_gb_add_mass(gpu_ctx.handle, dm.handle, 2.0, 0.5, g.C64, out.ctypes.data, n, g.HOST))
+    assert np.allclose(np.diag(out), (2.0 + 0.5j) * mesh.areas(), rtol=1e-6)
+    assert np.count_nonzero(out) == n
+
+
+def test_quads_on_one_mesh_are_refused(gpu_ctx):
+    with pytest.raises(g.InvalidArgumentError):
+        gpu_galerkin(gpu_ctx, meshes.cylinder(8, 3, 1), g.HELMHOLTZ_3D, g.SLP, 1.0, g.REGULAR_FP64, g.C128)

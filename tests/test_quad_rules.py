@@ -37,7 +37,7 @@ def test_gauss_legendre_exact(n):
         assert abs(np.sum(r[:, 1] * r[:, 0] ** p) - exact) < 1e-14
 
 
-@pytest.mark.parametrize("degree,npts", [(0, 1), (1, 1), (2, 3), (3, 4), (4, 6), (5, 7), (6, 12), (7, 13), (8, 16), (14, 42)])
+@pytest.mark.parametrize("degree,npts", [(0, 1), (1, 1), (2, 3), (3, 4), (4, 6), (5, 7), (6, 12), (7, 13), (8, 16), (9, 19), (14, 42)])
 def test_dunavant_exact(degree, npts):
     r = tri(degree)
     assert len(r) == npts
