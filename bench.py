@@ -52,12 +52,12 @@ def parse():
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-solve", action="store_true")
     p.add_argument("--no-cpu", action="store_true")
-    p.add_argument("--config", default="large", choices=["large", "small", "multirhs", "sweep", "serve", "bm", "p2p"],
+    p.add_argument("--config", default="large", choices=["large", "small", "multirhs", "sweep", "serve", "bm", "p2p", "galerkin"],
                    help="large: the headline line (20480-triangle icosphere); multirhs: the 40000-quad "
                         "cylinder with 64 plane waves; sweep: 256 wave numbers on three icospheres; serve: "
                         "the served stream; bm: the Burton-Miller system on the 20480-triangle icosphere; "
-                        "p2p: the Burton-Miller near field of a box partition of the same mesh "
-                        "(each a separate line)")
+                        "p2p: the Burton-Miller near field of a box partition of the same mesh; "
+                        "galerkin: Galerkin SLP and DLP on the same mesh (each a separate line)")
     p.add_argument("--requests", type=int, default=1000, help="serve: requests in the stream")
     p.add_argument("--quantum", type=int, default=8, help="serve: GMRES steps per system per round")
     p.add_argument("--plain-sample", type=int, default=4, help="serve: requests per mesh timed on the plain path")
@@ -1183,6 +1183,108 @@ def run_p2p(args):
     print(json.dumps(out), flush=True)
 
 
+def run_galerkin(args):
+    """Galerkin SLP and DLP on the headline mesh (icosphere s=5, 20480
+    triangles, Helmholtz, k = 5, complex64, FP32 regular quadrature: the
+    product rules, the singular Galerkin rules of the face, edge and corner
+    pairs and the unmatched close pairs) into device memory.  Metric: entries per second
+    (SLP and DLP counted separately)."""
+    import torch
+
+    import nihu_gb300 as g
+    from nihu_gb300 import meshes
+    from nihu_gb300 import _capi as C
+
+    mesh = meshes.icosphere(SUBDIV)
+    nodes, elems = mesh
+    n = len(elems)
+    k = K_WAVE
+    ctx = g.Context(0)
+    L = g.lib()
+    stream = torch.cuda.ExternalStream(ctx.stream)
+    dm = g.api.DeviceMesh(ctx, nodes, elems)
+    mat_bytes = n * n * 8
+    ps, pd = ctypes.c_void_p(), ctypes.c_void_p()
+    ctx.check(L.nihu_gb_device_alloc(ctx.handle, mat_bytes, ctypes.byref(ps)))
+    ctx.check(L.nihu_gb_device_alloc(ctx.handle, mat_bytes, ctypes.byref(pd)))
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+
+    def step():
+        ctx.check(L.nihu_gb_assemble_galerkin(ctx.handle, dm.handle, dm.handle, C.HELMHOLTZ_3D, C.SLP | C.DLP, k, 1.0,
+                                              0.0, C.REGULAR_FP32, C.C64, ps, pd, n, 0, C.DEVICE))
+
+    for _ in range(max(3, args.warmup)):
+        step()
+    counts = (ctypes.c_int64 * 11)()
+    ctx.check(L.nihu_gb_pair_statistics(ctx.handle, dm.handle, dm.handle, counts))
+    counts = np.array(list(counts))
+    n_regular = int(counts[2:].sum())
+    ctx.set_profiling(True)
+    ctx.profile_reset()
+    clocks = ClockSampler(0)
+    clocks.start()
+    launches0 = ctx.launch_count
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    torch.cuda.synchronize()
+    for s_ in range(args.steps):
+        flush.fill_(s_ & 0xFF)
+        torch.cuda.synchronize()
+        ev[s_][0].record(stream)
+        step()
+        ev[s_][1].record(stream)
+    torch.cuda.synchronize()
+    launches = ctx.launch_count - launches0
+    clk = clocks.stop()
+    prof = ctx.profile()
+    ctx.set_profiling(False)
+    ms = float(np.mean([a_.elapsed_time(b_) for a_, b_ in ev]))
+    entries = 2.0 * n * n
+    reg_ms, reg_n = prof.get("galerkin_regular", (0.0, 0))
+    reg_avg = reg_ms / max(reg_n, 1)
+    alg_bytes = 16.0 * n_regular
+    peak, peak_kind = measured_peaks()
+    achieved = alg_bytes / (reg_avg / 1e3) / 1e9
+    out = {
+        "metric": "Galerkin BEM entries/s", "impl": "ours", "value": entries / (ms / 1e3), "unit": "entries/s",
+        "n_gpus": 1, "steps": args.steps, "warmup": max(3, args.warmup), "ms_per_step": ms,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "fp32 (regular product rules, singular Galerkin rules, unmatched close pairs); complex64 storage",
+        "data": "synthetic (icosphere mesh generated in-process)",
+        "config": {"workload": "icosphere s=5 (%d flat constant triangles), Helmholtz 3D SLP+DLP Galerkin, k=5" % n,
+                   "n_elements": n, "entries_per_step": int(entries),
+                   "l2": "256 MB written between timed steps (L2 flushed); outputs 6.7 GB >> 129 MB L2"},
+        "gpu_launches": int(launches), "clocks": clk,
+        "roofline": {"kernel": "k_galerkin_regular (assemble_galerkin.cu)", "bound": "hbm", "achieved": achieved,
+                     "peak": peak, "unit": "GB/s", "frac": achieved / peak, "traffic": None,
+                     "peak_source": "%s (MEASURED_PEAKS.json hbm_gbs)" % peak_kind,
+                     "algorithmic_bytes_per_launch": alg_bytes, "avg_launch_ms": reg_avg,
+                     "regular_pairs": n_regular, "near_pairs": int(counts[1]), "self_pairs": int(counts[0])},
+        "phases": {kk: {"ms_per_step": v[0] / args.steps, "launches": v[1]} for kk, v in prof.items()},
+    }
+    L.nihu_gb_device_free(ctx.handle, ps)
+    L.nihu_gb_device_free(ctx.handle, pd)
+    dm.close()
+    ctx.close()
+    if not args.no_cpu:
+        from oracle import oracle
+        oracle.build()
+        threads = os.cpu_count() or 1
+        t0 = time.perf_counter()
+        for op in (oracle.SLP, oracle.DLP):
+            oracle.assemble_galerkin(mesh, mesh, oracle.HELMHOLTZ, op, k, rows=(0, 1))
+        per_row = time.perf_counter() - t0
+        rows = int(max(threads, min(4096, args.cpu_seconds * threads / max(per_row, 1e-6))))
+        rows = max(threads, (rows // threads) * threads)
+        t0 = time.perf_counter()
+        for op in (oracle.SLP, oracle.DLP):
+            oracle.assemble_galerkin(mesh, mesh, oracle.HELMHOLTZ, op, k, rows=(0, rows), threads=threads)
+        el = time.perf_counter() - t0
+        out["cpu_baseline"] = {"value": 2.0 * rows * n / el, "unit": "entries/s", "cores": threads, "kind": "port",
+                               "sample": "%d full rows x %d columns x (SLP, DLP), FP64 Galerkin oracle, %.1f s"
+                                         % (rows, n, el)}
+    print(json.dumps(out), flush=True)
+
+
 def main():
     args = parse()
     if args.config == "multirhs":
@@ -1202,6 +1304,9 @@ def main():
         return
     if args.config == "p2p":
         run_p2p(args)
+        return
+    if args.config == "galerkin":
+        run_galerkin(args)
         return
     if args.impl == "reference":
         run_reference(args)

@@ -17,11 +17,14 @@
 // Work layout: k_galerkin_regular (FP32 default / FP64) owns the pairs at
 // d/D >= 1.5 exactly as the collocation kernel does, with the test element's
 // points in the same rule as the trial element's (a far pair is the
-// collocation entry times the test element's area); k_galerkin_near (FP64,
-// one warp per pair, lanes over the rule's points) owns the self pairs, the
-// nearly singular list (d/D < 1.5: matched pairs, and unmatched ones with the
+// collocation entry times the test element's area); k_galerkin_near (one warp
+// per pair, lanes over the rule's points) owns the self pairs, the nearly
+// singular list (d/D < 1.5: matched pairs, and unmatched ones with the
 // degree-6/8 product rules) and the rare pairs beyond 1.5 D that still share
-// a node (collected by the regular kernel).
+// a node (collected by the regular kernel).  The near kernel follows the
+// regular quadrature's precision: FP64, or FP32 with r_vec formed from
+// vectors relative to the common node (matched pairs) or to the element
+// centres (unmatched pairs), which keeps FP32 relative accuracy as r -> 0.
 #include <algorithm>
 #include <mutex>
 #include <vector>
@@ -42,8 +45,11 @@ __host__ __device__ constexpr int gal_npts(int match) { return (match == 0 ? 2 :
 constexpr int GAL_TOTAL = gal_npts(0) + gal_npts(1) + gal_npts(2);
 
 // the singular rules, (test xi, eta, trial xi, eta, w) per point: corner
-// points first, then edge, then face
+// points first, then edge, then face; and in FP32 (test xi, eta, trial xi,
+// eta, w, trial xi - test xi, trial eta - test eta, 0), the differences formed
+// in FP64
 __device__ double g_gal_rule[GAL_TOTAL * 5];
+__device__ __align__(16) float g_gal_rule32[GAL_TOTAL * 8];
 
 __host__ __device__ constexpr int gal_offset(int match)
 {
@@ -103,6 +109,17 @@ static void gal_subdomain(int match, int sub, const double u[4], double &w, doub
     out[3] = a2 + b2;
 }
 
+// every Dunavant rule in FP32, (xi, eta, w) per point at the offsets of quad_rules.h
+struct TriF32 {
+    float v[NIHU_TRI_DATA_LEN];
+    constexpr TriF32() : v()
+    {
+        constexpr double d[NIHU_TRI_DATA_LEN] = NIHU_TRI_DATA;
+        for (int q = 0; q < NIHU_TRI_DATA_LEN; ++q) v[q] = (float)d[q];
+    }
+};
+__device__ constexpr TriF32 TRI_F32{};
+
 // host generation of the three rules (the Gauss nodes come from the device
 // tables' source, quad_rules.h)
 static std::vector<double> gal_rules()
@@ -148,7 +165,20 @@ cudaError_t prepare_galerkin(cudaStream_t s)
     std::lock_guard<std::mutex> lock(mu);
     if ((int)done.size() > dev && done[dev]) return cudaSuccess;
     static const std::vector<double> rules = gal_rules();
+    static const std::vector<float> rules32 = [] {
+        std::vector<float> f((size_t)GAL_TOTAL * 8, 0.0f);
+        for (size_t p = 0; p < (size_t)GAL_TOTAL; ++p) {
+            const double *q = rules.data() + 5 * p;
+            for (int c = 0; c < 5; ++c) f[8 * p + c] = (float)q[c];
+            f[8 * p + 5] = (float)(q[2] - q[0]);
+            f[8 * p + 6] = (float)(q[3] - q[1]);
+        }
+        return f;
+    }();
     e = cudaMemcpyToSymbolAsync(g_gal_rule, rules.data(), rules.size() * sizeof(double), 0, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess)
+        e = cudaMemcpyToSymbolAsync(g_gal_rule32, rules32.data(), rules32.size() * sizeof(float), 0,
+                                    cudaMemcpyHostToDevice, s);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
     if (e != cudaSuccess) return e;
     if ((int)done.size() <= dev) done.resize(dev + 1, 0);
@@ -229,7 +259,14 @@ __global__ void __launch_bounds__(GAL_THREADS) k_galerkin_regular(GalArgs a)
     for (int c = 0; c < ncols; ++c) {
         const int j = jb + c;
         int ind1, ind2;
-        const int shared = a.same_mesh ? common_nodes(inid, inc, s_nid[c], s_nc[c], ind1, ind2) : 0;
+        // elements can share a node only when their centres are closer than
+        // the sum of their centre-to-corner distances (< 2 D each): compare
+        // node ids only then
+        const float4 hj = s_hi[c];
+        const float ex0 = hj.x - ih.x, ex1 = hj.y - ih.y, ex2 = hj.z - ih.z;
+        const float reach = 2.0f * (rsqrtf(ih.w) + rsqrtf(hj.w));
+        const bool may_share = a.same_mesh && ex0 * ex0 + ex1 * ex1 + ex2 * ex2 <= 1.01f * reach * reach;
+        const int shared = may_share ? common_nodes(inid, inc, s_nid[c], s_nc[c], ind1, ind2) : 0;
         R sr = 0, si = 0, dr = 0, di = 0;
         bool done = false;
         if constexpr (sizeof(R) == 4) {
@@ -406,7 +443,70 @@ __global__ void __launch_bounds__(GAL_WARPS * 32) k_galerkin_near(GalArgs a, Nea
             }
         }
         double sr = 0, si = 0, dr = 0, di = 0;
-        if (match >= 0) {
+        if (match >= 0 && a.precision == 0) {
+            // FP32 regular quadrature: the matched pair's rule in FP32 too.  Both
+            // rotated triangles start at the common node P, so r_vec = y - x is
+            // formed from P-relative edge vectors and the rule's FP64-formed
+            // coordinate differences, keeping FP32 relative accuracy as r -> 0
+            int pt[3], pr[3];
+#pragma unroll
+            for (int q = 0; q < 3; ++q) {
+                pt[q] = match == 2 ? q : (ind1 + q) % 3;
+                pr[q] = match == 2 ? q : (match == 1 ? (ind2 + 1 + 3 - q) % 3 : (ind2 + q) % 3);
+            }
+            float at[3], bt[3], ar[3], br[3], nrm[3];
+            double o1[3], o2[3], nv[3];
+            for (int d = 0; d < 3; ++d) {
+                at[d] = (float)(te.c[pt[1]][d] - te.c[pt[0]][d]);
+                bt[d] = (float)(te.c[pt[2]][d] - te.c[pt[0]][d]);
+                ar[d] = (float)(re.c[pr[1]][d] - re.c[pr[0]][d]);
+                br[d] = (float)(re.c[pr[2]][d] - re.c[pr[0]][d]);
+                o1[d] = re.c[1][d] - re.c[0][d];
+                o2[d] = re.c[2][d] - re.c[0][d];
+            }
+            cross3(o1, o2, nv);  // the trial element's own orientation
+            const double Jr = norm3(nv);
+            for (int d = 0; d < 3; ++d) nrm[d] = (float)(nv[d] / Jr);
+            double tv1[3], tv2[3], tn[3];
+            for (int d = 0; d < 3; ++d) {
+                tv1[d] = te.c[1][d] - te.c[0][d];
+                tv2[d] = te.c[2][d] - te.c[0][d];
+            }
+            cross3(tv1, tv2, tn);
+            const float wscale = (float)(norm3(tn) * Jr / FOUR_PI);
+            const float kf = (float)k;
+            const float *rule = g_gal_rule32 + 8 * (size_t)gal_offset(match);
+            const int np = gal_npts(match);
+            float fsr = 0, fsi = 0, fdr = 0, fdi = 0;
+            for (int p = lane; p < np; p += 32) {
+                const float4 q0 = *reinterpret_cast<const float4 *>(rule + 8 * p);
+                const float4 q1 = *reinterpret_cast<const float4 *>(rule + 8 * p + 4);
+                // q0 = (xi1, xi2, eta1, eta2), q1 = (w, eta1 - xi1, eta2 - xi2, 0)
+                float rv[3];
+                for (int d = 0; d < 3; ++d) {
+                    if (match == 2) rv[d] = q1.y * at[d] + q1.z * bt[d];
+                    else if (match == 1) rv[d] = q1.y * at[d] + q0.w * br[d] - q0.y * bt[d];
+                    else rv[d] = q0.z * ar[d] + q0.w * br[d] - q0.x * at[d] - q0.y * bt[d];
+                }
+                const float r2 = rv[0] * rv[0] + rv[1] * rv[1] + rv[2] * rv[2];
+                const float rinv = rsqrtf(r2);
+                const float g = q1.x * wscale * rinv;  // w Jt Jr / (4 pi r)
+                float sn = 0.0f, cs = 1.0f, kr = 0.0f;
+                if (fam == FAM_HELMHOLTZ) {
+                    kr = kf * (r2 * rinv);
+                    sincosf(kr, &sn, &cs);
+                }
+                fsr += g * cs;
+                fsi -= g * sn;
+                const float f = -g * rinv * (rv[0] * nrm[0] + rv[1] * nrm[1] + rv[2] * nrm[2]) * rinv;
+                fdr += f * (cs + kr * sn);
+                fdi += f * (kr * cs - sn);
+            }
+            sr = fsr;
+            si = fsi;
+            dr = do_d ? fdr : 0.0f;
+            di = do_d ? fdi : 0.0f;
+        } else if (match >= 0) {
             // matched triangles (quads were refused by the host): flat elements
             int pt[3], pr[3];
 #pragma unroll
@@ -441,6 +541,76 @@ __global__ void __launch_bounds__(GAL_WARPS * 32) k_galerkin_near(GalArgs a, Nea
                 dr += kd.re * w;
                 di += kd.im * w;
             }
+        } else if (a.precision == 0 && te.nc == 3 && re.nc == 3) {
+            // unmatched close triangles under FP32 regular quadrature: the same
+            // product rules in FP32, points relative to the element centres
+            // (r_vec = (c_j - c_i) + (y - c_j) - (x - c_i), the first term in FP64)
+            double dc[3];
+            for (int d = 0; d < 3; ++d) dc[d] = a.trial.center[3 * (int64_t)j + d] - a.test.center[3 * (int64_t)i + d];
+            const double ratio = norm3(dc) / a.trial.size[j];
+            const int deg_s = ratio < 11.0 / 10.0 ? 6 : (ratio < T_S1 ? 4 : (ratio < T_S0 ? 2 : 0));
+            const int deg_d = ratio < 11.0 / 10.0 ? 8 : (ratio < T_NEAR ? 6 : (ratio < T_D1 ? 4 : (ratio < T_D0 ? 2 : 0)));
+            float c0[3], ti1[3], ti2[3], tj0[3], tj1[3], tj2[3], nrm[3];
+            double v1[3], v2[3], nt[3], w1[3], w2[3], nr[3];
+            for (int d = 0; d < 3; ++d) {
+                v1[d] = te.c[1][d] - te.c[0][d];
+                v2[d] = te.c[2][d] - te.c[0][d];
+                w1[d] = re.c[1][d] - re.c[0][d];
+                w2[d] = re.c[2][d] - re.c[0][d];
+            }
+            cross3(v1, v2, nt);
+            cross3(w1, w2, nr);
+            const double Jt = norm3(nt), Jr = norm3(nr);
+            for (int d = 0; d < 3; ++d) {
+                c0[d] = (float)dc[d];
+                // test corner 0 relative to its centre, trial corner 0 relative to its centre
+                ti1[d] = (float)v1[d];
+                ti2[d] = (float)v2[d];
+                tj0[d] = (float)(re.c[0][d] - a.trial.center[3 * (int64_t)j + d]);
+                tj1[d] = (float)w1[d];
+                tj2[d] = (float)w2[d];
+                nrm[d] = (float)(nr[d] / Jr);
+            }
+            float ti0[3];
+            for (int d = 0; d < 3; ++d) ti0[d] = (float)(te.c[0][d] - a.test.center[3 * (int64_t)i + d]);
+            const float kf = (float)k, wscale = (float)(Jt * Jr / FOUR_PI);
+            const bool one_pass = !do_s || !do_d || deg_s == deg_d;
+            float fsr = 0, fsi = 0, fdr = 0, fdi = 0;
+            for (int pass = 0; pass < (one_pass ? 1 : 2); ++pass) {
+                const bool use_s = one_pass ? do_s : pass == 0;
+                const bool use_d = one_pass ? do_d : pass == 1;
+                const int deg = use_s ? deg_s : deg_d;
+                const int npt = g_tri_npts[deg];
+                const float *rule = TRI_F32.v + 3 * g_tri_off[deg];
+                for (int p = lane; p < npt * npt; p += 32) {
+                    const float *qa = rule + 3 * (p / npt), *qb = rule + 3 * (p % npt);
+                    const float fxa = qa[0], fea = qa[1], wa = qa[2], fxb = qb[0], feb = qb[1], wb = qb[2];
+                    float rv[3];
+                    for (int d = 0; d < 3; ++d)
+                        rv[d] = c0[d] + (tj0[d] + fxb * tj1[d] + feb * tj2[d]) - (ti0[d] + fxa * ti1[d] + fea * ti2[d]);
+                    const float r2 = rv[0] * rv[0] + rv[1] * rv[1] + rv[2] * rv[2];
+                    const float rinv = rsqrtf(r2);
+                    const float g = wa * wb * wscale * rinv;
+                    float sn = 0.0f, cs = 1.0f, kr = 0.0f;
+                    if (fam == FAM_HELMHOLTZ) {
+                        kr = kf * (r2 * rinv);
+                        sincosf(kr, &sn, &cs);
+                    }
+                    if (use_s) {
+                        fsr += g * cs;
+                        fsi -= g * sn;
+                    }
+                    if (use_d) {
+                        const float f = -g * rinv * (rv[0] * nrm[0] + rv[1] * nrm[1] + rv[2] * nrm[2]) * rinv;
+                        fdr += f * (cs + kr * sn);
+                        fdi += f * (kr * cs - sn);
+                    }
+                }
+            }
+            sr = fsr;
+            si = fsi;
+            dr = fdr;
+            di = fdi;
         } else {
             // unmatched close pair: product of the degree C + interval(d/D)
             // rules (up to degree 8 + 1), the SLP and DLP degrees apart
@@ -528,8 +698,10 @@ cudaError_t launch_galerkin_near(const GalArgs &a, const NearList &near, int ext
     int dev = 0, sms = 148;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    // two 4-warp blocks per SM: the kernel runs beside the regular one and
+    // must leave it most of the register file
     const int64_t want = (max_items + GAL_WARPS - 1) / GAL_WARPS;
-    const int blocks = (int)std::max<int64_t>(1, std::min<int64_t>(want, 8 * (int64_t)sms));
+    const int blocks = (int)std::max<int64_t>(1, std::min<int64_t>(want, 2 * (int64_t)sms));
     if (a.dtype == 0) k_galerkin_near<float2><<<blocks, GAL_WARPS * 32, 0, s>>>(a, near, extra);
     else k_galerkin_near<double2><<<blocks, GAL_WARPS * 32, 0, s>>>(a, near, extra);
     return cudaGetLastError();

@@ -3,8 +3,8 @@ oracle's Galerkin restatement, through the C ABI and the NiHu-shaped Python
 front end.
 
 Tolerances (every entry, normwise max |A_gpu - A_oracle| / max |A_oracle|):
-FP64 regular quadrature 1e-11, FP32 1e-5.  Matched (face / edge / corner)
-and nearly singular pairs are FP64 in both modes.
+FP64 regular quadrature 1e-11, FP32 1e-5 (in FP32 mode the matched and
+nearly singular pairs are summed in FP32 as well).
 """
 import numpy as np
 import pytest
