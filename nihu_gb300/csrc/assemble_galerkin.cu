@@ -454,26 +454,43 @@ __global__ void __launch_bounds__(GAL_WARPS * 32) k_galerkin_near(GalArgs a, Nea
                 pt[q] = match == 2 ? q : (ind1 + q) % 3;
                 pr[q] = match == 2 ? q : (match == 1 ? (ind2 + 1 + 3 - q) % 3 : (ind2 + q) % 3);
             }
-            float at[3], bt[3], ar[3], br[3], nrm[3];
-            double o1[3], o2[3], nv[3];
+            // corners relative to the test element's corner 0 in FP32 (the
+            // differences in FP64); the rest of the set-up in FP32, so the
+            // warp's lanes do not repeat FP64 work on the narrow FP64 pipe
+            float tc[3][3], rc[3][3];
+#pragma unroll
+            for (int q = 0; q < 3; ++q)
+#pragma unroll
+                for (int d = 0; d < 3; ++d) {
+                    tc[q][d] = (float)(te.c[q][d] - te.c[0][d]);
+                    rc[q][d] = (float)(re.c[q][d] - te.c[0][d]);
+                }
+            auto pick = [](const float (&c)[3][3], int idx, int d) {
+                return idx == 0 ? c[0][d] : (idx == 1 ? c[1][d] : c[2][d]);
+            };
+            float at[3], bt[3], ar[3], br[3], nrm[3], ntv[3], nrv[3], e1[3], e2[3], f1[3], f2[3];
+#pragma unroll
             for (int d = 0; d < 3; ++d) {
-                at[d] = (float)(te.c[pt[1]][d] - te.c[pt[0]][d]);
-                bt[d] = (float)(te.c[pt[2]][d] - te.c[pt[0]][d]);
-                ar[d] = (float)(re.c[pr[1]][d] - re.c[pr[0]][d]);
-                br[d] = (float)(re.c[pr[2]][d] - re.c[pr[0]][d]);
-                o1[d] = re.c[1][d] - re.c[0][d];
-                o2[d] = re.c[2][d] - re.c[0][d];
+                at[d] = pick(tc, pt[1], d) - pick(tc, pt[0], d);
+                bt[d] = pick(tc, pt[2], d) - pick(tc, pt[0], d);
+                ar[d] = pick(rc, pr[1], d) - pick(rc, pr[0], d);
+                br[d] = pick(rc, pr[2], d) - pick(rc, pr[0], d);
+                e1[d] = tc[1][d] - tc[0][d];
+                e2[d] = tc[2][d] - tc[0][d];
+                f1[d] = rc[1][d] - rc[0][d];  // the trial element's own orientation
+                f2[d] = rc[2][d] - rc[0][d];
             }
-            cross3(o1, o2, nv);  // the trial element's own orientation
-            const double Jr = norm3(nv);
-            for (int d = 0; d < 3; ++d) nrm[d] = (float)(nv[d] / Jr);
-            double tv1[3], tv2[3], tn[3];
-            for (int d = 0; d < 3; ++d) {
-                tv1[d] = te.c[1][d] - te.c[0][d];
-                tv2[d] = te.c[2][d] - te.c[0][d];
-            }
-            cross3(tv1, tv2, tn);
-            const float wscale = (float)(norm3(tn) * Jr / FOUR_PI);
+            ntv[0] = e1[1] * e2[2] - e1[2] * e2[1];
+            ntv[1] = e1[2] * e2[0] - e1[0] * e2[2];
+            ntv[2] = e1[0] * e2[1] - e1[1] * e2[0];
+            nrv[0] = f1[1] * f2[2] - f1[2] * f2[1];
+            nrv[1] = f1[2] * f2[0] - f1[0] * f2[2];
+            nrv[2] = f1[0] * f2[1] - f1[1] * f2[0];
+            const float Jtf = sqrtf(ntv[0] * ntv[0] + ntv[1] * ntv[1] + ntv[2] * ntv[2]);
+            const float Jrf = sqrtf(nrv[0] * nrv[0] + nrv[1] * nrv[1] + nrv[2] * nrv[2]);
+#pragma unroll
+            for (int d = 0; d < 3; ++d) nrm[d] = nrv[d] / Jrf;
+            const float wscale = Jtf * Jrf * (float)(1.0 / FOUR_PI);
             const float kf = (float)k;
             const float *rule = g_gal_rule32 + 8 * (size_t)gal_offset(match);
             const int np = gal_npts(match);
@@ -544,36 +561,42 @@ __global__ void __launch_bounds__(GAL_WARPS * 32) k_galerkin_near(GalArgs a, Nea
         } else if (a.precision == 0 && te.nc == 3 && re.nc == 3) {
             // unmatched close triangles under FP32 regular quadrature: the same
             // product rules in FP32, points relative to the element centres
-            // (r_vec = (c_j - c_i) + (y - c_j) - (x - c_i), the first term in FP64)
-            double dc[3];
-            for (int d = 0; d < 3; ++d) dc[d] = a.trial.center[3 * (int64_t)j + d] - a.test.center[3 * (int64_t)i + d];
-            const double ratio = norm3(dc) / a.trial.size[j];
-            const int deg_s = ratio < 11.0 / 10.0 ? 6 : (ratio < T_S1 ? 4 : (ratio < T_S0 ? 2 : 0));
-            const int deg_d = ratio < 11.0 / 10.0 ? 8 : (ratio < T_NEAR ? 6 : (ratio < T_D1 ? 4 : (ratio < T_D0 ? 2 : 0)));
-            float c0[3], ti1[3], ti2[3], tj0[3], tj1[3], tj2[3], nrm[3];
-            double v1[3], v2[3], nt[3], w1[3], w2[3], nr[3];
-            for (int d = 0; d < 3; ++d) {
-                v1[d] = te.c[1][d] - te.c[0][d];
-                v2[d] = te.c[2][d] - te.c[0][d];
-                w1[d] = re.c[1][d] - re.c[0][d];
-                w2[d] = re.c[2][d] - re.c[0][d];
+            // (r_vec = (c_j - c_i) + (y - c_j) - (x - c_i), the first term
+            // formed in FP64); the degree decision in FP32 with the FP64 guard
+            // band of the classification
+            double dcd[3];
+            for (int d = 0; d < 3; ++d) dcd[d] = a.trial.center[3 * (int64_t)j + d] - a.test.center[3 * (int64_t)i + d];
+            float c0[3];
+            for (int d = 0; d < 3; ++d) c0[d] = (float)dcd[d];
+            const float size_j = (float)a.trial.size[j];
+            const float ratio = sqrtf(c0[0] * c0[0] + c0[1] * c0[1] + c0[2] * c0[2]) / size_j;
+            int deg_s, deg_d;
+            {
+                const double rx = (fabsf(ratio - 1.1f) < 1e-4f || fabsf(ratio - 1.5f) < 1e-4f || fabsf(ratio - 1.8f) < 1e-4f)
+                                      ? norm3(dcd) / a.trial.size[j]
+                                      : (double)ratio;
+                deg_s = rx < 11.0 / 10.0 ? 6 : (rx < T_S1 ? 4 : (rx < T_S0 ? 2 : 0));
+                deg_d = rx < 11.0 / 10.0 ? 8 : (rx < T_NEAR ? 6 : (rx < T_D1 ? 4 : (rx < T_D0 ? 2 : 0)));
             }
-            cross3(v1, v2, nt);
-            cross3(w1, w2, nr);
-            const double Jt = norm3(nt), Jr = norm3(nr);
+            float ti0[3], ti1[3], ti2[3], tj0[3], tj1[3], tj2[3], nrm[3], nt[3], nr[3];
             for (int d = 0; d < 3; ++d) {
-                c0[d] = (float)dc[d];
-                // test corner 0 relative to its centre, trial corner 0 relative to its centre
-                ti1[d] = (float)v1[d];
-                ti2[d] = (float)v2[d];
+                ti0[d] = (float)(te.c[0][d] - a.test.center[3 * (int64_t)i + d]);
+                ti1[d] = (float)(te.c[1][d] - te.c[0][d]);
+                ti2[d] = (float)(te.c[2][d] - te.c[0][d]);
                 tj0[d] = (float)(re.c[0][d] - a.trial.center[3 * (int64_t)j + d]);
-                tj1[d] = (float)w1[d];
-                tj2[d] = (float)w2[d];
-                nrm[d] = (float)(nr[d] / Jr);
+                tj1[d] = (float)(re.c[1][d] - re.c[0][d]);
+                tj2[d] = (float)(re.c[2][d] - re.c[0][d]);
             }
-            float ti0[3];
-            for (int d = 0; d < 3; ++d) ti0[d] = (float)(te.c[0][d] - a.test.center[3 * (int64_t)i + d]);
-            const float kf = (float)k, wscale = (float)(Jt * Jr / FOUR_PI);
+            nt[0] = ti1[1] * ti2[2] - ti1[2] * ti2[1];
+            nt[1] = ti1[2] * ti2[0] - ti1[0] * ti2[2];
+            nt[2] = ti1[0] * ti2[1] - ti1[1] * ti2[0];
+            nr[0] = tj1[1] * tj2[2] - tj1[2] * tj2[1];
+            nr[1] = tj1[2] * tj2[0] - tj1[0] * tj2[2];
+            nr[2] = tj1[0] * tj2[1] - tj1[1] * tj2[0];
+            const float Jt = sqrtf(nt[0] * nt[0] + nt[1] * nt[1] + nt[2] * nt[2]);
+            const float Jr = sqrtf(nr[0] * nr[0] + nr[1] * nr[1] + nr[2] * nr[2]);
+            for (int d = 0; d < 3; ++d) nrm[d] = nr[d] / Jr;
+            const float kf = (float)k, wscale = Jt * Jr * (float)(1.0 / FOUR_PI);
             const bool one_pass = !do_s || !do_d || deg_s == deg_d;
             float fsr = 0, fsi = 0, fdr = 0, fdi = 0;
             for (int pass = 0; pass < (one_pass ? 1 : 2); ++pass) {
