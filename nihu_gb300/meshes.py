@@ -59,6 +59,40 @@ def icosphere(subdivisions: int, radius: float = 1.0):
     return _pack(nodes, faces, TRIA_1)
 
 
+def cube_sphere(n: int, radius: float = 1.0):
+    """Sphere of 6 n^2 flat quads: every face of the cube [-1, 1]^3 split into
+    n x n squares (equiangular spacing), vertices projected to the sphere;
+    shared edges share nodes, faces oriented outward."""
+    t = np.tan(np.linspace(-np.pi / 4, np.pi / 4, n + 1))
+    index = {}
+    nodes = []
+
+    def node(p):
+        key = tuple(np.round(p, 12))
+        if key not in index:
+            index[key] = len(nodes)
+            nodes.append(p / np.linalg.norm(p))
+        return index[key]
+
+    faces = []
+    # (normal axis, sign): u, v axes chosen so that u x v = sign * e_axis
+    for axis in range(3):
+        a1, a2 = (axis + 1) % 3, (axis + 2) % 3
+        for sign in (1.0, -1.0):
+            grid = np.empty((n + 1, n + 1), dtype=np.int64)
+            for i in range(n + 1):
+                for j in range(n + 1):
+                    p = np.zeros(3)
+                    p[axis] = sign
+                    p[a1] = t[i]
+                    p[a2] = t[j] * sign
+                    grid[i, j] = node(p)
+            for i in range(n):
+                for j in range(n):
+                    faces.append((grid[i, j], grid[i + 1, j], grid[i + 1, j + 1], grid[i, j + 1]))
+    return _pack(np.array(nodes) * radius, faces, QUAD_1)
+
+
 def cylinder(n_theta: int, n_z: int, n_ring: int, radius: float = 1.0, length: float = 4.0, smooth: int = 200):
     """Closed cylinder of flat quads: an ``n_theta x n_z`` side grid plus two
     O-grid caps.  Each cap is an ``m x m`` square core (m = n_theta/4) blended

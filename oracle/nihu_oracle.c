@@ -1111,16 +1111,16 @@ static void gal_build(int match)
 
 /* first common node of two triangles in each (cyclic order: the one the
  * common edge starts from), as nihu/core/element.hpp:376-413 */
-static int common_nodes(const int *ta, const int *tb, int *ind1, int *ind2)
+static int common_nodes(const int *ta, int na, const int *tb, int nb, int *ind1, int *ind2)
 {
     int num = 0, s1 = 0, s2 = 0;
-    for (int i = 0; i < 3; ++i)
-        for (int j = 0; j < 3; ++j) {
+    for (int i = 0; i < na; ++i)
+        for (int j = 0; j < nb; ++j) {
             if (ta[i] != tb[j]) continue;
             if (num == 0) { s1 = i; s2 = j; }
             else {
-                if (i < s1 || (i == 2 && s1 == 0 && num == 1)) s1 = i;
-                if (j < s2 || (j == 2 && s2 == 0 && num == 1)) s2 = j;
+                if (i < s1 || (i == na - 1 && s1 == 0 && num == 1)) s1 = i;
+                if (j < s2 || (j == nb - 1 && s2 == 0 && num == 1)) s2 = j;
             }
             ++num;
         }
@@ -1169,6 +1169,146 @@ static cplx galerkin_singular(const elem_t *te, const elem_t *re, int fam, int o
     return sum;
 }
 
+/* Singular Galerkin quadrature on a pair of quads (nihu/core/singular_galerkin_quadrature.hpp:430-600):
+ * the coordinate difference mu = eta' - xi (eta' = the trial point after a
+ * reflection that puts both elements side by side: none for a face match,
+ * (eta_0, -2 - eta_1) for an edge, -2 - eta for a corner) is integrated over
+ * Duffy quads (corners 0 and 1 at the singularity; 4 / 6 / 5 of them) with
+ * the 4 x 4 Gauss rule, and for each mu the test point xi over the part of
+ * [-1, 1]^2 that keeps the trial point inside its square, again 4 x 4 Gauss;
+ * both maps bilinear with signed Jacobians (quadrature.hpp:112-127).  A face
+ * match is symmetric (each point also with test and trial swapped). */
+#define GALQ_MAX (4 * 16 * 16 * 2)
+static int g_galq_count[3];
+static double g_galq[3][GALQ_MAX][5];
+
+static const double GALQ_FACE[4][4][2] = {{{0, 0}, {0, 0}, {2, -2}, {2, 0}}, {{0, 0}, {0, 0}, {2, 0}, {2, 2}},
+                                          {{0, 0}, {0, 0}, {2, 2}, {0, 2}}, {{0, 0}, {0, 0}, {0, 2}, {-2, 2}}};
+static const double GALQ_EDGE[6][4][2] = {{{0, 0}, {0, 0}, {-2, 0}, {-2, -2}}, {{0, 0}, {0, 0}, {-2, -2}, {0, -2}},
+                                          {{0, 0}, {0, 0}, {0, -2}, {2, -2}},  {{0, 0}, {0, 0}, {2, -2}, {2, 0}},
+                                          {{-2, -2}, {-2, -4}, {0, -4}, {0, -2}}, {{0, -2}, {0, -4}, {2, -4}, {2, -2}}};
+static const double GALQ_CORNER[5][4][2] = {{{0, 0}, {0, 0}, {-2, 0}, {-2, -2}}, {{0, 0}, {0, 0}, {-2, -2}, {0, -2}},
+                                            {{-4, 0}, {-4, -2}, {-2, -2}, {-2, 0}},
+                                            {{-4, -2}, {-4, -4}, {-2, -4}, {-2, -2}},
+                                            {{-2, -2}, {-2, -4}, {0, -4}, {0, -2}}};
+
+/* bilinear map of (u, v) in [-1,1]^2 onto the quad with corners C: point and signed Jacobian */
+static void quad_map(const double C[4][2], double u, double v, double *x, double *y, double *det)
+{
+    double N[4], dN[4][2];
+    shape(4, u, v, N);
+    dshape(4, u, v, dN);
+    double a = 0, b = 0, j00 = 0, j01 = 0, j10 = 0, j11 = 0;
+    for (int c = 0; c < 4; ++c) {
+        a += N[c] * C[c][0]; b += N[c] * C[c][1];
+        j00 += dN[c][0] * C[c][0]; j01 += dN[c][0] * C[c][1];
+        j10 += dN[c][1] * C[c][0]; j11 += dN[c][1] * C[c][1];
+    }
+    *x = a; *y = b;
+    *det = j00 * j11 - j01 * j10;
+}
+
+static void reflect(int match, double e0, double e1, double *o0, double *o1)
+{
+    if (match == 2) { *o0 = e0; *o1 = e1; }
+    else if (match == 1) { *o0 = e0; *o1 = -2.0 - e1; }
+    else { *o0 = -2.0 - e0; *o1 = -2.0 - e1; }
+}
+
+static void galq_build(int match)
+{
+    const double *g = gauss_rule(GAL_N);
+    const int subs = match == 2 ? 4 : (match == 1 ? 6 : 5);
+    const double (*tab)[4][2] = match == 2 ? GALQ_FACE : (match == 1 ? GALQ_EDGE : GALQ_CORNER);
+    double lo[2], hi[2];
+    reflect(match, -1.0, -1.0, &lo[0], &lo[1]);
+    reflect(match, 1.0, 1.0, &hi[0], &hi[1]);
+    for (int c = 0; c < 2; ++c)
+        if (lo[c] > hi[c]) { double t = lo[c]; lo[c] = hi[c]; hi[c] = t; }
+    int n = 0;
+    for (int d = 0; d < subs; ++d)
+        for (int a = 0; a < GAL_N; ++a)
+            for (int b = 0; b < GAL_N; ++b) {
+                double mu0, mu1, det;
+                quad_map(tab[d], g[2 * a], g[2 * b], &mu0, &mu1, &det);
+                const double wo = g[2 * a + 1] * g[2 * b + 1] * det;
+                /* the test points that keep mu + xi in the reflected trial square */
+                double R[4][2];
+                double x0 = -mu0 + lo[0], x1 = -mu0 + hi[0], y0 = -mu1 + lo[1], y1 = -mu1 + hi[1];
+                x0 = x0 < -1.0 ? -1.0 : (x0 > 1.0 ? 1.0 : x0);
+                x1 = x1 < -1.0 ? -1.0 : (x1 > 1.0 ? 1.0 : x1);
+                y0 = y0 < -1.0 ? -1.0 : (y0 > 1.0 ? 1.0 : y0);
+                y1 = y1 < -1.0 ? -1.0 : (y1 > 1.0 ? 1.0 : y1);
+                R[0][0] = x0; R[0][1] = y0; R[1][0] = x1; R[1][1] = y0;
+                R[2][0] = x1; R[2][1] = y1; R[3][0] = x0; R[3][1] = y1;
+                for (int c = 0; c < GAL_N; ++c)
+                    for (int e = 0; e < GAL_N; ++e) {
+                        double xi0, xi1, di;
+                        quad_map(R, g[2 * c], g[2 * e], &xi0, &xi1, &di);
+                        const double w = wo * g[2 * c + 1] * g[2 * e + 1] * di;
+                        double et0, et1;
+                        reflect(match, mu0 + xi0, mu1 + xi1, &et0, &et1);
+                        double *q = g_galq[match][n++];
+                        q[0] = xi0; q[1] = xi1; q[2] = et0; q[3] = et1; q[4] = w;
+                        if (match == 2) {
+                            q = g_galq[match][n++];
+                            q[0] = et0; q[1] = et1; q[2] = xi0; q[3] = xi1; q[4] = w;
+                        }
+                    }
+            }
+    g_galq_count[match] = n;
+}
+
+/* quad point under a corner rotation: corner k of the rotated square is
+ * corner perm[k] of (-1,-1), (1,-1), (1,1), (-1,1) */
+static void quad_rotate(const int perm[4], double u, double v, double *ou, double *ov)
+{
+    static const double C[4][2] = {{-1, -1}, {1, -1}, {1, 1}, {-1, 1}};
+    double N[4];
+    shape(4, u, v, N);
+    *ou = 0.0; *ov = 0.0;
+    for (int k = 0; k < 4; ++k) { *ou += N[k] * C[perm[k]][0]; *ov += N[k] * C[perm[k]][1]; }
+}
+
+/* singular Galerkin integral of a matched quad pair (rotations as for
+ * triangles: nihu/core/singular_accelerator.hpp:270-310) */
+static cplx galerkin_singular_quad(const elem_t *te, const elem_t *re, int fam, int op, double k, int match, int ind1,
+                                   int ind2)
+{
+    if (!g_galq_count[match]) galq_build(match);
+    int pt[4], pr[4];
+    for (int q = 0; q < 4; ++q) {
+        pt[q] = match == 2 ? q : (ind1 + q) % 4;
+        pr[q] = match == 2 ? q : (match == 1 ? (ind2 + 1 + 4 - q) % 4 : (ind2 + q) % 4);
+    }
+    cplx sum = 0.0;
+    for (int p = 0; p < g_galq_count[match]; ++p) {
+        const double *d = g_galq[match][p];
+        double a, b, x[3], y[3], nt[3], nr[3];
+        quad_rotate(pt, d[0], d[1], &a, &b);
+        elem_x(te, a, b, x);
+        elem_normal(te, a, b, nt);
+        quad_rotate(pr, d[2], d[3], &a, &b);
+        elem_x(re, a, b, y);
+        elem_normal(re, a, b, nr);
+        const double Jt = norm3(nt), Jr = norm3(nr);
+        double un[3] = {nr[0] / Jr, nr[1] / Jr, nr[2] / Jr};
+        sum += d[4] * Jt * kern(fam, op, k, x, NULL, y, un) * Jr;
+    }
+    return sum;
+}
+
+/* the quad rule of a match type for tests: count, then points */
+int oracle_galerkin_quad_rule(int match, double *out)
+{
+    if (match < 0 || match > 2) return 0;
+    if (!g_galq_count[match]) galq_build(match);
+    if (out)
+        for (int p = 0; p < g_galq_count[match]; ++p)
+            for (int c = 0; c < 5; ++c) out[5 * p + c] = g_galq[match][p][c];
+    return g_galq_count[match];
+}
+
 /* One Galerkin entry (nihu/core/double_integral.hpp:318-384): face match for
  * the same element of one mesh, edge / corner match for triangles of one mesh
  * sharing 2 / 1 nodes, otherwise the regular rule of degree C + interval(d/D) */
@@ -1182,22 +1322,18 @@ static int galerkin_entry(const elem_t *te, const elem_t *re, const int *tn, con
     int match = -1, ind1 = 0, ind2 = 0;
     if (same_mesh) {
         if (same_id) match = 2;
-        else if (te->nc == 3 && re->nc == 3) {
-            int num = common_nodes(tn, rn, &ind1, &ind2);
+        else {
+            int num = common_nodes(tn, te->nc, rn, re->nc, &ind1, &ind2);
             match = num > 1 ? 1 : (num == 1 ? 0 : -1);
-        } else {
-            int num = 0;
-            for (int i = 0; i < te->nc; ++i)
-                for (int j = 0; j < re->nc; ++j) num += tn[i] == rn[j];
-            if (num > 0) match = 0;
         }
     }
     if (match >= 0) {
-        if (te->nc != 3 || re->nc != 3) {
-            snprintf(g_err, sizeof g_err, "Galerkin singular quadrature: constant triangles only");
+        if (te->nc != re->nc) {
+            snprintf(g_err, sizeof g_err, "Galerkin singular quadrature: triangle-quad matches are not built");
             return 0;
         }
-        *out = galerkin_singular(te, re, fam, op, k, match, ind1, ind2);
+        *out = te->nc == 3 ? galerkin_singular(te, re, fam, op, k, match, ind1, ind2)
+                           : galerkin_singular_quad(te, re, fam, op, k, match, ind1, ind2);
         return 1;
     }
     double ratio = centre_distance(te, re) / re->size;

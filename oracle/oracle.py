@@ -54,6 +54,8 @@ def lib():
             L.oracle_assemble_galerkin.restype = c_int
             L.oracle_galerkin_rule.argtypes = [c_int, dp]
             L.oracle_galerkin_rule.restype = c_int
+            L.oracle_galerkin_quad_rule.argtypes = [c_int, dp]
+            L.oracle_galerkin_quad_rule.restype = c_int
             L.oracle_classify.argtypes = [dp, c_int, ip, c_int, c_int, dp, c_int, ip, c_int, c_int,
                                           c_int, c_int, c_int, ip]
             L.oracle_classify.restype = c_int
@@ -158,13 +160,14 @@ def assemble_galerkin(test_mesh, trial_mesh, family, op, k, same_mesh=None, rows
     return out
 
 
-def galerkin_rule(match):
-    """The singular Galerkin rule of a triangle pair for match 2 (face), 1
-    (edge), 0 (corner): array of (test xi, eta, trial xi, eta, w)."""
+def galerkin_rule(match, quad=False):
+    """The singular Galerkin rule of a triangle (or quad) pair for match 2
+    (face), 1 (edge), 0 (corner): array of (test xi, eta, trial xi, eta, w)."""
     L = lib()
-    n = L.oracle_galerkin_rule(match, None)
+    fn = L.oracle_galerkin_quad_rule if quad else L.oracle_galerkin_rule
+    n = fn(match, None)
     out = np.zeros((n, 5))
-    L.oracle_galerkin_rule(match, ctypes.cast(out.ctypes.data, ctypes.POINTER(ctypes.c_double)))
+    fn(match, ctypes.cast(out.ctypes.data, ctypes.POINTER(ctypes.c_double)))
     return out
 
 

@@ -12,6 +12,7 @@ from oracle import oracle
 from test_quad_rules import tri
 
 TRIA = 32303
+QUAD_ID = 32404
 
 
 def exact_tri_moment(a, b):
@@ -147,8 +148,80 @@ def test_pulsating_sphere_galerkin():
     assert np.abs(L - L.T).max() <= 1e-5 * np.abs(L).max()
 
 
-def test_quads_in_a_matched_pair_are_refused():
-    from nihu_gb300 import meshes
-    mesh = meshes.cylinder(8, 3, 1)
+def test_triangle_quad_matches_are_refused():
+    nodes = np.array([[0, 0, 0], [1, 0, 0], [1, 1, 0], [0, 1, 0], [0.5, -1, 0.2]], float)
+    elems = np.array([[QUAD_ID, 0, 1, 2, 3], [TRIA, 1, 0, 4, -1]], np.int32)
     with pytest.raises(RuntimeError):
-        oracle.assemble_galerkin(mesh, mesh, oracle.HELMHOLTZ, oracle.SLP, 1.0)
+        oracle.assemble_galerkin((nodes, elems), (nodes, elems), oracle.HELMHOLTZ, oracle.SLP, 1.0, same_mesh=True)
+
+
+QUAD = 32404
+
+
+@pytest.mark.parametrize("match", [2, 1, 0])
+def test_quad_singular_rules_integrate_polynomials(match):
+    r = oracle.galerkin_rule(match, quad=True)
+    assert len(r) == {2: 2048, 1: 1536, 0: 1280}[match]
+
+    def m(a):  # integral of x^a over [-1, 1]
+        return 0.0 if a % 2 else 2.0 / (a + 1)
+
+    for a, b, c, d in [(0, 0, 0, 0), (2, 0, 0, 0), (1, 1, 1, 1), (2, 0, 0, 2), (0, 2, 2, 0), (3, 0, 1, 0)]:
+        got = np.sum(r[:, 4] * r[:, 0] ** a * r[:, 1] ** b * r[:, 2] ** c * r[:, 3] ** d)
+        assert abs(got - m(a) * m(b) * m(c) * m(d)) <= 1e-12 * 16, (match, a, b, c, d)
+
+
+def square_points(corners, levels, n=8):
+    """(points, weights) of an n x n Gauss rule on 4^levels sub-squares of a flat quad"""
+    g, w = np.polynomial.legendre.leggauss(n)
+    c = np.asarray(corners, float)
+    pts, ws = [], []
+    m = 2 ** levels
+    for i in range(m):
+        for j in range(m):
+            for a, wa in zip(g, w):
+                for b, wb in zip(g, w):
+                    u = -1 + (2 * i + 1 + a) / m
+                    v = -1 + (2 * j + 1 + b) / m
+                    N = np.array([(1 - u) * (1 - v), (1 + u) * (1 - v), (1 + u) * (1 + v), (1 - u) * (1 + v)]) / 4
+                    dNu = np.array([-(1 - v), (1 - v), (1 + v), -(1 + v)]) / 4
+                    dNv = np.array([-(1 - u), -(1 + u), (1 + u), (1 - u)]) / 4
+                    J = np.linalg.norm(np.cross(dNu @ c, dNv @ c))
+                    pts.append(N @ c)
+                    ws.append(wa * wb * J / m ** 2)
+    return np.array(pts), np.array(ws)
+
+
+QNODES = np.array([[0, 0, 0], [1, 0, 0], [1, 1, 0], [0, 1, 0], [1, -0.9, 0.35], [0, -0.9, 0.35],
+                   [2.0, 1.0, 0.4], [2.0, 2.0, 0.4], [1.0, 2.0, 0.0]], float)
+QELEMS = np.array([[QUAD, 0, 1, 2, 3], [QUAD, 5, 4, 1, 0], [QUAD, 2, 6, 7, 8]], np.int32)
+
+
+@pytest.mark.parametrize("j,name,tol", [(0, "face", 1e-4), (1, "edge", 1e-4), (2, "corner", 1e-5)])
+def test_quad_laplace_slp_against_outer_inner_integration(fine_angles, j, name, tol):
+    """Flat square with a folded edge neighbour and a corner neighbour: the
+    n = 4 Duffy rules against outer Gauss over the semi-analytic inner integral."""
+    G = oracle.assemble_galerkin((QNODES, QELEMS), (QNODES, QELEMS), oracle.LAPLACE, oracle.SLP, 0.0, same_mesh=True)
+    pts, ws = square_points(QNODES[QELEMS[0, 1:5]], 3)
+    trial = QNODES[QELEMS[j, 1:5]]
+    ref = sum(w * oracle.elem_integral(trial, x, oracle.LAPLACE, oracle.SLP, 0.0, kind=3).real
+              for x, w in zip(pts, ws))
+    assert abs(G[0, j].real - ref) <= tol * abs(ref), (name, G[0, j], ref)
+
+
+def test_pulsating_sphere_galerkin_quads():
+    """The quad version of the reference's pulsating-sphere test (its mesh
+    sphere_1_5.off is a quad sphere): a cube-sphere of 216 quads."""
+    from nihu_gb300 import meshes
+    mesh = meshes.cube_sphere(6)
+    nodes, elems = mesh
+    n = len(elems)
+    import nihu_gb300 as g
+    area = g.create_mesh(nodes, elems).areas()
+    k = 1.0
+    L = oracle.assemble_galerkin(mesh, mesh, oracle.HELMHOLTZ, oracle.SLP, k, threads=4)
+    M = oracle.assemble_galerkin(mesh, mesh, oracle.HELMHOLTZ, oracle.DLP, k, threads=4)
+    p = np.linalg.solve(M - 0.5 * np.diag(area), L @ np.ones(n))
+    pa = -1.0 / (1.0 + 1j * k)
+    assert np.abs(p - pa).max() / abs(pa) < 0.02
+    assert np.abs(L - L.T).max() <= 1e-4 * np.abs(L).max()
