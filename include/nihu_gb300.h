@@ -167,10 +167,11 @@ nihu_gb_status nihu_gb_add_identity(nihu_gb_ctx *ctx, const nihu_gb_mesh *mesh, 
  * nihu_gb_assemble (test == trial handle = one mesh).  On one mesh, pairs
  * that share the element, an edge or a corner take the singular Galerkin
  * rules of their match type (4 Gauss points per direction of a 4D Duffy-type
- * split: 1536 / 1536 / 512 points); all other pairs the product of the
- * regular rule of degree C + interval(d/D) on both elements.  Elements of one
- * mesh must be constant triangles (quads: NIHU_GB_ERR_INVALID_ARGUMENT; the
- * reference's quad rules are not built); a separate test mesh may hold quads.
+ * split: 1536 / 1536 / 512 points on triangles, 2048 / 1536 / 1280 on quads);
+ * all other pairs the product of the regular rule of degree C + interval(d/D)
+ * on both elements.  One mesh holds triangles or quads, not both
+ * (triangle-quad matches are not built: NIHU_GB_ERR_INVALID_ARGUMENT); a
+ * separate test mesh may mix them.
  * Replaces: test_space * Op[trial_space] with a function-space test space
  * (nihu/core/double_integral.hpp:143-384, element_match.hpp:60-90,
  * singular_accelerator.hpp:142-330, singular_galerkin_quadrature.hpp:200-420),

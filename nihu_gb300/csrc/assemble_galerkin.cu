@@ -49,6 +49,15 @@ constexpr int GAL_TOTAL = gal_npts(0) + gal_npts(1) + gal_npts(2);
 // eta, w, trial xi - test xi, trial eta - test eta, 0), the differences formed
 // in FP64
 __device__ double g_gal_rule[GAL_TOTAL * 5];
+
+// the quad-quad rules (corner 1280, edge 1536, face 2048 points), the same layout
+__host__ __device__ constexpr int galq_npts(int match) { return match == 0 ? 1280 : (match == 1 ? 1536 : 2048); }
+__host__ __device__ constexpr int galq_offset(int match)
+{
+    return match == 0 ? 0 : (match == 1 ? galq_npts(0) : galq_npts(0) + galq_npts(1));
+}
+constexpr int GALQ_TOTAL = galq_npts(0) + galq_npts(1) + galq_npts(2);
+__device__ double g_galq_rule[GALQ_TOTAL * 5];
 __device__ __align__(16) float g_gal_rule32[GAL_TOTAL * 8];
 
 __host__ __device__ constexpr int gal_offset(int match)
@@ -155,6 +164,88 @@ static std::vector<double> gal_rules()
     return out;
 }
 
+// Duffy quads of the coordinate difference mu for the quad-quad rules
+// (nihu/library/lib_singular_galerkin_quadrature.cpp)
+static const double QF[4][4][2] = {{{0, 0}, {0, 0}, {2, -2}, {2, 0}}, {{0, 0}, {0, 0}, {2, 0}, {2, 2}},
+                                   {{0, 0}, {0, 0}, {2, 2}, {0, 2}}, {{0, 0}, {0, 0}, {0, 2}, {-2, 2}}};
+static const double QE[6][4][2] = {{{0, 0}, {0, 0}, {-2, 0}, {-2, -2}}, {{0, 0}, {0, 0}, {-2, -2}, {0, -2}},
+                                   {{0, 0}, {0, 0}, {0, -2}, {2, -2}},  {{0, 0}, {0, 0}, {2, -2}, {2, 0}},
+                                   {{-2, -2}, {-2, -4}, {0, -4}, {0, -2}}, {{0, -2}, {0, -4}, {2, -4}, {2, -2}}};
+static const double QC[5][4][2] = {{{0, 0}, {0, 0}, {-2, 0}, {-2, -2}}, {{0, 0}, {0, 0}, {-2, -2}, {0, -2}},
+                                   {{-4, 0}, {-4, -2}, {-2, -2}, {-2, 0}}, {{-4, -2}, {-4, -4}, {-2, -4}, {-2, -2}},
+                                   {{-2, -2}, {-2, -4}, {0, -4}, {0, -2}}};
+
+// bilinear map of (u, v) in [-1,1]^2 onto the quad with corners C, signed Jacobian
+static void quad_corner_map(const double C[4][2], double u, double v, double &x, double &y, double &det)
+{
+    const double N[4] = {(1 - u) * (1 - v) / 4, (1 + u) * (1 - v) / 4, (1 + u) * (1 + v) / 4, (1 - u) * (1 + v) / 4};
+    const double du[4] = {-(1 - v) / 4, (1 - v) / 4, (1 + v) / 4, -(1 + v) / 4};
+    const double dv[4] = {-(1 - u) / 4, -(1 + u) / 4, (1 + u) / 4, (1 - u) / 4};
+    double j00 = 0, j01 = 0, j10 = 0, j11 = 0;
+    x = y = 0;
+    for (int c = 0; c < 4; ++c) {
+        x += N[c] * C[c][0];
+        y += N[c] * C[c][1];
+        j00 += du[c] * C[c][0];
+        j01 += du[c] * C[c][1];
+        j10 += dv[c] * C[c][0];
+        j11 += dv[c] * C[c][1];
+    }
+    det = j00 * j11 - j01 * j10;
+}
+
+// the trial point's reflection that sets the two squares side by side:
+// none (face), (eta_0, -2 - eta_1) (edge), -2 - eta (corner)
+static void quad_reflect(int match, double e0, double e1, double &o0, double &o1)
+{
+    o0 = match == 0 ? -2.0 - e0 : e0;
+    o1 = match == 2 ? e1 : -2.0 - e1;
+}
+
+static std::vector<double> galq_rules()
+{
+    static const double gdata[NIHU_GAUSS_DATA_LEN] = NIHU_GAUSS_DATA;
+    static const int goff[NIHU_GAUSS_MAX_N] = NIHU_GAUSS_OFFSETS;
+    const double *g = gdata + 2 * goff[GAL_GAUSS - 1];
+    std::vector<double> out((size_t)GALQ_TOTAL * 5);
+    for (int match = 0; match < 3; ++match) {
+        const int subs = match == 2 ? 4 : (match == 1 ? 6 : 5);
+        const double (*tab)[4][2] = match == 2 ? QF : (match == 1 ? QE : QC);
+        double lo[2], hi[2];
+        quad_reflect(match, -1.0, -1.0, lo[0], lo[1]);
+        quad_reflect(match, 1.0, 1.0, hi[0], hi[1]);
+        for (int c = 0; c < 2; ++c)
+            if (lo[c] > hi[c]) std::swap(lo[c], hi[c]);
+        double *d = out.data() + 5 * (size_t)galq_offset(match);
+        for (int sd = 0; sd < subs; ++sd)
+            for (int a = 0; a < GAL_GAUSS; ++a)
+                for (int b = 0; b < GAL_GAUSS; ++b) {
+                    double mu0, mu1, det;
+                    quad_corner_map(tab[sd], g[2 * a], g[2 * b], mu0, mu1, det);
+                    const double wo = g[2 * a + 1] * g[2 * b + 1] * det;
+                    auto clip = [](double v) { return std::min(1.0, std::max(-1.0, v)); };
+                    const double x0 = clip(lo[0] - mu0), x1 = clip(hi[0] - mu0);
+                    const double y0 = clip(lo[1] - mu1), y1 = clip(hi[1] - mu1);
+                    const double R[4][2] = {{x0, y0}, {x1, y0}, {x1, y1}, {x0, y1}};
+                    for (int c = 0; c < GAL_GAUSS; ++c)
+                        for (int e = 0; e < GAL_GAUSS; ++e) {
+                            double xi0, xi1, di;
+                            quad_corner_map(R, g[2 * c], g[2 * e], xi0, xi1, di);
+                            const double w = wo * g[2 * c + 1] * g[2 * e + 1] * di;
+                            double et0, et1;
+                            quad_reflect(match, mu0 + xi0, mu1 + xi1, et0, et1);
+                            d[0] = xi0; d[1] = xi1; d[2] = et0; d[3] = et1; d[4] = w;
+                            d += 5;
+                            if (match == 2) {
+                                d[0] = et0; d[1] = et1; d[2] = xi0; d[3] = xi1; d[4] = w;
+                                d += 5;
+                            }
+                        }
+                }
+    }
+    return out;
+}
+
 cudaError_t prepare_galerkin(cudaStream_t s)
 {
     static std::mutex mu;
@@ -178,6 +269,10 @@ cudaError_t prepare_galerkin(cudaStream_t s)
     e = cudaMemcpyToSymbolAsync(g_gal_rule, rules.data(), rules.size() * sizeof(double), 0, cudaMemcpyHostToDevice, s);
     if (e == cudaSuccess)
         e = cudaMemcpyToSymbolAsync(g_gal_rule32, rules32.data(), rules32.size() * sizeof(float), 0,
+                                    cudaMemcpyHostToDevice, s);
+    static const std::vector<double> qrules = galq_rules();
+    if (e == cudaSuccess)
+        e = cudaMemcpyToSymbolAsync(g_galq_rule, qrules.data(), qrules.size() * sizeof(double), 0,
                                     cudaMemcpyHostToDevice, s);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
     if (e != cudaSuccess) return e;
@@ -395,6 +490,21 @@ __device__ __forceinline__ void tri_rotate(const int perm[3], double xi, double 
     }
 }
 
+// reference point of the square under a corner rotation: corner k of the
+// rotated square is corner perm[k] of (-1,-1), (1,-1), (1,1), (-1,1)
+__device__ __forceinline__ void quad_rotate(const int perm[4], double u, double v, double &ou, double &ov)
+{
+    const double N[4] = {(1 - u) * (1 - v) / 4, (1 + u) * (1 - v) / 4, (1 + u) * (1 + v) / 4, (1 - u) * (1 + v) / 4};
+    ou = 0.0;
+    ov = 0.0;
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        const int c = perm[q];
+        ou += (c == 1 || c == 2) ? N[q] : -N[q];
+        ov += (c >= 2) ? N[q] : -N[q];
+    }
+}
+
 // The self pairs, the nearly singular list of columns [j0, j1) (extra = 0)
 // or the extra list (extra = 1): one warp per pair
 template <typename Out>
@@ -443,7 +553,35 @@ __global__ void __launch_bounds__(GAL_WARPS * 32) k_galerkin_near(GalArgs a, Nea
             }
         }
         double sr = 0, si = 0, dr = 0, di = 0;
-        if (match >= 0 && a.precision == 0) {
+        if (match >= 0 && te.nc == 4) {
+            // matched quads (FP64, both precisions): points by the bilinear
+            // maps, Jacobians and normals per point
+            int pt[4], pr[4];
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                pt[q] = match == 2 ? q : (ind1 + q) % 4;
+                pr[q] = match == 2 ? q : (match == 1 ? (ind2 + 1 + 4 - q) % 4 : (ind2 + q) % 4);
+            }
+            const double *rule = g_galq_rule + 5 * (size_t)galq_offset(match);
+            const int np = galq_npts(match);
+            for (int p = lane; p < np; p += 32) {
+                const double *q = rule + 5 * p;
+                double u, v, x[3], y[3], nt3[3], nr3[3];
+                quad_rotate(pt, q[0], q[1], u, v);
+                ex(te, u, v, x);
+                enormal(te, u, v, nt3);
+                quad_rotate(pr, q[2], q[3], u, v);
+                ex(re, u, v, y);
+                enormal(re, u, v, nr3);
+                cd ks{0, 0}, kd{0, 0};
+                kern_point(fam, k, x, y, nr3, norm3(nr3), do_s, do_d, ks, kd);
+                const double w = q[4] * norm3(nt3);
+                sr += ks.re * w;
+                si += ks.im * w;
+                dr += kd.re * w;
+                di += kd.im * w;
+            }
+        } else if (match >= 0 && a.precision == 0) {
             // FP32 regular quadrature: the matched pair's rule in FP32 too.  Both
             // rotated triangles start at the common node P, so r_vec = y - x is
             // formed from P-relative edge vectors and the rule's FP64-formed

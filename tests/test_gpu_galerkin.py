@@ -41,7 +41,7 @@ def graded_fan():
 
 
 MESHES = {"ico2": lambda: meshes.icosphere(2), "ico3": lambda: meshes.icosphere(3), "two": two_spheres,
-          "fan": graded_fan}
+          "fan": graded_fan, "cube": lambda: meshes.cube_sphere(5)}
 _cache, _ocache = {}, {}
 
 
@@ -73,7 +73,7 @@ def gpu_galerkin(ctx, mesh, family, ops, k, precision, dtype, alpha=1.0, test_me
     return outs
 
 
-@pytest.mark.parametrize("name", ["ico2", "ico3", "two", "fan"])
+@pytest.mark.parametrize("name", ["ico2", "ico3", "two", "fan", "cube"])
 @pytest.mark.parametrize("family,k", [(g.HELMHOLTZ_3D, 1.3), (g.HELMHOLTZ_3D, 4.0), (g.LAPLACE_3D, 0.0)])
 @pytest.mark.parametrize("precision,tol", [(g.REGULAR_FP64, 1e-11), (g.REGULAR_FP32, 1e-5)])
 def test_galerkin_against_oracle(gpu_ctx, oracle, name, family, k, precision, tol):
@@ -155,6 +155,21 @@ def test_mass_matrix_entry_point(gpu_ctx):
     assert np.count_nonzero(out) == n
 
 
-def test_quads_on_one_mesh_are_refused(gpu_ctx):
+def test_pulsating_cube_sphere(gpu_ctx):
+    """Quads on one mesh (face, edge and corner quad rules): the pulsating
+    sphere on a cube-sphere of 384 quads."""
+    nodes, elems = meshes.cube_sphere(8)
+    mesh = g.create_mesh(nodes, elems)
+    n = mesh.num_elements
+    k = 1.0
+    outs = gpu_galerkin(gpu_ctx, (nodes, elems), g.HELMHOLTZ_3D, g.SLP | g.DLP, k, g.REGULAR_FP32, g.C128)
+    p = np.linalg.solve(outs[g.DLP] - 0.5 * np.diag(mesh.areas()), outs[g.SLP] @ np.ones(n))
+    pa = -1.0 / (1.0 + 1j * k)
+    assert np.abs(p - pa).max() / abs(pa) < 0.01
+
+
+def test_mixed_mesh_is_refused(gpu_ctx):
+    nodes = np.array([[0, 0, 0], [1, 0, 0], [1, 1, 0], [0, 1, 0], [0.5, -1, 0.2]], float)
+    elems = np.array([[g.QUAD_1, 0, 1, 2, 3], [TRIA, 1, 0, 4, -1]], np.int32)
     with pytest.raises(g.InvalidArgumentError):
-        gpu_galerkin(gpu_ctx, meshes.cylinder(8, 3, 1), g.HELMHOLTZ_3D, g.SLP, 1.0, g.REGULAR_FP64, g.C128)
+        gpu_galerkin(gpu_ctx, (nodes, elems), g.HELMHOLTZ_3D, g.SLP, 1.0, g.REGULAR_FP64, g.C128)
