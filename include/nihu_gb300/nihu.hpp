@@ -24,6 +24,7 @@
 // does nihu_gb300::dense_matrix below.
 #pragma once
 
+#include <cmath>
 #include <complex>
 #include <cstdint>
 #include <memory>
@@ -111,6 +112,30 @@ public:
             throw std::invalid_argument("create_mesh: nodes must be n x 3, elements m x cols (cols >= 4)");
     }
     int64_t num_elements() const { return (int64_t)(elems_.size() / (size_t)cols_); }
+
+    // element areas with the one-point rule of the Galerkin identity
+    // (nihu/core/single_integral.hpp:97-140): |e1 x e2| / 2 on triangles,
+    // 4 |x_xi x x_eta| at the centre on quads
+    std::vector<double> areas() const
+    {
+        std::vector<double> a((size_t)num_elements());
+        for (int64_t e = 0; e < num_elements(); ++e) {
+            const int32_t *row = elems_.data() + (size_t)(e * cols_);
+            const bool quad = row[0] == NIHU_GB_QUAD_1;
+            double c[4][3];
+            for (int k = 0; k < (quad ? 4 : 3); ++k)
+                for (int d = 0; d < 3; ++d) c[k][d] = nodes_[(size_t)(3 * row[1 + k] + d)];
+            double t1[3], t2[3];
+            for (int d = 0; d < 3; ++d) {
+                t1[d] = quad ? (c[1][d] + c[2][d] - c[0][d] - c[3][d]) / 4 : c[1][d] - c[0][d];
+                t2[d] = quad ? (c[2][d] + c[3][d] - c[0][d] - c[1][d]) / 4 : c[2][d] - c[0][d];
+            }
+            const double n0 = t1[1] * t2[2] - t1[2] * t2[1], n1 = t1[2] * t2[0] - t1[0] * t2[2],
+                         n2 = t1[0] * t2[1] - t1[1] * t2[0];
+            a[(size_t)e] = std::sqrt(n0 * n0 + n1 * n1 + n2 * n2) * (quad ? 4.0 : 0.5);
+        }
+        return a;
+    }
 
     nihu_gb_mesh *on(context &ctx) const
     {
@@ -276,9 +301,14 @@ Res &operator<<(Res &result, weighted_residual<TS> const &wr)
     if ((int64_t)result.rows() != m || (int64_t)result.cols() != n)
         throw std::invalid_argument("result matrix size does not match the operator");
     integral_operator const &op = wr.tr.op;
-    if (op.identity) {  // (alpha I)[sp]: collocational identity on coinciding elements
-        if (&tm == &rm)
-            for (int64_t i = 0; i < m; ++i) detail::add_scalar(result.data()[i + i * m], op.scale);
+    // a function-space test space is the Galerkin formalism, dirac() collocation
+    constexpr bool galerkin = std::is_same<TS, function_space>::value;
+    if (op.identity) {  // (alpha I)[sp] on coinciding elements: 1 (collocation) or the area (Galerkin)
+        if (&tm == &rm) {
+            const std::vector<double> area = galerkin ? tm.areas() : std::vector<double>();
+            for (int64_t i = 0; i < m; ++i)
+                detail::add_scalar(result.data()[i + i * m], op.scale * (galerkin ? area[(size_t)i] : 1.0));
+        }
         return result;
     }
     context &ctx = *wr.ctx;
@@ -288,9 +318,12 @@ Res &operator<<(Res &result, weighted_residual<TS> const &wr)
     if (kop == NIHU_GB_SLP || kop == NIHU_GB_DLP) {
         void *out_s = kop == NIHU_GB_SLP ? (void *)result.data() : nullptr;
         void *out_d = kop == NIHU_GB_DLP ? (void *)result.data() : nullptr;
-        check(ctx.handle(), nihu_gb_assemble(ctx.handle(), tmh, rmh, op.kernel.family, kop, op.kernel.k,
-                                             op.scale.real(), op.scale.imag(), wr.precision, detail::storage<T>::dtype,
-                                             out_s, out_d, m, 1, NIHU_GB_HOST));
+        auto fn = galerkin ? nihu_gb_assemble_galerkin : nihu_gb_assemble;
+        check(ctx.handle(), fn(ctx.handle(), tmh, rmh, op.kernel.family, kop, op.kernel.k, op.scale.real(),
+                               op.scale.imag(), wr.precision, detail::storage<T>::dtype, out_s, out_d, m, 1,
+                               NIHU_GB_HOST));
+    } else if (galerkin) {
+        throw std::invalid_argument("Galerkin formalism: SLP and DLP kernels only");
     } else {
         void *out_t = kop == NIHU_GB_DLPT ? (void *)result.data() : nullptr;
         void *out_h = kop == NIHU_GB_HSP ? (void *)result.data() : nullptr;

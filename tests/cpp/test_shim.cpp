@@ -7,7 +7,9 @@
 //   mesh.bin: int64 n_nodes, int64 n_elems, n_nodes*3 doubles, n_elems*5 int32
 //   out.bin : Ls, Ms (n*n complex128 each, column-major), p (n complex128),
 //             then the Burton-Miller matrices Gs, Hs and pressure p_bm of
-//             nihu/applications/helmholtz/helmholtz_3d_coll.cpp:36-120 (BM defined)
+//             nihu/applications/helmholtz/helmholtz_3d_coll.cpp:36-120 (BM defined),
+//             then the Galerkin L, M, I and pressure of
+//             nihu/test/stallone_unit/helmholtz_3d_pulsating_sphere_test.cpp:40-70
 #include <cstdio>
 #include <cstdlib>
 #include <fstream>
@@ -94,6 +96,20 @@ int main(int argc, char **argv)
             for (int64_t i = 0; i < n; ++i) rhs_bm[(size_t)i] += Gs(i, j) * q[(size_t)j];
         std::vector<C> p_bm = gmres(Hs, rhs_bm, 1e-10, 50, 1000);
 
+        // Galerkin: I, L, M << test_space * Op[trial_space] with the function space as test space
+        dense_matrix<C> Lg(n, n), Mg(n, n), Ig(n, n);
+        Ig << surf_sp * I[surf_sp];
+        Lg << surf_sp * Lop[surf_sp];
+        Mg << surf_sp * Mop[surf_sp];
+        dense_matrix<C> Ag(n, n);
+        std::vector<C> rhs_g((size_t)n, 0.0);
+        for (int64_t j = 0; j < n; ++j)
+            for (int64_t i = 0; i < n; ++i) {
+                Ag(i, j) = Mg(i, j) - 0.5 * Ig(i, j);
+                rhs_g[(size_t)i] += Lg(i, j) * q[(size_t)j];
+            }
+        std::vector<C> p_g = lu_solve(Ag, rhs_g);
+
         std::ofstream out(argv[3], std::ios::binary);
         out.write((const char *)Ls.data(), n * n * 16);
         out.write((const char *)Ms.data(), n * n * 16);
@@ -101,6 +117,10 @@ int main(int argc, char **argv)
         out.write((const char *)Gs.data(), n * n * 16);
         out.write((const char *)Hs.data(), n * n * 16);
         out.write((const char *)p_bm.data(), n * 16);
+        out.write((const char *)Lg.data(), n * n * 16);
+        out.write((const char *)Mg.data(), n * n * 16);
+        out.write((const char *)Ig.data(), n * n * 16);
+        out.write((const char *)p_g.data(), n * 16);
         C pa = -1.0 / (1.0 + C(0.0, k));
         double err = 0.0;
         for (auto v : p) err = std::max(err, std::abs(v - pa) / std::abs(pa));

@@ -47,7 +47,12 @@ def test_shim_acoustic_bem_sequence(tmp_path, oracle):
     o = 2 * n * n + n
     Gs = raw[o:o + n * n].reshape(n, n, order="F")
     Hs = raw[o + n * n:o + 2 * n * n].reshape(n, n, order="F")
-    p_bm = raw[o + 2 * n * n:]
+    p_bm = raw[o + 2 * n * n:o + 2 * n * n + n]
+    o2 = o + 2 * n * n + n
+    Lg = raw[o2:o2 + n * n].reshape(n, n, order="F")
+    Mg = raw[o2 + n * n:o2 + 2 * n * n].reshape(n, n, order="F")
+    Ig = raw[o2 + 2 * n * n:o2 + 3 * n * n].reshape(n, n, order="F")
+    p_g = raw[o2 + 3 * n * n:]
     mesh = (nodes, elems)
     L = oracle.assemble(mesh, mesh, oracle.HELMHOLTZ, oracle.SLP, k, threads=8)
     M = oracle.assemble(mesh, mesh, oracle.HELMHOLTZ, oracle.DLP, k, threads=8) - 0.5 * np.eye(n)
@@ -65,3 +70,13 @@ def test_shim_acoustic_bem_sequence(tmp_path, oracle):
     assert np.abs(Hs - H_ref).max() / np.abs(H_ref).max() < 1e-5
     p_bm_ref = np.linalg.solve(H_ref, G_ref @ np.ones(n))
     assert np.abs(p_bm - p_bm_ref).max() / np.abs(p_bm_ref).max() < 1e-4
+    # the Galerkin formalism of the reference's own pulsating-sphere test
+    Lgr = oracle.assemble_galerkin(mesh, mesh, oracle.HELMHOLTZ, oracle.SLP, k, threads=8)
+    Mgr = oracle.assemble_galerkin(mesh, mesh, oracle.HELMHOLTZ, oracle.DLP, k, threads=8)
+    c = nodes[elems[:, 1:4]]
+    area = 0.5 * np.linalg.norm(np.cross(c[:, 1] - c[:, 0], c[:, 2] - c[:, 0]), axis=1)
+    assert np.allclose(np.diag(Ig).real, area, rtol=1e-12) and np.count_nonzero(Ig) == n
+    assert np.abs(Lg - Lgr).max() / np.abs(Lgr).max() < 1e-5
+    assert np.abs(Mg - Mgr).max() / np.abs(Mgr).max() < 1e-5
+    p_gr = np.linalg.solve(Mgr - 0.5 * np.diag(area), Lgr @ np.ones(n))
+    assert np.abs(p_g - p_gr).max() / np.abs(p_gr).max() < 1e-4
