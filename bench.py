@@ -238,6 +238,19 @@ def recorded_traffic():
         return None
 
 
+def replicas_summary(ms_per_step, units_per_step, dist=None, device="cpu"):
+    """Replicas: the slowest rank's step time (all-reduce MAX) and the whole
+    job's throughput, every rank processing units_per_step per step."""
+    ws = 1
+    if dist is not None:
+        import torch
+        ws = dist.get_world_size()
+        t = torch.tensor([ms_per_step], dtype=torch.float64, device=device)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms_per_step = float(t.item())
+    return ms_per_step, units_per_step * ws / (ms_per_step / 1e3)
+
+
 def run_ours(args):
     import torch
 
@@ -299,13 +312,8 @@ def run_ours(args):
     prof = ctx.profile()
     ctx.set_profiling(False)
     step_ms = [a.elapsed_time(b) for a, b in ev]
-    ms_per_step = float(np.mean(step_ms))
-    if dist:
-        t = torch.tensor([ms_per_step], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms_per_step = float(t.item())
     entries = 2.0 * n * n
-    value = entries * ws / (ms_per_step / 1e3)
+    ms_per_step, value = replicas_summary(float(np.mean(step_ms)), entries, dist, "cuda")
 
     reg_ms, reg_n = prof.get("assemble_regular", (0.0, 0))
     sing_ms, sing_n = prof.get("assemble_singular", (0.0, 0))
