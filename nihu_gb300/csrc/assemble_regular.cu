@@ -14,7 +14,15 @@
 // cost -- storing 2 x 8 bytes per pair -- streams at full HBM width.
 // Self and nearly singular pairs are skipped (assemble_singular.cu writes
 // them), so every entry is written exactly once.
+//
+// Right-hand-side mode (frequency batches, RegularArgs::rhs_part): the SLP
+// entries are not stored; each thread sums SLP_f(i, j) q_f(j) over its
+// block's columns per wave number in shared memory, the block writes one
+// partial sum per (wave number, row), and k_rhs_reduce adds the partials and
+// the FP64 kernel's nearly singular and self entries in a fixed order.  This
+// is b = SLP q of the collocation system without the SLP matrix.
 #include <algorithm>
+#include <type_traits>
 
 #include "classify.cuh"
 #include "kernels.h"
@@ -86,6 +94,22 @@ __device__ __forceinline__ void store_entry(Out *p, R re, R im, R are, R aim, bo
     *p = o;
 }
 
+// right-hand-side mode: wave numbers per block (the gridDim.z split keeps at
+// most this many), which sizes the shared row sums and Neumann data
+template <typename R>
+__host__ __device__ constexpr int rhs_f_max() { return sizeof(R) == 4 ? 16 : 8; }
+
+template <typename R>
+using Cplx = std::conditional_t<sizeof(R) == 4, float2, double2>;
+
+// acc += (sr + i si) q
+template <typename R2, typename R>
+__device__ __forceinline__ void rhs_add(R2 &acc, const R2 q, R sr, R si)
+{
+    acc.x += sr * q.x - si * q.y;
+    acc.y += sr * q.y + si * q.x;
+}
+
 // Squared distance ratio above which a pair is certainly regular with the
 // 1-point rule for both SLP (x >= 9.1) and DLP (x >= 15.8): 15.8^2 with a
 // relative margin far larger than the FP32 error of the plain centre
@@ -94,11 +118,17 @@ constexpr float Q_FAR = 249.64f * (1.0f + 1e-4f);
 
 // BATCH: frequency batch (a.nk > 1), a separate instantiation so that the
 // single wave number kernel carries none of its code
-template <typename R, typename Out, int FAM, int OPS, bool BATCH>
+// RHS: right-hand-side mode (BATCH only; the SLP entries go into the row sums)
+template <typename R, typename Out, int FAM, int OPS, bool BATCH, bool RHS = false>
 __global__ void __launch_bounds__(REG_THREADS) k_regular(RegularArgs a)
 {
+    using R2 = Cplx<R>;
     __shared__ float4 s_hi[REG_COLS], s_lo[REG_COLS], s_p0[REG_COLS];
     __shared__ int s_nc[REG_COLS];
+    // RHS: Neumann data [f - f_lo][c], then the row sums [f - f_lo][threadIdx.x]
+    extern __shared__ __align__(16) unsigned char s_rhs[];
+    R2 *s_q = reinterpret_cast<R2 *>(s_rhs);
+    R2 *s_acc = s_q + rhs_f_max<R>() * REG_COLS;
     constexpr bool DO_S = (OPS & OP_SLP) != 0;
     constexpr bool DO_D = (OPS & OP_DLP) != 0;
     const DevMesh &test = a.test;
@@ -106,11 +136,35 @@ __global__ void __launch_bounds__(REG_THREADS) k_regular(RegularArgs a)
     const int i = blockIdx.x * REG_THREADS + threadIdx.x;
     const int jb = a.j0 + blockIdx.y * REG_COLS;
     const int ncols = min(REG_COLS, a.j1 - jb);
+    // frequency batch: this block's wave numbers [f_lo, f_hi) (gridDim.z chunks)
+    const int f_per = (a.nk + gridDim.z - 1) / gridDim.z;
+    const int f_lo = min(a.nk, (int)blockIdx.z * f_per), f_hi = min(a.nk, f_lo + f_per);
     if (threadIdx.x < ncols) {
         s_hi[threadIdx.x] = trial.chi[jb + threadIdx.x];
         s_lo[threadIdx.x] = trial.clo[jb + threadIdx.x];
         s_nc[threadIdx.x] = trial.nc[jb + threadIdx.x];
         s_p0[threadIdx.x] = trial.p0[jb + threadIdx.x];
+    }
+    if constexpr (RHS) {
+        const int nf = f_hi - f_lo;  // at most rhs_f_max (launch_assemble_regular)
+        for (int t = threadIdx.x; t < nf * REG_COLS; t += REG_THREADS) {
+            const int fl = t / REG_COLS, c = t - fl * REG_COLS;
+            R2 v;
+            v.x = 0;
+            v.y = 0;
+            if (c < ncols) {
+                const double2 qv = a.rhs_q[(int64_t)(f_lo + fl) * trial.n + jb + c];
+                v.x = R(qv.x);
+                v.y = R(qv.y);
+            }
+            s_q[t] = v;
+        }
+        for (int fl = 0; fl < nf; ++fl) {
+            R2 z;
+            z.x = 0;
+            z.y = 0;
+            s_acc[fl * REG_THREADS + threadIdx.x] = z;
+        }
     }
     __syncthreads();
     // whole warps beyond the last row leave; a partial last warp keeps its
@@ -146,9 +200,6 @@ __global__ void __launch_bounds__(REG_THREADS) k_regular(RegularArgs a)
     }
     Out *out_s = reinterpret_cast<Out *>(a.out_s);
     Out *out_d = reinterpret_cast<Out *>(a.out_d);
-    // frequency batch: this block's wave numbers [f_lo, f_hi) (gridDim.z chunks)
-    const int f_per = (a.nk + gridDim.z - 1) / gridDim.z;
-    const int f_lo = min(a.nk, (int)blockIdx.z * f_per), f_hi = min(a.nk, f_lo + f_per);
 
     for (int c = 0; c < ncols; ++c) {
         const int j = jb + c;
@@ -167,7 +218,10 @@ __global__ void __launch_bounds__(REG_THREADS) k_regular(RegularArgs a)
                         R sr = 0, si = 0, dr = 0, di = 0;
                         point_freq<FAM, float>(gm, a.ks32[f], sr, si, dr, di);
                         if (row_ok) {
-                            if (DO_S) store_entry(batch_matrix<Out>(a, false, f) + off, sr, si, are, aim, unit_alpha, accumulate);
+                            if constexpr (RHS)
+                                rhs_add(s_acc[(f - f_lo) * REG_THREADS + threadIdx.x], s_q[(f - f_lo) * REG_COLS + c], sr, si);
+                            else if (DO_S)
+                                store_entry(batch_matrix<Out>(a, false, f) + off, sr, si, are, aim, unit_alpha, accumulate);
                             if (DO_D) store_entry(batch_matrix<Out>(a, true, f) + off, dr, di, are, aim, unit_alpha, accumulate);
                         }
                     }
@@ -230,7 +284,10 @@ __global__ void __launch_bounds__(REG_THREADS) k_regular(RegularArgs a)
                 for (int u = 0; u < FREQ_TILE; ++u) {
                     if (f0 + u >= f_hi) break;
                     const int64_t off = (int64_t)(j - a.j0) * a.ld + i;
-                    if (DO_S)
+                    if constexpr (RHS)
+                        rhs_add(s_acc[(f0 + u - f_lo) * REG_THREADS + threadIdx.x], s_q[(f0 + u - f_lo) * REG_COLS + c],
+                                sr[u], si[u]);
+                    else if (DO_S)
                         store_entry(batch_matrix<Out>(a, false, f0 + u) + off, sr[u], si[u], are, aim, unit_alpha, accumulate);
                     if (DO_D)
                         store_entry(batch_matrix<Out>(a, true, f0 + u) + off, dr[u], di[u], are, aim, unit_alpha, accumulate);
@@ -262,11 +319,71 @@ __global__ void __launch_bounds__(REG_THREADS) k_regular(RegularArgs a)
             if (DO_D) store_entry(out_d + off, dr, di, are, aim, unit_alpha, accumulate);
         }
     }
+    if constexpr (RHS) {
+        if (row_ok) {
+            R2 *part = reinterpret_cast<R2 *>(a.rhs_part);
+            for (int f = f_lo; f < f_hi; ++f) {
+                R2 v = s_acc[(f - f_lo) * REG_THREADS + threadIdx.x];
+                if (!unit_alpha) {
+                    const R vr = are * v.x - aim * v.y;
+                    v.y = are * v.y + aim * v.x;
+                    v.x = vr;
+                }
+                part[((int64_t)f * gridDim.y + blockIdx.y) * test.n + i] = v;
+            }
+        }
+    }
+}
+
+// partial sums of the same row added in FP32 before one FP64 addition
+constexpr int RHS_GROUP = 8;
+
+template <typename R2>
+__global__ void __launch_bounds__(256) k_rhs_reduce(const R2 *__restrict__ part, int n_cb, int n, int64_t items,
+                                                    const int64_t *__restrict__ row_ptr, const int2 *__restrict__ row_ent,
+                                                    const double2 *__restrict__ near_slp, const double2 *__restrict__ q,
+                                                    int qn, double2 *__restrict__ b)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int f = blockIdx.y;
+    if (i >= n) return;
+    using R = decltype(R2::x);
+    double re = 0.0, im = 0.0;
+    const R2 *p = part + (int64_t)f * n_cb * n + i;
+    for (int cb0 = 0; cb0 < n_cb; cb0 += RHS_GROUP) {
+        R gr = 0, gi = 0;
+        const int cb1 = min(n_cb, cb0 + RHS_GROUP);
+        for (int cb = cb0; cb < cb1; ++cb) {
+            const R2 v = p[(int64_t)cb * n];
+            gr += v.x;
+            gi += v.y;
+        }
+        re += (double)gr;
+        im += (double)gi;
+    }
+    const double2 *qf = q + (int64_t)f * qn;
+    const double2 *sf = near_slp + (int64_t)f * items;
+    R nr = 0, ni = 0;
+    for (int64_t t = row_ptr[i]; t < row_ptr[i + 1]; ++t) {
+        const int2 e = row_ent[t];
+        const double2 sv = sf[e.x], qv = qf[e.y];
+        const R sr = R(sv.x), si = R(sv.y), qr = R(qv.x), qi = R(qv.y);
+        nr += sr * qr - si * qi;
+        ni += sr * qi + si * qr;
+    }
+    b[(int64_t)f * n + i] = make_double2(re + (double)nr, im + (double)ni);
 }
 
 template <typename R, typename Out, int FAM, bool BATCH>
 static void launch_ops(const RegularArgs &a, dim3 grid, cudaStream_t s)
 {
+    if constexpr (BATCH) {
+        if (a.rhs_part) {
+            const size_t smem = sizeof(Cplx<R>) * rhs_f_max<R>() * (REG_COLS + REG_THREADS);
+            k_regular<R, Out, FAM, OP_SLP | OP_DLP, true, true><<<grid, REG_THREADS, smem, s>>>(a);
+            return;
+        }
+    }
     if (a.ops == OP_SLP) k_regular<R, Out, FAM, OP_SLP, BATCH><<<grid, REG_THREADS, 0, s>>>(a);
     else if (a.ops == OP_DLP) k_regular<R, Out, FAM, OP_DLP, BATCH><<<grid, REG_THREADS, 0, s>>>(a);
     else k_regular<R, Out, FAM, OP_SLP | OP_DLP, BATCH><<<grid, REG_THREADS, 0, s>>>(a);
@@ -300,6 +417,11 @@ cudaError_t launch_assemble_regular(const RegularArgs &a, cudaStream_t s)
         const int64_t want = (4 * (int64_t)sms + xy - 1) / xy;
         const int most = (a.nk + FREQ_TILE - 1) / FREQ_TILE;
         grid.z = (unsigned)std::max<int64_t>(1, std::min<int64_t>(want, most));
+        // right-hand-side mode: at most rhs_f_max wave numbers per block
+        if (a.rhs_part) {
+            const int fmax = a.precision == 0 ? rhs_f_max<float>() : rhs_f_max<double>();
+            grid.z = std::max<unsigned>(grid.z, (unsigned)((a.nk + fmax - 1) / fmax));
+        }
     }
     if (a.precision == 0) {
         if (a.dtype == 0) launch_fam<float, float2>(a, grid, s);
@@ -308,6 +430,28 @@ cudaError_t launch_assemble_regular(const RegularArgs &a, cudaStream_t s)
         if (a.dtype == 0) launch_fam<double, float2>(a, grid, s);
         else launch_fam<double, double2>(a, grid, s);
     }
+    return cudaGetLastError();
+}
+
+size_t rhs_part_bytes(const RegularArgs &a)
+{
+    const int64_t n_cb = (a.j1 - a.j0 + REG_COLS - 1) / REG_COLS;
+    return (a.precision == 0 ? sizeof(float2) : sizeof(double2)) * (size_t)a.nk * n_cb * a.test.n;
+}
+
+cudaError_t launch_rhs_reduce(const RegularArgs &a, const NearList &near, double2 *b, cudaStream_t s)
+{
+    const int n = a.test.n;
+    if (n == 0 || a.nk == 0) return cudaSuccess;
+    const int n_cb = (a.j1 - a.j0 + REG_COLS - 1) / REG_COLS;
+    const int64_t items = near.nnz + (a.same_mesh ? a.trial.n : 0);
+    dim3 grid((n + 255) / 256, a.nk);
+    if (a.precision == 0)
+        k_rhs_reduce<float2><<<grid, 256, 0, s>>>((const float2 *)a.rhs_part, n_cb, n, items, near.row_ptr,
+                                                  near.row_ent, a.near_slp, a.rhs_q, a.trial.n, b);
+    else
+        k_rhs_reduce<double2><<<grid, 256, 0, s>>>((const double2 *)a.rhs_part, n_cb, n, items, near.row_ptr,
+                                                   near.row_ent, a.near_slp, a.rhs_q, a.trial.n, b);
     return cudaGetLastError();
 }
 

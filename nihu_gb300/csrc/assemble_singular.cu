@@ -258,6 +258,19 @@ __device__ void self_tria(const Elem64 &e, int fam, double k, const double x0[3]
 
 // ------------------------------------------------------------------ driver
 
+// the SLP entry of item `item` of wave number f: into the matrix, or in
+// right-hand-side mode into near_slp (the regular kernel sums the rest)
+template <typename Out>
+__device__ __forceinline__ void store_slp(const RegularArgs &a, int f, int64_t items, int64_t item, int64_t off,
+                                          const Acc &acc)
+{
+    if (a.near_slp)
+        a.near_slp[(int64_t)f * items + item] =
+            make_double2(a.alpha_re * acc.sr - a.alpha_im * acc.si, a.alpha_re * acc.si + a.alpha_im * acc.sr);
+    else
+        store64(batch_matrix<Out>(a, false, f) + off, acc.sr, acc.si, a.alpha_re, a.alpha_im, a.accumulate);
+}
+
 // BATCH: frequency batch (a.nk > 1), a separate kernel so that the single
 // wave number kernel carries none of its code.
 template <typename Out, bool BATCH>
@@ -334,7 +347,7 @@ __device__ __forceinline__ void singular_pairs(const RegularArgs &a, const NearL
                         else near_dynamic(e, kf, x0, do_s, do_d, acc, pts, kf * 3.0 * a.trial_size_max <= 0.75);
                     }
                 }
-                if (do_s) store64(batch_matrix<Out>(a, false, f) + off, acc.sr, acc.si, a.alpha_re, a.alpha_im, a.accumulate);
+                if (do_s) store_slp<Out>(a, f, total, item, off, acc);
                 if (do_d) store64(batch_matrix<Out>(a, true, f) + off, acc.dr, acc.di, a.alpha_re, a.alpha_im, a.accumulate);
             }
             continue;
@@ -371,7 +384,7 @@ __device__ __forceinline__ void singular_pairs(const RegularArgs &a, const NearL
                 atomicCAS(err, 0, (int)min(item + 1, (int64_t)0x7fffffff));
                 break;
             }
-            if (do_s) store64(batch_matrix<Out>(a, false, f) + off, acc.sr, acc.si, a.alpha_re, a.alpha_im, a.accumulate);
+            if (do_s) store_slp<Out>(a, f, total, item, off, acc);
             if (do_d) store64(batch_matrix<Out>(a, true, f) + off, acc.dr, acc.di, a.alpha_re, a.alpha_im, a.accumulate);
         }
     }

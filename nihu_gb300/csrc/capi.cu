@@ -129,6 +129,8 @@ void free_near(nihu_gb_ctx *ctx, NearList &nl)
 {
     dfree(ctx, nl.col_ptr);
     dfree(ctx, nl.rows);
+    dfree(ctx, nl.row_ptr);
+    dfree(ctx, nl.row_ent);
     nl = NearList();
 }
 
@@ -237,6 +239,53 @@ nihu_gb_status get_near(nihu_gb_ctx *ctx, const nihu_gb_mesh *test, const nihu_g
     if (e != cudaSuccess) { free_near(ctx, nl); return cuda_fail(ctx, e, "nearly singular pair fill"); }
     ctx->near[key] = nl;
     *out = &ctx->near[key];
+    return NIHU_GB_OK;
+}
+
+// the row index of a near list (NearList::row_ptr / row_ent), built once on
+// the host from the column lists: the items of each row in column order
+nihu_gb_status near_rows(nihu_gb_ctx *ctx, NearList *nl, bool same_mesh, int64_t n_rows)
+{
+    if (nl->row_ptr) return NIHU_GB_OK;
+    const int64_t nnz = nl->nnz, n_cols = nl->n_cols;
+    if (nnz + n_cols > 0x7fffffff) return fail(ctx, NIHU_GB_ERR_INVALID_ARGUMENT, "near list too long for a row index");
+    std::vector<int64_t> cp(n_cols + 1);
+    std::vector<int> rows(nnz);
+    CK(cudaMemcpyAsync(cp.data(), nl->col_ptr, sizeof(int64_t) * cp.size(), cudaMemcpyDeviceToHost, ctx->stream));
+    if (nnz) CK(cudaMemcpyAsync(rows.data(), nl->rows, sizeof(int) * nnz, cudaMemcpyDeviceToHost, ctx->stream));
+    nihu_gb_status st = sync(ctx);
+    if (st) return st;
+    const int64_t n_self = same_mesh ? std::min(n_cols, n_rows) : 0;
+    std::vector<int64_t> rp(n_rows + 1, 0);
+    for (int64_t p = 0; p < nnz; ++p) {
+        if (rows[p] < 0 || rows[p] >= n_rows) return fail(ctx, NIHU_GB_ERR_RUNTIME, "near list row out of range");
+        ++rp[rows[p] + 1];
+    }
+    for (int64_t j = 0; j < n_self; ++j) ++rp[j + 1];
+    for (int64_t i = 0; i < n_rows; ++i) rp[i + 1] += rp[i];
+    std::vector<int2> ent(std::max<int64_t>(rp[n_rows], 1));
+    std::vector<int64_t> fill(rp.begin(), rp.end() - 1);
+    for (int64_t j = 0; j < n_cols; ++j) {
+        for (int64_t p = cp[j]; p < cp[j + 1]; ++p) ent[fill[rows[p]]++] = make_int2((int)p, (int)j);
+        if (j < n_self) ent[fill[j]++] = make_int2((int)(nnz + j), (int)j);
+    }
+    void *drp = nullptr, *dent = nullptr;
+    if ((st = dmalloc(ctx, sizeof(int64_t) * rp.size(), &drp))) return st;
+    if ((st = dmalloc(ctx, sizeof(int2) * ent.size(), &dent))) {
+        dfree(ctx, drp);
+        return st;
+    }
+    cudaError_t e = cudaMemcpyAsync(drp, rp.data(), sizeof(int64_t) * rp.size(), cudaMemcpyHostToDevice, ctx->stream);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(dent, ent.data(), sizeof(int2) * ent.size(), cudaMemcpyHostToDevice, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);  // the host vectors die here
+    if (e != cudaSuccess) {
+        dfree(ctx, drp);
+        dfree(ctx, dent);
+        return cuda_fail(ctx, e, "near list row index");
+    }
+    nl->row_ptr = (int64_t *)drp;
+    nl->row_ent = (int2 *)dent;
     return NIHU_GB_OK;
 }
 
@@ -1829,10 +1878,13 @@ nihu_gb_status upload_ks(nihu_gb_ctx *ctx, const double *ks, int nk, const doubl
 namespace {
 
 // frequency batch of one mesh pair: matrices f at out + f * mat_stride, or
-// (outs_dev, nk > 1) at the device pointers outs_dev[f] / outs_dev[nk + f]
+// (outs_dev, nk > 1) at the device pointers outs_dev[f] / outs_dev[nk + f];
+// with rhs_b (SLP and DLP, one mesh): b_f = SLP_f q_f at rhs_b + f * n from
+// q_f at rhs_q + f * n, and no SLP matrix (out_slp unused)
 nihu_gb_status assemble_batch(nihu_gb_ctx *ctx, const nihu_gb_mesh *test, const nihu_gb_mesh *trial, int family, int ops,
                               const double *ks, int nk, int precision, int dtype, void *out_slp, void *out_dlp,
-                              int64_t ld, int64_t mat_stride, void *const *outs_dev, bool force_batch = false)
+                              int64_t ld, int64_t mat_stride, void *const *outs_dev, bool force_batch = false,
+                              const double2 *rhs_q = nullptr, double2 *rhs_b = nullptr)
 {
     nihu_gb_status st;
     NearList *nl = nullptr;
@@ -1864,8 +1916,25 @@ nihu_gb_status assemble_batch(nihu_gb_ctx *ctx, const nihu_gb_mesh *test, const 
     a.mat_stride = mat_stride;
     a.force_batch = force_batch;
     a.outs = (nk > 1 || force_batch) ? outs_dev : nullptr;
+    if (rhs_b) {
+        if ((st = near_rows(ctx, nl, a.same_mesh, test->n))) return st;
+        void *rp, *ns;
+        const int64_t items = nl->nnz + (a.same_mesh ? trial->n : 0);
+        a.force_batch = 1;
+        a.out_s = nullptr;
+        if ((st = scratch(ctx, "sw_rpart", rhs_part_bytes(a), &rp))) return st;
+        if ((st = scratch(ctx, "sw_nslp", 16 * (size_t)std::max<int64_t>(items, 1) * nk, &ns))) return st;
+        a.rhs_q = rhs_q;
+        a.rhs_part = rp;
+        a.near_slp = (double2 *)ns;
+    }
     if ((st = upload_ks(ctx, ks, nk, &a.ks, &a.ks32))) return st;
     if ((st = assemble_panel(ctx, a, nl))) return st;
+    if (rhs_b) {
+        Phase ph(ctx, "rhs_reduce");
+        CK(launch_rhs_reduce(a, *nl, rhs_b, ctx->stream));
+        ctx->launches += 1;
+    }
     return check_flag(ctx);
 }
 
@@ -2106,25 +2175,17 @@ nihu_gb_status sweep_solve_impl(nihu_gb_ctx *ctx, int n_meshes, const nihu_gb_me
         }
         const int cnt = (int)fs.size();
         const int64_t stride = n * n;
-        void *G, *H, *part;
+        void *H;
         const std::string tag = std::to_string(i);
-        if ((st = scratch(ctx, ("swb_G" + tag).c_str(), 8 * (size_t)stride * cnt, &G))) return st;
         if ((st = scratch(ctx, ("swb_H" + tag).c_str(), 8 * (size_t)stride * cnt, &H))) return st;
-        if ((st = nihu_gb_assemble_sweep(ctx, mesh, mesh, family, NIHU_GB_SLP | NIHU_GB_DLP, ki.data(), cnt, precision,
-                                         NIHU_GB_C64, G, H, n, stride)))
+        // the DLP matrices and b_f = SLP_f q_f (the mesh's instances are
+        // contiguous in q_dev / b): no SLP matrix
+        const int64_t o = off[fs[0]];
+        if ((st = assemble_batch(ctx, mesh, mesh, family, NIHU_GB_SLP | NIHU_GB_DLP, ki.data(), cnt, precision,
+                                 NIHU_GB_C64, nullptr, H, n, stride, nullptr, true, q_dev + o, b + o)))
             return st;
         CK(launch_add_identity_batched((int)n, -0.5, 0.0, NIHU_GB_C64, H, n, stride, cnt, ctx->stream));
         ctx->launches += 1;
-        // b_f = SLP_f q_f: the mesh's instances are contiguous in q_dev / b
-        const int splits = gemv_splits(n, n, NIHU_GB_C64);
-        if ((st = scratch(ctx, "swb_part", 16 * (size_t)splits * n * cnt, &part))) return st;
-        const int64_t o = off[fs[0]];
-        {
-            Phase ph(ctx, "gemv_c64");
-            CK(launch_gemv_batched(NIHU_GB_C64, G, n, n, n, stride, cnt, q_dev + o, b + o, 1.0, 0.0, 0.0, 0.0,
-                                   (double2 *)part, splits, ctx->stream, nullptr));
-        }
-        ctx->launches += 2;
         for (int j = 0; j < cnt; ++j) {
             const int f = fs[j];
             sys[f] = BatchSystem{(const char *)H + 8 * (size_t)stride * j, n, n, b + off[f], p_dev + off[f],
@@ -2265,7 +2326,7 @@ struct nihu_gb_server {
         double k = 0.0;
         std::vector<double2> q;  // Neumann data until admission; then the result p
         size_t held = 0;         // budget bytes held
-        void *G = nullptr, *H = nullptr, *blk = nullptr;
+        void *H = nullptr, *blk = nullptr;  // DLP matrix; vectors and Krylov state
         double2 *dq = nullptr, *b = nullptr, *x = nullptr, *V = nullptr, *S = nullptr;
         int slot = -1;  // status word in the server's state array
         PersistentState st{};
@@ -2300,10 +2361,9 @@ size_t srv_block_bytes(int64_t n, int m)
 void srv_release(nihu_gb_server *sv, SrvReq *r)
 {
     cudaStream_t s = sv->ctx->stream;
-    if (r->G) cudaFreeAsync(r->G, s);
     if (r->H) cudaFreeAsync(r->H, s);
     if (r->blk) cudaFreeAsync(r->blk, s);
-    r->G = r->H = r->blk = nullptr;
+    r->H = r->blk = nullptr;
     if (r->slot >= 0) sv->free_slots.push_back(r->slot);
     r->slot = -1;
     sv->held -= r->held;
@@ -2378,7 +2438,7 @@ extern "C" nihu_gb_status nihu_gb_server_submit(nihu_gb_server *sv, int mesh, do
     if (mesh < 0 || mesh >= (int)sv->meshes.size() || !std::isfinite(k) || !q)
         return fail(ctx, NIHU_GB_ERR_INVALID_ARGUMENT, "nihu_gb_server_submit: bad argument");
     const int64_t n = sv->meshes[mesh]->n;
-    const size_t need = 16 * (size_t)n * n + srv_block_bytes(n, sv->restart);
+    const size_t need = 8 * (size_t)n * n + srv_block_bytes(n, sv->restart);
     if (need > sv->budget)
         return fail(ctx, NIHU_GB_ERR_OUT_OF_MEMORY, "nihu_gb_server_submit: request larger than the HBM budget");
     SrvReq *r = new SrvReq;
@@ -2405,11 +2465,10 @@ extern "C" nihu_gb_status nihu_gb_server_step(nihu_gb_server *sv, int *n_queued,
         SrvReq *r = sv->queue.front();
         const int64_t n = sv->meshes[r->mesh]->n;
         const size_t mat = 8 * (size_t)n * n, blk = srv_block_bytes(n, m);
-        if (sv->held + 2 * mat + blk > sv->budget) break;
-        CK(cudaMallocFromPoolAsync(&r->G, mat, sv->pool, s));
+        if (sv->held + mat + blk > sv->budget) break;
         CK(cudaMallocFromPoolAsync(&r->H, mat, sv->pool, s));
         CK(cudaMallocFromPoolAsync(&r->blk, blk, sv->pool, s));
-        r->held = 2 * mat + blk;
+        r->held = mat + blk;
         sv->held += r->held;
         char *p = (char *)r->blk;
         r->dq = (double2 *)p;
@@ -2426,7 +2485,8 @@ extern "C" nihu_gb_status nihu_gb_server_step(nihu_gb_server *sv, int *n_queued,
         sv->queue.pop_front();
         fresh.push_back(r);
     }
-    // 2. assembly of the new requests, one frequency batch per mesh; right-hand sides
+    // 2. assembly of the new requests, one frequency batch per mesh: the DLP
+    // matrices and the right-hand sides b = SLP q (no SLP matrix)
     std::vector<std::vector<void *>> tables;  // host sources of the pointer uploads, alive until the round's wait
     for (int i = 0; i < (int)sv->meshes.size(); ++i) {
         std::vector<SrvReq *> grp;
@@ -2439,10 +2499,14 @@ extern "C" nihu_gb_status nihu_gb_server_step(nihu_gb_server *sv, int *n_queued,
         std::vector<double> ks(nk);
         tables.emplace_back(2 * (size_t)nk);
         std::vector<void *> &tab = tables.back();
+        void *gq, *gb;  // the group's Neumann data and right-hand sides, back to back
+        if ((st = scratch(ctx, "srv_q", 16 * (size_t)n * nk, &gq))) return st;
+        if ((st = scratch(ctx, "srv_b", 16 * (size_t)n * nk, &gb))) return st;
         for (int f = 0; f < nk; ++f) {
             ks[f] = grp[f]->k;
-            tab[f] = grp[f]->G;
+            tab[f] = nullptr;
             tab[nk + f] = grp[f]->H;
+            CK(cudaMemcpyAsync((double2 *)gq + (size_t)f * n, grp[f]->dq, 16 * (size_t)n, cudaMemcpyDeviceToDevice, s));
         }
         // always the frequency-batch kernels: an entry is then the same whatever else arrived with it
         void *douts = nullptr;
@@ -2450,20 +2514,14 @@ extern "C" nihu_gb_status nihu_gb_server_step(nihu_gb_server *sv, int *n_queued,
         if ((st = scratch(ctx, name.c_str(), sizeof(void *) * 2 * (size_t)nk, &douts))) return st;
         CK(cudaMemcpyAsync(douts, tab.data(), sizeof(void *) * 2 * (size_t)nk, cudaMemcpyHostToDevice, s));
         if ((st = assemble_batch(ctx, mesh, mesh, sv->family, NIHU_GB_SLP | NIHU_GB_DLP, ks.data(), nk, sv->precision,
-                                 NIHU_GB_C64, grp[0]->G, grp[0]->H, n, n * n, (void *const *)douts, true)))
+                                 NIHU_GB_C64, nullptr, grp[0]->H, n, n * n, (void *const *)douts, true,
+                                 (const double2 *)gq, (double2 *)gb)))
             return st;
-        const int splits = gemv_splits(n, n, NIHU_GB_C64);
-        void *part;
-        if ((st = scratch(ctx, "srv_part", 16 * (size_t)splits * n, &part))) return st;
-        for (SrvReq *r : grp) {
+        for (int f = 0; f < nk; ++f) {
+            SrvReq *r = grp[f];
             CK(launch_add_identity((int)n, -0.5, 0.0, NIHU_GB_C64, r->H, n, s));
-            CK(timed_gemv(ctx, NIHU_GB_C64, r->G, n, n, n, r->dq, r->b, 1.0, 0.0, 0.0, 0.0, (double2 *)part, splits));
+            CK(cudaMemcpyAsync(r->b, (double2 *)gb + (size_t)f * n, 16 * (size_t)n, cudaMemcpyDeviceToDevice, s));
             ctx->launches += 1;
-            // the single-layer matrix is only needed for the right-hand side
-            CK(cudaFreeAsync(r->G, s));
-            r->G = nullptr;
-            r->held -= 8 * (size_t)n * n;
-            sv->held -= 8 * (size_t)n * n;
         }
         sv->active.insert(sv->active.end(), grp.begin(), grp.end());
     }
@@ -2551,9 +2609,9 @@ struct nihu_gb_sweep_plan {
         int mesh = 0;
         std::vector<int> fs;       // instances, in instance order
         int64_t n = 0, first = 0;  // elements; position of the group's first instance
-        void *G = nullptr, *H = nullptr;
-        double2 *part = nullptr;
-        int splits = 1;
+        void *H = nullptr;          // DLP matrices (no SLP matrix: right-hand-side mode)
+        void *rpart = nullptr;      // regular kernel's partial sums of b
+        double2 *nslp = nullptr;    // FP64 kernel's SLP entries
         NearList *nl = nullptr;
     };
     nihu_gb_ctx *ctx = nullptr;
@@ -2643,7 +2701,7 @@ nihu_gb_status plan_capture(nihu_gb_sweep_plan *pl)
             a.alpha_re32 = 1.0f;
             a.alpha_im32 = 0.0f;
             a.unit_alpha = 1;
-            a.out_s = g.G;
+            a.out_s = nullptr;
             a.out_d = g.H;
             a.ld = g.n;
             a.j0 = 0;
@@ -2654,12 +2712,14 @@ nihu_gb_status plan_capture(nihu_gb_sweep_plan *pl)
             a.mat_stride = g.n * g.n;
             a.k_absmax = pl->kmax;
             a.force_batch = 1;
+            const int64_t o = pl->off[g.fs[0]];
+            a.rhs_q = pl->d_q + o;
+            a.rhs_part = g.rpart;
+            a.near_slp = g.nslp;
             st = assemble_panel(ctx, a, g.nl);
             if (st) break;
-            const int64_t o = pl->off[g.fs[0]];
             chk(launch_add_identity_batched((int)g.n, -0.5, 0.0, NIHU_GB_C64, g.H, g.n, g.n * g.n, cnt, s));
-            chk(launch_gemv_batched(NIHU_GB_C64, g.G, g.n, g.n, g.n, g.n * g.n, cnt, pl->d_q + o, pl->d_b + o, 1.0, 0.0,
-                                    0.0, 0.0, g.part, g.splits, s, nullptr));
+            chk(launch_rhs_reduce(a, *g.nl, pl->d_b + o, s));
         }
         chk(cudaMemsetAsync(pl->d_st, 0, sizeof(PersistentState) * (size_t)pl->nk, s));
         chk(cudaMemsetAsync(pl->pargs.counter, 0, sizeof(int), s));
@@ -2755,13 +2815,19 @@ extern "C" nihu_gb_status nihu_gb_sweep_plan_create(nihu_gb_ctx *ctx, int n_mesh
     if ((st = plan_alloc(pl.get(), sizeof(PersistentState) * (size_t)nk, &dst))) return st;
     pl->d_st = (PersistentState *)dst;
     for (auto &g : pl->groups) {
-        const size_t mat = 8 * (size_t)g.n * g.n * g.fs.size();
-        if ((st = plan_alloc(pl.get(), mat, &g.G))) return st;
-        if ((st = plan_alloc(pl.get(), mat, &g.H))) return st;
-        g.splits = gemv_splits(g.n, g.n, NIHU_GB_C64);
-        if ((st = plan_alloc(pl.get(), 16 * (size_t)g.splits * g.n * g.fs.size(), &p))) return st;
-        g.part = (double2 *)p;
+        const size_t cnt = g.fs.size();
+        if ((st = plan_alloc(pl.get(), 8 * (size_t)g.n * g.n * cnt, &g.H))) return st;
         if ((st = get_near(ctx, meshes[g.mesh], meshes[g.mesh], &g.nl))) return st;
+        if ((st = near_rows(ctx, g.nl, true, g.n))) return st;
+        RegularArgs ra;
+        ra.test = meshes[g.mesh]->dm;
+        ra.precision = precision;
+        ra.j0 = 0;
+        ra.j1 = (int)g.n;
+        ra.nk = (int)cnt;
+        if ((st = plan_alloc(pl.get(), rhs_part_bytes(ra), &g.rpart))) return st;
+        if ((st = plan_alloc(pl.get(), 16 * (size_t)(g.nl->nnz + g.n) * cnt, &p))) return st;
+        g.nslp = (double2 *)p;
     }
     // the persistent launch: items, order and launch shape fixed by the plan
     std::vector<PersistentItem> items(nk);

@@ -15,6 +15,12 @@ struct NearList {
     int64_t nnz = 0;
     int64_t *col_ptr = nullptr;  // [n_cols + 1]
     int *rows = nullptr;         // [nnz]
+    // row index of the FP64 kernel's items (built on demand): the items of
+    // row i at row_ent[row_ptr[i] .. row_ptr[i + 1]), each (item, column),
+    // in increasing column order; items are near-list positions, then
+    // nnz + j for the self term of column j (same mesh)
+    int64_t *row_ptr = nullptr;  // [n_rows + 1]
+    int2 *row_ent = nullptr;
 };
 
 // mesh.cu -----------------------------------------------------------------
@@ -67,6 +73,15 @@ struct RegularArgs {
     // 1: the frequency-batch kernels even for nk = 1, so that an entry is the
     // same whatever the batch it is assembled in
     int force_batch = 0;
+    // frequency batch with right-hand sides b_f = SLP_f q_f in place of the SLP
+    // matrices (all columns in one launch, j0 = 0): q_f at rhs_q + f * trial.n;
+    // the regular kernel leaves per block of REG_COLS columns cb the partial
+    // sums rhs_part[(f * n_cb + cb) * test.n + i] (float2 in FP32 mode, double2
+    // in FP64) over the block's regular pairs; the FP64 kernel leaves the SLP
+    // entry of its item p (NearList row index numbering) in near_slp[f * items + p]
+    const double2 *rhs_q = nullptr;
+    void *rhs_part = nullptr;
+    double2 *near_slp = nullptr;
 };
 
 // matrix f of a frequency batch (dlp: the DLP output)
@@ -77,6 +92,11 @@ __device__ __forceinline__ Out *batch_matrix(const RegularArgs &a, bool dlp, int
     return reinterpret_cast<Out *>(dlp ? a.out_d : a.out_s) + (int64_t)f * a.mat_stride;
 }
 cudaError_t launch_assemble_regular(const RegularArgs &a, cudaStream_t s);
+// right-hand-side mode: the partial sums per wave number of the regular kernel
+size_t rhs_part_bytes(const RegularArgs &a);
+// b_f(i) = sum_cb rhs_part_f(cb, i) + sum over row i's items p of
+// near_slp_f(p) q_f(column of p), in FP64 and a fixed order
+cudaError_t launch_rhs_reduce(const RegularArgs &a, const NearList &near, double2 *b, cudaStream_t s);
 
 // assemble_singular.cu ----------------------------------------------------
 // nearly singular pairs of columns [j0, j1) and, for the same mesh, the

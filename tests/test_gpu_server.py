@@ -110,8 +110,8 @@ def test_budget_admission_and_oversize_requests(gpu_ctx):
     arrays = [meshes.icosphere(s) for s in (2, 3)]
     ms = [g.create_mesh(*a) for a in arrays]
     n1 = ms[1].num_elements
-    # room for one request of the 1280-element mesh at a time (two 8 n^2 matrices + state)
-    budget = 16 * n1 * n1 + 60 * 16 * n1 + (1 << 20)
+    # room for one request of the 1280-element mesh at a time (its 8 n^2 DLP matrix + state)
+    budget = 8 * n1 * n1 + 60 * 16 * n1 + (1 << 20)
     sv = g.Server(ms, hbm_budget_bytes=budget, tol=1e-6, quantum=0, ctx=gpu_ctx)
     rng = np.random.default_rng(23)
     ids = [sv.submit(1, float(k), meshes.plane_wave_neumann(*arrays[1], float(k), [rng.standard_normal(3)])[:, 0])
