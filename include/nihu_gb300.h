@@ -426,6 +426,11 @@ nihu_gb_status nihu_gb_sweep_plan_create(nihu_gb_ctx *ctx, int n_meshes, const n
  * at max_iters. */
 nihu_gb_status nihu_gb_sweep_plan_run(nihu_gb_sweep_plan *plan, const double *ks, const void *q, void *p, int *iters,
                                       double *rel_residuals, int *converged);
+/* The plan's pinned staging buffers (complex128, the instances' columns back
+ * to back in instance order, as q and p of nihu_gb_sweep_plan_run).  A run
+ * given these very pointers as q and p reads and writes them in place, with
+ * no host copy; they stay valid until nihu_gb_sweep_plan_destroy. */
+nihu_gb_status nihu_gb_sweep_plan_host_buffers(nihu_gb_sweep_plan *plan, void **q, void **p);
 void nihu_gb_sweep_plan_destroy(nihu_gb_sweep_plan *plan);
 
 /* ------------------------------------------------------------ serving */

@@ -689,28 +689,43 @@ class SweepPlan:
             self.ctx.handle, len(self._dms), handles, family, self.nk, self.mesh_of.ctypes.data, float(k_max),
             C.REGULAR_FP64 if precision == "fp64" else C.REGULAR_FP32, restart, max_iters, tol, ctypes.byref(h)))
         self.handle = h
+        # the plan's pinned staging (instance order): Neumann data are written
+        # and solutions read in place, with no further host copy
+        self._off = np.concatenate([[0], np.cumsum(self.sizes)]).astype(np.int64)
+        total = int(self._off[-1])
+        qp, pp = ctypes.c_void_p(), ctypes.c_void_p()
+        self.ctx.check(C.lib().nihu_gb_sweep_plan_host_buffers(h, ctypes.byref(qp), ctypes.byref(pp)))
+        self._qptr, self._pptr = qp, pp
+        self._q = np.frombuffer((ctypes.c_double * (2 * total)).from_address(qp.value), np.complex128)
+        self._p = np.frombuffer((ctypes.c_double * (2 * total)).from_address(pp.value), np.complex128)
 
     def run(self, ks, q=None, check: bool = True):
         """Returns (list of p_f, iterations, relative residual estimates, converged)."""
         ks = np.ascontiguousarray(ks, dtype=np.float64)
         if ks.shape != (self.nk,):
             raise ValueError("one wave number per instance")
-        total = sum(self.sizes)
-        qf = np.ones(total, np.complex128) if q is None else np.concatenate([_c128(v) for v in q])
-        if qf.shape != (total,):
-            raise ValueError("q: one vector per instance with its mesh's element count")
-        pf = np.zeros_like(qf)
+        if q is None:
+            self._q[:] = 1.0
+        else:
+            if len(q) != self.nk:
+                raise ValueError("q: one vector per instance with its mesh's element count")
+            for f, v in enumerate(q):
+                v = np.asarray(v)
+                if v.shape != (self.sizes[f],):
+                    raise ValueError("q: one vector per instance with its mesh's element count")
+                self._q[self._off[f]:self._off[f + 1]] = v
         it = np.zeros(self.nk, np.int32)
         rel = np.zeros(self.nk)
         conv = np.zeros(self.nk, np.int32)
-        st = C.lib().nihu_gb_sweep_plan_run(self.handle, ks.ctypes.data, qf.ctypes.data, pf.ctypes.data,
+        st = C.lib().nihu_gb_sweep_plan_run(self.handle, ks.ctypes.data, self._qptr, self._pptr,
                                             it.ctypes.data, rel.ctypes.data, conv.ctypes.data)
         if st != C.OK and (check or st != 6):
             self.ctx.check(st)
-        return np.split(pf, np.cumsum(self.sizes)[:-1]), it, rel, conv.astype(bool)
+        return np.split(self._p.copy(), self._off[1:-1]), it, rel, conv.astype(bool)
 
     def close(self):
         if getattr(self, "handle", None):
+            self._q = self._p = None  # views of the plan's staging
             C.lib().nihu_gb_sweep_plan_destroy(self.handle)
             self.handle = None
 

@@ -59,7 +59,7 @@ __device__ __forceinline__ void point_freq(const PointGeom<R> &p, R k, R &sr, R 
     if constexpr (FAM == FAM_HELMHOLTZ) {
         R kr = k * p.r;
         R s, c;
-        if constexpr (sizeof(R) == 4) sincos_2pi(kr * 0.159154943091895335769f, s, c);
+        if constexpr (sizeof(R) == 4) sincos_reduced(kr, s, c);
         else sincos(kr, &s, &c);
         sr += p.gs * c;
         si -= p.gs * s;
@@ -109,6 +109,38 @@ __device__ __forceinline__ void rhs_add(R2 &acc, const R2 q, R sr, R si)
     acc.x += sr * q.x - si * q.y;
     acc.y += sr * q.y + si * q.x;
 }
+
+// frequency batches store plain entries (unit scale, no accumulation:
+// launch_assemble_regular refuses anything else)
+template <typename Out, typename R>
+__device__ __forceinline__ void store_plain(Out *p, R re, R im)
+{
+    Out o;
+    o.x = re;
+    o.y = im;
+    *p = o;
+}
+
+// the DLP outputs of a frequency batch from wave number f on: a pointer that
+// steps by mat_stride, or the device table outs (separate matrices)
+template <typename Out>
+struct BatchCursor {
+    Out *p;
+    int64_t step, off;
+    void *const *tab;
+    __device__ __forceinline__ BatchCursor(const RegularArgs &a, bool dlp, int f, int64_t off_)
+        : step(a.mat_stride), off(off_), tab(a.outs ? a.outs + (dlp ? a.nk : 0) + f : nullptr)
+    {
+        Out *base = reinterpret_cast<Out *>(dlp ? a.out_d : a.out_s);
+        p = (tab || !base) ? nullptr : base + (int64_t)f * a.mat_stride + off;
+    }
+    __device__ __forceinline__ Out *get() const { return tab ? reinterpret_cast<Out *>(*tab) + off : p; }
+    __device__ __forceinline__ void next()
+    {
+        if (tab) ++tab;
+        else p += step;
+    }
+};
 
 // Squared distance ratio above which a pair is certainly regular with the
 // 1-point rule for both SLP (x >= 9.1) and DLP (x >= 15.8): 15.8^2 with a
@@ -214,16 +246,25 @@ __global__ void __launch_bounds__(REG_THREADS) k_regular(RegularArgs a)
                 const int64_t off = (int64_t)(j - a.j0) * a.ld + i;
                 if constexpr (BATCH) {
                     const PointGeom<float> gm = point_geom<float>(fx, fy, fz, p.x, p.y, p.z, p.w, R(DO_S), R(DO_D));
+                    BatchCursor<Out> cs(a, false, f_lo, off), cd(a, true, f_lo, off);
+                    R2 *acc = s_acc + threadIdx.x;
+                    const R2 *qc = s_q + c;
+                    const float *kp = a.ks32 + f_lo;
                     for (int f = f_lo; f < f_hi; ++f) {
                         R sr = 0, si = 0, dr = 0, di = 0;
-                        point_freq<FAM, float>(gm, a.ks32[f], sr, si, dr, di);
+                        point_freq<FAM, float>(gm, *kp++, sr, si, dr, di);
                         if (row_ok) {
-                            if constexpr (RHS)
-                                rhs_add(s_acc[(f - f_lo) * REG_THREADS + threadIdx.x], s_q[(f - f_lo) * REG_COLS + c], sr, si);
-                            else if (DO_S)
-                                store_entry(batch_matrix<Out>(a, false, f) + off, sr, si, are, aim, unit_alpha, accumulate);
-                            if (DO_D) store_entry(batch_matrix<Out>(a, true, f) + off, dr, di, are, aim, unit_alpha, accumulate);
+                            if constexpr (RHS) rhs_add(*acc, *qc, sr, si);
+                            else if (DO_S) store_plain(cs.get(), sr, si);
+                            if (DO_D) store_plain(cd.get(), dr, di);
                         }
+                        if constexpr (RHS) {
+                            acc += REG_THREADS;
+                            qc += REG_COLS;
+                        } else if (DO_S) {
+                            cs.next();
+                        }
+                        if (DO_D) cd.next();
                     }
                 } else {
                     R sr = 0, si = 0, dr = 0, di = 0;
@@ -252,6 +293,10 @@ __global__ void __launch_bounds__(REG_THREADS) k_regular(RegularArgs a)
         const int64_t base = ((int64_t)j * 2 + par) * SLOTS;
         if constexpr (BATCH) {
             // frequency batch: each point's geometry once per tile of wave numbers
+            const int64_t off = (int64_t)(j - a.j0) * a.ld + i;
+            BatchCursor<Out> cs(a, false, f_lo, off), cd(a, true, f_lo, off);
+            R2 *acc = s_acc + threadIdx.x;
+            const R2 *qc = s_q + c;
             for (int f0 = f_lo; f0 < f_hi; f0 += FREQ_TILE) {
                 R kf[FREQ_TILE], sr[FREQ_TILE], si[FREQ_TILE], dr[FREQ_TILE], di[FREQ_TILE];
 #pragma unroll
@@ -283,14 +328,18 @@ __global__ void __launch_bounds__(REG_THREADS) k_regular(RegularArgs a)
 #pragma unroll
                 for (int u = 0; u < FREQ_TILE; ++u) {
                     if (f0 + u >= f_hi) break;
-                    const int64_t off = (int64_t)(j - a.j0) * a.ld + i;
-                    if constexpr (RHS)
-                        rhs_add(s_acc[(f0 + u - f_lo) * REG_THREADS + threadIdx.x], s_q[(f0 + u - f_lo) * REG_COLS + c],
-                                sr[u], si[u]);
-                    else if (DO_S)
-                        store_entry(batch_matrix<Out>(a, false, f0 + u) + off, sr[u], si[u], are, aim, unit_alpha, accumulate);
-                    if (DO_D)
-                        store_entry(batch_matrix<Out>(a, true, f0 + u) + off, dr[u], di[u], are, aim, unit_alpha, accumulate);
+                    if constexpr (RHS) {
+                        rhs_add(*acc, *qc, sr[u], si[u]);
+                        acc += REG_THREADS;
+                        qc += REG_COLS;
+                    } else if (DO_S) {
+                        store_plain(cs.get(), sr[u], si[u]);
+                        cs.next();
+                    }
+                    if (DO_D) {
+                        store_plain(cd.get(), dr[u], di[u]);
+                        cd.next();
+                    }
                 }
             }
         } else {
@@ -416,6 +465,7 @@ cudaError_t launch_assemble_regular(const RegularArgs &a, cudaStream_t s)
         const int64_t xy = (int64_t)grid.x * grid.y;
         const int64_t want = (4 * (int64_t)sms + xy - 1) / xy;
         const int most = (a.nk + FREQ_TILE - 1) / FREQ_TILE;
+        if (a.accumulate || !a.unit_alpha) return cudaErrorInvalidValue;  // batches store plain entries
         grid.z = (unsigned)std::max<int64_t>(1, std::min<int64_t>(want, most));
         // right-hand-side mode: at most rhs_f_max wave numbers per block
         if (a.rhs_part) {

@@ -34,7 +34,7 @@ __device__ __forceinline__ void eval_bm(R rx, R ry, R rz, R wj, R ny0, R ny1, R 
     if constexpr (FAM == FAM_HELMHOLTZ) {
         const R kr = k * (r2 * rinv);
         R s, c;
-        if constexpr (sizeof(R) == 4) sincos_2pi(kr * 0.159154943091895335769f, s, c);
+        if constexpr (sizeof(R) == 4) sincos_reduced(kr, s, c);
         else sincos(kr, &s, &c);
         // (1 + ikr) e^{-ikr} = p + i q
         const R p = c + kr * s, q = kr * c - s;
@@ -81,7 +81,7 @@ __device__ __forceinline__ void eval_h(R rx, R ry, R rz, R wj, R ny0, R ny1, R n
     if constexpr (FAM == FAM_HELMHOLTZ) {
         const R kr = k * (r2 * rinv);
         R s, c;
-        if constexpr (sizeof(R) == 4) sincos_2pi(kr * 0.159154943091895335769f, s, c);
+        if constexpr (sizeof(R) == 4) sincos_reduced(kr, s, c);
         else sincos(kr, &s, &c);
         const R u = m - aa * kr * kr, v = kr * m;
         o.hr += g3 * (u * c + v * s);

@@ -2036,6 +2036,74 @@ nihu_gb_status plan_persistent(nihu_gb_ctx *ctx, const std::vector<int64_t> &ns,
     return NIHU_GB_OK;
 }
 
+// One persistent launch of a plan: its items (indices into the caller's item
+// array) in processing order, the largest system and the launch shape
+struct PersistentLaunch {
+    std::vector<int> order;
+    int64_t n_max = 1;
+    PersistentPlan plan;
+};
+
+// The persistent launches over items of sizes ns, each in order of
+// decreasing key: one over all; or, when the shape chosen for the larger
+// systems (n >= n_max / 2) leaves SMs idle -- clusters of 8 CTAs fit whole
+// GPCs, not every SM -- and smaller systems exist, a second launch of the
+// smaller systems, one CTA per system, sized to the idle SMs and started
+// beside the first as its programmatic dependent (launch_persistent_gmres).
+nihu_gb_status plan_launches(nihu_gb_ctx *ctx, const std::vector<int64_t> &ns, const std::vector<double> &key, int m,
+                             std::vector<PersistentLaunch> *out)
+{
+    nihu_gb_status st;
+    out->clear();
+    const int count = (int)ns.size();
+    int64_t n_max = 1;
+    for (int64_t n : ns) n_max = std::max(n_max, n);
+    auto sorted = [&](std::vector<int> v) {
+        std::stable_sort(v.begin(), v.end(), [&](int x, int y) { return key[x] > key[y]; });
+        return v;
+    };
+    std::vector<int> big, small;
+    for (int q = 0; q < count; ++q) (2 * ns[q] >= n_max ? big : small).push_back(q);
+    if (!small.empty()) {
+        PersistentLaunch A, B;
+        std::vector<int64_t> nsa;
+        for (int q : big) nsa.push_back(ns[q]);
+        for (int q : small) B.n_max = std::max(B.n_max, ns[q]);
+        if ((st = plan_persistent(ctx, nsa, m, &A.plan))) return st;
+        int sms = 0, smem_optin = 0;
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device);
+        cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, ctx->device);
+        const int spare = sms - A.plan.cluster * A.plan.clusters;
+        const int vs = persistent_smem_layout((int)B.n_max, 1, m, 1).total <= (size_t)smem_optin ? 1 : 0;
+        int act = 0;
+        size_t smem = 0;
+        if (A.plan.cluster >= 4 && spare >= 1 && persistent_smem_layout((int)B.n_max, 1, m, vs).total <= (size_t)smem_optin) {
+            if (persistent_gmres_plan((int)B.n_max, m, 1, vs, (int)small.size(), &act, &smem) == cudaSuccess) {
+                B.plan.cluster = 1;
+                B.plan.clusters = std::min(act, spare);
+                B.plan.vx_smem = vs;
+                B.plan.smem = smem;
+                A.order = sorted(big);
+                A.n_max = n_max;
+                B.order = sorted(small);
+                CK(persistent_gmres_smem_limit(std::max(A.plan.smem, B.plan.smem)));
+                out->push_back(A);
+                out->push_back(B);
+                return NIHU_GB_OK;
+            }
+            cudaGetLastError();
+        }
+    }
+    PersistentLaunch one;
+    if ((st = plan_persistent(ctx, ns, m, &one.plan))) return st;
+    std::vector<int> all(count);
+    for (int q = 0; q < count; ++q) all[q] = q;
+    one.order = sorted(all);
+    one.n_max = n_max;
+    out->push_back(one);
+    return NIHU_GB_OK;
+}
+
 // one persistent launch over the items (states in device memory), in order
 // of decreasing `work`; asynchronous on the context stream
 nihu_gb_status launch_persistent(nihu_gb_ctx *ctx, std::vector<PersistentItem> &items, const std::vector<double> &work,
@@ -2050,44 +2118,57 @@ nihu_gb_status launch_persistent(nihu_gb_ctx *ctx, std::vector<PersistentItem> &
         ns[f] = items[f].n;
         n_max = std::max<int64_t>(n_max, items[f].n);
     }
-    PersistentPlan plan;
-    if ((st = plan_persistent(ctx, ns, m, &plan))) return st;
+    std::vector<PersistentLaunch> launches;
+    if ((st = plan_launches(ctx, ns, work, m, &launches))) return st;
     int l2 = 0;
     cudaDeviceGetAttribute(&l2, cudaDevAttrL2CacheSize, ctx->device);
-    for (PersistentItem &it : items) {
-        it.vec = (it.n % 2 == 0) && (it.lda % 2 == 0) && ((reinterpret_cast<uintptr_t>(it.A) & 15) == 0);
-        it.stream = 8.0 * (double)it.n * (double)it.n * std::min(count, plan.clusters) > 0.5 * l2;
-    }
-    std::vector<int> order(count);
-    for (int f = 0; f < count; ++f) order[f] = f;
-    std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return work[x] > work[y]; });
-    void *pitems, *porder, *pcnt, *pvx = nullptr;
+    for (const PersistentLaunch &L : launches)
+        for (int q : L.order) {
+            PersistentItem &it = items[q];
+            it.vec = (it.n % 2 == 0) && (it.lda % 2 == 0) && ((reinterpret_cast<uintptr_t>(it.A) & 15) == 0);
+            it.stream = 8.0 * (double)it.n * (double)it.n * std::min<int>((int)L.order.size(), L.plan.clusters) >
+                        0.5 * l2;
+        }
+    void *pitems;
     if ((st = scratch(ctx, "pg_items", sizeof(PersistentItem) * (size_t)count, &pitems))) return st;
-    if ((st = scratch(ctx, "pg_order", sizeof(int) * (size_t)count, &porder))) return st;
-    if ((st = scratch(ctx, "pg_counter", sizeof(int), &pcnt))) return st;
-    if (!plan.vx_smem && (st = scratch(ctx, "pg_vx", 8 * (size_t)plan.clusters * n_max, &pvx))) return st;
-    PersistentArgs a;
-    a.items = (const PersistentItem *)pitems;
-    a.order = (const int *)porder;
-    a.count = count;
-    a.n_max = (int)n_max;
-    a.restart = m;
-    a.max_iters = max_iters;
-    a.quantum = quantum;
-    a.tol = tol;
-    a.counter = (int *)pcnt;
-    a.vxg = (float2 *)pvx;
     CK(cudaMemcpyAsync(pitems, items.data(), sizeof(PersistentItem) * count, cudaMemcpyHostToDevice, ctx->stream));
-    CK(cudaMemcpyAsync(porder, order.data(), sizeof(int) * count, cudaMemcpyHostToDevice, ctx->stream));
-    CK(cudaMemsetAsync(pcnt, 0, sizeof(int), ctx->stream));
-    {
-        // the phase name records the launch shape: clusters x CTAs per cluster
-        const std::string name = "persistent_gmres[" + std::to_string(plan.clusters) + "x" + std::to_string(plan.cluster) +
-                                 (plan.vx_smem ? "" : ",vx global") + "]";
-        Phase ph(ctx, name.c_str());
-        CK(launch_persistent_gmres(a, plan.cluster, plan.clusters, plan.smem, ctx->stream));
+    std::vector<PersistentArgs> args;
+    std::string name = "persistent_gmres[";  // the launch shapes: clusters x CTAs per cluster
+    for (size_t t = 0; t < launches.size(); ++t) {
+        const PersistentLaunch &L = launches[t];
+        const int cnt = (int)L.order.size();
+        const std::string tag = std::to_string(t);
+        void *porder, *pcnt, *pvx = nullptr;
+        if ((st = scratch(ctx, ("pg_order" + tag).c_str(), sizeof(int) * (size_t)cnt, &porder))) return st;
+        if ((st = scratch(ctx, ("pg_counter" + tag).c_str(), sizeof(int), &pcnt))) return st;
+        if (!L.plan.vx_smem && (st = scratch(ctx, ("pg_vx" + tag).c_str(), 8 * (size_t)L.plan.clusters * L.n_max, &pvx)))
+            return st;
+        CK(cudaMemcpyAsync(porder, L.order.data(), sizeof(int) * cnt, cudaMemcpyHostToDevice, ctx->stream));
+        CK(cudaMemsetAsync(pcnt, 0, sizeof(int), ctx->stream));
+        PersistentArgs a{};
+        a.items = (const PersistentItem *)pitems;
+        a.order = (const int *)porder;
+        a.count = cnt;
+        a.n_max = (int)L.n_max;
+        a.restart = m;
+        a.max_iters = max_iters;
+        a.quantum = quantum;
+        a.tol = tol;
+        a.counter = (int *)pcnt;
+        a.vxg = (float2 *)pvx;
+        a.wait_primary = t > 0;
+        args.push_back(a);
+        name += (t ? "+" : "") + std::to_string(L.plan.clusters) + "x" + std::to_string(L.plan.cluster) +
+                (L.plan.vx_smem ? "" : ",vx global");
     }
-    ctx->launches += 1;
+    name += "]";
+    {
+        Phase ph(ctx, name.c_str());
+        for (size_t t = 0; t < launches.size(); ++t)
+            CK(launch_persistent_gmres(args[t], launches[t].plan.cluster, launches[t].plan.clusters,
+                                       launches[t].plan.smem, ctx->stream, t > 0));
+    }
+    ctx->launches += (int)launches.size();
     // the host vectors above are read by the copies: wait for them before they go
     return sync(ctx);
 }
@@ -2602,7 +2683,10 @@ extern "C" nihu_gb_status nihu_gb_server_take(nihu_gb_server *sv, int64_t *id, v
 // the identities and right-hand sides, the persistent GMRES launch over all
 // systems, and the downloads of the solutions, states and error flag.  Each
 // run refills pinned staging buffers and replays the graph: no host work,
-// allocation or synchronisation inside.
+// allocation or synchronisation inside.  The staging buffers hold the
+// instances in the caller's order (one copy each way); the graph permutes
+// them to and from the device's mesh-grouped order, and a caller that writes
+// into them directly (nihu_gb_sweep_plan_host_buffers) saves the host copies.
 
 struct nihu_gb_sweep_plan {
     struct Group {
@@ -2619,6 +2703,7 @@ struct nihu_gb_sweep_plan {
     std::vector<int> mesh_of;
     std::vector<Group> groups;
     std::vector<int> order_of;       // instance f -> position (groups in mesh order)
+    std::vector<int64_t> pos_n;      // position -> elements
     std::vector<int64_t> off, user;  // device (position order) and user (instance order) column offsets
     int family = 0, precision = 0, nk = 0, restart = 0, max_iters = 0;
     double tol = 0.0, kmax = 0.0;
@@ -2627,17 +2712,31 @@ struct nihu_gb_sweep_plan {
     double *d_ks = nullptr;
     float *d_ks32 = nullptr;
     double2 *d_q = nullptr, *d_b = nullptr, *d_x = nullptr;
+    double2 *d_user = nullptr;  // Neumann data in, solutions out, in instance order
+    int64_t *d_src = nullptr, *d_dst = nullptr;  // permute tables: instance order -> device order
+    int *d_len = nullptr;
+    int max_len = 0;
     PersistentState *d_st = nullptr;
     // pinned host staging
     double *h_ks = nullptr;
     float *h_ks32 = nullptr;
     double2 *h_q = nullptr, *h_p = nullptr;
     PersistentState *h_st = nullptr;
+    // processing order of each persistent launch, refreshed per run (larger
+    // n^2 (1 + |k|) first): launch t's items are launch_items[t], its order
+    // h_order[order_off[t] ...] and, uploaded in the graph, d_order[...]
+    std::vector<std::vector<int>> launch_items;
+    std::vector<int> order_off;
+    int *h_order = nullptr, *d_order = nullptr;
     int *h_flag = nullptr;
-    PersistentArgs pargs{};
-    PersistentPlan pplan;
+    std::vector<PersistentArgs> pargs;  // one or two persistent launches (plan_launches)
+    std::vector<PersistentPlan> pplans;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
+    // the side chain of the capture (every group but the largest): its main
+    // and FP64 streams, their fork / join events, and the split / merge events
+    cudaStream_t side = nullptr, side_aux = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr, ev_split = nullptr, ev_merge = nullptr;
 };
 
 namespace {
@@ -2650,8 +2749,12 @@ void plan_free(nihu_gb_sweep_plan *pl)
     cudaStreamSynchronize(ctx->stream);
     if (pl->exec) cudaGraphExecDestroy(pl->exec);
     if (pl->graph) cudaGraphDestroy(pl->graph);
+    for (cudaStream_t t : {pl->side, pl->side_aux})
+        if (t) cudaStreamDestroy(t);
+    for (cudaEvent_t ev : {pl->ev_fork, pl->ev_join, pl->ev_split, pl->ev_merge})
+        if (ev) cudaEventDestroy(ev);
     for (void *p : pl->dbufs) dfree(ctx, p);
-    for (void *h : {(void *)pl->h_ks, (void *)pl->h_ks32, (void *)pl->h_q, (void *)pl->h_p, (void *)pl->h_st,
+    for (void *h : {(void *)pl->h_ks, (void *)pl->h_ks32, (void *)pl->h_q, (void *)pl->h_p, (void *)pl->h_st, (void *)pl->h_order,
                     (void *)pl->h_flag})
         if (h) cudaFreeHost(h);
     delete pl;
@@ -2679,9 +2782,30 @@ nihu_gb_status plan_capture(nihu_gb_sweep_plan *pl)
     if (e == cudaSuccess) {
         chk(cudaMemcpyAsync(pl->d_ks, pl->h_ks, 8 * (size_t)pl->nk, cudaMemcpyHostToDevice, s));
         chk(cudaMemcpyAsync(pl->d_ks32, pl->h_ks32, 4 * (size_t)pl->nk, cudaMemcpyHostToDevice, s));
-        chk(cudaMemcpyAsync(pl->d_q, pl->h_q, 16 * (size_t)pl->total, cudaMemcpyHostToDevice, s));
-        for (auto &g : pl->groups) {
+        chk(cudaMemcpyAsync(pl->d_user, pl->h_q, 16 * (size_t)pl->total, cudaMemcpyHostToDevice, s));
+        chk(launch_permute_segments(pl->d_user, pl->d_q, pl->d_src, pl->d_dst, pl->d_len, pl->nk, pl->max_len, s));
+        // the largest group's assembly on the context's streams; the others on
+        // the side chain beside it, where their small, latency-bound kernels
+        // fill in around the large ones; the chains meet before the solve
+        size_t big = 0;
+        for (size_t gi = 0; gi < pl->groups.size(); ++gi) {
+            const auto &g = pl->groups[gi], &b = pl->groups[big];
+            if ((double)g.n * g.n * g.fs.size() > (double)b.n * b.n * b.fs.size()) big = gi;
+        }
+        chk(cudaEventRecord(pl->ev_split, s));
+        chk(cudaStreamWaitEvent(pl->side, pl->ev_split, 0));
+        const cudaStream_t main_s = ctx->stream, main_aux = ctx->aux_stream;
+        const cudaEvent_t main_fork = ctx->ev_fork, main_join = ctx->ev_join;
+        for (size_t gi = 0; gi < pl->groups.size(); ++gi) {
             if (e != cudaSuccess || st) break;
+            auto &g = pl->groups[gi];
+            // assemble_panel forks and joins on the context's streams: point them at this group's chain
+            const bool on_side = gi != big;
+            ctx->stream = on_side ? pl->side : main_s;
+            ctx->aux_stream = on_side ? pl->side_aux : main_aux;
+            ctx->ev_fork = on_side ? pl->ev_fork : main_fork;
+            ctx->ev_join = on_side ? pl->ev_join : main_join;
+            const cudaStream_t gs = ctx->stream;
             const int cnt = (int)g.fs.size();
             const nihu_gb_mesh *mesh = pl->meshes[g.mesh];
             RegularArgs a;
@@ -2718,13 +2842,23 @@ nihu_gb_status plan_capture(nihu_gb_sweep_plan *pl)
             a.near_slp = g.nslp;
             st = assemble_panel(ctx, a, g.nl);
             if (st) break;
-            chk(launch_add_identity_batched((int)g.n, -0.5, 0.0, NIHU_GB_C64, g.H, g.n, g.n * g.n, cnt, s));
-            chk(launch_rhs_reduce(a, *g.nl, pl->d_b + o, s));
+            chk(launch_add_identity_batched((int)g.n, -0.5, 0.0, NIHU_GB_C64, g.H, g.n, g.n * g.n, cnt, gs));
+            chk(launch_rhs_reduce(a, *g.nl, pl->d_b + o, gs));
         }
+        ctx->stream = main_s;
+        ctx->aux_stream = main_aux;
+        ctx->ev_fork = main_fork;
+        ctx->ev_join = main_join;
+        chk(cudaEventRecord(pl->ev_merge, pl->side));
+        chk(cudaStreamWaitEvent(s, pl->ev_merge, 0));
         chk(cudaMemsetAsync(pl->d_st, 0, sizeof(PersistentState) * (size_t)pl->nk, s));
-        chk(cudaMemsetAsync(pl->pargs.counter, 0, sizeof(int), s));
-        chk(launch_persistent_gmres(pl->pargs, pl->pplan.cluster, pl->pplan.clusters, pl->pplan.smem, s));
-        chk(cudaMemcpyAsync(pl->h_p, pl->d_x, 16 * (size_t)pl->total, cudaMemcpyDeviceToHost, s));
+        for (const PersistentArgs &pa : pl->pargs) chk(cudaMemsetAsync(pa.counter, 0, sizeof(int), s));
+        chk(cudaMemcpyAsync(pl->d_order, pl->h_order, sizeof(int) * (size_t)pl->nk, cudaMemcpyHostToDevice, s));
+        for (size_t t = 0; t < pl->pargs.size(); ++t)
+            chk(launch_persistent_gmres(pl->pargs[t], pl->pplans[t].cluster, pl->pplans[t].clusters, pl->pplans[t].smem,
+                                        s, t > 0));
+        chk(launch_permute_segments(pl->d_x, pl->d_user, pl->d_dst, pl->d_src, pl->d_len, pl->nk, pl->max_len, s));
+        chk(cudaMemcpyAsync(pl->h_p, pl->d_user, 16 * (size_t)pl->total, cudaMemcpyDeviceToHost, s));
         chk(cudaMemcpyAsync(pl->h_st, pl->d_st, sizeof(PersistentState) * (size_t)pl->nk, cudaMemcpyDeviceToHost, s));
         chk(cudaMemcpyAsync(pl->h_flag, ctx->d_flag, sizeof(int), cudaMemcpyDeviceToHost, s));
         chk(cudaMemsetAsync(ctx->d_flag, 0, sizeof(int), s));
@@ -2801,14 +2935,31 @@ extern "C" nihu_gb_status nihu_gb_sweep_plan_create(nihu_gb_ctx *ctx, int n_mesh
     pl->d_ks = (double *)p;
     if ((st = plan_alloc(pl.get(), 4 * (size_t)nk, &p))) return st;
     pl->d_ks32 = (float *)p;
-    double2 *bufs[3];
-    for (int t = 0; t < 3; ++t) {
+    double2 *bufs[4];
+    for (int t = 0; t < 4; ++t) {
         if ((st = plan_alloc(pl.get(), 16 * (size_t)pl->total, &p))) return st;
         bufs[t] = (double2 *)p;
     }
     pl->d_q = bufs[0];
     pl->d_b = bufs[1];
     pl->d_x = bufs[2];
+    pl->d_user = bufs[3];
+    {
+        std::vector<int> len(nk);
+        for (int f = 0; f < nk; ++f) {
+            len[f] = (int)meshes[mesh_of[f]]->n;
+            pl->max_len = std::max(pl->max_len, len[f]);
+        }
+        if ((st = plan_alloc(pl.get(), sizeof(int64_t) * nk, &p))) return st;
+        pl->d_src = (int64_t *)p;
+        if ((st = plan_alloc(pl.get(), sizeof(int64_t) * nk, &p))) return st;
+        pl->d_dst = (int64_t *)p;
+        if ((st = plan_alloc(pl.get(), sizeof(int) * nk, &p))) return st;
+        pl->d_len = (int *)p;
+        CK(cudaMemcpy(pl->d_src, pl->user.data(), sizeof(int64_t) * nk, cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(pl->d_dst, pl->off.data(), sizeof(int64_t) * nk, cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(pl->d_len, len.data(), sizeof(int) * nk, cudaMemcpyHostToDevice));
+    }
     void *dV, *dS, *dst, *ditems, *dorder, *dcnt, *dvx = nullptr;
     if ((st = plan_alloc(pl.get(), 16 * (size_t)pl->total * (m + 1), &dV))) return st;
     if ((st = plan_alloc(pl.get(), 16 * ss * nk, &dS))) return st;
@@ -2834,9 +2985,11 @@ extern "C" nihu_gb_status nihu_gb_sweep_plan_create(nihu_gb_ctx *ctx, int n_mesh
     std::vector<int64_t> ns(nk);
     int l2 = 0;
     cudaDeviceGetAttribute(&l2, cudaDevAttrL2CacheSize, ctx->device);
+    pl->pos_n.assign(nk, 0);
     for (auto &g : pl->groups)
         for (size_t j = 0; j < g.fs.size(); ++j) {
             const int f = g.fs[j], q = pl->order_of[f];
+            pl->pos_n[q] = g.n;
             PersistentItem &it = items[q];
             it.A = (const float2 *)g.H + (size_t)g.n * g.n * j;
             it.lda = g.n;
@@ -2849,32 +3002,45 @@ extern "C" nihu_gb_status nihu_gb_sweep_plan_create(nihu_gb_ctx *ctx, int n_mesh
             it.pad = 0;
             ns[q] = g.n;
         }
-    if ((st = plan_persistent(ctx, ns, m, &pl->pplan))) return st;
-    std::vector<int> order(nk);
-    for (int q = 0; q < nk; ++q) {
-        PersistentItem &it = items[q];
-        it.vec = (it.n % 2 == 0) && (it.lda % 2 == 0) && ((reinterpret_cast<uintptr_t>(it.A) & 15) == 0);
-        it.stream = 8.0 * (double)it.n * (double)it.n * std::min(nk, pl->pplan.clusters) > 0.5 * l2;
-        order[q] = q;
-    }
-    std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return ns[x] > ns[y]; });
+    std::vector<PersistentLaunch> launches;
+    if ((st = plan_launches(ctx, ns, std::vector<double>(ns.begin(), ns.end()), m, &launches))) return st;
+    for (const PersistentLaunch &L : launches)
+        for (int q : L.order) {
+            PersistentItem &it = items[q];
+            it.vec = (it.n % 2 == 0) && (it.lda % 2 == 0) && ((reinterpret_cast<uintptr_t>(it.A) & 15) == 0);
+            it.stream = 8.0 * (double)it.n * (double)it.n * std::min<int>((int)L.order.size(), L.plan.clusters) >
+                        0.5 * l2;
+        }
     if ((st = plan_alloc(pl.get(), sizeof(PersistentItem) * (size_t)nk, &ditems))) return st;
-    if ((st = plan_alloc(pl.get(), sizeof(int) * (size_t)nk, &dorder))) return st;
-    if ((st = plan_alloc(pl.get(), sizeof(int), &dcnt))) return st;
-    if (!pl->pplan.vx_smem && (st = plan_alloc(pl.get(), 8 * (size_t)pl->pplan.clusters * n_max, &dvx))) return st;
     CK(cudaMemcpy(ditems, items.data(), sizeof(PersistentItem) * nk, cudaMemcpyHostToDevice));
-    CK(cudaMemcpy(dorder, order.data(), sizeof(int) * nk, cudaMemcpyHostToDevice));
-    PersistentArgs &a = pl->pargs;
-    a.items = (const PersistentItem *)ditems;
-    a.order = (const int *)dorder;
-    a.count = nk;
-    a.n_max = (int)n_max;
-    a.restart = m;
-    a.max_iters = max_iters;
-    a.quantum = 0;
-    a.tol = tol;
-    a.counter = (int *)dcnt;
-    a.vxg = (float2 *)dvx;
+    if ((st = plan_alloc(pl.get(), sizeof(int) * (size_t)nk, &dorder))) return st;
+    pl->d_order = (int *)dorder;
+    CK(cudaMallocHost((void **)&pl->h_order, sizeof(int) * (size_t)nk));
+    for (size_t t = 0, o = 0; t < launches.size(); ++t) {
+        const PersistentLaunch &L = launches[t];
+        const int cnt = (int)L.order.size();
+        pl->launch_items.push_back(L.order);
+        pl->order_off.push_back((int)o);
+        std::copy(L.order.begin(), L.order.end(), pl->h_order + o);
+        if ((st = plan_alloc(pl.get(), sizeof(int), &dcnt))) return st;
+        dvx = nullptr;
+        if (!L.plan.vx_smem && (st = plan_alloc(pl.get(), 8 * (size_t)L.plan.clusters * L.n_max, &dvx))) return st;
+        PersistentArgs a{};
+        a.items = (const PersistentItem *)ditems;
+        a.order = pl->d_order + o;
+        o += cnt;
+        a.count = cnt;
+        a.n_max = (int)L.n_max;
+        a.restart = m;
+        a.max_iters = max_iters;
+        a.quantum = 0;
+        a.tol = tol;
+        a.counter = (int *)dcnt;
+        a.vxg = (float2 *)dvx;
+        a.wait_primary = t > 0;
+        pl->pargs.push_back(a);
+        pl->pplans.push_back(L.plan);
+    }
     // pinned staging
     CK(cudaMallocHost((void **)&pl->h_ks, 8 * (size_t)nk));
     CK(cudaMallocHost((void **)&pl->h_ks32, 4 * (size_t)nk));
@@ -2882,6 +3048,14 @@ extern "C" nihu_gb_status nihu_gb_sweep_plan_create(nihu_gb_ctx *ctx, int n_mesh
     CK(cudaMallocHost((void **)&pl->h_p, 16 * (size_t)pl->total));
     CK(cudaMallocHost((void **)&pl->h_st, sizeof(PersistentState) * (size_t)nk));
     CK(cudaMallocHost((void **)&pl->h_flag, sizeof(int)));
+    {
+        int prio_lo = 0, prio_hi = 0;
+        CK(cudaDeviceGetStreamPriorityRange(&prio_lo, &prio_hi));
+        CK(cudaStreamCreateWithFlags(&pl->side, cudaStreamNonBlocking));
+        CK(cudaStreamCreateWithPriority(&pl->side_aux, cudaStreamNonBlocking, prio_hi));
+        for (cudaEvent_t *ev : {&pl->ev_fork, &pl->ev_join, &pl->ev_split, &pl->ev_merge})
+            CK(cudaEventCreateWithFlags(ev, cudaEventDisableTiming));
+    }
     CK(prepare_singular_batch(ctx->stream));
     if ((st = sync(ctx))) return st;
     if ((st = plan_capture(pl.get()))) return st;
@@ -2903,8 +3077,16 @@ extern "C" nihu_gb_status nihu_gb_sweep_plan_run(nihu_gb_sweep_plan *pl, const d
         const int q_ = pl->order_of[f];
         pl->h_ks[q_] = ks[f];
         pl->h_ks32[q_] = (float)ks[f];
-        std::memcpy(pl->h_q + pl->off[f], (const double2 *)q + pl->user[f], 16 * (size_t)pl->meshes[pl->mesh_of[f]]->n);
     }
+    // each launch's systems, larger n^2 (1 + |k|) first (iteration counts grow with k)
+    for (size_t t = 0; t < pl->launch_items.size(); ++t) {
+        std::vector<int> ord = pl->launch_items[t];
+        std::vector<double> key(pl->nk, 0.0);
+        for (int q_ : ord) key[q_] = (double)pl->pos_n[q_] * pl->pos_n[q_] * (1.0 + std::fabs(pl->h_ks[q_]));
+        std::stable_sort(ord.begin(), ord.end(), [&](int x, int y) { return key[x] > key[y]; });
+        std::copy(ord.begin(), ord.end(), pl->h_order + pl->order_off[t]);
+    }
+    if (q != pl->h_q) std::memcpy(pl->h_q, q, 16 * (size_t)pl->total);
     {
         Phase ph(ctx, "sweep_graph");
         CK(cudaGraphLaunch(pl->exec, ctx->stream));
@@ -2915,9 +3097,9 @@ extern "C" nihu_gb_status nihu_gb_sweep_plan_run(nihu_gb_sweep_plan *pl, const d
     if (*pl->h_flag)
         return fail(ctx, NIHU_GB_ERR_RUNTIME, "Could not perform inverse mapping (nearly singular pair " +
                                                   std::to_string(*pl->h_flag - 1) + ")");
+    if (p != pl->h_p) std::memcpy(p, pl->h_p, 16 * (size_t)pl->total);
     bool all = true;
     for (int f = 0; f < pl->nk; ++f) {
-        std::memcpy((double2 *)p + pl->user[f], pl->h_p + pl->off[f], 16 * (size_t)pl->meshes[pl->mesh_of[f]]->n);
         const PersistentState &s = pl->h_st[pl->order_of[f]];
         if (iters) iters[f] = s.iters;
         if (rel_residuals) rel_residuals[f] = s.rel;
@@ -2925,6 +3107,14 @@ extern "C" nihu_gb_status nihu_gb_sweep_plan_run(nihu_gb_sweep_plan *pl, const d
         all = all && s.converged;
     }
     if (!all) return fail(ctx, NIHU_GB_ERR_NOT_CONVERGED, "sweep plan: some systems did not reach the tolerance");
+    return NIHU_GB_OK;
+}
+
+extern "C" nihu_gb_status nihu_gb_sweep_plan_host_buffers(nihu_gb_sweep_plan *pl, void **q, void **p)
+{
+    if (!pl || !q || !p) return NIHU_GB_ERR_INVALID_ARGUMENT;
+    *q = pl->h_q;
+    *p = pl->h_p;
     return NIHU_GB_OK;
 }
 

@@ -71,13 +71,14 @@ __host__ __device__ inline int level_npts(int trial_nc, int test_c, int level)
     return level == 0 ? 1 : (level == 1 ? 4 : 7);
 }
 
-// sin and cos of 2 pi t for any t: the period count is removed exactly
-// (t - rint(t) is exact in binary floating point), leaving |2 pi f| <= pi for
-// the hardware approximation (absolute error about 4e-7 there)
-__device__ __forceinline__ void sincos_2pi(float t, float &s, float &c)
+// sin and cos of x (radians) in FP32: x less the nearest multiple n of 2 pi,
+// formed with one fused multiply-add (Cody-Waite reduction with a one-term
+// constant: the FP32 rounding of 2 pi adds |n| x 1.75e-7 rad), leaves about
+// [-pi, pi] for the hardware approximation (absolute error about 4e-7 there)
+__device__ __forceinline__ void sincos_reduced(float x, float &s, float &c)
 {
-    float f = t - rintf(t);
-    __sincosf(6.28318530717958647692f * f, &s, &c);
+    const float n = rintf(x * 0.159154943091895335769f);
+    __sincosf(fmaf(-6.28318530717958647692f, n, x), &s, &c);
 }
 
 // one quadrature point of the SLP (weight ws) and DLP (weight wd) kernels at
@@ -97,7 +98,7 @@ __device__ __forceinline__ void eval_point(R rx, R ry, R rz, R wj, R nx, R ny, R
     if constexpr (FAM == FAM_HELMHOLTZ) {
         R kr = k * (r2 * rinv);
         R s, c;
-        if constexpr (sizeof(R) == 4) sincos_2pi(kr * 0.159154943091895335769f, s, c);
+        if constexpr (sizeof(R) == 4) sincos_reduced(kr, s, c);
         else sincos(kr, &s, &c);
         // SLP: G = e^{-ikr}/(4 pi r) = (c - i s)/(4 pi r)
         R gs = g * ws;

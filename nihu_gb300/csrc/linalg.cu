@@ -1,5 +1,7 @@
 // Dense linear algebra of the solve: identity shift, streamed complex matvec,
 // GMRES building blocks (FP64 Gram-Schmidt) and an FP64 LU factorisation.
+#include <algorithm>
+
 #include "kernels.h"
 #include "linalg.h"
 
@@ -235,6 +237,26 @@ cudaError_t launch_add_identity_batched(int n, double are, double aim, int dtype
     dim3 g((n + 255) / 256, batch);
     if (dtype == 0) k_add_identity_batched<float2><<<g, 256, 0, s>>>(n, are, aim, (float2 *)out, ld, stride);
     else k_add_identity_batched<double2><<<g, 256, 0, s>>>(n, are, aim, (double2 *)out, ld, stride);
+    return cudaGetLastError();
+}
+
+__global__ void k_permute_segments(const double2 *__restrict__ src, double2 *__restrict__ dst,
+                                   const int64_t *__restrict__ src_off, const int64_t *__restrict__ dst_off,
+                                   const int *__restrict__ len)
+{
+    const int t = blockIdx.y;
+    const int n = len[t];
+    const double2 *a = src + src_off[t];
+    double2 *b = dst + dst_off[t];
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) b[i] = a[i];
+}
+
+cudaError_t launch_permute_segments(const double2 *src, double2 *dst, const int64_t *src_off, const int64_t *dst_off,
+                                    const int *len, int count, int max_len, cudaStream_t s)
+{
+    if (count == 0 || max_len == 0) return cudaSuccess;
+    dim3 g((unsigned)std::min(64, (max_len + 255) / 256), count);
+    k_permute_segments<<<g, 256, 0, s>>>(src, dst, src_off, dst_off, len);
     return cudaGetLastError();
 }
 

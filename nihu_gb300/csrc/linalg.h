@@ -20,6 +20,10 @@ cudaError_t launch_gemv_batched(int dtype, const void *A, int64_t m, int64_t n, 
                                 double bim, double2 *partial, int splits, cudaStream_t s, const int *active);
 cudaError_t launch_add_identity_batched(int n, double are, double aim, int dtype, void *out, int64_t ld, int64_t stride,
                                         int batch, cudaStream_t s);
+// segment t: dst[dst_off[t] + i] = src[src_off[t] + i] for i < len[t]
+// (device tables of count entries; max_len bounds every len[t])
+cudaError_t launch_permute_segments(const double2 *src, double2 *dst, const int64_t *src_off, const int64_t *dst_off,
+                                    const int *len, int count, int max_len, cudaStream_t s);
 
 int dot_blocks(int64_t n);
 cudaError_t launch_multidot(const double2 *V, int64_t n, int nv, const double2 *w, double2 *partial, int blocks,

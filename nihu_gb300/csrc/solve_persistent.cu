@@ -206,6 +206,10 @@ __global__ void __launch_bounds__(PT, 1) k_persistent_gmres(PersistentArgs a)
         return d;
     };
 
+    // a programmatic dependent launch of this stream may start now, on the
+    // SMs this grid leaves free (no effect on a plain launch)
+    asm volatile("griddepcontrol.launch_dependents;");
+
     for (;;) {
         if (rank == 0 && tid == 0) ctl[0] = atomicAdd(a.counter, 1);
         cl.sync();
@@ -463,6 +467,9 @@ __global__ void __launch_bounds__(PT, 1) k_persistent_gmres(PersistentArgs a)
             *it.st = o;
         }
     }
+    // dependent launch: the primary launch runs to completion by itself (it
+    // never waits on this grid), so this wait ends when it does
+    if (a.wait_primary) asm volatile("griddepcontrol.wait;" ::: "memory");
 }
 
 }  // namespace
@@ -497,21 +504,29 @@ cudaError_t persistent_gmres_plan(int n_max, int restart, int cluster, int vx_sm
     return cudaSuccess;
 }
 
-cudaError_t launch_persistent_gmres(const PersistentArgs &a, int cluster, int clusters, size_t smem, cudaStream_t s)
+cudaError_t launch_persistent_gmres(const PersistentArgs &a, int cluster, int clusters, size_t smem, cudaStream_t s,
+                                    bool dependent)
 {
     cudaLaunchConfig_t cfg = {};
-    cudaLaunchAttribute attr[1];
+    cudaLaunchAttribute attr[2];
     attr[0].id = cudaLaunchAttributeClusterDimension;
     attr[0].val.clusterDim.x = cluster;
     attr[0].val.clusterDim.y = 1;
     attr[0].val.clusterDim.z = 1;
+    attr[1].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[1].val.programmaticStreamSerializationAllowed = 1;
     cfg.gridDim = dim3(clusters * cluster);
     cfg.blockDim = dim3(PT);
     cfg.dynamicSmemBytes = smem;
     cfg.stream = s;
     cfg.attrs = attr;
-    cfg.numAttrs = 1;
+    cfg.numAttrs = dependent ? 2 : 1;
     return cudaLaunchKernelEx(&cfg, k_persistent_gmres, a);
+}
+
+cudaError_t persistent_gmres_smem_limit(size_t smem)
+{
+    return cudaFuncSetAttribute(k_persistent_gmres, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
 }
 
 }  // namespace nihu

@@ -53,6 +53,11 @@ struct PersistentArgs {
     double tol;
     int *counter;  // zero before the launch
     float2 *vxg;   // NULL: matvec input in shared memory; else clusters * n_max complex64
+    // 1: launched as the programmatic dependent of the previous persistent
+    // launch of its stream (launch_persistent_gmres, dependent = true); the
+    // grid's CTAs end by waiting for that launch to complete, so that work
+    // ordered after this launch also follows the other
+    int wait_primary = 0;
 };
 
 // dynamic shared memory of one CTA, byte offsets
@@ -101,6 +106,13 @@ __host__ __device__ inline PersistentSmem persistent_smem_layout(int n_max, int 
 // clusters that can run at once (at most count) and the dynamic shared memory per CTA
 cudaError_t persistent_gmres_plan(int n_max, int restart, int cluster, int vx_smem, int count, int *clusters,
                                   size_t *smem);
-cudaError_t launch_persistent_gmres(const PersistentArgs &a, int cluster, int clusters, size_t smem, cudaStream_t s);
+// dependent: programmatic dependent launch, started as soon as every CTA of
+// the previous persistent launch of the stream is running (on the SMs that
+// one leaves free); a.wait_primary must then be 1
+cudaError_t launch_persistent_gmres(const PersistentArgs &a, int cluster, int clusters, size_t smem, cudaStream_t s,
+                                    bool dependent = false);
+// raise the kernel's dynamic shared memory limit to smem bytes (several
+// launch shapes in one stream: the largest of them)
+cudaError_t persistent_gmres_smem_limit(size_t smem);
 
 }  // namespace nihu
