@@ -427,6 +427,15 @@ cudaError_t prepare_singular_batch(cudaStream_t s)
         e = cudaFuncSetAttribute(k_singular_batch<float2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)MOM_SMEM);
     if (e == cudaSuccess)
         e = cudaFuncSetAttribute(k_singular_batch<double2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)MOM_SMEM);
+    // the whole carveout as shared memory on the SMs this kernel starts on, so
+    // that the concurrent regular kernel's blocks (with their shared row sums
+    // in right-hand-side mode) still fit beside its block
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_singular_batch<float2>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                 (int)cudaSharedmemCarveoutMaxShared);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_singular_batch<double2>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                 (int)cudaSharedmemCarveoutMaxShared);
     return e;
 }
 
