@@ -2048,8 +2048,9 @@ struct PersistentLaunch {
 // decreasing key: one over all; or, when the shape chosen for the larger
 // systems (n >= n_max / 2) leaves SMs idle -- clusters of 8 CTAs fit whole
 // GPCs, not every SM -- and smaller systems exist, a second launch of the
-// smaller systems, one CTA per system, sized to the idle SMs and started
-// beside the first as its programmatic dependent (launch_persistent_gmres).
+// smaller systems in the smallest clusters that hold them, sized to the idle
+// SMs and started beside the first as its programmatic dependent
+// (launch_persistent_gmres).
 nihu_gb_status plan_launches(nihu_gb_ctx *ctx, const std::vector<int64_t> &ns, const std::vector<double> &key, int m,
                              std::vector<PersistentLaunch> *out)
 {
@@ -2074,24 +2075,28 @@ nihu_gb_status plan_launches(nihu_gb_ctx *ctx, const std::vector<int64_t> &ns, c
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device);
         cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, ctx->device);
         const int spare = sms - A.plan.cluster * A.plan.clusters;
-        const int vs = persistent_smem_layout((int)B.n_max, 1, m, 1).total <= (size_t)smem_optin ? 1 : 0;
-        int act = 0;
-        size_t smem = 0;
-        if (A.plan.cluster >= 4 && spare >= 1 && persistent_smem_layout((int)B.n_max, 1, m, vs).total <= (size_t)smem_optin) {
-            if (persistent_gmres_plan((int)B.n_max, m, 1, vs, (int)small.size(), &act, &smem) == cudaSuccess) {
-                B.plan.cluster = 1;
-                B.plan.clusters = std::min(act, spare);
-                B.plan.vx_smem = vs;
-                B.plan.smem = smem;
-                A.order = sorted(big);
-                A.n_max = n_max;
-                B.order = sorted(small);
-                CK(persistent_gmres_smem_limit(std::max(A.plan.smem, B.plan.smem)));
-                out->push_back(A);
-                out->push_back(B);
-                return NIHU_GB_OK;
+        // the smallest cluster whose shared memory holds the smaller systems
+        for (int c : {1, 2, 4}) {
+            if (A.plan.cluster < 4 || spare < c) break;
+            const int vs = persistent_smem_layout((int)B.n_max, c, m, 1).total <= (size_t)smem_optin ? 1 : 0;
+            if (persistent_smem_layout((int)B.n_max, c, m, vs).total > (size_t)smem_optin) continue;
+            int act = 0;
+            size_t smem = 0;
+            if (persistent_gmres_plan((int)B.n_max, m, c, vs, (int)small.size(), &act, &smem) != cudaSuccess) {
+                cudaGetLastError();
+                continue;
             }
-            cudaGetLastError();
+            B.plan.cluster = c;
+            B.plan.clusters = std::min(act, spare / c);
+            B.plan.vx_smem = vs;
+            B.plan.smem = smem;
+            A.order = sorted(big);
+            A.n_max = n_max;
+            B.order = sorted(small);
+            CK(persistent_gmres_smem_limit(std::max(A.plan.smem, B.plan.smem)));
+            out->push_back(A);
+            out->push_back(B);
+            return NIHU_GB_OK;
         }
     }
     PersistentLaunch one;
