@@ -364,7 +364,13 @@ __device__ __forceinline__ void singular_pairs(const RegularArgs &a, const NearL
                     self_quad(e, fam, kf, x0, do_s, do_d, acc);
                 }
             } else if (e.nc == 3) {
-                near_plane(e, fam, kf, x0, do_s, do_d, acc, a.trial.dyn42 + 42 * (int64_t)j, short_f);
+                if (a.precision == 0 && fam == FAM_HELMHOLTZ) {
+                    // FP32 regular quadrature: the dynamic part in FP32 as well
+                    near_dynamic_f32(e, kf, x0, do_s, do_d, acc);
+                    near_static(e, x0, do_s, do_d, acc);
+                } else {
+                    near_plane(e, fam, kf, x0, do_s, do_d, acc, a.trial.dyn42 + 42 * (int64_t)j, short_f);
+                }
             } else {
                 const bool telles = fam == FAM_HELMHOLTZ && do_d;
                 const bool polar_d = fam == FAM_LAPLACE && do_d;

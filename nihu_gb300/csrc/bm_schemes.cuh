@@ -258,18 +258,6 @@ __device__ inline void near_dynamic4(const Elem64 &e, double k, const double x0[
     }
 }
 
-// The 42-point degree-14 Dunavant rule in FP32, (xi, eta, w) per point
-struct Tri14 {
-    float p[42][3];
-    constexpr Tri14() : p()
-    {
-        constexpr double d[NIHU_TRI_DATA_LEN] = NIHU_TRI_DATA;
-        constexpr int off[15] = NIHU_TRI_OFFSETS;
-        for (int q = 0; q < 42; ++q)
-            for (int c = 0; c < 3; ++c) p[q][c] = (float)d[3 * (off[14] + q) + c];
-    }
-};
-__device__ constexpr Tri14 TRI14{};
 
 // The same dynamic parts in FP32 (regular quadrature in FP32): K_k - K_0 is
 // smooth and, for a nearly singular pair, of relative size (kr)^2 against the

@@ -212,4 +212,17 @@ __device__ __forceinline__ void store64(Out *p, double re, double im, double are
     *p = o;
 }
 
+// The 42-point degree-14 Dunavant rule in FP32, (xi, eta, w) per point
+struct Tri14 {
+    float p[42][3];
+    constexpr Tri14() : p()
+    {
+        constexpr double d[NIHU_TRI_DATA_LEN] = NIHU_TRI_DATA;
+        constexpr int off[15] = NIHU_TRI_OFFSETS;
+        for (int q = 0; q < 42; ++q)
+            for (int c = 0; c < 3; ++c) p[q][c] = (float)d[3 * (off[14] + q) + c];
+    }
+};
+__device__ constexpr Tri14 TRI14{};
+
 }  // namespace nihu

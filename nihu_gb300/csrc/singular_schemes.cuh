@@ -149,6 +149,58 @@ __device__ inline void near_dynamic(const Elem64 &e, double k, const double x0[3
     }
 }
 
+// The same dynamic part in FP32 (triangles, regular quadrature in FP32):
+// K_k - K_0 is smooth and, for a nearly singular pair, of relative size
+// (kr)^2 against the FP64 static part, so FP32 point sums keep the entry
+// within a few 1e-7 of the FP64 value while taking the narrow FP64 pipe out
+// of 42 points per pair.  The points are formed in FP32 relative to x0 from
+// the corners (the corner offsets in FP64), and cos(kr) - 1 as
+// -2 sin^2(kr/2), without cancellation.
+__device__ inline void near_dynamic_f32(const Elem64 &e, double k, const double x0[3], bool do_s, bool do_d, Acc &a)
+{
+    double e1[3], e2[3], nt[3];
+    for (int d = 0; d < 3; ++d) { e1[d] = e.c[1][d] - e.c[0][d]; e2[d] = e.c[2][d] - e.c[0][d]; }
+    cross3(e1, e2, nt);
+    const double J = norm3(nt);
+    float b[3], f1[3], f2[3], en[3];
+    for (int d = 0; d < 3; ++d) {
+        b[d] = (float)(e.c[0][d] - x0[d]);
+        f1[d] = (float)e1[d];
+        f2[d] = (float)e2[d];
+        en[d] = (float)(nt[d] / J);
+    }
+    const float kf = (float)k;
+    const float wj = (float)(J * INV_FOUR_PI);
+    float sr = 0, si = 0, dr = 0, di = 0;
+    for (int p = 0; p < 42; ++p) {
+        const float xi = TRI14.p[p][0], eta = TRI14.p[p][1], w = TRI14.p[p][2];
+        const float rv0 = b[0] + xi * f1[0] + eta * f2[0];
+        const float rv1 = b[1] + xi * f1[1] + eta * f2[1];
+        const float rv2 = b[2] + xi * f1[2] + eta * f2[2];
+        const float r2 = rv0 * rv0 + rv1 * rv1 + rv2 * rv2;
+        const float rinv = rsqrtf(r2);
+        const float kr = kf * (r2 * rinv);
+        float sn, cs;
+        sincosf(kr, &sn, &cs);
+        const float hs = sinf(0.5f * kr);
+        const float cm1 = -2.0f * hs * hs;
+        const float t = w * wj * rinv;
+        if (do_s) {
+            sr += t * cm1;
+            si -= t * sn;
+        }
+        if (do_d) {
+            const float u = t * rinv * ((rv0 * en[0] + rv1 * en[1] + rv2 * en[2]) * rinv);
+            dr -= u * (cm1 + kr * sn);
+            di -= u * (kr * cs - sn);
+        }
+    }
+    a.sr += sr;
+    a.si += si;
+    a.dr += dr;
+    a.di += di;
+}
+
 // full planar constant-element nearly singular integral
 __device__ inline void near_plane(const Elem64 &e, int fam, double k, const double x0[3], bool do_s, bool do_d, Acc &a,
                            const Pt4 *__restrict__ pts42 = nullptr, bool short_series = false)
