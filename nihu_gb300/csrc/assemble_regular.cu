@@ -151,7 +151,9 @@ constexpr float Q_FAR = 249.64f * (1.0f + 1e-4f);
 // BATCH: frequency batch (a.nk > 1), a separate instantiation so that the
 // single wave number kernel carries none of its code
 // RHS: right-hand-side mode (BATCH only; the SLP entries go into the row sums)
-template <typename R, typename Out, int FAM, int OPS, bool BATCH, bool RHS = false>
+// PLAIN: unit scale and no accumulation (single wave number, FP32), so the
+// stores carry no run-time checks
+template <typename R, typename Out, int FAM, int OPS, bool BATCH, bool RHS = false, bool PLAIN = false>
 __global__ void __launch_bounds__(REG_THREADS) k_regular(RegularArgs a)
 {
     using R2 = Cplx<R>;
@@ -232,8 +234,17 @@ __global__ void __launch_bounds__(REG_THREADS) k_regular(RegularArgs a)
     }
     Out *out_s = reinterpret_cast<Out *>(a.out_s);
     Out *out_d = reinterpret_cast<Out *>(a.out_d);
+    // single wave number: this thread's entries of the current column, one
+    // column (ld entries) further per step
+    const int64_t ldo = a.ld;
+    Out *ps = DO_S && !BATCH ? out_s + (int64_t)(jb - a.j0) * ldo + i : nullptr;
+    Out *pd = DO_D && !BATCH ? out_d + (int64_t)(jb - a.j0) * ldo + i : nullptr;
+    auto put = [&](Out *p, R re, R im) {
+        if constexpr (PLAIN) store_plain(p, re, im);
+        else store_entry(p, re, im, are, aim, unit_alpha, accumulate);
+    };
 
-    for (int c = 0; c < ncols; ++c) {
+    for (int c = 0; c < ncols; ++c, ps += DO_S && !BATCH ? ldo : 0, pd += DO_D && !BATCH ? ldo : 0) {
         const int j = jb + c;
         if constexpr (sizeof(R) == 4) {
             // far-field fast path, taken when every lane of the warp is a far
@@ -243,8 +254,8 @@ __global__ void __launch_bounds__(REG_THREADS) k_regular(RegularArgs a)
             const float q = (fx * fx + fy * fy + fz * fz) * h.w;
             if (__all_sync(0xffffffffu, q > Q_FAR)) {
                 const float4 p = s_p0[c];
-                const int64_t off = (int64_t)(j - a.j0) * a.ld + i;
                 if constexpr (BATCH) {
+                    const int64_t off = (int64_t)(j - a.j0) * a.ld + i;
                     const PointGeom<float> gm = point_geom<float>(fx, fy, fz, p.x, p.y, p.z, p.w, R(DO_S), R(DO_D));
                     BatchCursor<Out> cs(a, false, f_lo, off), cd(a, true, f_lo, off);
                     R2 *acc = s_acc + threadIdx.x;
@@ -270,8 +281,8 @@ __global__ void __launch_bounds__(REG_THREADS) k_regular(RegularArgs a)
                     R sr = 0, si = 0, dr = 0, di = 0;
                     eval_point<FAM, float>(fx, fy, fz, p.x, p.y, p.z, p.w, k, R(DO_S), R(DO_D), sr, si, dr, di);
                     if (row_ok) {
-                        if (DO_S) store_entry(out_s + off, sr, si, are, aim, unit_alpha, accumulate);
-                        if (DO_D) store_entry(out_d + off, dr, di, are, aim, unit_alpha, accumulate);
+                        if (DO_S) put(ps, sr, si);
+                        if (DO_D) put(pd, dr, di);
                     }
                 }
                 continue;
@@ -363,9 +374,8 @@ __global__ void __launch_bounds__(REG_THREADS) k_regular(RegularArgs a)
                                             si, dr, di);
                 }
             }
-            const int64_t off = (int64_t)(j - a.j0) * a.ld + i;
-            if (DO_S) store_entry(out_s + off, sr, si, are, aim, unit_alpha, accumulate);
-            if (DO_D) store_entry(out_d + off, dr, di, are, aim, unit_alpha, accumulate);
+            if (DO_S) put(ps, sr, si);
+            if (DO_D) put(pd, dr, di);
         }
     }
     if constexpr (RHS) {
@@ -430,6 +440,14 @@ static void launch_ops(const RegularArgs &a, dim3 grid, cudaStream_t s)
         if (a.rhs_part) {
             const size_t smem = sizeof(Cplx<R>) * rhs_f_max<R>() * (REG_COLS + REG_THREADS);
             k_regular<R, Out, FAM, OP_SLP | OP_DLP, true, true><<<grid, REG_THREADS, smem, s>>>(a);
+            return;
+        }
+    }
+    if constexpr (!BATCH && sizeof(R) == 4) {
+        if (a.unit_alpha && !a.accumulate) {
+            if (a.ops == OP_SLP) k_regular<R, Out, FAM, OP_SLP, false, false, true><<<grid, REG_THREADS, 0, s>>>(a);
+            else if (a.ops == OP_DLP) k_regular<R, Out, FAM, OP_DLP, false, false, true><<<grid, REG_THREADS, 0, s>>>(a);
+            else k_regular<R, Out, FAM, OP_SLP | OP_DLP, false, false, true><<<grid, REG_THREADS, 0, s>>>(a);
             return;
         }
     }

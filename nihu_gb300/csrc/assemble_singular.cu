@@ -396,8 +396,11 @@ __device__ __forceinline__ void singular_pairs(const RegularArgs &a, const NearL
     }
 }
 
+// held to 128 registers so that three blocks of the concurrent regular kernel
+// keep every SM beside this kernel's one (it would take 164 by itself, with
+// the FP32 dynamic part beside the FP64 schemes, which left room for two)
 template <typename Out>
-__global__ void __launch_bounds__(SING_THREADS) k_singular(RegularArgs a, NearList near, int *err)
+__global__ void __launch_bounds__(SING_THREADS, 4) k_singular(RegularArgs a, NearList near, int *err)
 {
     singular_pairs<Out, false>(a, near, err);
 }
