@@ -565,7 +565,11 @@ def run_multirhs(args):
     prof_asm = ctx.profile()
     ctx.profile_reset()
     ctx.check(L.nihu_gb_add_identity(ctx.handle, dm.handle, -0.5, 0.0, C.C64, pd, n, C.DEVICE))
+    # warm-up of every GEMM mode (the library's first call of a mode loads its kernels)
+    for mode in (C.GEMM_FP32, C.GEMM_TF32, C.GEMM_BF16X9):
+        ctx.check(L.nihu_gb_gemm(ctx.handle, mode, ps, n, n, n, pq, n, nrhs, px, n, 1.0, 0.0, 0.0, 0.0, C.DEVICE))
     torch.cuda.synchronize()
+    ctx.profile_reset()
     t0 = time.perf_counter()
     ctx.check(L.nihu_gb_gemm(ctx.handle, C.GEMM_FP32, ps, n, n, n, pq, n, nrhs, pb, n, 1.0, 0.0, 0.0, 0.0, C.DEVICE))
     torch.cuda.synchronize()
@@ -582,6 +586,8 @@ def run_multirhs(args):
                           "complex_tflops": 8.0 * n * n * nrhs / (ms_ / 1e3) / 1e12}
     oi, ii = ctypes.c_int(0), ctypes.c_int(0)
     res = np.zeros(nrhs)
+    torch.cuda.synchronize()
+    ctx.profile_reset()  # the solve's phases alone
     t0 = time.perf_counter()
     st = L.nihu_gb_solve_multi(ctx.handle, pd, n, n, pb, px, nrhs, C.GEMM_TF32, C.GEMM_FP32, 30, 20, 1e-6, 1e-3,
                                ctypes.byref(oi), ctypes.byref(ii), res.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),

@@ -376,9 +376,12 @@ nihu_gb_status nihu_gb_gmres(nihu_gb_ctx *ctx, int dtype_a, const void *A, int64
                              const void *b, void *x, int restart, int max_iters, double tol,
                              int *iters, double *rel_residual, int where);
 
-/* Solve A x = b by LU factorisation with partial pivoting in FP64 (complex128
- * A, n x n, lda).  A is overwritten by its factors when where = DEVICE; a host
- * A is copied to the device and left unchanged. */
+/* Solve A x = b by LU factorisation with partial pivoting (complex128 A,
+ * n x n, lda): the FP32 factors of A, refined in FP64 (x += (LU)^{-1}
+ * (b - A x) with the FP64 residual) until the correction is at FP64
+ * rounding; an FP64 factorisation when the order is beyond the FP32 kernels
+ * or the refinement stops converging (then a device A is overwritten by its
+ * factors).  A host A is copied to the device and left unchanged. */
 nihu_gb_status nihu_gb_lu_solve(nihu_gb_ctx *ctx, void *A, int64_t n, int64_t lda, const void *b, void *x,
                                 int where);
 

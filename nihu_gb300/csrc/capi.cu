@@ -49,6 +49,12 @@ struct nihu_gb_ctx {
     std::vector<std::pair<std::string, std::pair<cudaEvent_t, cudaEvent_t>>> pending;
     std::vector<cudaEvent_t> event_pool;
     cublasHandle_t cublas = nullptr;  // created on first multi-RHS product
+    // the FP32 LU factorisation of the last order, captured as a CUDA graph
+    // (one kernel pair per panel): valid for these buffers
+    cudaGraphExec_t lu_exec = nullptr;
+    int lu_n = 0;
+    int64_t lu_launches = 0;
+    void *lu_F = nullptr, *lu_piv = nullptr;
 };
 
 struct nihu_gb_mesh {
@@ -467,6 +473,7 @@ void nihu_gb_ctx_destroy(nihu_gb_ctx *ctx)
     dfree(ctx, ctx->d_flag);
     if (ctx->h_small) cudaFreeHost(ctx->h_small);
     if (ctx->cublas) cublasDestroy(ctx->cublas);
+    if (ctx->lu_exec) cudaGraphExecDestroy(ctx->lu_exec);
     collect_phases(ctx);
     for (cudaEvent_t e : ctx->event_pool) cudaEventDestroy(e);
     if (ctx->aux_stream) cudaStreamSynchronize(ctx->aux_stream);
@@ -1384,6 +1391,96 @@ nihu_gb_status nihu_gb_gmres(nihu_gb_ctx *ctx, int dtype_a, const void *A, int64
 
 // ------------------------------------------------------------------ LU
 
+}  // extern "C"
+
+namespace {
+
+// A x = b (complex128, device) with the FP32 LU factors of A refined in FP64:
+// x_0 = 0, then d = (LU)^{-1} r, x += d, r = b - A x (FP64 matvec) until the
+// correction is within 64 FP64 roundings of x (|d| <= 64 eps |x|, the
+// accuracy of an FP64 factorisation).  *refined = false (and nothing solved)
+// when the order is beyond the FP32 kernels' shared memory or the
+// corrections stop shrinking (cond(A) near 1 / eps32): the caller then
+// factorises in FP64.  A is left unchanged.
+nihu_gb_status lu_solve_mixed(nihu_gb_ctx *ctx, const double2 *A, int64_t n, int64_t lda, const double2 *b, double2 *x,
+                              bool *refined)
+{
+    *refined = false;
+    int smem_optin = 0;
+    cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, ctx->device);
+    if (!lu32_fits((int)n, (size_t)smem_optin)) return NIHU_GB_OK;
+    nihu_gb_status st;
+    void *pf, *ppiv, *pd, *pr, *psums, *ppart;
+    const int splits = gemv_splits(n, n, NIHU_GB_C128);
+    if ((st = scratch(ctx, "lu32_F", 8 * (size_t)n * n, &pf))) return st;
+    if ((st = scratch(ctx, "lu_piv", sizeof(int) * n, &ppiv))) return st;
+    if ((st = scratch(ctx, "lu32_d", 16 * (size_t)n, &pd))) return st;
+    if ((st = scratch(ctx, "lu32_r", 16 * (size_t)n, &pr))) return st;
+    if ((st = scratch(ctx, "lu32_sums", 2 * sizeof(double), &psums))) return st;
+    if ((st = scratch(ctx, "lu32_part", 16 * (size_t)splits * n, &ppart))) return st;
+    double2 *d = (double2 *)pd, *r = (double2 *)pr;
+    size_t panel_smem = 0;
+    CK(lu32_prepare((int)n, (size_t)smem_optin, &panel_smem));
+    if (!(ctx->lu_exec && ctx->lu_n == n && ctx->lu_F == pf && ctx->lu_piv == ppiv)) {
+        // record the panel sequence once per order and buffers
+        if (ctx->lu_exec) cudaGraphExecDestroy(ctx->lu_exec);
+        ctx->lu_exec = nullptr;
+        cudaGraph_t graph = nullptr;
+        int64_t counted = 0;
+        CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+        cudaError_t e = launch_lu32_factor((float2 *)pf, (int)n, (int *)ppiv, ctx->d_flag + 1, panel_smem, &counted,
+                                           ctx->stream);
+        cudaError_t e2 = cudaStreamEndCapture(ctx->stream, &graph);
+        if (e == cudaSuccess) e = e2;
+        if (e == cudaSuccess) e = cudaGraphInstantiate(&ctx->lu_exec, graph, 0);
+        if (graph) cudaGraphDestroy(graph);
+        if (e != cudaSuccess) {
+            ctx->lu_exec = nullptr;
+            return cuda_fail(ctx, e, "LU graph capture");
+        }
+        ctx->lu_n = (int)n;
+        ctx->lu_F = pf;
+        ctx->lu_piv = ppiv;
+        ctx->lu_launches = counted;
+    }
+    CK(cudaMemsetAsync(ctx->d_flag + 1, 0, sizeof(int), ctx->stream));
+    {
+        Phase ph(ctx, "lu_factor");
+        CK(launch_to_c64(A, lda, (int)n, (float2 *)pf, ctx->stream));
+        CK(cudaGraphLaunch(ctx->lu_exec, ctx->stream));
+        ctx->launches += 1 + ctx->lu_launches;
+    }
+    int info = 0;
+    CK(cudaMemcpyAsync(&info, ctx->d_flag + 1, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    if ((st = sync(ctx))) return st;
+    if (info) return fail(ctx, NIHU_GB_ERR_RUNTIME, "LU: exactly singular matrix (zero pivot in column " + std::to_string(info - 1) + ")");
+    Phase ph(ctx, "lu_solve");
+    CK(cudaMemsetAsync(x, 0, 16 * (size_t)n, ctx->stream));
+    CK(cudaMemcpyAsync(r, b, 16 * (size_t)n, cudaMemcpyDeviceToDevice, ctx->stream));
+    double sums[2] = {0.0, 0.0}, prev = 0.0;
+    const double eps = 2.220446049250313e-16;
+    for (int it = 0; it < 12; ++it) {
+        CK(launch_lu32_solve((const float2 *)pf, (int)n, (const int *)ppiv, r, d, ctx->stream));
+        CK(launch_lu32_update_x(x, d, (int)n, (double *)psums, ctx->stream));
+        CK(cudaMemcpyAsync(r, b, 16 * (size_t)n, cudaMemcpyDeviceToDevice, ctx->stream));
+        CK(launch_gemv(NIHU_GB_C128, A, n, n, lda, x, r, -1.0, 0.0, 1.0, 0.0, (double2 *)ppart, splits, ctx->stream));
+        CK(cudaMemcpyAsync(sums, psums, sizeof(sums), cudaMemcpyDeviceToHost, ctx->stream));
+        ctx->launches += 4;
+        if ((st = sync(ctx))) return st;
+        if (!(sums[1] > 0.0) || sums[0] <= 4096.0 * eps * eps * sums[1]) {
+            *refined = true;
+            return NIHU_GB_OK;
+        }
+        if (it > 0 && !(sums[0] < 0.25 * prev)) break;  // no longer converging
+        prev = sums[0];
+    }
+    return NIHU_GB_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
 nihu_gb_status nihu_gb_lu_solve(nihu_gb_ctx *ctx, void *A, int64_t n, int64_t lda, const void *b, void *x, int where)
 {
     if (!ctx) return NIHU_GB_ERR_INVALID_ARGUMENT;
@@ -1407,15 +1504,22 @@ nihu_gb_status nihu_gb_lu_solve(nihu_gb_ctx *ctx, void *A, int64_t n, int64_t ld
         dx = (double2 *)px;
         lda = n;
     }
+    bool refined = false;
+    if ((st = lu_solve_mixed(ctx, dA, n, lda, db, dx, &refined))) return st;
+    if (refined) {
+        if (where == NIHU_GB_HOST) CK(cudaMemcpyAsync(x, dx, 16 * n, cudaMemcpyDeviceToHost, ctx->stream));
+        return sync(ctx);
+    }
+    // FP64 factorisation (beyond the FP32 kernels, or the refinement stalled)
     void *ppiv;
     if ((st = scratch(ctx, "lu_piv", sizeof(int) * n, &ppiv))) return st;
     CK(cudaMemsetAsync(ctx->d_flag + 1, 0, sizeof(int), ctx->stream));
     {
-        Phase ph(ctx, "lu_factor");
+        Phase ph(ctx, "lu_factor_fp64");
         CK(launch_lu_factor(dA, n, lda, (int *)ppiv, ctx->d_flag + 1, &ctx->launches, ctx->stream));
     }
     {
-        Phase ph(ctx, "lu_solve");
+        Phase ph(ctx, "lu_solve_fp64");
         CK(launch_lu_solve(dA, n, lda, (const int *)ppiv, db, dx, ctx->stream));
     }
     ctx->launches += 1;
@@ -1449,12 +1553,18 @@ nihu_gb_status solve_tail(nihu_gb_ctx *ctx, int64_t n, int dtype, void *G, void 
                           max_iters, tol, iters, rel_residual);
         if (st && st != NIHU_GB_ERR_NOT_CONVERGED) return st;
     } else {
-        void *ppiv;
-        if ((st = scratch(ctx, "lu_piv", sizeof(int) * n, &ppiv))) return st;
-        CK(cudaMemsetAsync(ctx->d_flag + 1, 0, sizeof(int), ctx->stream));
-        CK(launch_lu_factor((double2 *)Hm, n, n, (int *)ppiv, ctx->d_flag + 1, &ctx->launches, ctx->stream));
-        CK(launch_lu_solve((const double2 *)Hm, n, n, (const int *)ppiv, (const double2 *)drhs, (double2 *)dp, ctx->stream));
-        ctx->launches += 1;
+        bool refined = false;
+        if ((st = lu_solve_mixed(ctx, (const double2 *)Hm, n, n, (const double2 *)drhs, (double2 *)dp, &refined)))
+            return st;
+        if (!refined) {
+            void *ppiv;
+            if ((st = scratch(ctx, "lu_piv", sizeof(int) * n, &ppiv))) return st;
+            CK(cudaMemsetAsync(ctx->d_flag + 1, 0, sizeof(int), ctx->stream));
+            CK(launch_lu_factor((double2 *)Hm, n, n, (int *)ppiv, ctx->d_flag + 1, &ctx->launches, ctx->stream));
+            CK(launch_lu_solve((const double2 *)Hm, n, n, (const int *)ppiv, (const double2 *)drhs, (double2 *)dp,
+                               ctx->stream));
+            ctx->launches += 1;
+        }
         if (iters) *iters = 1;
         if (rel_residual) *rel_residual = 0.0;
         st = NIHU_GB_OK;

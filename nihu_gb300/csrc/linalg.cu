@@ -517,4 +517,436 @@ cudaError_t launch_lu_solve(const double2 *A, int64_t n, int64_t lda, const int 
     return cudaGetLastError();
 }
 
+// --------------------------------------------------- mixed-precision LU
+//
+// Complex LU with partial pivoting in FP32, blocked by LU32_NB columns: each
+// panel is factorised by one CTA in shared memory (pivot search, row swap,
+// scaling and the panel's rank-1 updates), its row swaps are applied to the
+// other columns, the panel's rows of U come from a unit-lower triangular
+// solve, and the trailing matrix takes one rank-LU32_NB update.  The FP64
+// caller refines the solution with the FP64 matrix (residual b - A x in FP64,
+// corrections from these factors), so the FP32 factors set the speed and the
+// FP64 residual the accuracy.  Row swaps are applied to every column (the
+// factors are those of P A = L U, pivots as LAPACK's getrf records them).
+
+constexpr int LU32_NB = 16;
+constexpr int LU32_THREADS = 1024;
+
+__device__ __forceinline__ float2 cmulf(float2 a, float2 b)
+{
+    return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+
+// B (n x n, leading dimension n) = A rounded to complex64
+__global__ void k_to_c64(const double2 *__restrict__ A, int64_t lda, int n, float2 *__restrict__ B)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y;
+    if (i >= n) return;
+    const double2 v = A[(int64_t)j * lda + i];
+    B[(int64_t)j * n + i] = make_float2((float)v.x, (float)v.y);
+}
+
+// panel [j0, j0 + nb) of the n x n matrix A (leading dimension n), rows j0..n
+// in shared memory; piv[j0 + kk] = the global pivot row of column j0 + kk;
+// info = 1 + the first column with a zero pivot
+__global__ void __launch_bounds__(LU32_THREADS) k_lu32_panel(float2 *A, int n, int j0, int nb, int *piv, int *info)
+{
+    extern __shared__ float2 P[];  // column c of the panel at P + c * m
+    __shared__ float wbest[LU32_THREADS / 32];
+    __shared__ int wbi[LU32_THREADS / 32];
+    __shared__ int s_p;
+    __shared__ float2 s_d, s_dk;  // the pivot and the old diagonal entry of the current column
+    const int m = n - j0;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    float2 *G = A + (int64_t)j0 * n + j0;
+    for (int c = 0; c < nb; ++c)
+        for (int r = tid; r < m; r += blockDim.x) P[c * m + r] = G[(int64_t)c * n + r];
+    __syncthreads();
+    for (int kk = 0; kk < nb; ++kk) {
+        float2 *col = P + kk * m;
+        float bv = -1.0f;
+        int bi = kk;
+        for (int r = kk + tid; r < m; r += blockDim.x) {
+            const float v = col[r].x * col[r].x + col[r].y * col[r].y;
+            if (v > bv) {
+                bv = v;
+                bi = r;
+            }
+        }
+        for (int o = 16; o > 0; o >>= 1) {
+            const float ov = __shfl_xor_sync(0xffffffffu, bv, o);
+            const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+            if (ov > bv || (ov == bv && oi < bi)) {
+                bv = ov;
+                bi = oi;
+            }
+        }
+        if (lane == 0) {
+            wbest[warp] = bv;
+            wbi[warp] = bi;
+        }
+        __syncthreads();
+        if (warp == 0) {
+            bv = wbest[lane];
+            bi = wbi[lane];
+            for (int o = 16; o > 0; o >>= 1) {
+                const float ov = __shfl_xor_sync(0xffffffffu, bv, o);
+                const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+                if (ov > bv || (ov == bv && oi < bi)) {
+                    bv = ov;
+                    bi = oi;
+                }
+            }
+            if (lane == 0) {
+                s_p = bi;
+                s_d = col[bi];
+                s_dk = col[kk];
+                piv[j0 + kk] = j0 + bi;
+                if (!(bv > 0.0f) && *info == 0) *info = j0 + kk + 1;
+            }
+        }
+        __syncthreads();
+        // swap rows kk and p (columns other than kk) and, in the same pass,
+        // column kk: the pivot to row kk, the rest divided by it
+        const int p = s_p;
+        const float2 d = s_d, dk = s_dk;
+        if (p != kk && tid < nb && tid != kk) {
+            const float2 t = P[tid * m + kk];
+            P[tid * m + kk] = P[tid * m + p];
+            P[tid * m + p] = t;
+        }
+        const float den = d.x * d.x + d.y * d.y;
+        const float2 inv = den > 0.0f ? make_float2(d.x / den, -d.y / den) : make_float2(1.0f, 0.0f);
+        for (int r = kk + 1 + tid; r < m; r += blockDim.x) {
+            const float2 v = r == p ? dk : col[r];
+            col[r] = den > 0.0f ? cmulf(v, inv) : v;
+        }
+        __syncthreads();
+        if (tid == 0) col[kk] = d;
+        // rank-1 update of the panel's later columns, one row per thread
+        for (int r = kk + 1 + tid; r < m; r += blockDim.x) {
+            const float2 l = col[r];
+            for (int c = kk + 1; c < nb; ++c) {
+                const float2 u = P[c * m + kk];
+                float2 v = P[c * m + r];
+                v.x -= l.x * u.x - l.y * u.y;
+                v.y -= l.x * u.y + l.y * u.x;
+                P[c * m + r] = v;
+            }
+        }
+        __syncthreads();
+    }
+    for (int c = 0; c < nb; ++c)
+        for (int r = tid; r < m; r += blockDim.x) G[(int64_t)c * n + r] = P[c * m + r];
+}
+
+// the panel's row swaps on every column outside [j0, j0 + nb), in order
+__global__ void k_lu32_swap(float2 *A, int n, int j0, int nb, const int *__restrict__ piv)
+{
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= n || (j >= j0 && j < j0 + nb)) return;
+    float2 *col = A + (int64_t)j * n;
+    for (int kk = 0; kk < nb; ++kk) {
+        const int p = piv[j0 + kk];
+        if (p != j0 + kk) {
+            const float2 t = col[j0 + kk];
+            col[j0 + kk] = col[p];
+            col[p] = t;
+        }
+    }
+}
+
+// rows [j0, j0 + nb) of columns j >= j0 + nb: U12 = L11^{-1} A12 (unit lower L11)
+__global__ void __launch_bounds__(256) k_lu32_trsm(float2 *A, int n, int j0, int nb)
+{
+    __shared__ float2 L[LU32_NB][LU32_NB];
+    for (int t = threadIdx.x; t < LU32_NB * LU32_NB; t += blockDim.x) {
+        const int r = t % LU32_NB, c = t / LU32_NB;
+        L[r][c] = (r < nb && c < nb) ? A[(int64_t)(j0 + c) * n + j0 + r] : make_float2(0.0f, 0.0f);
+    }
+    __syncthreads();
+    const int j = j0 + nb + blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= n) return;
+    float2 *col = A + (int64_t)j * n + j0;
+    float2 x[LU32_NB];
+#pragma unroll
+    for (int r = 0; r < LU32_NB; ++r) x[r] = r < nb ? col[r] : make_float2(0.0f, 0.0f);
+#pragma unroll
+    for (int r = 1; r < LU32_NB; ++r)
+#pragma unroll
+        for (int q = 0; q < r; ++q) {
+            const float2 l = L[r][q];
+            x[r].x -= l.x * x[q].x - l.y * x[q].y;
+            x[r].y -= l.x * x[q].y + l.y * x[q].x;
+        }
+#pragma unroll
+    for (int r = 0; r < LU32_NB; ++r)
+        if (r < nb) col[r] = x[r];
+}
+
+// A22 -= L21 U12 on the trailing matrix (rows and columns >= j0 + nb), one
+// 64 x 64 tile per 256-thread block, 4 x 4 entries per thread
+__global__ void __launch_bounds__(256) k_lu32_update(float2 *A, int n, int j0, int nb)
+{
+    __shared__ float2 Ls[LU32_NB][64], Us[LU32_NB][64];
+    const int base = j0 + nb;
+    const int i0 = base + blockIdx.x * 64, c0 = base + blockIdx.y * 64;
+    const int tid = threadIdx.x;
+    for (int t = tid; t < 64 * LU32_NB; t += 256) {
+        const int q = t / 64, ii = t % 64;
+        const int i = i0 + ii;
+        Ls[q][ii] = (q < nb && i < n) ? A[(int64_t)(j0 + q) * n + i] : make_float2(0.0f, 0.0f);
+        const int jj = t / LU32_NB, qq = t % LU32_NB;
+        const int c = c0 + jj;
+        Us[qq][jj] = (qq < nb && c < n) ? A[(int64_t)c * n + j0 + qq] : make_float2(0.0f, 0.0f);
+    }
+    __syncthreads();
+    const int tx = tid & 15, ty = tid >> 4;
+    float2 acc[4][4];
+#pragma unroll
+    for (int a = 0; a < 4; ++a)
+#pragma unroll
+        for (int b = 0; b < 4; ++b) acc[a][b] = make_float2(0.0f, 0.0f);
+    for (int q = 0; q < nb; ++q) {
+        float2 l[4], u[4];
+#pragma unroll
+        for (int a = 0; a < 4; ++a) l[a] = Ls[q][tx + 16 * a];
+#pragma unroll
+        for (int b = 0; b < 4; ++b) u[b] = Us[q][ty * 4 + b];
+#pragma unroll
+        for (int a = 0; a < 4; ++a)
+#pragma unroll
+            for (int b = 0; b < 4; ++b) {
+                acc[a][b].x += l[a].x * u[b].x - l[a].y * u[b].y;
+                acc[a][b].y += l[a].x * u[b].y + l[a].y * u[b].x;
+            }
+    }
+#pragma unroll
+    for (int b = 0; b < 4; ++b) {
+        const int c = c0 + ty * 4 + b;
+        if (c >= n) continue;
+#pragma unroll
+        for (int a = 0; a < 4; ++a) {
+            const int i = i0 + tx + 16 * a;
+            if (i >= n) continue;
+            float2 *p = A + (int64_t)c * n + i;
+            float2 v = *p;
+            v.x -= acc[a][b].x;
+            v.y -= acc[a][b].y;
+            *p = v;
+        }
+    }
+}
+
+// d = U^{-1} L^{-1} P r from the FP32 factors (one CTA, the vector in shared
+// memory): the pivots in order, then blocks of 32 rows -- warp 0 solves the
+// diagonal block, every thread updates the remaining rows
+// rows [i_begin, i_end) of y less the block's 32 columns (or bn < 32) of the
+// factor times y[b0 ..]: loads issued 8 at a time
+__device__ __forceinline__ void lu32_block_update(const float2 *__restrict__ A, int n, float2 *y, int b0, int bn,
+                                                  int i_begin, int i_end)
+{
+    for (int i = i_begin + threadIdx.x; i < i_end; i += blockDim.x) {
+        float2 acc = y[i];
+        if (bn == 32) {
+#pragma unroll 8
+            for (int q = 0; q < 32; ++q) {
+                const float2 l = A[(int64_t)(b0 + q) * n + i], yq = y[b0 + q];
+                acc.x -= l.x * yq.x - l.y * yq.y;
+                acc.y -= l.x * yq.y + l.y * yq.x;
+            }
+        } else {
+            for (int q = 0; q < bn; ++q) {
+                const float2 l = A[(int64_t)(b0 + q) * n + i], yq = y[b0 + q];
+                acc.x -= l.x * yq.x - l.y * yq.y;
+                acc.y -= l.x * yq.y + l.y * yq.x;
+            }
+        }
+        y[i] = acc;
+    }
+}
+
+__global__ void __launch_bounds__(LU32_THREADS) k_lu32_solve(const float2 *__restrict__ A, int n,
+                                                             const int *__restrict__ piv, const double2 *__restrict__ r,
+                                                             double2 *__restrict__ d)
+{
+    extern __shared__ float2 y[];
+    __shared__ float2 D[32][33];  // the current diagonal block, D[row][col]
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    for (int i = tid; i < n; i += blockDim.x) y[i] = make_float2((float)r[i].x, (float)r[i].y);
+    __syncthreads();
+    if (tid == 0)
+        for (int k = 0; k < n; ++k) {
+            const int p = piv[k];
+            if (p != k) {
+                const float2 t = y[k];
+                y[k] = y[p];
+                y[p] = t;
+            }
+        }
+    __syncthreads();
+    for (int b0 = 0; b0 < n; b0 += 32) {
+        const int bn = min(32, n - b0);
+        for (int t = tid; t < bn * bn; t += blockDim.x) {
+            const int c = t / bn, rr = t - c * bn;
+            D[rr][c] = A[(int64_t)(b0 + c) * n + b0 + rr];
+        }
+        __syncthreads();
+        if (warp == 0) {
+            float2 v = lane < bn ? y[b0 + lane] : make_float2(0.0f, 0.0f);
+            for (int q = 0; q < bn - 1; ++q) {
+                const float2 yq = make_float2(__shfl_sync(0xffffffffu, v.x, q), __shfl_sync(0xffffffffu, v.y, q));
+                if (lane > q && lane < bn) {
+                    const float2 l = D[lane][q];
+                    v.x -= l.x * yq.x - l.y * yq.y;
+                    v.y -= l.x * yq.y + l.y * yq.x;
+                }
+            }
+            if (lane < bn) y[b0 + lane] = v;
+        }
+        __syncthreads();
+        lu32_block_update(A, n, y, b0, bn, b0 + bn, n);
+        __syncthreads();
+    }
+    for (int b1 = n; b1 > 0; b1 -= 32) {
+        const int b0 = max(0, b1 - 32), bn = b1 - b0;
+        for (int t = tid; t < bn * bn; t += blockDim.x) {
+            const int c = t / bn, rr = t - c * bn;
+            D[rr][c] = A[(int64_t)(b0 + c) * n + b0 + rr];
+        }
+        __syncthreads();
+        if (warp == 0) {
+            float2 v = lane < bn ? y[b0 + lane] : make_float2(0.0f, 0.0f);
+            for (int q = bn - 1; q >= 0; --q) {
+                if (lane == q) {
+                    const float2 u = D[q][q];
+                    const float den = u.x * u.x + u.y * u.y;
+                    v = make_float2((v.x * u.x + v.y * u.y) / den, (v.y * u.x - v.x * u.y) / den);
+                }
+                const float2 yq = make_float2(__shfl_sync(0xffffffffu, v.x, q), __shfl_sync(0xffffffffu, v.y, q));
+                if (lane < q) {
+                    const float2 u = D[lane][q];
+                    v.x -= u.x * yq.x - u.y * yq.y;
+                    v.y -= u.x * yq.y + u.y * yq.x;
+                }
+            }
+            if (lane < bn) y[b0 + lane] = v;
+        }
+        __syncthreads();
+        lu32_block_update(A, n, y, b0, bn, 0, b0);
+        __syncthreads();
+    }
+    for (int i = tid; i < n; i += blockDim.x) d[i] = make_double2((double)y[i].x, (double)y[i].y);
+}
+
+// x += d; sums[0] = |d|^2, sums[1] = |x|^2 (one block, fixed order)
+__global__ void __launch_bounds__(1024) k_lu32_update_x(double2 *x, const double2 *__restrict__ d, int n, double *sums)
+{
+    __shared__ double sd[32], sx[32];
+    double ad = 0.0, ax = 0.0;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        const double2 di = d[i];
+        double2 xi = x[i];
+        xi.x += di.x;
+        xi.y += di.y;
+        x[i] = xi;
+        ad += di.x * di.x + di.y * di.y;
+        ax += xi.x * xi.x + xi.y * xi.y;
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        ad += __shfl_xor_sync(0xffffffffu, ad, o);
+        ax += __shfl_xor_sync(0xffffffffu, ax, o);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        sd[threadIdx.x >> 5] = ad;
+        sx[threadIdx.x >> 5] = ax;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double td = 0.0, tx = 0.0;
+        for (int w = 0; w < (int)(blockDim.x / 32); ++w) {
+            td += sd[w];
+            tx += sx[w];
+        }
+        sums[0] = td;
+        sums[1] = tx;
+    }
+}
+
+size_t lu32_solve_smem(int n) { return sizeof(float2) * (size_t)n; }
+
+// columns of the panel at j0: as many as LU32_NB and the shared memory allow
+static int lu32_panel_cols(int n, int j0, size_t smem_max)
+{
+    const size_t per_col = sizeof(float2) * (size_t)(n - j0);
+    return (int)std::min<size_t>({(size_t)LU32_NB, (size_t)(n - j0), smem_max / per_col});
+}
+
+// dynamic shared memory a kernel may take: the per-block limit less its static part
+template <typename K>
+static size_t dyn_smem_max(K kernel, size_t smem_max)
+{
+    cudaFuncAttributes fa;
+    if (cudaFuncGetAttributes(&fa, kernel) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    return smem_max > fa.sharedSizeBytes ? smem_max - fa.sharedSizeBytes : 0;
+}
+
+bool lu32_fits(int n, size_t smem_max)
+{
+    return n >= 1 && n <= 65535 && lu32_panel_cols(n, 0, dyn_smem_max(k_lu32_panel, smem_max)) >= 1 &&
+           lu32_solve_smem(n) <= dyn_smem_max(k_lu32_solve, smem_max);
+}
+
+cudaError_t lu32_prepare(int n, size_t smem_max, size_t *panel_smem)
+{
+    if (!lu32_fits(n, smem_max)) return cudaErrorInvalidValue;
+    // every panel's shared memory (n - j0 rows x its columns) is within the limit
+    *panel_smem = dyn_smem_max(k_lu32_panel, smem_max);
+    cudaError_t e = cudaFuncSetAttribute(k_lu32_panel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)*panel_smem);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_lu32_solve, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)lu32_solve_smem(n));
+    return e;
+}
+
+cudaError_t launch_to_c64(const double2 *A, int64_t lda, int n, float2 *F, cudaStream_t s)
+{
+    k_to_c64<<<dim3((n + 255) / 256, n), 256, 0, s>>>(A, lda, n, F);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_lu32_factor(float2 *F, int n, int *piv, int *info, size_t panel_smem, int64_t *launches,
+                               cudaStream_t s)
+{
+    const size_t smem_max = panel_smem;
+    for (int j0 = 0, nb; j0 < n; j0 += nb) {
+        nb = lu32_panel_cols(n, j0, smem_max);
+        k_lu32_panel<<<1, LU32_THREADS, sizeof(float2) * (size_t)(n - j0) * nb, s>>>(F, n, j0, nb, piv, info);
+        k_lu32_swap<<<(n + 255) / 256, 256, 0, s>>>(F, n, j0, nb, piv);
+        *launches += 2;
+        const int rest = n - j0 - nb;
+        if (rest > 0) {
+            k_lu32_trsm<<<(rest + 255) / 256, 256, 0, s>>>(F, n, j0, nb);
+            const unsigned t = (unsigned)((rest + 63) / 64);
+            k_lu32_update<<<dim3(t, t), 256, 0, s>>>(F, n, j0, nb);
+            *launches += 2;
+        }
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_lu32_solve(const float2 *F, int n, const int *piv, const double2 *r, double2 *d, cudaStream_t s)
+{
+    k_lu32_solve<<<1, LU32_THREADS, lu32_solve_smem(n), s>>>(F, n, piv, r, d);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_lu32_update_x(double2 *x, const double2 *d, int n, double *sums, cudaStream_t s)
+{
+    k_lu32_update_x<<<1, 1024, 0, s>>>(x, d, n, sums);
+    return cudaGetLastError();
+}
+
 }  // namespace nihu

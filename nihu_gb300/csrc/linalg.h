@@ -35,6 +35,24 @@ cudaError_t launch_sub(const double2 *a, const double2 *b, double2 *dst, int64_t
 
 cudaError_t launch_lu_factor(double2 *A, int64_t n, int64_t lda, int *piv, int *info, int64_t *launches,
                              cudaStream_t s);
+// mixed-precision LU (FP32 factors of the FP64 matrix, refined by the caller):
+// whether order n fits the kernels' shared memory (smem_max: the device's
+// per-block opt-in limit), and the solve kernel's shared memory
+bool lu32_fits(int n, size_t smem_max);
+size_t lu32_solve_smem(int n);
+// kernel attributes for order n (outside any stream capture); panel_smem
+// receives the panel kernel's dynamic shared memory limit
+cudaError_t lu32_prepare(int n, size_t smem_max, size_t *panel_smem);
+// F (n x n complex64, leading dimension n) = A rounded to complex64
+cudaError_t launch_to_c64(const double2 *A, int64_t lda, int n, float2 *F, cudaStream_t s);
+// F in place = its FP32 LU factors with partial pivoting (piv as getrf,
+// info = 1 + first zero pivot column); stream-capturable
+cudaError_t launch_lu32_factor(float2 *F, int n, int *piv, int *info, size_t panel_smem, int64_t *launches,
+                               cudaStream_t s);
+// d = (P^T L U)^{-1} r with the FP32 factors
+cudaError_t launch_lu32_solve(const float2 *F, int n, const int *piv, const double2 *r, double2 *d, cudaStream_t s);
+// x += d; sums[0] = |d|^2, sums[1] = |x|^2
+cudaError_t launch_lu32_update_x(double2 *x, const double2 *d, int n, double *sums, cudaStream_t s);
 cudaError_t launch_lu_solve(const double2 *A, int64_t n, int64_t lda, const int *piv, const double2 *b, double2 *x,
                             cudaStream_t s);
 
