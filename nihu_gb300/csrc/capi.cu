@@ -1778,13 +1778,16 @@ nihu_gb_status gmres_cycle_multi(nihu_gb_ctx *ctx, const ApplyFn &apply, int64_t
         CK(cudaMemcpyAsync(dact, runi.data(), sizeof(int) * nrhs, cudaMemcpyHostToDevice, ctx->stream));
         if ((st = apply(V + (size_t)k * blk, W, dact))) return st;
         std::vector<std::vector<C>> h(nrhs, std::vector<C>(k + 2, C(0)));
-        for (int pass = 0; pass < 2; ++pass) {  // CGS2
-            CK(launch_bdot(V, k + 1, W, n, nrhs, part, hd, ctx->stream));
+        // CGS2 with FP32 products and sums on the FP64-stored basis: this is the
+        // inner solve of a refinement (inner tolerance 1e-3 or so), whose
+        // residual the outer loop forms in FP64; the FP64 pipe stays free
+        for (int pass = 0; pass < 2; ++pass) {
+            CK(launch_bdot(V, k + 1, W, n, nrhs, part, hd, ctx->stream, true));
             CK(cudaMemcpyAsync(hh.data(), hd, 16 * (size_t)(k + 1) * nrhs, cudaMemcpyDeviceToHost, ctx->stream));
             if ((st = sync(ctx))) return st;
             for (int v = 0; v <= k; ++v)
                 for (int r = 0; r < nrhs; ++r) h[r][v] += C(hh[(size_t)v * nrhs + r].x, hh[(size_t)v * nrhs + r].y);
-            CK(launch_bcombo(V, n, nrhs, k + 1, hd, -1.0, W, ctx->stream));
+            CK(launch_bcombo(V, n, nrhs, k + 1, hd, -1.0, W, ctx->stream, true));
             ctx->launches += 3;
         }
         std::vector<double> hn(nrhs);

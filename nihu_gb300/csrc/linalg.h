@@ -61,10 +61,12 @@ cudaError_t launch_gemm_c64(void *cublas, int mode, const void *A, int64_t m, in
                             int64_t ldx, int nrhs, double2 *Y, int64_t ldy, double are, double aim, double bre,
                             double bim, float *Xp, float *Z, cudaStream_t s, int *cublas_status);
 int bdot_blocks(int64_t n);
+// fp32: products and partial sums in FP32 on the FP64-stored vectors (the
+// inner Arnoldi of a refinement), else FP64
 cudaError_t launch_bdot(const double2 *V, int nv, const double2 *W, int64_t n, int nrhs, double2 *part, double2 *out,
-                        cudaStream_t s);
+                        cudaStream_t s, bool fp32 = false);
 cudaError_t launch_bcombo(const double2 *V, int64_t n, int nrhs, int nv, const double2 *h, double sign, double2 *W,
-                          cudaStream_t s);
+                          cudaStream_t s, bool fp32 = false);
 cudaError_t launch_bscale(const double2 *src, double2 *dst, int64_t n, int nrhs, const double *sc, cudaStream_t s);
 cudaError_t launch_rsub(const double2 *B, double2 *R, size_t count, cudaStream_t s);
 

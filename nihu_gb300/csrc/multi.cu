@@ -12,6 +12,8 @@
 // FP32-accurate at tensor-core speed).
 #include <cublas_v2.h>
 
+#include <type_traits>
+
 #include "kernels.h"
 #include "linalg.h"
 
@@ -88,7 +90,9 @@ cudaError_t launch_gemm_c64(void *cublas, int mode, const void *A, int64_t m, in
 
 constexpr int BT = 256;
 
-// part[((v * nrhs + r) * blocks + b)] = sum over the block's rows of conj(V_v[:, r]) . W[:, r]
+// part[((v * nrhs + r) * blocks + b)] = sum over the block's rows of conj(V_v[:, r]) . W[:, r];
+// F32: products and the thread's and warp's sums in FP32 (the block's in FP64)
+template <bool F32>
 __global__ void __launch_bounds__(BT) k_bdot(const double2 *__restrict__ V, const double2 *__restrict__ W, int64_t n,
                                              int nrhs, double2 *part)
 {
@@ -96,11 +100,13 @@ __global__ void __launch_bounds__(BT) k_bdot(const double2 *__restrict__ V, cons
     const int v = blockIdx.z, r = blockIdx.y;
     const double2 *a = V + ((int64_t)v * nrhs + r) * n;
     const double2 *b = W + (int64_t)r * n;
-    double ar = 0.0, ai = 0.0;
+    using T = std::conditional_t<F32, float, double>;
+    T ar = 0, ai = 0;
     for (int64_t i = (int64_t)blockIdx.x * BT + threadIdx.x; i < n; i += (int64_t)gridDim.x * BT) {
-        double2 x = a[i], y = b[i];
-        ar += x.x * y.x + x.y * y.y;
-        ai += x.x * y.y - x.y * y.x;
+        const double2 x = a[i], y = b[i];
+        const T xr = (T)x.x, xi = (T)x.y, yr = (T)y.x, yi = (T)y.y;
+        ar += xr * yr + xi * yi;
+        ai += xr * yi - xi * yr;
     }
     ar = warp_sum(ar);
     ai = warp_sum(ai);
@@ -127,19 +133,25 @@ __global__ void k_bdot_reduce(const double2 *__restrict__ part, int count, int b
     out[t] = make_double2(sr, si);
 }
 
-// W[:, r] += sign * sum_{v < nv} V_v[:, r] h[v * nrhs + r]
+// W[:, r] += sign * sum_{v < nv} V_v[:, r] h[v * nrhs + r]; F32: the sum in FP32
+template <bool F32>
 __global__ void k_bcombo(const double2 *__restrict__ V, int64_t n, int nrhs, int nv, const double2 *__restrict__ h,
                          double sign, double2 *W)
 {
     int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     int r = blockIdx.y;
     if (i >= n) return;
-    double2 acc = W[(int64_t)r * n + i];
+    using T = std::conditional_t<F32, float, double>;
+    T sr = 0, si = 0;
     for (int v = 0; v < nv; ++v) {
-        double2 a = V[((int64_t)v * nrhs + r) * n + i], c = h[v * nrhs + r];
-        acc.x += sign * (a.x * c.x - a.y * c.y);
-        acc.y += sign * (a.x * c.y + a.y * c.x);
+        const double2 a = V[((int64_t)v * nrhs + r) * n + i], c = h[v * nrhs + r];
+        const T ar = (T)a.x, ai = (T)a.y, cr = (T)c.x, ci = (T)c.y;
+        sr += ar * cr - ai * ci;
+        si += ar * ci + ai * cr;
     }
+    double2 acc = W[(int64_t)r * n + i];
+    acc.x += sign * (double)sr;
+    acc.y += sign * (double)si;
     W[(int64_t)r * n + i] = acc;
 }
 
@@ -177,21 +189,23 @@ int bdot_blocks(int64_t n)
 }
 
 cudaError_t launch_bdot(const double2 *V, int nv, const double2 *W, int64_t n, int nrhs, double2 *part, double2 *out,
-                        cudaStream_t s)
+                        cudaStream_t s, bool fp32)
 {
     int blocks = bdot_blocks(n);
     dim3 g(blocks, nrhs, nv);
-    k_bdot<<<g, BT, 0, s>>>(V, W, n, nrhs, part);
+    if (fp32) k_bdot<true><<<g, BT, 0, s>>>(V, W, n, nrhs, part);
+    else k_bdot<false><<<g, BT, 0, s>>>(V, W, n, nrhs, part);
     int count = nv * nrhs;
     k_bdot_reduce<<<(count + 255) / 256, 256, 0, s>>>(part, count, blocks, out);
     return cudaGetLastError();
 }
 
 cudaError_t launch_bcombo(const double2 *V, int64_t n, int nrhs, int nv, const double2 *h, double sign, double2 *W,
-                          cudaStream_t s)
+                          cudaStream_t s, bool fp32)
 {
     dim3 g((unsigned)((n + 255) / 256), nrhs);
-    k_bcombo<<<g, 256, 0, s>>>(V, n, nrhs, nv, h, sign, W);
+    if (fp32) k_bcombo<true><<<g, 256, 0, s>>>(V, n, nrhs, nv, h, sign, W);
+    else k_bcombo<false><<<g, 256, 0, s>>>(V, n, nrhs, nv, h, sign, W);
     return cudaGetLastError();
 }
 
