@@ -78,3 +78,31 @@ def test_pulsating_sphere(gpu_ctx, oracle, solver, dtype):
     assert np.abs(p - p_ref).max() / np.abs(p_ref).max() < 1e-4
     pa = -1.0 / (1 + 1j * k)
     assert np.abs(p - pa).max() / abs(pa) < 0.02
+
+
+def test_lu_ill_conditioned_falls_back_to_fp64(gpu_ctx):
+    """cond(A) = 1e9: the FP32 factors cannot be refined (cond x eps32 > 1), so
+    the solve takes the FP64 factorisation; the result is as accurate as an FP64
+    LU can be (cond x eps64)."""
+    rng = np.random.default_rng(11)
+    n = 200
+    Q1, _ = np.linalg.qr(rand_c(rng, n, n))
+    Q2, _ = np.linalg.qr(rand_c(rng, n, n))
+    A = (Q1 * np.logspace(0, -9, n)) @ Q2.conj().T
+    b = rand_c(rng, n)
+    x = g.lu_solve(A, b, ctx=gpu_ctx)
+    # backward stable: the residual is a few eps |A| |x|; the error is cond x that
+    assert np.linalg.norm(A @ x - b) / (np.linalg.norm(A, 2) * np.linalg.norm(x)) < 1e-13
+    ref = np.linalg.solve(A, b)
+    assert np.linalg.norm(x - ref) / np.linalg.norm(ref) < 1e-5
+
+
+@pytest.mark.parametrize("n", [2048, 3000])
+def test_lu_panel_widths_below_sixteen(gpu_ctx, n):
+    """Orders whose first panels hold fewer than 16 columns in shared memory."""
+    rng = np.random.default_rng(n)
+    A = rand_c(rng, n, n) + n * np.eye(n) * 0.05
+    b = rand_c(rng, n)
+    x = g.lu_solve(A, b, ctx=gpu_ctx)
+    ref = np.linalg.solve(A, b)
+    assert np.linalg.norm(x - ref) / np.linalg.norm(ref) < 1e-11

@@ -137,3 +137,33 @@ def test_sweep_right_hand_sides_without_slp_matrices(gpu_ctx, precision):
     for f in range(nk):
         p1, it1, res1 = g.solve_cbie(ms[mesh_of[f]], float(ks[f]), q[f], tol=1e-7, precision=precision, ctx=gpu_ctx)
         assert np.abs(P[f] - p1).max() <= 1e-5 * np.abs(p1).max(), f
+
+
+def test_sweep_plan_in_place_staging(gpu_ctx):
+    """nihu_gb_sweep_plan_host_buffers: Neumann data written straight into the
+    plan's pinned staging give the same pressures as host arrays passed in."""
+    import ctypes
+    L = g.lib()
+    ms = [g.create_mesh(*meshes.icosphere(s)) for s in (1, 2)]
+    mesh_of = np.array([0, 1, 1, 0, 1], np.int32)
+    plan = g.SweepPlan(ms, mesh_of, k_max=4.0, tol=1e-7, ctx=gpu_ctx)
+    rng = np.random.default_rng(8)
+    ks = rng.uniform(0.3, 4.0, len(mesh_of))
+    q = [rng.standard_normal(ms[i].num_elements) + 1j * rng.standard_normal(ms[i].num_elements) for i in mesh_of]
+    P_ref, it_ref, _, _ = plan.run(ks, q, check=False)
+    qp, pp = ctypes.c_void_p(), ctypes.c_void_p()
+    gpu_ctx.check(L.nihu_gb_sweep_plan_host_buffers(plan.handle, ctypes.byref(qp), ctypes.byref(pp)))
+    total = sum(ms[i].num_elements for i in mesh_of)
+    qbuf = np.frombuffer((ctypes.c_double * (2 * total)).from_address(qp.value), np.complex128)
+    pbuf = np.frombuffer((ctypes.c_double * (2 * total)).from_address(pp.value), np.complex128)
+    qbuf[:] = 0
+    qbuf[:] = np.concatenate(q)
+    it = np.zeros(len(mesh_of), np.int32)
+    st = L.nihu_gb_sweep_plan_run(plan.handle, np.ascontiguousarray(ks).ctypes.data, qp, pp, it.ctypes.data, None, None)
+    assert st in (0, 6)  # OK, or not converged (the plan's result is still written)
+    assert list(it) == list(it_ref)
+    assert np.array_equal(np.concatenate(P_ref), pbuf)
+    # the Python front end's own copies are not views of the staging
+    P2, _, _, _ = plan.run(ks * 0.5, q, check=False)
+    assert not np.array_equal(np.concatenate(P_ref), np.concatenate(P2))
+    plan.close()
