@@ -416,8 +416,9 @@ nihu_gb_status nihu_gb_solve_burton_miller(nihu_gb_ctx *ctx, const nihu_gb_mesh 
  * series of the nearly singular terms are sized for it).  Creation builds
  * the near-pair lists, allocates every buffer (matrices of all instances,
  * Krylov state, pinned staging) and records: the uploads, each mesh's
- * frequency-batch assembly, identities and right-hand sides, one persistent
- * GMRES(restart) launch over all instances, and the downloads. */
+ * frequency-batch assembly, identities and right-hand sides, the persistent
+ * GMRES(restart) launches over all instances, and the downloads; its launch
+ * set-up is chosen by measurement (nihu_gb_sweep_plan_tuning). */
 nihu_gb_status nihu_gb_sweep_plan_create(nihu_gb_ctx *ctx, int n_meshes, const nihu_gb_mesh *const *meshes, int family,
                                          int nk, const int *mesh_of, double k_max, int precision, int restart,
                                          int max_iters, double tol, nihu_gb_sweep_plan **out);
@@ -434,6 +435,13 @@ nihu_gb_status nihu_gb_sweep_plan_run(nihu_gb_sweep_plan *plan, const double *ks
  * given these very pointers as q and p reads and writes them in place, with
  * no host copy; they stay valid until nihu_gb_sweep_plan_destroy. */
 nihu_gb_status nihu_gb_sweep_plan_host_buffers(nihu_gb_sweep_plan *plan, void **q, void **p);
+/* The launch set-up the plan's autotuner measured fastest at creation (each
+ * candidate captured and replayed on wave numbers spread over (0.1, 1] k_max
+ * with unit Neumann data): CTAs per cluster of the persistent GMRES launch,
+ * wave numbers per block of the regular assembly kernel, and that replay's
+ * time in ms.  Any pointer may be NULL. */
+nihu_gb_status nihu_gb_sweep_plan_tuning(const nihu_gb_sweep_plan *plan, int *cluster, int *freq_per_block,
+                                         double *replay_ms);
 void nihu_gb_sweep_plan_destroy(nihu_gb_sweep_plan *plan);
 
 /* ------------------------------------------------------------ serving */

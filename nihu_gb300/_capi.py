@@ -64,6 +64,7 @@ SIGNATURES = {
     "nihu_gb_sweep_plan_create": (_i, [_vp, _i, _vp, _i, _i, _vp, _d, _i, _i, _i, _d, ctypes.POINTER(_vp)]),
     "nihu_gb_sweep_plan_run": (_i, [_vp, _vp, _vp, _vp, _vp, _vp, _vp]),
     "nihu_gb_sweep_plan_host_buffers": (_i, [_vp, ctypes.POINTER(_vp), ctypes.POINTER(_vp)]),
+    "nihu_gb_sweep_plan_tuning": (_i, [_vp, _vp, _vp, _vp]),
     "nihu_gb_sweep_plan_destroy": (None, [_vp]),
     "nihu_gb_server_create": (_i, [_vp, _i, _vp, _i, _i, _sz, _i, _i, _i, _d, _i, ctypes.POINTER(_vp)]),
     "nihu_gb_server_destroy": (None, [_vp]),

@@ -699,21 +699,19 @@ class SweepPlan:
         self._q = np.frombuffer((ctypes.c_double * (2 * total)).from_address(qp.value), np.complex128)
         self._p = np.frombuffer((ctypes.c_double * (2 * total)).from_address(pp.value), np.complex128)
 
-    def run(self, ks, q=None, check: bool = True):
-        """Returns (list of p_f, iterations, relative residual estimates, converged)."""
+    def run(self, ks, q=None, check: bool = True, copy: bool = True):
+        """Returns (list of p_f, iterations, relative residual estimates, converged).
+        copy=False returns views of the plan's pinned staging (no host copy),
+        valid until the next run or close()."""
         ks = np.ascontiguousarray(ks, dtype=np.float64)
         if ks.shape != (self.nk,):
             raise ValueError("one wave number per instance")
         if q is None:
             self._q[:] = 1.0
         else:
-            if len(q) != self.nk:
+            if len(q) != self.nk or [np.shape(v) for v in q] != [(n,) for n in self.sizes]:
                 raise ValueError("q: one vector per instance with its mesh's element count")
-            for f, v in enumerate(q):
-                v = np.asarray(v)
-                if v.shape != (self.sizes[f],):
-                    raise ValueError("q: one vector per instance with its mesh's element count")
-                self._q[self._off[f]:self._off[f + 1]] = v
+            np.concatenate(q, out=self._q)  # one pass, straight into the pinned staging
         it = np.zeros(self.nk, np.int32)
         rel = np.zeros(self.nk)
         conv = np.zeros(self.nk, np.int32)
@@ -721,7 +719,14 @@ class SweepPlan:
                                             it.ctypes.data, rel.ctypes.data, conv.ctypes.data)
         if st != C.OK and (check or st != 6):
             self.ctx.check(st)
-        return np.split(self._p.copy(), self._off[1:-1]), it, rel, conv.astype(bool)
+        return np.split(self._p.copy() if copy else self._p, self._off[1:-1]), it, rel, conv.astype(bool)
+
+    def tuning(self) -> dict:
+        """The launch set-up the plan's autotuner chose at creation."""
+        c, f, ms = ctypes.c_int(0), ctypes.c_int(0), ctypes.c_double(0.0)
+        self.ctx.check(C.lib().nihu_gb_sweep_plan_tuning(self.handle, ctypes.byref(c), ctypes.byref(f),
+                                                         ctypes.byref(ms)))
+        return {"cluster": c.value, "freq_per_block": f.value, "replay_ms": ms.value}
 
     def close(self):
         if getattr(self, "handle", None):

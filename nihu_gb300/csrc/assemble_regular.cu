@@ -99,6 +99,15 @@ __device__ __forceinline__ void store_entry(Out *p, R re, R im, R are, R aim, bo
 template <typename R>
 __host__ __device__ constexpr int rhs_f_max() { return sizeof(R) == 4 ? 16 : 8; }
 
+// the wave numbers per block a launch uses: RegularArgs::rhs_fmax within the
+// cap that keeps the shared memory under 48 KB, else the default
+template <typename R>
+__host__ __device__ inline int rhs_fmax_of(const RegularArgs &a)
+{
+    constexpr int cap = sizeof(R) == 4 ? 20 : 10;
+    return a.rhs_fmax > 0 ? (a.rhs_fmax < cap ? a.rhs_fmax : cap) : rhs_f_max<R>();
+}
+
 template <typename R>
 using Cplx = std::conditional_t<sizeof(R) == 4, float2, double2>;
 
@@ -121,23 +130,32 @@ __device__ __forceinline__ void store_plain(Out *p, R re, R im)
     *p = o;
 }
 
-// the DLP outputs of a frequency batch from wave number f on: a pointer that
-// steps by mat_stride, or the device table outs (separate matrices)
-template <typename Out>
+// the outputs of a frequency batch from wave number f on: a pointer that
+// steps by mat_stride, or (TAB) the device table outs (separate matrices);
+// the kernel picks the variant once, outside its wave number loops
+template <typename Out, bool TAB>
 struct BatchCursor {
-    Out *p;
+    Out *p = nullptr;
+    void *const *tab = nullptr;
     int64_t step, off;
-    void *const *tab;
     __device__ __forceinline__ BatchCursor(const RegularArgs &a, bool dlp, int f, int64_t off_)
-        : step(a.mat_stride), off(off_), tab(a.outs ? a.outs + (dlp ? a.nk : 0) + f : nullptr)
+        : step(a.mat_stride), off(off_)
     {
-        Out *base = reinterpret_cast<Out *>(dlp ? a.out_d : a.out_s);
-        p = (tab || !base) ? nullptr : base + (int64_t)f * a.mat_stride + off;
+        if constexpr (TAB) {
+            tab = a.outs + (dlp ? a.nk : 0) + f;
+        } else {
+            Out *base = reinterpret_cast<Out *>(dlp ? a.out_d : a.out_s);
+            p = base ? base + (int64_t)f * a.mat_stride + off : nullptr;
+        }
     }
-    __device__ __forceinline__ Out *get() const { return tab ? reinterpret_cast<Out *>(*tab) + off : p; }
+    __device__ __forceinline__ Out *get() const
+    {
+        if constexpr (TAB) return reinterpret_cast<Out *>(*tab) + off;
+        else return p;
+    }
     __device__ __forceinline__ void next()
     {
-        if (tab) ++tab;
+        if constexpr (TAB) ++tab;
         else p += step;
     }
 };
@@ -162,7 +180,7 @@ __global__ void __launch_bounds__(REG_THREADS) k_regular(RegularArgs a)
     // RHS: Neumann data [f - f_lo][c], then the row sums [f - f_lo][threadIdx.x]
     extern __shared__ __align__(16) unsigned char s_rhs[];
     R2 *s_q = reinterpret_cast<R2 *>(s_rhs);
-    R2 *s_acc = s_q + rhs_f_max<R>() * REG_COLS;
+    R2 *s_acc = s_q + rhs_fmax_of<R>(a) * REG_COLS;
     constexpr bool DO_S = (OPS & OP_SLP) != 0;
     constexpr bool DO_D = (OPS & OP_DLP) != 0;
     const DevMesh &test = a.test;
@@ -180,7 +198,7 @@ __global__ void __launch_bounds__(REG_THREADS) k_regular(RegularArgs a)
         s_p0[threadIdx.x] = trial.p0[jb + threadIdx.x];
     }
     if constexpr (RHS) {
-        const int nf = f_hi - f_lo;  // at most rhs_f_max (launch_assemble_regular)
+        const int nf = f_hi - f_lo;  // at most rhs_fmax_of (launch_assemble_regular)
         for (int t = threadIdx.x; t < nf * REG_COLS; t += REG_THREADS) {
             const int fl = t / REG_COLS, c = t - fl * REG_COLS;
             R2 v;
@@ -257,26 +275,31 @@ __global__ void __launch_bounds__(REG_THREADS) k_regular(RegularArgs a)
                 if constexpr (BATCH) {
                     const int64_t off = (int64_t)(j - a.j0) * a.ld + i;
                     const PointGeom<float> gm = point_geom<float>(fx, fy, fz, p.x, p.y, p.z, p.w, R(DO_S), R(DO_D));
-                    BatchCursor<Out> cs(a, false, f_lo, off), cd(a, true, f_lo, off);
-                    R2 *acc = s_acc + threadIdx.x;
-                    const R2 *qc = s_q + c;
-                    const float *kp = a.ks32 + f_lo;
-                    for (int f = f_lo; f < f_hi; ++f) {
-                        R sr = 0, si = 0, dr = 0, di = 0;
-                        point_freq<FAM, float>(gm, *kp++, sr, si, dr, di);
-                        if (row_ok) {
-                            if constexpr (RHS) rhs_add(*acc, *qc, sr, si);
-                            else if (DO_S) store_plain(cs.get(), sr, si);
-                            if (DO_D) store_plain(cd.get(), dr, di);
+                    auto freqs = [&](auto tab) {
+                        constexpr bool TAB = decltype(tab)::value;
+                        BatchCursor<Out, TAB> cs(a, false, f_lo, off), cd(a, true, f_lo, off);
+                        R2 *acc = s_acc + threadIdx.x;
+                        const R2 *qc = s_q + c;
+                        const float *kp = a.ks32 + f_lo;
+                        for (int f = f_lo; f < f_hi; ++f) {
+                            R sr = 0, si = 0, dr = 0, di = 0;
+                            point_freq<FAM, float>(gm, *kp++, sr, si, dr, di);
+                            if (row_ok) {
+                                if constexpr (RHS) rhs_add(*acc, *qc, sr, si);
+                                else if (DO_S) store_plain(cs.get(), sr, si);
+                                if (DO_D) store_plain(cd.get(), dr, di);
+                            }
+                            if constexpr (RHS) {
+                                acc += REG_THREADS;
+                                qc += REG_COLS;
+                            } else if (DO_S) {
+                                cs.next();
+                            }
+                            if (DO_D) cd.next();
                         }
-                        if constexpr (RHS) {
-                            acc += REG_THREADS;
-                            qc += REG_COLS;
-                        } else if (DO_S) {
-                            cs.next();
-                        }
-                        if (DO_D) cd.next();
-                    }
+                    };
+                    if (a.outs) freqs(std::true_type{});
+                    else freqs(std::false_type{});
                 } else {
                     R sr = 0, si = 0, dr = 0, di = 0;
                     eval_point<FAM, float>(fx, fy, fz, p.x, p.y, p.z, p.w, k, R(DO_S), R(DO_D), sr, si, dr, di);
@@ -305,54 +328,59 @@ __global__ void __launch_bounds__(REG_THREADS) k_regular(RegularArgs a)
         if constexpr (BATCH) {
             // frequency batch: each point's geometry once per tile of wave numbers
             const int64_t off = (int64_t)(j - a.j0) * a.ld + i;
-            BatchCursor<Out> cs(a, false, f_lo, off), cd(a, true, f_lo, off);
-            R2 *acc = s_acc + threadIdx.x;
-            const R2 *qc = s_q + c;
-            for (int f0 = f_lo; f0 < f_hi; f0 += FREQ_TILE) {
-                R kf[FREQ_TILE], sr[FREQ_TILE], si[FREQ_TILE], dr[FREQ_TILE], di[FREQ_TILE];
+            auto tiles = [&](auto tab) {
+                constexpr bool TAB = decltype(tab)::value;
+                BatchCursor<Out, TAB> cs(a, false, f_lo, off), cd(a, true, f_lo, off);
+                R2 *acc = s_acc + threadIdx.x;
+                const R2 *qc = s_q + c;
+                for (int f0 = f_lo; f0 < f_hi; f0 += FREQ_TILE) {
+                    R kf[FREQ_TILE], sr[FREQ_TILE], si[FREQ_TILE], dr[FREQ_TILE], di[FREQ_TILE];
 #pragma unroll
-                for (int u = 0; u < FREQ_TILE; ++u) {
-                    if constexpr (sizeof(R) == 4) kf[u] = f0 + u < f_hi ? a.ks32[f0 + u] : 0.0f;
-                    else kf[u] = f0 + u < f_hi ? a.ks[f0 + u] : 0.0;
-                    sr[u] = si[u] = dr[u] = di[u] = 0;
-                }
-                for (int q = 0; q < n_eval; ++q) {
-                    int slot;
-                    R ws, wd;
-                    if (ls == ld) { slot = level_slot0(ls) + q; ws = R(DO_S); wd = R(DO_D); }
-                    else if (q < nps) { slot = level_slot0(ls) + q; ws = R(1); wd = R(0); }
-                    else { slot = level_slot0(ld) + q - nps; ws = R(0); wd = R(1); }
-                    PointGeom<R> gm;
-                    if constexpr (sizeof(R) == 4) {
-                        const float4 y = __ldg(trial.pts32 + 2 * (base + slot));
-                        const float4 n = __ldg(trial.pts32 + 2 * (base + slot) + 1);
-                        const bool centre = slot == 0;
-                        gm = point_geom<float>(centre ? dx : y.x - x0, centre ? dy : y.y - x1,
-                                               centre ? dz : y.z - x2, y.w, n.x, n.y, n.z, ws, wd);
-                    } else {
-                        const double *y = trial.pts64 + 8 * (base + slot);
-                        gm = point_geom<double>(y[0] - x0, y[1] - x1, y[2] - x2, y[3], y[4], y[5], y[6], ws, wd);
+                    for (int u = 0; u < FREQ_TILE; ++u) {
+                        if constexpr (sizeof(R) == 4) kf[u] = f0 + u < f_hi ? a.ks32[f0 + u] : 0.0f;
+                        else kf[u] = f0 + u < f_hi ? a.ks[f0 + u] : 0.0;
+                        sr[u] = si[u] = dr[u] = di[u] = 0;
+                    }
+                    for (int q = 0; q < n_eval; ++q) {
+                        int slot;
+                        R ws, wd;
+                        if (ls == ld) { slot = level_slot0(ls) + q; ws = R(DO_S); wd = R(DO_D); }
+                        else if (q < nps) { slot = level_slot0(ls) + q; ws = R(1); wd = R(0); }
+                        else { slot = level_slot0(ld) + q - nps; ws = R(0); wd = R(1); }
+                        PointGeom<R> gm;
+                        if constexpr (sizeof(R) == 4) {
+                            const float4 y = __ldg(trial.pts32 + 2 * (base + slot));
+                            const float4 n = __ldg(trial.pts32 + 2 * (base + slot) + 1);
+                            const bool centre = slot == 0;
+                            gm = point_geom<float>(centre ? dx : y.x - x0, centre ? dy : y.y - x1,
+                                                   centre ? dz : y.z - x2, y.w, n.x, n.y, n.z, ws, wd);
+                        } else {
+                            const double *y = trial.pts64 + 8 * (base + slot);
+                            gm = point_geom<double>(y[0] - x0, y[1] - x1, y[2] - x2, y[3], y[4], y[5], y[6], ws, wd);
+                        }
+#pragma unroll
+                        for (int u = 0; u < FREQ_TILE; ++u) point_freq<FAM, R>(gm, kf[u], sr[u], si[u], dr[u], di[u]);
                     }
 #pragma unroll
-                    for (int u = 0; u < FREQ_TILE; ++u) point_freq<FAM, R>(gm, kf[u], sr[u], si[u], dr[u], di[u]);
-                }
-#pragma unroll
-                for (int u = 0; u < FREQ_TILE; ++u) {
-                    if (f0 + u >= f_hi) break;
-                    if constexpr (RHS) {
-                        rhs_add(*acc, *qc, sr[u], si[u]);
-                        acc += REG_THREADS;
-                        qc += REG_COLS;
-                    } else if (DO_S) {
-                        store_plain(cs.get(), sr[u], si[u]);
-                        cs.next();
-                    }
-                    if (DO_D) {
-                        store_plain(cd.get(), dr[u], di[u]);
-                        cd.next();
+                    for (int u = 0; u < FREQ_TILE; ++u) {
+                        if (f0 + u >= f_hi) break;
+                        if constexpr (RHS) {
+                            rhs_add(*acc, *qc, sr[u], si[u]);
+                            acc += REG_THREADS;
+                            qc += REG_COLS;
+                        } else if (DO_S) {
+                            store_plain(cs.get(), sr[u], si[u]);
+                            cs.next();
+                        }
+                        if (DO_D) {
+                            store_plain(cd.get(), dr[u], di[u]);
+                            cd.next();
+                        }
                     }
                 }
-            }
+            };
+            if (a.outs) tiles(std::true_type{});
+            else tiles(std::false_type{});
         } else {
             R sr = 0, si = 0, dr = 0, di = 0;
             for (int q = 0; q < n_eval; ++q) {
@@ -438,7 +466,7 @@ static void launch_ops(const RegularArgs &a, dim3 grid, cudaStream_t s)
 {
     if constexpr (BATCH) {
         if (a.rhs_part) {
-            const size_t smem = sizeof(Cplx<R>) * rhs_f_max<R>() * (REG_COLS + REG_THREADS);
+            const size_t smem = sizeof(Cplx<R>) * rhs_fmax_of<R>(a) * (REG_COLS + REG_THREADS);
             k_regular<R, Out, FAM, OP_SLP | OP_DLP, true, true><<<grid, REG_THREADS, smem, s>>>(a);
             return;
         }
@@ -487,7 +515,7 @@ cudaError_t launch_assemble_regular(const RegularArgs &a, cudaStream_t s)
         grid.z = (unsigned)std::max<int64_t>(1, std::min<int64_t>(want, most));
         // right-hand-side mode: at most rhs_f_max wave numbers per block
         if (a.rhs_part) {
-            const int fmax = a.precision == 0 ? rhs_f_max<float>() : rhs_f_max<double>();
+            const int fmax = a.precision == 0 ? rhs_fmax_of<float>(a) : rhs_fmax_of<double>(a);
             grid.z = std::max<unsigned>(grid.z, (unsigned)((a.nk + fmax - 1) / fmax));
         }
     }

@@ -2096,7 +2096,8 @@ struct PersistentPlan {
 // in proportion when more CTAs stream at once than HBM feeds (about 60 GB/s
 // per 512-thread CTA).  The matvec input moves from shared memory to a
 // global buffer when a cluster size's shared memory cannot hold it.
-nihu_gb_status plan_persistent(nihu_gb_ctx *ctx, const std::vector<int64_t> &ns, int m, PersistentPlan *out)
+nihu_gb_status plan_persistent(nihu_gb_ctx *ctx, const std::vector<int64_t> &ns, int m, PersistentPlan *out,
+                               int force_cluster = 0)
 {
     int smem_optin = 0, mem_khz = 0, bus_bits = 0;
     cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, ctx->device);
@@ -2112,6 +2113,7 @@ nihu_gb_status plan_persistent(nihu_gb_ctx *ctx, const std::vector<int64_t> &ns,
     PersistentPlan best;
     double best_t = 0.0;
     for (int c : {2, 4, 8, 16, 1}) {
+        if (force_cluster && c != force_cluster) continue;
         int vs = 1;
         if (persistent_smem_layout((int)n_max, c, m, 1).total > (size_t)smem_optin) vs = 0;
         if (persistent_smem_layout((int)n_max, c, m, vs).total > (size_t)smem_optin) continue;
@@ -2165,7 +2167,7 @@ struct PersistentLaunch {
 // SMs and started beside the first as its programmatic dependent
 // (launch_persistent_gmres).
 nihu_gb_status plan_launches(nihu_gb_ctx *ctx, const std::vector<int64_t> &ns, const std::vector<double> &key, int m,
-                             std::vector<PersistentLaunch> *out)
+                             std::vector<PersistentLaunch> *out, int force_cluster = 0)
 {
     nihu_gb_status st;
     out->clear();
@@ -2183,7 +2185,7 @@ nihu_gb_status plan_launches(nihu_gb_ctx *ctx, const std::vector<int64_t> &ns, c
         std::vector<int64_t> nsa;
         for (int q : big) nsa.push_back(ns[q]);
         for (int q : small) B.n_max = std::max(B.n_max, ns[q]);
-        if ((st = plan_persistent(ctx, nsa, m, &A.plan))) return st;
+        if ((st = plan_persistent(ctx, nsa, m, &A.plan, force_cluster))) return st;
         int sms = 0, smem_optin = 0;
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device);
         cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, ctx->device);
@@ -2213,7 +2215,7 @@ nihu_gb_status plan_launches(nihu_gb_ctx *ctx, const std::vector<int64_t> &ns, c
         }
     }
     PersistentLaunch one;
-    if ((st = plan_persistent(ctx, ns, m, &one.plan))) return st;
+    if ((st = plan_persistent(ctx, ns, m, &one.plan, force_cluster))) return st;
     std::vector<int> all(count);
     for (int q = 0; q < count; ++q) all[q] = q;
     one.order = sorted(all);
@@ -2846,6 +2848,14 @@ struct nihu_gb_sweep_plan {
     std::vector<std::vector<int>> launch_items;
     std::vector<int> order_off;
     int *h_order = nullptr, *d_order = nullptr;
+    // the systems of the persistent launches (positions), their device copy,
+    // and the launch set-up the autotuner chose at creation
+    std::vector<PersistentItem> items;
+    std::vector<int64_t> ns;
+    PersistentItem *d_items = nullptr;
+    int rhs_fmax = 0;        // wave numbers per regular block (right-hand-side mode)
+    int tuned_cluster = 0;   // CTAs per cluster of the (first) persistent launch
+    double tuned_ms = 0.0;   // the chosen set-up's replay time on the representative inputs
     int *h_flag = nullptr;
     std::vector<PersistentArgs> pargs;  // one or two persistent launches (plan_launches)
     std::vector<PersistentPlan> pplans;
@@ -2958,6 +2968,7 @@ nihu_gb_status plan_capture(nihu_gb_sweep_plan *pl)
             a.rhs_q = pl->d_q + o;
             a.rhs_part = g.rpart;
             a.near_slp = g.nslp;
+            a.rhs_fmax = pl->rhs_fmax;
             st = assemble_panel(ctx, a, g.nl);
             if (st) break;
             chk(launch_add_identity_batched((int)g.n, -0.5, 0.0, NIHU_GB_C64, g.H, g.n, g.n * g.n, cnt, gs));
@@ -2989,6 +3000,152 @@ nihu_gb_status plan_capture(nihu_gb_sweep_plan *pl)
     if (e != cudaSuccess) return cuda_fail(ctx, e, "sweep plan capture");
     CK(cudaGraphInstantiate(&pl->exec, pl->graph, 0));
     return NIHU_GB_OK;
+}
+
+}  // namespace
+
+namespace {
+
+// each persistent launch's systems in processing order for the wave numbers
+// in h_ks: larger n^2 (1 + |k|) first (iteration counts grow with k)
+void plan_set_order(nihu_gb_sweep_plan *pl)
+{
+    for (size_t t = 0; t < pl->launch_items.size(); ++t) {
+        std::vector<int> ord = pl->launch_items[t];
+        std::vector<double> key(pl->nk, 0.0);
+        for (int q_ : ord) key[q_] = (double)pl->pos_n[q_] * pl->pos_n[q_] * (1.0 + std::fabs(pl->h_ks[q_]));
+        std::stable_sort(ord.begin(), ord.end(), [&](int x, int y) { return key[x] > key[y]; });
+        std::copy(ord.begin(), ord.end(), pl->h_order + pl->order_off[t]);
+    }
+}
+
+// the persistent launches over the plan's systems (force_cluster: the CTAs
+// per cluster of the first launch, 0 = the launch model's choice); the
+// systems' device copy, counters and matvec-input buffers follow
+nihu_gb_status plan_setup_launches(nihu_gb_sweep_plan *pl, int force_cluster)
+{
+    nihu_gb_ctx *ctx = pl->ctx;
+    nihu_gb_status st;
+    pl->launch_items.clear();
+    pl->order_off.clear();
+    pl->pargs.clear();
+    pl->pplans.clear();
+    std::vector<PersistentLaunch> launches;
+    if ((st = plan_launches(ctx, pl->ns, std::vector<double>(pl->ns.begin(), pl->ns.end()), pl->restart, &launches,
+                            force_cluster)))
+        return st;
+    int l2 = 0;
+    cudaDeviceGetAttribute(&l2, cudaDevAttrL2CacheSize, ctx->device);
+    std::vector<PersistentItem> items = pl->items;
+    for (const PersistentLaunch &L : launches)
+        for (int q : L.order) {
+            PersistentItem &it = items[q];
+            it.vec = (it.n % 2 == 0) && (it.lda % 2 == 0) && ((reinterpret_cast<uintptr_t>(it.A) & 15) == 0);
+            it.stream = 8.0 * (double)it.n * (double)it.n * std::min<int>((int)L.order.size(), L.plan.clusters) >
+                        0.5 * l2;
+        }
+    CK(cudaMemcpy(pl->d_items, items.data(), sizeof(PersistentItem) * (size_t)pl->nk, cudaMemcpyHostToDevice));
+    for (size_t t = 0, o = 0; t < launches.size(); ++t) {
+        const PersistentLaunch &L = launches[t];
+        const int cnt = (int)L.order.size();
+        pl->launch_items.push_back(L.order);
+        pl->order_off.push_back((int)o);
+        void *dcnt, *dvx = nullptr;
+        if ((st = plan_alloc(pl, sizeof(int), &dcnt))) return st;
+        if (!L.plan.vx_smem && (st = plan_alloc(pl, 8 * (size_t)L.plan.clusters * L.n_max, &dvx))) return st;
+        PersistentArgs a{};
+        a.items = pl->d_items;
+        a.order = pl->d_order + o;
+        o += cnt;
+        a.count = cnt;
+        a.n_max = (int)L.n_max;
+        a.restart = pl->restart;
+        a.max_iters = pl->max_iters;
+        a.quantum = 0;
+        a.tol = pl->tol;
+        a.counter = (int *)dcnt;
+        a.vxg = (float2 *)dvx;
+        a.wait_primary = t > 0;
+        pl->pargs.push_back(a);
+        pl->pplans.push_back(L.plan);
+    }
+    return NIHU_GB_OK;
+}
+
+void plan_drop_graph(nihu_gb_sweep_plan *pl)
+{
+    if (pl->exec) cudaGraphExecDestroy(pl->exec);
+    if (pl->graph) cudaGraphDestroy(pl->graph);
+    pl->exec = nullptr;
+    pl->graph = nullptr;
+}
+
+// The autotuner: the plan's launch set-up is measured, not modelled.  Each
+// candidate -- the persistent launch's CTAs per cluster (the launch model's
+// choice, 4, 8, 16) times the wave numbers per regular block (8, 16, 20) -- is
+// captured and replayed on representative inputs (wave numbers spread over
+// (0.1, 1] k_max, unit Neumann data); the fastest replay's set-up is kept
+// and captured for good.
+nihu_gb_status plan_autotune(nihu_gb_sweep_plan *pl)
+{
+    nihu_gb_ctx *ctx = pl->ctx;
+    nihu_gb_status st;
+    for (int f = 0; f < pl->nk; ++f) {
+        const int q_ = pl->order_of[f];
+        pl->h_ks[q_] = pl->kmax * (0.1 + 0.9 * (f + 0.5) / pl->nk);
+        pl->h_ks32[q_] = (float)pl->h_ks[q_];
+    }
+    for (int64_t i = 0; i < pl->total; ++i) pl->h_q[i] = make_double2(1.0, 0.0);
+    cudaEvent_t t0, t1;
+    CK(cudaEventCreate(&t0));
+    CK(cudaEventCreate(&t1));
+    double best_ms = -1.0;
+    int best_c = 0, best_f = 0;
+    std::vector<int> seen;
+    for (int c : {0, 4, 8, 16}) {
+        if (plan_setup_launches(pl, c) != NIHU_GB_OK) {
+            cudaGetLastError();
+            continue;
+        }
+        const int shape = pl->pplans[0].cluster;
+        if (std::find(seen.begin(), seen.end(), shape) != seen.end()) continue;
+        seen.push_back(shape);
+        for (int fm : {8, 16, 20}) {
+            pl->rhs_fmax = fm;
+            plan_drop_graph(pl);
+            if (plan_capture(pl) != NIHU_GB_OK) {
+                cudaGetLastError();
+                continue;
+            }
+            plan_set_order(pl);
+            float ms = 0.0f;
+            cudaError_t e = cudaGraphLaunch(pl->exec, ctx->stream);  // warm-up
+            if (e == cudaSuccess) e = cudaEventRecord(t0, ctx->stream);
+            if (e == cudaSuccess) e = cudaGraphLaunch(pl->exec, ctx->stream);
+            if (e == cudaSuccess) e = cudaEventRecord(t1, ctx->stream);
+            if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+            if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, t0, t1);
+            if (e != cudaSuccess) {
+                cudaEventDestroy(t0);
+                cudaEventDestroy(t1);
+                return cuda_fail(ctx, e, "sweep plan autotuning");
+            }
+            if (best_ms < 0.0 || ms < best_ms) {
+                best_ms = ms;
+                best_c = c;
+                best_f = fm;
+            }
+        }
+    }
+    cudaEventDestroy(t0);
+    cudaEventDestroy(t1);
+    plan_drop_graph(pl);
+    if (best_ms < 0.0) return fail(ctx, NIHU_GB_ERR_RUNTIME, "sweep plan: no launch set-up could be captured");
+    if ((st = plan_setup_launches(pl, best_c))) return st;
+    pl->rhs_fmax = best_f;
+    pl->tuned_cluster = pl->pplans[0].cluster;
+    pl->tuned_ms = best_ms;
+    return plan_capture(pl);
 }
 
 }  // namespace
@@ -3078,7 +3235,7 @@ extern "C" nihu_gb_status nihu_gb_sweep_plan_create(nihu_gb_ctx *ctx, int n_mesh
         CK(cudaMemcpy(pl->d_dst, pl->off.data(), sizeof(int64_t) * nk, cudaMemcpyHostToDevice));
         CK(cudaMemcpy(pl->d_len, len.data(), sizeof(int) * nk, cudaMemcpyHostToDevice));
     }
-    void *dV, *dS, *dst, *ditems, *dorder, *dcnt, *dvx = nullptr;
+    void *dV, *dS, *dst, *ditems, *dorder;
     if ((st = plan_alloc(pl.get(), 16 * (size_t)pl->total * (m + 1), &dV))) return st;
     if ((st = plan_alloc(pl.get(), 16 * ss * nk, &dS))) return st;
     if ((st = plan_alloc(pl.get(), sizeof(PersistentState) * (size_t)nk, &dst))) return st;
@@ -3098,17 +3255,15 @@ extern "C" nihu_gb_status nihu_gb_sweep_plan_create(nihu_gb_ctx *ctx, int n_mesh
         if ((st = plan_alloc(pl.get(), 16 * (size_t)(g.nl->nnz + g.n) * cnt, &p))) return st;
         g.nslp = (double2 *)p;
     }
-    // the persistent launch: items, order and launch shape fixed by the plan
-    std::vector<PersistentItem> items(nk);
-    std::vector<int64_t> ns(nk);
-    int l2 = 0;
-    cudaDeviceGetAttribute(&l2, cudaDevAttrL2CacheSize, ctx->device);
+    // the persistent launches' systems (launch shape: plan_setup_launches)
+    pl->items.assign(nk, PersistentItem{});
+    pl->ns.assign(nk, 0);
     pl->pos_n.assign(nk, 0);
     for (auto &g : pl->groups)
         for (size_t j = 0; j < g.fs.size(); ++j) {
             const int f = g.fs[j], q = pl->order_of[f];
             pl->pos_n[q] = g.n;
-            PersistentItem &it = items[q];
+            PersistentItem &it = pl->items[q];
             it.A = (const float2 *)g.H + (size_t)g.n * g.n * j;
             it.lda = g.n;
             it.b = pl->d_b + pl->off[f];
@@ -3118,47 +3273,13 @@ extern "C" nihu_gb_status nihu_gb_sweep_plan_create(nihu_gb_ctx *ctx, int n_mesh
             it.st = pl->d_st + q;
             it.n = (int)g.n;
             it.pad = 0;
-            ns[q] = g.n;
-        }
-    std::vector<PersistentLaunch> launches;
-    if ((st = plan_launches(ctx, ns, std::vector<double>(ns.begin(), ns.end()), m, &launches))) return st;
-    for (const PersistentLaunch &L : launches)
-        for (int q : L.order) {
-            PersistentItem &it = items[q];
-            it.vec = (it.n % 2 == 0) && (it.lda % 2 == 0) && ((reinterpret_cast<uintptr_t>(it.A) & 15) == 0);
-            it.stream = 8.0 * (double)it.n * (double)it.n * std::min<int>((int)L.order.size(), L.plan.clusters) >
-                        0.5 * l2;
+            pl->ns[q] = g.n;
         }
     if ((st = plan_alloc(pl.get(), sizeof(PersistentItem) * (size_t)nk, &ditems))) return st;
-    CK(cudaMemcpy(ditems, items.data(), sizeof(PersistentItem) * nk, cudaMemcpyHostToDevice));
+    pl->d_items = (PersistentItem *)ditems;
     if ((st = plan_alloc(pl.get(), sizeof(int) * (size_t)nk, &dorder))) return st;
     pl->d_order = (int *)dorder;
     CK(cudaMallocHost((void **)&pl->h_order, sizeof(int) * (size_t)nk));
-    for (size_t t = 0, o = 0; t < launches.size(); ++t) {
-        const PersistentLaunch &L = launches[t];
-        const int cnt = (int)L.order.size();
-        pl->launch_items.push_back(L.order);
-        pl->order_off.push_back((int)o);
-        std::copy(L.order.begin(), L.order.end(), pl->h_order + o);
-        if ((st = plan_alloc(pl.get(), sizeof(int), &dcnt))) return st;
-        dvx = nullptr;
-        if (!L.plan.vx_smem && (st = plan_alloc(pl.get(), 8 * (size_t)L.plan.clusters * L.n_max, &dvx))) return st;
-        PersistentArgs a{};
-        a.items = (const PersistentItem *)ditems;
-        a.order = pl->d_order + o;
-        o += cnt;
-        a.count = cnt;
-        a.n_max = (int)L.n_max;
-        a.restart = m;
-        a.max_iters = max_iters;
-        a.quantum = 0;
-        a.tol = tol;
-        a.counter = (int *)dcnt;
-        a.vxg = (float2 *)dvx;
-        a.wait_primary = t > 0;
-        pl->pargs.push_back(a);
-        pl->pplans.push_back(L.plan);
-    }
     // pinned staging
     CK(cudaMallocHost((void **)&pl->h_ks, 8 * (size_t)nk));
     CK(cudaMallocHost((void **)&pl->h_ks32, 4 * (size_t)nk));
@@ -3176,7 +3297,7 @@ extern "C" nihu_gb_status nihu_gb_sweep_plan_create(nihu_gb_ctx *ctx, int n_mesh
     }
     CK(prepare_singular_batch(ctx->stream));
     if ((st = sync(ctx))) return st;
-    if ((st = plan_capture(pl.get()))) return st;
+    if ((st = plan_autotune(pl.get()))) return st;
     *out = pl.release();
     return NIHU_GB_OK;
 }
@@ -3196,14 +3317,7 @@ extern "C" nihu_gb_status nihu_gb_sweep_plan_run(nihu_gb_sweep_plan *pl, const d
         pl->h_ks[q_] = ks[f];
         pl->h_ks32[q_] = (float)ks[f];
     }
-    // each launch's systems, larger n^2 (1 + |k|) first (iteration counts grow with k)
-    for (size_t t = 0; t < pl->launch_items.size(); ++t) {
-        std::vector<int> ord = pl->launch_items[t];
-        std::vector<double> key(pl->nk, 0.0);
-        for (int q_ : ord) key[q_] = (double)pl->pos_n[q_] * pl->pos_n[q_] * (1.0 + std::fabs(pl->h_ks[q_]));
-        std::stable_sort(ord.begin(), ord.end(), [&](int x, int y) { return key[x] > key[y]; });
-        std::copy(ord.begin(), ord.end(), pl->h_order + pl->order_off[t]);
-    }
+    plan_set_order(pl);
     if (q != pl->h_q) std::memcpy(pl->h_q, q, 16 * (size_t)pl->total);
     {
         Phase ph(ctx, "sweep_graph");
@@ -3233,6 +3347,16 @@ extern "C" nihu_gb_status nihu_gb_sweep_plan_host_buffers(nihu_gb_sweep_plan *pl
     if (!pl || !q || !p) return NIHU_GB_ERR_INVALID_ARGUMENT;
     *q = pl->h_q;
     *p = pl->h_p;
+    return NIHU_GB_OK;
+}
+
+extern "C" nihu_gb_status nihu_gb_sweep_plan_tuning(const nihu_gb_sweep_plan *pl, int *cluster, int *freq_per_block,
+                                                    double *replay_ms)
+{
+    if (!pl) return NIHU_GB_ERR_INVALID_ARGUMENT;
+    if (cluster) *cluster = pl->tuned_cluster;
+    if (freq_per_block) *freq_per_block = pl->rhs_fmax;
+    if (replay_ms) *replay_ms = pl->tuned_ms;
     return NIHU_GB_OK;
 }
 

@@ -82,6 +82,9 @@ struct RegularArgs {
     const double2 *rhs_q = nullptr;
     void *rhs_part = nullptr;
     double2 *near_slp = nullptr;
+    // right-hand-side mode: wave numbers per block of the regular kernel
+    // (0: the default; at most 20 in FP32 mode, 10 in FP64 mode)
+    int rhs_fmax = 0;
 };
 
 // matrix f of a frequency batch (dlp: the DLP output)

@@ -166,4 +166,7 @@ def test_sweep_plan_in_place_staging(gpu_ctx):
     # the Python front end's own copies are not views of the staging
     P2, _, _, _ = plan.run(ks * 0.5, q, check=False)
     assert not np.array_equal(np.concatenate(P_ref), np.concatenate(P2))
+    # copy=False: views of the staging, the same values
+    P3, _, _, _ = plan.run(ks, q, check=False, copy=False)
+    assert np.shares_memory(P3[0], pbuf) and np.array_equal(np.concatenate(P3), np.concatenate(P_ref))
     plan.close()
