@@ -106,6 +106,10 @@ def test_sweep_plan_graph_matches_eager_sweep(gpu_ctx):
     nk = 10
     mesh_of = np.arange(nk) % 3
     plan = g.SweepPlan(ms, mesh_of, k_max=6.0, tol=1e-7, ctx=gpu_ctx)
+    # the autotuner kept one of its candidates (the launch model's choice or 4, 8, 16 CTAs per cluster)
+    tuning = plan.tuning()
+    assert tuning["cluster"] in (1, 2, 4, 8, 16) and tuning["freq_per_block"] in (8, 16, 20)
+    assert tuning["replay_ms"] > 0.0
     for rep in range(2):
         ks = rng.uniform(0.2, 6.0, nk)
         q = [rng.standard_normal(ms[i].num_elements) + 1j * rng.standard_normal(ms[i].num_elements) for i in mesh_of]
