@@ -304,7 +304,8 @@ __device__ __forceinline__ int common_nodes(int4 a, int na, int4 b, int nb, int 
     return num;
 }
 
-template <typename R, typename Out, int FAM, int OPS>
+// PLAIN: unit scale and no accumulation (FP32): stores without run-time checks
+template <typename R, typename Out, int FAM, int OPS, bool PLAIN = false>
 __global__ void __launch_bounds__(GAL_THREADS) k_galerkin_regular(GalArgs a)
 {
     __shared__ float4 s_hi[GAL_COLS], s_lo[GAL_COLS], s_p0[GAL_COLS];
@@ -351,7 +352,11 @@ __global__ void __launch_bounds__(GAL_THREADS) k_galerkin_regular(GalArgs a)
     }
     Out *out_s = reinterpret_cast<Out *>(a.out_s);
     Out *out_d = reinterpret_cast<Out *>(a.out_d);
-    for (int c = 0; c < ncols; ++c) {
+    // this thread's entries of the current column, one column (ld entries) further per step
+    const int64_t ldo = a.ld;
+    Out *ps = DO_S ? out_s + (int64_t)(jb - a.j0) * ldo + i : nullptr;
+    Out *pd = DO_D ? out_d + (int64_t)(jb - a.j0) * ldo + i : nullptr;
+    for (int c = 0; c < ncols; ++c, ps += DO_S ? ldo : 0, pd += DO_D ? ldo : 0) {
         const int j = jb + c;
         int ind1, ind2;
         // elements can share a node only when their centres are closer than
@@ -435,22 +440,26 @@ __global__ void __launch_bounds__(GAL_THREADS) k_galerkin_regular(GalArgs a)
             }
         }
         if (!row_ok) continue;
-        const int64_t off = (int64_t)(j - a.j0) * a.ld + i;
         auto store = [&](Out *p, R re, R im) {
-            const R vr = are * re - aim * im, vi = are * im + aim * re;
             Out o;
-            if (a.accumulate) {
-                o = *p;
-                o.x += vr;
-                o.y += vi;
+            if constexpr (PLAIN) {
+                o.x = re;
+                o.y = im;
             } else {
-                o.x = vr;
-                o.y = vi;
+                const R vr = are * re - aim * im, vi = are * im + aim * re;
+                if (a.accumulate) {
+                    o = *p;
+                    o.x += vr;
+                    o.y += vi;
+                } else {
+                    o.x = vr;
+                    o.y = vi;
+                }
             }
             *p = o;
         };
-        if (DO_S) store(out_s + off, sr, si);
-        if (DO_D) store(out_d + off, dr, di);
+        if (DO_S) store(ps, sr, si);
+        if (DO_D) store(pd, dr, di);
     }
 }
 
@@ -826,6 +835,14 @@ __global__ void __launch_bounds__(GAL_WARPS * 32) k_galerkin_near(GalArgs a, Nea
 template <typename R, typename Out, int FAM>
 static void launch_gal_ops(const GalArgs &a, dim3 grid, cudaStream_t s)
 {
+    if constexpr (sizeof(R) == 4) {
+        if (a.alpha_re == 1.0 && a.alpha_im == 0.0 && !a.accumulate) {
+            if (a.ops == OP_SLP) k_galerkin_regular<R, Out, FAM, OP_SLP, true><<<grid, GAL_THREADS, 0, s>>>(a);
+            else if (a.ops == OP_DLP) k_galerkin_regular<R, Out, FAM, OP_DLP, true><<<grid, GAL_THREADS, 0, s>>>(a);
+            else k_galerkin_regular<R, Out, FAM, OP_SLP | OP_DLP, true><<<grid, GAL_THREADS, 0, s>>>(a);
+            return;
+        }
+    }
     if (a.ops == OP_SLP) k_galerkin_regular<R, Out, FAM, OP_SLP><<<grid, GAL_THREADS, 0, s>>>(a);
     else if (a.ops == OP_DLP) k_galerkin_regular<R, Out, FAM, OP_DLP><<<grid, GAL_THREADS, 0, s>>>(a);
     else k_galerkin_regular<R, Out, FAM, OP_SLP | OP_DLP><<<grid, GAL_THREADS, 0, s>>>(a);
