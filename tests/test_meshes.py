@@ -53,3 +53,36 @@ def test_cylinder_40k_count():
     nodes, elems = meshes.cylinder_40k()
     assert len(elems) == 40000
     assert np.all(elems[:, 0] == meshes.QUAD_1)
+
+
+def _write_off(path, nodes, elems):
+    """An OFF file as NiHu's reader takes it (nihu/interface/read_off_mesh.hpp):
+    header, counts (nodes, faces, edges), coordinates, faces `n i0 .. i(n-1)`."""
+    with open(path, "w") as f:
+        f.write("OFF\n%d %d 0\n" % (len(nodes), len(elems)))
+        for x in nodes:
+            f.write("%.17g %.17g %.17g\n" % tuple(x))
+        for e in elems:
+            idx = [int(v) for v in e[1:] if v >= 0]
+            f.write("%d %s\n" % (len(idx), " ".join(map(str, idx))))
+
+
+def test_read_off_round_trip(tmp_path):
+    from nihu_gb300 import meshes
+    for name, (nodes, elems) in {"tria": meshes.icosphere(2), "quad": meshes.cylinder(8, 3, 2)}.items():
+        p = tmp_path / (name + ".off")
+        _write_off(p, nodes, elems)
+        n2, e2 = meshes.read_off(p)
+        assert np.array_equal(n2, nodes)
+        assert np.array_equal(e2, elems)
+
+
+def test_read_off_errors(tmp_path):
+    from nihu_gb300 import meshes
+    p = tmp_path / "bad.off"
+    p.write_text("PLY\n3 1 0\n0 0 0\n1 0 0\n0 1 0\n3 0 1 2\n")
+    with pytest.raises(RuntimeError):
+        meshes.read_off(p)
+    p.write_text("OFF\n5 1 0\n" + "0 0 0\n" * 5 + "5 0 1 2 3 4\n")
+    with pytest.raises(RuntimeError):
+        meshes.read_off(p)
