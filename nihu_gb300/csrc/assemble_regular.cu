@@ -311,6 +311,40 @@ __global__ void __launch_bounds__(REG_THREADS) k_regular(RegularArgs a)
                 continue;
             }
         }
+        if constexpr (sizeof(R) == 4 && !BATCH && OPS == (OP_SLP | OP_DLP)) {
+            // every lane certainly has the 1-point SLP rule (d/D >= 9.1) and a
+            // certain DLP level, 0 (d/D >= 15.8) or 1 (below): the general
+            // path's points in its order -- the centroid, then for level 1 the
+            // DLP-only points -- without its per-lane dispatch.  "Certainly"
+            // is classify_pair's FP32 guard band, so the levels are its own.
+            const float4 jh = s_hi[c], jl = s_lo[c];
+            const float mx = (jh.x - ih.x) + (jl.x - il.x), my = (jh.y - ih.y) + (jl.y - il.y),
+                        mz = (jh.z - ih.z) + (jl.z - il.z);
+            const float mq = (mx * mx + my * my + mz * mz) * jh.w;
+            const float mlo = mq * (1.0f - 1e-5f), mhi = mq * (1.0f + 1e-5f);
+            const bool d_far = mlo >= 249.64f;
+            if (__all_sync(0xffffffffu, mlo >= 82.81f && (d_far || mhi < 249.64f))) {
+                if (row_ok) {
+                    const int64_t base = ((int64_t)j * 2 + par) * SLOTS;
+                    R sr = 0, si = 0, dr = 0, di = 0;
+                    const float4 yc = __ldg(trial.pts32 + 2 * base), nc = __ldg(trial.pts32 + 2 * base + 1);
+                    eval_point<FAM, float>(mx, my, mz, yc.w, nc.x, nc.y, nc.z, k, R(1), d_far ? R(1) : R(0), sr, si,
+                                           dr, di);
+                    if (!d_far) {
+                        const int npd = level_npts(s_nc[c], par, 1);
+                        for (int q = 0; q < npd; ++q) {
+                            const int64_t sl = base + level_slot0(1) + q;
+                            const float4 y = __ldg(trial.pts32 + 2 * sl), n = __ldg(trial.pts32 + 2 * sl + 1);
+                            eval_point<FAM, float>(y.x - x0, y.y - x1, y.z - x2, y.w, n.x, n.y, n.z, k, R(0), R(1), sr,
+                                                   si, dr, di);
+                        }
+                    }
+                    put(ps, sr, si);
+                    put(pd, dr, di);
+                }
+                continue;
+            }
+        }
         int ls, ld;
         float dx, dy, dz;
         int kind = classify_pair(ih, il, s_hi[c], s_lo[c], ii, j, test.center, trial.center, trial.size,
