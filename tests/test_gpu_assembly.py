@@ -4,7 +4,8 @@ Tolerances (written here, checked on every entry of the matrix):
   * FP64 regular mode: max |A_gpu - A_oracle| / max |A_oracle| <= 1e-11 (summation order only)
   * FP32 regular mode (the default): normwise entry error <= 1e-5, and for
     the SLP every entry within 1e-5 of its own magnitude; on a sphere of 5120
-    triangles every SLP and DLP entry within 5e-5 of its own magnitude
+    triangles and a cylinder of 4608 quads every SLP and DLP entry within
+    5e-5 of its own magnitude (coplanar DLP pairs: 1e-6 of the largest entry)
 Singular and nearly singular entries are FP64 in both modes.
 """
 import ctypes
@@ -139,6 +140,42 @@ def test_fp32_mode_every_entry_on_sphere(gpu_ctx, family, k):
         assert np.abs(ref).min() > 0.0
         err = np.abs(got - ref) / np.abs(ref)
         assert err.max() < 5e-5, (op, err.max(), np.unravel_index(err.argmax(), err.shape))
+
+
+def coplanar_pairs(mesh):
+    """Boolean (n, n): element j lies in the plane of element i (flat quads)."""
+    c = meshes.element_corners(*mesh)
+    nrm = np.cross(c[:, 2] - c[:, 0], c[:, 3] - c[:, 1])
+    nrm /= np.linalg.norm(nrm, axis=1)[:, None]
+    cen = c.mean(axis=1)
+    parallel = np.abs(nrm @ nrm.T) > 1.0 - 1e-9
+    offset = np.abs(cen @ nrm.T - np.einsum("ij,ij->i", cen, nrm)[None, :])
+    return parallel & (offset < 1e-9)
+
+
+@pytest.mark.parametrize("k", [5.0, 0.5])
+def test_fp32_mode_every_entry_on_quads(gpu_ctx, k):
+    """The same per-entry check on a closed cylinder of 4608 flat quads
+    (64 x 48 side grid, O-grid caps): the four-corner quadrature levels of
+    the FP32 kernel.  Every SLP entry, and every DLP entry of a pair that is
+    not coplanar, within 5e-5 of its own magnitude (measured: 3.5e-6 SLP,
+    1.2e-5 DLP).  A coplanar pair (a side column, a cap) has a DLP entry of
+    rounding size only (below 5e-13 of the largest in FP64); its FP32 value
+    within 1e-6 of the largest entry (measured: 4.4e-8)."""
+    mesh = meshes.cylinder(64, 48, 8, radius=1.0, length=3.0)
+    o32 = gpu_assemble(gpu_ctx, mesh, g.HELMHOLTZ_3D, g.SLP | g.DLP, k, g.REGULAR_FP32, g.C64)
+    o64 = gpu_assemble(gpu_ctx, mesh, g.HELMHOLTZ_3D, g.SLP | g.DLP, k, g.REGULAR_FP64, g.C128)
+    cop = coplanar_pairs(mesh)
+    assert cop.sum() > len(cop)
+    for op in (g.SLP, g.DLP):
+        ref, got = o64[op], o32[op]
+        big = np.abs(ref).max()
+        d = np.abs(got - ref)
+        rest = ~cop if op == g.DLP else np.ones_like(cop)
+        if op == g.DLP:
+            assert d[cop].max() < 1e-6 * big
+        err = d[rest] / np.abs(ref[rest])
+        assert err.max() < 5e-5, (op, err.max())
 
 
 @pytest.mark.parametrize("ops", [g.SLP, g.DLP])
