@@ -181,3 +181,23 @@ def test_invalid_arguments(gpu_ctx):
         st = L.nihu_gb_assemble_bm(gpu_ctx.handle, tri.handle, tri.handle, g.HELMHOLTZ_3D, ops, 1.0, 1.0, 0.0,
                                    g.REGULAR_FP64, g.C128, out.ctypes.data, out.ctypes.data, tri.n, 0, g.HOST)
         assert st == 1, ops
+
+
+@pytest.mark.parametrize("family,k", [(g.HELMHOLTZ_3D, 5.0), (g.LAPLACE_3D, 0.0)])
+def test_fp32_mode_every_entry_on_sphere(gpu_ctx, family, k):
+    """Every DLPt and HSP entry of the FP32 mode against the FP64 mode on an
+    icosphere of 5120 triangles, within 5e-5 of its own magnitude (measured:
+    9.7e-6 DLPt, 2.6e-6 HSP; the DLPt diagonal, zero on flat elements,
+    excluded): a pair integrated with too
+    few points by the regular kernel's warp-uniform paths fails here."""
+    mesh = meshes.icosphere(4)
+    o32 = gpu_bm(gpu_ctx, mesh, family, g.DLPT | g.HSP, k, g.REGULAR_FP32, g.C64)
+    o64 = gpu_bm(gpu_ctx, mesh, family, g.DLPT | g.HSP, k, g.REGULAR_FP64, g.C128)
+    for op in (g.DLPT, g.HSP):
+        ref, got = o64[op].copy(), o32[op].astype(np.complex128)
+        if op == g.DLPT:
+            assert np.abs(np.diagonal(got)).max() < 1e-6 * np.abs(ref).max()
+            np.fill_diagonal(ref, 1.0)
+            np.fill_diagonal(got, 1.0)
+        err = np.abs(got - ref) / np.abs(ref)
+        assert err.max() < 5e-5, (op, err.max())
