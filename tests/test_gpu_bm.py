@@ -188,8 +188,8 @@ def test_fp32_mode_every_entry_on_sphere(gpu_ctx, family, k):
     """Every DLPt and HSP entry of the FP32 mode against the FP64 mode on an
     icosphere of 5120 triangles, within 5e-5 of its own magnitude (measured:
     9.7e-6 DLPt, 2.6e-6 HSP; the DLPt diagonal, zero on flat elements,
-    excluded): a pair integrated with too
-    few points by the regular kernel's warp-uniform paths fails here."""
+    excluded): a pair integrated with too few points by the regular
+    kernel's warp-uniform paths fails here."""
     mesh = meshes.icosphere(4)
     o32 = gpu_bm(gpu_ctx, mesh, family, g.DLPT | g.HSP, k, g.REGULAR_FP32, g.C64)
     o64 = gpu_bm(gpu_ctx, mesh, family, g.DLPT | g.HSP, k, g.REGULAR_FP64, g.C128)
