@@ -42,7 +42,7 @@ METRIC = "BEM entries/s"
 UNIT = "entries/s"
 
 
-def parse():
+def parse(argv=None):
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
     p.add_argument("--steps", type=int, default=10)
@@ -52,16 +52,35 @@ def parse():
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-solve", action="store_true")
     p.add_argument("--no-cpu", action="store_true")
-    p.add_argument("--config", default="large", choices=["large", "small", "multirhs", "sweep", "serve", "bm", "p2p", "galerkin"],
-                   help="large: the headline line (20480-triangle icosphere); multirhs: the 40000-quad "
-                        "cylinder with 64 plane waves; sweep: 256 wave numbers on three icospheres; serve: "
-                        "the served stream; bm: the Burton-Miller system on the 20480-triangle icosphere; "
+    p.add_argument("--config", default="large",
+                   choices=["large", "small", "multirhs", "sweep", "serve", "bm", "p2p", "galerkin", "profile"],
+                   help="large: the headline line (20480-triangle icosphere), with short runs of the small, "
+                        "multirhs, sweep and serve configurations in its 'configs' object; multirhs: the "
+                        "40000-quad cylinder with 64 plane waves; sweep: 256 wave numbers on three icospheres; "
+                        "serve: the served stream; bm: the Burton-Miller system on the 20480-triangle icosphere; "
                         "p2p: the Burton-Miller near field of a box partition of the same mesh; "
-                        "galerkin: Galerkin SLP and DLP on the same mesh (each a separate line)")
+                        "galerkin: Galerkin SLP and DLP on the same mesh (each a separate line); "
+                        "profile: per-phase device times of one assembly or sweep (an ncu target, see --subdiv)")
+    p.add_argument("--no-configs", action="store_true", help="large: leave out the short runs of the other configs")
+    p.add_argument("--no-fp64-check", action="store_true",
+                   help="multirhs: leave out the per-right-hand-side error against the FP64 solution")
     p.add_argument("--requests", type=int, default=1000, help="serve: requests in the stream")
     p.add_argument("--quantum", type=int, default=8, help="serve: GMRES steps per system per round")
     p.add_argument("--plain-sample", type=int, default=4, help="serve: requests per mesh timed on the plain path")
-    return p.parse_args()
+    prof = p.add_argument_group("profile", "--config profile: the assembly of one mesh, or a sweep")
+    prof.add_argument("--subdiv", type=int, default=5, help="icosphere subdivisions (20 * 4^s triangles)")
+    prof.add_argument("--cylinder", type=int, default=0, metavar="N_THETA",
+                      help="closed quad cylinder with this many elements around instead (n_z = 1.25 n_theta)")
+    prof.add_argument("--k", type=float, default=5.0, help="wave number")
+    prof.add_argument("--laplace", action="store_true")
+    prof.add_argument("--budget-mb", type=int, default=0,
+                      help="HBM budget: host output in column panels, so that one launch covers one panel")
+    prof.add_argument("--reps", type=int, default=2)
+    prof.add_argument("--fp64", action="store_true", help="FP64 regular quadrature")
+    prof.add_argument("--bm", action="store_true", help="the Burton-Miller system instead of SLP and DLP")
+    prof.add_argument("--sweep", type=int, default=0, metavar="N", help="frequency sweep of N wave numbers")
+    prof.add_argument("--sweep-config4", action="store_true", help="the 256-instance sweep on three icospheres")
+    return p.parse_args(argv)
 
 
 def dist_env():
@@ -147,12 +166,17 @@ def run_reference(args):
         rows_tot += rows
         el_tot += el
     value = float(np.mean(vals))
-    ms_per_step = 1e3 * 2.0 * n * n / value
+    # a step is one bounded row sample of the workload (timed), not the whole
+    # 2 n^2 entries, which would take minutes per step on the host
+    ms_per_step = 1e3 * el_tot / max(1, args.steps)
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "fp64", "data": "synthetic (icosphere mesh generated in-process)", "impl": "reference",
         "config": workload_config(n),
+        "step": "one sample of %d full rows (both matrices); ms_per_step is its measured time; the whole "
+                "20480 x 20480 pair at this rate would take %.0f ms" % (rows_tot // max(1, args.steps),
+                                                                        1e3 * 2.0 * n * n / value),
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
                          "sample": "%d full rows x %d columns x (SLP, DLP) per step, FP64 restatement of NiHu's "
                                    "collocational assembly (the reference needs Eigen/Boost, absent)" % (rows_tot // max(1, args.steps), n)},
@@ -425,6 +449,8 @@ def run_ours(args):
         out["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
                                "sample": "%d full rows x %d columns x (SLP, DLP), FP64 oracle (restatement of NiHu's "
                                          "collocational assembly), %.1f s" % (rows, n, el)}
+    if not args.no_configs and rank == 0 and ws == 1:
+        out["configs"] = other_configs(args)
     if dist:
         dist.barrier()
         dist.destroy_process_group()
@@ -493,7 +519,8 @@ def run_small(args):
         e2e.append(time.perf_counter() - t0)
     pa = -1.0 / (1.0 + 1j * k)
     out = {"metric": "plain small solve (config 1)", "impl": "ours", "value": ms, "unit": "ms",
-           "higher_is_better": False, "n_elements": n, "k": k, "dtype": "complex128, FP64 assembly and LU",
+           "higher_is_better": False, "n_elements": n, "k": k,
+           "dtype": "complex128: FP64 assembly; FP32 LU with FP64 iterative refinement (FP64 LU fallback)",
            "data": "synthetic (icosphere generated in-process), pulsating sphere q = 1",
            "steps": args.steps, "ms_per_step": ms,
            "e2e": {"value": 1e3 * float(np.median(e2e)), "unit": "ms", "h2d_bytes_per_step": 16 * n + 20 * len(nodes),
@@ -519,7 +546,7 @@ def run_small(args):
     for p_ in (ps, pd, pb, px, pq):
         L.nihu_gb_device_free(ctx.handle, p_)
     ctx.close()
-    print(json.dumps(out), flush=True)
+    return out
 
 
 def run_multirhs(args):
@@ -596,6 +623,7 @@ def run_multirhs(args):
     solve_ms = (time.perf_counter() - t0) * 1e3
     prof_solve = ctx.profile()
     ctx.set_profiling(False)
+    err = fp64_error_per_rhs(ctx, L, C, dm, n, nrhs, k, pd, pq, px) if not args.no_fp64_check else None
     peak, _ = measured_peaks()
     gem = {}
     for name, (ms_, cnt) in prof_solve.items():
@@ -611,15 +639,78 @@ def run_multirhs(args):
         "near_pairs": int(counts[1]), "rhs_gemm_ms": rhs_ms, "solve_ms": solve_ms, "solve_status": int(st),
         "outer_iterations": oi.value, "inner_iterations": ii.value, "max_rel_residual": float(res.max()),
         "gemm": gem, "gemm_modes_one_product": mode_ms, "solves_per_s": nrhs / ((rhs_ms + solve_ms) / 1e3),
-        "note": "per-RHS accuracy is the FP64-accumulated residual |B - A X|/|B|; the entries of this "
-                "cylinder are checked against the FP64 oracle in tests/test_gpu_multi.py (first 64 columns), and "
-                "the oracle solution on a smaller cylinder",
+        "value": nrhs / ((rhs_ms + solve_ms) / 1e3), "unit": "solves/s", "err_per_rhs": err,
+        "note": "max_rel_residual is |B - A X|/|B| of the complex64 system the solver sees; err_per_rhs is "
+                "each right-hand side's solution against the FP64 solution of the FP64-quadrature system "
+                "(the oracle's arithmetic; the GPU FP64 mode matches the oracle to 1e-11), reached by FP64 "
+                "iterative refinement; tests/test_gpu_multi.py checks the solution against the oracle's own "
+                "dense FP64 solve on a 10080-quad cylinder",
     }
     for p_ in (ps, pd, pq, pb, px):
         L.nihu_gb_device_free(ctx.handle, p_)
     dm.close()
     ctx.close()
-    print(json.dumps(out), flush=True)
+    return out
+
+
+def fp64_error_per_rhs(ctx, L, C, dm, n, nrhs, k, pd32, pq, px, steps=3):
+    """Error of each right-hand side's solution X (device, complex128 n x nrhs)
+    against the FP64 solution X64 of the FP64-quadrature system
+    (DLP64 - I/2) X64 = SLP64 Q.  The FP64 matrices are assembled in the
+    FP64 mode; X64 is reached from X by iterative refinement whose residuals
+    B64 - A64 X64 are FP64 matrix-vector products and whose corrections are
+    solved on the complex64 matrix pd32.  Returns max and median of
+    |X - X64|_2 / |X64|_2 over the right-hand sides, and the FP64 relative
+    residual of X itself."""
+    col = 16 * n
+    p64s, p64d, pb64, pr, pdx = (ctypes.c_void_p() for _ in range(5))
+    for p_, size in ((p64s, 16 * n * n), (p64d, 16 * n * n), (pb64, col * nrhs), (pr, col * nrhs),
+                     (pdx, col * nrhs)):
+        ctx.check(L.nihu_gb_device_alloc(ctx.handle, size, ctypes.byref(p_)))
+    try:
+        ctx.check(L.nihu_gb_assemble(ctx.handle, dm.handle, dm.handle, C.HELMHOLTZ_3D, C.SLP | C.DLP, k, 1.0, 0.0,
+                                     C.REGULAR_FP64, C.C128, p64s, p64d, n, 0, C.DEVICE))
+        ctx.check(L.nihu_gb_add_identity(ctx.handle, dm.handle, -0.5, 0.0, C.C128, p64d, n, C.DEVICE))
+
+        def cols(p_, j):
+            return ctypes.c_void_p(p_.value + col * j)
+
+        for j in range(nrhs):  # B64 = SLP64 Q
+            ctx.check(L.nihu_gb_matvec(ctx.handle, C.C128, p64s, n, n, n, cols(pq, j), cols(pb64, j), 1.0, 0.0, 0.0,
+                                       0.0, C.DEVICE))
+        X = np.zeros((n, nrhs), np.complex128, order="F")
+        ctx.check(L.nihu_gb_memcpy(ctx.handle, X.ctypes.data, C.HOST, px, C.DEVICE, X.nbytes))
+        B64 = np.zeros_like(X)
+        ctx.check(L.nihu_gb_memcpy(ctx.handle, B64.ctypes.data, C.HOST, pb64, C.DEVICE, B64.nbytes))
+        X64 = X.copy()
+        res0 = None
+        for s_ in range(steps):
+            ctx.check(L.nihu_gb_memcpy(ctx.handle, pdx, C.DEVICE, X64.ctypes.data, C.HOST, X64.nbytes))
+            ctx.check(L.nihu_gb_memcpy(ctx.handle, pr, C.DEVICE, pb64, C.DEVICE, col * nrhs))
+            for j in range(nrhs):  # R = B64 - A64 X64
+                ctx.check(L.nihu_gb_matvec(ctx.handle, C.C128, p64d, n, n, n, cols(pdx, j), cols(pr, j), -1.0, 0.0,
+                                           1.0, 0.0, C.DEVICE))
+            R = np.zeros_like(X)
+            ctx.check(L.nihu_gb_memcpy(ctx.handle, R.ctypes.data, C.HOST, pr, C.DEVICE, R.nbytes))
+            if res0 is None:
+                res0 = np.linalg.norm(R, axis=0) / np.linalg.norm(B64, axis=0)
+            oi, ii = ctypes.c_int(0), ctypes.c_int(0)
+            rr = np.zeros(nrhs)
+            ctx.check(L.nihu_gb_solve_multi(ctx.handle, pd32, n, n, pr, pdx, nrhs, C.GEMM_TF32, C.GEMM_FP32, 30, 20,
+                                            1e-6, 1e-3, ctypes.byref(oi), ctypes.byref(ii),
+                                            rr.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), C.DEVICE))
+            D = np.zeros_like(X)
+            ctx.check(L.nihu_gb_memcpy(ctx.handle, D.ctypes.data, C.HOST, pdx, C.DEVICE, D.nbytes))
+            X64 += D
+        e = np.linalg.norm(X - X64, axis=0) / np.linalg.norm(X64, axis=0)
+        last = float((np.linalg.norm(D, axis=0) / np.linalg.norm(X64, axis=0)).max())
+        return {"max": float(e.max()), "median": float(np.median(e)),
+                "fp64_rel_residual_max": float(res0.max()), "refinement_steps": steps,
+                "last_correction_rel": last,
+                "reference": "FP64-quadrature matrices (GPU FP64 mode), FP64 residuals"}
+    finally:
+        for p_ in (p64s, p64d, pb64, pr, pdx):
+            L.nihu_gb_device_free(ctx.handle, p_)
 
 
 def run_sweep(args):
@@ -745,7 +836,7 @@ def run_sweep(args):
         out["persistent_gmres"] = {"ms": ms_, "matrix_bytes": mat_bytes,
                                    "achieved_GBs": mat_bytes / (ms_ * 1e-3) / 1e9}
     ctx.close()
-    print(json.dumps(out), flush=True)
+    return out
 
 
 def run_serve(args):
@@ -860,7 +951,7 @@ def run_serve(args):
     out["speedup_vs_plain_gpu"] = out["value"] / out["plain_solves_per_s"]
     out["served_vs_plain_max_rel_difference"] = agree
     ctx.close()
-    print(json.dumps(out), flush=True)
+    return out
 
 
 def run_bm(args):
@@ -1030,7 +1121,7 @@ def run_bm(args):
         out["cpu_baseline"] = {"value": 2.0 * rows * n / el, "unit": "entries/s", "cores": threads, "kind": "port",
                                "sample": "%d full rows x %d columns x (SLP, DLP, DLPt, HSP), FP64 oracle, %.1f s "
                                          "(system entries: two operators per entry of A and of B)" % (rows, n, el)}
-    print(json.dumps(out), flush=True)
+    return out
 
 
 def box_near_field(centres, h):
@@ -1197,7 +1288,7 @@ def run_p2p(args):
                                "sample": "%d random pairs of the list x (SLP, DLP, DLPt, HSP), FP64 oracle, %.1f s "
                                          "(near-field entries: two operators per entry of a and of b)"
                                          % (len(sample), el)}
-    print(json.dumps(out), flush=True)
+    return out
 
 
 def run_galerkin(args):
@@ -1299,31 +1390,143 @@ def run_galerkin(args):
         out["cpu_baseline"] = {"value": 2.0 * rows * n / el, "unit": "entries/s", "cores": threads, "kind": "port",
                                "sample": "%d full rows x %d columns x (SLP, DLP), FP64 Galerkin oracle, %.1f s"
                                          % (rows, n, el)}
-    print(json.dumps(out), flush=True)
+    return out
+
+
+def run_profile(args):
+    """Per-phase device times of the collocational assembly, and a small
+    target for ncu.  Assembles the Helmholtz (--laplace: Laplace) SLP and DLP
+    matrices of an icosphere (--subdiv) or a quad cylinder (--cylinder), or
+    with --bm the two Burton-Miller system matrices, --reps times.  With
+    --budget-mb the context's HBM budget forces host output in column panels,
+    so that every kernel launch covers one panel of the full-size problem and
+    the device holds only about the budget: small enough for an ncu capture
+    of single launches.  Without it both matrices are assembled into device
+    memory in one launch each.  --sweep N solves N wave numbers uniform in
+    [0.1, 10] on one icosphere and --sweep-config4 the 256-instance sweep
+    (nihu_gb_solve_sweep_batched, run --reps times; the first call builds the
+    near-pair lists).  Returns the per-phase times of the last repetition."""
+    import nihu_gb300 as g
+    from nihu_gb300 import _capi as C
+    from nihu_gb300 import api, meshes
+
+    if args.sweep or args.sweep_config4:
+        rng = np.random.default_rng(2026)
+        if args.sweep_config4:
+            mesh_list = [api.create_mesh(*meshes.icosphere(s_)) for s_ in (2, 3, 4)]
+            ks = rng.uniform(0.1, 10.0, 256)
+            mesh_of = np.arange(256) % 3
+        else:
+            mesh_list = [api.create_mesh(*meshes.icosphere(args.subdiv))]
+            ks = rng.uniform(0.1, 10.0, args.sweep)
+            mesh_of = np.zeros(args.sweep, np.int32)
+        ctx = api.Context(0)
+        ctx.set_profiling(True)
+        for _ in range(max(1, args.reps)):
+            ctx.profile_reset()
+            P, it, rel, conv = api.solve_sweep_batched(mesh_list, ks, mesh_of, restart=50, max_iters=1000, tol=1e-6,
+                                                       ctx=ctx, check=False)
+        prof = ctx.profile()
+        ctx.close()
+        return {"config": "profile (sweep)", "instances": len(ks), "meshes": [m.num_elements for m in mesh_list],
+                "iterations_total": int(np.sum(it)), "converged": int(np.sum(conv)),
+                "phases_ms": {k: round(v[0], 4) for k, v in prof.items()},
+                "launches": {k: v[1] for k, v in prof.items()}}
+
+    if args.cylinder:
+        nt = args.cylinder
+        nodes, elems = meshes.cylinder(nt, int(1.25 * nt), max(2, nt // 10))
+    else:
+        nodes, elems = meshes.icosphere(args.subdiv)
+    ctx = api.Context(0, hbm_budget_bytes=args.budget_mb << 20)
+    L = g.lib()
+    dm = api.DeviceMesh(ctx, nodes, elems)
+    n = dm.n
+    fam = C.LAPLACE_3D if args.laplace else C.HELMHOLTZ_3D
+    prec = C.REGULAR_FP64 if args.fp64 else C.REGULAR_FP32
+    if args.budget_mb:
+        hs = np.zeros((n, n), np.complex64, order="F")
+        hd = np.zeros((n, n), np.complex64, order="F")
+        ps, pd, where = hs.ctypes.data, hd.ctypes.data, C.HOST
+    else:
+        ps, pd = ctypes.c_void_p(), ctypes.c_void_p()
+        ctx.check(L.nihu_gb_device_alloc(ctx.handle, 8 * n * n, ctypes.byref(ps)))
+        ctx.check(L.nihu_gb_device_alloc(ctx.handle, 8 * n * n, ctypes.byref(pd)))
+        where = C.DEVICE
+    ctx.set_profiling(True)
+    for _ in range(max(1, args.reps)):
+        ctx.profile_reset()
+        if args.bm:
+            c = api.burton_miller_coupling(args.k) if fam == C.HELMHOLTZ_3D else 1.0 + 0.0j
+            ctx.check(L.nihu_gb_assemble_burton_miller(ctx.handle, dm.handle, fam, args.k, c.real, c.imag, prec,
+                                                       C.C64, pd, ps, n, where))
+        else:
+            ctx.check(L.nihu_gb_assemble(ctx.handle, dm.handle, dm.handle, fam, C.SLP | C.DLP, args.k, 1.0, 0.0, prec,
+                                         C.C64, ps, pd, n, 0, where))
+    prof = ctx.profile()
+    if not args.budget_mb:
+        L.nihu_gb_device_free(ctx.handle, ps)
+        L.nihu_gb_device_free(ctx.handle, pd)
+    dm.close()
+    ctx.close()
+    return {"config": "profile (assembly)", "n_elements": n, "where": "host panels" if args.budget_mb else "device",
+            "phases_ms": {k: round(v[0], 4) for k, v in prof.items()},
+            "launches": {k: v[1] for k, v in prof.items()}}
+
+
+def other_configs(args):
+    """Short runs of the other configurations, summarised for the headline
+    line: the plain small solve, the multi-RHS solve, the batched sweep and
+    the served stream (300 requests), each with its comparison against the
+    plain single-instance GPU path where it has one.  A failing leg is
+    reported as an error string and does not stop the others."""
+    import copy
+
+    def sub(**kw):
+        a = copy.copy(args)
+        for k_, v_ in kw.items():
+            setattr(a, k_, v_)
+        return a
+
+    def keep(d, keys):
+        return {k_: d[k_] for k_ in keys if k_ in d}
+
+    res = {}
+    legs = (
+        ("small", lambda: run_small(sub(steps=5, warmup=3)),
+         ("metric", "value", "unit", "higher_is_better", "n_elements", "k", "dtype", "e2e", "phases_ms",
+          "pressure_error_vs_analytic", "pressure_gpu_vs_cpu_oracle", "cpu_baseline")),
+        ("multirhs", lambda: run_multirhs(sub(steps=1, warmup=1)),
+         ("metric", "value", "unit", "n_elements", "nrhs", "k", "assembly_ms", "rhs_gemm_ms", "solve_ms",
+          "solve_status", "outer_iterations", "inner_iterations", "max_rel_residual", "err_per_rhs", "gemm",
+          "solves_per_s")),
+        ("sweep", lambda: run_sweep(sub(steps=3, warmup=2)),
+         ("metric", "value", "unit", "instances", "meshes", "batched_seconds", "plain_solves_per_s",
+          "speedup_vs_plain_gpu", "batched_vs_plain_max_rel_difference", "phases_ms", "plan_tuning")),
+        ("serve", lambda: run_serve(sub(requests=300, plain_sample=3)),
+         ("metric", "value", "unit", "requests", "arrival_rate_per_s", "latency_ms", "converged",
+          "plain_solves_per_s", "speedup_vs_plain_gpu", "served_vs_plain_max_rel_difference", "rounds",
+          "phases_ms")),
+    )
+    for name, fn, keys in legs:
+        t0 = time.perf_counter()
+        try:
+            d = fn()
+            res[name] = keep(d, keys)
+        except Exception as e:  # reported, not fatal for the headline
+            res[name] = {"error": "%s: %s" % (type(e).__name__, e)}
+        res[name]["wall_s"] = round(time.perf_counter() - t0, 2)
+    return res
 
 
 def main():
     args = parse()
-    if args.config == "multirhs":
-        run_multirhs(args)
-        return
-    if args.config == "small":
-        run_small(args)
-        return
-    if args.config == "sweep":
-        run_sweep(args)
-        return
-    if args.config == "serve":
-        run_serve(args)
-        return
-    if args.config == "bm":
-        run_bm(args)
-        return
-    if args.config == "p2p":
-        run_p2p(args)
-        return
-    if args.config == "galerkin":
-        run_galerkin(args)
+    runs = {"multirhs": run_multirhs, "small": run_small, "sweep": run_sweep, "serve": run_serve, "bm": run_bm,
+            "p2p": run_p2p, "galerkin": run_galerkin, "profile": run_profile}
+    if args.config in runs:
+        out = runs[args.config](args)
+        if out is not None:
+            print(json.dumps(out), flush=True)
         return
     if args.impl == "reference":
         run_reference(args)

@@ -269,7 +269,9 @@ nihu_gb_status nihu_gb_matvec(nihu_gb_ctx *ctx, int dtype_a, const void *A, int6
  * stream reaches that point.  m above NIHU_GB_NOALLOC_PARTIAL_ELEMS returns
  * NIHU_GB_ERR_OUT_OF_RANGE.  The first call on a device looks up the array's
  * device address (cudaGetSymbolAddress), so make it before any stream
- * capture.  All calls share the array and every call overwrites the part it
+ * capture; the address is kept per CUDA context, so the first call after a
+ * cudaDeviceReset (which makes a new context) looks it up again and should
+ * likewise come before any capture.  All calls share the array and every call overwrites the part it
  * reads, so nothing needs clearing -- but two calls that run on the GPU at the
  * same time (different streams or host threads) race and corrupt each other.
  * This entry point has no counterpart in the reference. */

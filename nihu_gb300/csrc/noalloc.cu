@@ -20,10 +20,44 @@ constexpr int64_t PARTIAL_ELEMS = NIHU_GB_NOALLOC_PARTIAL_ELEMS;
 static __device__ __align__(256) double2 g_partial[PARTIAL_ELEMS];
 
 // Host code cannot use g_partial's name as an address; the device address is
-// looked up once per device (with that device current) and cached.
+// looked up (with the device current) once per CUDA context and cached.  The
+// cache is keyed by the context's unique id, so that after a cudaDeviceReset
+// (or any other teardown of the primary context) the first call on the new
+// context looks the address up again instead of launching on a stale one.
 constexpr int MAX_DEVICES = 64;
-double2 *g_partial_addr[MAX_DEVICES] = {};
+struct PartialAddr {
+    unsigned long long ctx_id = 0;
+    double2 *addr = nullptr;
+};
+PartialAddr g_partial_addr[MAX_DEVICES];
 std::mutex g_setup_mu;
+
+// the current context's unique id through the driver API (found once through
+// the runtime, so the library needs no link against the driver)
+using CtxGetCurrentFn = int (*)(void **);
+using CtxGetIdFn = int (*)(void *, unsigned long long *);
+
+bool current_context_id(unsigned long long *id)
+{
+    static CtxGetCurrentFn get_current = nullptr;
+    static CtxGetIdFn get_id = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void *f = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            get_current = reinterpret_cast<CtxGetCurrentFn>(f);
+        f = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            get_id = reinterpret_cast<CtxGetIdFn>(f);
+        cudaGetLastError();
+    });
+    void *ctx = nullptr;
+    if (!get_current || !get_id || get_current(&ctx) != 0 || !ctx) return false;
+    return get_id(ctx, id) == 0;
+}
 
 nihu_gb_status partial_address(double2 **out)
 {
@@ -32,17 +66,24 @@ nihu_gb_status partial_address(double2 **out)
         cudaGetLastError();
         return NIHU_GB_ERR_NO_DEVICE;
     }
+    // no context may be current yet (a process whose first CUDA call this is):
+    // the symbol lookup below makes the device's primary context current
+    unsigned long long id = 0;
+    bool have_id = current_context_id(&id);
     std::lock_guard<std::mutex> lock(g_setup_mu);
-    if (!g_partial_addr[dev]) {
+    PartialAddr &slot = g_partial_addr[dev];
+    if (!slot.addr || !have_id || slot.ctx_id != id) {
         void *p = nullptr;
         cudaError_t e = cudaGetSymbolAddress(&p, g_partial);
         if (e != cudaSuccess || !p) {
             cudaGetLastError();
             return NIHU_GB_ERR_CUDA;
         }
-        g_partial_addr[dev] = static_cast<double2 *>(p);
+        if (!have_id) have_id = current_context_id(&id);
+        slot.addr = static_cast<double2 *>(p);
+        slot.ctx_id = have_id ? id : 0;  // 0: looked up again on the next call
     }
-    *out = g_partial_addr[dev];
+    *out = slot.addr;
     return NIHU_GB_OK;
 }
 

@@ -63,6 +63,39 @@ def test_solve_multi_cylinder_plane_waves(gpu_ctx, oracle):
     assert err.max() < 1e-4, err
 
 
+def test_per_rhs_error_against_oracle_solution_10k_quads(gpu_ctx, oracle):
+    """The multi-RHS precision path on a 10080-quad closed cylinder (R = 1,
+    L = 4: 80 x 100 side grid and O-grid caps of 8 rings), k = 4, 64 plane
+    waves with seeded directions: complex64 matrices with FP32 regular
+    quadrature, B = SLP Q by the FP32-accurate product, and the
+    mixed-precision refinement solve (TF32 inner products, FP64 residual).
+    Each right-hand side's surface pressure against the oracle's dense FP64
+    solve of the FP64 system within 1e-4 in the 2-norm (the surface pressure
+    target); the median is reported in the assertion message."""
+    mesh = meshes.cylinder(80, 100, 8, radius=1.0, length=4.0)
+    n = len(mesh[1])
+    assert n == 10080
+    k, nrhs = 4.0, 64
+    Q = meshes.plane_wave_neumann(*mesh, k, meshes.sphere_directions(nrhs, seed=2026))
+    Lo = oracle.assemble(mesh, mesh, oracle.HELMHOLTZ, oracle.SLP, k, threads=16)
+    Mo = oracle.assemble(mesh, mesh, oracle.HELMHOLTZ, oracle.DLP, k, threads=16)
+    Mo[np.diag_indices(n)] -= 0.5
+    P_ref = np.linalg.solve(Mo, Lo @ Q)
+    del Lo, Mo
+    m = g.create_mesh(*mesh)
+    sp = g.constant_view(m)
+    Lg = np.zeros((n, n), np.complex64, order="F")
+    Mg = np.zeros((n, n), np.complex64, order="F")
+    Lg << g.dirac(sp) * g.create_integral_operator(g.helmholtz_3d_SLP_kernel(k))[sp]
+    Mg << g.dirac(sp) * g.create_integral_operator(g.helmholtz_3d_DLP_kernel(k))[sp]
+    Mg << g.dirac(sp) * (-.5 * g.identity_integral_operator())[sp]
+    Bg = g.gemm(Lg, Q, mode=g.GEMM_FP32, ctx=gpu_ctx)
+    X, outer, inner, res = g.solve_multi(Mg, Bg, inner_mode=g.GEMM_TF32, tol=1e-6, ctx=gpu_ctx)
+    assert res.max() <= 1e-6
+    err = np.linalg.norm(X - P_ref, axis=0) / np.linalg.norm(P_ref, axis=0)
+    assert err.max() < 1e-4, (err.max(), np.median(err))
+
+
 def test_cylinder_40k_entries_match_oracle(gpu_ctx, oracle):
     """The full-size 40000-quad cylinder (k = 4): both matrices assembled on the
     device, their first 64 columns (every row) against the FP64 oracle."""
