@@ -682,7 +682,7 @@ def fp64_error_per_rhs(ctx, L, C, dm, n, nrhs, k, pd32, pq, px, steps=3):
         ctx.check(L.nihu_gb_memcpy(ctx.handle, X.ctypes.data, C.HOST, px, C.DEVICE, X.nbytes))
         B64 = np.zeros_like(X)
         ctx.check(L.nihu_gb_memcpy(ctx.handle, B64.ctypes.data, C.HOST, pb64, C.DEVICE, B64.nbytes))
-        X64 = X.copy()
+        X64 = X.copy(order="F")  # ndarray.copy defaults to C order
         res0 = None
         for s_ in range(steps):
             ctx.check(L.nihu_gb_memcpy(ctx.handle, pdx, C.DEVICE, X64.ctypes.data, C.HOST, X64.nbytes))

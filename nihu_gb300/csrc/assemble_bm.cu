@@ -137,8 +137,8 @@ __global__ void __launch_bounds__(BM_THREADS, sizeof(R) == 4 ? 4 : 1) k_regular_
                 if constexpr (sizeof(R) == 4) {
                     const float4 y = __ldg(trial.pts32 + 2 * (base + slot));
                     const float4 n = __ldg(trial.pts32 + 2 * (base + slot) + 1);
-                    const bool centre = slot == 0;  // the accurate hi/lo centre difference
-                    f(centre ? dx : y.x - x0, centre ? dy : y.y - x1, centre ? dz : y.z - x2, y.w, n.x, n.y, n.z);
+                    // the hi/lo centre difference plus the point's offset from the centre
+                    f(dx + y.x, dy + y.y, dz + y.z, y.w, n.x, n.y, n.z);
                 } else {
                     const double *y = trial.pts64 + 8 * (base + slot);
                     f(y[0] - x0, y[1] - x1, y[2] - x2, y[3], y[4], y[5], y[6]);
@@ -146,8 +146,9 @@ __global__ void __launch_bounds__(BM_THREADS, sizeof(R) == 4 ? 4 : 1) k_regular_
             }
         };
         if constexpr (sizeof(R) == 4) {
-            const float4 h = s_hi[c];
-            const float fx = h.x - x0, fy = h.y - x1, fz = h.z - x2;
+            const float4 h = s_hi[c], l = s_lo[c];  // hi/lo centre difference (as k_regular)
+            const float fx = (h.x - ih.x) + (l.x - il.x), fy = (h.y - ih.y) + (l.y - il.y),
+                        fz = (h.z - ih.z) + (l.z - il.z);
             const float q = (fx * fx + fy * fy + fz * fz) * h.w;
             if (__all_sync(0xffffffffu, q > q_far)) {
                 const float4 p = s_p0[c];

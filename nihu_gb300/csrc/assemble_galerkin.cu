@@ -371,8 +371,9 @@ __global__ void __launch_bounds__(GAL_THREADS) k_galerkin_regular(GalArgs a)
         bool done = false;
         if constexpr (sizeof(R) == 4) {
             // far field: both one-point rules, the centroid kernel times both areas
-            const float4 h = s_hi[c];
-            const float fx = h.x - x0, fy = h.y - x1, fz = h.z - x2;
+            const float4 h = s_hi[c], l = s_lo[c];  // hi/lo centre difference (as k_regular)
+            const float fx = (h.x - ih.x) + (l.x - il.x), fy = (h.y - ih.y) + (l.y - il.y),
+                        fz = (h.z - ih.z) + (l.z - il.z);
             const float q = (fx * fx + fy * fy + fz * fz) * h.w;
             if (__all_sync(0xffffffffu, q > 249.64f * (1.0f + 1e-4f) && shared == 0)) {
                 const float4 p = s_p0[c];
@@ -425,11 +426,10 @@ __global__ void __launch_bounds__(GAL_THREADS) k_galerkin_regular(GalArgs a)
                         if constexpr (sizeof(R) == 4) {
                             const float4 y = __ldg(trial.pts32 + 2 * (bj + sq));
                             const float4 n = __ldg(trial.pts32 + 2 * (bj + sq) + 1);
-                            // centroid pair: the accurate hi/lo difference
-                            const bool centre = sp == 0 && sq == 0;
-                            eval_point<FAM, float>(centre ? dx : y.x - xp0, centre ? dy : y.y - xp1,
-                                                   centre ? dz : y.z - xp2, y.w, n.x, n.y, n.z, k, ws * wp, wd * wp,
-                                                   sr, si, dr, di);
+                            // r = (c_j - c_i) + (y - c_j) - (x_p - c_i): the hi/lo centre
+                            // difference and the points' offsets from their centres
+                            eval_point<FAM, float>(dx + (y.x - xp0), dy + (y.y - xp1), dz + (y.z - xp2), y.w, n.x, n.y,
+                                                   n.z, k, ws * wp, wd * wp, sr, si, dr, di);
                         } else {
                             const double *y = trial.pts64 + 8 * (bj + sq);
                             eval_point<FAM, double>(y[0] - xp0, y[1] - xp1, y[2] - xp2, y[3], y[4], y[5], y[6], k,

@@ -114,9 +114,8 @@ __global__ void __launch_bounds__(PAIR_THREADS) k_pairs_regular(PairArgs a)
                 if constexpr (sizeof(R) == 4) {
                     const float4 y = __ldg(trial.pts32 + 2 * (base + slot));
                     const float4 n = __ldg(trial.pts32 + 2 * (base + slot) + 1);
-                    const bool centre = slot == 0;
-                    eval_bm<FAM, true, float>(centre ? dx : y.x - x0, centre ? dy : y.y - x1, centre ? dz : y.z - x2,
-                                              y.w, n.x, n.y, n.z, nx0, nx1, nx2, k, ws, wd, wt, wh, o);
+                    eval_bm<FAM, true, float>(dx + y.x, dy + y.y, dz + y.z, y.w, n.x, n.y, n.z, nx0, nx1, nx2, k,
+                                              ws, wd, wt, wh, o);
                 } else {
                     const double *y = trial.pts64 + 8 * (base + slot);
                     eval_bm<FAM, true, double>(y[0] - x0, y[1] - x1, y[2] - x2, y[3], y[4], y[5], y[6], nx0, nx1, nx2,

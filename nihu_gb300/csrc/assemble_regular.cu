@@ -267,8 +267,11 @@ __global__ void __launch_bounds__(REG_THREADS) k_regular(RegularArgs a)
         if constexpr (sizeof(R) == 4) {
             // far-field fast path, taken when every lane of the warp is a far
             // pair: one centroid point for both operators
-            const float4 h = s_hi[c];
-            const float fx = h.x - x0, fy = h.y - x1, fz = h.z - x2;
+            // the hi/lo centre difference: FP32 relative accuracy of r, which
+            // the DLP's r.n of nearly coplanar far pairs needs
+            const float4 h = s_hi[c], l = s_lo[c];
+            const float fx = (h.x - ih.x) + (l.x - il.x), fy = (h.y - ih.y) + (l.y - il.y),
+                        fz = (h.z - ih.z) + (l.z - il.z);
             const float q = (fx * fx + fy * fy + fz * fz) * h.w;
             if (__all_sync(0xffffffffu, q > Q_FAR)) {
                 const float4 p = s_p0[c];
@@ -335,7 +338,7 @@ __global__ void __launch_bounds__(REG_THREADS) k_regular(RegularArgs a)
                         for (int q = 0; q < npd; ++q) {
                             const int64_t sl = base + level_slot0(1) + q;
                             const float4 y = __ldg(trial.pts32 + 2 * sl), n = __ldg(trial.pts32 + 2 * sl + 1);
-                            eval_point<FAM, float>(y.x - x0, y.y - x1, y.z - x2, y.w, n.x, n.y, n.z, k, R(0), R(1), sr,
+                            eval_point<FAM, float>(mx + y.x, my + y.y, mz + y.z, y.w, n.x, n.y, n.z, k, R(0), R(1), sr,
                                                    si, dr, di);
                         }
                     }
@@ -385,9 +388,7 @@ __global__ void __launch_bounds__(REG_THREADS) k_regular(RegularArgs a)
                         if constexpr (sizeof(R) == 4) {
                             const float4 y = __ldg(trial.pts32 + 2 * (base + slot));
                             const float4 n = __ldg(trial.pts32 + 2 * (base + slot) + 1);
-                            const bool centre = slot == 0;
-                            gm = point_geom<float>(centre ? dx : y.x - x0, centre ? dy : y.y - x1,
-                                                   centre ? dz : y.z - x2, y.w, n.x, n.y, n.z, ws, wd);
+                            gm = point_geom<float>(dx + y.x, dy + y.y, dz + y.z, y.w, n.x, n.y, n.z, ws, wd);
                         } else {
                             const double *y = trial.pts64 + 8 * (base + slot);
                             gm = point_geom<double>(y[0] - x0, y[1] - x1, y[2] - x2, y[3], y[4], y[5], y[6], ws, wd);
@@ -426,10 +427,10 @@ __global__ void __launch_bounds__(REG_THREADS) k_regular(RegularArgs a)
                 if constexpr (sizeof(R) == 4) {
                     const float4 y = __ldg(trial.pts32 + 2 * (base + slot));
                     const float4 n = __ldg(trial.pts32 + 2 * (base + slot) + 1);
-                    // level-0 point: the trial centre; use the accurate hi/lo difference
-                    const bool centre = slot == 0;
-                    eval_point<FAM, float>(centre ? dx : y.x - x0, centre ? dy : y.y - x1, centre ? dz : y.z - x2, y.w,
-                                           n.x, n.y, n.z, k, ws, wd, sr, si, dr, di);
+                    // r = (c_j - x) + (y - c_j): the hi/lo centre difference plus the
+                    // point's offset from the trial centre
+                    eval_point<FAM, float>(dx + y.x, dy + y.y, dz + y.z, y.w, n.x, n.y, n.z, k, ws, wd, sr, si, dr,
+                                           di);
                 } else {
                     const double *y = trial.pts64 + 8 * (base + slot);
                     eval_point<FAM, double>(y[0] - x0, y[1] - x1, y[2] - x2, y[3], y[4], y[5], y[6], k, ws, wd, sr,

@@ -88,7 +88,10 @@ __global__ void k_mesh_geometry(const double *__restrict__ nodes, int64_t n_node
                 double wj = w * J;
                 int slot = level_slot0(lev) + p;
                 int64_t base = ((int64_t)e * 2 + par) * SLOTS + slot;
-                m.pts32[2 * base] = make_float4((float)y[0], (float)y[1], (float)y[2], (float)wj);
+                // FP32 points relative to the element centre: r = (c_j - x) + (y - c_j)
+                // keeps FP32 relative accuracy of r however far the mesh is from the origin
+                m.pts32[2 * base] = make_float4((float)(y[0] - cen[0]), (float)(y[1] - cen[1]), (float)(y[2] - cen[2]),
+                                                (float)wj);
                 m.pts32[2 * base + 1] = make_float4((float)(nv[0] / J), (float)(nv[1] / J), (float)(nv[2] / J), 0.0f);
                 double *d64 = m.pts64 + 8 * base;
                 d64[0] = y[0]; d64[1] = y[1]; d64[2] = y[2]; d64[3] = wj;
