@@ -6,6 +6,8 @@ Tolerances (every entry, normwise max |A_gpu - A_oracle| / max |A_oracle|):
 FP64 regular quadrature 1e-11, FP32 1e-5 (in FP32 mode the matched and
 nearly singular pairs are summed in FP32 as well).
 """
+import os
+
 import numpy as np
 import pytest
 
@@ -142,6 +144,41 @@ def test_pulsating_sphere_through_the_operator_algebra(gpu_ctx, oracle):
     pr = np.linalg.solve(Mr - 0.5 * np.diag(mesh.areas()), Lr @ np.ones(n))
     assert np.abs(p - pr).max() / np.abs(pr).max() <= 1e-9
     assert np.allclose(np.diag(I).real, mesh.areas(), rtol=1e-12)
+
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+@pytest.mark.parametrize("name,band", [("sphere_1_3.off", 0.015), ("sphere_1_5.off", 0.006)])
+@pytest.mark.parametrize("precision,tol", [("fp64", 1e-9), ("fp32", 1e-4)])
+def test_reference_pulsating_sphere_sequence(gpu_ctx, oracle, name, band, precision, tol):
+    """The reference's own test (nihu/test/stallone_unit/
+    helmholtz_3d_pulsating_sphere_test.cpp:28-76) on its own meshes (432
+    triangles, 600 quads): I, L, M << test_space * Op[trial_space] with
+    k = 1, q = 1, p = (M - I/2)^-1 L q.  The pressure within `tol` of the
+    oracle's solution of the same sequence and within `band` of the analytic
+    -R/(1 + ikR) (the oracle's own discretisation error is 1.0e-2 / 4.5e-3;
+    the reference prints log10 of the RMS error, -2.2 / -2.7 here)."""
+    nodes, elems = meshes.read_off(os.path.join(GOLDEN, name))
+    mesh = g.create_mesh(nodes, elems)
+    sp = g.constant_view(mesh)
+    n = sp.get_num_dofs()
+    k = 1.0
+    I = np.zeros((n, n), np.complex128)
+    L = np.zeros((n, n), np.complex128)
+    M = np.zeros((n, n), np.complex128)
+    I << sp * g.identity_integral_operator()[sp]
+    (sp * g.create_integral_operator(g.helmholtz_3d_SLP_kernel(k))[sp]).eval_into(L, precision=precision,
+                                                                                  ctx=gpu_ctx)
+    (sp * g.create_integral_operator(g.helmholtz_3d_DLP_kernel(k))[sp]).eval_into(M, precision=precision,
+                                                                                  ctx=gpu_ctx)
+    p = np.linalg.solve(M - 0.5 * I, L @ np.ones(n))
+    Lr = oracle.assemble_galerkin((nodes, elems), (nodes, elems), oracle.HELMHOLTZ, oracle.SLP, k, threads=8)
+    Mr = oracle.assemble_galerkin((nodes, elems), (nodes, elems), oracle.HELMHOLTZ, oracle.DLP, k, threads=8)
+    pr = np.linalg.solve(Mr - 0.5 * np.diag(mesh.areas()), Lr @ np.ones(n))
+    assert np.abs(p - pr).max() / np.abs(pr).max() <= tol
+    pa = -1.0 / (1.0 + 1j * k)
+    assert np.abs(p - pa).max() / abs(pa) < band
 
 
 def test_mass_matrix_entry_point(gpu_ctx):
