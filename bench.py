@@ -552,8 +552,10 @@ def run_small(args):
 def run_multirhs(args):
     """Multi-RHS precision path: closed cylinder R=1, L=4, 40000 flat quads,
     k=4, 64 plane waves with seeded uniform directions.  Times the assembly of
-    SLP and DLP (complex64), the right-hand sides B = SLP Q (split-BF16 GEMM)
-    and the mixed-precision refinement solve of (DLP - I/2) X = B."""
+    SLP and DLP (complex64), the right-hand sides B = SLP Q (the FP32-accurate
+    split-BF16 product, BF16x6 on tcgen05) and the mixed-precision refinement
+    solve of (DLP - I/2) X = B (BF16x3 tcgen05 products inside GMRES, BF16x6
+    residuals combined in FP64), and one product of every GEMM mode."""
     import torch
 
     import nihu_gb300 as g
@@ -593,17 +595,19 @@ def run_multirhs(args):
     ctx.profile_reset()
     ctx.check(L.nihu_gb_add_identity(ctx.handle, dm.handle, -0.5, 0.0, C.C64, pd, n, C.DEVICE))
     # warm-up of every GEMM mode (the library's first call of a mode loads its kernels)
-    for mode in (C.GEMM_FP32, C.GEMM_TF32, C.GEMM_BF16X9):
+    for mode in (C.GEMM_FP32, C.GEMM_TF32, C.GEMM_BF16X9, C.GEMM_BF16X3, C.GEMM_BF16X6):
         ctx.check(L.nihu_gb_gemm(ctx.handle, mode, ps, n, n, n, pq, n, nrhs, px, n, 1.0, 0.0, 0.0, 0.0, C.DEVICE))
     torch.cuda.synchronize()
     ctx.profile_reset()
     t0 = time.perf_counter()
-    ctx.check(L.nihu_gb_gemm(ctx.handle, C.GEMM_FP32, ps, n, n, n, pq, n, nrhs, pb, n, 1.0, 0.0, 0.0, 0.0, C.DEVICE))
+    ctx.check(L.nihu_gb_gemm(ctx.handle, C.GEMM_BF16X6, ps, n, n, n, pq, n, nrhs, pb, n, 1.0, 0.0, 0.0, 0.0, C.DEVICE))
     torch.cuda.synchronize()
     rhs_ms = (time.perf_counter() - t0) * 1e3
     # one product of each GEMM mode on the 40000 x 40000 matrix (64 right-hand sides)
     mode_ms = {}
-    for mname, mode in (("fp32_cuda_cores", C.GEMM_FP32), ("tf32_tensor", C.GEMM_TF32), ("bf16x9_tensor", C.GEMM_BF16X9)):
+    for mname, mode in (("fp32_cuda_cores_cublas", C.GEMM_FP32), ("tf32_tensor_cublas", C.GEMM_TF32),
+                        ("bf16x9_tensor_cublas", C.GEMM_BF16X9), ("bf16x3_tcgen05", C.GEMM_BF16X3),
+                        ("bf16x6_tcgen05", C.GEMM_BF16X6)):
         torch.cuda.synchronize()
         t1 = time.perf_counter()
         ctx.check(L.nihu_gb_gemm(ctx.handle, mode, ps, n, n, n, pq, n, nrhs, px, n, 1.0, 0.0, 0.0, 0.0, C.DEVICE))
@@ -616,7 +620,7 @@ def run_multirhs(args):
     torch.cuda.synchronize()
     ctx.profile_reset()  # the solve's phases alone
     t0 = time.perf_counter()
-    st = L.nihu_gb_solve_multi(ctx.handle, pd, n, n, pb, px, nrhs, C.GEMM_TF32, C.GEMM_FP32, 30, 20, 1e-6, 1e-3,
+    st = L.nihu_gb_solve_multi(ctx.handle, pd, n, n, pb, px, nrhs, C.GEMM_BF16X3, C.GEMM_BF16X6, 30, 20, 1e-6, 1e-3,
                                ctypes.byref(oi), ctypes.byref(ii), res.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
                                C.DEVICE)
     torch.cuda.synchronize()
@@ -632,6 +636,10 @@ def run_multirhs(args):
             gem[name] = {"launches": cnt, "avg_ms": avg, "hbm_gbs": 8.0 * n * n / (avg / 1e3) / 1e9,
                          "hbm_frac": 8.0 * n * n / (avg / 1e3) / 1e9 / peak,
                          "tflops_complex": 8.0 * n * n * nrhs / (avg / 1e3) / 1e12}
+            parts_products = {"gemm_bf16x3": 3, "gemm_bf16x6": 6}.get(name)
+            if parts_products:
+                # BF16 tensor work: products x 2 (2n rows of the float view) (2 nrhs) n
+                gem[name]["tensor_tflops_bf16"] = parts_products * 2.0 * (2 * n) * (2 * nrhs) * n / (avg / 1e3) / 1e12
     out = {
         "metric": "multi-RHS solve (config 3)", "impl": "ours", "n_elements": n, "nrhs": nrhs, "k": k,
         "assembly_ms": asm_ms, "assembly_entries_per_s": 2.0 * n * n / (asm_ms / 1e3),
@@ -696,7 +704,7 @@ def fp64_error_per_rhs(ctx, L, C, dm, n, nrhs, k, pd32, pq, px, steps=3):
                 res0 = np.linalg.norm(R, axis=0) / np.linalg.norm(B64, axis=0)
             oi, ii = ctypes.c_int(0), ctypes.c_int(0)
             rr = np.zeros(nrhs)
-            ctx.check(L.nihu_gb_solve_multi(ctx.handle, pd32, n, n, pr, pdx, nrhs, C.GEMM_TF32, C.GEMM_FP32, 30, 20,
+            ctx.check(L.nihu_gb_solve_multi(ctx.handle, pd32, n, n, pr, pdx, nrhs, C.GEMM_BF16X3, C.GEMM_BF16X6, 30, 20,
                                             1e-6, 1e-3, ctypes.byref(oi), ctypes.byref(ii),
                                             rr.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), C.DEVICE))
             D = np.zeros_like(X)

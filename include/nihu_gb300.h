@@ -280,10 +280,18 @@ nihu_gb_status nihu_gb_matvec_noalloc(int dtype_a, const void *A, int64_t m, int
                                       void *y, double alpha_re, double alpha_im, double beta_re, double beta_im,
                                       void *stream);
 
-/* arithmetic of a multi-right-hand-side product (nihu_gb_gemm) */
-#define NIHU_GB_GEMM_FP32 0   /* FP32 on the CUDA cores */
-#define NIHU_GB_GEMM_TF32 1   /* TF32 tensor cores, FP32 accumulation */
-#define NIHU_GB_GEMM_BF16X9 2 /* split BF16 (3 parts, 9 products) on the tensor cores: FP32-accurate */
+/* arithmetic of a multi-right-hand-side product (nihu_gb_gemm).  BF16X3 and
+ * BF16X6 are this library's own tcgen05 kernel: one pass over A, each FP32
+ * value split into BF16 parts (2 or 3) in shared and tensor memory, the part
+ * products above the target precision accumulated in FP32 in tensor memory
+ * (about 1e-5 and FP32 accuracy).  They need A 16-byte aligned with an even
+ * lda; otherwise BF16X3 runs as FP32 and BF16X6 as BF16X9.  FP32, TF32 and
+ * BF16X9 are cuBLAS (a plain library GEMM on the same real view). */
+#define NIHU_GB_GEMM_FP32 0   /* FP32 on the CUDA cores (cuBLAS) */
+#define NIHU_GB_GEMM_TF32 1   /* TF32 tensor cores, FP32 accumulation (cuBLAS) */
+#define NIHU_GB_GEMM_BF16X9 2 /* split BF16 (3 parts, 9 products), cuBLAS emulation: FP32-accurate */
+#define NIHU_GB_GEMM_BF16X3 3 /* split BF16 (2 parts, 3 products), tcgen05: about 1e-5 */
+#define NIHU_GB_GEMM_BF16X6 4 /* split BF16 (3 parts, 6 products), tcgen05: FP32-accurate */
 
 /* Y = alpha * A X + beta * Y for nrhs right-hand sides: A complex64 m x n
  * (lda), X n x nrhs (ldx) and Y m x nrhs (ldy) complex128, column-major.
@@ -303,7 +311,8 @@ nihu_gb_status nihu_gb_gemm(nihu_gb_ctx *ctx, int mode, const void *A, int64_t m
  * normally TF32 tensor cores; FP64 Arnoldi), stops a column when its residual
  * estimate falls by inner_tol, adds the correction to X in FP64 and
  * recomputes the residual B - A X with FP32-accurate products (residual_mode
- * NIHU_GB_GEMM_FP32 or NIHU_GB_GEMM_BF16X9) combined in FP64.  Stops when
+ * NIHU_GB_GEMM_FP32, NIHU_GB_GEMM_BF16X9 or NIHU_GB_GEMM_BF16X6) combined in
+ * FP64.  Stops when
  * every column has |B - A X| <= tol |B|.  X starts from zero.
  * rel_residuals (nrhs doubles) receives the final relative residuals. */
 nihu_gb_status nihu_gb_solve_multi(nihu_gb_ctx *ctx, const void *A, int64_t n, int64_t lda, const void *B, void *X,

@@ -23,7 +23,7 @@ SLP, DLP = 1, 2
 DLPT, HSP = 4, 8  # Burton-Miller operators
 C64, C128 = 0, 1
 REGULAR_FP32, REGULAR_FP64 = 0, 1
-GEMM_FP32, GEMM_TF32, GEMM_BF16X9 = 0, 1, 2
+GEMM_FP32, GEMM_TF32, GEMM_BF16X9, GEMM_BF16X3, GEMM_BF16X6 = 0, 1, 2, 3, 4
 HOST, DEVICE = 0, 1
 NOALLOC_PARTIAL_ELEMS = 1 << 20  # NIHU_GB_NOALLOC_PARTIAL_ELEMS
 

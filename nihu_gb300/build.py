@@ -16,7 +16,7 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libnihu_gb300.so")
 SOURCES = ["mesh.cu", "classify.cu", "assemble_regular.cu", "assemble_singular.cu", "linalg.cu", "capi.cu",
-           "noalloc.cu", "multi.cu", "solve_persistent.cu", "assemble_bm.cu",
+           "noalloc.cu", "multi.cu", "gemm_tc.cu", "solve_persistent.cu", "assemble_bm.cu",
            "assemble_pairs.cu", "assemble_galerkin.cu"]
 HEADERS = ["common.cuh", "geom.cuh", "classify.cuh", "kernels.h", "linalg.h", "quad_rules.h", "solve_persistent.h",
            "planar.cuh", "singular_schemes.cuh", "bm_schemes.cuh"]

@@ -1650,12 +1650,59 @@ nihu_gb_status ensure_cublas(nihu_gb_ctx *ctx)
     return NIHU_GB_OK;
 }
 
+// the error word of the tensor-core product (zeroed when first allocated)
+nihu_gb_status gemm_tc_err(nihu_gb_ctx *ctx, int **out)
+{
+    const bool fresh = ctx->scratch.find("gemm_err") == ctx->scratch.end();
+    void *p;
+    nihu_gb_status st = scratch(ctx, "gemm_err", 256, &p);
+    if (st) return st;
+    if (fresh) CK(cudaMemsetAsync(p, 0, sizeof(int), ctx->stream));
+    *out = (int *)p;
+    return NIHU_GB_OK;
+}
+
+// after a sync: a nonzero error word means a tensor-core product stopped on
+// a pipeline wait that ran out (its result is invalid); the word is cleared
+nihu_gb_status gemm_tc_check(nihu_gb_ctx *ctx)
+{
+    auto it = ctx->scratch.find("gemm_err");
+    if (it == ctx->scratch.end()) return NIHU_GB_OK;
+    int code = 0;
+    CK(cudaMemcpy(&code, it->second.first, sizeof(int), cudaMemcpyDeviceToHost));
+    if (!code) return NIHU_GB_OK;
+    CK(cudaMemset(it->second.first, 0, sizeof(int)));
+    return fail(ctx, NIHU_GB_ERR_CUDA, "tensor-core GEMM stopped: a pipeline wait ran out (code " +
+                                           std::to_string(code) + ")");
+}
+
 // Y = alpha A X + beta Y on the device (A complex64)
 nihu_gb_status gemm_device(nihu_gb_ctx *ctx, int mode, const void *A, int64_t m, int64_t n, int64_t lda,
                            const double2 *X, int64_t ldx, int64_t nrhs, double2 *Y, int64_t ldy, double are, double aim,
                            double bre, double bim)
 {
     nihu_gb_status st;
+    if (mode == NIHU_GB_GEMM_BF16X3 || mode == NIHU_GB_GEMM_BF16X6) {
+        if (gemm_tc_supported(A, lda) && n > 0) {
+            const int parts = mode == NIHU_GB_GEMM_BF16X3 ? 2 : 3;
+            void *ws;
+            int *err;
+            if ((st = scratch(ctx, "gemm_tc", gemm_tc_scratch_bytes(parts, m, n, nrhs), &ws))) return st;
+            if ((st = gemm_tc_err(ctx, &err))) return st;
+            cudaError_t e;
+            {
+                Phase ph(ctx, parts == 2 ? "gemm_bf16x3" : "gemm_bf16x6");
+                e = launch_gemm_tc(parts, A, m, n, lda, X, ldx, nrhs, Y, ldy, are, aim, bre, bim, ws, err,
+                                   ctx->stream);
+            }
+            ctx->launches += 3 * ((nrhs + 63) / 64);
+            if (e != cudaSuccess) return cuda_fail(ctx, e, "gemm (tensor cores)");
+            return NIHU_GB_OK;
+        }
+        // the float view of A cannot be tiled by TMA (unaligned A or odd lda):
+        // the library GEMM of the same or better accuracy
+        mode = mode == NIHU_GB_GEMM_BF16X3 ? NIHU_GB_GEMM_FP32 : NIHU_GB_GEMM_BF16X9;
+    }
     if ((st = ensure_cublas(ctx))) return st;
     void *xp, *z;
     if ((st = scratch(ctx, "gemm_xp", sizeof(float) * 2 * std::max<int64_t>(n, 1) * nrhs, &xp))) return st;
@@ -1680,7 +1727,8 @@ extern "C" nihu_gb_status nihu_gb_gemm(nihu_gb_ctx *ctx, int mode, const void *A
                                        double alpha_im, double beta_re, double beta_im, int where)
 {
     if (!ctx) return NIHU_GB_ERR_INVALID_ARGUMENT;
-    if (mode < 0 || mode > 2 || !valid_where(where) || m < 0 || n < 0 || nrhs < 0 || lda < std::max<int64_t>(m, 1) ||
+    if (mode < 0 || mode > NIHU_GB_GEMM_BF16X6 || !valid_where(where) || m < 0 || n < 0 || nrhs < 0 ||
+        lda < std::max<int64_t>(m, 1) ||
         ldx < std::max<int64_t>(n, 1) || ldy < std::max<int64_t>(m, 1) || (m && nrhs && (!A || !Y)) ||
         (n && nrhs && !X) || m > 0x3fffffff || n > 0x7fffffff || nrhs > 0x3fffffff)
         return fail(ctx, NIHU_GB_ERR_INVALID_ARGUMENT, "nihu_gb_gemm: bad argument");
@@ -1709,7 +1757,8 @@ extern "C" nihu_gb_status nihu_gb_gemm(nihu_gb_ctx *ctx, int mode, const void *A
         return st;
     if (where == NIHU_GB_HOST)
         CK(cudaMemcpy2DAsync(Y, 16 * ldy, dY, 16 * m, 16 * m, nrhs, cudaMemcpyDeviceToHost, ctx->stream));
-    return sync(ctx);
+    if ((st = sync(ctx))) return st;
+    return gemm_tc_check(ctx);
 }
 
 namespace {
@@ -1923,7 +1972,9 @@ extern "C" nihu_gb_status nihu_gb_solve_multi(nihu_gb_ctx *ctx, const void *A, i
                                               int *inner_iters, double *rel_residuals, int where)
 {
     if (!ctx) return NIHU_GB_ERR_INVALID_ARGUMENT;
-    if (inner_mode < 0 || inner_mode > 2 || (residual_mode != NIHU_GB_GEMM_FP32 && residual_mode != NIHU_GB_GEMM_BF16X9) ||
+    if (inner_mode < 0 || inner_mode > NIHU_GB_GEMM_BF16X6 ||
+        (residual_mode != NIHU_GB_GEMM_FP32 && residual_mode != NIHU_GB_GEMM_BF16X9 &&
+         residual_mode != NIHU_GB_GEMM_BF16X6) ||
         !valid_where(where) || n < 0 || nrhs < 0 || lda < std::max<int64_t>(n, 1) || restart < 1 || restart > 200 ||
         max_outer < 1 || !(tol > 0.0) || !(inner_tol > 0.0) || (n && nrhs && (!A || !B || !X)) || n > 0x3fffffff ||
         nrhs > 4096)
@@ -1962,6 +2013,7 @@ extern "C" nihu_gb_status nihu_gb_solve_multi(nihu_gb_ctx *ctx, const void *A, i
     if (where == NIHU_GB_HOST) CK(cudaMemcpyAsync(X, dX, blk, cudaMemcpyDeviceToHost, ctx->stream));
     else CK(cudaMemcpyAsync(X, dX, blk, cudaMemcpyDeviceToDevice, ctx->stream));
     if ((st = sync(ctx))) return st;
+    if ((st = gemm_tc_check(ctx))) return st;
     ctx->err = msg;
     if (rel_residuals)
         for (int64_t r = 0; r < nrhs; ++r) rel_residuals[r] = rel[r];

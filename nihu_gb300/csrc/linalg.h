@@ -60,6 +60,16 @@ cudaError_t launch_lu_solve(const double2 *A, int64_t n, int64_t lda, const int 
 cudaError_t launch_gemm_c64(void *cublas, int mode, const void *A, int64_t m, int64_t n, int64_t lda, const double2 *X,
                             int64_t ldx, int nrhs, double2 *Y, int64_t ldy, double are, double aim, double bre,
                             double bim, float *Xp, float *Z, cudaStream_t s, int *cublas_status);
+// gemm_tc.cu: the same product on the tcgen05 tensor cores, split BF16 with
+// FP32 accumulation (parts = 2: BF16x3, parts = 3: BF16x6, FP32-accurate).
+// Needs a 16-byte aligned A with an even lda (TMA on the float view);
+// scratch holds gemm_tc_scratch_bytes(); err receives a nonzero code if a
+// pipeline wait ran out (the kernel then stops and frees its tensor memory).
+bool gemm_tc_supported(const void *A, int64_t lda);
+size_t gemm_tc_scratch_bytes(int parts, int64_t m, int64_t n, int64_t nrhs);
+cudaError_t launch_gemm_tc(int parts, const void *A, int64_t m, int64_t n, int64_t lda, const double2 *X, int64_t ldx,
+                           int64_t nrhs, double2 *Y, int64_t ldy, double are, double aim, double bre, double bim,
+                           void *scratch, int *err, cudaStream_t s);
 int bdot_blocks(int64_t n);
 // fp32: products and partial sums in FP32 on the FP64-stored vectors (the
 // inner Arnoldi of a refinement), else FP64

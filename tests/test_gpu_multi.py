@@ -13,8 +13,10 @@ def rand_c(rng, *shape):
     return rng.standard_normal(shape) + 1j * rng.standard_normal(shape)
 
 
-@pytest.mark.parametrize("mode,tol", [(g.GEMM_FP32, 1e-5), (g.GEMM_BF16X9, 1e-5), (g.GEMM_TF32, 3e-3)])
-@pytest.mark.parametrize("m,n,nrhs", [(1000, 700, 64), (333, 517, 5)])
+@pytest.mark.parametrize("mode,tol", [(g.GEMM_FP32, 1e-5), (g.GEMM_BF16X9, 1e-5), (g.GEMM_TF32, 3e-3),
+                                      (g.GEMM_BF16X3, 1e-4), (g.GEMM_BF16X6, 1e-5)])
+@pytest.mark.parametrize("m,n,nrhs", [(1000, 700, 64), (333, 517, 5), (1024, 4096, 64), (640, 1000, 100),
+                                      (130, 70, 1)])
 def test_gemm_modes(gpu_ctx, mode, tol, m, n, nrhs):
     rng = np.random.default_rng(m + n + nrhs)
     A = rand_c(rng, m, n).astype(np.complex64)
