@@ -270,13 +270,16 @@ constexpr size_t smem_bytes()
 }
 static_assert(smem_bytes<2>() <= 232448 && smem_bytes<3>() <= 232448, "shared memory per CTA");
 
-// the K range [kt0, kt1) of unit u (split s of row block rb)
+// the K range [kt0, kt1) of unit u (split s of row block rb).  Row blocks
+// vary fastest, so CTAs that run at the same time read neighbouring row
+// blocks of the same columns: one column's segments of 512 B from many CTAs
+// form long contiguous runs in DRAM.
 struct Unit {
     int rb, s, kt0, kt1;
-    __device__ __forceinline__ Unit(int u, int S, int KT)
+    __device__ __forceinline__ Unit(int u, int RB, int S, int KT)
     {
-        rb = u / S;
-        s = u - rb * S;
+        s = u / RB;
+        rb = u - s * RB;
         kt0 = (int)((int64_t)s * KT / S);
         kt1 = (int)((int64_t)(s + 1) * KT / S);
     }
@@ -351,7 +354,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             // the prefetch cursor runs PREFETCH_TILES tiles ahead through this
             // CTA's sequence of units
             int pu = blockIdx.x, pkt = 0;
-            Unit pn(pu < a.units ? pu : 0, S, KT);
+            Unit pn(pu < a.units ? pu : 0, a.rb_count, S, KT);
             pkt = pn.kt0;
             auto prefetch_next = [&]() {
                 if (pu >= a.units) return;
@@ -359,14 +362,14 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                 if (++pkt >= pn.kt1) {
                     pu += gridDim.x;
                     if (pu < a.units) {
-                        pn = Unit(pu, S, KT);
+                        pn = Unit(pu, a.rb_count, S, KT);
                         pkt = pn.kt0;
                     }
                 }
             };
             for (int p = 0; p < PREFETCH_TILES; ++p) prefetch_next();
             for (int u = blockIdx.x; ok && u < a.units; u += gridDim.x) {
-                const Unit un(u, S, KT);
+                const Unit un(u, a.rb_count, S, KT);
                 for (int kt = un.kt0; kt < un.kt1; ++kt) {
                     const uint32_t st = ia % NSA, ph = (ia / NSA) & 1;
                     if (!(ok = mbar_wait(&a_empty[st], ph ^ 1, stop, a.err, ERR_WAIT_TMA))) break;
@@ -391,7 +394,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             bool ok = true;
             const uint32_t x_bytes = (uint32_t)SA * a.npad * TC_BK * 2;
             for (int u = blockIdx.x; ok && u < a.units; u += gridDim.x) {
-                const Unit un(u, S, KT);
+                const Unit un(u, a.rb_count, S, KT);
                 for (int kt = un.kt0; kt < un.kt1; ++kt) {
                     const uint32_t xs = ix % X_STAGES, xph = (ix / X_STAGES) & 1;
                     if (!(ok = mbar_wait(&x_empty[xs], xph ^ 1, stop, a.err, ERR_WAIT_TMA))) break;
@@ -416,7 +419,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         uint32_t ia = 0, it = 0;
         bool ok = true;
         for (int u = blockIdx.x; ok && u < a.units; u += gridDim.x) {
-            const Unit un(u, S, KT);
+            const Unit un(u, a.rb_count, S, KT);
             for (int kt = un.kt0; kt < un.kt1; ++kt) {
                 const uint32_t st = ia % NSA, ph = (ia / NSA) & 1;
                 if (!(ok = mbar_wait(&a_full[st], ph, stop, a.err, ERR_WAIT_CONVERT))) break;
@@ -465,7 +468,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             uint32_t it = 0, ic = 0;
             bool ok = true;
             for (int u = blockIdx.x; ok && u < a.units; u += gridDim.x) {
-                const Unit un(u, S, KT);
+                const Unit un(u, a.rb_count, S, KT);
                 for (int c0 = un.kt0; ok && c0 < un.kt1; c0 += CHAIN_TILES) {
                     // one accumulator chain: at most CHAIN_TILES K tiles
                     const uint32_t cb = ic & 1, cph = (ic >> 1) & 1;
@@ -513,7 +516,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         uint32_t ic = 0;
         bool ok = true;
         for (int u = blockIdx.x; ok && u < a.units; u += gridDim.x) {
-            const Unit un(u, S, KT);
+            const Unit un(u, a.rb_count, S, KT);
             // the unit's sum over its accumulator chains, column c of this row
             float run[TC_MAXN];
 #pragma unroll
