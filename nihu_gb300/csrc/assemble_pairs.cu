@@ -230,10 +230,20 @@ __global__ void __launch_bounds__(PAIR_SING_THREADS) k_pairs_singular(PairArgs a
                 if (S || polar_d) {
                     Elem64 lin;
                     linearized(e, r5[0], r5[1], lin);
-                    near_polar_sum(e, lin, fam, k, x0, r5[0], r5[1], S, polar_d, q);
-                    near_plane(lin, fam, k, x0, S, polar_d, q);
+                    if (a.precision == 0) {
+                        // FP32 regular quadrature: the schemes' sums in FP32 as well
+                        near_polar_sum_f32(e, fam, k, x0, r5[0], r5[1], S, polar_d, q);
+                        if (fam == FAM_HELMHOLTZ) near_dynamic_quad_f32(lin, k, x0, S, polar_d, q);
+                        near_static(lin, x0, S, polar_d, q);
+                    } else {
+                        near_polar_sum(e, lin, fam, k, x0, r5[0], r5[1], S, polar_d, q);
+                        near_plane(lin, fam, k, x0, S, polar_d, q);
+                    }
                 }
-                if (telles) near_telles_sum(e, fam, k, x0, r6, q);
+                if (telles) {
+                    if (a.precision == 0) near_telles_sum_f32(e, fam, k, x0, r6, q);
+                    else near_telles_sum(e, fam, k, x0, r6, q);
+                }
             }
             acc.sr = q.sr;
             acc.si = q.si;

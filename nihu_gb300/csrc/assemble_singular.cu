@@ -380,10 +380,20 @@ __device__ __forceinline__ void singular_pairs(const RegularArgs &a, const NearL
                     if (do_s || polar_d) {
                         Elem64 lin;
                         linearized(e, r5[0], r5[1], lin);
-                        near_polar_sum(e, lin, fam, kf, x0, r5[0], r5[1], do_s, polar_d, acc);
-                        near_plane(lin, fam, kf, x0, do_s, polar_d, acc);
+                        if (a.precision == 0) {
+                            // FP32 regular quadrature: the schemes' sums in FP32 as well
+                            near_polar_sum_f32(e, fam, kf, x0, r5[0], r5[1], do_s, polar_d, acc);
+                            if (fam == FAM_HELMHOLTZ) near_dynamic_quad_f32(lin, kf, x0, do_s, polar_d, acc);
+                            near_static(lin, x0, do_s, polar_d, acc);
+                        } else {
+                            near_polar_sum(e, lin, fam, kf, x0, r5[0], r5[1], do_s, polar_d, acc);
+                            near_plane(lin, fam, kf, x0, do_s, polar_d, acc);
+                        }
                     }
-                    if (telles) near_telles_sum(e, fam, kf, x0, r6, acc);
+                    if (telles) {
+                        if (a.precision == 0) near_telles_sum_f32(e, fam, kf, x0, r6, acc);
+                        else near_telles_sum(e, fam, kf, x0, r6, acc);
+                    }
                 }
             }
             if (!ok) {
@@ -458,7 +468,10 @@ cudaError_t launch_assemble_singular(const RegularArgs &a, const NearList &near,
     // to the concurrently running regular kernel
     int64_t total = (near.col_ptr ? near.nnz : 0) + (a.same_mesh ? (a.j1 - a.j0) : 0);
     int64_t want = (total + SING_THREADS - 1) / SING_THREADS;
-    int blocks = (int)max((int64_t)1, min(want, (int64_t)sms));
+    // quads: the pairs' FP32 sums need more warps than the FP64 pipe does;
+    // up to four blocks per SM once the regular kernel's blocks drain
+    const int per_sm = (a.trial.has_quad && a.precision == 0 && a.nk <= 1 && !a.force_batch) ? 4 : 1;
+    int blocks = (int)max((int64_t)1, min(want, (int64_t)sms * per_sm));
     // a frequency batch of few pairs: split the wave numbers over gridDim.y so
     // that about one block per SM runs
     dim3 grid(blocks, 1);

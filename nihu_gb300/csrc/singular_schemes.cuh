@@ -384,6 +384,255 @@ __device__ inline void near_telles_sum(const Elem64 &e, int fam, double k, const
     }
 }
 
+// ------------------------------------------------- FP32 sums of the quad schemes
+// Under FP32 regular quadrature the sums of the nearly singular quad schemes
+// run in FP32 while the rule stays FP64 (inverse mapping, side limits and
+// angles, Telles coefficients, the planar static part).  A bilinear quad
+// around the parameter point (xi0, eta0) is exactly
+//   y - x0 = p + u t1 + v t2 + u v d,   u = xi - xi0, v = eta - eta0,
+// p = y(xi0, eta0) - x0, t1, t2 the tangents there, d = (c0 - c1 + c2 - c3)/4,
+// with normal N = t1 x t2 + u (t1 x d) + v (d x t2); its linearisation at
+// (xi0, eta0) drops the u v d term and has normal t1 x t2.  Formed from these
+// FP64-made vectors, r = y - x0 keeps FP32 relative accuracy as r -> 0, and so
+// does the element-minus-linearisation difference of the polar scheme.
+struct QuadAround32 {
+    float p[3], t1[3], t2[3], d[3], n0[3], nu[3], nv[3];
+};
+
+__device__ inline void quad_around32(const Elem64 &e, const double x0[3], double xi0, double eta0, QuadAround32 &q)
+{
+    double y[3], a[3], b[3];
+    ex(e, xi0, eta0, y);
+    edx(e, xi0, eta0, a, b);
+    double d[3], n0[3], nu[3], nv[3];
+    for (int k = 0; k < 3; ++k) d[k] = 0.25 * (e.c[0][k] - e.c[1][k] + e.c[2][k] - e.c[3][k]);
+    cross3(a, b, n0);
+    cross3(a, d, nu);
+    cross3(d, b, nv);
+    for (int k = 0; k < 3; ++k) {
+        q.p[k] = (float)(y[k] - x0[k]);
+        q.t1[k] = (float)a[k];
+        q.t2[k] = (float)b[k];
+        q.d[k] = (float)d[k];
+        q.n0[k] = (float)n0[k];
+        q.nu[k] = (float)nu[k];
+        q.nv[k] = (float)nv[k];
+    }
+}
+
+// kernel values times the Jacobian at r = y - x0 with unnormalised normal N
+// (|N| = J): SLP = G J, DLP = dG/dr (r.N)/r; kern_point in FP32
+__device__ __forceinline__ void kern32(int fam, float k, const float rv[3], const float N[3], bool do_s, bool do_d,
+                                       float &sr, float &si, float &dr, float &di)
+{
+    constexpr float INV4PI = (float)INV_FOUR_PI;
+    const float r2 = rv[0] * rv[0] + rv[1] * rv[1] + rv[2] * rv[2];
+    const float rinv = rsqrtf(r2);
+    const float a = rinv * INV4PI;
+    const float rn = (rv[0] * N[0] + rv[1] * N[1] + rv[2] * N[2]) * rinv;
+    if (fam == FAM_LAPLACE) {
+        sr = do_s ? a * sqrtf(N[0] * N[0] + N[1] * N[1] + N[2] * N[2]) : 0.0f;
+        si = 0.0f;
+        dr = do_d ? -a * rinv * rn : 0.0f;
+        di = 0.0f;
+        return;
+    }
+    const float kr = k * (r2 * rinv);
+    float s, c;
+    sincos_reduced(kr, s, c);
+    if (do_s) {
+        const float J = sqrtf(N[0] * N[0] + N[1] * N[1] + N[2] * N[2]);
+        sr = c * a * J;
+        si = -s * a * J;
+    } else {
+        sr = si = 0.0f;
+    }
+    if (do_d) {
+        const float b = a * rinv * rn;
+        dr = -(c + kr * s) * b;
+        di = -(kr * c - s) * b;
+    } else {
+        dr = di = 0.0f;
+    }
+}
+
+// near_polar_sum with the FP32 sums (quads)
+static __device__ __noinline__ void near_polar_sum_f32(const Elem64 &e, int fam, double k, const double x0[3], double xi0,
+                                          double eta0, bool do_s, bool do_d, Acc &a)
+{
+    const int N = e.nc;
+    double tl[4], t0[4], dr[4];
+    for (int n = 0; n < N; ++n) {
+        double c1[2], c2[2];
+        domain_corner(N, n, c1[0], c1[1]);
+        domain_corner(N, (n + 1) % N, c2[0], c2[1]);
+        c1[0] -= xi0; c1[1] -= eta0;
+        c2[0] -= xi0; c2[1] -= eta0;
+        side_geometry(c1, c2, tl[n], t0[n], dr[n], true);
+    }
+    QuadAround32 q;
+    quad_around32(e, x0, xi0, eta0, q);
+    const float kf = (float)k;
+    float sr = 0, si = 0, dsr = 0, dsi = 0;
+    for (int n = 0; n < N; ++n) {
+        double t1 = tl[n], t2 = tl[(n + 1) % N];
+        wrap_limits(t1, t2);
+        if (fabs(t2 - t1) < 1e-3) continue;
+        for (int ia = 0; ia < 8; ++ia) {
+            double xx, wa;
+            gauss_pt(8, ia, xx, wa);
+            const double th = ((1.0 - xx) * t1 + (1.0 + xx) * t2) / 2.0;
+            double cth, sth;
+            sincos(th, &sth, &cth);
+            const float wth = (float)(wa * (t2 - t1) / 2.0);
+            const float rho_lim = (float)(dr[n] / cos_angle(th - t0[n]));
+            const float cf = (float)cth, sf = (float)sth;
+            float ps = 0, pi = 0, pds = 0, pdi = 0;
+            for (int ib = 0; ib < 8; ++ib) {
+                double xr, wb;
+                gauss_pt(8, ib, xr, wb);
+                const float rho = (1.0f + (float)xr) * rho_lim * 0.5f;
+                const float wt = (float)wb * rho_lim * 0.5f * rho;
+                const float u = rho * cf, v = rho * sf, uv = u * v;
+                float rl[3], re[3], ne[3];
+#pragma unroll
+                for (int c = 0; c < 3; ++c) {
+                    rl[c] = q.p[c] + u * q.t1[c] + v * q.t2[c];
+                    re[c] = rl[c] + uv * q.d[c];
+                    ne[c] = q.n0[c] + u * q.nu[c] + v * q.nv[c];
+                }
+                float fsr, fsi, fdr, fdi, lsr, lsi, ldr, ldi;
+                kern32(fam, kf, re, ne, do_s, do_d, fsr, fsi, fdr, fdi);
+                kern32(fam, kf, rl, q.n0, do_s, do_d, lsr, lsi, ldr, ldi);
+                ps += wt * (fsr - lsr);
+                pi += wt * (fsi - lsi);
+                pds += wt * (fdr - ldr);
+                pdi += wt * (fdi - ldi);
+            }
+            sr += wth * ps;
+            si += wth * pi;
+            dsr += wth * pds;
+            dsi += wth * pdi;
+        }
+    }
+    a.sr += sr;
+    a.si += si;
+    a.dr += dsr;
+    a.di += dsi;
+}
+
+// near_telles_sum with the FP32 sums (quads): the Telles coefficients in FP64,
+// the points expanded around the inverse-mapped point
+static __device__ __noinline__ void near_telles_sum_f32(const Elem64 &e, int fam, double k, const double x0[3], const double im[3],
+                                           Acc &a)
+{
+    double dist = im[2];
+    double rb;
+    if (dist < 0.05) rb = 0.0;
+    else if (dist <= 1.3) rb = 0.85 + 0.24 * log(dist);
+    else if (dist <= 3.618) rb = 0.893 + 0.0832 * log(dist);
+    else rb = 1.0;
+    double ca[2], cb[2], cc[2], cdd[2];
+    for (int dim = 0; dim < 2; ++dim) {
+        double eb = im[dim];
+        double f = 1.0 + 2.0 * rb;
+        double qq = 1.0 / (2.0 * f) * ((eb * (3.0 - 2.0 * rb) - 2.0 * eb * eb * eb / f) * 1.0 / f - eb);
+        double p = 1.0 / (3.0 * f * f) * (4.0 * rb * (1.0 - rb) + 3.0 * (1.0 - eb * eb));
+        double s = sqrt(qq * qq + p * p * p);
+        double gb = cbrt(-qq + s) + cbrt(-qq - s) + eb / f;
+        double Q = 1.0 + 3.0 * gb * gb;
+        ca[dim] = (1.0 - rb) / Q;
+        cb[dim] = -3.0 * (1.0 - rb) * gb / Q;
+        cc[dim] = (3.0 * gb * gb + rb) / Q;
+        cdd[dim] = -cb[dim];
+    }
+    QuadAround32 q;
+    quad_around32(e, x0, im[0], im[1], q);
+    float vv[16], tw[16];  // eta - eta0 at the transformed nodes, and their weights
+    for (int b = 0; b < 16; ++b) {
+        double x, w;
+        gauss_pt(16, b, x, w);
+        vv[b] = (float)(ca[1] * x * x * x + cb[1] * x * x + cc[1] * x + cdd[1] - im[1]);
+        tw[b] = (float)(w * (3.0 * ca[1] * x * x + 2.0 * cb[1] * x + cc[1]));
+    }
+    const float kf = (float)k;
+    float sdr = 0, sdi = 0;
+    for (int ia = 0; ia < 16; ++ia) {
+        double x, w;
+        gauss_pt(16, ia, x, w);
+        const float u = (float)(ca[0] * x * x * x + cb[0] * x * x + cc[0] * x + cdd[0] - im[0]);
+        const float w0 = (float)(w * (3.0 * ca[0] * x * x + 2.0 * cb[0] * x + cc[0]));
+        float pr = 0, pim = 0;
+        for (int ib = 0; ib < 16; ++ib) {
+            const float v = vv[ib], uv = u * v;
+            float rv[3], nv[3];
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                rv[c] = q.p[c] + u * q.t1[c] + v * q.t2[c] + uv * q.d[c];
+                nv[c] = q.n0[c] + u * q.nu[c] + v * q.nv[c];
+            }
+            float sr, si, dr, di;
+            kern32(fam, kf, rv, nv, false, true, sr, si, dr, di);
+            pr += dr * tw[ib];
+            pim += di * tw[ib];
+        }
+        sdr += w0 * pr;
+        sdi += w0 * pim;
+    }
+    a.dr += sdr;
+    a.di += sdi;
+}
+
+// the dynamic part K_k - K_0 of near_plane over a flat (linearised) quad in
+// FP32: 8 x 8 Gauss as near_dynamic, points expanded around the centre
+static __device__ __noinline__ void near_dynamic_quad_f32(const Elem64 &e, double k, const double x0[3], bool do_s, bool do_d,
+                                             Acc &a)
+{
+    QuadAround32 q;
+    quad_around32(e, x0, 0.0, 0.0, q);
+    const float J0 = sqrtf(q.n0[0] * q.n0[0] + q.n0[1] * q.n0[1] + q.n0[2] * q.n0[2]);
+    float en[3];
+    for (int c = 0; c < 3; ++c) en[c] = q.n0[c] / J0;  // centre normal (near_dynamic's en)
+    constexpr float INV4PI = (float)INV_FOUR_PI;
+    const float kf = (float)k;
+    float sr = 0, si = 0, dr = 0, di = 0;
+    for (int p = 0; p < 64; ++p) {
+        double xi, eta, w0, w1;
+        gauss_pt(8, p / 8, xi, w0);
+        gauss_pt(8, p % 8, eta, w1);
+        const float u = (float)xi, v = (float)eta, uv = u * v;
+        float rv[3], nv[3];
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            rv[c] = q.p[c] + u * q.t1[c] + v * q.t2[c] + uv * q.d[c];
+            nv[c] = q.n0[c] + u * q.nu[c] + v * q.nv[c];
+        }
+        const float J = sqrtf(nv[0] * nv[0] + nv[1] * nv[1] + nv[2] * nv[2]);
+        const float r2 = rv[0] * rv[0] + rv[1] * rv[1] + rv[2] * rv[2];
+        const float rinv = rsqrtf(r2);
+        const float kr = kf * (r2 * rinv);
+        float sn, cs;
+        sincos_reduced(kr, sn, cs);
+        const float hs = sinf(0.5f * kr);
+        const float cm1 = -2.0f * hs * hs;  // cos kr - 1 without cancellation
+        const float t = (float)(w0 * w1) * J * rinv * INV4PI;
+        if (do_s) {
+            sr += t * cm1;
+            si -= t * sn;
+        }
+        if (do_d) {
+            const float uu = t * rinv * ((rv[0] * en[0] + rv[1] * en[1] + rv[2] * en[2]) * rinv);
+            dr -= uu * (cm1 + kr * sn);
+            di -= uu * (kr * cs - sn);
+        }
+    }
+    a.sr += sr;
+    a.si += si;
+    a.dr += dr;
+    a.di += di;
+}
+
+
 __device__ inline void self_quad(const Elem64 &e, int fam, double k, const double x0[3], bool do_s, bool do_d, Acc &a)
 {
     for (int d = 0; d < 4; ++d) {
