@@ -170,14 +170,14 @@ static void elem_init(elem_t *e, int nc, const double *coords /* nc x 3 */)
 /* ------------------------------------------------------------------ kernels */
 
 /* G(r) (nihu/library/helmholtz_kernel.hpp:180-186, laplace_kernel.hpp:137-141) */
-static cplx green(int fam, double k, double r)
+static cplx green(int fam, cplx k, double r)
 {
     if (fam == FAM_LAPLACE) return 1.0 / r / (4.0 * PI);
     return cexp(-I * (k * r)) / r / (4.0 * PI);
 }
 
 /* dG/dr (nihu/library/helmholtz_kernel.hpp:190-195, laplace_kernel.hpp:143-147) */
-static cplx dgreen(int fam, double k, double r)
+static cplx dgreen(int fam, cplx k, double r)
 {
     if (fam == FAM_LAPLACE) return -1.0 / (r * r) / (4.0 * PI);
     cplx ikr = I * (k * r);
@@ -185,7 +185,7 @@ static cplx dgreen(int fam, double k, double r)
 }
 
 /* SLP kernel G(|y-x|) (nihu/library/normal_derivative_kernel.hpp:131-136) */
-static cplx kern_slp(int fam, double k, const double x[3], const double y[3])
+static cplx kern_slp(int fam, cplx k, const double x[3], const double y[3])
 {
     double rv[3] = {y[0] - x[0], y[1] - x[1], y[2] - x[2]};
     return green(fam, k, norm3(rv));
@@ -193,7 +193,7 @@ static cplx kern_slp(int fam, double k, const double x[3], const double y[3])
 
 /* DLP kernel dG/dr (r_vec.n_y)/r, n_y unit
  * (nihu/library/normal_derivative_kernel.hpp:167-175) */
-static cplx kern_dlp(int fam, double k, const double x[3], const double y[3], const double ny[3])
+static cplx kern_dlp(int fam, cplx k, const double x[3], const double y[3], const double ny[3])
 {
     double rv[3] = {y[0] - x[0], y[1] - x[1], y[2] - x[2]};
     double r = norm3(rv);
@@ -203,7 +203,7 @@ static cplx kern_dlp(int fam, double k, const double x[3], const double y[3], co
 
 /* DLPt kernel dG/dr (-r_vec.n_x)/r, n_x the unit normal at the collocation point
  * (nihu/library/normal_derivative_kernel.hpp:199-206) */
-static cplx kern_dlpt(int fam, double k, const double x[3], const double nx[3], const double y[3])
+static cplx kern_dlpt(int fam, cplx k, const double x[3], const double nx[3], const double y[3])
 {
     double rv[3] = {y[0] - x[0], y[1] - x[1], y[2] - x[2]};
     double r = norm3(rv);
@@ -213,7 +213,7 @@ static cplx kern_dlpt(int fam, double k, const double x[3], const double nx[3], 
 
 /* f[0] = G'' - G'/r, f[1] = G'/r (nihu/library/helmholtz_kernel.hpp:198-205,
  * the Laplace kernel being its k = 0 case) */
-static void ddgreen(int fam, double k, double r, cplx f[2])
+static void ddgreen(int fam, cplx k, double r, cplx f[2])
 {
     cplx ikr = fam == FAM_LAPLACE ? 0.0 : I * (k * r);
     cplx g = cexp(-ikr) / (r * r * r) / (4.0 * PI);
@@ -223,7 +223,7 @@ static void ddgreen(int fam, double k, double r, cplx f[2])
 
 /* HSP kernel f0 (r.n_x)(r.n_y)-terms - f1 n_x.n_y
  * (nihu/library/normal_derivative_kernel.hpp:242-251) */
-static cplx kern_hsp(int fam, double k, const double x[3], const double nx[3], const double y[3], const double ny[3])
+static cplx kern_hsp(int fam, cplx k, const double x[3], const double nx[3], const double y[3], const double ny[3])
 {
     double rv[3] = {y[0] - x[0], y[1] - x[1], y[2] - x[2]};
     double r = norm3(rv);
@@ -235,7 +235,7 @@ static cplx kern_hsp(int fam, double k, const double x[3], const double nx[3], c
 }
 
 /* nx: unit normal at the collocation point (used by DLPt and HSP only) */
-static cplx kern(int fam, int op, double k, const double x[3], const double *nx, const double y[3], const double ny[3])
+static cplx kern(int fam, int op, cplx k, const double x[3], const double *nx, const double y[3], const double ny[3])
 {
     if (op == OP_SLP) return kern_slp(fam, k, x, y);
     if (op == OP_DLP) return kern_dlp(fam, k, x, y, ny);
@@ -288,7 +288,7 @@ static double centre_distance(const elem_t *a, const elem_t *b)
 
 /* sum_q w_q K(x, y_q) J_q over the trial element with the rule of the given
  * degree (nihu/core/double_integral.hpp:445-467 with the accelerator of :576-585) */
-static cplx regular_integral(const elem_t *e, int fam, int op, double k, const double x[3], const double *nx,
+static cplx regular_integral(const elem_t *e, int fam, int op, cplx k, const double x[3], const double *nx,
                              int degree)
 {
     cplx sum = 0.0;
@@ -355,16 +355,16 @@ static double static_self_integral(const elem_t *e, const double x0[3])
 }
 
 /* sinc with the reference's small-argument series (nihu/util/math_functions.hpp:54-61) */
-static double sinc_ref(double x)
+static cplx sinc_ref(cplx x)
 {
-    if (fabs(x) > 1e-3) return sin(x) / x;
+    if (cabs(x) > 1e-3) return csin(x) / x;
     return 1.0 - x * x / 6.0 * (1.0 - x * x / 20.0);
 }
 
 /* constant flat triangle, Helmholtz SLP self term: analytic static part plus
  * the regular dynamic part (e^{-ikr}-1)/r with the degree-7 Dunavant rule
  * (nihu/library/helmholtz_singular_integrals.hpp:703-762) */
-static cplx self_tria_slp(const elem_t *e, int fam, double k)
+static cplx self_tria_slp(const elem_t *e, int fam, cplx k)
 {
     double stat = static_self_integral(e, e->center);
     if (fam == FAM_LAPLACE) return stat / (4.0 * PI);
@@ -387,7 +387,7 @@ static cplx self_tria_slp(const elem_t *e, int fam, double k)
  * Gauss rule of degree 7 (nihu/core/duffy_quadrature.hpp:82-141,
  * nihu/core/singular_accelerator.hpp:440-448, nihu/core/quadrature.hpp:112-130,
  * evaluated as in nihu/core/double_integral.hpp:474-510) */
-static cplx self_quad_duffy(const elem_t *e, int fam, int op, double k)
+static cplx self_quad_duffy(const elem_t *e, int fam, int op, cplx k)
 {
     const int ng = 7 / 2 + 1;
     const double *g = gauss_rule(ng);
@@ -428,7 +428,7 @@ static cplx self_quad_duffy(const elem_t *e, int fam, int op, double k)
 /* the regular remainder (e^{-ikr}(1+ikr) - 1 + (ikr)^2/2) / r^3 of the HSP
  * kernel's expansion, with the reference's series below r = 1e-3
  * (nihu/library/helmholtz_singular_integrals.hpp:768-777) */
-static cplx hsp_dynamic(double r, double k)
+static cplx hsp_dynamic(double r, cplx k)
 {
     cplx ikr = I * (k * r);
     if (fabs(r) > 1e-3) return (cexp(-ikr) * (1.0 + ikr) - 1.0 + ikr * ikr / 2.0) / r / r / r;
@@ -441,7 +441,7 @@ static cplx hsp_dynamic(double r, double k)
  * IG0 (the 1/r integral), sides with theta < 1e-3 skipped, plus the dynamic
  * remainder with the degree-7 Dunavant rule; (IddG0 + k^2/2 IG0 + I_dyn)/(4 pi)
  * (nihu/library/helmholtz_singular_integrals.hpp:764-839) */
-static cplx self_tria_hsp(const elem_t *e, int fam, double k)
+static cplx self_tria_hsp(const elem_t *e, int fam, cplx k)
 {
     double r[4], th[4], al[4];
     plane_element_helper(e, e->center, r, th, al);
@@ -468,7 +468,7 @@ static cplx self_tria_hsp(const elem_t *e, int fam, double k)
  * SLP and HSP shortcuts, DLP and DLPt = 0 on a flat triangle
  * (nihu/library/normal_derivative_singular_integrals.hpp:13-56), quads by Duffy
  * (SLP and DLP only) */
-static cplx self_integral(const elem_t *e, int fam, int op, double k)
+static cplx self_integral(const elem_t *e, int fam, int op, cplx k)
 {
     if (e->nc == 3) {
         if (op == OP_SLP) return self_tria_slp(e, fam, k);
@@ -624,7 +624,7 @@ static double static_near_bm(const elem_t *e, const double x0in[3], const double
  * dynamic part (K_k - K_0) with the degree-14 regular rule (Dunavant 42 points
  * on triangles, 8x8 Gauss on quads)
  * (nihu/library/helmholtz_nearly_singular_integrals.hpp:48-84 SLP, :91-129 DLP) */
-static cplx near_plane(const elem_t *e, int fam, int op, double k, const double x0[3], const double *nx)
+static cplx near_plane(const elem_t *e, int fam, int op, cplx k, const double x0[3], const double *nx)
 {
     double st = (op == OP_DLPT || op == OP_HSP) ? static_near_bm(e, x0, nx, op) : static_near(e, x0, op);
     if (fam == FAM_LAPLACE) return st;
@@ -731,7 +731,7 @@ static void linearized_elem(const elem_t *e, double xi0, double eta0, elem_t *li
     elem_init(lin, e->nc, coords);
 }
 
-static cplx kern_on_elem(const elem_t *e, int fam, int op, double k, const double x0[3], double xi, double eta)
+static cplx kern_on_elem(const elem_t *e, int fam, int op, cplx k, const double x0[3], double xi, double eta)
 {
     double y[3], n[3];
     elem_x(e, xi, eta, y);
@@ -745,7 +745,7 @@ static cplx kern_on_elem(const elem_t *e, int fam, int op, double k, const doubl
  * linearized-element integrand subtracted, plus the planar constant-element
  * shortcut on the linearized element; radial and tangential Gauss order 15
  * (8 points) (nihu/library/nearly_singular_collocational.hpp:87-198) */
-static int near_polar(const elem_t *e, int fam, int op, double k, const double x0[3], cplx *out)
+static int near_polar(const elem_t *e, int fam, int op, cplx k, const double x0[3], cplx *out)
 {
     double im[3];
     if (!inverse_mapping(e, x0, 1e-5, 100, im)) return 0;
@@ -801,7 +801,7 @@ static int near_polar(const elem_t *e, int fam, int op, double k, const double x
 /* Telles (1987) cubic transformation of a tensor Gauss rule towards the image
  * of x0 (nihu/library/telles_1987.hpp:44-113), 16x16 points (order 30)
  * (nihu/library/nearly_singular_collocational_telles.hpp:85-110) */
-static int near_telles(const elem_t *e, int fam, int op, double k, const double x0[3], cplx *out)
+static int near_telles(const elem_t *e, int fam, int op, cplx k, const double x0[3], cplx *out)
 {
     double im[3];
     if (!inverse_mapping(e, x0, 1e-6, 100, im)) return 0;
@@ -848,7 +848,7 @@ static int near_telles(const elem_t *e, int fam, int op, double k, const double 
  * nihu/library/laplace_nearly_singular_integrals.hpp:399-590): constant triangles
  * use the planar semi-analytic scheme; quads use polar subtraction, except
  * Helmholtz DLP which uses Telles */
-static int near_integral(const elem_t *e, int fam, int op, double k, const double x0[3], const double *nx, cplx *out)
+static int near_integral(const elem_t *e, int fam, int op, cplx k, const double x0[3], const double *nx, cplx *out)
 {
     if (e->nc == 3) { *out = near_plane(e, fam, op, k, x0, nx); return 1; }
     if (fam == FAM_HELMHOLTZ && op == OP_DLP) return near_telles(e, fam, op, k, x0, out);
@@ -892,7 +892,7 @@ static void unit_normal_center(const elem_t *e, double n[3])
     for (int d = 0; d < 3; ++d) n[d] /= nn;
 }
 
-static int entry(const elem_t *te, const elem_t *re, int same_id, int fam, int op, double k, cplx *out)
+static int entry(const elem_t *te, const elem_t *re, int same_id, int fam, int op, cplx k, cplx *out)
 {
     double nx[3];
     if (op == OP_DLPT || op == OP_HSP) {
@@ -929,9 +929,10 @@ static int entry(const elem_t *te, const elem_t *re, int same_id, int fam, int o
  */
 int oracle_assemble(const double *tnodes, int tn_nodes, const int *telems, int tn_elems, int tcols,
                     const double *rnodes, int rn_nodes, const int *relems, int rn_elems, int rcols,
-                    int same_mesh, int fam, int op, double k, double alpha_re, double alpha_im,
+                    int same_mesh, int fam, int op, double k_re, double k_im, double alpha_re, double alpha_im,
                     int row_begin, int row_end, int col_begin, int col_end, double *out, long ld, int accumulate)
 {
+    const cplx k = k_re + I * k_im;  /* complex for a lossy medium (nihu/library/helmholtz_kernel.hpp:42-54) */
     if (row_begin < 0 || row_end > tn_elems || row_begin > row_end) { snprintf(g_err, sizeof g_err, "bad row range"); return 0; }
     if (col_begin < 0 || col_end > rn_elems || col_begin > col_end) { snprintf(g_err, sizeof g_err, "bad column range"); return 0; }
     cplx alpha = alpha_re + I * alpha_im;
@@ -964,9 +965,10 @@ int oracle_assemble(const double *tnodes, int tn_nodes, const int *telems, int t
  */
 int oracle_assemble_pairs(const double *tnodes, int tn_nodes, const int *telems, int tn_elems, int tcols,
                           const double *rnodes, int rn_nodes, const int *relems, int rn_elems, int rcols,
-                          int same_mesh, int fam, int op, double k, long n, const int *rows, const int *cols,
-                          double *out)
+                          int same_mesh, int fam, int op, double k_re, double k_im, long n, const int *rows,
+                          const int *cols, double *out)
 {
+    const cplx k = k_re + I * k_im;
     for (long p = 0; p < n; ++p) {
         int i = rows[p], j = cols[p];
         if (i < 0 || i >= tn_elems || j < 0 || j >= rn_elems) {
@@ -990,7 +992,7 @@ int oracle_assemble_pairs(const double *tnodes, int tn_nodes, const int *telems,
  * elements, every test point against every trial point, constant shape
  * functions (nihu/core/double_integral.hpp:175-202 with the diadic dual
  * accelerator of :300-312) */
-static cplx galerkin_regular(const elem_t *te, const elem_t *re, int fam, int op, double k, int degree)
+static cplx galerkin_regular(const elem_t *te, const elem_t *re, int fam, int op, cplx k, int degree)
 {
     double tx[64][3], tw[64], ty[64][3], tn[64][3], rw[64];
     int nt = 0, nr = 0;
@@ -1142,7 +1144,7 @@ static void tri_rotate(const int perm[3], double xi, double eta, double *oxi, do
  * rotated so that its first common node sits at corner 0, the trial rule so
  * that the common edge runs the opposite way (edge) or its common node sits
  * at corner 0 (corner) (nihu/core/singular_accelerator.hpp:270-310) */
-static cplx galerkin_singular(const elem_t *te, const elem_t *re, int fam, int op, double k, int match, int ind1,
+static cplx galerkin_singular(const elem_t *te, const elem_t *re, int fam, int op, cplx k, int match, int ind1,
                               int ind2)
 {
     if (!g_gal_count[match]) gal_build(match);
@@ -1272,7 +1274,7 @@ static void quad_rotate(const int perm[4], double u, double v, double *ou, doubl
 
 /* singular Galerkin integral of a matched quad pair (rotations as for
  * triangles: nihu/core/singular_accelerator.hpp:270-310) */
-static cplx galerkin_singular_quad(const elem_t *te, const elem_t *re, int fam, int op, double k, int match, int ind1,
+static cplx galerkin_singular_quad(const elem_t *te, const elem_t *re, int fam, int op, cplx k, int match, int ind1,
                                    int ind2)
 {
     if (!g_galq_count[match]) galq_build(match);
@@ -1313,7 +1315,7 @@ int oracle_galerkin_quad_rule(int match, double *out)
  * the same element of one mesh, edge / corner match for triangles of one mesh
  * sharing 2 / 1 nodes, otherwise the regular rule of degree C + interval(d/D) */
 static int galerkin_entry(const elem_t *te, const elem_t *re, const int *tn, const int *rn, int same_mesh, int same_id,
-                          int fam, int op, double k, cplx *out)
+                          int fam, int op, cplx k, cplx *out)
 {
     if (op != OP_SLP && op != OP_DLP) {
         snprintf(g_err, sizeof g_err, "Galerkin: SLP and DLP only");
@@ -1351,10 +1353,11 @@ static int galerkin_entry(const elem_t *te, const elem_t *re, const int *tn, con
  * with the conventions of oracle_assemble (nihu/core/assembly.hpp:69-76) */
 int oracle_assemble_galerkin(const double *tnodes, int tn_nodes, const int *telems, int tn_elems, int tcols,
                              const double *rnodes, int rn_nodes, const int *relems, int rn_elems, int rcols,
-                             int same_mesh, int fam, int op, double k, double alpha_re, double alpha_im,
-                             int row_begin, int row_end, int col_begin, int col_end, double *out, long ld,
-                             int accumulate)
+                             int same_mesh, int fam, int op, double k_re, double k_im, double alpha_re,
+                             double alpha_im, int row_begin, int row_end, int col_begin, int col_end, double *out,
+                             long ld, int accumulate)
 {
+    const cplx k = k_re + I * k_im;
     if (row_begin < 0 || row_end > tn_elems || row_begin > row_end) { snprintf(g_err, sizeof g_err, "bad row range"); return 0; }
     if (col_begin < 0 || col_end > rn_elems || col_begin > col_end) { snprintf(g_err, sizeof g_err, "bad column range"); return 0; }
     cplx alpha = alpha_re + I * alpha_im;
@@ -1405,8 +1408,9 @@ int oracle_elem_geometry(const double *coords, int nc, double *out7)
  * degree), 1 nearly singular dispatch, 2 self, 3 planar near-singular scheme
  * (constant-plane formula even on quads). out = (re, im). */
 int oracle_elem_integral_nx(const double *coords, int nc, const double *x0, const double *nx, int fam, int op,
-                            double k, int kind, int degree, double *out)
+                            double k_re, double k_im, int kind, int degree, double *out)
 {
+    const cplx k = k_re + I * k_im;
     elem_t e;
     elem_init(&e, nc, coords);
     cplx v = 0.0;
@@ -1421,11 +1425,11 @@ int oracle_elem_integral_nx(const double *coords, int nc, const double *x0, cons
 }
 
 /* the same for SLP and DLP (no normal at the collocation point) */
-int oracle_elem_integral(const double *coords, int nc, const double *x0, int fam, int op, double k,
-                         int kind, int degree, double *out)
+int oracle_elem_integral(const double *coords, int nc, const double *x0, int fam, int op, double k_re,
+                         double k_im, int kind, int degree, double *out)
 {
     if (op != OP_SLP && op != OP_DLP) return 0;
-    return oracle_elem_integral_nx(coords, nc, x0, NULL, fam, op, k, kind, degree, out);
+    return oracle_elem_integral_nx(coords, nc, x0, NULL, fam, op, k_re, k_im, kind, degree, out);
 }
 
 /* per-pair quadrature degree of one operator for tests: -1 self, -2 near */

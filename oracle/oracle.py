@@ -42,14 +42,15 @@ def lib():
             dp, ip = ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_int)
             c_int, c_double, c_long = ctypes.c_int, ctypes.c_double, ctypes.c_long
             L.oracle_assemble.argtypes = [dp, c_int, ip, c_int, c_int, dp, c_int, ip, c_int, c_int,
-                                          c_int, c_int, c_int, c_double, c_double, c_double,
+                                          c_int, c_int, c_int, c_double, c_double, c_double, c_double,
                                           c_int, c_int, c_int, c_int, dp, c_long, c_int]
             L.oracle_assemble.restype = c_int
             L.oracle_assemble_pairs.argtypes = [dp, c_int, ip, c_int, c_int, dp, c_int, ip, c_int, c_int,
-                                                c_int, c_int, c_int, c_double, ctypes.c_long, ip, ip, dp]
+                                                c_int, c_int, c_int, c_double, c_double, ctypes.c_long, ip, ip, dp]
             L.oracle_assemble_pairs.restype = c_int
             L.oracle_assemble_galerkin.argtypes = [dp, c_int, ip, c_int, c_int, dp, c_int, ip, c_int, c_int, c_int,
-                                                   c_int, c_int, c_double, c_double, c_double, c_int, c_int, c_int,
+                                                   c_int, c_int, c_double, c_double, c_double, c_double, c_int, c_int,
+                                                   c_int,
                                                    c_int, dp, ctypes.c_long, c_int]
             L.oracle_assemble_galerkin.restype = c_int
             L.oracle_galerkin_rule.argtypes = [c_int, dp]
@@ -59,9 +60,10 @@ def lib():
             L.oracle_classify.argtypes = [dp, c_int, ip, c_int, c_int, dp, c_int, ip, c_int, c_int,
                                           c_int, c_int, c_int, ip]
             L.oracle_classify.restype = c_int
-            L.oracle_elem_integral.argtypes = [dp, c_int, dp, c_int, c_int, c_double, c_int, c_int, dp]
+            L.oracle_elem_integral.argtypes = [dp, c_int, dp, c_int, c_int, c_double, c_double, c_int, c_int, dp]
             L.oracle_elem_integral.restype = c_int
-            L.oracle_elem_integral_nx.argtypes = [dp, c_int, dp, dp, c_int, c_int, c_double, c_int, c_int, dp]
+            L.oracle_elem_integral_nx.argtypes = [dp, c_int, dp, dp, c_int, c_int, c_double, c_double, c_int, c_int,
+                                                  dp]
             L.oracle_elem_integral_nx.restype = c_int
             L.oracle_degree.argtypes = [dp, c_int, ip, c_int, c_int, dp, c_int, ip, c_int, c_int,
                                         c_int, c_int, c_int, c_int, ip]
@@ -101,7 +103,7 @@ def assemble(test_mesh, trial_mesh, family, op, k, same_mesh=None, rows=None, al
     def work(a, b):
         buf = np.zeros((b - a, n), dtype=np.complex128, order="F")
         ptr = ctypes.cast(buf.ctypes.data, ctypes.POINTER(ctypes.c_double))
-        ok = L.oracle_assemble(*targs, *rargs, int(same_mesh), family, op, float(k), alpha.real, alpha.imag,
+        ok = L.oracle_assemble(*targs, *rargs, int(same_mesh), family, op, complex(k).real, complex(k).imag, alpha.real, alpha.imag,
                                a, b, c0, c1, ptr, b - a, 0)
         if not ok:
             errors.append(RuntimeError(L.oracle_last_error().decode()))
@@ -138,7 +140,7 @@ def assemble_galerkin(test_mesh, trial_mesh, family, op, k, same_mesh=None, rows
 
     def work(a, b):
         buf = np.zeros((b - a, n), dtype=np.complex128, order="F")
-        ok = L.oracle_assemble_galerkin(*targs, *rargs, int(same_mesh), family, op, float(k), alpha.real, alpha.imag,
+        ok = L.oracle_assemble_galerkin(*targs, *rargs, int(same_mesh), family, op, complex(k).real, complex(k).imag, alpha.real, alpha.imag,
                                         a, b, 0, n, ctypes.cast(buf.ctypes.data, ctypes.POINTER(ctypes.c_double)),
                                         b - a, 0)
         if not ok:
@@ -187,7 +189,7 @@ def assemble_pairs(test_mesh, trial_mesh, family, op, k, rows, cols, same_mesh=N
 
     def work(a, b):
         buf = np.zeros(b - a, dtype=np.complex128)
-        ok = L.oracle_assemble_pairs(*targs, *rargs, int(same_mesh), family, op, float(k), b - a,
+        ok = L.oracle_assemble_pairs(*targs, *rargs, int(same_mesh), family, op, complex(k).real, complex(k).imag, b - a,
                                      _ptr(rows[a:b], ctypes.c_int), _ptr(cols[a:b], ctypes.c_int),
                                      ctypes.cast(buf.ctypes.data, ctypes.POINTER(ctypes.c_double)))
         if not ok:
@@ -229,12 +231,12 @@ def elem_integral(coords, x0, family, op, k, kind, degree=0, nx=None):
     out = np.zeros(2)
     if nx is None:
         ok = lib().oracle_elem_integral(_ptr(coords, ctypes.c_double), coords.shape[0], _ptr(x0, ctypes.c_double),
-                                        family, op, float(k), kind, degree, _ptr(out, ctypes.c_double))
+                                        family, op, complex(k).real, complex(k).imag, kind, degree, _ptr(out, ctypes.c_double))
     else:
         nx = np.ascontiguousarray(nx, dtype=np.float64)
         ok = lib().oracle_elem_integral_nx(_ptr(coords, ctypes.c_double), coords.shape[0],
                                            _ptr(x0, ctypes.c_double), _ptr(nx, ctypes.c_double), family, op,
-                                           float(k), kind, degree, _ptr(out, ctypes.c_double))
+                                           complex(k).real, complex(k).imag, kind, degree, _ptr(out, ctypes.c_double))
     if not ok:
         raise RuntimeError("element integral failed")
     return complex(out[0], out[1])
