@@ -156,6 +156,16 @@ nihu_gb_status nihu_gb_assemble(nihu_gb_ctx *ctx, const nihu_gb_mesh *test, cons
                                 int precision, int dtype, void *out_slp, void *out_dlp, int64_t ld,
                                 int accumulate, int where);
 
+/* nihu_gb_assemble() for a complex wave number k + i k_im: a lossy medium
+ * (k_im < 0 damps e^{-ikr} as e^{k_im r}), as the reference's kernels take a
+ * complex WaveNumber type (nihu/library/helmholtz_kernel.hpp:42-54).
+ * k_im = 0 is nihu_gb_assemble() itself; a nonzero k_im runs separate kernel
+ * instantiations (the nearly singular and self terms in FP64 in both
+ * precision modes) and is ignored for the Laplace family. */
+nihu_gb_status nihu_gb_assemble_c(nihu_gb_ctx *ctx, const nihu_gb_mesh *test, const nihu_gb_mesh *trial, int family,
+                                  int ops, double k, double k_im, double alpha_re, double alpha_im, int precision,
+                                  int dtype, void *out_slp, void *out_dlp, int64_t ld, int accumulate, int where);
+
 /* out(i, i) += alpha for every element i (collocational identity operator on
  * constant elements, nihu/core/single_integral.hpp:146-180).  The matrix is
  * n x n with n = number of mesh elements. */
@@ -408,6 +418,12 @@ nihu_gb_status nihu_gb_lu_solve(nihu_gb_ctx *ctx, void *A, int64_t n, int64_t ld
 nihu_gb_status nihu_gb_solve_cbie(nihu_gb_ctx *ctx, const nihu_gb_mesh *mesh, int family, double k,
                                   int precision, int dtype, const void *q, void *p, int solver,
                                   int restart, int max_iters, double tol, int *iters, double *rel_residual);
+
+/* nihu_gb_solve_cbie() for a complex wave number k + i k_im (a lossy medium;
+ * the assembly of nihu_gb_assemble_c()). */
+nihu_gb_status nihu_gb_solve_cbie_c(nihu_gb_ctx *ctx, const nihu_gb_mesh *mesh, int family, double k, double k_im,
+                                    int precision, int dtype, const void *q, void *p, int solver, int restart,
+                                    int max_iters, double tol, int *iters, double *rel_residual);
 
 /* Burton-Miller exterior solve A p = B q (matrices of
  * nihu_gb_assemble_burton_miller) by GMRES (solver 0) or LU (solver 1,

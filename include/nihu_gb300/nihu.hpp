@@ -202,12 +202,20 @@ inline dirac_space dirac(function_space const &s) { return dirac_space(s); }
 struct kernel_desc {
     int family, op;
     double k;
+    double k_im = 0.0;  // imaginary part of a complex (lossy) wave number
 };
 
+namespace detail {
+// the wave number as (k, k_im): double, or std::complex<double> as the
+// reference's WaveNumber template parameter allows (nihu/library/helmholtz_kernel.hpp:42-54)
+inline kernel_desc with_k(int family, int op, double k) { return {family, op, k, 0.0}; }
+inline kernel_desc with_k(int family, int op, std::complex<double> k) { return {family, op, k.real(), k.imag()}; }
+}  // namespace detail
+
 template <class WaveNumber = double>
-inline kernel_desc helmholtz_3d_SLP_kernel(WaveNumber k) { return {NIHU_GB_HELMHOLTZ_3D, NIHU_GB_SLP, (double)k}; }
+inline kernel_desc helmholtz_3d_SLP_kernel(WaveNumber k) { return detail::with_k(NIHU_GB_HELMHOLTZ_3D, NIHU_GB_SLP, k); }
 template <class WaveNumber = double>
-inline kernel_desc helmholtz_3d_DLP_kernel(WaveNumber k) { return {NIHU_GB_HELMHOLTZ_3D, NIHU_GB_DLP, (double)k}; }
+inline kernel_desc helmholtz_3d_DLP_kernel(WaveNumber k) { return detail::with_k(NIHU_GB_HELMHOLTZ_3D, NIHU_GB_DLP, k); }
 inline kernel_desc laplace_3d_SLP_kernel() { return {NIHU_GB_LAPLACE_3D, NIHU_GB_SLP, 0.0}; }
 inline kernel_desc laplace_3d_DLP_kernel() { return {NIHU_GB_LAPLACE_3D, NIHU_GB_DLP, 0.0}; }
 // Burton-Miller kernels (nihu/library/helmholtz_kernel.hpp:326-334): constant
@@ -318,13 +326,21 @@ Res &operator<<(Res &result, weighted_residual<TS> const &wr)
     if (kop == NIHU_GB_SLP || kop == NIHU_GB_DLP) {
         void *out_s = kop == NIHU_GB_SLP ? (void *)result.data() : nullptr;
         void *out_d = kop == NIHU_GB_DLP ? (void *)result.data() : nullptr;
-        auto fn = galerkin ? nihu_gb_assemble_galerkin : nihu_gb_assemble;
-        check(ctx.handle(), fn(ctx.handle(), tmh, rmh, op.kernel.family, kop, op.kernel.k, op.scale.real(),
-                               op.scale.imag(), wr.precision, detail::storage<T>::dtype, out_s, out_d, m, 1,
-                               NIHU_GB_HOST));
+        if (op.kernel.k_im != 0.0) {
+            if (galerkin) throw std::invalid_argument("complex wave numbers: collocation SLP and DLP only");
+            check(ctx.handle(), nihu_gb_assemble_c(ctx.handle(), tmh, rmh, op.kernel.family, kop, op.kernel.k,
+                                                   op.kernel.k_im, op.scale.real(), op.scale.imag(), wr.precision,
+                                                   detail::storage<T>::dtype, out_s, out_d, m, 1, NIHU_GB_HOST));
+        } else {
+            auto fn = galerkin ? nihu_gb_assemble_galerkin : nihu_gb_assemble;
+            check(ctx.handle(), fn(ctx.handle(), tmh, rmh, op.kernel.family, kop, op.kernel.k, op.scale.real(),
+                                   op.scale.imag(), wr.precision, detail::storage<T>::dtype, out_s, out_d, m, 1,
+                                   NIHU_GB_HOST));
+        }
     } else if (galerkin) {
         throw std::invalid_argument("Galerkin formalism: SLP and DLP kernels only");
     } else {
+        if (op.kernel.k_im != 0.0) throw std::invalid_argument("complex wave numbers: collocation SLP and DLP only");
         void *out_t = kop == NIHU_GB_DLPT ? (void *)result.data() : nullptr;
         void *out_h = kop == NIHU_GB_HSP ? (void *)result.data() : nullptr;
         check(ctx.handle(), nihu_gb_assemble_bm(ctx.handle(), tmh, rmh, op.kernel.family, kop, op.kernel.k,

@@ -49,6 +49,7 @@ SIGNATURES = {
     "nihu_gb_mesh_destroy": (None, [_vp]),
     "nihu_gb_mesh_num_elements": (_i64, [_vp]),
     "nihu_gb_assemble": (_i, [_vp, _vp, _vp, _i, _i, _d, _d, _d, _i, _i, _vp, _vp, _i64, _i, _i]),
+    "nihu_gb_assemble_c": (_i, [_vp, _vp, _vp, _i, _i, _d, _d, _d, _d, _i, _i, _vp, _vp, _i64, _i, _i]),
     "nihu_gb_add_identity": (_i, [_vp, _vp, _d, _d, _i, _vp, _i64, _i]),
     "nihu_gb_pair_statistics": (_i, [_vp, _vp, _vp, ctypes.POINTER(ctypes.c_int64)]),
     "nihu_gb_matvec": (_i, [_vp, _i, _vp, _i64, _i64, _i64, _vp, _vp, _d, _d, _d, _d, _i]),
@@ -72,6 +73,7 @@ SIGNATURES = {
     "nihu_gb_server_step": (_i, [_vp, _ip, _ip, _ip]),
     "nihu_gb_server_take": (_i, [_vp, ctypes.POINTER(ctypes.c_int64), _vp, _i64, _ip, _dp, _ip]),
     "nihu_gb_solve_cbie": (_i, [_vp, _vp, _i, _d, _i, _i, _vp, _vp, _i, _i, _i, _d, _ip, _dp]),
+    "nihu_gb_solve_cbie_c": (_i, [_vp, _vp, _i, _d, _d, _i, _i, _vp, _vp, _i, _i, _i, _d, _ip, _dp]),
     "nihu_gb_assemble_galerkin": (_i, [_vp, _vp, _vp, _i, _i, _d, _d, _d, _i, _i, _vp, _vp, _i64, _i, _i]),
     "nihu_gb_add_mass": (_i, [_vp, _vp, _d, _d, _i, _vp, _i64, _i]),
     "nihu_gb_assemble_bm": (_i, [_vp, _vp, _vp, _i, _i, _d, _d, _d, _i, _i, _vp, _vp, _i64, _i, _i]),

@@ -195,10 +195,16 @@ def dirac(space: FunctionSpace) -> DiracSpace:
 
 
 class Kernel:
-    def __init__(self, family: int, op: int, k: float = 0.0, name: str = ""):
-        self.family, self.op, self.k, self.name = family, op, float(k), name
+    """A kernel with its wave number: real, or complex for a lossy medium (the
+    reference's kernels take a complex WaveNumber type,
+    nihu/library/helmholtz_kernel.hpp:42-54)."""
 
-    def get_wave_number(self) -> float:
+    def __init__(self, family: int, op: int, k: complex = 0.0, name: str = ""):
+        kc = complex(k)
+        self.family, self.op, self.name = family, op, name
+        self.k = kc.real if kc.imag == 0 else kc
+
+    def get_wave_number(self):
         return self.k
 
 
@@ -357,12 +363,22 @@ def _assemble_into(ctx, result, test_mesh, trial_mesh, family, op, k, alpha, pre
     if op in (C.SLP, C.DLP):
         out_s = buf.ctypes.data if op == C.SLP else None
         out_d = buf.ctypes.data if op == C.DLP else None
-        fn = L.nihu_gb_assemble_galerkin if galerkin else L.nihu_gb_assemble
-        ctx.check(fn(ctx.handle, tdm.handle, rdm_handle, family, op, k, alpha.real, alpha.imag, prec,
-                     dtype, out_s, out_d, max(result.shape[0], 1), accumulate, C.HOST))
+        kc = complex(k)
+        if kc.imag != 0 and not galerkin:
+            ctx.check(L.nihu_gb_assemble_c(ctx.handle, tdm.handle, rdm_handle, family, op, kc.real, kc.imag,
+                                           alpha.real, alpha.imag, prec, dtype, out_s, out_d,
+                                           max(result.shape[0], 1), accumulate, C.HOST))
+        else:
+            if kc.imag != 0:
+                raise NotImplementedError("complex wave numbers: collocation SLP and DLP only")
+            fn = L.nihu_gb_assemble_galerkin if galerkin else L.nihu_gb_assemble
+            ctx.check(fn(ctx.handle, tdm.handle, rdm_handle, family, op, kc.real, alpha.real, alpha.imag, prec,
+                         dtype, out_s, out_d, max(result.shape[0], 1), accumulate, C.HOST))
     elif galerkin:
         raise NotImplementedError("Galerkin formalism: SLP and DLP kernels only")
     else:
+        if complex(k).imag != 0:
+            raise NotImplementedError("complex wave numbers: collocation SLP and DLP only")
         out_t = buf.ctypes.data if op == C.DLPT else None
         out_h = buf.ctypes.data if op == C.HSP else None
         ctx.check(L.nihu_gb_assemble_bm(ctx.handle, tdm.handle, rdm_handle, family, op, k, alpha.real, alpha.imag,
@@ -465,10 +481,11 @@ def solve_cbie(mesh: Mesh, k: float, q, family: int = C.HELMHOLTZ_3D, dtype: int
     p = np.zeros_like(q)
     it, res = ctypes.c_int(0), ctypes.c_double(0.0)
     dm = mesh.device(ctx)
-    st = C.lib().nihu_gb_solve_cbie(ctx.handle, dm.handle, family, k,
-                                    C.REGULAR_FP64 if precision == "fp64" else C.REGULAR_FP32, dtype,
-                                    q.ctypes.data, p.ctypes.data, 0 if solver == "gmres" else 1, restart,
-                                    max_iters, tol, ctypes.byref(it), ctypes.byref(res))
+    kc = complex(k)  # a complex k is a lossy medium
+    st = C.lib().nihu_gb_solve_cbie_c(ctx.handle, dm.handle, family, kc.real, kc.imag,
+                                      C.REGULAR_FP64 if precision == "fp64" else C.REGULAR_FP32, dtype,
+                                      q.ctypes.data, p.ctypes.data, 0 if solver == "gmres" else 1, restart,
+                                      max_iters, tol, ctypes.byref(it), ctypes.byref(res))
     if st != C.OK and (check or st != 6):
         ctx.check(st)
     return p, it.value, res.value

@@ -171,7 +171,10 @@ constexpr float Q_FAR = 249.64f * (1.0f + 1e-4f);
 // RHS: right-hand-side mode (BATCH only; the SLP entries go into the row sums)
 // PLAIN: unit scale and no accumulation (single wave number, FP32), so the
 // stores carry no run-time checks
-template <typename R, typename Out, int FAM, int OPS, bool BATCH, bool RHS = false, bool PLAIN = false>
+// CK: a complex (lossy) wave number k + i k_im (single wave number, Helmholtz;
+// its own instantiation, so the real-k kernels carry none of it)
+template <typename R, typename Out, int FAM, int OPS, bool BATCH, bool RHS = false, bool PLAIN = false,
+          bool CK = false>
 __global__ void __launch_bounds__(REG_THREADS) k_regular(RegularArgs a)
 {
     using R2 = Cplx<R>;
@@ -228,16 +231,24 @@ __global__ void __launch_bounds__(REG_THREADS) k_regular(RegularArgs a)
 
     const float4 ih = test.chi[ii], il = test.clo[ii];
     const int par = il.w != 0.0f ? 1 : 0;
-    R k, are, aim;
+    R k, are, aim, kim;
     if constexpr (sizeof(R) == 4) {
+        kim = a.k_im32;
         k = a.k32;
         are = a.alpha_re32;
         aim = a.alpha_im32;
     } else {
+        kim = a.k_im;
         k = a.k;
         are = a.alpha_re;
         aim = a.alpha_im;
     }
+    (void)kim;
+    // one quadrature point of the single wave number paths
+    auto ev = [&](R rx, R ry, R rz, R wj, R nx, R ny, R nz, R ws, R wd, R &sr, R &si, R &dr, R &di) {
+        if constexpr (CK) eval_point_ck<R>(rx, ry, rz, wj, nx, ny, nz, k, kim, ws, wd, sr, si, dr, di);
+        else eval_point<FAM, R>(rx, ry, rz, wj, nx, ny, nz, k, ws, wd, sr, si, dr, di);
+    };
     const bool unit_alpha = a.unit_alpha != 0;
     const int accumulate = a.accumulate;
     R x0, x1, x2;
@@ -305,7 +316,7 @@ __global__ void __launch_bounds__(REG_THREADS) k_regular(RegularArgs a)
                     else freqs(std::false_type{});
                 } else {
                     R sr = 0, si = 0, dr = 0, di = 0;
-                    eval_point<FAM, float>(fx, fy, fz, p.x, p.y, p.z, p.w, k, R(DO_S), R(DO_D), sr, si, dr, di);
+                    ev(fx, fy, fz, p.x, p.y, p.z, p.w, R(DO_S), R(DO_D), sr, si, dr, di);
                     if (row_ok) {
                         if (DO_S) put(ps, sr, si);
                         if (DO_D) put(pd, dr, di);
@@ -331,15 +342,13 @@ __global__ void __launch_bounds__(REG_THREADS) k_regular(RegularArgs a)
                     const int64_t base = ((int64_t)j * 2 + par) * SLOTS;
                     R sr = 0, si = 0, dr = 0, di = 0;
                     const float4 yc = __ldg(trial.pts32 + 2 * base), nc = __ldg(trial.pts32 + 2 * base + 1);
-                    eval_point<FAM, float>(mx, my, mz, yc.w, nc.x, nc.y, nc.z, k, R(1), d_far ? R(1) : R(0), sr, si,
-                                           dr, di);
+                    ev(mx, my, mz, yc.w, nc.x, nc.y, nc.z, R(1), d_far ? R(1) : R(0), sr, si, dr, di);
                     if (!d_far) {
                         const int npd = level_npts(s_nc[c], par, 1);
                         for (int q = 0; q < npd; ++q) {
                             const int64_t sl = base + level_slot0(1) + q;
                             const float4 y = __ldg(trial.pts32 + 2 * sl), n = __ldg(trial.pts32 + 2 * sl + 1);
-                            eval_point<FAM, float>(mx + y.x, my + y.y, mz + y.z, y.w, n.x, n.y, n.z, k, R(0), R(1), sr,
-                                                   si, dr, di);
+                            ev(mx + y.x, my + y.y, mz + y.z, y.w, n.x, n.y, n.z, R(0), R(1), sr, si, dr, di);
                         }
                     }
                     put(ps, sr, si);
@@ -429,12 +438,10 @@ __global__ void __launch_bounds__(REG_THREADS) k_regular(RegularArgs a)
                     const float4 n = __ldg(trial.pts32 + 2 * (base + slot) + 1);
                     // r = (c_j - x) + (y - c_j): the hi/lo centre difference plus the
                     // point's offset from the trial centre
-                    eval_point<FAM, float>(dx + y.x, dy + y.y, dz + y.z, y.w, n.x, n.y, n.z, k, ws, wd, sr, si, dr,
-                                           di);
+                    ev(dx + y.x, dy + y.y, dz + y.z, y.w, n.x, n.y, n.z, ws, wd, sr, si, dr, di);
                 } else {
                     const double *y = trial.pts64 + 8 * (base + slot);
-                    eval_point<FAM, double>(y[0] - x0, y[1] - x1, y[2] - x2, y[3], y[4], y[5], y[6], k, ws, wd, sr,
-                                            si, dr, di);
+                    ev(y[0] - x0, y[1] - x1, y[2] - x2, y[3], y[4], y[5], y[6], ws, wd, sr, si, dr, di);
                 }
             }
             if (DO_S) put(ps, sr, si);
@@ -503,6 +510,15 @@ static void launch_ops(const RegularArgs &a, dim3 grid, cudaStream_t s)
         if (a.rhs_part) {
             const size_t smem = sizeof(Cplx<R>) * rhs_fmax_of<R>(a) * (REG_COLS + REG_THREADS);
             k_regular<R, Out, FAM, OP_SLP | OP_DLP, true, true><<<grid, REG_THREADS, smem, s>>>(a);
+            return;
+        }
+    }
+    if constexpr (!BATCH && FAM == FAM_HELMHOLTZ) {
+        if (a.k_im != 0.0) {
+            if (a.ops == OP_SLP) k_regular<R, Out, FAM, OP_SLP, false, false, false, true><<<grid, REG_THREADS, 0, s>>>(a);
+            else if (a.ops == OP_DLP)
+                k_regular<R, Out, FAM, OP_DLP, false, false, false, true><<<grid, REG_THREADS, 0, s>>>(a);
+            else k_regular<R, Out, FAM, OP_SLP | OP_DLP, false, false, false, true><<<grid, REG_THREADS, 0, s>>>(a);
             return;
         }
     }

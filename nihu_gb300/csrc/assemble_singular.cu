@@ -256,6 +256,72 @@ __device__ void self_tria(const Elem64 &e, int fam, double k, const double x0[3]
     // DLP of a flat triangle over itself is zero
 }
 
+// self term of a constant triangle, complex (lossy) wave number: the static
+// part as self_tria, the dynamic (e^{-ikr} - 1)/r on the same 13 points,
+// written as expm1(k.im r) cos(k.re r) - 2 sin^2(k.re r / 2) - i e^{k.im r} sin(k.re r)
+__device__ void self_tria_ck(const Elem64 &e, int fam, cd k, const double x0[3], Acc &a)
+{
+    double st = self_static(e, x0);
+    double dr = 0.0, di = 0.0;
+    if (fam == FAM_HELMHOLTZ) {
+        double e1[3], e2[3], nt[3];
+        for (int d = 0; d < 3; ++d) { e1[d] = e.c[1][d] - e.c[0][d]; e2[d] = e.c[2][d] - e.c[0][d]; }
+        cross3(e1, e2, nt);
+        const double J = norm3(nt);
+        for (int p = 0; p < 13; ++p) {
+            double xi, eta, w;
+            tri_pt(7, p, xi, eta, w);
+            double rv[3];
+            for (int d = 0; d < 3; ++d) rv[d] = e.c[0][d] + xi * e1[d] + eta * e2[d] - x0[d];
+            const double r = norm3(rv);
+            double sn, cs, sh, ch;
+            sincos(k.re * r, &sn, &cs);
+            sincos(0.5 * k.re * r, &sh, &ch);
+            const double em1_re = expm1(k.im * r) * cs - 2.0 * sh * sh, em1_im = -exp(k.im * r) * sn;
+            const double wj = w * J / r;
+            dr += em1_re * wj;
+            di += em1_im * wj;
+        }
+    }
+    a.sr += (st + dr) * INV_FOUR_PI;
+    a.si += di * INV_FOUR_PI;
+}
+
+// one nearly singular or self pair with a complex (lossy) wave number: the
+// FP64 schemes with the complex kernel, in both precision modes
+__device__ bool pair_ck(const RegularArgs &a, const Elem64 &e, const double x0[3], bool self, int j, bool do_s,
+                        bool do_d, Acc &acc)
+{
+    const int fam = a.family;
+    const cd kc{a.k, a.k_im};
+    if (self) {
+        if (e.nc == 3) {
+            if (do_s) self_tria_ck(e, fam, kc, x0, acc);
+        } else {
+            self_quad(e, fam, kc, x0, do_s, do_d, acc);
+        }
+        return true;
+    }
+    if (e.nc == 3) {
+        if (fam == FAM_HELMHOLTZ) near_dynamic_ck(e, kc, x0, do_s, do_d, acc, a.trial.dyn42 + 42 * (int64_t)j);
+        near_static(e, x0, do_s, do_d, acc);
+        return true;
+    }
+    const bool telles = fam == FAM_HELMHOLTZ && do_d;
+    const bool polar_d = fam == FAM_LAPLACE && do_d;
+    double r5[3] = {0, 0, 0}, r6[3] = {0, 0, 0};
+    if (!inverse_mapping(e, x0, telles, r5, r6)) return false;
+    if (do_s || polar_d) {
+        Elem64 lin;
+        linearized(e, r5[0], r5[1], lin);
+        near_polar_sum(e, lin, fam, kc, x0, r5[0], r5[1], do_s, polar_d, acc);
+        if (fam == FAM_HELMHOLTZ) near_dynamic_ck(lin, kc, x0, do_s, polar_d, acc, nullptr);
+        near_static(lin, x0, do_s, polar_d, acc);
+    }
+    if (telles) near_telles_sum(e, fam, kc, x0, r6, acc);
+    return true;
+}
+
 // ------------------------------------------------------------------ driver
 
 // the SLP entry of item `item` of wave number f: into the matrix, or in
@@ -273,7 +339,7 @@ __device__ __forceinline__ void store_slp(const RegularArgs &a, int f, int64_t i
 
 // BATCH: frequency batch (a.nk > 1), a separate kernel so that the single
 // wave number kernel carries none of its code.
-template <typename Out, bool BATCH>
+template <typename Out, bool BATCH, bool CK = false>
 __device__ __forceinline__ void singular_pairs(const RegularArgs &a, const NearList &near, int *err)
 {
     // frequency batches: per-thread series coefficients (MOM_SMEM bytes, launched only with nk > 1)
@@ -312,6 +378,17 @@ __device__ __forceinline__ void singular_pairs(const RegularArgs &a, const NearL
         Elem64 e;
         load_elem(a.trial, j, e);
         const int64_t off = (int64_t)(j - a.j0) * a.ld + i;
+        if constexpr (CK) {
+            // complex (lossy) wave number: single wave number only
+            Acc acc;
+            if (!pair_ck(a, e, x0, self, j, do_s, do_d, acc)) {
+                atomicCAS(err, 0, (int)min(item + 1, (int64_t)0x7fffffff));
+                break;
+            }
+            if (do_s) store_slp<Out>(a, 0, total, item, off, acc);
+            if (do_d) store64(batch_matrix<Out>(a, true, 0) + off, acc.dr, acc.di, a.alpha_re, a.alpha_im, a.accumulate);
+            continue;
+        }
         if (BATCH && e.nc == 3) {
             // frequency batch on a triangle: the k-independent static part and
             // the moments of the dynamic part once, then per wave number the
@@ -415,6 +492,13 @@ __global__ void __launch_bounds__(SING_THREADS, 4) k_singular(RegularArgs a, Nea
     singular_pairs<Out, false>(a, near, err);
 }
 
+// complex (lossy) wave number: its own kernel, so the real-k kernel carries none of it
+template <typename Out>
+__global__ void __launch_bounds__(SING_THREADS, 4) k_singular_ck(RegularArgs a, NearList near, int *err)
+{
+    singular_pairs<Out, false, true>(a, near, err);
+}
+
 // held to 128 registers (its code alone would take about 166), so that the
 // concurrent regular kernel keeps three of its blocks on every SM beside this
 // kernel's one; the single wave number kernel comes to 128 by itself, where
@@ -487,6 +571,9 @@ cudaError_t launch_assemble_singular(const RegularArgs &a, const NearList &near,
         smem = MOM_SMEM;
         if (a.dtype == 0) k_singular_batch<float2><<<grid, SING_THREADS, smem, s>>>(a, near, err);
         else k_singular_batch<double2><<<grid, SING_THREADS, smem, s>>>(a, near, err);
+    } else if (a.k_im != 0.0) {
+        if (a.dtype == 0) k_singular_ck<float2><<<blocks, SING_THREADS, 0, s>>>(a, near, err);
+        else k_singular_ck<double2><<<blocks, SING_THREADS, 0, s>>>(a, near, err);
     } else {
         if (a.dtype == 0) k_singular<float2><<<blocks, SING_THREADS, 0, s>>>(a, near, err);
         else k_singular<double2><<<blocks, SING_THREADS, 0, s>>>(a, near, err);

@@ -675,6 +675,14 @@ nihu_gb_status nihu_gb_assemble(nihu_gb_ctx *ctx, const nihu_gb_mesh *test, cons
                                 int ops, double k, double alpha_re, double alpha_im, int precision, int dtype,
                                 void *out_slp, void *out_dlp, int64_t ld, int accumulate, int where)
 {
+    return nihu_gb_assemble_c(ctx, test, trial, family, ops, k, 0.0, alpha_re, alpha_im, precision, dtype, out_slp,
+                              out_dlp, ld, accumulate, where);
+}
+
+nihu_gb_status nihu_gb_assemble_c(nihu_gb_ctx *ctx, const nihu_gb_mesh *test, const nihu_gb_mesh *trial, int family,
+                                  int ops, double k, double k_im, double alpha_re, double alpha_im, int precision,
+                                  int dtype, void *out_slp, void *out_dlp, int64_t ld, int accumulate, int where)
+{
     if (!ctx) return NIHU_GB_ERR_INVALID_ARGUMENT;
     if (!test || !trial || test->ctx != ctx || trial->ctx != ctx)
         return fail(ctx, NIHU_GB_ERR_INVALID_ARGUMENT, "nihu_gb_assemble: meshes must belong to the context");
@@ -686,7 +694,7 @@ nihu_gb_status nihu_gb_assemble(nihu_gb_ctx *ctx, const nihu_gb_mesh *test, cons
     if (!valid_dtype(dtype) || !valid_where(where) || (precision != 0 && precision != 1))
         return fail(ctx, NIHU_GB_ERR_INVALID_ARGUMENT, "nihu_gb_assemble: bad dtype, precision or location");
     if (ld < std::max<int64_t>(test->n, 1)) return fail(ctx, NIHU_GB_ERR_INVALID_ARGUMENT, "nihu_gb_assemble: ld < rows");
-    if (!std::isfinite(k) || !std::isfinite(alpha_re) || !std::isfinite(alpha_im))
+    if (!std::isfinite(k) || !std::isfinite(k_im) || !std::isfinite(alpha_re) || !std::isfinite(alpha_im))
         return fail(ctx, NIHU_GB_ERR_INVALID_ARGUMENT, "nihu_gb_assemble: non-finite wave number or scale");
     if (test->n == 0 || trial->n == 0) return NIHU_GB_OK;
     cudaSetDevice(ctx->device);
@@ -701,6 +709,7 @@ nihu_gb_status nihu_gb_assemble(nihu_gb_ctx *ctx, const nihu_gb_mesh *test, cons
     a.family = family;
     a.ops = ops;
     a.k = family == NIHU_GB_HELMHOLTZ_3D ? k : 0.0;
+    a.k_im = family == NIHU_GB_HELMHOLTZ_3D ? k_im : 0.0;
     a.alpha_re = alpha_re;
     a.alpha_im = alpha_im;
     a.precision = precision;
@@ -708,6 +717,7 @@ nihu_gb_status nihu_gb_assemble(nihu_gb_ctx *ctx, const nihu_gb_mesh *test, cons
     a.accumulate = accumulate ? 1 : 0;
     a.trial_size_max = trial->size_max;
     a.k32 = (float)a.k;
+    a.k_im32 = (float)a.k_im;
     a.alpha_re32 = (float)alpha_re;
     a.alpha_im32 = (float)alpha_im;
     a.unit_alpha = alpha_re == 1.0 && alpha_im == 0.0;
@@ -1585,6 +1595,14 @@ nihu_gb_status nihu_gb_solve_cbie(nihu_gb_ctx *ctx, const nihu_gb_mesh *mesh, in
                                   int dtype, const void *q, void *p, int solver, int restart, int max_iters,
                                   double tol, int *iters, double *rel_residual)
 {
+    return nihu_gb_solve_cbie_c(ctx, mesh, family, k, 0.0, precision, dtype, q, p, solver, restart, max_iters, tol,
+                                iters, rel_residual);
+}
+
+nihu_gb_status nihu_gb_solve_cbie_c(nihu_gb_ctx *ctx, const nihu_gb_mesh *mesh, int family, double k, double k_im,
+                                    int precision, int dtype, const void *q, void *p, int solver, int restart,
+                                    int max_iters, double tol, int *iters, double *rel_residual)
+{
     if (!ctx) return NIHU_GB_ERR_INVALID_ARGUMENT;
     if (!mesh || !q || !p || (solver != 0 && solver != 1) || (solver == 1 && dtype != NIHU_GB_C128) || !valid_dtype(dtype))
         return fail(ctx, NIHU_GB_ERR_INVALID_ARGUMENT, "nihu_gb_solve_cbie: bad argument");
@@ -1600,8 +1618,8 @@ nihu_gb_status nihu_gb_solve_cbie(nihu_gb_ctx *ctx, const nihu_gb_mesh *mesh, in
     if ((st = scratch(ctx, "cbie_rhs", 16 * n, &drhs))) return st;
     if ((st = scratch(ctx, "cbie_p", 16 * n, &dp))) return st;
     CK(cudaMemcpyAsync(dq, q, 16 * n, cudaMemcpyHostToDevice, ctx->stream));
-    st = nihu_gb_assemble(ctx, mesh, mesh, family, NIHU_GB_SLP | NIHU_GB_DLP, k, 1.0, 0.0, precision, dtype, G, Hm, n, 0,
-                          NIHU_GB_DEVICE);
+    st = nihu_gb_assemble_c(ctx, mesh, mesh, family, NIHU_GB_SLP | NIHU_GB_DLP, k, k_im, 1.0, 0.0, precision, dtype, G,
+                            Hm, n, 0, NIHU_GB_DEVICE);
     if (st) return st;
     CK(launch_add_identity((int)n, -0.5, 0.0, dtype, Hm, n, ctx->stream));
     ctx->launches += 1;

@@ -114,6 +114,43 @@ __device__ __forceinline__ void eval_point(R rx, R ry, R rz, R wj, R nx, R ny, R
     }
 }
 
+// eval_point for a complex (lossy) wave number k + i ki:
+// e^{-i(k + i ki) r} = e^{ki r} (cos kr - i sin kr) and 1 + i(k + i ki) r =
+// (1 - ki r) + i kr, so the SLP is damped by e^{ki r} and the DLP factor
+// -(1 + ikr) e^{-ikr} takes 1 - ki r in place of 1
+// (nihu/library/helmholtz_kernel.hpp:42-54,180-195 with a complex wave number)
+template <typename R>
+__device__ __forceinline__ void eval_point_ck(R rx, R ry, R rz, R wj, R nx, R ny, R nz, R k, R ki, R ws, R wd, R &sr,
+                                              R &si, R &dr, R &di)
+{
+    constexpr R INV4PI = R(1.0 / (4.0 * 3.14159265358979323846));
+    R r2 = rx * rx + ry * ry + rz * rz;
+    R rinv;
+    if constexpr (sizeof(R) == 4) rinv = rsqrtf(r2);
+    else rinv = rsqrt(r2);
+    const R g = wj * rinv * INV4PI;
+    const R rdn = (rx * nx + ry * ny + rz * nz) * rinv;
+    const R r = r2 * rinv;
+    const R kr = k * r;
+    R s, c, damp;
+    if constexpr (sizeof(R) == 4) {
+        sincos_reduced(kr, s, c);
+        damp = expf(ki * r);
+    } else {
+        sincos(kr, &s, &c);
+        damp = exp(ki * r);
+    }
+    c *= damp;
+    s *= damp;
+    const R gs = g * ws;
+    sr += gs * c;
+    si -= gs * s;
+    const R f = -g * rinv * rdn * wd;
+    const R a1 = R(1) - ki * r;
+    dr += f * (a1 * c + kr * s);
+    di += f * (kr * c - a1 * s);
+}
+
 struct cd { double re, im; };
 
 // four doubles in one 32-byte aligned record (point + weight)

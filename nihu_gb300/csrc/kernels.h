@@ -60,6 +60,10 @@ struct RegularArgs {
     // FP64 instruction (the FP64 pipe belongs to the concurrent singular kernel)
     float k32, alpha_re32, alpha_im32;
     int unit_alpha;
+    // imaginary part of a complex (lossy) wave number k + i k_im (single wave
+    // number only; 0 for the real wave numbers the fast instantiations take)
+    double k_im = 0.0;
+    float k_im32 = 0.0f;
     // frequency batch: nk > 1 assembles one matrix per wave number ks[f]
     // (FP64 and FP32 copies on the device) at out + f * mat_stride
     int nk = 1;

@@ -21,9 +21,23 @@ __device__ __forceinline__ void helm_g_dg(double k, double r, double rinv, cd &g
     dg = {-(c + kr * s) * b, -(kr * c - s) * b};
 }
 
+// the same for a complex (lossy) wave number k = k.re + i k.im:
+// e^{-ikr} = e^{k.im r} (cos k.re r - i sin k.re r), 1 + ikr = (1 - k.im r) + i k.re r
+__device__ __forceinline__ void helm_g_dg(cd k, double r, double rinv, cd &g, cd &dg)
+{
+    double s, c;
+    sincos(k.re * r, &s, &c);
+    const double a = rinv * INV_FOUR_PI * exp(k.im * r);
+    g = {c * a, -s * a};
+    const double p = 1.0 - k.im * r, q = k.re * r;
+    dg = {-(p * g.re - q * g.im) * rinv, -(p * g.im + q * g.re) * rinv};
+}
+
 // kernel values times the Jacobian at a point y with (unnormalised) normal n:
-// SLP = G J, DLP = dG/dr (r.n)/r (n = N/J, so the J cancels)
-__device__ __forceinline__ void kern_point(int fam, double k, const double x0[3], const double y[3], const double n[3],
+// SLP = G J, DLP = dG/dr (r.n)/r (n = N/J, so the J cancels); K is the wave
+// number's type (double, or cd for a complex one)
+template <class K>
+__device__ __forceinline__ void kern_point(int fam, K k, const double x0[3], const double y[3], const double n[3],
                                            double J, bool do_s, bool do_d, cd &ks, cd &kd)
 {
     double rv0 = y[0] - x0[0], rv1 = y[1] - x0[1], rv2 = y[2] - x0[2];
@@ -43,7 +57,8 @@ __device__ __forceinline__ void kern_point(int fam, double k, const double x0[3]
     if (do_d) kd = cscale(dg, rn);
 }
 
-__device__ __forceinline__ void kern_on_elem(const Elem64 &e, int fam, double k, const double x0[3], double xi,
+template <class K>
+__device__ __forceinline__ void kern_on_elem(const Elem64 &e, int fam, K k, const double x0[3], double xi,
                                              double eta, bool do_s, bool do_d, cd &ks, cd &kd)
 {
     double y[3], n[3];
@@ -145,6 +160,71 @@ __device__ inline void near_dynamic(const Elem64 &e, double k, const double x0[3
             double u = t * rinv * ((rv0 * en[0] + rv1 * en[1] + rv2 * en[2]) * rinv);
             a.dr -= u * (cs + kr * sn - 1.0);
             a.di -= u * (kr * cs - sn);
+        }
+    }
+}
+
+// near_dynamic for a complex (lossy) wave number: the same points, with
+// e^{-ikr} - 1 = expm1(k.im r) cos(k.re r) - 2 sin^2(k.re r / 2) - i e^{k.im r} sin(k.re r)
+// (no cancellation as k r -> 0) and the DLP's (e^{-ikr} - 1) + ikr e^{-ikr}
+__device__ inline void near_dynamic_ck(const Elem64 &e, cd k, const double x0[3], bool do_s, bool do_d, Acc &a,
+                                       const Pt4 *__restrict__ pts42)
+{
+    double en[3];
+    {
+        double xi, eta;
+        domain_center(e.nc, xi, eta);
+        enormal(e, xi, eta, en);
+        double nn = 1.0 / norm3(en);
+        for (int d = 0; d < 3; ++d) en[d] *= nn;
+    }
+    const int np = e.nc == 3 ? 42 : 64;
+    for (int p = 0; p < np; ++p) {
+        double xi, eta, w, J;
+        double y[3];
+        if (pts42) {
+            const Pt4 v = pts42[p];
+            y[0] = v.x; y[1] = v.y; y[2] = v.z;
+            w = v.w;
+            J = 1.0;
+        } else if (e.nc == 3) {
+            double e1[3], e2[3], nt[3];
+            for (int d = 0; d < 3; ++d) { e1[d] = e.c[1][d] - e.c[0][d]; e2[d] = e.c[2][d] - e.c[0][d]; }
+            cross3(e1, e2, nt);
+            tri_pt(14, p, xi, eta, w);
+            for (int d = 0; d < 3; ++d) y[d] = e.c[0][d] + xi * e1[d] + eta * e2[d];
+            J = norm3(nt);
+        } else {
+            double w0, w1, n[3];
+            gauss_pt(8, p / 8, xi, w0);
+            gauss_pt(8, p % 8, eta, w1);
+            w = w0 * w1;
+            ex(e, xi, eta, y);
+            enormal(e, xi, eta, n);
+            J = norm3(n);
+        }
+        double rv0 = y[0] - x0[0], rv1 = y[1] - x0[1], rv2 = y[2] - x0[2];
+        double r2 = rv0 * rv0 + rv1 * rv1 + rv2 * rv2;
+        double rinv = rsqrt(r2);
+        double r = r2 * rinv;
+        double sn, cs, sh, chh;
+        sincos(k.re * r, &sn, &cs);
+        sincos(0.5 * k.re * r, &sh, &chh);
+        const double ea = exp(k.im * r);
+        const double em1_re = expm1(k.im * r) * cs - 2.0 * sh * sh, em1_im = -ea * sn;  // e^{-ikr} - 1
+        const double E_re = ea * cs, E_im = -ea * sn;                                      // e^{-ikr}
+        const double t = w * J * rinv * INV_FOUR_PI;
+        if (do_s) {
+            a.sr += t * em1_re;
+            a.si += t * em1_im;
+        }
+        if (do_d) {
+            // ikr = -k.im r + i k.re r
+            const double ar = -k.im * r, ai = k.re * r;
+            const double d_re = em1_re + (ar * E_re - ai * E_im), d_im = em1_im + (ar * E_im + ai * E_re);
+            double u = t * rinv * ((rv0 * en[0] + rv1 * en[1] + rv2 * en[2]) * rinv);
+            a.dr -= u * d_re;
+            a.di -= u * d_im;
         }
     }
 }
@@ -289,7 +369,8 @@ __device__ inline void linearized(const Elem64 &e, double xi0, double eta0, Elem
 }
 
 // polar scheme around (xi0, eta0) with linearized-element subtraction
-__device__ inline void near_polar_sum(const Elem64 &e, const Elem64 &lin, int fam, double k, const double x0[3], double xi0,
+template <class K>
+__device__ inline void near_polar_sum(const Elem64 &e, const Elem64 &lin, int fam, K k, const double x0[3], double xi0,
                                double eta0, bool do_s, bool do_d, Acc &a)
 {
     const int N = e.nc;
@@ -340,7 +421,8 @@ __device__ inline void near_polar_sum(const Elem64 &e, const Elem64 &lin, int fa
 }
 
 // Telles-transformed 16x16 Gauss rule (DLP only)
-__device__ inline void near_telles_sum(const Elem64 &e, int fam, double k, const double x0[3], const double im[3], Acc &a)
+template <class K>
+__device__ inline void near_telles_sum(const Elem64 &e, int fam, K k, const double x0[3], const double im[3], Acc &a)
 {
     double dist = im[2];
     double rb;
@@ -633,7 +715,8 @@ static __device__ __noinline__ void near_dynamic_quad_f32(const Elem64 &e, doubl
 }
 
 
-__device__ inline void self_quad(const Elem64 &e, int fam, double k, const double x0[3], bool do_s, bool do_d, Acc &a)
+template <class K>
+__device__ inline void self_quad(const Elem64 &e, int fam, K k, const double x0[3], bool do_s, bool do_d, Acc &a)
 {
     for (int d = 0; d < 4; ++d) {
         double P2[2], P3[2];

@@ -85,10 +85,11 @@ def gpu_assemble(ctx, mesh, family, ops, k, precision, dtype, test_mesh=None, al
             outs[op] = (np.array(accumulate_into[op], dtype=cdt, order="F") if accumulate_into
                         else np.zeros((m, n), dtype=cdt, order="F"))
     alpha = complex(alpha)
-    ctx.check(L.nihu_gb_assemble(ctx.handle, test.handle, trial.handle, family, ops, k, alpha.real, alpha.imag,
-                                 precision, dtype, outs[g.SLP].ctypes.data if g.SLP in outs else None,
-                                 outs[g.DLP].ctypes.data if g.DLP in outs else None, m,
-                                 1 if accumulate_into else 0, g.HOST))
+    kc = complex(k)
+    ctx.check(L.nihu_gb_assemble_c(ctx.handle, test.handle, trial.handle, family, ops, kc.real, kc.imag, alpha.real,
+                                   alpha.imag, precision, dtype, outs[g.SLP].ctypes.data if g.SLP in outs else None,
+                                   outs[g.DLP].ctypes.data if g.DLP in outs else None, m,
+                                   1 if accumulate_into else 0, g.HOST))
     test.close()
     if test_mesh is not None:
         trial.close()
@@ -100,7 +101,10 @@ def gpu_assemble(ctx, mesh, family, ops, k, precision, dtype, test_mesh=None, al
 CASES = [("ico2", g.HELMHOLTZ_3D, 1.0), ("ico2", g.LAPLACE_3D, 0.0), ("ico3", g.HELMHOLTZ_3D, 5.0),
          ("ico3", g.HELMHOLTZ_3D, 1.0), ("cyl", g.HELMHOLTZ_3D, 2.0), ("cyl", g.LAPLACE_3D, 0.0),
          ("mixed", g.HELMHOLTZ_3D, 1.5), ("sphere_1_3", g.HELMHOLTZ_3D, 1.0), ("sphere_1_3", g.LAPLACE_3D, 0.0),
-         ("sphere_1_5", g.HELMHOLTZ_3D, 1.0), ("sphere_1_5", g.HELMHOLTZ_3D, 4.0)]
+         ("sphere_1_5", g.HELMHOLTZ_3D, 1.0), ("sphere_1_5", g.HELMHOLTZ_3D, 4.0),
+         # complex (lossy) wave numbers: nihu_gb_assemble_c
+         ("ico2", g.HELMHOLTZ_3D, 2.0 - 0.3j), ("ico3", g.HELMHOLTZ_3D, 5.0 - 0.5j), ("cyl", g.HELMHOLTZ_3D, 2.0 - 0.3j),
+         ("mixed", g.HELMHOLTZ_3D, 1.5 - 0.2j)]
 
 
 @pytest.mark.parametrize("name,family,k", CASES)
@@ -294,3 +298,39 @@ def test_invalid_arguments_raise(gpu_ctx):
         gpu_ctx.check(L.nihu_gb_assemble(gpu_ctx.handle, dm.handle, dm.handle, 0, 3, 1.0, 1.0, 0.0, 0, 0,
                                          out.ctypes.data, None, n, 0, g.HOST))
     dm.close()
+
+
+@pytest.mark.parametrize("k", [2.0 - 0.3j, 1.0 - 1.0j])
+def test_pulsating_sphere_complex_wave_number(gpu_ctx, oracle, k):
+    """A lossy medium: the exterior CBIE with a complex wave number through
+    nihu_gb_solve_cbie_c; the analytic pressure p = -R/(1 + ikR) holds for
+    complex k (nihu/test/stallone_unit/helmholtz_3d_pulsating_sphere_test.cpp:51-56).
+    Pressure within 1e-4 of the oracle's dense solve (FP32 mode) and 1e-9
+    (FP64 mode, LU), and within the discretisation error of the analytic."""
+    mesh = get_mesh("ico3")
+    n = len(mesh[1])
+    m = g.create_mesh(*mesh)
+    L = oracle_matrix(oracle, "ico3", g.HELMHOLTZ_3D, g.SLP, k)
+    M = oracle_matrix(oracle, "ico3", g.HELMHOLTZ_3D, g.DLP, k) - 0.5 * np.eye(n)
+    pr = np.linalg.solve(M, L @ np.ones(n))
+    p32, it, res = g.solve_cbie(m, k, np.ones(n), ctx=gpu_ctx)
+    p64, _, _ = g.solve_cbie(m, k, np.ones(n), dtype=g.C128, solver="lu", precision="fp64", ctx=gpu_ctx)
+    assert np.abs(p32 - pr).max() / np.abs(pr).max() < 1e-4
+    assert np.abs(p64 - pr).max() / np.abs(pr).max() < 1e-9
+    pa = -1.0 / (1.0 + 1j * k)
+    assert np.abs(p64 - pa).max() / abs(pa) < 0.01
+
+
+def test_complex_wave_number_through_the_operator_algebra(gpu_ctx, oracle):
+    """helmholtz_3d_SLP_kernel(k) with a complex k in the NiHu-shaped front end."""
+    nodes, elems = get_mesh("ico2")
+    mesh = g.create_mesh(nodes, elems)
+    sp = g.constant_view(mesh)
+    n = sp.get_num_dofs()
+    k = 2.0 - 0.3j
+    Ls = np.zeros((n, n), np.complex128, order="F")
+    Ls << g.dirac(sp) * g.create_integral_operator(g.helmholtz_3d_SLP_kernel(k))[sp]
+    assert rel_norm(Ls, oracle_matrix(oracle, "ico2", g.HELMHOLTZ_3D, g.SLP, k)) < 1e-5
+    with pytest.raises(NotImplementedError):
+        Gs = np.zeros((n, n), np.complex128)
+        (sp * g.create_integral_operator(g.helmholtz_3d_SLP_kernel(k))[sp]).eval_into(Gs, ctx=gpu_ctx)
