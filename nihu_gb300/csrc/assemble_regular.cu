@@ -464,6 +464,141 @@ __global__ void __launch_bounds__(REG_THREADS) k_regular(RegularArgs a)
     }
 }
 
+// ------------------------------------------------- two rows per thread
+// The single wave number FP32 kernel for the common case (SLP and DLP, unit
+// scale, no accumulation, complex64 columns that allow 16-byte stores): each
+// thread owns two adjacent rows, so that one far vote, one set of shared
+// loads and the loop's bookkeeping serve two pairs, and each column takes one
+// 16-byte store per matrix for both rows.  The points, levels and their order
+// are those of k_regular (the far path, the certain-level path, and the
+// general per-lane dispatch, here per row), so the entries are the same.
+constexpr int REG2_THREADS = 256;
+constexpr int REG2_ROWS = 2 * REG2_THREADS;
+
+// one pair by the general path of k_regular (classify_pair, the uniform loop
+// over the lane's points); false when the pair is not regular
+template <int FAM>
+__device__ __forceinline__ bool pair_general32(const RegularArgs &a, const float4 ih, const float4 il, int par, int i,
+                                               int j, const float4 jh, const float4 jl, int tnc, float k, float &sr,
+                                               float &si, float &dr, float &di)
+{
+    int ls, ld;
+    float dx, dy, dz;
+    const int kind = classify_pair(ih, il, jh, jl, i, j, a.test.center, a.trial.center, a.trial.size, a.same_mesh,
+                                   ls, ld, dx, dy, dz);
+    if (kind != KIND_REGULAR) return false;
+    const int nps = level_npts(tnc, par, ls);
+    const int npd = level_npts(tnc, par, ld);
+    const int n_eval = ls == ld ? nps : nps + npd;
+    const int64_t base = ((int64_t)j * 2 + par) * SLOTS;
+    sr = si = dr = di = 0.0f;
+    for (int q = 0; q < n_eval; ++q) {
+        int slot;
+        float ws, wd;
+        if (ls == ld) { slot = level_slot0(ls) + q; ws = 1.0f; wd = 1.0f; }
+        else if (q < nps) { slot = level_slot0(ls) + q; ws = 1.0f; wd = 0.0f; }
+        else { slot = level_slot0(ld) + q - nps; ws = 0.0f; wd = 1.0f; }
+        const float4 y = __ldg(a.trial.pts32 + 2 * (base + slot));
+        const float4 n = __ldg(a.trial.pts32 + 2 * (base + slot) + 1);
+        eval_point<FAM, float>(dx + y.x, dy + y.y, dz + y.z, y.w, n.x, n.y, n.z, k, ws, wd, sr, si, dr, di);
+    }
+    return true;
+}
+
+template <int FAM>
+// 64 registers: three blocks fit beside the concurrent singular kernel's one
+__global__ void __launch_bounds__(REG2_THREADS, 4) k_regular2(RegularArgs a)
+{
+    __shared__ float4 s_hi[REG_COLS], s_lo[REG_COLS], s_p0[REG_COLS];
+    __shared__ int s_nc[REG_COLS];
+    const DevMesh &test = a.test;
+    const DevMesh &trial = a.trial;
+    const int jb = a.j0 + blockIdx.y * REG_COLS;
+    const int ncols = min(REG_COLS, a.j1 - jb);
+    if (threadIdx.x < ncols) {
+        s_hi[threadIdx.x] = trial.chi[jb + threadIdx.x];
+        s_lo[threadIdx.x] = trial.clo[jb + threadIdx.x];
+        s_nc[threadIdx.x] = trial.nc[jb + threadIdx.x];
+        s_p0[threadIdx.x] = trial.p0[jb + threadIdx.x];
+    }
+    __syncthreads();
+    const int i0 = blockIdx.x * REG2_ROWS + 2 * threadIdx.x;
+    // whole warps beyond the last row leave; a partial warp keeps its lanes
+    // (clamped rows, stores masked) so that the votes see every lane
+    if (((i0 - 2 * (int)(threadIdx.x & 31))) >= test.n) return;
+    const bool ok0 = i0 < test.n, ok1 = i0 + 1 < test.n;
+    const int r0 = ok0 ? i0 : test.n - 1, r1 = ok1 ? i0 + 1 : test.n - 1;
+    const float4 ih0 = test.chi[r0], il0 = test.clo[r0], ih1 = test.chi[r1], il1 = test.clo[r1];
+    const int par0 = il0.w != 0.0f ? 1 : 0, par1 = il1.w != 0.0f ? 1 : 0;
+    const float k = a.k32;
+    const int64_t ldo = a.ld;
+    float2 *ps = reinterpret_cast<float2 *>(a.out_s) + (int64_t)(jb - a.j0) * ldo + i0;
+    float2 *pd = reinterpret_cast<float2 *>(a.out_d) + (int64_t)(jb - a.j0) * ldo + i0;
+
+    for (int c = 0; c < ncols; ++c, ps += ldo, pd += ldo) {
+        const int j = jb + c;
+        const float4 h = s_hi[c], l = s_lo[c];
+        // hi/lo centre differences of both rows (FP32 relative accuracy of r)
+        const float ax = (h.x - ih0.x) + (l.x - il0.x), ay = (h.y - ih0.y) + (l.y - il0.y),
+                    az = (h.z - ih0.z) + (l.z - il0.z);
+        const float bx = (h.x - ih1.x) + (l.x - il1.x), by = (h.y - ih1.y) + (l.y - il1.y),
+                    bz = (h.z - ih1.z) + (l.z - il1.z);
+        const float qa = (ax * ax + ay * ay + az * az) * h.w;
+        const float qb = (bx * bx + by * by + bz * bz) * h.w;
+        if (__all_sync(0xffffffffu, qa > Q_FAR && qb > Q_FAR)) {
+            // far: the centroid for both operators, both rows
+            const float4 p = s_p0[c];
+            float sr0 = 0, si0 = 0, dr0 = 0, di0 = 0, sr1 = 0, si1 = 0, dr1 = 0, di1 = 0;
+            eval_point<FAM, float>(ax, ay, az, p.x, p.y, p.z, p.w, k, 1.0f, 1.0f, sr0, si0, dr0, di0);
+            eval_point<FAM, float>(bx, by, bz, p.x, p.y, p.z, p.w, k, 1.0f, 1.0f, sr1, si1, dr1, di1);
+            if (ok1) {
+                *reinterpret_cast<float4 *>(ps) = make_float4(sr0, si0, sr1, si1);
+                *reinterpret_cast<float4 *>(pd) = make_float4(dr0, di0, dr1, di1);
+            } else if (ok0) {
+                *ps = make_float2(sr0, si0);
+                *pd = make_float2(dr0, di0);
+            }
+            continue;
+        }
+        // otherwise each row as k_regular: the certain-level path when every
+        // lane's row is certain, else the general dispatch
+        const int tnc = s_nc[c];
+        auto row = [&](const float4 ih, const float4 il, int par, int ri, bool okr, float mx, float my, float mz,
+                       float mq, float2 *qs, float2 *qd) {
+            const float mlo = mq * (1.0f - 1e-5f), mhi = mq * (1.0f + 1e-5f);
+            const bool d_far = mlo >= 249.64f;
+            if (__all_sync(0xffffffffu, mlo >= 82.81f && (d_far || mhi < 249.64f))) {
+                const int64_t base = ((int64_t)j * 2 + par) * SLOTS;
+                float sr = 0, si = 0, dr = 0, di = 0;
+                const float4 yc = __ldg(trial.pts32 + 2 * base), nc = __ldg(trial.pts32 + 2 * base + 1);
+                eval_point<FAM, float>(mx, my, mz, yc.w, nc.x, nc.y, nc.z, k, 1.0f, d_far ? 1.0f : 0.0f, sr, si, dr,
+                                       di);
+                if (!d_far) {
+                    const int npd = level_npts(tnc, par, 1);
+                    for (int q = 0; q < npd; ++q) {
+                        const int64_t sl = base + level_slot0(1) + q;
+                        const float4 y = __ldg(trial.pts32 + 2 * sl), n = __ldg(trial.pts32 + 2 * sl + 1);
+                        eval_point<FAM, float>(mx + y.x, my + y.y, mz + y.z, y.w, n.x, n.y, n.z, k, 0.0f, 1.0f, sr,
+                                               si, dr, di);
+                    }
+                }
+                if (okr) {
+                    *qs = make_float2(sr, si);
+                    *qd = make_float2(dr, di);
+                }
+                return;
+            }
+            float sr, si, dr, di;
+            if (okr && pair_general32<FAM>(a, ih, il, par, ri, j, h, l, tnc, k, sr, si, dr, di)) {
+                *qs = make_float2(sr, si);
+                *qd = make_float2(dr, di);
+            }
+        };
+        row(ih0, il0, par0, r0, ok0, ax, ay, az, qa, ps, pd);
+        row(ih1, il1, par1, r1, ok1, bx, by, bz, qb, ps + 1, pd + 1);
+    }
+}
+
 // partial sums of the same row added in FP32 before one FP64 addition
 constexpr int RHS_GROUP = 8;
 
@@ -569,6 +704,15 @@ cudaError_t launch_assemble_regular(const RegularArgs &a, cudaStream_t s)
             const int fmax = a.precision == 0 ? rhs_fmax_of<float>(a) : rhs_fmax_of<double>(a);
             grid.z = std::max<unsigned>(grid.z, (unsigned)((a.nk + fmax - 1) / fmax));
         }
+    }
+    if (a.precision == 0 && a.dtype == 0 && a.nk <= 1 && !a.force_batch && a.ops == (OP_SLP | OP_DLP) &&
+        a.unit_alpha && !a.accumulate && a.k_im == 0.0 && (a.ld & 1) == 0 &&
+        (reinterpret_cast<uintptr_t>(a.out_s) & 15) == 0 && (reinterpret_cast<uintptr_t>(a.out_d) & 15) == 0) {
+        // two rows per thread with 16-byte stores
+        dim3 g2((a.test.n + REG2_ROWS - 1) / REG2_ROWS, grid.y);
+        if (a.family == FAM_HELMHOLTZ) k_regular2<FAM_HELMHOLTZ><<<g2, REG2_THREADS, 0, s>>>(a);
+        else k_regular2<FAM_LAPLACE><<<g2, REG2_THREADS, 0, s>>>(a);
+        return cudaGetLastError();
     }
     if (a.precision == 0) {
         if (a.dtype == 0) launch_fam<float, float2>(a, grid, s);

@@ -103,6 +103,57 @@ __device__ inline void near_static(const Elem64 &e, const double x0[3], bool do_
     a.dr += sg * d_sum * INV_FOUR_PI;
 }
 
+// near_static with the angular point sums in FP32 (the FP32 regular
+// quadrature mode).  The plane frame, the side distances and the angle limits
+// stay FP64.  Per side, with the reference's 6 points: the SLP sums
+// r - |z| = R^2 / (r + |z|) (positive, no cancellation) and the DLP sums
+// 1 - |z|/r as sum(w) (t2 - t1)/2 - sum(w |z|/r) (t2 - t1)/2, the first part
+// in FP64 -- over the sides it adds up to 2 pi or 0, and summing the O(1)
+// terms in FP32 instead would leave FP32 rounding of that size in a DLP
+// entry of a point whose foot lies outside the element, where the sides
+// cancel -- and the second in FP32; the sides are added in FP64.
+__device__ inline void near_static_f32(const Elem64 &e, const double x0[3], bool do_s, bool do_d, Acc &a)
+{
+    double loc[4][2], z;
+    plane_local(e, x0, loc, z);
+    const int N = e.nc;
+    double tl[4], t0[4], dr[4];
+    for (int s = 0; s < N; ++s) side_geometry(loc[s], loc[(s + 1) % N], tl[s], t0[s], dr[s], false);
+    const float az = (float)fabs(z), z2 = az * az;
+    double wsum = 0.0;
+    for (int q = 0; q < 6; ++q) {
+        double xi, w;
+        gauss_pt(6, q, xi, w);
+        wsum += w;
+    }
+    double s_sum = 0.0, d_sum = 0.0;
+    for (int s = 0; s < N; ++s) {
+        double t1 = tl[s], t2 = tl[(s + 1) % N];
+        wrap_limits(t1, t2);
+        const double jac = (t2 - t1) / 2.0;
+        // the angle from the side's foot direction at the rule's ends
+        const float p1 = (float)(t1 - t0[s]), p2 = (float)(t2 - t0[s]);
+        const float ds = (float)dr[s];
+        float ss = 0.0f, sz = 0.0f;
+        for (int q = 0; q < 6; ++q) {
+            double xi, w;
+            gauss_pt(6, q, xi, w);
+            const float xf = (float)xi, wf = (float)w;
+            const float ph = p1 * (1.0f - xf) * 0.5f + p2 * (1.0f + xf) * 0.5f;
+            const float R = ds / cosf(ph);
+            const float R2 = R * R;
+            const float r = sqrtf(R2 + z2);
+            ss += wf * (R2 / (r + az));  // r - |z|
+            sz += wf * (az / r);         // |z| / r
+        }
+        s_sum += jac * (double)ss;
+        d_sum += jac * (wsum - (double)sz);
+    }
+    const double sg = (0.0 < z) - (z < 0.0);
+    if (do_s) a.sr += s_sum * INV_FOUR_PI;
+    if (do_d) a.dr += sg * d_sum * INV_FOUR_PI;
+}
+
 // dynamic part (K_k - K_0) of the planar nearly singular scheme with the
 // degree-14 rule (42-point Dunavant on triangles, 8x8 Gauss on quads)
 __device__ inline void near_dynamic(const Elem64 &e, double k, const double x0[3], bool do_s, bool do_d, Acc &a,
