@@ -97,7 +97,7 @@ def workload_config(n):
         "entries_per_step": 2 * n * n,
         "storage": "complex64",
         "regular_quadrature": "fp32, distance-adaptive 1/3/6-point Dunavant",
-        "singular_nearly_singular": "fp64 self terms and nearly singular static parts (semi-analytic), fp32 nearly singular dynamic parts (42-point K_k - K_0)",
+        "singular_nearly_singular": "fp64 self terms; nearly singular static parts (semi-analytic) with fp64 plane frame, foot vectors and winding angle and fp32 angular point sums; fp32 nearly singular dynamic parts (42-point K_k - K_0)",
         "l2": "256 MB written between timed steps (L2 flushed); outputs 6.7 GB >> 129 MB L2",
         "parallelism": "replicas only (1 GPU per instance)",
     }
@@ -360,7 +360,7 @@ def run_ours(args):
     out = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "fp32 regular quadrature and nearly singular dynamic parts, fp64 self terms and nearly singular static parts; complex64 storage",
+        "dtype": "fp32 regular quadrature, nearly singular dynamic parts and static angular sums, fp64 self terms and nearly singular geometry; complex64 storage",
         "data": "synthetic (icosphere mesh generated in-process)",
         "config": workload_config(n), "gpu_launches": int(launches), "clocks": clk, "roofline": roofline,
         "phases": phases, "wall_s_timed_region": t_wall,
@@ -1031,7 +1031,7 @@ def run_bm(args):
         "metric": "Burton-Miller system entries/s", "impl": "ours", "value": entries / (ms / 1e3),
         "unit": "entries/s", "n_gpus": 1, "steps": args.steps, "warmup": max(3, args.warmup), "ms_per_step": ms,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "fp32 regular quadrature and nearly singular dynamic parts, fp64 self terms and nearly singular static parts; complex64 storage",
+        "dtype": "fp32 regular quadrature, nearly singular dynamic parts and static angular sums, fp64 self terms and nearly singular geometry; complex64 storage",
         "data": "synthetic (icosphere mesh generated in-process)",
         "config": {"workload": "icosphere s=5 (%d flat constant triangles), Helmholtz 3D Burton-Miller system "
                                "A = DLP - I/2 + c HSP, B = SLP + c DLPt + c/2 I, c = -i/k, k=5" % n,

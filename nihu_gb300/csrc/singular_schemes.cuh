@@ -104,36 +104,62 @@ __device__ inline void near_static(const Elem64 &e, const double x0[3], bool do_
 }
 
 // near_static with the angular point sums in FP32 (the FP32 regular
-// quadrature mode).  The plane frame, the side distances and the angle limits
-// stay FP64.  Per side, with the reference's 6 points: the SLP sums
-// r - |z| = R^2 / (r + |z|) (positive, no cancellation) and the DLP sums
-// 1 - |z|/r as sum(w) (t2 - t1)/2 - sum(w |z|/r) (t2 - t1)/2, the first part
-// in FP64 -- over the sides it adds up to 2 pi or 0, and summing the O(1)
-// terms in FP32 instead would leave FP32 rounding of that size in a DLP
-// entry of a point whose foot lies outside the element, where the sides
-// cancel -- and the second in FP32; the sides are added in FP64.
+// quadrature mode).  The plane frame and the foot vectors stay FP64.  Per side,
+// with the reference's 6 points: the SLP sums r - |z| = R^2 / (r + |z|)
+// (positive, no cancellation) and the DLP sums 1 - |z|/r as
+// sum(w) (t2 - t1)/2 - sum(w |z|/r) (t2 - t1)/2.  Over the sides the first
+// part adds up to sum(w)/2 times the winding angle of the polygon around the
+// foot point: 2 pi inside, 0 outside, which an FP64 point-in-polygon test
+// gives exactly (summed in FP32, those O(1) terms would leave FP32 rounding
+// of that size in a DLP entry whose foot point lies outside the element,
+// where the sides cancel).  A foot point within rounding of a side takes
+// near_static itself.
 __device__ inline void near_static_f32(const Elem64 &e, const double x0[3], bool do_s, bool do_d, Acc &a)
 {
     double loc[4][2], z;
     plane_local(e, x0, loc, z);
     const int N = e.nc;
-    double tl[4], t0[4], dr[4];
-    for (int s = 0; s < N; ++s) side_geometry(loc[s], loc[(s + 1) % N], tl[s], t0[s], dr[s], false);
-    const float az = (float)fabs(z), z2 = az * az;
+    // winding of the (counter-clockwise) polygon around the foot point
+    double scale = 0.0;
+    for (int s = 0; s < N; ++s) scale = fmax(scale, loc[s][0] * loc[s][0] + loc[s][1] * loc[s][1]);
+    int pos = 0, neg = 0;
+    for (int s = 0; s < N; ++s) {
+        const double *c1 = loc[s], *c2 = loc[(s + 1) % N];
+        const double cr = c1[0] * c2[1] - c1[1] * c2[0];
+        if (fabs(cr) <= 1e-9 * scale) {
+            near_static(e, x0, do_s, do_d, a);
+            return;
+        }
+        if (cr > 0.0) ++pos;
+        else ++neg;
+    }
+    const double wind = pos == N ? 2.0 * PI : (neg == N ? -2.0 * PI : 0.0);
     double wsum = 0.0;
     for (int q = 0; q < 6; ++q) {
         double xi, w;
         gauss_pt(6, q, xi, w);
         wsum += w;
     }
-    double s_sum = 0.0, d_sum = 0.0;
+    const float az = (float)fabs(z), z2 = az * az;
+    double s_sum = 0.0, dz_sum = 0.0;
     for (int s = 0; s < N; ++s) {
-        double t1 = tl[s], t2 = tl[(s + 1) % N];
-        wrap_limits(t1, t2);
-        const double jac = (t2 - t1) / 2.0;
-        // the angle from the side's foot direction at the rule's ends
-        const float p1 = (float)(t1 - t0[s]), p2 = (float)(t2 - t0[s]);
-        const float ds = (float)dr[s];
+        const double *c1 = loc[s], *c2 = loc[(s + 1) % N];
+        // side s seen from the foot point: the foot vector f (distance ds) and
+        // the corners' angles measured from it, p = atan2(f x c, f . c) in
+        // (-pi/2, pi/2), so that the reference's th - t0 = p1 (1 - x)/2 +
+        // p2 (1 + x)/2 and t2 - t1 = p2 - p1 come without cancellation.  f is
+        // a difference of nearly equal vectors when ds is small against the
+        // corners' distance, so it and the angle arguments are FP64; the
+        // angles themselves and the point sums are FP32.
+        const double d0 = c2[0] - c1[0], d1 = c2[1] - c1[1];
+        const double il = rsqrt(d0 * d0 + d1 * d1);
+        const double l0 = d0 * il, l1 = d1 * il;
+        const double pr = c1[0] * l0 + c1[1] * l1;
+        const double f0 = c1[0] - l0 * pr, f1 = c1[1] - l1 * pr;
+        const float ds = (float)sqrt(f0 * f0 + f1 * f1);
+        const float p1 = atan2f((float)(f0 * c1[1] - f1 * c1[0]), (float)(f0 * c1[0] + f1 * c1[1]));
+        const float p2 = atan2f((float)(f0 * c2[1] - f1 * c2[0]), (float)(f0 * c2[0] + f1 * c2[1]));
+        const float jac = (p2 - p1) * 0.5f;
         float ss = 0.0f, sz = 0.0f;
         for (int q = 0; q < 6; ++q) {
             double xi, w;
@@ -146,9 +172,10 @@ __device__ inline void near_static_f32(const Elem64 &e, const double x0[3], bool
             ss += wf * (R2 / (r + az));  // r - |z|
             sz += wf * (az / r);         // |z| / r
         }
-        s_sum += jac * (double)ss;
-        d_sum += jac * (wsum - (double)sz);
+        s_sum += (double)(jac * ss);
+        dz_sum += (double)(jac * sz);
     }
+    const double d_sum = 0.5 * wind * wsum - dz_sum;
     const double sg = (0.0 < z) - (z < 0.0);
     if (do_s) a.sr += s_sum * INV_FOUR_PI;
     if (do_d) a.dr += sg * d_sum * INV_FOUR_PI;
