@@ -258,6 +258,19 @@ nihu_gb_status nihu_gb_assemble_pairs(nihu_gb_ctx *ctx, const nihu_gb_mesh *test
 nihu_gb_status nihu_gb_pair_statistics(nihu_gb_ctx *ctx, const nihu_gb_mesh *test, const nihu_gb_mesh *trial,
                                        int64_t counts[11]);
 
+/* The nearly singular pair list that the assemblies of (test, trial) use,
+ * column-sorted: the rows of trial column j, in increasing order, are
+ * rows[col_ptr[j] .. col_ptr[j + 1]).  *nnz receives the length; col_ptr
+ * (n_trial + 1 entries) and rows (*nnz entries) are written when not NULL,
+ * so a first call with NULL arrays sizes them.  The list is built once per
+ * mesh pair and kept in the context.
+ * Replaces: the per-pair nearly singular test of the reference's double
+ * integral dispatch (nihu/core/double_integral.hpp:543-639 with
+ * nihu/library/helmholtz_nearly_singular_integrals.hpp:234-246), which it
+ * evaluates for every pair of every assembly. */
+nihu_gb_status nihu_gb_near_pairs(nihu_gb_ctx *ctx, const nihu_gb_mesh *test, const nihu_gb_mesh *trial,
+                                  int64_t *nnz, int64_t *col_ptr, int32_t *rows);
+
 /* ------------------------------------------------------------- linear algebra */
 
 /* y = alpha * A x + beta * y; A is m x n (dtype_a, column-major, lda), x and

@@ -11,7 +11,7 @@ from .api import (Context, DeviceMesh, Mesh, Server, SweepPlan, assemble_burton_
                   constant_view, create_integral_operator, create_mesh, default_context,
                   dirac, gemm, gmres, helmholtz_3d_DLP_kernel, helmholtz_3d_DLPt_kernel, helmholtz_3d_HSP_kernel,
                   helmholtz_3d_SLP_kernel, identity_integral_operator, laplace_3d_DLP_kernel, laplace_3d_DLPt_kernel,
-                  laplace_3d_HSP_kernel, laplace_3d_SLP_kernel, lu_solve, matvec, pair_statistics, solve_burton_miller, solve_cbie,
+                  laplace_3d_HSP_kernel, laplace_3d_SLP_kernel, lu_solve, matvec, near_pairs, pair_statistics, solve_burton_miller, solve_cbie,
                   solve_batched, solve_multi, solve_sweep, solve_sweep_batched)
 from . import meshes
 
@@ -20,7 +20,7 @@ __all__ = [
     "SLP", "TRIA_1", "InvalidArgumentError", "NihuError", "NotConvergedError", "OutOfRangeError", "lib", "Context", "Server", "SweepPlan",
     "DeviceMesh", "Mesh", "constant_view", "create_integral_operator", "create_mesh", "default_context", "dirac",
     "gmres", "helmholtz_3d_DLP_kernel", "helmholtz_3d_SLP_kernel", "identity_integral_operator",
-    "laplace_3d_DLP_kernel", "laplace_3d_SLP_kernel", "lu_solve", "matvec", "pair_statistics", "solve_cbie", "meshes",
+    "laplace_3d_DLP_kernel", "laplace_3d_SLP_kernel", "lu_solve", "matvec", "near_pairs", "pair_statistics", "solve_cbie", "meshes",
     "DLPT", "HSP", "helmholtz_3d_DLPt_kernel", "helmholtz_3d_HSP_kernel", "laplace_3d_DLPt_kernel", "laplace_3d_HSP_kernel",
     "assemble_burton_miller", "assemble_pairs", "burton_miller_coupling", "solve_burton_miller",
 ]

@@ -52,6 +52,7 @@ SIGNATURES = {
     "nihu_gb_assemble_c": (_i, [_vp, _vp, _vp, _i, _i, _d, _d, _d, _d, _i, _i, _vp, _vp, _i64, _i, _i]),
     "nihu_gb_add_identity": (_i, [_vp, _vp, _d, _d, _i, _vp, _i64, _i]),
     "nihu_gb_pair_statistics": (_i, [_vp, _vp, _vp, ctypes.POINTER(ctypes.c_int64)]),
+    "nihu_gb_near_pairs": (_i, [_vp, _vp, _vp, ctypes.POINTER(ctypes.c_int64), _vp, _vp]),
     "nihu_gb_matvec": (_i, [_vp, _i, _vp, _i64, _i64, _i64, _vp, _vp, _d, _d, _d, _d, _i]),
     "nihu_gb_matvec_noalloc": (_i, [_i, _vp, _i64, _i64, _i64, _vp, _vp, _d, _d, _d, _d, _vp]),
     "nihu_gb_gmres": (_i, [_vp, _i, _vp, _i64, _i64, _vp, _vp, _i, _i, _d, _ip, _dp, _i]),

@@ -825,6 +825,21 @@ class Server:
             pass
 
 
+def near_pairs(test: Mesh, trial: Mesh, ctx: Context | None = None) -> tuple[np.ndarray, np.ndarray]:
+    """The nearly singular pair list of (test, trial): (col_ptr, rows), the
+    rows of trial column j in increasing order at rows[col_ptr[j]:col_ptr[j+1]]."""
+    ctx = ctx or default_context()
+    tdm = test.device(ctx)
+    rdm = tdm if test is trial else trial.device(ctx)
+    nnz = ctypes.c_int64()
+    ctx.check(C.lib().nihu_gb_near_pairs(ctx.handle, tdm.handle, rdm.handle, ctypes.byref(nnz), None, None))
+    col_ptr = np.zeros(rdm.n + 1, np.int64)
+    rows = np.zeros(max(nnz.value, 1), np.int32)
+    ctx.check(C.lib().nihu_gb_near_pairs(ctx.handle, tdm.handle, rdm.handle, ctypes.byref(nnz),
+                                         col_ptr.ctypes.data, rows.ctypes.data))
+    return col_ptr, rows[:nnz.value]
+
+
 def pair_statistics(test: Mesh, trial: Mesh, ctx: Context | None = None) -> np.ndarray:
     """[self, near, regular (SLP level, DLP level) 3x3] pair counts."""
     ctx = ctx or default_context()

@@ -214,32 +214,36 @@ nihu_gb_status get_near(nihu_gb_ctx *ctx, const nihu_gb_mesh *test, const nihu_g
     NearList nl;
     nl.n_cols = (int)trial->n;
     int same = test == trial;
-    void *counts = nullptr, *colptr = nullptr;
+    void *counts = nullptr, *colptr = nullptr, *grid = nullptr;
     nihu_gb_status st = dmalloc(ctx, sizeof(int) * (trial->n + 1), &counts);
     if (st) return st;
     st = dmalloc(ctx, sizeof(int64_t) * (trial->n + 1), &colptr);
     if (st) { dfree(ctx, counts); return st; }
     nl.col_ptr = (int64_t *)colptr;
+    st = scratch(ctx, "near_grid", near_grid_scratch_bytes((int)test->n), &grid);
+    if (st) { dfree(ctx, counts); free_near(ctx, nl); return st; }
     cudaError_t e;
     {
         Phase ph(ctx, "near_list");
-        e = launch_near_count(test->dm, trial->dm, same, (int *)counts, ctx->stream);
+        e = launch_near_grid_count(test->dm, trial->dm, same, grid, (int *)counts, ctx->stream);
         if (e == cudaSuccess) e = launch_scan((int *)counts, (int)trial->n, nl.col_ptr, ctx->stream);
     }
-    ctx->launches += 2;
+    ctx->launches += 5;
     int64_t nnz = 0;
     if (e == cudaSuccess) e = cudaMemcpyAsync(&nnz, nl.col_ptr + trial->n, sizeof(int64_t), cudaMemcpyDeviceToHost, ctx->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
     dfree(ctx, counts);
     if (e != cudaSuccess) { free_near(ctx, nl); return cuda_fail(ctx, e, "nearly singular pair count"); }
     nl.nnz = nnz;
-    void *rows = nullptr;
+    void *rows = nullptr, *tmp = nullptr;
     st = dmalloc(ctx, sizeof(int) * (nnz > 0 ? nnz : 1), &rows);
     if (st) { free_near(ctx, nl); return st; }
     nl.rows = (int *)rows;
+    st = scratch(ctx, "near_grid_rows", sizeof(int) * (nnz > 0 ? nnz : 1), &tmp);
+    if (st) { free_near(ctx, nl); return st; }
     {
         Phase ph(ctx, "near_list");
-        e = launch_near_fill(test->dm, trial->dm, same, nl.col_ptr, nl.rows, ctx->stream);
+        e = launch_near_grid_fill(test->dm, trial->dm, same, grid, nl.col_ptr, (int *)tmp, nl.rows, ctx->stream);
     }
     ctx->launches += 1;
     if (e != cudaSuccess) { free_near(ctx, nl); return cuda_fail(ctx, e, "nearly singular pair fill"); }
@@ -1174,6 +1178,21 @@ nihu_gb_status nihu_gb_pair_statistics(nihu_gb_ctx *ctx, const nihu_gb_mesh *tes
     st = sync(ctx);
     for (int q = 0; q < 11; ++q) counts[q] = (int64_t)h[q];
     return st;
+}
+
+nihu_gb_status nihu_gb_near_pairs(nihu_gb_ctx *ctx, const nihu_gb_mesh *test, const nihu_gb_mesh *trial,
+                                  int64_t *nnz, int64_t *col_ptr, int32_t *rows)
+{
+    if (!ctx) return NIHU_GB_ERR_INVALID_ARGUMENT;
+    if (!test || !trial || !nnz) return fail(ctx, NIHU_GB_ERR_INVALID_ARGUMENT, "nihu_gb_near_pairs: bad argument");
+    cudaSetDevice(ctx->device);
+    NearList *nl = nullptr;
+    nihu_gb_status st = get_near(ctx, test, trial, &nl);
+    if (st) return st;
+    *nnz = nl->nnz;
+    if (col_ptr) CK(cudaMemcpyAsync(col_ptr, nl->col_ptr, sizeof(int64_t) * (trial->n + 1), cudaMemcpyDeviceToHost, ctx->stream));
+    if (rows && nl->nnz) CK(cudaMemcpyAsync(rows, nl->rows, sizeof(int32_t) * nl->nnz, cudaMemcpyDeviceToHost, ctx->stream));
+    return sync(ctx);
 }
 
 // ------------------------------------------------------------------ matvec

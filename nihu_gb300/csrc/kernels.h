@@ -31,13 +31,20 @@ cudaError_t launch_mesh_geometry(const double *nodes, int64_t n_nodes, const int
                                  int cols, DevMesh m, int *bad, unsigned long long *size_max, cudaStream_t s);
 
 // classify.cu -------------------------------------------------------------
-// count the nearly singular rows of every column: counts[j]
-cudaError_t launch_near_count(const DevMesh &test, const DevMesh &trial, int same_mesh, int *counts,
-                              cudaStream_t s);
+// nearly singular pair lists over a uniform grid of the test centres; the
+// grid lives in a scratch buffer of near_grid_scratch_bytes(test.n) bytes
+size_t near_grid_buckets(int n_test);
+size_t near_grid_scratch_bytes(int n_test);
+// builds the grid in scratch and counts the nearly singular rows of every
+// column: counts[j]
+cudaError_t launch_near_grid_count(const DevMesh &test, const DevMesh &trial, int same_mesh, void *scratch,
+                                   int *counts, cudaStream_t s);
 // exclusive scan of counts into col_ptr (n + 1 entries), single block
 cudaError_t launch_scan(const int *counts, int n, int64_t *col_ptr, cudaStream_t s);
-cudaError_t launch_near_fill(const DevMesh &test, const DevMesh &trial, int same_mesh, const int64_t *col_ptr,
-                             int *rows, cudaStream_t s);
+// with the grid of launch_near_grid_count still in scratch: the rows of
+// column j in increasing order to rows[col_ptr[j] ..]; tmp has the size of rows
+cudaError_t launch_near_grid_fill(const DevMesh &test, const DevMesh &trial, int same_mesh, void *scratch,
+                                  const int64_t *col_ptr, int *tmp, int *rows, cudaStream_t s);
 // histogram of pair classes (see nihu_gb_pair_statistics)
 cudaError_t launch_pair_stats(const DevMesh &test, const DevMesh &trial, int same_mesh,
                               unsigned long long *counts, cudaStream_t s);

@@ -251,6 +251,59 @@ def test_pair_statistics_match_oracle(gpu_ctx, oracle, name):
     assert stats.sum() == codes.size
 
 
+def graded_mesh():
+    """A quad cylinder stretched along its axis (element sizes over a range
+    of about 8), two far-apart copies of a small icosphere, and one triangle
+    about 60 times the mean element size across the cylinder: columns whose
+    search box covers 1 to many grid cells, and one that scans all rows."""
+    cn, ce = meshes.cylinder(12, 10, 2, radius=1.0, length=3.0)
+    cn = cn.copy()
+    z = cn[:, 2] / 3.0
+    cn[:, 2] = 3.0 * np.sign(z) * np.abs(z) ** 2.5
+    sn, se = meshes.icosphere(2)
+    parts_n, parts_e, off = [cn], [ce], len(cn)
+    for shift in ((1.0e4, 0.0, 0.0), (-3.0e3, 2.0e3, 5.0)):
+        parts_n.append(0.3 * sn + np.array(shift))
+        e = se.copy()
+        e[:, 1:4] += off
+        parts_e.append(e)
+        off += len(sn)
+    big = np.array([[-6.0, -4.0, 1.2], [6.0, -4.0, 1.2], [0.0, 7.0, 1.2]])
+    parts_n.append(big)
+    parts_e.append(np.array([[g.TRIA_1, off, off + 1, off + 2, -1]], dtype=np.int32))
+    width = max(e.shape[1] for e in parts_e)
+    parts_e = [np.hstack([e, -np.ones((len(e), width - e.shape[1]), np.int32)]) for e in parts_e]
+    return np.vstack(parts_n), np.vstack(parts_e).astype(np.int32)
+
+
+def check_near_pairs(ctx, oracle, test_mesh, trial_mesh, same):
+    test = g.create_mesh(*test_mesh)
+    trial = test if same else g.create_mesh(*trial_mesh)
+    col_ptr, rows = g.near_pairs(test, trial, ctx=ctx)
+    codes = oracle.classify(test_mesh, trial_mesh, same_mesh=same)
+    assert col_ptr[0] == 0 and len(rows) == col_ptr[-1]
+    for j in range(codes.shape[1]):
+        np.testing.assert_array_equal(rows[col_ptr[j]:col_ptr[j + 1]], np.flatnonzero(codes[:, j] == -2))
+    return len(rows)
+
+
+@pytest.mark.parametrize("name", ["ico3", "cyl", "mixed", "sphere_1_5", "graded"])
+def test_near_pairs_match_oracle(gpu_ctx, oracle, name):
+    """The grid-built nearly singular list is the brute-force list of the
+    reference's test d / D_j < 1.5, rows in increasing order per column."""
+    mesh = graded_mesh() if name == "graded" else get_mesh(name)
+    assert check_near_pairs(gpu_ctx, oracle, mesh, mesh, True) > 0
+
+
+def test_near_pairs_two_meshes(gpu_ctx, oracle):
+    """Test and trial meshes of different sizes and element scales."""
+    ico = meshes.icosphere(3)
+    small = (0.97 * meshes.icosphere(2)[0], meshes.icosphere(2)[1])
+    assert check_near_pairs(gpu_ctx, oracle, small, ico, False) > 0
+    assert check_near_pairs(gpu_ctx, oracle, ico, small, False) > 0
+    assert check_near_pairs(gpu_ctx, oracle, graded_mesh(), ico, False) >= 0
+
+
 def test_nihu_shaped_api(gpu_ctx, oracle):
     """Ls << dirac(sp) * Lop[sp]; Ms << dirac(sp) * Mop[sp]; Ms << dirac(sp) * (-.5*I)[sp]
     (nihu/test/matlab/acoustic_bem.mex.cpp:30-50)."""
