@@ -70,7 +70,8 @@ def parse(argv=None):
     prof = p.add_argument_group("profile", "--config profile: the assembly of one mesh, or a sweep")
     prof.add_argument("--subdiv", type=int, default=5, help="icosphere subdivisions (20 * 4^s triangles)")
     prof.add_argument("--cylinder", type=int, default=0, metavar="N_THETA",
-                      help="closed quad cylinder with this many elements around instead (n_z = 1.25 n_theta)")
+                      help="closed quad cylinder with this many elements around instead (n_z = 1.25 n_theta, "
+                           "15 n_theta / 160 cap rings: 160 gives the 40000-quad cylinder's proportions)")
     prof.add_argument("--k", type=float, default=5.0, help="wave number")
     prof.add_argument("--laplace", action="store_true")
     prof.add_argument("--budget-mb", type=int, default=0,
@@ -80,6 +81,9 @@ def parse(argv=None):
     prof.add_argument("--bm", action="store_true", help="the Burton-Miller system instead of SLP and DLP")
     prof.add_argument("--sweep", type=int, default=0, metavar="N", help="frequency sweep of N wave numbers")
     prof.add_argument("--sweep-config4", action="store_true", help="the 256-instance sweep on three icospheres")
+    prof.add_argument("--gemm", type=int, nargs=3, default=None, metavar=("M", "N", "NRHS"),
+                      help="the multi-RHS product Y = A X of a random complex64 M x N matrix in device memory")
+    prof.add_argument("--gemm-mode", type=int, default=3, help="GEMM arithmetic (nihu_gb300.h NIHU_GB_GEMM_*)")
     return p.parse_args(argv)
 
 
@@ -887,10 +891,13 @@ def run_serve(args):
     while sv.take() is not None:
         pass
     torch.cuda.synchronize()
+    ctx.set_profiling(True)
+    ctx.profile_reset()
     done_t = np.full(n_req, np.nan)
     results = {}
     id_of = {}
     steps = 0
+    host = {"submit": 0.0, "step": 0.0, "take": 0.0, "idle": 0.0}
     t0 = time.perf_counter()
     nxt = 0
     n_done = 0
@@ -899,9 +906,12 @@ def run_serve(args):
         while nxt < n_req and arrivals[nxt] <= now:
             id_of[sv.submit(int(which[nxt]), float(ks[nxt]), qs[nxt])] = nxt
             nxt += 1
+        t_a = time.perf_counter()
+        host["submit"] += t_a - t0 - now
         queued, active, _ = sv.step()
         steps += 1
         t_step = time.perf_counter() - t0
+        host["step"] += t_step - (t_a - t0)
         while True:
             t = sv.take()
             if t is None:
@@ -910,11 +920,15 @@ def run_serve(args):
             done_t[r] = t_step
             results[r] = t
             n_done += 1
+        host["take"] += time.perf_counter() - t0 - t_step
         if queued == 0 and active == 0 and nxt < n_req:
             wait = arrivals[nxt] - (time.perf_counter() - t0)
             if wait > 0:
                 time.sleep(wait)
+                host["idle"] += wait
     t_end = float(np.nanmax(done_t))
+    prof = ctx.profile()
+    ctx.set_profiling(False)
     sv.close()
     lat = done_t - arrivals
     its = np.array([results[r][2] for r in range(n_req)])
@@ -928,6 +942,16 @@ def run_serve(args):
                           "mean": float(lat.mean() * 1e3), "max": float(lat.max() * 1e3)},
            "converged": int(conv.sum()),
            "per_mesh": {}}
+    # where the wall time goes: device phases (CUDA events on the server's
+    # stream), host time inside the calls, and the HBM floor of the stream --
+    # every DLP matrix written once and read once per GMRES iteration
+    # (complex64, 8 n^2 bytes), at the measured copy bandwidth
+    peak, _ = measured_peaks()
+    floor_bytes = sum(8.0 * sizes[which[r]] ** 2 * (1 + its[r]) for r in range(n_req))
+    out["phases_ms"] = {k_: round(v_[0], 3) for k_, v_ in prof.items()}
+    out["host_s"] = {k_: round(v_, 4) for k_, v_ in host.items()}
+    out["hbm_floor"] = {"bytes": floor_bytes, "seconds": floor_bytes / (peak * 1e9),
+                        "solves_per_s": n_req / (floor_bytes / (peak * 1e9))}
     for i, n in enumerate(sizes):
         sel = which == i
         if sel.any():
@@ -1441,9 +1465,12 @@ def run_profile(args):
                 "phases_ms": {k: round(v[0], 4) for k, v in prof.items()},
                 "launches": {k: v[1] for k, v in prof.items()}}
 
+    if args.gemm:
+        return profile_gemm(args)
+
     if args.cylinder:
         nt = args.cylinder
-        nodes, elems = meshes.cylinder(nt, int(1.25 * nt), max(2, nt // 10))
+        nodes, elems = meshes.cylinder(nt, int(1.25 * nt), max(2, round(15 * nt / 160)))
     else:
         nodes, elems = meshes.icosphere(args.subdiv)
     ctx = api.Context(0, hbm_budget_bytes=args.budget_mb << 20)
@@ -1482,6 +1509,42 @@ def run_profile(args):
             "launches": {k: v[1] for k, v in prof.items()}}
 
 
+def profile_gemm(args):
+    """--config profile --gemm M N NRHS: nihu_gb_gemm on device buffers,
+    --reps times, timed with CUDA events on the context's stream."""
+    import nihu_gb300 as g
+    from nihu_gb300 import _capi as C
+    from nihu_gb300 import api
+
+    m, n, nrhs = args.gemm
+    ctx = api.Context(0)
+    L = g.lib()
+    rng = np.random.default_rng(7)
+    bufs = []
+
+    def dev(host):
+        p = ctypes.c_void_p()
+        ctx.check(L.nihu_gb_device_alloc(ctx.handle, host.nbytes, ctypes.byref(p)))
+        ctx.check(L.nihu_gb_memcpy(ctx.handle, p, C.DEVICE, host.ctypes.data, C.HOST, host.nbytes))
+        bufs.append(p)
+        return p
+
+    A = dev((rng.standard_normal((m, n)) + 1j * rng.standard_normal((m, n))).astype(np.complex64, order="F"))
+    X = dev(np.asfortranarray(rng.standard_normal((n, nrhs)) + 1j * rng.standard_normal((n, nrhs))))
+    Y = dev(np.zeros((m, nrhs), np.complex128, order="F"))
+    times = []
+    for _ in range(max(1, args.reps)):
+        t0 = time.perf_counter()
+        ctx.check(L.nihu_gb_gemm(ctx.handle, args.gemm_mode, A, m, n, m, X, n, nrhs, Y, m, 1.0, 0.0, 0.0, 0.0,
+                                 C.DEVICE))
+        times.append((time.perf_counter() - t0) * 1e3)
+    for p in bufs:
+        L.nihu_gb_device_free(ctx.handle, p)
+    ctx.close()
+    return {"config": "profile (gemm)", "m": m, "n": n, "nrhs": nrhs, "mode": args.gemm_mode,
+            "host_ms": [round(t, 4) for t in times], "a_bytes": 8 * m * n}
+
+
 def other_configs(args):
     """Short runs of the other configurations, summarised for the headline
     line: the plain small solve, the multi-RHS solve, the batched sweep and
@@ -1514,7 +1577,7 @@ def other_configs(args):
         ("serve", lambda: run_serve(sub(requests=300, plain_sample=3)),
          ("metric", "value", "unit", "requests", "arrival_rate_per_s", "latency_ms", "converged",
           "plain_solves_per_s", "speedup_vs_plain_gpu", "served_vs_plain_max_rel_difference", "rounds",
-          "phases_ms")),
+          "phases_ms", "host_s", "hbm_floor", "plain_seconds_per_request", "per_mesh")),
     )
     for name, fn, keys in legs:
         t0 = time.perf_counter()

@@ -2751,6 +2751,7 @@ extern "C" nihu_gb_status nihu_gb_server_step(nihu_gb_server *sv, int *n_queued,
     const int m = sv->restart;
     // 1. admission, first come first served, while the budget and the state slots hold
     std::vector<SrvReq *> fresh;
+    std::unique_ptr<Phase> ph_admit(new Phase(ctx, "serve_admit"));
     while (!sv->queue.empty() && !sv->free_slots.empty()) {
         SrvReq *r = sv->queue.front();
         const int64_t n = sv->meshes[r->mesh]->n;
@@ -2775,6 +2776,7 @@ extern "C" nihu_gb_status nihu_gb_server_step(nihu_gb_server *sv, int *n_queued,
         sv->queue.pop_front();
         fresh.push_back(r);
     }
+    ph_admit.reset();
     // 2. assembly of the new requests, one frequency batch per mesh: the DLP
     // matrices and the right-hand sides b = SLP q (no SLP matrix)
     std::vector<std::vector<void *>> tables;  // host sources of the pointer uploads, alive until the round's wait
@@ -2807,6 +2809,7 @@ extern "C" nihu_gb_status nihu_gb_server_step(nihu_gb_server *sv, int *n_queued,
                                  NIHU_GB_C64, nullptr, grp[0]->H, n, n * n, (void *const *)douts, true,
                                  (const double2 *)gq, (double2 *)gb)))
             return st;
+        Phase ph_rhs(ctx, "serve_identity_rhs");
         for (int f = 0; f < nk; ++f) {
             SrvReq *r = grp[f];
             CK(launch_add_identity((int)n, -0.5, 0.0, NIHU_GB_C64, r->H, n, s));
@@ -2838,7 +2841,10 @@ extern "C" nihu_gb_status nihu_gb_server_step(nihu_gb_server *sv, int *n_queued,
     }
     // 4. retire the finished systems
     std::vector<PersistentState> hs(sv->n_slots);
-    CK(cudaMemcpyAsync(hs.data(), sv->d_states, sizeof(PersistentState) * sv->n_slots, cudaMemcpyDeviceToHost, s));
+    {
+        Phase ph(ctx, "serve_state_read");
+        CK(cudaMemcpyAsync(hs.data(), sv->d_states, sizeof(PersistentState) * sv->n_slots, cudaMemcpyDeviceToHost, s));
+    }
     if ((st = sync(ctx))) return st;
     std::vector<SrvReq *> still;
     std::vector<SrvReq *> finished;
@@ -2847,10 +2853,13 @@ extern "C" nihu_gb_status nihu_gb_server_step(nihu_gb_server *sv, int *n_queued,
         if (r->st.status == PG_DONE) finished.push_back(r);
         else still.push_back(r);
     }
-    for (SrvReq *r : finished) {
-        const int64_t n = sv->meshes[r->mesh]->n;
-        r->q.resize(n);
-        CK(cudaMemcpyAsync(r->q.data(), r->x, 16 * (size_t)n, cudaMemcpyDeviceToHost, s));
+    {
+        Phase ph(ctx, "serve_result_read");
+        for (SrvReq *r : finished) {
+            const int64_t n = sv->meshes[r->mesh]->n;
+            r->q.resize(n);
+            CK(cudaMemcpyAsync(r->q.data(), r->x, 16 * (size_t)n, cudaMemcpyDeviceToHost, s));
+        }
     }
     if (!finished.empty() && (st = sync(ctx))) return st;
     for (SrvReq *r : finished) {
