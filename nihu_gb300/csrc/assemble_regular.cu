@@ -464,16 +464,39 @@ __global__ void __launch_bounds__(REG_THREADS) k_regular(RegularArgs a)
     }
 }
 
+int regular_carveout_percent()
+{
+    // four blocks of k_regular2 (under 10 KB of shared memory each, plus the
+    // 1 KB the runtime reserves per block): the 64 KB configuration
+    return 25;
+}
+
 // ------------------------------------------------- two rows per thread
 // The single wave number FP32 kernel for the common case (SLP and DLP, unit
 // scale, no accumulation, complex64 columns that allow 16-byte stores): each
 // thread owns two adjacent rows, so that one far vote, one set of shared
 // loads and the loop's bookkeeping serve two pairs, and each column takes one
-// 16-byte store per matrix for both rows.  The points, levels and their order
-// are those of k_regular (the far path, the certain-level path, and the
-// general per-lane dispatch, here per row), so the entries are the same.
+// 16-byte store per matrix for both rows.
+//
+// A column whose 64 rows of a warp are not all far (about 13% of the warp
+// iterations on an icosphere, with some 45 of the 64 pairs not far) is not
+// evaluated in that warp: its far rows take the centroid there, certainly
+// nearly singular and self pairs are left to the singular kernel, and the
+// others are appended to a block-local list in shared memory (one 16-bit
+// code per pair: row in the block, column in the block), from the front when
+// their levels are certain without the FP64 check (SLP 1 point, DLP level 1:
+// most of them) and from the back otherwise.  Every REG2_CHUNK columns all
+// 256 threads work through the two lists, so that a pair's cost is its own
+// point count, not the largest one in its warp.  A list holds every pair of
+// a chunk, so it cannot overflow, and a block needs under 10 KB of shared
+// memory.  The points, levels and their order are those of k_regular (the
+// far path, the certain-level path and the general dispatch), so the entries
+// are the same.
 constexpr int REG2_THREADS = 256;
 constexpr int REG2_ROWS = 2 * REG2_THREADS;
+constexpr int REG2_CHUNK = 8;                        // columns per list flush
+constexpr int REG2_LIST = REG2_ROWS * REG2_CHUNK;    // every pair of a chunk
+static_assert(REG2_ROWS <= 512 && REG_COLS <= 128, "a pair code is row (9 bits) | column << 9 in 16 bits");
 
 // one pair by the general path of k_regular (classify_pair, the uniform loop
 // over the lane's points); false when the pair is not regular
@@ -505,97 +528,155 @@ __device__ __forceinline__ bool pair_general32(const RegularArgs &a, const float
     return true;
 }
 
+// the deferred pairs of one chunk: certain levels (the centroid for the SLP,
+// the level-1 points for the DLP) from the front of the list, the others
+// (classify_pair and the pair's own rule) from the back
+template <int FAM>
+__device__ __forceinline__ void regular2_flush(const RegularArgs &a, const unsigned short *s_list, int nA, int nB,
+                                               int ib, int jb, const float4 *s_hi, const float4 *s_lo,
+                                               const int *s_nc, float2 *out_s, float2 *out_d, int64_t ldo, float k)
+{
+    const DevMesh &test = a.test;
+    const DevMesh &trial = a.trial;
+    for (int t = threadIdx.x; t < nA; t += REG2_THREADS) {
+        const int code = s_list[t];
+        const int i = ib + (code & 511), c = code >> 9, j = jb + c;
+        const float4 ih = test.chi[i], il = test.clo[i], h = s_hi[c], l = s_lo[c];
+        const int par = il.w != 0.0f ? 1 : 0;
+        const float mx = (h.x - ih.x) + (l.x - il.x), my = (h.y - ih.y) + (l.y - il.y),
+                    mz = (h.z - ih.z) + (l.z - il.z);
+        const int64_t base = ((int64_t)j * 2 + par) * SLOTS;
+        float sr = 0, si = 0, dr = 0, di = 0;
+        const float4 yc = __ldg(trial.pts32 + 2 * base), nc = __ldg(trial.pts32 + 2 * base + 1);
+        eval_point<FAM, float>(mx, my, mz, yc.w, nc.x, nc.y, nc.z, k, 1.0f, 0.0f, sr, si, dr, di);
+        const int npd = level_npts(s_nc[c], par, 1);
+        for (int q = 0; q < npd; ++q) {
+            const int64_t sl = base + level_slot0(1) + q;
+            const float4 y = __ldg(trial.pts32 + 2 * sl), n = __ldg(trial.pts32 + 2 * sl + 1);
+            eval_point<FAM, float>(mx + y.x, my + y.y, mz + y.z, y.w, n.x, n.y, n.z, k, 0.0f, 1.0f, sr, si, dr, di);
+        }
+        out_s[(int64_t)c * ldo + i] = make_float2(sr, si);
+        out_d[(int64_t)c * ldo + i] = make_float2(dr, di);
+    }
+    for (int t = threadIdx.x; t < nB; t += REG2_THREADS) {
+        const int code = s_list[REG2_LIST - 1 - t];
+        const int i = ib + (code & 511), c = code >> 9, j = jb + c;
+        const float4 ih = test.chi[i], il = test.clo[i];
+        float sr, si, dr, di;
+        if (pair_general32<FAM>(a, ih, il, il.w != 0.0f ? 1 : 0, i, j, s_hi[c], s_lo[c], s_nc[c], k, sr, si, dr, di)) {
+            out_s[(int64_t)c * ldo + i] = make_float2(sr, si);
+            out_d[(int64_t)c * ldo + i] = make_float2(dr, di);
+        }
+    }
+}
+
 template <int FAM>
 // 64 registers: three blocks fit beside the concurrent singular kernel's one
 __global__ void __launch_bounds__(REG2_THREADS, 4) k_regular2(RegularArgs a)
 {
     __shared__ float4 s_hi[REG_COLS], s_lo[REG_COLS], s_p0[REG_COLS];
     __shared__ int s_nc[REG_COLS];
+    __shared__ unsigned short s_list[REG2_LIST];
+    // per chunk parity: certain-level pairs (from the front), the others (from the back)
+    __shared__ int s_cnt[2][2];
     const DevMesh &test = a.test;
     const DevMesh &trial = a.trial;
     const int jb = a.j0 + blockIdx.y * REG_COLS;
     const int ncols = min(REG_COLS, a.j1 - jb);
+    const int ib = blockIdx.x * REG2_ROWS;
     if (threadIdx.x < ncols) {
         s_hi[threadIdx.x] = trial.chi[jb + threadIdx.x];
         s_lo[threadIdx.x] = trial.clo[jb + threadIdx.x];
         s_nc[threadIdx.x] = trial.nc[jb + threadIdx.x];
         s_p0[threadIdx.x] = trial.p0[jb + threadIdx.x];
     }
+    if (threadIdx.x < 4) s_cnt[threadIdx.x >> 1][threadIdx.x & 1] = 0;
     __syncthreads();
-    const int i0 = blockIdx.x * REG2_ROWS + 2 * threadIdx.x;
-    // whole warps beyond the last row leave; a partial warp keeps its lanes
-    // (clamped rows, stores masked) so that the votes see every lane
-    if (((i0 - 2 * (int)(threadIdx.x & 31))) >= test.n) return;
+    const int lane = threadIdx.x & 31;
+    const float k = a.k32;
+    const int64_t ldo = a.ld;
+    float2 *const out_s = reinterpret_cast<float2 *>(a.out_s) + (int64_t)(jb - a.j0) * ldo;
+    float2 *const out_d = reinterpret_cast<float2 *>(a.out_d) + (int64_t)(jb - a.j0) * ldo;
+    const int i0 = ib + 2 * threadIdx.x;
+    // warps wholly beyond the last row skip the columns (they still take part
+    // in the flushes); a partial warp keeps its lanes (clamped rows, stores
+    // masked) so that the votes see every lane
+    const bool live = i0 - 2 * lane < test.n;
     const bool ok0 = i0 < test.n, ok1 = i0 + 1 < test.n;
     const int r0 = ok0 ? i0 : test.n - 1, r1 = ok1 ? i0 + 1 : test.n - 1;
     const float4 ih0 = test.chi[r0], il0 = test.clo[r0], ih1 = test.chi[r1], il1 = test.clo[r1];
-    const int par0 = il0.w != 0.0f ? 1 : 0, par1 = il1.w != 0.0f ? 1 : 0;
-    const float k = a.k32;
-    const int64_t ldo = a.ld;
-    float2 *ps = reinterpret_cast<float2 *>(a.out_s) + (int64_t)(jb - a.j0) * ldo + i0;
-    float2 *pd = reinterpret_cast<float2 *>(a.out_d) + (int64_t)(jb - a.j0) * ldo + i0;
-
-    for (int c = 0; c < ncols; ++c, ps += ldo, pd += ldo) {
-        const int j = jb + c;
-        const float4 h = s_hi[c], l = s_lo[c];
-        // hi/lo centre differences of both rows (FP32 relative accuracy of r)
-        const float ax = (h.x - ih0.x) + (l.x - il0.x), ay = (h.y - ih0.y) + (l.y - il0.y),
-                    az = (h.z - ih0.z) + (l.z - il0.z);
-        const float bx = (h.x - ih1.x) + (l.x - il1.x), by = (h.y - ih1.y) + (l.y - il1.y),
-                    bz = (h.z - ih1.z) + (l.z - il1.z);
-        const float qa = (ax * ax + ay * ay + az * az) * h.w;
-        const float qb = (bx * bx + by * by + bz * bz) * h.w;
-        if (__all_sync(0xffffffffu, qa > Q_FAR && qb > Q_FAR)) {
-            // far: the centroid for both operators, both rows
+    const unsigned lt = (1u << lane) - 1u;
+    for (int c0 = 0, par = 0; c0 < ncols; c0 += REG2_CHUNK, par ^= 1) {
+        int *cnt = s_cnt[par];
+        const int c1 = min(ncols, c0 + REG2_CHUNK);
+        for (int c = c0; live && c < c1; ++c) {
+            float2 *ps = out_s + (int64_t)c * ldo + i0, *pd = out_d + (int64_t)c * ldo + i0;
+            const float4 h = s_hi[c], l = s_lo[c];
+            // hi/lo centre differences of both rows (FP32 relative accuracy of r)
+            const float ax = (h.x - ih0.x) + (l.x - il0.x), ay = (h.y - ih0.y) + (l.y - il0.y),
+                        az = (h.z - ih0.z) + (l.z - il0.z);
+            const float bx = (h.x - ih1.x) + (l.x - il1.x), by = (h.y - ih1.y) + (l.y - il1.y),
+                        bz = (h.z - ih1.z) + (l.z - il1.z);
+            const float qa = (ax * ax + ay * ay + az * az) * h.w;
+            const float qb = (bx * bx + by * by + bz * bz) * h.w;
+            const bool fa = qa > Q_FAR, fb = qb > Q_FAR;
             const float4 p = s_p0[c];
-            float sr0 = 0, si0 = 0, dr0 = 0, di0 = 0, sr1 = 0, si1 = 0, dr1 = 0, di1 = 0;
-            eval_point<FAM, float>(ax, ay, az, p.x, p.y, p.z, p.w, k, 1.0f, 1.0f, sr0, si0, dr0, di0);
-            eval_point<FAM, float>(bx, by, bz, p.x, p.y, p.z, p.w, k, 1.0f, 1.0f, sr1, si1, dr1, di1);
-            if (ok1) {
-                *reinterpret_cast<float4 *>(ps) = make_float4(sr0, si0, sr1, si1);
-                *reinterpret_cast<float4 *>(pd) = make_float4(dr0, di0, dr1, di1);
-            } else if (ok0) {
-                *ps = make_float2(sr0, si0);
-                *pd = make_float2(dr0, di0);
+            if (__all_sync(0xffffffffu, fa && fb)) {
+                // far: the centroid for both operators, both rows
+                float sr0 = 0, si0 = 0, dr0 = 0, di0 = 0, sr1 = 0, si1 = 0, dr1 = 0, di1 = 0;
+                eval_point<FAM, float>(ax, ay, az, p.x, p.y, p.z, p.w, k, 1.0f, 1.0f, sr0, si0, dr0, di0);
+                eval_point<FAM, float>(bx, by, bz, p.x, p.y, p.z, p.w, k, 1.0f, 1.0f, sr1, si1, dr1, di1);
+                if (ok1) {
+                    *reinterpret_cast<float4 *>(ps) = make_float4(sr0, si0, sr1, si1);
+                    *reinterpret_cast<float4 *>(pd) = make_float4(dr0, di0, dr1, di1);
+                } else if (ok0) {
+                    *ps = make_float2(sr0, si0);
+                    *pd = make_float2(dr0, di0);
+                }
+                continue;
             }
-            continue;
-        }
-        // otherwise each row as k_regular: the certain-level path when every
-        // lane's row is certain, else the general dispatch
-        const int tnc = s_nc[c];
-        auto row = [&](const float4 ih, const float4 il, int par, int ri, bool okr, float mx, float my, float mz,
-                       float mq, float2 *qs, float2 *qd) {
-            const float mlo = mq * (1.0f - 1e-5f), mhi = mq * (1.0f + 1e-5f);
-            const bool d_far = mlo >= 249.64f;
-            if (__all_sync(0xffffffffu, mlo >= 82.81f && (d_far || mhi < 249.64f))) {
-                const int64_t base = ((int64_t)j * 2 + par) * SLOTS;
+            // far rows here; the others deferred to the block's lists
+            if (fa && ok0) {
                 float sr = 0, si = 0, dr = 0, di = 0;
-                const float4 yc = __ldg(trial.pts32 + 2 * base), nc = __ldg(trial.pts32 + 2 * base + 1);
-                eval_point<FAM, float>(mx, my, mz, yc.w, nc.x, nc.y, nc.z, k, 1.0f, d_far ? 1.0f : 0.0f, sr, si, dr,
-                                       di);
-                if (!d_far) {
-                    const int npd = level_npts(tnc, par, 1);
-                    for (int q = 0; q < npd; ++q) {
-                        const int64_t sl = base + level_slot0(1) + q;
-                        const float4 y = __ldg(trial.pts32 + 2 * sl), n = __ldg(trial.pts32 + 2 * sl + 1);
-                        eval_point<FAM, float>(mx + y.x, my + y.y, mz + y.z, y.w, n.x, n.y, n.z, k, 0.0f, 1.0f, sr,
-                                               si, dr, di);
-                    }
-                }
-                if (okr) {
-                    *qs = make_float2(sr, si);
-                    *qd = make_float2(dr, di);
-                }
-                return;
+                eval_point<FAM, float>(ax, ay, az, p.x, p.y, p.z, p.w, k, 1.0f, 1.0f, sr, si, dr, di);
+                ps[0] = make_float2(sr, si);
+                pd[0] = make_float2(dr, di);
             }
-            float sr, si, dr, di;
-            if (okr && pair_general32<FAM>(a, ih, il, par, ri, j, h, l, tnc, k, sr, si, dr, di)) {
-                *qs = make_float2(sr, si);
-                *qd = make_float2(dr, di);
+            if (fb && ok1) {
+                float sr = 0, si = 0, dr = 0, di = 0;
+                eval_point<FAM, float>(bx, by, bz, p.x, p.y, p.z, p.w, k, 1.0f, 1.0f, sr, si, dr, di);
+                ps[1] = make_float2(sr, si);
+                pd[1] = make_float2(dr, di);
             }
-        };
-        row(ih0, il0, par0, r0, ok0, ax, ay, az, qa, ps, pd);
-        row(ih1, il1, par1, r1, ok1, bx, by, bz, qb, ps + 1, pd + 1);
+            // the FP32 guard band of classify_pair: outside it the class is the FP64 class
+            const float alo = qa * (1.0f - 1e-5f), ahi = qa * (1.0f + 1e-5f);
+            const float blo = qb * (1.0f - 1e-5f), bhi = qb * (1.0f + 1e-5f);
+            const bool da = ok0 && !fa && ahi >= 2.25f, db = ok1 && !fb && bhi >= 2.25f;  // not certainly near
+            const bool ca = da && alo >= 82.81f && ahi < 249.64f, cb = db && blo >= 82.81f && bhi < 249.64f;
+            const unsigned mA0 = __ballot_sync(0xffffffffu, ca), mA1 = __ballot_sync(0xffffffffu, cb);
+            const unsigned mB0 = __ballot_sync(0xffffffffu, da && !ca), mB1 = __ballot_sync(0xffffffffu, db && !cb);
+            const int nA0 = __popc(mA0), nB0 = __popc(mB0);
+            int baseA = 0, baseB = 0;
+            if (lane == 0) {
+                baseA = atomicAdd(&cnt[0], nA0 + __popc(mA1));
+                baseB = atomicAdd(&cnt[1], nB0 + __popc(mB1));
+            }
+            baseA = __shfl_sync(0xffffffffu, baseA, 0);
+            baseB = __shfl_sync(0xffffffffu, baseB, 0);
+            const unsigned short code0 = (unsigned short)((i0 - ib) | (c << 9));
+            const unsigned short code1 = (unsigned short)((i0 + 1 - ib) | (c << 9));
+            if (ca) s_list[baseA + __popc(mA0 & lt)] = code0;
+            if (cb) s_list[baseA + nA0 + __popc(mA1 & lt)] = code1;
+            if (da && !ca) s_list[REG2_LIST - 1 - (baseB + __popc(mB0 & lt))] = code0;
+            if (db && !cb) s_list[REG2_LIST - 1 - (baseB + nB0 + __popc(mB1 & lt))] = code1;
+        }
+        __syncthreads();  // the chunk's lists are complete
+        const int nA = cnt[0], nB = cnt[1];
+        // the other parity's counters were last read before the previous
+        // chunk's second barrier: reset them for the next chunk
+        if (threadIdx.x < 2) s_cnt[par ^ 1][threadIdx.x] = 0;
+        regular2_flush<FAM>(a, s_list, nA, nB, ib, jb, s_hi, s_lo, s_nc, out_s, out_d, ldo, k);
+        __syncthreads();  // the lists are read before the next chunk appends
     }
 }
 
@@ -710,6 +791,18 @@ cudaError_t launch_assemble_regular(const RegularArgs &a, cudaStream_t s)
         (reinterpret_cast<uintptr_t>(a.out_s) & 15) == 0 && (reinterpret_cast<uintptr_t>(a.out_d) & 15) == 0) {
         // two rows per thread with 16-byte stores
         dim3 g2((a.test.n + REG2_ROWS - 1) / REG2_ROWS, grid.y);
+        int dev = 0;
+        cudaGetDevice(&dev);
+        static bool carveout_set[64] = {};
+        if (dev >= 0 && dev < 64 && !carveout_set[dev]) {
+            cudaError_t e = cudaFuncSetAttribute(k_regular2<FAM_HELMHOLTZ>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                                 regular_carveout_percent());
+            if (e == cudaSuccess)
+                e = cudaFuncSetAttribute(k_regular2<FAM_LAPLACE>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                         regular_carveout_percent());
+            if (e != cudaSuccess) return e;
+            carveout_set[dev] = true;
+        }
         if (a.family == FAM_HELMHOLTZ) k_regular2<FAM_HELMHOLTZ><<<g2, REG2_THREADS, 0, s>>>(a);
         else k_regular2<FAM_LAPLACE><<<g2, REG2_THREADS, 0, s>>>(a);
         return cudaGetLastError();

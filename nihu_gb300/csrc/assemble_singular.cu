@@ -566,6 +566,19 @@ cudaError_t launch_assemble_singular(const RegularArgs &a, const NearList &near,
     int dev = 0, sms = 148;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    // this kernel needs no shared memory, but the regular kernel's blocks
+    // beside it do: the same carveout preference as theirs, so that an SM
+    // this kernel starts on is configured for both (set once per device)
+    static bool carveout_set[64] = {};
+    if (dev >= 0 && dev < 64 && !carveout_set[dev]) {
+        cudaError_t e = cudaSuccess;
+        const int pct = regular_carveout_percent();
+        for (const void *f : {(const void *)k_singular<float2>, (const void *)k_singular<double2>,
+                              (const void *)k_singular_ck<float2>, (const void *)k_singular_ck<double2>})
+            if (e == cudaSuccess) e = cudaFuncSetAttribute(f, cudaFuncAttributePreferredSharedMemoryCarveout, pct);
+        if (e != cudaSuccess) return e;
+        carveout_set[dev] = true;
+    }
     // one 4-warp block per SM keeps the narrow FP64 pipe busy (a warp-wide
     // FP64 instruction occupies it for many cycles) and leave most of every SM
     // to the concurrently running regular kernel

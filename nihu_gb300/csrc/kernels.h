@@ -50,6 +50,9 @@ cudaError_t launch_pair_stats(const DevMesh &test, const DevMesh &trial, int sam
                               unsigned long long *counts, cudaStream_t s);
 
 // assemble_regular.cu -----------------------------------------------------
+// shared-memory carveout preference (percent) of the two-rows regular kernel
+// and of the singular kernel that runs beside it
+int regular_carveout_percent();
 struct RegularArgs {
     DevMesh test, trial;
     int same_mesh;
