@@ -482,21 +482,49 @@ int regular_carveout_percent()
 // iterations on an icosphere, with some 45 of the 64 pairs not far) is not
 // evaluated in that warp: its far rows take the centroid there, certainly
 // nearly singular and self pairs are left to the singular kernel, and the
-// others are appended to a block-local list in shared memory (one 16-bit
-// code per pair: row in the block, column in the block), from the front when
-// their levels are certain without the FP64 check (SLP 1 point, DLP level 1:
-// most of them) and from the back otherwise.  Every REG2_CHUNK columns all
-// 256 threads work through the two lists, so that a pair's cost is its own
-// point count, not the largest one in its warp.  A list holds every pair of
-// a chunk, so it cannot overflow, and a block needs under 10 KB of shared
-// memory.  The points, levels and their order are those of k_regular (the
-// far path, the certain-level path and the general dispatch), so the entries
-// are the same.
+// others are appended to the warp's list in shared memory (one 16-bit code
+// per pair: row in the block, column in the block), from the front when their
+// levels are certain without the FP64 check (SLP 1 point, DLP level 1: most
+// of them) and from the back otherwise.  Every REG2_CHUNK columns the warp
+// works through its two lists, one pair per lane, so that a pair's cost is
+// its own point count, not the largest one in its warp; warps do not wait
+// for one another.  A list holds every pair of a chunk, so it cannot
+// overflow, and a block needs under 10 KB of shared memory.  The points,
+// levels and their order are those of k_regular (the far path, the
+// certain-level path and the general dispatch).
 constexpr int REG2_THREADS = 256;
 constexpr int REG2_ROWS = 2 * REG2_THREADS;
-constexpr int REG2_CHUNK = 8;                        // columns per list flush
-constexpr int REG2_LIST = REG2_ROWS * REG2_CHUNK;    // every pair of a chunk
+constexpr int REG2_CHUNK = 8;                  // columns per list flush
+constexpr int REG2_WLIST = 64 * REG2_CHUNK;    // every pair of a warp's chunk
 static_assert(REG2_ROWS <= 512 && REG_COLS <= 128, "a pair code is row (9 bits) | column << 9 in 16 bits");
+
+// the far rule (the element centroid for both operators) with the weight
+// w J / (4 pi) given: e^{-ikr}/(4 pi r) and its DLP counterpart
+// -(1 + ikr) e^{-ikr} (r.n) / (4 pi r^3)
+template <int FAM>
+__device__ __forceinline__ void far_point(float rx, float ry, float rz, float w4, float nx, float ny, float nz,
+                                          float k, float &sr, float &si, float &dr, float &di)
+{
+    const float r2 = rx * rx + ry * ry + rz * rz;
+    const float rinv = rsqrtf(r2);
+    const float g = w4 * rinv;
+    const float rn = rx * nx + ry * ny + rz * nz;
+    const float f = -g * (rinv * rinv) * rn;
+    if constexpr (FAM == FAM_HELMHOLTZ) {
+        const float kr = k * (r2 * rinv);
+        float sn, cs;
+        sincos_reduced(kr, sn, cs);
+        sr = g * cs;
+        si = -g * sn;
+        dr = f * (cs + kr * sn);
+        di = f * (kr * cs - sn);
+    } else {
+        sr = g;
+        si = 0.0f;
+        dr = f;
+        di = 0.0f;
+    }
+}
 
 // one pair by the general path of k_regular (classify_pair, the uniform loop
 // over the lane's points); false when the pair is not regular
@@ -528,18 +556,18 @@ __device__ __forceinline__ bool pair_general32(const RegularArgs &a, const float
     return true;
 }
 
-// the deferred pairs of one chunk: certain levels (the centroid for the SLP,
-// the level-1 points for the DLP) from the front of the list, the others
+// one warp's deferred pairs: certain levels (the centroid for the SLP, the
+// level-1 points for the DLP) from the front of its list, the others
 // (classify_pair and the pair's own rule) from the back
 template <int FAM>
-__device__ __forceinline__ void regular2_flush(const RegularArgs &a, const unsigned short *s_list, int nA, int nB,
-                                               int ib, int jb, const float4 *s_hi, const float4 *s_lo,
+__device__ __forceinline__ void regular2_flush(const RegularArgs &a, const unsigned short *wl, int nA, int nB,
+                                               int lane, int ib, int jb, const float4 *s_hi, const float4 *s_lo,
                                                const int *s_nc, float2 *out_s, float2 *out_d, int64_t ldo, float k)
 {
     const DevMesh &test = a.test;
     const DevMesh &trial = a.trial;
-    for (int t = threadIdx.x; t < nA; t += REG2_THREADS) {
-        const int code = s_list[t];
+    for (int t = lane; t < nA; t += 32) {
+        const int code = wl[t];
         const int i = ib + (code & 511), c = code >> 9, j = jb + c;
         const float4 ih = test.chi[i], il = test.clo[i], h = s_hi[c], l = s_lo[c];
         const int par = il.w != 0.0f ? 1 : 0;
@@ -558,8 +586,8 @@ __device__ __forceinline__ void regular2_flush(const RegularArgs &a, const unsig
         out_s[(int64_t)c * ldo + i] = make_float2(sr, si);
         out_d[(int64_t)c * ldo + i] = make_float2(dr, di);
     }
-    for (int t = threadIdx.x; t < nB; t += REG2_THREADS) {
-        const int code = s_list[REG2_LIST - 1 - t];
+    for (int t = lane; t < nB; t += 32) {
+        const int code = wl[REG2_WLIST - 1 - t];
         const int i = ib + (code & 511), c = code >> 9, j = jb + c;
         const float4 ih = test.chi[i], il = test.clo[i];
         float sr, si, dr, di;
@@ -574,11 +602,10 @@ template <int FAM>
 // 64 registers: three blocks fit beside the concurrent singular kernel's one
 __global__ void __launch_bounds__(REG2_THREADS, 4) k_regular2(RegularArgs a)
 {
+    constexpr float INV4PI = 0.0795774715459476679f;
     __shared__ float4 s_hi[REG_COLS], s_lo[REG_COLS], s_p0[REG_COLS];
     __shared__ int s_nc[REG_COLS];
-    __shared__ unsigned short s_list[REG2_LIST];
-    // per chunk parity: certain-level pairs (from the front), the others (from the back)
-    __shared__ int s_cnt[2][2];
+    __shared__ unsigned short s_list[REG2_THREADS / 32][REG2_WLIST];
     const DevMesh &test = a.test;
     const DevMesh &trial = a.trial;
     const int jb = a.j0 + blockIdx.y * REG_COLS;
@@ -588,29 +615,31 @@ __global__ void __launch_bounds__(REG2_THREADS, 4) k_regular2(RegularArgs a)
         s_hi[threadIdx.x] = trial.chi[jb + threadIdx.x];
         s_lo[threadIdx.x] = trial.clo[jb + threadIdx.x];
         s_nc[threadIdx.x] = trial.nc[jb + threadIdx.x];
-        s_p0[threadIdx.x] = trial.p0[jb + threadIdx.x];
+        float4 p = trial.p0[jb + threadIdx.x];
+        p.x *= INV4PI;  // the far rule's weight w J / (4 pi)
+        s_p0[threadIdx.x] = p;
     }
-    if (threadIdx.x < 4) s_cnt[threadIdx.x >> 1][threadIdx.x & 1] = 0;
     __syncthreads();
     const int lane = threadIdx.x & 31;
+    const int i0 = ib + 2 * threadIdx.x;
+    // warps wholly beyond the last row have nothing to do; a partial warp
+    // keeps its lanes (clamped rows, stores masked) so that the votes see
+    // every lane.  No block barrier follows.
+    if (i0 - 2 * lane >= test.n) return;
+    unsigned short *wl = s_list[threadIdx.x >> 5];
     const float k = a.k32;
     const int64_t ldo = a.ld;
     float2 *const out_s = reinterpret_cast<float2 *>(a.out_s) + (int64_t)(jb - a.j0) * ldo;
     float2 *const out_d = reinterpret_cast<float2 *>(a.out_d) + (int64_t)(jb - a.j0) * ldo;
-    const int i0 = ib + 2 * threadIdx.x;
-    // warps wholly beyond the last row skip the columns (they still take part
-    // in the flushes); a partial warp keeps its lanes (clamped rows, stores
-    // masked) so that the votes see every lane
-    const bool live = i0 - 2 * lane < test.n;
     const bool ok0 = i0 < test.n, ok1 = i0 + 1 < test.n;
     const int r0 = ok0 ? i0 : test.n - 1, r1 = ok1 ? i0 + 1 : test.n - 1;
     const float4 ih0 = test.chi[r0], il0 = test.clo[r0], ih1 = test.chi[r1], il1 = test.clo[r1];
     const unsigned lt = (1u << lane) - 1u;
-    for (int c0 = 0, par = 0; c0 < ncols; c0 += REG2_CHUNK, par ^= 1) {
-        int *cnt = s_cnt[par];
+    float2 *ps = out_s + i0, *pd = out_d + i0;
+    for (int c0 = 0; c0 < ncols; c0 += REG2_CHUNK) {
         const int c1 = min(ncols, c0 + REG2_CHUNK);
-        for (int c = c0; live && c < c1; ++c) {
-            float2 *ps = out_s + (int64_t)c * ldo + i0, *pd = out_d + (int64_t)c * ldo + i0;
+        int nA = 0, nB = 0;  // warp-uniform list lengths
+        for (int c = c0; c < c1; ++c, ps += ldo, pd += ldo) {
             const float4 h = s_hi[c], l = s_lo[c];
             // hi/lo centre differences of both rows (FP32 relative accuracy of r)
             const float ax = (h.x - ih0.x) + (l.x - il0.x), ay = (h.y - ih0.y) + (l.y - il0.y),
@@ -623,9 +652,9 @@ __global__ void __launch_bounds__(REG2_THREADS, 4) k_regular2(RegularArgs a)
             const float4 p = s_p0[c];
             if (__all_sync(0xffffffffu, fa && fb)) {
                 // far: the centroid for both operators, both rows
-                float sr0 = 0, si0 = 0, dr0 = 0, di0 = 0, sr1 = 0, si1 = 0, dr1 = 0, di1 = 0;
-                eval_point<FAM, float>(ax, ay, az, p.x, p.y, p.z, p.w, k, 1.0f, 1.0f, sr0, si0, dr0, di0);
-                eval_point<FAM, float>(bx, by, bz, p.x, p.y, p.z, p.w, k, 1.0f, 1.0f, sr1, si1, dr1, di1);
+                float sr0, si0, dr0, di0, sr1, si1, dr1, di1;
+                far_point<FAM>(ax, ay, az, p.x, p.y, p.z, p.w, k, sr0, si0, dr0, di0);
+                far_point<FAM>(bx, by, bz, p.x, p.y, p.z, p.w, k, sr1, si1, dr1, di1);
                 if (ok1) {
                     *reinterpret_cast<float4 *>(ps) = make_float4(sr0, si0, sr1, si1);
                     *reinterpret_cast<float4 *>(pd) = make_float4(dr0, di0, dr1, di1);
@@ -635,16 +664,16 @@ __global__ void __launch_bounds__(REG2_THREADS, 4) k_regular2(RegularArgs a)
                 }
                 continue;
             }
-            // far rows here; the others deferred to the block's lists
+            // far rows here; the others deferred to the warp's lists
             if (fa && ok0) {
-                float sr = 0, si = 0, dr = 0, di = 0;
-                eval_point<FAM, float>(ax, ay, az, p.x, p.y, p.z, p.w, k, 1.0f, 1.0f, sr, si, dr, di);
+                float sr, si, dr, di;
+                far_point<FAM>(ax, ay, az, p.x, p.y, p.z, p.w, k, sr, si, dr, di);
                 ps[0] = make_float2(sr, si);
                 pd[0] = make_float2(dr, di);
             }
             if (fb && ok1) {
-                float sr = 0, si = 0, dr = 0, di = 0;
-                eval_point<FAM, float>(bx, by, bz, p.x, p.y, p.z, p.w, k, 1.0f, 1.0f, sr, si, dr, di);
+                float sr, si, dr, di;
+                far_point<FAM>(bx, by, bz, p.x, p.y, p.z, p.w, k, sr, si, dr, di);
                 ps[1] = make_float2(sr, si);
                 pd[1] = make_float2(dr, di);
             }
@@ -656,27 +685,20 @@ __global__ void __launch_bounds__(REG2_THREADS, 4) k_regular2(RegularArgs a)
             const unsigned mA0 = __ballot_sync(0xffffffffu, ca), mA1 = __ballot_sync(0xffffffffu, cb);
             const unsigned mB0 = __ballot_sync(0xffffffffu, da && !ca), mB1 = __ballot_sync(0xffffffffu, db && !cb);
             const int nA0 = __popc(mA0), nB0 = __popc(mB0);
-            int baseA = 0, baseB = 0;
-            if (lane == 0) {
-                baseA = atomicAdd(&cnt[0], nA0 + __popc(mA1));
-                baseB = atomicAdd(&cnt[1], nB0 + __popc(mB1));
-            }
-            baseA = __shfl_sync(0xffffffffu, baseA, 0);
-            baseB = __shfl_sync(0xffffffffu, baseB, 0);
             const unsigned short code0 = (unsigned short)((i0 - ib) | (c << 9));
             const unsigned short code1 = (unsigned short)((i0 + 1 - ib) | (c << 9));
-            if (ca) s_list[baseA + __popc(mA0 & lt)] = code0;
-            if (cb) s_list[baseA + nA0 + __popc(mA1 & lt)] = code1;
-            if (da && !ca) s_list[REG2_LIST - 1 - (baseB + __popc(mB0 & lt))] = code0;
-            if (db && !cb) s_list[REG2_LIST - 1 - (baseB + nB0 + __popc(mB1 & lt))] = code1;
+            if (ca) wl[nA + __popc(mA0 & lt)] = code0;
+            if (cb) wl[nA + nA0 + __popc(mA1 & lt)] = code1;
+            if (da && !ca) wl[REG2_WLIST - 1 - (nB + __popc(mB0 & lt))] = code0;
+            if (db && !cb) wl[REG2_WLIST - 1 - (nB + nB0 + __popc(mB1 & lt))] = code1;
+            nA += nA0 + __popc(mA1);
+            nB += nB0 + __popc(mB1);
         }
-        __syncthreads();  // the chunk's lists are complete
-        const int nA = cnt[0], nB = cnt[1];
-        // the other parity's counters were last read before the previous
-        // chunk's second barrier: reset them for the next chunk
-        if (threadIdx.x < 2) s_cnt[par ^ 1][threadIdx.x] = 0;
-        regular2_flush<FAM>(a, s_list, nA, nB, ib, jb, s_hi, s_lo, s_nc, out_s, out_d, ldo, k);
-        __syncthreads();  // the lists are read before the next chunk appends
+        if (nA + nB) {  // warp-uniform
+            __syncwarp();  // the list entries are visible to the whole warp
+            regular2_flush<FAM>(a, wl, nA, nB, lane, ib, jb, s_hi, s_lo, s_nc, out_s, out_d, ldo, k);
+            __syncwarp();  // read before the next chunk appends
+        }
     }
 }
 
