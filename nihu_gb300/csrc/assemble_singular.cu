@@ -463,7 +463,7 @@ __device__ __forceinline__ void singular_pairs(const RegularArgs &a, const NearL
                     // FP32 regular quadrature: the dynamic part and the static
                     // part's angular point sums in FP32 as well
                     if (fam == FAM_HELMHOLTZ) near_dynamic_f32(e, kf, x0, do_s, do_d, acc);
-                    near_static_f32(e, x0, do_s, do_d, acc);
+                    near_static_f32(e, a.trial.frame + 16 * (int64_t)j, x0, do_s, do_d, acc);
                 } else {
                     near_plane(e, fam, kf, x0, do_s, do_d, acc, a.trial.dyn42 + 42 * (int64_t)j, short_f);
                 }

@@ -578,12 +578,12 @@ nihu_gb_status nihu_gb_mesh_create(nihu_gb_ctx *ctx, const double *nodes, int64_
     m->dm.n = (int)n_elems;
     const int64_t n = std::max<int64_t>(n_elems, 1);
     struct Req { void **p; size_t bytes; };
-    void *corners, *center, *size, *nc, *chi, *clo, *p0, *pts32, *pts64, *dyn42, *nid;
+    void *corners, *center, *size, *nc, *chi, *clo, *p0, *pts32, *pts64, *dyn42, *nid, *frame;
     Req reqs[] = {{&corners, sizeof(double) * 12 * n}, {&center, sizeof(double) * 3 * n}, {&size, sizeof(double) * n},
                   {&nc, sizeof(int8_t) * n}, {&chi, sizeof(float4) * n}, {&clo, sizeof(float4) * n},
                   {&p0, sizeof(float4) * n}, {&pts32, sizeof(float4) * 2 * 2 * SLOTS * n},
                   {&pts64, sizeof(double) * 8 * 2 * SLOTS * n}, {&dyn42, sizeof(Pt4) * 42 * n},
-                  {&nid, sizeof(int4) * n}};
+                  {&nid, sizeof(int4) * n}, {&frame, sizeof(double) * 16 * n}};
     for (auto &r : reqs) {
         nihu_gb_status st = dmalloc(ctx, r.bytes, r.p);
         if (st) { nihu_gb_mesh_destroy(m); return st; }
@@ -600,6 +600,7 @@ nihu_gb_status nihu_gb_mesh_create(nihu_gb_ctx *ctx, const double *nodes, int64_
     m->dm.pts64 = (double *)pts64;
     m->dm.dyn42 = (Pt4 *)dyn42;
     m->dm.nid = (int4 *)nid;
+    m->dm.frame = (double *)frame;
     for (int64_t e = 0; e < n_elems; ++e) {
         int32_t t = elems[e * elem_cols];
         if (t == NIHU_GB_TRIA_1) m->dm.has_tria = 1;

@@ -61,6 +61,11 @@ struct DevMesh {
     // corner node indices (-1 for the 4th of a triangle): element adjacency
     // of the Galerkin singular quadratures
     int4 *nid = nullptr;
+    // triangles: the plane frame of the nearly singular static part (rows
+    // T0, T1, T2: first side, in-plane normal to it, unit normal) and the
+    // corners' in-plane coordinates relative to corner 0, [n][16] doubles
+    // (T row-major, then (u, v) of corners 0..2, one unused)
+    double *frame = nullptr;
 };
 
 // number of points of a regular level for (trial corners, test complexity)

@@ -1,7 +1,7 @@
 // Element geometry on the GPU: centres, sizes, normals and the regular
 // quadrature points of every element, computed once per mesh.
-#include "geom.cuh"
 #include "kernels.h"
+#include "planar.cuh"
 
 namespace nihu {
 
@@ -52,6 +52,22 @@ __global__ void k_mesh_geometry(const double *__restrict__ nodes, int64_t n_node
     m.chi[e] = make_float4(hx, hy, hz, (float)(1.0 / (size * size)));
     m.clo[e] = make_float4((float)(cen[0] - (double)hx), (float)(cen[1] - (double)hy), (float)(cen[2] - (double)hz),
                            nc == 4 ? 1.0f : 0.0f);
+
+    // plane frame of the nearly singular static part (triangles): the
+    // frame of plane_local_frame, which depends on the element only, and the
+    // corners' in-plane coordinates relative to corner 0
+    if (nc == 3) {
+        double loc[4][2], z, T[3][3];
+        plane_local_frame(el, el.c[0], loc, z, T);
+        double *fr = m.frame + 16 * (int64_t)e;
+        for (int r = 0; r < 3; ++r)
+            for (int d = 0; d < 3; ++d) fr[3 * r + d] = T[r][d];
+        for (int a = 0; a < 3; ++a) {
+            fr[9 + 2 * a] = loc[a][0];
+            fr[10 + 2 * a] = loc[a][1];
+        }
+        fr[15] = 0.0;
+    }
 
     // degree-14 points of the nearly singular dynamic part (triangles)
     if (nc == 3) {

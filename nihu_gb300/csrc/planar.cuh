@@ -225,4 +225,21 @@ struct Tri14 {
 };
 __device__ constexpr Tri14 TRI14{};
 
+// an n-point Gauss-Legendre rule on [-1, 1] in FP32, (x, w) per point
+template <int N>
+struct GaussF {
+    float x[N], w[N];
+    constexpr GaussF() : x(), w()
+    {
+        constexpr double d[NIHU_GAUSS_DATA_LEN] = NIHU_GAUSS_DATA;
+        constexpr int off[NIHU_GAUSS_MAX_N] = NIHU_GAUSS_OFFSETS;
+        for (int q = 0; q < N; ++q) {
+            x[q] = (float)d[2 * (off[N - 1] + q)];
+            w[q] = (float)d[2 * (off[N - 1] + q) + 1];
+        }
+    }
+};
+__device__ constexpr GaussF<6> GAUSS6F{};
+__device__ constexpr GaussF<8> GAUSS8F{};
+
 }  // namespace nihu

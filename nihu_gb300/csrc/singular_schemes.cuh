@@ -104,21 +104,31 @@ __device__ inline void near_static(const Elem64 &e, const double x0[3], bool do_
 }
 
 // near_static with the angular point sums in FP32 (the FP32 regular
-// quadrature mode).  The plane frame and the foot vectors stay FP64.  Per side,
-// with the reference's 6 points: the SLP sums r - |z| = R^2 / (r + |z|)
-// (positive, no cancellation) and the DLP sums 1 - |z|/r as
-// sum(w) (t2 - t1)/2 - sum(w |z|/r) (t2 - t1)/2.  Over the sides the first
-// part adds up to sum(w)/2 times the winding angle of the polygon around the
-// foot point: 2 pi inside, 0 outside, which an FP64 point-in-polygon test
-// gives exactly (summed in FP32, those O(1) terms would leave FP32 rounding
-// of that size in a DLP entry whose foot point lies outside the element,
-// where the sides cancel).  A foot point within rounding of a side takes
-// near_static itself.
-__device__ inline void near_static_f32(const Elem64 &e, const double x0[3], bool do_s, bool do_d, Acc &a)
+// quadrature mode), for a triangle whose plane frame is precomputed (frame:
+// the element's DevMesh::frame record).  The plane coordinates and the foot
+// vectors stay FP64.  Per side, with the reference's 6 points: the SLP sums
+// r - |z| = R^2 / (r + |z|) (positive, no cancellation) and the DLP sums
+// 1 - |z|/r as sum(w) (t2 - t1)/2 - sum(w |z|/r) (t2 - t1)/2.  Over the sides
+// the first part adds up to sum(w)/2 times the winding angle of the polygon
+// around the foot point: 2 pi inside, 0 outside, which an FP64
+// point-in-polygon test gives exactly (summed in FP32, those O(1) terms would
+// leave FP32 rounding of that size in a DLP entry whose foot point lies
+// outside the element, where the sides cancel).  A foot point within rounding
+// of a side takes near_static itself.
+__device__ inline void near_static_f32(const Elem64 &e, const double *__restrict__ frame, const double x0[3],
+                                       bool do_s, bool do_d, Acc &a)
 {
-    double loc[4][2], z;
-    plane_local(e, x0, loc, z);
-    const int N = e.nc;
+    // plane_local with the element's own frame: corner a at (u_a + u0, v_a + v0)
+    const double dv0 = e.c[0][0] - x0[0], dv1 = e.c[0][1] - x0[1], dv2 = e.c[0][2] - x0[2];
+    const double u0 = frame[0] * dv0 + frame[1] * dv1 + frame[2] * dv2;
+    const double v0 = frame[3] * dv0 + frame[4] * dv1 + frame[5] * dv2;
+    const double z = -(frame[6] * dv0 + frame[7] * dv1 + frame[8] * dv2);
+    double loc[3][2];
+    for (int c = 0; c < 3; ++c) {
+        loc[c][0] = frame[9 + 2 * c] + u0;
+        loc[c][1] = frame[10 + 2 * c] + v0;
+    }
+    constexpr int N = 3;
     // winding of the (counter-clockwise) polygon around the foot point
     double scale = 0.0;
     for (int s = 0; s < N; ++s) scale = fmax(scale, loc[s][0] * loc[s][0] + loc[s][1] * loc[s][1]);
@@ -134,12 +144,6 @@ __device__ inline void near_static_f32(const Elem64 &e, const double x0[3], bool
         else ++neg;
     }
     const double wind = pos == N ? 2.0 * PI : (neg == N ? -2.0 * PI : 0.0);
-    double wsum = 0.0;
-    for (int q = 0; q < 6; ++q) {
-        double xi, w;
-        gauss_pt(6, q, xi, w);
-        wsum += w;
-    }
     const float az = (float)fabs(z), z2 = az * az;
     double s_sum = 0.0, dz_sum = 0.0;
     for (int s = 0; s < N; ++s) {
@@ -156,26 +160,26 @@ __device__ inline void near_static_f32(const Elem64 &e, const double x0[3], bool
         const double l0 = d0 * il, l1 = d1 * il;
         const double pr = c1[0] * l0 + c1[1] * l1;
         const double f0 = c1[0] - l0 * pr, f1 = c1[1] - l1 * pr;
-        const float ds = (float)sqrt(f0 * f0 + f1 * f1);
+        const float ds = sqrtf((float)(f0 * f0 + f1 * f1));
         const float p1 = atan2f((float)(f0 * c1[1] - f1 * c1[0]), (float)(f0 * c1[0] + f1 * c1[1]));
         const float p2 = atan2f((float)(f0 * c2[1] - f1 * c2[0]), (float)(f0 * c2[0] + f1 * c2[1]));
         const float jac = (p2 - p1) * 0.5f;
         float ss = 0.0f, sz = 0.0f;
+#pragma unroll
         for (int q = 0; q < 6; ++q) {
-            double xi, w;
-            gauss_pt(6, q, xi, w);
-            const float xf = (float)xi, wf = (float)w;
+            const float xf = GAUSS6F.x[q], wf = GAUSS6F.w[q];
             const float ph = p1 * (1.0f - xf) * 0.5f + p2 * (1.0f + xf) * 0.5f;
-            const float R = ds / cosf(ph);
+            const float R = __fdividef(ds, cosf(ph));
             const float R2 = R * R;
             const float r = sqrtf(R2 + z2);
-            ss += wf * (R2 / (r + az));  // r - |z|
-            sz += wf * (az / r);         // |z| / r
+            ss += wf * __fdividef(R2, r + az);  // r - |z|
+            sz += wf * __fdividef(az, r);       // |z| / r
         }
         s_sum += (double)(jac * ss);
         dz_sum += (double)(jac * sz);
     }
-    const double d_sum = 0.5 * wind * wsum - dz_sum;
+    // sum(w) = 2 for the 6-point rule
+    const double d_sum = wind - dz_sum;
     const double sg = (0.0 < z) - (z < 0.0);
     if (do_s) a.sr += s_sum * INV_FOUR_PI;
     if (do_d) a.dr += sg * d_sum * INV_FOUR_PI;
@@ -338,10 +342,15 @@ __device__ inline void near_dynamic_f32(const Elem64 &e, double k, const double 
         const float r2 = rv0 * rv0 + rv1 * rv1 + rv2 * rv2;
         const float rinv = rsqrtf(r2);
         const float kr = kf * (r2 * rinv);
-        float sn, cs;
-        sincosf(kr, &sn, &cs);
-        const float hs = sinf(0.5f * kr);
-        const float cm1 = -2.0f * hs * hs;
+        // the half angle by the hardware approximation after a reduction by
+        // the nearest multiple of 2 pi (absolute error about 4e-7): the
+        // dynamic part is of relative size (kr)^2 against the static one, so
+        // that stays far below the entries' 1e-5
+        float hs, hc;
+        sincos_reduced(0.5f * kr, hs, hc);
+        const float cm1 = -2.0f * hs * hs;  // cos kr - 1
+        const float sn = 2.0f * hs * hc;    // sin kr
+        const float cs = 1.0f + cm1;
         const float t = w * wj * rinv;
         if (do_s) {
             sr += t * cm1;
@@ -771,10 +780,11 @@ static __device__ __noinline__ void near_dynamic_quad_f32(const Elem64 &e, doubl
         const float r2 = rv[0] * rv[0] + rv[1] * rv[1] + rv[2] * rv[2];
         const float rinv = rsqrtf(r2);
         const float kr = kf * (r2 * rinv);
-        float sn, cs;
-        sincos_reduced(kr, sn, cs);
-        const float hs = sinf(0.5f * kr);
+        float hs, hc;  // the half angle, as in near_dynamic_f32
+        sincos_reduced(0.5f * kr, hs, hc);
         const float cm1 = -2.0f * hs * hs;  // cos kr - 1 without cancellation
+        const float sn = 2.0f * hs * hc;
+        const float cs = 1.0f + cm1;
         const float t = (float)(w0 * w1) * J * rinv * INV4PI;
         if (do_s) {
             sr += t * cm1;
