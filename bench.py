@@ -884,6 +884,7 @@ def run_serve(args):
                      quantum=quantum, ctx=ctx)
     # warm-up: one request per mesh (near lists, code paths, memory pool)
     sv = g.Server(mesh_list, **server_kw)
+    sv.reserve()  # the HBM budget mapped into the server's pool before serving starts
     for i in range(len(subdivs)):
         sv.submit(i, 1.0, np.ones(sizes[i]))
     while sv.step()[:2] != (0, 0):

@@ -503,6 +503,12 @@ nihu_gb_status nihu_gb_server_create(nihu_gb_ctx *ctx, int n_meshes, const nihu_
                                      int max_iters, double tol, int quantum, nihu_gb_server **out);
 void nihu_gb_server_destroy(nihu_gb_server *server);
 
+/* Map `bytes` of device memory (0 or more than the budget: the budget) into
+ * the server's memory pool now, so that admissions inside the serving loop
+ * map none: the pool keeps freed memory until the server is destroyed.
+ * NIHU_GB_ERR_OUT_OF_MEMORY when the device cannot provide it. */
+nihu_gb_status nihu_gb_server_reserve(nihu_gb_server *server, size_t bytes);
+
 /* Queue a request on meshes[mesh] at wave number k with Neumann data q
  * (complex128 host vector of the mesh's element count, copied).  *id
  * receives its number (0, 1, 2, ... in submission order).

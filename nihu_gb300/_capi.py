@@ -70,6 +70,7 @@ SIGNATURES = {
     "nihu_gb_sweep_plan_destroy": (None, [_vp]),
     "nihu_gb_server_create": (_i, [_vp, _i, _vp, _i, _i, _sz, _i, _i, _i, _d, _i, ctypes.POINTER(_vp)]),
     "nihu_gb_server_destroy": (None, [_vp]),
+    "nihu_gb_server_reserve": (_i, [_vp, _sz]),
     "nihu_gb_server_submit": (_i, [_vp, _i, _d, _vp, ctypes.POINTER(ctypes.c_int64)]),
     "nihu_gb_server_step": (_i, [_vp, _ip, _ip, _ip]),
     "nihu_gb_server_take": (_i, [_vp, ctypes.POINTER(ctypes.c_int64), _vp, _i64, _ip, _dp, _ip]),

@@ -783,6 +783,11 @@ class Server:
         self.handle = h
         self._mesh_of = {}
 
+    def reserve(self, nbytes: int = 0):
+        """Map nbytes (0: the whole budget) of device memory into the server's
+        pool now, so that admissions inside the serving loop map none."""
+        self.ctx.check(C.lib().nihu_gb_server_reserve(self.handle, int(nbytes)))
+
     def submit(self, mesh: int, k: float, q) -> int:
         q = _c128(q)
         if q.shape != (self.sizes[mesh],):

@@ -2618,7 +2618,7 @@ struct nihu_gb_server {
         std::vector<double2> q;  // Neumann data until admission; then the result p
         size_t held = 0;         // budget bytes held
         void *H = nullptr, *blk = nullptr;  // DLP matrix; vectors and Krylov state
-        double2 *dq = nullptr, *b = nullptr, *x = nullptr, *V = nullptr, *S = nullptr;
+        double2 *b = nullptr, *x = nullptr, *V = nullptr, *S = nullptr;
         int slot = -1;  // status word in the server's state array
         PersistentState st{};
     };
@@ -2628,6 +2628,8 @@ struct nihu_gb_server {
     double tol = 0.0;
     size_t budget = 0, held = 0;
     cudaMemPool_t pool = nullptr;
+    double2 *h_stage = nullptr;  // pinned staging of a round's Neumann data
+    size_t h_stage_bytes = 0;
     PersistentState *d_states = nullptr;  // one slot per admitted request
     int n_slots = 0;
     std::vector<int> free_slots;
@@ -2643,10 +2645,10 @@ typedef nihu_gb_server::Request SrvReq;
 
 size_t srv_align(size_t x) { return (x + 255) & ~(size_t)255; }
 
-// device bytes of one request's vectors, basis, small state: [q b x | V | S]
+// device bytes of one request's vectors, basis, small state: [b x | V | S]
 size_t srv_block_bytes(int64_t n, int m)
 {
-    return srv_align(3 * 16 * (size_t)n) + srv_align(16 * (size_t)n * (m + 1)) + srv_align(16 * persistent_small_state(m));
+    return srv_align(2 * 16 * (size_t)n) + srv_align(16 * (size_t)n * (m + 1)) + srv_align(16 * persistent_small_state(m));
 }
 
 void srv_release(nihu_gb_server *sv, SrvReq *r)
@@ -2695,6 +2697,7 @@ extern "C" nihu_gb_status nihu_gb_server_create(nihu_gb_ctx *ctx, int n_meshes, 
     CK(cudaMemPoolCreate(&sv->pool, &props));
     uint64_t keep = UINT64_MAX;  // freed blocks stay in the pool for the next requests
     CK(cudaMemPoolSetAttribute(sv->pool, cudaMemPoolAttrReleaseThreshold, &keep));
+
     sv->n_slots = max_active;
     void *p;
     nihu_gb_status st;
@@ -2718,8 +2721,28 @@ extern "C" void nihu_gb_server_destroy(nihu_gb_server *sv)
     for (SrvReq *r : sv->active) delete r;
     for (SrvReq *r : sv->done) delete r;
     dfree(sv->ctx, sv->d_states);
+    if (sv->h_stage) cudaFreeHost(sv->h_stage);
     cudaMemPoolDestroy(sv->pool);
     delete sv;
+}
+
+extern "C" nihu_gb_status nihu_gb_server_reserve(nihu_gb_server *sv, size_t bytes)
+{
+    if (!sv) return NIHU_GB_ERR_INVALID_ARGUMENT;
+    nihu_gb_ctx *ctx = sv->ctx;
+    if (bytes == 0 || bytes > sv->budget) bytes = sv->budget;
+    cudaSetDevice(ctx->device);
+    // one allocation of the size, freed at once: the pool keeps the memory
+    // (release threshold: all), so later admissions map no new device memory
+    void *all = nullptr;
+    cudaError_t e = cudaMallocFromPoolAsync(&all, bytes, sv->pool, ctx->stream);
+    if (e == cudaSuccess) e = cudaFreeAsync(all, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return cuda_fail(ctx, e, "nihu_gb_server_reserve");
+    }
+    return NIHU_GB_OK;
 }
 
 extern "C" nihu_gb_status nihu_gb_server_submit(nihu_gb_server *sv, int mesh, double k, const void *q, int64_t *id)
@@ -2763,24 +2786,34 @@ extern "C" nihu_gb_status nihu_gb_server_step(nihu_gb_server *sv, int *n_queued,
         r->held = mat + blk;
         sv->held += r->held;
         char *p = (char *)r->blk;
-        r->dq = (double2 *)p;
-        r->b = r->dq + n;
+        r->b = (double2 *)p;
         r->x = r->b + n;
-        p += srv_align(3 * 16 * (size_t)n);
+        p += srv_align(2 * 16 * (size_t)n);
         r->V = (double2 *)p;
         p += srv_align(16 * (size_t)n * (m + 1));
         r->S = (double2 *)p;
         r->slot = sv->free_slots.back();
         sv->free_slots.pop_back();
-        CK(cudaMemcpyAsync(r->dq, r->q.data(), 16 * (size_t)n, cudaMemcpyHostToDevice, s));
         CK(cudaMemsetAsync(sv->d_states + r->slot, 0, sizeof(PersistentState), s));  // PG_FRESH
         sv->queue.pop_front();
         fresh.push_back(r);
+    }
+    // the round's Neumann data, grouped by mesh, into pinned staging: one
+    // upload per mesh group below
+    size_t stage = 0;
+    for (SrvReq *r : fresh) stage += 16 * (size_t)sv->meshes[r->mesh]->n;
+    if (stage > sv->h_stage_bytes) {
+        if (sv->h_stage) cudaFreeHost(sv->h_stage);
+        sv->h_stage = nullptr;
+        sv->h_stage_bytes = 0;
+        CK(cudaMallocHost((void **)&sv->h_stage, stage));
+        sv->h_stage_bytes = stage;
     }
     ph_admit.reset();
     // 2. assembly of the new requests, one frequency batch per mesh: the DLP
     // matrices and the right-hand sides b = SLP q (no SLP matrix)
     std::vector<std::vector<void *>> tables;  // host sources of the pointer uploads, alive until the round's wait
+    double2 *hq = sv->h_stage;
     for (int i = 0; i < (int)sv->meshes.size(); ++i) {
         std::vector<SrvReq *> grp;
         for (SrvReq *r : fresh)
@@ -2799,8 +2832,13 @@ extern "C" nihu_gb_status nihu_gb_server_step(nihu_gb_server *sv, int *n_queued,
             ks[f] = grp[f]->k;
             tab[f] = nullptr;
             tab[nk + f] = grp[f]->H;
-            CK(cudaMemcpyAsync((double2 *)gq + (size_t)f * n, grp[f]->dq, 16 * (size_t)n, cudaMemcpyDeviceToDevice, s));
+            std::memcpy(hq + (size_t)f * n, grp[f]->q.data(), 16 * (size_t)n);
         }
+        {
+            Phase ph(ctx, "serve_q_upload");
+            CK(cudaMemcpyAsync(gq, hq, 16 * (size_t)n * nk, cudaMemcpyHostToDevice, s));
+        }
+        hq += (size_t)n * nk;
         // always the frequency-batch kernels: an entry is then the same whatever else arrived with it
         void *douts = nullptr;
         const std::string name = "srv_outs" + std::to_string(i);

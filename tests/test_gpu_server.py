@@ -113,6 +113,7 @@ def test_budget_admission_and_oversize_requests(gpu_ctx):
     # room for one request of the 1280-element mesh at a time (its 8 n^2 DLP matrix + state)
     budget = 8 * n1 * n1 + 60 * 16 * n1 + (1 << 20)
     sv = g.Server(ms, hbm_budget_bytes=budget, tol=1e-6, quantum=0, ctx=gpu_ctx)
+    sv.reserve()  # the whole budget mapped into the pool first: admission is unchanged
     rng = np.random.default_rng(23)
     ids = [sv.submit(1, float(k), meshes.plane_wave_neumann(*arrays[1], float(k), [rng.standard_normal(3)])[:, 0])
            for k in (1.0, 1.5, 2.0)]
