@@ -257,7 +257,7 @@ def measured_peaks():
 
 
 def recorded_traffic():
-    """Per-launch DRAM bytes of assemble_regular from the committed ncu summary, if any."""
+    """Per-launch DRAM bytes of the regular kernel from the committed ncu summary, if any."""
     try:
         with open(os.path.join(ROOT, "profiles", "roofline_traffic.json")) as f:
             d = json.load(f)
@@ -351,9 +351,9 @@ def run_ours(args):
     achieved = alg_bytes / (reg_avg / 1e3) / 1e9
     tr = recorded_traffic()
     traffic = None
-    if tr and tr.get("kernel") == "k_regular" and tr.get("n_elements") == n:
+    if tr and tr.get("kernel") == "k_regular2" and tr.get("n_elements") == n:
         traffic = tr.get("dram_bytes_per_launch")
-    roofline = {"kernel": "k_regular (assemble_regular.cu)", "bound": "hbm", "achieved": achieved, "peak": peak,
+    roofline = {"kernel": "k_regular2 (assemble_regular.cu)", "bound": "hbm", "achieved": achieved, "peak": peak,
                 "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,
                 "peak_source": "%s (MEASURED_PEAKS.json hbm_gbs)" % peak_kind if peak_kind == "measured" else "fallback 6.8 TB/s",
                 "algorithmic_bytes_per_launch": alg_bytes, "avg_launch_ms": reg_avg,
