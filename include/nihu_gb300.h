@@ -218,6 +218,15 @@ nihu_gb_status nihu_gb_assemble_bm(nihu_gb_ctx *ctx, const nihu_gb_mesh *test, c
                                    int precision, int dtype, void *out_dlpt, void *out_hsp, int64_t ld,
                                    int accumulate, int where);
 
+/* nihu_gb_assemble_bm() for a complex wave number k + i k_im (a lossy
+ * medium, as nihu_gb_assemble_c): the four kernels with e^{-ikr}, 1 + ikr and
+ * (ikr)^2 complex, the nearly singular dynamic parts and the HSP self term's
+ * remainder in FP64 with the complex kernel.  k_im = 0 is nihu_gb_assemble_bm. */
+nihu_gb_status nihu_gb_assemble_bm_c(nihu_gb_ctx *ctx, const nihu_gb_mesh *test, const nihu_gb_mesh *trial,
+                                     int family, int ops, double k, double k_im, double alpha_re, double alpha_im,
+                                     int precision, int dtype, void *out_dlpt, void *out_hsp, int64_t ld,
+                                     int accumulate, int where);
+
 /* The two Burton-Miller system matrices of one mesh with coupling c
  * (the reference application uses c = -i/k):
  *     A = DLP - 1/2 I + c HSP,   B = SLP + c DLPt + c/2 I
@@ -228,6 +237,12 @@ nihu_gb_status nihu_gb_assemble_bm(nihu_gb_ctx *ctx, const nihu_gb_mesh *test, c
 nihu_gb_status nihu_gb_assemble_burton_miller(nihu_gb_ctx *ctx, const nihu_gb_mesh *mesh, int family, double k,
                                               double coupling_re, double coupling_im, int precision, int dtype,
                                               void *out_a, void *out_b, int64_t ld, int where);
+
+/* nihu_gb_assemble_burton_miller() for a complex wave number k + i k_im (the
+ * coupling is the caller's, e.g. -i / (k + i k_im)). */
+nihu_gb_status nihu_gb_assemble_burton_miller_c(nihu_gb_ctx *ctx, const nihu_gb_mesh *mesh, int family, double k,
+                                                double k_im, double coupling_re, double coupling_im, int precision,
+                                                int dtype, void *out_a, void *out_b, int64_t ld, int where);
 
 /* Entries of an explicit list of element pairs (test rows[p], trial cols[p]),
  * each with the full singular check of the dense path (self, nearly singular
@@ -250,6 +265,12 @@ nihu_gb_status nihu_gb_assemble_pairs(nihu_gb_ctx *ctx, const nihu_gb_mesh *test
                                       int family, int ops, double k, const double *coef, const double *ident,
                                       int precision, int dtype, int64_t n_pairs, const int32_t *rows,
                                       const int32_t *cols, void *out_a, void *out_b, int where);
+
+/* nihu_gb_assemble_pairs() for a complex wave number k + i k_im. */
+nihu_gb_status nihu_gb_assemble_pairs_c(nihu_gb_ctx *ctx, const nihu_gb_mesh *test, const nihu_gb_mesh *trial,
+                                        int family, int ops, double k, double k_im, const double *coef,
+                                        const double *ident, int precision, int dtype, int64_t n_pairs,
+                                        const int32_t *rows, const int32_t *cols, void *out_a, void *out_b, int where);
 
 /* Per-pair quadrature statistics of an assembly (no matrix is written):
  * counts[0] self pairs, counts[1] nearly singular pairs, counts[2 + 3*s + d]
@@ -448,6 +469,12 @@ nihu_gb_status nihu_gb_solve_burton_miller(nihu_gb_ctx *ctx, const nihu_gb_mesh 
                                            double coupling_re, double coupling_im, int precision, int dtype,
                                            const void *q, void *p, int solver, int restart, int max_iters, double tol,
                                            int *iters, double *rel_residual);
+
+/* nihu_gb_solve_burton_miller() for a complex wave number k + i k_im. */
+nihu_gb_status nihu_gb_solve_burton_miller_c(nihu_gb_ctx *ctx, const nihu_gb_mesh *mesh, int family, double k,
+                                             double k_im, double coupling_re, double coupling_im, int precision,
+                                             int dtype, const void *q, void *p, int solver, int restart, int max_iters,
+                                             double tol, int *iters, double *rel_residual);
 
 /* A frequency sweep over fixed meshes captured once as a CUDA graph and
  * replayed per set of wave numbers (the batched counterpart of running

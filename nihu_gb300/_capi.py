@@ -82,6 +82,10 @@ SIGNATURES = {
     "nihu_gb_assemble_burton_miller": (_i, [_vp, _vp, _i, _d, _d, _d, _i, _i, _vp, _vp, _i64, _i]),
     "nihu_gb_assemble_pairs": (_i, [_vp, _vp, _vp, _i, _i, _d, _vp, _vp, _i, _i, _i64, _vp, _vp, _vp, _vp, _i]),
     "nihu_gb_solve_burton_miller": (_i, [_vp, _vp, _i, _d, _d, _d, _i, _i, _vp, _vp, _i, _i, _i, _d, _ip, _dp]),
+    "nihu_gb_assemble_bm_c": (_i, [_vp, _vp, _vp, _i, _i, _d, _d, _d, _d, _i, _i, _vp, _vp, _i64, _i, _i]),
+    "nihu_gb_assemble_burton_miller_c": (_i, [_vp, _vp, _i, _d, _d, _d, _d, _i, _i, _vp, _vp, _i64, _i]),
+    "nihu_gb_assemble_pairs_c": (_i, [_vp, _vp, _vp, _i, _i, _d, _d, _vp, _vp, _i, _i, _i64, _vp, _vp, _vp, _vp, _i]),
+    "nihu_gb_solve_burton_miller_c": (_i, [_vp, _vp, _i, _d, _d, _d, _d, _i, _i, _vp, _vp, _i, _i, _i, _d, _ip, _dp]),
 }
 
 _lib = None

@@ -370,19 +370,19 @@ def _assemble_into(ctx, result, test_mesh, trial_mesh, family, op, k, alpha, pre
                                            max(result.shape[0], 1), accumulate, C.HOST))
         else:
             if kc.imag != 0:
-                raise NotImplementedError("complex wave numbers: collocation SLP and DLP only")
+                raise NotImplementedError("complex wave numbers: collocation operators only")
             fn = L.nihu_gb_assemble_galerkin if galerkin else L.nihu_gb_assemble
             ctx.check(fn(ctx.handle, tdm.handle, rdm_handle, family, op, kc.real, alpha.real, alpha.imag, prec,
                          dtype, out_s, out_d, max(result.shape[0], 1), accumulate, C.HOST))
     elif galerkin:
         raise NotImplementedError("Galerkin formalism: SLP and DLP kernels only")
     else:
-        if complex(k).imag != 0:
-            raise NotImplementedError("complex wave numbers: collocation SLP and DLP only")
+        kc = complex(k)
         out_t = buf.ctypes.data if op == C.DLPT else None
         out_h = buf.ctypes.data if op == C.HSP else None
-        ctx.check(L.nihu_gb_assemble_bm(ctx.handle, tdm.handle, rdm_handle, family, op, k, alpha.real, alpha.imag,
-                                        prec, dtype, out_t, out_h, max(result.shape[0], 1), accumulate, C.HOST))
+        ctx.check(L.nihu_gb_assemble_bm_c(ctx.handle, tdm.handle, rdm_handle, family, op, kc.real, kc.imag,
+                                          alpha.real, alpha.imag, prec, dtype, out_t, out_h,
+                                          max(result.shape[0], 1), accumulate, C.HOST))
     if buf is not result:
         if target is None:
             result += buf.real.astype(result.dtype)
@@ -491,7 +491,7 @@ def solve_cbie(mesh: Mesh, k: float, q, family: int = C.HELMHOLTZ_3D, dtype: int
     return p, it.value, res.value
 
 
-def assemble_pairs(test: Mesh, trial: Mesh, rows, cols, ops: int, k: float = 0.0, family: int = C.HELMHOLTZ_3D,
+def assemble_pairs(test: Mesh, trial: Mesh, rows, cols, ops: int, k: complex = 0.0, family: int = C.HELMHOLTZ_3D,
                    coef=None, ident=None, dtype: int = C.C128, precision: str = "fp32", ctx: Context | None = None):
     """Entries of the element pairs (rows[p], cols[p]) with the full singular
     check, as the FMM near field (nihu/fmm/p2p_precompute.hpp):
@@ -516,21 +516,22 @@ def assemble_pairs(test: Mesh, trial: Mesh, rows, cols, ops: int, k: float = 0.0
     b = np.zeros(n, cdt) if need_b else None
     tdm = test.device(ctx)
     rdm = tdm if trial is test else trial.device(ctx)
-    ctx.check(C.lib().nihu_gb_assemble_pairs(
-        ctx.handle, tdm.handle, rdm.handle, family, ops, k, None if c is None else c.ctypes.data,
+    kc = complex(k)
+    ctx.check(C.lib().nihu_gb_assemble_pairs_c(
+        ctx.handle, tdm.handle, rdm.handle, family, ops, kc.real, kc.imag, None if c is None else c.ctypes.data,
         None if idn is None else idn.ctypes.data, C.REGULAR_FP64 if precision == "fp64" else C.REGULAR_FP32, dtype,
         n, rows.ctypes.data, cols.ctypes.data, None if a is None else a.ctypes.data,
         None if b is None else b.ctypes.data, C.HOST))
     return a, b
 
 
-def burton_miller_coupling(k: float) -> complex:
+def burton_miller_coupling(k: complex) -> complex:
     """The reference application's coupling constant -i/k
-    (nihu/applications/helmholtz/helmholtz_3d_coll.cpp:44)."""
-    return complex(0.0, -1.0 / k)
+    (nihu/applications/helmholtz/helmholtz_3d_coll.cpp:44), k real or complex."""
+    return -1j / complex(k)
 
 
-def assemble_burton_miller(mesh: Mesh, k: float, coupling=None, family: int = C.HELMHOLTZ_3D, dtype: int = C.C64,
+def assemble_burton_miller(mesh: Mesh, k: complex, coupling=None, family: int = C.HELMHOLTZ_3D, dtype: int = C.C64,
                            precision: str = "fp32", ctx: Context | None = None):
     """The Burton-Miller system matrices A = DLP - I/2 + c HSP and B = SLP + c DLPt + c/2 I
     (c = -i/k by default), assembled on the GPU in one pass; returns (A, B)."""
@@ -541,13 +542,14 @@ def assemble_burton_miller(mesh: Mesh, k: float, coupling=None, family: int = C.
     A = np.zeros((n, n), cdt, order="F")
     B = np.zeros((n, n), cdt, order="F")
     dm = mesh.device(ctx)
-    ctx.check(C.lib().nihu_gb_assemble_burton_miller(ctx.handle, dm.handle, family, k, c.real, c.imag,
-                                                     C.REGULAR_FP64 if precision == "fp64" else C.REGULAR_FP32,
-                                                     dtype, A.ctypes.data, B.ctypes.data, max(n, 1), C.HOST))
+    kc = complex(k)
+    ctx.check(C.lib().nihu_gb_assemble_burton_miller_c(ctx.handle, dm.handle, family, kc.real, kc.imag, c.real,
+                                                       c.imag, C.REGULAR_FP64 if precision == "fp64" else C.REGULAR_FP32,
+                                                       dtype, A.ctypes.data, B.ctypes.data, max(n, 1), C.HOST))
     return A, B
 
 
-def solve_burton_miller(mesh: Mesh, k: float, q, coupling=None, family: int = C.HELMHOLTZ_3D, dtype: int = C.C64,
+def solve_burton_miller(mesh: Mesh, k: complex, q, coupling=None, family: int = C.HELMHOLTZ_3D, dtype: int = C.C64,
                         solver: str = "gmres", precision: str = "fp32", restart: int = 50, max_iters: int = 1000,
                         tol: float = 1e-6, ctx: Context | None = None, check: bool = True):
     """Burton-Miller exterior solve A p = B q on the GPU (c = -i/k by default);
@@ -558,8 +560,9 @@ def solve_burton_miller(mesh: Mesh, k: float, q, coupling=None, family: int = C.
     p = np.zeros_like(q)
     it, res = ctypes.c_int(0), ctypes.c_double(0.0)
     dm = mesh.device(ctx)
-    st = C.lib().nihu_gb_solve_burton_miller(ctx.handle, dm.handle, family, k, c.real, c.imag,
-                                             C.REGULAR_FP64 if precision == "fp64" else C.REGULAR_FP32, dtype,
+    kc = complex(k)
+    st = C.lib().nihu_gb_solve_burton_miller_c(ctx.handle, dm.handle, family, kc.real, kc.imag, c.real, c.imag,
+                                               C.REGULAR_FP64 if precision == "fp64" else C.REGULAR_FP32, dtype,
                                              q.ctypes.data, p.ctypes.data, 0 if solver == "gmres" else 1, restart,
                                              max_iters, tol, ctypes.byref(it), ctypes.byref(res))
     if st != C.OK and (check or st != 6):

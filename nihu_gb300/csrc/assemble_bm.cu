@@ -71,7 +71,7 @@ __device__ __forceinline__ void store_bm(Out *p, R r0, R i0, R c0r, R c0i, R r1,
 //   middle every lane d/D >= 15.8: SLP, DLP, DLPt at the centroid, HSP at the
 //          centroid or (d/D < 22.3) its 3- or 4-point level
 //   general the per-lane levels; a level that only HSP uses evaluates HSP alone
-template <typename R, typename Out, int FAM, bool ALL4>
+template <typename R, typename Out, int FAM, bool ALL4, bool CK = false>
 __global__ void __launch_bounds__(BM_THREADS, sizeof(R) == 4 ? 4 : 1) k_regular_bm(BmArgs a)
 {
     __shared__ float4 s_hi[BM_COLS], s_lo[BM_COLS], s_p0[BM_COLS];
@@ -96,9 +96,10 @@ __global__ void __launch_bounds__(BM_THREADS, sizeof(R) == 4 ? 4 : 1) k_regular_
     const bool do_t = ALL4 || (a.ops & OP_DLPT);
     const bool do_h = ALL4 || (a.ops & OP_HSP);
     const R wt_on = do_t ? R(1) : R(0);
-    R k, x0, x1, x2, nx0, nx1, nx2, cr[4], ci[4];
+    R k, ki, x0, x1, x2, nx0, nx1, nx2, cr[4], ci[4];
     if constexpr (sizeof(R) == 4) {
         k = a.k32;
+        ki = a.k_im32;
         x0 = ih.x + il.x;
         x1 = ih.y + il.y;
         x2 = ih.z + il.z;
@@ -110,6 +111,7 @@ __global__ void __launch_bounds__(BM_THREADS, sizeof(R) == 4 ? 4 : 1) k_regular_
         for (int o = 0; o < 4; ++o) { cr[o] = a.cre32[o]; ci[o] = a.cim32[o]; }
     } else {
         k = a.k;
+        ki = a.k_im;
         x0 = test.center[3 * (int64_t)ii];
         x1 = test.center[3 * (int64_t)ii + 1];
         x2 = test.center[3 * (int64_t)ii + 2];
@@ -152,8 +154,8 @@ __global__ void __launch_bounds__(BM_THREADS, sizeof(R) == 4 ? 4 : 1) k_regular_
             const float q = (fx * fx + fy * fy + fz * fz) * h.w;
             if (__all_sync(0xffffffffu, q > q_far)) {
                 const float4 p = s_p0[c];
-                eval_bm<FAM, ALL4, float>(fx, fy, fz, p.x, p.y, p.z, p.w, nx0, nx1, nx2, k, 1.0f, 1.0f, wt_on,
-                                          do_h ? 1.0f : 0.0f, o);
+                eval_bm<FAM, ALL4, float, CK>(fx, fy, fz, p.x, p.y, p.z, p.w, nx0, nx1, nx2, k, 1.0f, 1.0f, wt_on,
+                                          do_h ? 1.0f : 0.0f, o, ki);
                 done = true;
             } else if (do_h && __all_sync(0xffffffffu, q > Q_FAR_BM2)) {
                 int ls, ld, lh;
@@ -161,11 +163,11 @@ __global__ void __launch_bounds__(BM_THREADS, sizeof(R) == 4 ? 4 : 1) k_regular_
                 classify_bm(ih, il, s_hi[c], s_lo[c], ii, j, test.center, trial.center, trial.size, a.same_mesh, ls,
                             ld, lh, dx, dy, dz);
                 const float4 p = s_p0[c];
-                eval_bm<FAM, ALL4, float>(fx, fy, fz, p.x, p.y, p.z, p.w, nx0, nx1, nx2, k, 1.0f, 1.0f, wt_on,
-                                          lh == 0 ? 1.0f : 0.0f, o);
+                eval_bm<FAM, ALL4, float, CK>(fx, fy, fz, p.x, p.y, p.z, p.w, nx0, nx1, nx2, k, 1.0f, 1.0f, wt_on,
+                                          lh == 0 ? 1.0f : 0.0f, o, ki);
                 if (lh == 1)
                     level_points(1, dx, dy, dz, [&](R rx, R ry, R rz, R wj, R n0, R n1, R n2) {
-                        eval_h<FAM, R>(rx, ry, rz, wj, n0, n1, n2, nx0, nx1, nx2, k, o);
+                        eval_h<FAM, R, CK>(rx, ry, rz, wj, n0, n1, n2, nx0, nx1, nx2, k, o, ki);
                     });
                 done = true;
             }
@@ -182,11 +184,11 @@ __global__ void __launch_bounds__(BM_THREADS, sizeof(R) == 4 ? 4 : 1) k_regular_
                 if (bs || bd || bt) {
                     const R ws = bs ? R(1) : R(0), wd = bd ? R(1) : R(0), wt = bt ? R(1) : R(0), wh = bh ? R(1) : R(0);
                     level_points(L, dx, dy, dz, [&](R rx, R ry, R rz, R wj, R n0, R n1, R n2) {
-                        eval_bm<FAM, ALL4, R>(rx, ry, rz, wj, n0, n1, n2, nx0, nx1, nx2, k, ws, wd, wt, wh, o);
+                        eval_bm<FAM, ALL4, R, CK>(rx, ry, rz, wj, n0, n1, n2, nx0, nx1, nx2, k, ws, wd, wt, wh, o, ki);
                     });
                 } else if (bh) {
                     level_points(L, dx, dy, dz, [&](R rx, R ry, R rz, R wj, R n0, R n1, R n2) {
-                        eval_h<FAM, R>(rx, ry, rz, wj, n0, n1, n2, nx0, nx1, nx2, k, o);
+                        eval_h<FAM, R, CK>(rx, ry, rz, wj, n0, n1, n2, nx0, nx1, nx2, k, o, ki);
                     });
                 }
             }
@@ -214,10 +216,10 @@ __global__ void __launch_bounds__(BM_THREADS, sizeof(R) == 4 ? 4 : 1) k_regular_
                     const float4 p = s_p0[c];
                     for (int q = 0; q < np; ++q) {
                         const float *t = par ? TRI67.p7[q] : TRI67.p6[q];
-                        eval_h<FAM, float>(dx + (b[0] + t[0] * f1[0] + t[1] * f2[0]),
+                        eval_h<FAM, float, CK>(dx + (b[0] + t[0] * f1[0] + t[1] * f2[0]),
                                            dy + (b[1] + t[0] * f1[1] + t[1] * f2[1]),
                                            dz + (b[2] + t[0] * f1[2] + t[1] * f2[2]), t[2] * Jf, p.y, p.z, p.w, nx0,
-                                           nx1, nx2, k, o);
+                                           nx1, nx2, k, o, ki);
                     }
                 } else {
                     for (int q = 0; q < np; ++q) {
@@ -225,8 +227,8 @@ __global__ void __launch_bounds__(BM_THREADS, sizeof(R) == 4 ? 4 : 1) k_regular_
                         tri_pt(par ? 7 : 6, q, xi, eta, w);
                         double y[3];
                         for (int d = 0; d < 3; ++d) y[d] = cc[d] + xi * e1[d] + eta * e2[d];
-                        eval_h<FAM, double>(y[0] - x0, y[1] - x1, y[2] - x2, w * J, n64[0], n64[1], n64[2], nx0,
-                                            nx1, nx2, k, o);
+                        eval_h<FAM, double, CK>(y[0] - x0, y[1] - x1, y[2] - x2, w * J, n64[0], n64[1], n64[2], nx0,
+                                            nx1, nx2, k, o, ki);
                     }
                 }
             }
@@ -246,7 +248,15 @@ __global__ void __launch_bounds__(BM_THREADS, sizeof(R) == 4 ? 4 : 1) k_regular_
 template <typename R, typename Out, int FAM>
 static void launch_bm_ops(const BmArgs &a, dim3 grid, cudaStream_t s)
 {
-    if (a.ops == (OP_SLP | OP_DLP | OP_DLPT | OP_HSP)) k_regular_bm<R, Out, FAM, true><<<grid, BM_THREADS, 0, s>>>(a);
+    const bool all4 = a.ops == (OP_SLP | OP_DLP | OP_DLPT | OP_HSP);
+    if constexpr (FAM == FAM_HELMHOLTZ) {
+        if (a.k_im != 0.0) {  // complex (lossy) wave number: separate instantiations
+            if (all4) k_regular_bm<R, Out, FAM, true, true><<<grid, BM_THREADS, 0, s>>>(a);
+            else k_regular_bm<R, Out, FAM, false, true><<<grid, BM_THREADS, 0, s>>>(a);
+            return;
+        }
+    }
+    if (all4) k_regular_bm<R, Out, FAM, true><<<grid, BM_THREADS, 0, s>>>(a);
     else k_regular_bm<R, Out, FAM, false><<<grid, BM_THREADS, 0, s>>>(a);
 }
 
@@ -275,7 +285,8 @@ cudaError_t launch_assemble_regular_bm(const BmArgs &a, cudaStream_t s)
 // One FP64 thread per nearly singular or self pair, all operators of the
 // launch from one plane frame, one set of side angles and one pass over the
 // 42 dynamic points
-template <typename Out>
+// CK: a complex (lossy) wave number, the FP64 complex schemes in both modes
+template <typename Out, bool CK>
 __global__ void __launch_bounds__(BM_SING_THREADS) k_singular_bm(BmArgs a, NearList near)
 {
     const int64_t p_begin = near.col_ptr ? near.col_ptr[a.j0] : 0;
@@ -313,7 +324,15 @@ __global__ void __launch_bounds__(BM_SING_THREADS) k_singular_bm(BmArgs a, NearL
         Elem64 e;
         load_elem(a.trial, j, e);
         Acc4 acc;
-        if (self) {
+        if constexpr (CK) {
+            const cd kc{k, a.k_im};
+            if (self) {
+                self_tria4_ck(e, fam, kc, x0, ops, acc);
+            } else {
+                near_dynamic4_ck(e, kc, x0, nx, ops, acc, a.trial.dyn42 + 42 * (int64_t)j);
+                near_static4(e, x0, nx, ops, acc);
+            }
+        } else if (self) {
             self_tria4(e, fam, k, x0, ops, acc);
         } else {
             if (fam == FAM_HELMHOLTZ) {
@@ -342,8 +361,14 @@ cudaError_t launch_assemble_singular_bm(const BmArgs &a, const NearList &near, c
     // at most two 4-warp blocks per SM (the FP64 pipe is the limit)
     const int64_t want = (total + BM_SING_THREADS - 1) / BM_SING_THREADS;
     const int blocks = (int)std::max<int64_t>(1, std::min<int64_t>(want, 2 * (int64_t)sms));
-    if (a.dtype == 0) k_singular_bm<float2><<<blocks, BM_SING_THREADS, 0, s>>>(a, near);
-    else k_singular_bm<double2><<<blocks, BM_SING_THREADS, 0, s>>>(a, near);
+    const bool ck = a.family == FAM_HELMHOLTZ && a.k_im != 0.0;
+    if (ck) {
+        if (a.dtype == 0) k_singular_bm<float2, true><<<blocks, BM_SING_THREADS, 0, s>>>(a, near);
+        else k_singular_bm<double2, true><<<blocks, BM_SING_THREADS, 0, s>>>(a, near);
+    } else {
+        if (a.dtype == 0) k_singular_bm<float2, false><<<blocks, BM_SING_THREADS, 0, s>>>(a, near);
+        else k_singular_bm<double2, false><<<blocks, BM_SING_THREADS, 0, s>>>(a, near);
+    }
     return cudaGetLastError();
 }
 

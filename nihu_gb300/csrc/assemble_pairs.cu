@@ -44,7 +44,8 @@ __device__ __forceinline__ void store_pair(Out *p, V vr, V vi)
     *p = o;
 }
 
-template <typename R, typename Out, int FAM>
+// CK: a complex (lossy) wave number (the point kernels' complex form)
+template <typename R, typename Out, int FAM, bool CK = false>
 __global__ void __launch_bounds__(PAIR_THREADS) k_pairs_regular(PairArgs a)
 {
     const DevMesh &test = a.test;
@@ -78,9 +79,10 @@ __global__ void __launch_bounds__(PAIR_THREADS) k_pairs_regular(PairArgs a)
         const int tnc = trial.nc[j];
         const bool S = (a.ops & OP_SLP) != 0, D = (a.ops & OP_DLP) != 0;
         const bool T = (a.ops & OP_DLPT) != 0, H = (a.ops & OP_HSP) != 0;
-        R k, x0, x1, x2, nx0, nx1, nx2, cr[4], ci[4];
+        R k, ki, x0, x1, x2, nx0, nx1, nx2, cr[4], ci[4];
         if constexpr (sizeof(R) == 4) {
             k = a.k32;
+            ki = a.k_im32;
             x0 = ih.x + il.x;
             x1 = ih.y + il.y;
             x2 = ih.z + il.z;
@@ -92,6 +94,7 @@ __global__ void __launch_bounds__(PAIR_THREADS) k_pairs_regular(PairArgs a)
             for (int o = 0; o < 4; ++o) { cr[o] = a.cre32[o]; ci[o] = a.cim32[o]; }
         } else {
             k = a.k;
+            ki = a.k_im;
             x0 = test.center[3 * (int64_t)i];
             x1 = test.center[3 * (int64_t)i + 1];
             x2 = test.center[3 * (int64_t)i + 2];
@@ -114,12 +117,12 @@ __global__ void __launch_bounds__(PAIR_THREADS) k_pairs_regular(PairArgs a)
                 if constexpr (sizeof(R) == 4) {
                     const float4 y = __ldg(trial.pts32 + 2 * (base + slot));
                     const float4 n = __ldg(trial.pts32 + 2 * (base + slot) + 1);
-                    eval_bm<FAM, true, float>(dx + y.x, dy + y.y, dz + y.z, y.w, n.x, n.y, n.z, nx0, nx1, nx2, k,
-                                              ws, wd, wt, wh, o);
+                    eval_bm<FAM, true, float, CK>(dx + y.x, dy + y.y, dz + y.z, y.w, n.x, n.y, n.z, nx0, nx1, nx2, k,
+                                              ws, wd, wt, wh, o, ki);
                 } else {
                     const double *y = trial.pts64 + 8 * (base + slot);
-                    eval_bm<FAM, true, double>(y[0] - x0, y[1] - x1, y[2] - x2, y[3], y[4], y[5], y[6], nx0, nx1, nx2,
-                                               k, ws, wd, wt, wh, o);
+                    eval_bm<FAM, true, double, CK>(y[0] - x0, y[1] - x1, y[2] - x2, y[3], y[4], y[5], y[6], nx0, nx1, nx2,
+                                               k, ws, wd, wt, wh, o, ki);
                 }
             }
         }
@@ -145,10 +148,10 @@ __global__ void __launch_bounds__(PAIR_THREADS) k_pairs_regular(PairArgs a)
                 const float4 pj = trial.p0[j];
                 for (int q = 0; q < np; ++q) {
                     const float *t = par ? TRI67.p7[q] : TRI67.p6[q];
-                    eval_h<FAM, float>(dx + (b[0] + t[0] * f1[0] + t[1] * f2[0]),
+                    eval_h<FAM, float, CK>(dx + (b[0] + t[0] * f1[0] + t[1] * f2[0]),
                                        dy + (b[1] + t[0] * f1[1] + t[1] * f2[1]),
                                        dz + (b[2] + t[0] * f1[2] + t[1] * f2[2]), t[2] * Jf, pj.y, pj.z, pj.w, nx0,
-                                       nx1, nx2, k, o);
+                                       nx1, nx2, k, o, ki);
                 }
             } else {
                 for (int q = 0; q < np; ++q) {
@@ -156,8 +159,8 @@ __global__ void __launch_bounds__(PAIR_THREADS) k_pairs_regular(PairArgs a)
                     tri_pt(par ? 7 : 6, q, xi, eta, w);
                     double y[3];
                     for (int d = 0; d < 3; ++d) y[d] = cc[d] + xi * e1[d] + eta * e2[d];
-                    eval_h<FAM, double>(y[0] - x0, y[1] - x1, y[2] - x2, w * J, n64[0], n64[1], n64[2], nx0, nx1,
-                                        nx2, k, o);
+                    eval_h<FAM, double, CK>(y[0] - x0, y[1] - x1, y[2] - x2, w * J, n64[0], n64[1], n64[2], nx0, nx1,
+                                        nx2, k, o, ki);
                 }
             }
         }
@@ -175,7 +178,8 @@ __global__ void __launch_bounds__(PAIR_THREADS) k_pairs_regular(PairArgs a)
     }
 }
 
-template <typename Out>
+// CK: a complex (lossy) wave number, the FP64 complex schemes in both modes
+template <typename Out, bool CK>
 __global__ void __launch_bounds__(PAIR_SING_THREADS) k_pairs_singular(PairArgs a)
 {
     const unsigned long long n_near = a.n_sing[0], count = n_near + a.n_sing[1];
@@ -202,7 +206,15 @@ __global__ void __launch_bounds__(PAIR_SING_THREADS) k_pairs_singular(PairArgs a
             const double *np = a.test.pts64 + 8 * ((int64_t)i * 2 * SLOTS) + 4;
             const double nx[3] = {np[0], np[1], np[2]};
             const OpSet ops{S, D, T, H};
-            if (self) {
+            if constexpr (CK) {
+                const cd kc{k, a.k_im};
+                if (self) {
+                    self_tria4_ck(e, fam, kc, x0, ops, acc);
+                } else {
+                    near_dynamic4_ck(e, kc, x0, nx, ops, acc, a.trial.dyn42 + 42 * (int64_t)j);
+                    near_static4(e, x0, nx, ops, acc);
+                }
+            } else if (self) {
                 self_tria4(e, fam, k, x0, ops, acc);
             } else {
                 if (fam == FAM_HELMHOLTZ) {
@@ -217,7 +229,29 @@ __global__ void __launch_bounds__(PAIR_SING_THREADS) k_pairs_singular(PairArgs a
             // quads (SLP and DLP only): Duffy self term, inverse mapping with
             // polar quadrature (Telles for the Helmholtz DLP) when nearly singular
             Acc q;
-            if (self) {
+            if constexpr (CK) {
+                // complex (lossy) wave number: the FP64 schemes with the complex kernel
+                const cd kc{k, a.k_im};
+                if (self) {
+                    self_quad(e, fam, kc, x0, S, D, q);
+                } else {
+                    const bool telles = fam == FAM_HELMHOLTZ && D;
+                    const bool polar_d = fam == FAM_LAPLACE && D;
+                    double r5[3] = {0, 0, 0}, r6[3] = {0, 0, 0};
+                    if (!inverse_mapping(e, x0, telles, r5, r6)) {
+                        atomicCAS(a.err, 0, (int)min(p + 1, (int64_t)0x7fffffff));
+                        continue;
+                    }
+                    if (S || polar_d) {
+                        Elem64 lin;
+                        linearized(e, r5[0], r5[1], lin);
+                        near_polar_sum(e, lin, fam, kc, x0, r5[0], r5[1], S, polar_d, q);
+                        if (fam == FAM_HELMHOLTZ) near_dynamic_ck(lin, kc, x0, S, polar_d, q, nullptr);
+                        near_static(lin, x0, S, polar_d, q);
+                    }
+                    if (telles) near_telles_sum(e, fam, kc, x0, r6, q);
+                }
+            } else if (self) {
                 self_quad(e, fam, k, x0, S, D, q);
             } else {
                 const bool telles = fam == FAM_HELMHOLTZ && D;
@@ -268,8 +302,12 @@ __global__ void __launch_bounds__(PAIR_SING_THREADS) k_pairs_singular(PairArgs a
 template <typename R, typename Out>
 static void launch_pairs_fam(const PairArgs &a, int blocks, cudaStream_t s)
 {
-    if (a.family == FAM_HELMHOLTZ) k_pairs_regular<R, Out, FAM_HELMHOLTZ><<<blocks, PAIR_THREADS, 0, s>>>(a);
-    else k_pairs_regular<R, Out, FAM_LAPLACE><<<blocks, PAIR_THREADS, 0, s>>>(a);
+    if (a.family == FAM_HELMHOLTZ) {
+        if (a.k_im != 0.0) k_pairs_regular<R, Out, FAM_HELMHOLTZ, true><<<blocks, PAIR_THREADS, 0, s>>>(a);
+        else k_pairs_regular<R, Out, FAM_HELMHOLTZ><<<blocks, PAIR_THREADS, 0, s>>>(a);
+    } else {
+        k_pairs_regular<R, Out, FAM_LAPLACE><<<blocks, PAIR_THREADS, 0, s>>>(a);
+    }
 }
 
 cudaError_t launch_assemble_pairs(const PairArgs &a, cudaStream_t s)
@@ -293,8 +331,14 @@ cudaError_t launch_assemble_pairs(const PairArgs &a, cudaStream_t s)
     // the singular list's length stays on the device: the kernel reads it
     const int64_t swant = (a.n + PAIR_SING_THREADS - 1) / PAIR_SING_THREADS;
     const int sblocks = (int)std::max<int64_t>(1, std::min<int64_t>(swant, 2 * (int64_t)sms));
-    if (a.dtype == 0) k_pairs_singular<float2><<<sblocks, PAIR_SING_THREADS, 0, s>>>(a);
-    else k_pairs_singular<double2><<<sblocks, PAIR_SING_THREADS, 0, s>>>(a);
+    const bool ck = a.family == FAM_HELMHOLTZ && a.k_im != 0.0;
+    if (ck) {
+        if (a.dtype == 0) k_pairs_singular<float2, true><<<sblocks, PAIR_SING_THREADS, 0, s>>>(a);
+        else k_pairs_singular<double2, true><<<sblocks, PAIR_SING_THREADS, 0, s>>>(a);
+    } else {
+        if (a.dtype == 0) k_pairs_singular<float2, false><<<sblocks, PAIR_SING_THREADS, 0, s>>>(a);
+        else k_pairs_singular<double2, false><<<sblocks, PAIR_SING_THREADS, 0, s>>>(a);
+    }
     return cudaGetLastError();
 }
 

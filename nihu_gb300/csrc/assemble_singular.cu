@@ -257,52 +257,15 @@ __device__ void self_tria(const Elem64 &e, int fam, double k, const double x0[3]
 }
 
 // self term of a constant triangle, complex (lossy) wave number: the static
-// part as self_tria, the dynamic (e^{-ikr} - 1)/r on the same 13 points in
-// the reference's form -ik e^{-ikr/2} sinc(kr/2), finite at r = 0 (the rule
-// holds the centroid), with z = kr/2 complex:
-//   e^{-iz} = e^{Im z} (cos Re z - i sin Re z),
-//   sin z = sin Re z cosh Im z + i cos Re z sinh Im z,
-//   sinc z = sin z / z, or 1 - z^2/6 (1 - z^2/20) for |z| <= 1e-3 (nihu/util/math_functions.hpp:54-61)
+// part as self_tria, the dynamic part in the complex sinc form
+// (tria_self_slp_dynamic_ck)
 __device__ void self_tria_ck(const Elem64 &e, int fam, cd k, const double x0[3], Acc &a)
 {
-    double st = self_static(e, x0);
-    double dr = 0.0, di = 0.0;
-    if (fam == FAM_HELMHOLTZ) {
-        double e1[3], e2[3], nt[3];
-        for (int d = 0; d < 3; ++d) { e1[d] = e.c[1][d] - e.c[0][d]; e2[d] = e.c[2][d] - e.c[0][d]; }
-        cross3(e1, e2, nt);
-        const double J = norm3(nt);
-        const cd mik{k.im, -k.re};  // -i k
-        for (int p = 0; p < 13; ++p) {
-            double xi, eta, w;
-            tri_pt(7, p, xi, eta, w);
-            double rv[3];
-            for (int d = 0; d < 3; ++d) rv[d] = e.c[0][d] + xi * e1[d] + eta * e2[d] - x0[d];
-            const double r = norm3(rv);
-            const cd z{0.5 * k.re * r, 0.5 * k.im * r};
-            double sr, cr;
-            sincos(z.re, &sr, &cr);
-            const double ez = exp(z.im);
-            const cd em{ez * cr, -ez * sr};  // e^{-iz}
-            cd sc;
-            if (sqrt(z.re * z.re + z.im * z.im) > 1e-3) {
-                const cd sz{sr * cosh(z.im), cr * sinh(z.im)};
-                const double den = z.re * z.re + z.im * z.im;  // sz / z = sz conj(z) / |z|^2
-                sc = {(sz.re * z.re + sz.im * z.im) / den, (sz.im * z.re - sz.re * z.im) / den};
-            } else {
-                const cd z2 = cmul(z, z);
-                const cd t = {1.0 - z2.re / 20.0, -z2.im / 20.0};
-                const cd u = cmul(z2, t);
-                sc = {1.0 - u.re / 6.0, -u.im / 6.0};
-            }
-            const cd v = cmul(mik, cmul(em, sc));
-            const double wj = w * J;
-            dr += v.re * wj;
-            di += v.im * wj;
-        }
-    }
-    a.sr += (st + dr) * INV_FOUR_PI;
-    a.si += di * INV_FOUR_PI;
+    const double st = self_static(e, x0);
+    cd dyn{0.0, 0.0};
+    if (fam == FAM_HELMHOLTZ) dyn = tria_self_slp_dynamic_ck(e, k, x0);
+    a.sr += (st + dyn.re) * INV_FOUR_PI;
+    a.si += dyn.im * INV_FOUR_PI;
 }
 
 // one nearly singular or self pair with a complex (lossy) wave number: the

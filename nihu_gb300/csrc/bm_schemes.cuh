@@ -15,9 +15,13 @@ struct BmSum {
 
 // one quadrature point of all four kernels sharing r, 1/r and one sincos;
 // ws / wd / wt / wh select the operators whose rule holds this point
-template <int FAM, bool ALL4, typename R>
+// CK: a complex (lossy) wave number k + i ki: with z = ikr = -ki r + i k r and
+// E = e^{-ikr} = e^{ki r} (cos kr - i sin kr), the SLP takes E, the DLP and
+// DLPt (1 + z) E and the HSP [m (1 + z) + a z^2] E, which are the real-k
+// expressions below at ki = 0 (nihu/library/helmholtz_kernel.hpp:42-54)
+template <int FAM, bool ALL4, typename R, bool CK = false>
 __device__ __forceinline__ void eval_bm(R rx, R ry, R rz, R wj, R ny0, R ny1, R ny2, R nx0, R nx1, R nx2, R k, R ws,
-                                        R wd, R wt, R wh, BmSum<R> &o)
+                                        R wd, R wt, R wh, BmSum<R> &o, R ki = R(0))
 {
     constexpr R INV4PI = R(1.0 / (4.0 * 3.14159265358979323846));
     const R r2 = rx * rx + ry * ry + rz * rz;
@@ -31,7 +35,38 @@ __device__ __forceinline__ void eval_bm(R rx, R ry, R rz, R wj, R ny0, R ny1, R 
     const R rdnx = -(rx * nx0 + ry * nx1 + rz * nx2) * rinv;
     const R aa = rdnx * rdny;
     const R m = R(3) * aa + (nx0 * ny0 + nx1 * ny1 + nx2 * ny2);
-    if constexpr (FAM == FAM_HELMHOLTZ) {
+    if constexpr (FAM == FAM_HELMHOLTZ && CK) {
+        const R r = r2 * rinv;
+        const R kr = k * r;
+        R s, c, damp;
+        if constexpr (sizeof(R) == 4) {
+            sincos_reduced(kr, s, c);
+            damp = expf(ki * r);
+        } else {
+            sincos(kr, &s, &c);
+            damp = exp(ki * r);
+        }
+        c *= damp;
+        s *= damp;
+        const R zr = -ki * r, zi = kr;
+        // (1 + z) E = p + i q
+        const R p = (R(1) + zr) * c + zi * s, q = zi * c - (R(1) + zr) * s;
+        if constexpr (ALL4) {
+            o.sr += ws * g * c;
+            o.si -= ws * g * s;
+            const R fd = -wd * g2 * rdny;
+            o.dr += fd * p;
+            o.di += fd * q;
+        }
+        const R ft = -wt * g2 * rdnx;
+        o.tr += ft * p;
+        o.ti += ft * q;
+        // m (1 + z) + a z^2 = u + i v
+        const R u = m * (R(1) + zr) + aa * (zr * zr - zi * zi), v = m * zi + R(2) * aa * zr * zi;
+        const R fh = wh * g3;
+        o.hr += fh * (u * c + v * s);
+        o.hi += fh * (v * c - u * s);
+    } else if constexpr (FAM == FAM_HELMHOLTZ) {
         const R kr = k * (r2 * rinv);
         R s, c;
         if constexpr (sizeof(R) == 4) sincos_reduced(kr, s, c);
@@ -64,9 +99,9 @@ __device__ __forceinline__ void eval_bm(R rx, R ry, R rz, R wj, R ny0, R ny1, R 
 }
 
 // HSP alone at one point (levels that no other operator of the pair uses)
-template <int FAM, typename R>
+template <int FAM, typename R, bool CK = false>
 __device__ __forceinline__ void eval_h(R rx, R ry, R rz, R wj, R ny0, R ny1, R ny2, R nx0, R nx1, R nx2, R k,
-                                       BmSum<R> &o)
+                                       BmSum<R> &o, R ki = R(0))
 {
     constexpr R INV4PI = R(1.0 / (4.0 * 3.14159265358979323846));
     const R r2 = rx * rx + ry * ry + rz * rz;
@@ -78,7 +113,24 @@ __device__ __forceinline__ void eval_h(R rx, R ry, R rz, R wj, R ny0, R ny1, R n
     const R rdnx = -(rx * nx0 + ry * nx1 + rz * nx2) * rinv;
     const R aa = rdnx * rdny;
     const R m = R(3) * aa + (nx0 * ny0 + nx1 * ny1 + nx2 * ny2);
-    if constexpr (FAM == FAM_HELMHOLTZ) {
+    if constexpr (FAM == FAM_HELMHOLTZ && CK) {
+        const R r = r2 * rinv;
+        const R kr = k * r;
+        R s, c, damp;
+        if constexpr (sizeof(R) == 4) {
+            sincos_reduced(kr, s, c);
+            damp = expf(ki * r);
+        } else {
+            sincos(kr, &s, &c);
+            damp = exp(ki * r);
+        }
+        c *= damp;
+        s *= damp;
+        const R zr = -ki * r, zi = kr;
+        const R u = m * (R(1) + zr) + aa * (zr * zr - zi * zi), v = m * zi + R(2) * aa * zr * zi;
+        o.hr += g3 * (u * c + v * s);
+        o.hi += g3 * (v * c - u * s);
+    } else if constexpr (FAM == FAM_HELMHOLTZ) {
         const R kr = k * (r2 * rinv);
         R s, c;
         if constexpr (sizeof(R) == 4) sincos_reduced(kr, s, c);
@@ -333,6 +385,62 @@ __device__ inline void near_dynamic4_f32(const Elem64 &e, double k, const double
     a.hi += hi;
 }
 
+// near_dynamic4 for a complex (lossy) wave number, in FP64 in both modes:
+// with z = ikr and E = e^{-ikr}, E - 1 = expm1(ki r) cos(kr) - 2 sin^2(kr/2)
+// - i e^{ki r} sin(kr) (no cancellation as r -> 0), the DLP / DLPt part
+// (1 + z) E - 1 = (E - 1) + z E and the HSP part [m (1 + z) + a z^2] E - m
+// = m (E - 1) + [m z + a z^2] E
+__device__ inline void near_dynamic4_ck(const Elem64 &e, cd k, const double x0[3], const double nx[3], OpSet ops,
+                                        Acc4 &a, const Pt4 *__restrict__ pts42)
+{
+    double en[3];
+    enormal(e, 1.0 / 3.0, 1.0 / 3.0, en);
+    const double nn = 1.0 / norm3(en);
+    for (int d = 0; d < 3; ++d) en[d] *= nn;
+    const double nxny = dot3(nx, en);
+    for (int p = 0; p < 42; ++p) {
+        const Pt4 v = pts42[p];
+        const double rv0 = v.x - x0[0], rv1 = v.y - x0[1], rv2 = v.z - x0[2];
+        const double r2 = rv0 * rv0 + rv1 * rv1 + rv2 * rv2;
+        const double rinv = rsqrt(r2);
+        const double r = r2 * rinv;
+        double sn, cs, sh, chh;
+        sincos(k.re * r, &sn, &cs);
+        sincos(0.5 * k.re * r, &sh, &chh);
+        const double ea = exp(k.im * r);
+        const cd em1{expm1(k.im * r) * cs - 2.0 * sh * sh, -ea * sn};  // E - 1
+        const cd E{ea * cs, -ea * sn};
+        const cd z{-k.im * r, k.re * r};
+        const double t = v.w * rinv * INV_FOUR_PI;  // w J / (4 pi r)
+        const double rdnx = -(rv0 * nx[0] + rv1 * nx[1] + rv2 * nx[2]) * rinv;
+        const double rdny = (rv0 * en[0] + rv1 * en[1] + rv2 * en[2]) * rinv;
+        const cd pm = cadd(em1, cmul(z, E));  // (1 + z) E - 1
+        if (ops.s) {
+            a.sr += t * em1.re;
+            a.si += t * em1.im;
+        }
+        if (ops.d) {
+            const double u = t * rinv * rdny;
+            a.dr -= u * pm.re;
+            a.di -= u * pm.im;
+        }
+        if (ops.t) {
+            const double u = t * rinv * rdnx;
+            a.tr -= u * pm.re;
+            a.ti -= u * pm.im;
+        }
+        if (ops.h) {
+            const double g3 = t * rinv * rinv;
+            const double aa = rdnx * rdny;
+            const double m = 3.0 * aa + nxny;
+            const cd w = cadd(cscale(z, m), cscale(cmul(z, z), aa));  // m z + a z^2
+            const cd hv = cadd(cscale(em1, m), cmul(w, E));
+            a.hr += g3 * hv.re;
+            a.hi += g3 * hv.im;
+        }
+    }
+}
+
 // the bounded remainder (e^{-ikr}(1 + ikr) - 1 + (ikr)^2/2) / r^3 of the HSP
 // kernel's expansion, its series below r = 1e-3
 // (nihu/library/helmholtz_singular_integrals.hpp:768-777)
@@ -414,6 +522,77 @@ __device__ inline void self_tria4(const Elem64 &e, int fam, double k, const doub
         } else {
             a.hr += (IddG0 + k * k / 2.0 * IG0h + h_dr) * INV_FOUR_PI;
             a.hi += h_di * INV_FOUR_PI;
+        }
+    }
+}
+
+// hsp_remainder for a complex wave number: the same expression with z = ikr
+// complex, its series below r = 1e-3 times -i k^3
+__device__ __forceinline__ cd hsp_remainder_ck(double r, cd k)
+{
+    const cd z{-k.im * r, k.re * r};
+    if (fabs(r) > 1e-3) {
+        double sn, cs;
+        sincos(k.re * r, &sn, &cs);
+        const double ea = exp(k.im * r);
+        const cd E{ea * cs, -ea * sn};
+        const cd z2 = cmul(z, z);
+        const cd v = cadd(cadd(cmul(cd{1.0 + z.re, z.im}, E), cd{-1.0, 0.0}), cscale(z2, 0.5));
+        return cscale(v, 1.0 / (r * r * r));
+    }
+    cd h{1.0 / 840.0, 0.0};
+    h = cadd(h, cscale(z, -1.0 / 5760.0));
+    h = cadd(cd{1.0 / 144.0, 0.0}, cscale(cmul(z, h), -1.0));
+    h = cadd(cd{1.0 / 30.0, 0.0}, cscale(cmul(z, h), -1.0));
+    h = cadd(cd{1.0 / 8.0, 0.0}, cscale(cmul(z, h), -1.0));
+    h = cadd(cd{1.0 / 3.0, 0.0}, cscale(cmul(z, h), -1.0));
+    const cd k3 = cmul(k, cmul(k, k));
+    return cmul(cd{k3.im, -k3.re}, h);  // -i k^3 h
+}
+
+// self_tria4 for a complex (lossy) wave number: the SLP's dynamic part in the
+// complex sinc form (tria_self_slp_dynamic_ck), the HSP's IddG0 + k^2/2 IG0'
+// with complex k^2 and the complex remainder
+__device__ inline void self_tria4_ck(const Elem64 &e, int fam, cd k, const double x0[3], OpSet ops, Acc4 &a)
+{
+    double r[4], th[4], al[4];
+    corner_angles(e, x0, r, th, al);
+    double IG0 = 0.0, IG0h = 0.0, IddG0 = 0.0;
+    for (int i = 0; i < 3; ++i) {
+        const double g = r[i] * sin(al[i]) * log(tan((al[i] + th[i]) / 2.0) / tan(al[i] / 2.0));
+        IG0 += g;
+        if (th[i] < 1e-3) continue;
+        IG0h += g;
+        IddG0 += (cos(al[i] + th[i]) - cos(al[i])) / (r[i] * sin(al[i]));
+    }
+    cd sdyn{0.0, 0.0}, hdyn{0.0, 0.0};
+    if (fam == FAM_HELMHOLTZ) {
+        if (ops.s) sdyn = tria_self_slp_dynamic_ck(e, k, x0);
+        if (ops.h) {
+            double e1[3], e2[3], nt[3];
+            for (int d = 0; d < 3; ++d) { e1[d] = e.c[1][d] - e.c[0][d]; e2[d] = e.c[2][d] - e.c[0][d]; }
+            cross3(e1, e2, nt);
+            const double J = norm3(nt);
+            for (int p = 0; p < 13; ++p) {
+                double xi, eta, w;
+                tri_pt(7, p, xi, eta, w);
+                double rv[3];
+                for (int d = 0; d < 3; ++d) rv[d] = e.c[0][d] + xi * e1[d] + eta * e2[d] - x0[d];
+                hdyn = cadd(hdyn, cscale(hsp_remainder_ck(norm3(rv), k), w * J));
+            }
+        }
+    }
+    if (ops.s) {
+        a.sr += (IG0 + sdyn.re) * INV_FOUR_PI;
+        a.si += sdyn.im * INV_FOUR_PI;
+    }
+    if (ops.h) {
+        if (fam == FAM_LAPLACE) {
+            a.hr += IddG0 * INV_FOUR_PI;
+        } else {
+            const cd k2h = cscale(cmul(k, k), 0.5 * IG0h);
+            a.hr += (IddG0 + k2h.re + hdyn.re) * INV_FOUR_PI;
+            a.hi += (k2h.im + hdyn.im) * INV_FOUR_PI;
         }
     }
 }

@@ -799,8 +799,8 @@ nihu_gb_status bm_check(nihu_gb_ctx *ctx, const char *fn, const nihu_gb_mesh *te
     return NIHU_GB_OK;
 }
 
-BmArgs bm_args(const nihu_gb_mesh *test, const nihu_gb_mesh *trial, int family, int ops, double k, const double c[8],
-               int precision, int dtype, int accumulate)
+BmArgs bm_args(const nihu_gb_mesh *test, const nihu_gb_mesh *trial, int family, int ops, double k, double k_im,
+               const double c[8], int precision, int dtype, int accumulate)
 {
     BmArgs b;
     b.test = test->dm;
@@ -810,6 +810,8 @@ BmArgs bm_args(const nihu_gb_mesh *test, const nihu_gb_mesh *trial, int family, 
     b.ops = ops;
     b.k = family == NIHU_GB_HELMHOLTZ_3D ? k : 0.0;
     b.k32 = (float)b.k;
+    b.k_im = family == NIHU_GB_HELMHOLTZ_3D ? k_im : 0.0;
+    b.k_im32 = (float)b.k_im;
     for (int o = 0; o < 4; ++o) {
         b.cre[o] = c[2 * o];
         b.cim[o] = c[2 * o + 1];
@@ -856,9 +858,19 @@ nihu_gb_status nihu_gb_assemble_bm(nihu_gb_ctx *ctx, const nihu_gb_mesh *test, c
                                    int ops, double k, double alpha_re, double alpha_im, int precision, int dtype,
                                    void *out_dlpt, void *out_hsp, int64_t ld, int accumulate, int where)
 {
+    return nihu_gb_assemble_bm_c(ctx, test, trial, family, ops, k, 0.0, alpha_re, alpha_im, precision, dtype, out_dlpt,
+                                 out_hsp, ld, accumulate, where);
+}
+
+nihu_gb_status nihu_gb_assemble_bm_c(nihu_gb_ctx *ctx, const nihu_gb_mesh *test, const nihu_gb_mesh *trial,
+                                     int family, int ops, double k, double k_im, double alpha_re, double alpha_im,
+                                     int precision, int dtype, void *out_dlpt, void *out_hsp, int64_t ld,
+                                     int accumulate, int where)
+{
     if (!ctx) return NIHU_GB_ERR_INVALID_ARGUMENT;
     nihu_gb_status st = bm_check(ctx, "nihu_gb_assemble_bm", test, trial, family, k, precision, dtype, where, ld);
     if (st) return st;
+    if (!std::isfinite(k_im)) return fail(ctx, NIHU_GB_ERR_INVALID_ARGUMENT, "nihu_gb_assemble_bm: non-finite wave number");
     if (ops < NIHU_GB_DLPT || (ops & ~(NIHU_GB_DLPT | NIHU_GB_HSP)))
         return fail(ctx, NIHU_GB_ERR_INVALID_ARGUMENT, "nihu_gb_assemble_bm: ops must be DLPt, HSP or both");
     if (((ops & NIHU_GB_DLPT) && !out_dlpt) || ((ops & NIHU_GB_HSP) && !out_hsp))
@@ -870,7 +882,7 @@ nihu_gb_status nihu_gb_assemble_bm(nihu_gb_ctx *ctx, const nihu_gb_mesh *test, c
     NearList *nl = nullptr;
     if ((st = get_near(ctx, test, trial, &nl))) return st;
     const double c[8] = {0, 0, 0, 0, alpha_re, alpha_im, alpha_re, alpha_im};
-    BmArgs b = bm_args(test, trial, family, ops, k, c, precision, dtype, accumulate);
+    BmArgs b = bm_args(test, trial, family, ops, k, k_im, c, precision, dtype, accumulate);
     return assemble_bm_all(ctx, b, nl, (ops & NIHU_GB_HSP) ? out_hsp : nullptr,
                            (ops & NIHU_GB_DLPT) ? out_dlpt : nullptr, ld, where, test->n, trial->n);
 }
@@ -879,10 +891,20 @@ nihu_gb_status nihu_gb_assemble_burton_miller(nihu_gb_ctx *ctx, const nihu_gb_me
                                               double coupling_re, double coupling_im, int precision, int dtype,
                                               void *out_a, void *out_b, int64_t ld, int where)
 {
+    return nihu_gb_assemble_burton_miller_c(ctx, mesh, family, k, 0.0, coupling_re, coupling_im, precision, dtype,
+                                            out_a, out_b, ld, where);
+}
+
+nihu_gb_status nihu_gb_assemble_burton_miller_c(nihu_gb_ctx *ctx, const nihu_gb_mesh *mesh, int family, double k,
+                                                double k_im, double coupling_re, double coupling_im, int precision,
+                                                int dtype, void *out_a, void *out_b, int64_t ld, int where)
+{
     if (!ctx) return NIHU_GB_ERR_INVALID_ARGUMENT;
     nihu_gb_status st =
         bm_check(ctx, "nihu_gb_assemble_burton_miller", mesh, mesh, family, k, precision, dtype, where, ld);
     if (st) return st;
+    if (!std::isfinite(k_im))
+        return fail(ctx, NIHU_GB_ERR_INVALID_ARGUMENT, "nihu_gb_assemble_burton_miller: non-finite wave number");
     if (!out_a || !out_b) return fail(ctx, NIHU_GB_ERR_INVALID_ARGUMENT, "nihu_gb_assemble_burton_miller: missing output buffer");
     if (!std::isfinite(coupling_re) || !std::isfinite(coupling_im))
         return fail(ctx, NIHU_GB_ERR_INVALID_ARGUMENT, "nihu_gb_assemble_burton_miller: non-finite coupling");
@@ -892,7 +914,7 @@ nihu_gb_status nihu_gb_assemble_burton_miller(nihu_gb_ctx *ctx, const nihu_gb_me
     NearList *nl = nullptr;
     if ((st = get_near(ctx, mesh, mesh, &nl))) return st;
     const double c[8] = {1, 0, 1, 0, coupling_re, coupling_im, coupling_re, coupling_im};
-    BmArgs b = bm_args(mesh, mesh, family, BM_ALL, k, c, precision, dtype, 0);
+    BmArgs b = bm_args(mesh, mesh, family, BM_ALL, k, k_im, c, precision, dtype, 0);
     if (where == NIHU_GB_DEVICE) {
         if ((st = assemble_bm_all(ctx, b, nl, out_a, out_b, ld, where, n, n))) return st;
         // A -= I/2, B += c/2 I (helmholtz_3d_coll.cpp:71-72, 91)
@@ -911,7 +933,17 @@ nihu_gb_status nihu_gb_assemble_pairs(nihu_gb_ctx *ctx, const nihu_gb_mesh *test
                                       int dtype, int64_t n_pairs, const int32_t *rows, const int32_t *cols,
                                       void *out_a, void *out_b, int where)
 {
+    return nihu_gb_assemble_pairs_c(ctx, test, trial, family, ops, k, 0.0, coef, ident, precision, dtype, n_pairs,
+                                    rows, cols, out_a, out_b, where);
+}
+
+nihu_gb_status nihu_gb_assemble_pairs_c(nihu_gb_ctx *ctx, const nihu_gb_mesh *test, const nihu_gb_mesh *trial,
+                                        int family, int ops, double k, double k_im, const double *coef,
+                                        const double *ident, int precision, int dtype, int64_t n_pairs,
+                                        const int32_t *rows, const int32_t *cols, void *out_a, void *out_b, int where)
+{
     if (!ctx) return NIHU_GB_ERR_INVALID_ARGUMENT;
+    if (!std::isfinite(k_im)) return fail(ctx, NIHU_GB_ERR_INVALID_ARGUMENT, "nihu_gb_assemble_pairs: non-finite wave number");
     const char *fn = "nihu_gb_assemble_pairs";
     if (!test || !trial || test->ctx != ctx || trial->ctx != ctx)
         return fail(ctx, NIHU_GB_ERR_INVALID_ARGUMENT, std::string(fn) + ": meshes must belong to the context");
@@ -943,6 +975,8 @@ nihu_gb_status nihu_gb_assemble_pairs(nihu_gb_ctx *ctx, const nihu_gb_mesh *test
     a.ops = ops;
     a.k = family == NIHU_GB_HELMHOLTZ_3D ? k : 0.0;
     a.k32 = (float)a.k;
+    a.k_im = family == NIHU_GB_HELMHOLTZ_3D ? k_im : 0.0;
+    a.k_im32 = (float)a.k_im;
     for (int o = 0; o < 4; ++o) {
         a.cre[o] = coef ? coef[2 * o] : 1.0;
         a.cim[o] = coef ? coef[2 * o + 1] : 0.0;
@@ -1651,6 +1685,15 @@ nihu_gb_status nihu_gb_solve_burton_miller(nihu_gb_ctx *ctx, const nihu_gb_mesh 
                                            const void *q, void *p, int solver, int restart, int max_iters, double tol,
                                            int *iters, double *rel_residual)
 {
+    return nihu_gb_solve_burton_miller_c(ctx, mesh, family, k, 0.0, coupling_re, coupling_im, precision, dtype, q, p,
+                                         solver, restart, max_iters, tol, iters, rel_residual);
+}
+
+nihu_gb_status nihu_gb_solve_burton_miller_c(nihu_gb_ctx *ctx, const nihu_gb_mesh *mesh, int family, double k,
+                                             double k_im, double coupling_re, double coupling_im, int precision,
+                                             int dtype, const void *q, void *p, int solver, int restart, int max_iters,
+                                             double tol, int *iters, double *rel_residual)
+{
     if (!ctx) return NIHU_GB_ERR_INVALID_ARGUMENT;
     if (!mesh || !q || !p || (solver != 0 && solver != 1) || (solver == 1 && dtype != NIHU_GB_C128) || !valid_dtype(dtype))
         return fail(ctx, NIHU_GB_ERR_INVALID_ARGUMENT, "nihu_gb_solve_burton_miller: bad argument");
@@ -1666,8 +1709,8 @@ nihu_gb_status nihu_gb_solve_burton_miller(nihu_gb_ctx *ctx, const nihu_gb_mesh 
     if ((st = scratch(ctx, "cbie_rhs", 16 * n, &drhs))) return st;
     if ((st = scratch(ctx, "cbie_p", 16 * n, &dp))) return st;
     CK(cudaMemcpyAsync(dq, q, 16 * n, cudaMemcpyHostToDevice, ctx->stream));
-    st = nihu_gb_assemble_burton_miller(ctx, mesh, family, k, coupling_re, coupling_im, precision, dtype, A, B, n,
-                                        NIHU_GB_DEVICE);
+    st = nihu_gb_assemble_burton_miller_c(ctx, mesh, family, k, k_im, coupling_re, coupling_im, precision, dtype, A,
+                                          B, n, NIHU_GB_DEVICE);
     if (st) return st;
     return solve_tail(ctx, n, dtype, B, A, dq, drhs, dp, p, solver, restart, max_iters, tol, iters, rel_residual);
 }

@@ -135,6 +135,8 @@ struct BmArgs {
     int family = 0, ops = 0;
     double k = 0.0;
     float k32 = 0.0f;
+    double k_im = 0.0;  // imaginary part of a complex (lossy) wave number
+    float k_im32 = 0.0f;
     double cre[4] = {0, 0, 0, 0}, cim[4] = {0, 0, 0, 0};
     float cre32[4] = {0, 0, 0, 0}, cim32[4] = {0, 0, 0, 0};
     int precision = 0;  // regular entries: 0 FP32, 1 FP64
@@ -166,6 +168,8 @@ struct PairArgs {
     int family = 0, ops = 0;
     double k = 0.0;
     float k32 = 0.0f;
+    double k_im = 0.0;  // imaginary part of a complex (lossy) wave number
+    float k_im32 = 0.0f;
     double cre[4] = {0, 0, 0, 0}, cim[4] = {0, 0, 0, 0};
     float cre32[4] = {0, 0, 0, 0}, cim32[4] = {0, 0, 0, 0};
     double id_re[2] = {0, 0}, id_im[2] = {0, 0};

@@ -69,9 +69,11 @@ def gpu_bm(ctx, mesh, family, ops, k, precision, dtype, test_mesh=None, alpha=1.
     cdt = np.complex64 if dtype == g.C64 else np.complex128
     outs = {op: np.zeros((m, n), dtype=cdt, order="F") for op in (g.DLPT, g.HSP) if ops & op}
     alpha = complex(alpha)
-    ctx.check(L.nihu_gb_assemble_bm(ctx.handle, test.handle, trial.handle, family, ops, k, alpha.real, alpha.imag,
-                                    precision, dtype, outs[g.DLPT].ctypes.data if g.DLPT in outs else None,
-                                    outs[g.HSP].ctypes.data if g.HSP in outs else None, m, 0, where))
+    kc = complex(k)
+    ctx.check(L.nihu_gb_assemble_bm_c(ctx.handle, test.handle, trial.handle, family, ops, kc.real, kc.imag,
+                                      alpha.real, alpha.imag, precision, dtype,
+                                      outs[g.DLPT].ctypes.data if g.DLPT in outs else None,
+                                      outs[g.HSP].ctypes.data if g.HSP in outs else None, m, 0, where))
     return outs
 
 
@@ -140,6 +142,50 @@ def test_burton_miller_system_matrices(gpu_ctx, oracle, precision, dtype, tol):
              + 0.5 * c * np.eye(n))
     assert rel_norm(A.astype(np.complex128), A_ref) <= tol
     assert rel_norm(B.astype(np.complex128), B_ref) <= tol
+
+
+@pytest.mark.parametrize("name,k", [("ico2", 2.0 - 0.3j), ("ico3", 4.0 - 0.5j), ("ico3", 1.3 + 0.2j)])
+def test_complex_wave_number_against_oracle(gpu_ctx, oracle, name, k):
+    """DLPt and HSP with a complex (lossy) wave number (nihu_gb_assemble_bm_c):
+    FP64 mode within 1e-11 of the oracle (normwise); FP32 mode every entry
+    within 1e-5 of its own magnitude (the DLPt diagonal, zero on flat
+    elements, within 1e-6 of the largest entry)."""
+    mesh = get_mesh(name)
+    o64 = gpu_bm(gpu_ctx, mesh, g.HELMHOLTZ_3D, g.DLPT | g.HSP, k, g.REGULAR_FP64, g.C128)
+    o32 = gpu_bm(gpu_ctx, mesh, g.HELMHOLTZ_3D, g.DLPT | g.HSP, k, g.REGULAR_FP32, g.C64)
+    for op, oop in ((g.DLPT, oracle.DLPT), (g.HSP, oracle.HSP)):
+        ref = oracle_matrix(oracle, name, g.HELMHOLTZ_3D, oop, k)
+        assert rel_norm(o64[op], ref) <= 1e-11, (op, rel_norm(o64[op], ref))
+        got = o32[op].astype(np.complex128)
+        ref = ref.copy()
+        if op == g.DLPT:
+            assert np.abs(np.diagonal(got)).max() < 1e-6 * np.abs(ref).max()
+            np.fill_diagonal(ref, 1.0)
+            np.fill_diagonal(got, 1.0)
+        err = np.abs(got - ref) / np.abs(ref)
+        assert err.max() < 1e-5, (op, err.max())
+
+
+def test_burton_miller_complex_wave_number(gpu_ctx, oracle):
+    """The system matrices with k = 2 - 0.3i and the coupling -i/k, and the
+    GMRES solve of the pulsating sphere against the oracle's dense solve."""
+    name, k = "ico3", 2.0 - 0.3j
+    n = len(get_mesh(name)[1])
+    c = g.burton_miller_coupling(k)
+    H = g.HELMHOLTZ_3D
+    A_ref = (oracle_matrix(oracle, name, H, oracle.DLP, k) - 0.5 * np.eye(n)
+             + c * oracle_matrix(oracle, name, H, oracle.HSP, k))
+    B_ref = (oracle_matrix(oracle, name, H, oracle.SLP, k) + c * oracle_matrix(oracle, name, H, oracle.DLPT, k)
+             + 0.5 * c * np.eye(n))
+    m = g.create_mesh(*get_mesh(name))
+    for precision, dtype, tol in (("fp64", g.C128, 1e-11), ("fp32", g.C64, 1e-5)):
+        A, B = g.assemble_burton_miller(m, k, dtype=dtype, precision=precision, ctx=gpu_ctx)
+        assert rel_norm(A.astype(np.complex128), A_ref) <= tol
+        assert rel_norm(B.astype(np.complex128), B_ref) <= tol
+    q = np.ones(n, np.complex128)
+    p, it, res = g.solve_burton_miller(m, k, q, dtype=g.C128, precision="fp64", tol=1e-10, ctx=gpu_ctx)
+    p_ref = np.linalg.solve(A_ref, B_ref @ q)
+    assert np.abs(p - p_ref).max() / np.abs(p_ref).max() < 1e-8
 
 
 @pytest.mark.parametrize("k", [np.pi, 4.4934])

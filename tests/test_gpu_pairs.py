@@ -169,3 +169,27 @@ def test_device_arrays_and_errors(gpu_ctx):
     # an empty list is a no-op
     a, b = g.assemble_pairs(m, m, [], [], g.SLP | g.DLP, 1.0, ctx=gpu_ctx)
     assert len(a) == 0 and len(b) == 0
+
+
+@pytest.mark.parametrize("name", ["ico3", "mixed"])
+@pytest.mark.parametrize("precision,tol", [("fp64", 1e-11), ("fp32", 1e-5)])
+def test_complex_wave_number_pairs(gpu_ctx, oracle, name, precision, tol):
+    """A complex (lossy) wave number (nihu_gb_assemble_pairs_c): SLP and DLP
+    on triangles and quads (Duffy self terms, inverse-mapped nearly singular
+    quads), and on the icosphere the Burton-Miller near field with DLPt and
+    HSP, against the oracle's entries of the same pairs."""
+    mesh = meshes.icosphere(3) if name == "ico3" else mixed_mesh()
+    k = 2.5 - 0.4j
+    rows, cols = pair_list(mesh, seed=3)
+    m = g.create_mesh(*mesh)
+    ops = g.SLP | g.DLP | g.DLPT | g.HSP if name == "ico3" else g.SLP | g.DLP
+    alpha = -1j / k
+    coef = [1.0, 1.0, alpha, alpha]
+    a, b = g.assemble_pairs(m, m, rows, cols, ops, k, coef=coef, precision=precision, ctx=gpu_ctx)
+    A = oracle_dense(oracle, name, mesh, oracle.DLP, k)
+    B = oracle_dense(oracle, name, mesh, oracle.SLP, k)
+    if name == "ico3":
+        A = A + alpha * oracle_dense(oracle, name, mesh, oracle.HSP, k)
+        B = B + alpha * oracle_dense(oracle, name, mesh, oracle.DLPT, k)
+    assert np.abs(a - A[rows, cols]).max() / np.abs(A).max() <= tol
+    assert np.abs(b - B[rows, cols]).max() / np.abs(B).max() <= tol
