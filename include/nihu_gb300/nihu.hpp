@@ -221,9 +221,9 @@ inline kernel_desc laplace_3d_DLP_kernel() { return {NIHU_GB_LAPLACE_3D, NIHU_GB
 // Burton-Miller kernels (nihu/library/helmholtz_kernel.hpp:326-334): constant
 // triangle trial elements only
 template <class WaveNumber = double>
-inline kernel_desc helmholtz_3d_DLPt_kernel(WaveNumber k) { return {NIHU_GB_HELMHOLTZ_3D, NIHU_GB_DLPT, (double)k}; }
+inline kernel_desc helmholtz_3d_DLPt_kernel(WaveNumber k) { return detail::with_k(NIHU_GB_HELMHOLTZ_3D, NIHU_GB_DLPT, k); }
 template <class WaveNumber = double>
-inline kernel_desc helmholtz_3d_HSP_kernel(WaveNumber k) { return {NIHU_GB_HELMHOLTZ_3D, NIHU_GB_HSP, (double)k}; }
+inline kernel_desc helmholtz_3d_HSP_kernel(WaveNumber k) { return detail::with_k(NIHU_GB_HELMHOLTZ_3D, NIHU_GB_HSP, k); }
 inline kernel_desc laplace_3d_DLPt_kernel() { return {NIHU_GB_LAPLACE_3D, NIHU_GB_DLPT, 0.0}; }
 inline kernel_desc laplace_3d_HSP_kernel() { return {NIHU_GB_LAPLACE_3D, NIHU_GB_HSP, 0.0}; }
 
@@ -327,7 +327,7 @@ Res &operator<<(Res &result, weighted_residual<TS> const &wr)
         void *out_s = kop == NIHU_GB_SLP ? (void *)result.data() : nullptr;
         void *out_d = kop == NIHU_GB_DLP ? (void *)result.data() : nullptr;
         if (op.kernel.k_im != 0.0) {
-            if (galerkin) throw std::invalid_argument("complex wave numbers: collocation SLP and DLP only");
+            if (galerkin) throw std::invalid_argument("complex wave numbers: collocation operators only");
             check(ctx.handle(), nihu_gb_assemble_c(ctx.handle(), tmh, rmh, op.kernel.family, kop, op.kernel.k,
                                                    op.kernel.k_im, op.scale.real(), op.scale.imag(), wr.precision,
                                                    detail::storage<T>::dtype, out_s, out_d, m, 1, NIHU_GB_HOST));
@@ -340,12 +340,11 @@ Res &operator<<(Res &result, weighted_residual<TS> const &wr)
     } else if (galerkin) {
         throw std::invalid_argument("Galerkin formalism: SLP and DLP kernels only");
     } else {
-        if (op.kernel.k_im != 0.0) throw std::invalid_argument("complex wave numbers: collocation SLP and DLP only");
         void *out_t = kop == NIHU_GB_DLPT ? (void *)result.data() : nullptr;
         void *out_h = kop == NIHU_GB_HSP ? (void *)result.data() : nullptr;
-        check(ctx.handle(), nihu_gb_assemble_bm(ctx.handle(), tmh, rmh, op.kernel.family, kop, op.kernel.k,
-                                                op.scale.real(), op.scale.imag(), wr.precision,
-                                                detail::storage<T>::dtype, out_t, out_h, m, 1, NIHU_GB_HOST));
+        check(ctx.handle(), nihu_gb_assemble_bm_c(ctx.handle(), tmh, rmh, op.kernel.family, kop, op.kernel.k,
+                                                  op.kernel.k_im, op.scale.real(), op.scale.imag(), wr.precision,
+                                                  detail::storage<T>::dtype, out_t, out_h, m, 1, NIHU_GB_HOST));
     }
     return result;
 }
