@@ -191,6 +191,14 @@ nihu_gb_status nihu_gb_assemble_galerkin(nihu_gb_ctx *ctx, const nihu_gb_mesh *t
                                          int precision, int dtype, void *out_slp, void *out_dlp, int64_t ld,
                                          int accumulate, int where);
 
+/* nihu_gb_assemble_galerkin() for a complex wave number k + i k_im (a lossy
+ * medium): the regular pairs with the complex point kernel, the singular and
+ * nearly singular rules in FP64 with the complex kernel in both modes. */
+nihu_gb_status nihu_gb_assemble_galerkin_c(nihu_gb_ctx *ctx, const nihu_gb_mesh *test, const nihu_gb_mesh *trial,
+                                           int family, int ops, double k, double k_im, double alpha_re,
+                                           double alpha_im, int precision, int dtype, void *out_slp, void *out_dlp,
+                                           int64_t ld, int accumulate, int where);
+
 /* out(i, i) += alpha * area_i: the Galerkin identity operator of constant
  * elements (test_space * I[trial_space], nihu/core/single_integral.hpp:97-140). */
 nihu_gb_status nihu_gb_add_mass(nihu_gb_ctx *ctx, const nihu_gb_mesh *mesh, double alpha_re, double alpha_im,

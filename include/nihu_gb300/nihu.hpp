@@ -327,10 +327,10 @@ Res &operator<<(Res &result, weighted_residual<TS> const &wr)
         void *out_s = kop == NIHU_GB_SLP ? (void *)result.data() : nullptr;
         void *out_d = kop == NIHU_GB_DLP ? (void *)result.data() : nullptr;
         if (op.kernel.k_im != 0.0) {
-            if (galerkin) throw std::invalid_argument("complex wave numbers: collocation operators only");
-            check(ctx.handle(), nihu_gb_assemble_c(ctx.handle(), tmh, rmh, op.kernel.family, kop, op.kernel.k,
-                                                   op.kernel.k_im, op.scale.real(), op.scale.imag(), wr.precision,
-                                                   detail::storage<T>::dtype, out_s, out_d, m, 1, NIHU_GB_HOST));
+            auto fn = galerkin ? nihu_gb_assemble_galerkin_c : nihu_gb_assemble_c;
+            check(ctx.handle(), fn(ctx.handle(), tmh, rmh, op.kernel.family, kop, op.kernel.k, op.kernel.k_im,
+                                   op.scale.real(), op.scale.imag(), wr.precision, detail::storage<T>::dtype, out_s,
+                                   out_d, m, 1, NIHU_GB_HOST));
         } else {
             auto fn = galerkin ? nihu_gb_assemble_galerkin : nihu_gb_assemble;
             check(ctx.handle(), fn(ctx.handle(), tmh, rmh, op.kernel.family, kop, op.kernel.k, op.scale.real(),

@@ -77,6 +77,7 @@ SIGNATURES = {
     "nihu_gb_solve_cbie": (_i, [_vp, _vp, _i, _d, _i, _i, _vp, _vp, _i, _i, _i, _d, _ip, _dp]),
     "nihu_gb_solve_cbie_c": (_i, [_vp, _vp, _i, _d, _d, _i, _i, _vp, _vp, _i, _i, _i, _d, _ip, _dp]),
     "nihu_gb_assemble_galerkin": (_i, [_vp, _vp, _vp, _i, _i, _d, _d, _d, _i, _i, _vp, _vp, _i64, _i, _i]),
+    "nihu_gb_assemble_galerkin_c": (_i, [_vp, _vp, _vp, _i, _i, _d, _d, _d, _d, _i, _i, _vp, _vp, _i64, _i, _i]),
     "nihu_gb_add_mass": (_i, [_vp, _vp, _d, _d, _i, _vp, _i64, _i]),
     "nihu_gb_assemble_bm": (_i, [_vp, _vp, _vp, _i, _i, _d, _d, _d, _i, _i, _vp, _vp, _i64, _i, _i]),
     "nihu_gb_assemble_burton_miller": (_i, [_vp, _vp, _i, _d, _d, _d, _i, _i, _vp, _vp, _i64, _i]),

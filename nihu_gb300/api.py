@@ -364,13 +364,11 @@ def _assemble_into(ctx, result, test_mesh, trial_mesh, family, op, k, alpha, pre
         out_s = buf.ctypes.data if op == C.SLP else None
         out_d = buf.ctypes.data if op == C.DLP else None
         kc = complex(k)
-        if kc.imag != 0 and not galerkin:
-            ctx.check(L.nihu_gb_assemble_c(ctx.handle, tdm.handle, rdm_handle, family, op, kc.real, kc.imag,
-                                           alpha.real, alpha.imag, prec, dtype, out_s, out_d,
-                                           max(result.shape[0], 1), accumulate, C.HOST))
+        if kc.imag != 0:
+            fn = L.nihu_gb_assemble_galerkin_c if galerkin else L.nihu_gb_assemble_c
+            ctx.check(fn(ctx.handle, tdm.handle, rdm_handle, family, op, kc.real, kc.imag, alpha.real, alpha.imag,
+                         prec, dtype, out_s, out_d, max(result.shape[0], 1), accumulate, C.HOST))
         else:
-            if kc.imag != 0:
-                raise NotImplementedError("complex wave numbers: collocation operators only")
             fn = L.nihu_gb_assemble_galerkin if galerkin else L.nihu_gb_assemble
             ctx.check(fn(ctx.handle, tdm.handle, rdm_handle, family, op, kc.real, alpha.real, alpha.imag, prec,
                          dtype, out_s, out_d, max(result.shape[0], 1), accumulate, C.HOST))

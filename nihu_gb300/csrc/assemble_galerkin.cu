@@ -304,8 +304,9 @@ __device__ __forceinline__ int common_nodes(int4 a, int na, int4 b, int nb, int 
     return num;
 }
 
-// PLAIN: unit scale and no accumulation (FP32): stores without run-time checks
-template <typename R, typename Out, int FAM, int OPS, bool PLAIN = false>
+// PLAIN: unit scale and no accumulation (FP32): stores without run-time checks;
+// CK: a complex (lossy) wave number (eval_point_ck)
+template <typename R, typename Out, int FAM, int OPS, bool PLAIN = false, bool CK = false>
 __global__ void __launch_bounds__(GAL_THREADS) k_galerkin_regular(GalArgs a)
 {
     __shared__ float4 s_hi[GAL_COLS], s_lo[GAL_COLS], s_p0[GAL_COLS];
@@ -334,9 +335,10 @@ __global__ void __launch_bounds__(GAL_THREADS) k_galerkin_regular(GalArgs a)
     const int4 inid = test.nid[ii];
     const int inc = test.nc[ii];
     const float area_i = test.p0[ii].x;  // w J of the one-point rule: the element's area
-    R k, are, aim, x0, x1, x2;
+    R k, ki, are, aim, x0, x1, x2;
     if constexpr (sizeof(R) == 4) {
         k = a.k32;
+        ki = a.k_im32;
         are = a.alpha_re32;
         aim = a.alpha_im32;
         x0 = ih.x + il.x;
@@ -344,6 +346,7 @@ __global__ void __launch_bounds__(GAL_THREADS) k_galerkin_regular(GalArgs a)
         x2 = ih.z + il.z;
     } else {
         k = a.k;
+        ki = a.k_im;
         are = a.alpha_re;
         aim = a.alpha_im;
         x0 = test.center[3 * (int64_t)ii];
@@ -377,8 +380,12 @@ __global__ void __launch_bounds__(GAL_THREADS) k_galerkin_regular(GalArgs a)
             const float q = (fx * fx + fy * fy + fz * fz) * h.w;
             if (__all_sync(0xffffffffu, q > 249.64f * (1.0f + 1e-4f) && shared == 0)) {
                 const float4 p = s_p0[c];
-                eval_point<FAM, float>(fx, fy, fz, p.x, p.y, p.z, p.w, k, DO_S ? area_i : 0.0f, DO_D ? area_i : 0.0f,
-                                       sr, si, dr, di);
+                if constexpr (CK)
+                    eval_point_ck<float>(fx, fy, fz, p.x, p.y, p.z, p.w, k, ki, DO_S ? area_i : 0.0f,
+                                         DO_D ? area_i : 0.0f, sr, si, dr, di);
+                else
+                    eval_point<FAM, float>(fx, fy, fz, p.x, p.y, p.z, p.w, k, DO_S ? area_i : 0.0f,
+                                           DO_D ? area_i : 0.0f, sr, si, dr, di);
                 done = true;
             }
         }
@@ -428,12 +435,20 @@ __global__ void __launch_bounds__(GAL_THREADS) k_galerkin_regular(GalArgs a)
                             const float4 n = __ldg(trial.pts32 + 2 * (bj + sq) + 1);
                             // r = (c_j - c_i) + (y - c_j) - (x_p - c_i): the hi/lo centre
                             // difference and the points' offsets from their centres
-                            eval_point<FAM, float>(dx + (y.x - xp0), dy + (y.y - xp1), dz + (y.z - xp2), y.w, n.x, n.y,
-                                                   n.z, k, ws * wp, wd * wp, sr, si, dr, di);
+                            if constexpr (CK)
+                                eval_point_ck<float>(dx + (y.x - xp0), dy + (y.y - xp1), dz + (y.z - xp2), y.w, n.x,
+                                                     n.y, n.z, k, ki, ws * wp, wd * wp, sr, si, dr, di);
+                            else
+                                eval_point<FAM, float>(dx + (y.x - xp0), dy + (y.y - xp1), dz + (y.z - xp2), y.w, n.x,
+                                                       n.y, n.z, k, ws * wp, wd * wp, sr, si, dr, di);
                         } else {
                             const double *y = trial.pts64 + 8 * (bj + sq);
-                            eval_point<FAM, double>(y[0] - xp0, y[1] - xp1, y[2] - xp2, y[3], y[4], y[5], y[6], k,
-                                                    ws * wp, wd * wp, sr, si, dr, di);
+                            if constexpr (CK)
+                                eval_point_ck<double>(y[0] - xp0, y[1] - xp1, y[2] - xp2, y[3], y[4], y[5], y[6], k, ki,
+                                                      ws * wp, wd * wp, sr, si, dr, di);
+                            else
+                                eval_point<FAM, double>(y[0] - xp0, y[1] - xp1, y[2] - xp2, y[3], y[4], y[5], y[6], k,
+                                                        ws * wp, wd * wp, sr, si, dr, di);
                         }
                     }
                 }
@@ -516,7 +531,8 @@ __device__ __forceinline__ void quad_rotate(const int perm[4], double u, double 
 
 // The self pairs, the nearly singular list of columns [j0, j1) (extra = 0)
 // or the extra list (extra = 1): one warp per pair
-template <typename Out>
+// CK: a complex (lossy) wave number: the FP64 rules with the complex kernel in both modes
+template <typename Out, bool CK>
 __global__ void __launch_bounds__(GAL_WARPS * 32) k_galerkin_near(GalArgs a, NearList near, int extra)
 {
     const int lane = threadIdx.x & 31;
@@ -533,6 +549,12 @@ __global__ void __launch_bounds__(GAL_WARPS * 32) k_galerkin_near(GalArgs a, Nea
     const bool do_s = (a.ops & OP_SLP) != 0, do_d = (a.ops & OP_DLP) != 0;
     const int fam = a.family;
     const double k = a.k;
+    const cd kc{a.k, a.k_im};
+    // kernel values at one point pair: the real or the complex wave number
+    auto kp = [&](const double *x, const double *y, const double *n, double J, bool s_, bool d_, cd &ks, cd &kd) {
+        if constexpr (CK) kern_point(fam, kc, x, y, n, J, s_, d_, ks, kd);
+        else kern_point(fam, k, x, y, n, J, s_, d_, ks, kd);
+    };
     Out *out_s = reinterpret_cast<Out *>(a.out_s);
     Out *out_d = reinterpret_cast<Out *>(a.out_d);
     for (int64_t item = warp; item < total; item += nwarps) {
@@ -583,14 +605,14 @@ __global__ void __launch_bounds__(GAL_WARPS * 32) k_galerkin_near(GalArgs a, Nea
                 ex(re, u, v, y);
                 enormal(re, u, v, nr3);
                 cd ks{0, 0}, kd{0, 0};
-                kern_point(fam, k, x, y, nr3, norm3(nr3), do_s, do_d, ks, kd);
+                kp(x, y, nr3, norm3(nr3), do_s, do_d, ks, kd);
                 const double w = q[4] * norm3(nt3);
                 sr += ks.re * w;
                 si += ks.im * w;
                 dr += kd.re * w;
                 di += kd.im * w;
             }
-        } else if (match >= 0 && a.precision == 0) {
+        } else if (match >= 0 && a.precision == 0 && !CK) {
             // FP32 regular quadrature: the matched pair's rule in FP32 too.  Both
             // rotated triangles start at the common node P, so r_vec = y - x is
             // formed from P-relative edge vectors and the rule's FP64-formed
@@ -698,14 +720,14 @@ __global__ void __launch_bounds__(GAL_WARPS * 32) k_galerkin_near(GalArgs a, Nea
                 tri_rotate(pr, q[2], q[3], u, v);
                 for (int d = 0; d < 3; ++d) y[d] = re.c[0][d] + u * r1[d] + v * r2[d];
                 cd ks{0, 0}, kd{0, 0};
-                kern_point(fam, k, x, y, nr, Jr, do_s, do_d, ks, kd);
+                kp(x, y, nr, Jr, do_s, do_d, ks, kd);
                 const double w = q[4] * Jt;
                 sr += ks.re * w;
                 si += ks.im * w;
                 dr += kd.re * w;
                 di += kd.im * w;
             }
-        } else if (a.precision == 0 && te.nc == 3 && re.nc == 3) {
+        } else if (a.precision == 0 && te.nc == 3 && re.nc == 3 && !CK) {
             // unmatched close triangles under FP32 regular quadrature: the same
             // product rules in FP32, points relative to the element centres
             // (r_vec = (c_j - c_i) + (y - c_j) - (x - c_i), the first term
@@ -807,7 +829,7 @@ __global__ void __launch_bounds__(GAL_WARPS * 32) k_galerkin_near(GalArgs a, Nea
                     ex(re, xr, er, y);
                     enormal(re, xr, er, n);
                     cd ks{0, 0}, kd{0, 0};
-                    kern_point(fam, k, x, y, n, norm3(n), use_s, use_d, ks, kd);
+                    kp(x, y, n, norm3(n), use_s, use_d, ks, kd);
                     const double w = wt * norm3(nx) * wr;
                     if (use_s) {
                         sr += ks.re * w;
@@ -835,6 +857,14 @@ __global__ void __launch_bounds__(GAL_WARPS * 32) k_galerkin_near(GalArgs a, Nea
 template <typename R, typename Out, int FAM>
 static void launch_gal_ops(const GalArgs &a, dim3 grid, cudaStream_t s)
 {
+    if constexpr (FAM == FAM_HELMHOLTZ) {
+        if (a.k_im != 0.0) {  // complex (lossy) wave number: separate instantiations
+            if (a.ops == OP_SLP) k_galerkin_regular<R, Out, FAM, OP_SLP, false, true><<<grid, GAL_THREADS, 0, s>>>(a);
+            else if (a.ops == OP_DLP) k_galerkin_regular<R, Out, FAM, OP_DLP, false, true><<<grid, GAL_THREADS, 0, s>>>(a);
+            else k_galerkin_regular<R, Out, FAM, OP_SLP | OP_DLP, false, true><<<grid, GAL_THREADS, 0, s>>>(a);
+            return;
+        }
+    }
     if constexpr (sizeof(R) == 4) {
         if (a.alpha_re == 1.0 && a.alpha_im == 0.0 && !a.accumulate) {
             if (a.ops == OP_SLP) k_galerkin_regular<R, Out, FAM, OP_SLP, true><<<grid, GAL_THREADS, 0, s>>>(a);
@@ -880,8 +910,13 @@ cudaError_t launch_galerkin_near(const GalArgs &a, const NearList &near, int ext
     // must leave it most of the register file
     const int64_t want = (max_items + GAL_WARPS - 1) / GAL_WARPS;
     const int blocks = (int)std::max<int64_t>(1, std::min<int64_t>(want, 2 * (int64_t)sms));
-    if (a.dtype == 0) k_galerkin_near<float2><<<blocks, GAL_WARPS * 32, 0, s>>>(a, near, extra);
-    else k_galerkin_near<double2><<<blocks, GAL_WARPS * 32, 0, s>>>(a, near, extra);
+    if (a.family == FAM_HELMHOLTZ && a.k_im != 0.0) {
+        if (a.dtype == 0) k_galerkin_near<float2, true><<<blocks, GAL_WARPS * 32, 0, s>>>(a, near, extra);
+        else k_galerkin_near<double2, true><<<blocks, GAL_WARPS * 32, 0, s>>>(a, near, extra);
+    } else {
+        if (a.dtype == 0) k_galerkin_near<float2, false><<<blocks, GAL_WARPS * 32, 0, s>>>(a, near, extra);
+        else k_galerkin_near<double2, false><<<blocks, GAL_WARPS * 32, 0, s>>>(a, near, extra);
+    }
     return cudaGetLastError();
 }
 

@@ -1040,8 +1040,18 @@ nihu_gb_status nihu_gb_assemble_galerkin(nihu_gb_ctx *ctx, const nihu_gb_mesh *t
                                          int family, int ops, double k, double alpha_re, double alpha_im, int precision,
                                          int dtype, void *out_slp, void *out_dlp, int64_t ld, int accumulate, int where)
 {
+    return nihu_gb_assemble_galerkin_c(ctx, test, trial, family, ops, k, 0.0, alpha_re, alpha_im, precision, dtype,
+                                       out_slp, out_dlp, ld, accumulate, where);
+}
+
+nihu_gb_status nihu_gb_assemble_galerkin_c(nihu_gb_ctx *ctx, const nihu_gb_mesh *test, const nihu_gb_mesh *trial,
+                                           int family, int ops, double k, double k_im, double alpha_re,
+                                           double alpha_im, int precision, int dtype, void *out_slp, void *out_dlp,
+                                           int64_t ld, int accumulate, int where)
+{
     if (!ctx) return NIHU_GB_ERR_INVALID_ARGUMENT;
     const std::string fn = "nihu_gb_assemble_galerkin";
+    if (!std::isfinite(k_im)) return fail(ctx, NIHU_GB_ERR_INVALID_ARGUMENT, fn + ": non-finite wave number");
     if (!test || !trial || test->ctx != ctx || trial->ctx != ctx)
         return fail(ctx, NIHU_GB_ERR_INVALID_ARGUMENT, fn + ": meshes must belong to the context");
     if (family != NIHU_GB_HELMHOLTZ_3D && family != NIHU_GB_LAPLACE_3D)
@@ -1072,6 +1082,8 @@ nihu_gb_status nihu_gb_assemble_galerkin(nihu_gb_ctx *ctx, const nihu_gb_mesh *t
     g.ops = ops;
     g.k = family == NIHU_GB_HELMHOLTZ_3D ? k : 0.0;
     g.k32 = (float)g.k;
+    g.k_im = family == NIHU_GB_HELMHOLTZ_3D ? k_im : 0.0;
+    g.k_im32 = (float)g.k_im;
     g.alpha_re = alpha_re;
     g.alpha_im = alpha_im;
     g.alpha_re32 = (float)alpha_re;

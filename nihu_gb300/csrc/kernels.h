@@ -194,6 +194,8 @@ struct GalArgs {
     int family = 0, ops = 0;
     double k = 0.0;
     float k32 = 0.0f;
+    double k_im = 0.0;  // imaginary part of a complex (lossy) wave number
+    float k_im32 = 0.0f;
     double alpha_re = 1.0, alpha_im = 0.0;
     float alpha_re32 = 1.0f, alpha_im32 = 0.0f;
     int precision = 0, dtype = 0;

@@ -375,7 +375,7 @@ def test_pulsating_sphere_complex_wave_number(gpu_ctx, oracle, k):
 
 
 def test_complex_wave_number_through_the_operator_algebra(gpu_ctx, oracle):
-    """helmholtz_3d_SLP_kernel(k) with a complex k in the NiHu-shaped front end."""
+    """helmholtz_3d_SLP_kernel(k) with a complex k in the NiHu-shaped front end, collocation and Galerkin."""
     nodes, elems = get_mesh("ico2")
     mesh = g.create_mesh(nodes, elems)
     sp = g.constant_view(mesh)
@@ -384,6 +384,8 @@ def test_complex_wave_number_through_the_operator_algebra(gpu_ctx, oracle):
     Ls = np.zeros((n, n), np.complex128, order="F")
     Ls << g.dirac(sp) * g.create_integral_operator(g.helmholtz_3d_SLP_kernel(k))[sp]
     assert rel_norm(Ls, oracle_matrix(oracle, "ico2", g.HELMHOLTZ_3D, g.SLP, k)) < 1e-5
-    with pytest.raises(NotImplementedError):
-        Gs = np.zeros((n, n), np.complex128)
-        (sp * g.create_integral_operator(g.helmholtz_3d_SLP_kernel(k))[sp]).eval_into(Gs, ctx=gpu_ctx)
+    # the Galerkin formalism (test space * operator[trial space]) with the same k
+    Gs = np.zeros((n, n), np.complex128)
+    (sp * g.create_integral_operator(g.helmholtz_3d_SLP_kernel(k))[sp]).eval_into(Gs, precision="fp64", ctx=gpu_ctx)
+    ref = oracle.assemble_galerkin((nodes, elems), (nodes, elems), g.HELMHOLTZ_3D, g.SLP, k, same_mesh=True, threads=8)
+    assert rel_norm(Gs, ref) < 1e-11

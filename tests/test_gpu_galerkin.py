@@ -68,10 +68,11 @@ def gpu_galerkin(ctx, mesh, family, ops, k, precision, dtype, alpha=1.0, test_me
     cdt = np.complex64 if dtype == g.C64 else np.complex128
     outs = {op: np.zeros((test.n, trial.n), cdt, order="F") for op in (g.SLP, g.DLP) if ops & op}
     alpha = complex(alpha)
-    ctx.check(L.nihu_gb_assemble_galerkin(ctx.handle, test.handle, trial.handle, family, ops, k, alpha.real,
-                                          alpha.imag, precision, dtype,
-                                          outs[g.SLP].ctypes.data if g.SLP in outs else None,
-                                          outs[g.DLP].ctypes.data if g.DLP in outs else None, test.n, 0, g.HOST))
+    kc = complex(k)
+    ctx.check(L.nihu_gb_assemble_galerkin_c(ctx.handle, test.handle, trial.handle, family, ops, kc.real, kc.imag,
+                                            alpha.real, alpha.imag, precision, dtype,
+                                            outs[g.SLP].ctypes.data if g.SLP in outs else None,
+                                            outs[g.DLP].ctypes.data if g.DLP in outs else None, test.n, 0, g.HOST))
     return outs
 
 
@@ -83,6 +84,20 @@ def test_galerkin_against_oracle(gpu_ctx, oracle, name, family, k, precision, to
                         g.C128 if precision == g.REGULAR_FP64 else g.C64)
     for op, oop in ((g.SLP, oracle.SLP), (g.DLP, oracle.DLP)):
         ref = oracle_g(oracle, name, family, oop, k)
+        err = rel_norm(outs[op].astype(np.complex128), ref)
+        assert err <= tol, (name, op, err)
+
+
+@pytest.mark.parametrize("name,k", [("ico2", 2.0 - 0.3j), ("two", 1.3 - 0.2j), ("fan", 4.0 - 0.5j),
+                                    ("cube", 2.0 + 0.1j)])
+@pytest.mark.parametrize("precision,tol", [(g.REGULAR_FP64, 1e-11), (g.REGULAR_FP32, 1e-5)])
+def test_complex_wave_number_against_oracle(gpu_ctx, oracle, name, k, precision, tol):
+    """Galerkin SLP and DLP with a complex (lossy) wave number
+    (nihu_gb_assemble_galerkin_c): triangle and quad meshes, all match types."""
+    outs = gpu_galerkin(gpu_ctx, get_mesh(name), g.HELMHOLTZ_3D, g.SLP | g.DLP, k, precision,
+                        g.C128 if precision == g.REGULAR_FP64 else g.C64)
+    for op, oop in ((g.SLP, oracle.SLP), (g.DLP, oracle.DLP)):
+        ref = oracle_g(oracle, name, g.HELMHOLTZ_3D, oop, k)
         err = rel_norm(outs[op].astype(np.complex128), ref)
         assert err <= tol, (name, op, err)
 
