@@ -635,71 +635,78 @@ __global__ void __launch_bounds__(REG2_THREADS, 4) k_regular2(RegularArgs a)
     const int r0 = ok0 ? i0 : test.n - 1, r1 = ok1 ? i0 + 1 : test.n - 1;
     const float4 ih0 = test.chi[r0], il0 = test.clo[r0], ih1 = test.chi[r1], il1 = test.clo[r1];
     const unsigned lt = (1u << lane) - 1u;
-    float2 *ps = out_s + i0, *pd = out_d + i0;
-    for (int c0 = 0; c0 < ncols; c0 += REG2_CHUNK) {
-        const int c1 = min(ncols, c0 + REG2_CHUNK);
-        int nA = 0, nB = 0;  // warp-uniform list lengths
-        for (int c = c0; c < c1; ++c, ps += ldo, pd += ldo) {
-            const float4 h = s_hi[c], l = s_lo[c];
-            // hi/lo centre differences of both rows (FP32 relative accuracy of r)
-            const float ax = (h.x - ih0.x) + (l.x - il0.x), ay = (h.y - ih0.y) + (l.y - il0.y),
-                        az = (h.z - ih0.z) + (l.z - il0.z);
-            const float bx = (h.x - ih1.x) + (l.x - il1.x), by = (h.y - ih1.y) + (l.y - il1.y),
-                        bz = (h.z - ih1.z) + (l.z - il1.z);
-            const float qa = (ax * ax + ay * ay + az * az) * h.w;
-            const float qb = (bx * bx + by * by + bz * bz) * h.w;
-            const bool fa = qa > Q_FAR, fb = qb > Q_FAR;
-            const float4 p = s_p0[c];
-            if (__all_sync(0xffffffffu, fa && fb)) {
-                // far: the centroid for both operators, both rows
-                float sr0, si0, dr0, di0, sr1, si1, dr1, di1;
-                far_point<FAM>(ax, ay, az, p.x, p.y, p.z, p.w, k, sr0, si0, dr0, di0);
-                far_point<FAM>(bx, by, bz, p.x, p.y, p.z, p.w, k, sr1, si1, dr1, di1);
-                if (ok1) {
-                    *reinterpret_cast<float4 *>(ps) = make_float4(sr0, si0, sr1, si1);
-                    *reinterpret_cast<float4 *>(pd) = make_float4(dr0, di0, dr1, di1);
-                } else if (ok0) {
-                    *ps = make_float2(sr0, si0);
-                    *pd = make_float2(dr0, di0);
+    // FULL: every row of the block exists (all blocks but the last row
+    // block): the row checks drop out of the column loop
+    auto columns = [&](auto full_tag) {
+        constexpr bool FULL = decltype(full_tag)::value;
+        float2 *ps = out_s + i0, *pd = out_d + i0;
+        for (int c0 = 0; c0 < ncols; c0 += REG2_CHUNK) {
+            const int c1 = min(ncols, c0 + REG2_CHUNK);
+            int nA = 0, nB = 0;  // warp-uniform list lengths
+            for (int c = c0; c < c1; ++c, ps += ldo, pd += ldo) {
+                const float4 h = s_hi[c], l = s_lo[c];
+                // hi/lo centre differences of both rows (FP32 relative accuracy of r)
+                const float ax = (h.x - ih0.x) + (l.x - il0.x), ay = (h.y - ih0.y) + (l.y - il0.y),
+                            az = (h.z - ih0.z) + (l.z - il0.z);
+                const float bx = (h.x - ih1.x) + (l.x - il1.x), by = (h.y - ih1.y) + (l.y - il1.y),
+                            bz = (h.z - ih1.z) + (l.z - il1.z);
+                const float qa = (ax * ax + ay * ay + az * az) * h.w;
+                const float qb = (bx * bx + by * by + bz * bz) * h.w;
+                const bool fa = qa > Q_FAR, fb = qb > Q_FAR;
+                const float4 p = s_p0[c];
+                if (__all_sync(0xffffffffu, fa && fb)) {
+                    // far: the centroid for both operators, both rows
+                    float sr0, si0, dr0, di0, sr1, si1, dr1, di1;
+                    far_point<FAM>(ax, ay, az, p.x, p.y, p.z, p.w, k, sr0, si0, dr0, di0);
+                    far_point<FAM>(bx, by, bz, p.x, p.y, p.z, p.w, k, sr1, si1, dr1, di1);
+                    if (FULL || ok1) {
+                        *reinterpret_cast<float4 *>(ps) = make_float4(sr0, si0, sr1, si1);
+                        *reinterpret_cast<float4 *>(pd) = make_float4(dr0, di0, dr1, di1);
+                    } else if (ok0) {
+                        *ps = make_float2(sr0, si0);
+                        *pd = make_float2(dr0, di0);
+                    }
+                    continue;
                 }
-                continue;
+                // far rows here; the others deferred to the warp's lists
+                if (fa && (FULL || ok0)) {
+                    float sr, si, dr, di;
+                    far_point<FAM>(ax, ay, az, p.x, p.y, p.z, p.w, k, sr, si, dr, di);
+                    ps[0] = make_float2(sr, si);
+                    pd[0] = make_float2(dr, di);
+                }
+                if (fb && (FULL || ok1)) {
+                    float sr, si, dr, di;
+                    far_point<FAM>(bx, by, bz, p.x, p.y, p.z, p.w, k, sr, si, dr, di);
+                    ps[1] = make_float2(sr, si);
+                    pd[1] = make_float2(dr, di);
+                }
+                // the FP32 guard band of classify_pair: outside it the class is the FP64 class
+                const float alo = qa * (1.0f - 1e-5f), ahi = qa * (1.0f + 1e-5f);
+                const float blo = qb * (1.0f - 1e-5f), bhi = qb * (1.0f + 1e-5f);
+                const bool da = (FULL || ok0) && !fa && ahi >= 2.25f, db = (FULL || ok1) && !fb && bhi >= 2.25f;  // not certainly near
+                const bool ca = da && alo >= 82.81f && ahi < 249.64f, cb = db && blo >= 82.81f && bhi < 249.64f;
+                const unsigned mA0 = __ballot_sync(0xffffffffu, ca), mA1 = __ballot_sync(0xffffffffu, cb);
+                const unsigned mB0 = __ballot_sync(0xffffffffu, da && !ca), mB1 = __ballot_sync(0xffffffffu, db && !cb);
+                const int nA0 = __popc(mA0), nB0 = __popc(mB0);
+                const unsigned short code0 = (unsigned short)((i0 - ib) | (c << 9));
+                const unsigned short code1 = (unsigned short)((i0 + 1 - ib) | (c << 9));
+                if (ca) wl[nA + __popc(mA0 & lt)] = code0;
+                if (cb) wl[nA + nA0 + __popc(mA1 & lt)] = code1;
+                if (da && !ca) wl[REG2_WLIST - 1 - (nB + __popc(mB0 & lt))] = code0;
+                if (db && !cb) wl[REG2_WLIST - 1 - (nB + nB0 + __popc(mB1 & lt))] = code1;
+                nA += nA0 + __popc(mA1);
+                nB += nB0 + __popc(mB1);
             }
-            // far rows here; the others deferred to the warp's lists
-            if (fa && ok0) {
-                float sr, si, dr, di;
-                far_point<FAM>(ax, ay, az, p.x, p.y, p.z, p.w, k, sr, si, dr, di);
-                ps[0] = make_float2(sr, si);
-                pd[0] = make_float2(dr, di);
+            if (nA + nB) {  // warp-uniform
+                __syncwarp();  // the list entries are visible to the whole warp
+                regular2_flush<FAM>(a, wl, nA, nB, lane, ib, jb, s_hi, s_lo, s_nc, out_s, out_d, ldo, k);
+                __syncwarp();  // read before the next chunk appends
             }
-            if (fb && ok1) {
-                float sr, si, dr, di;
-                far_point<FAM>(bx, by, bz, p.x, p.y, p.z, p.w, k, sr, si, dr, di);
-                ps[1] = make_float2(sr, si);
-                pd[1] = make_float2(dr, di);
-            }
-            // the FP32 guard band of classify_pair: outside it the class is the FP64 class
-            const float alo = qa * (1.0f - 1e-5f), ahi = qa * (1.0f + 1e-5f);
-            const float blo = qb * (1.0f - 1e-5f), bhi = qb * (1.0f + 1e-5f);
-            const bool da = ok0 && !fa && ahi >= 2.25f, db = ok1 && !fb && bhi >= 2.25f;  // not certainly near
-            const bool ca = da && alo >= 82.81f && ahi < 249.64f, cb = db && blo >= 82.81f && bhi < 249.64f;
-            const unsigned mA0 = __ballot_sync(0xffffffffu, ca), mA1 = __ballot_sync(0xffffffffu, cb);
-            const unsigned mB0 = __ballot_sync(0xffffffffu, da && !ca), mB1 = __ballot_sync(0xffffffffu, db && !cb);
-            const int nA0 = __popc(mA0), nB0 = __popc(mB0);
-            const unsigned short code0 = (unsigned short)((i0 - ib) | (c << 9));
-            const unsigned short code1 = (unsigned short)((i0 + 1 - ib) | (c << 9));
-            if (ca) wl[nA + __popc(mA0 & lt)] = code0;
-            if (cb) wl[nA + nA0 + __popc(mA1 & lt)] = code1;
-            if (da && !ca) wl[REG2_WLIST - 1 - (nB + __popc(mB0 & lt))] = code0;
-            if (db && !cb) wl[REG2_WLIST - 1 - (nB + nB0 + __popc(mB1 & lt))] = code1;
-            nA += nA0 + __popc(mA1);
-            nB += nB0 + __popc(mB1);
         }
-        if (nA + nB) {  // warp-uniform
-            __syncwarp();  // the list entries are visible to the whole warp
-            regular2_flush<FAM>(a, wl, nA, nB, lane, ib, jb, s_hi, s_lo, s_nc, out_s, out_d, ldo, k);
-            __syncwarp();  // read before the next chunk appends
-        }
-    }
+    };
+    if (ib + REG2_ROWS <= test.n) columns(std::true_type{});
+    else columns(std::false_type{});
 }
 
 // partial sums of the same row added in FP32 before one FP64 addition
