@@ -179,9 +179,9 @@ nihu_gb_status nihu_gb_add_identity(nihu_gb_ctx *ctx, const nihu_gb_mesh *mesh, 
  * rules of their match type (4 Gauss points per direction of a 4D Duffy-type
  * split: 1536 / 1536 / 512 points on triangles, 2048 / 1536 / 1280 on quads);
  * all other pairs the product of the regular rule of degree C + interval(d/D)
- * on both elements.  One mesh holds triangles or quads, not both
- * (triangle-quad matches are not built: NIHU_GB_ERR_INVALID_ARGUMENT); a
- * separate test mesh may mix them.
+ * on both elements.  A mesh may mix triangles and quads: a triangle-quad
+ * match takes the triangle-triangle rules on the quad split into two
+ * triangles (singular_galerkin_quadrature.hpp:624-790).
  * Replaces: test_space * Op[trial_space] with a function-space test space
  * (nihu/core/double_integral.hpp:143-384, element_match.hpp:60-90,
  * singular_accelerator.hpp:142-330, singular_galerkin_quadrature.hpp:200-420),

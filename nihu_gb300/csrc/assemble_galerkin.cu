@@ -584,7 +584,51 @@ __global__ void __launch_bounds__(GAL_WARPS * 32) k_galerkin_near(GalArgs a, Nea
             }
         }
         double sr = 0, si = 0, dr = 0, di = 0;
-        if (match >= 0 && te.nc == 4) {
+        if (match >= 0 && te.nc != re.nc) {
+            // triangle-quad match, corner or edge (FP64 in both modes;
+            // nihu/core/singular_galerkin_quadrature.hpp:624-790): the quad's
+            // reference square split into the triangles (0, 1, 2) and (0, 2, 3)
+            // of its rotated corners, the triangle-triangle corner rule on both
+            // (corner match) or the edge rule on (0, 1, 2) and the corner rule on
+            // (0, 2, 3) (edge match); the rule's first triangle on the quad half
+            // by its linear map (Jacobian 4), its second on the triangle.  The
+            // rotations are those of the other pairs.
+            const int ntc = te.nc, nrc = re.nc;
+            int pt[4], pr[4];
+            for (int q = 0; q < ntc; ++q) pt[q] = (ind1 + q) % ntc;
+            for (int q = 0; q < nrc; ++q) pr[q] = match == 1 ? (ind2 + 1 + nrc - q) % nrc : (ind2 + q) % nrc;
+            const bool quad_test = ntc == 4;
+            const int m_first = match == 1 ? 1 : 0;
+            const int na = gal_npts(m_first), total_p = na + gal_npts(0);
+            for (int p = lane; p < total_p; p += 32) {
+                const int sub = p < na ? 0 : 1;
+                const double *q = g_gal_rule + 5 * (size_t)(sub == 0 ? gal_offset(m_first) + p : gal_offset(0) + p - na);
+                const double N0 = 1.0 - q[0] - q[1], N1 = q[0], N2 = q[1];
+                // half (0, 1, 2): (-1,-1), (1,-1), (1,1); half (0, 2, 3): (-1,-1), (1,1), (-1,1)
+                const double qu = sub == 0 ? -N0 + N1 + N2 : -N0 + N1 - N2;
+                const double qv = sub == 0 ? -N0 - N1 + N2 : -N0 + N1 + N2;
+                double tu, tv, ru, rv;
+                if (quad_test) {
+                    quad_rotate(pt, qu, qv, tu, tv);
+                    tri_rotate(pr, q[2], q[3], ru, rv);
+                } else {
+                    tri_rotate(pt, q[2], q[3], tu, tv);
+                    quad_rotate(pr, qu, qv, ru, rv);
+                }
+                double x[3], y[3], ntv[3], nrv[3];
+                ex(te, tu, tv, x);
+                enormal(te, tu, tv, ntv);
+                ex(re, ru, rv, y);
+                enormal(re, ru, rv, nrv);
+                cd ks{0, 0}, kd{0, 0};
+                kp(x, y, nrv, norm3(nrv), do_s, do_d, ks, kd);
+                const double w = 4.0 * q[4] * norm3(ntv);
+                sr += ks.re * w;
+                si += ks.im * w;
+                dr += kd.re * w;
+                di += kd.im * w;
+            }
+        } else if (match >= 0 && te.nc == 4) {
             // matched quads (FP64, both precisions): points by the bilinear
             // maps, Jacobians and normals per point
             int pt[4], pr[4];
@@ -693,7 +737,7 @@ __global__ void __launch_bounds__(GAL_WARPS * 32) k_galerkin_near(GalArgs a, Nea
             dr = do_d ? fdr : 0.0f;
             di = do_d ? fdi : 0.0f;
         } else if (match >= 0) {
-            // matched triangles (quads were refused by the host): flat elements
+            // matched triangles: flat elements
             int pt[3], pr[3];
 #pragma unroll
             for (int q = 0; q < 3; ++q) {

@@ -1065,9 +1065,6 @@ nihu_gb_status nihu_gb_assemble_galerkin_c(nihu_gb_ctx *ctx, const nihu_gb_mesh 
     if (!std::isfinite(k) || !std::isfinite(alpha_re) || !std::isfinite(alpha_im))
         return fail(ctx, NIHU_GB_ERR_INVALID_ARGUMENT, fn + ": non-finite wave number or scale");
     const bool same = test == trial;
-    if (same && test->dm.has_quad && test->dm.has_tria)
-        return fail(ctx, NIHU_GB_ERR_INVALID_ARGUMENT,
-                    fn + ": Galerkin singular quadrature: triangle-quad matches are not built (one mesh of both)");
     if (test->n == 0 || trial->n == 0) return NIHU_GB_OK;
     cudaSetDevice(ctx->device);
     NearList *nl = nullptr;

@@ -1300,6 +1300,59 @@ static cplx galerkin_singular_quad(const elem_t *te, const elem_t *re, int fam, 
     return sum;
 }
 
+/* singular Galerkin integral of a matched triangle-quad pair (corner or
+ * edge match; nihu/core/singular_galerkin_quadrature.hpp:624-790).  The
+ * reference square of the quad is split into the triangles (0, 1, 2) and
+ * (0, 2, 3) of its corners (-1,-1), (1,-1), (1,1), (-1,1); a corner match
+ * takes the triangle-triangle corner rule on both, an edge match the edge
+ * rule on (0, 1, 2) (which holds the common edge) and the corner rule on
+ * (0, 2, 3).  The rule's triangle points go onto the sub-triangle by its
+ * linear map (weights times its Jacobian, 4).  A triangle test element with
+ * a quad trial element takes the same rule with test and trial swapped
+ * (:767-790).  Rotations as for the other pairs
+ * (nihu/core/singular_accelerator.hpp:290-320). */
+static cplx galerkin_singular_mixed(const elem_t *te, const elem_t *re, int fam, int op, cplx k, int match,
+                                    int ind1, int ind2)
+{
+    static const double Q[4][2] = {{-1, -1}, {1, -1}, {1, 1}, {-1, 1}};
+    static const int SUB[2][3] = {{0, 1, 2}, {0, 2, 3}};
+    if (!g_gal_count[0]) gal_build(0);
+    if (!g_gal_count[1]) gal_build(1);
+    const int nt = te->nc, nr = re->nc;
+    int pt[4], pr[4];
+    for (int q = 0; q < nt; ++q) pt[q] = (ind1 + q) % nt;
+    for (int q = 0; q < nr; ++q) pr[q] = match == 1 ? (ind2 + 1 + nr - q) % nr : (ind2 + q) % nr;
+    const int quad_is_test = nt == 4;
+    cplx sum = 0.0;
+    for (int sub = 0; sub < 2; ++sub) {
+        const int m = (match == 1 && sub == 0) ? 1 : 0;  /* edge rule on (0, 1, 2) of an edge match */
+        for (int p = 0; p < g_gal_count[m]; ++p) {
+            const double *d = g_gal[m][p];
+            /* the rule's first triangle goes onto the quad's sub-triangle */
+            const double N[3] = {1.0 - d[0] - d[1], d[0], d[1]};
+            double qu = 0.0, qv = 0.0;
+            for (int c = 0; c < 3; ++c) { qu += N[c] * Q[SUB[sub][c]][0]; qv += N[c] * Q[SUB[sub][c]][1]; }
+            double tu, tv, ru, rv;
+            if (quad_is_test) {
+                quad_rotate(pt, qu, qv, &tu, &tv);
+                tri_rotate(pr, d[2], d[3], &ru, &rv);
+            } else {
+                tri_rotate(pt, d[2], d[3], &tu, &tv);
+                quad_rotate(pr, qu, qv, &ru, &rv);
+            }
+            double x[3], y[3], ntv[3], nrv[3];
+            elem_x(te, tu, tv, x);
+            elem_normal(te, tu, tv, ntv);
+            elem_x(re, ru, rv, y);
+            elem_normal(re, ru, rv, nrv);
+            const double Jt = norm3(ntv), Jr = norm3(nrv);
+            double un[3] = {nrv[0] / Jr, nrv[1] / Jr, nrv[2] / Jr};
+            sum += 4.0 * d[4] * Jt * kern(fam, op, k, x, NULL, y, un) * Jr;
+        }
+    }
+    return sum;
+}
+
 /* the quad rule of a match type for tests: count, then points */
 int oracle_galerkin_quad_rule(int match, double *out)
 {
@@ -1330,12 +1383,9 @@ static int galerkin_entry(const elem_t *te, const elem_t *re, const int *tn, con
         }
     }
     if (match >= 0) {
-        if (te->nc != re->nc) {
-            snprintf(g_err, sizeof g_err, "Galerkin singular quadrature: triangle-quad matches are not built");
-            return 0;
-        }
-        *out = te->nc == 3 ? galerkin_singular(te, re, fam, op, k, match, ind1, ind2)
-                           : galerkin_singular_quad(te, re, fam, op, k, match, ind1, ind2);
+        if (te->nc != re->nc) *out = galerkin_singular_mixed(te, re, fam, op, k, match, ind1, ind2);
+        else *out = te->nc == 3 ? galerkin_singular(te, re, fam, op, k, match, ind1, ind2)
+                                : galerkin_singular_quad(te, re, fam, op, k, match, ind1, ind2);
         return 1;
     }
     double ratio = centre_distance(te, re) / re->size;

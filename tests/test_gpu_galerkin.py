@@ -221,11 +221,36 @@ def test_pulsating_cube_sphere(gpu_ctx):
     assert np.abs(p - pa).max() / abs(pa) < 0.01
 
 
-def test_mixed_mesh_is_refused(gpu_ctx):
-    nodes = np.array([[0, 0, 0], [1, 0, 0], [1, 1, 0], [0, 1, 0], [0.5, -1, 0.2]], float)
-    elems = np.array([[g.QUAD_1, 0, 1, 2, 3], [TRIA, 1, 0, 4, -1]], np.int32)
-    with pytest.raises(g.InvalidArgumentError):
-        gpu_galerkin(gpu_ctx, (nodes, elems), g.HELMHOLTZ_3D, g.SLP, 1.0, g.REGULAR_FP64, g.C128)
+def mixed_cylinder():
+    """A closed quad cylinder with every third side quad split into two
+    triangles: triangle-quad corner and edge matches on one mesh."""
+    nodes, elems = meshes.cylinder(12, 6, 2, radius=1.0, length=3.0)
+    rows = []
+    for e, row in enumerate(elems):
+        if e < 12 * 6 and e % 3 == 0:
+            a, b, c, d = row[1:5]
+            rows.append([TRIA, a, b, c, -1])
+            rows.append([TRIA, a, c, d, -1])
+        else:
+            rows.append(list(row))
+    return nodes, np.array(rows, dtype=np.int32)
+
+
+@pytest.mark.parametrize("k", [1.3, 2.0 - 0.3j])
+@pytest.mark.parametrize("precision,tol", [(g.REGULAR_FP64, 1e-11), (g.REGULAR_FP32, 1e-5)])
+def test_mixed_triangle_quad_mesh(gpu_ctx, oracle, k, precision, tol):
+    """One mesh of triangles and quads: the triangle-quad corner and edge
+    matches (the triangle rules on the split quad) and every other class,
+    against the oracle."""
+    mesh = mixed_cylinder()
+    outs = gpu_galerkin(gpu_ctx, mesh, g.HELMHOLTZ_3D, g.SLP | g.DLP, k, precision,
+                        g.C128 if precision == g.REGULAR_FP64 else g.C64)
+    for op, oop in ((g.SLP, oracle.SLP), (g.DLP, oracle.DLP)):
+        key = ("mixed_cyl", g.HELMHOLTZ_3D, oop, k)
+        if key not in _ocache:
+            _ocache[key] = oracle.assemble_galerkin(mesh, mesh, g.HELMHOLTZ_3D, oop, k, threads=8)
+        err = rel_norm(outs[op].astype(np.complex128), _ocache[key])
+        assert err <= tol, (op, err)
 
 
 @pytest.mark.parametrize("family,k", [(g.HELMHOLTZ_3D, 5.0), (g.LAPLACE_3D, 0.0)])

@@ -148,11 +148,34 @@ def test_pulsating_sphere_galerkin():
     assert np.abs(L - L.T).max() <= 1e-5 * np.abs(L).max()
 
 
-def test_triangle_quad_matches_are_refused():
-    nodes = np.array([[0, 0, 0], [1, 0, 0], [1, 1, 0], [0, 1, 0], [0.5, -1, 0.2]], float)
-    elems = np.array([[QUAD_ID, 0, 1, 2, 3], [TRIA, 1, 0, 4, -1]], np.int32)
-    with pytest.raises(RuntimeError):
-        oracle.assemble_galerkin((nodes, elems), (nodes, elems), oracle.HELMHOLTZ, oracle.SLP, 1.0, same_mesh=True)
+@pytest.mark.parametrize("fam,k", [(oracle.HELMHOLTZ, 1.5), (oracle.LAPLACE, 0.0), (oracle.HELMHOLTZ, 2.0 - 0.3j)])
+@pytest.mark.parametrize("op", [oracle.SLP, oracle.DLP])
+def test_triangle_quad_matches_are_the_triangle_rules_on_the_split_quad(fam, k, op):
+    """Triangle-quad matches (nihu/core/singular_galerkin_quadrature.hpp:624-790):
+    the quad's reference square split into the triangles (0, 1, 2) and
+    (0, 2, 3) of its rotated corners, the triangle-triangle corner and edge
+    rules on them.  On a parallelogram (whose bilinear map is affine on each
+    half) an entry equals the sum of the triangle-triangle entries of the
+    mesh split along the same diagonal, to rounding: the quad's rotation
+    puts corner 0 on the first common node, so an edge match with a quad
+    trial element (whose rotation reverses the edge) splits along the other
+    diagonal than a quad test element.  A quad test element, a triangle
+    sharing its edge (P1, P0) and one sharing its corner P2."""
+    T = TRIA
+    P = np.array([[0, 0, 0], [1, 0, 0], [1.3, 0.9, 0], [0.3, 0.9, 0], [0.5, -0.8, 0.1], [2.0, 1.2, 0.2],
+                  [1.5, 1.8, -0.1]], float)
+    mixed = (P, np.array([[32404, 0, 1, 2, 3], [T, 1, 0, 4, -1], [T, 2, 5, 6, -1]], np.int32))
+    split02 = (P, np.array([[T, 0, 1, 2, -1], [T, 0, 2, 3, -1], [T, 1, 0, 4, -1], [T, 2, 5, 6, -1]], np.int32))
+    split13 = (P, np.array([[T, 0, 1, 3, -1], [T, 1, 2, 3, -1], [T, 1, 0, 4, -1], [T, 2, 5, 6, -1]], np.int32))
+    M = oracle.assemble_galerkin(mixed, mixed, fam, op, k, same_mesh=True)
+    A = oracle.assemble_galerkin(split02, split02, fam, op, k, same_mesh=True)
+    B = oracle.assemble_galerkin(split13, split13, fam, op, k, same_mesh=True)
+    pairs = [(M[0, 1], A[0, 2] + A[1, 2]),   # quad test, edge: rotated corner 0 = P0, diagonal P0-P2
+             (M[1, 0], B[2, 0] + B[2, 1]),   # quad trial, edge: the reversed edge puts P1 first, diagonal P1-P3
+             (M[0, 2], A[0, 3] + A[1, 3]),   # corner P2: diagonal P2-P0
+             (M[2, 0], A[3, 0] + A[3, 1])]
+    for got, ref in pairs:
+        assert abs(got - ref) <= 1e-12 * abs(ref), (got, ref)
 
 
 QUAD = 32404
