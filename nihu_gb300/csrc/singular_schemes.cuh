@@ -334,6 +334,8 @@ __device__ inline void near_dynamic_f32(const Elem64 &e, double k, const double 
     const float kf = (float)k;
     const float wj = (float)(J * INV_FOUR_PI);
     float sr = 0, si = 0, dr = 0, di = 0;
+    // six points in flight: one warp per scheduler leaves the loop latency-bound
+#pragma unroll 6
     for (int p = 0; p < 42; ++p) {
         const float xi = TRI14.p[p][0], eta = TRI14.p[p][1], w = TRI14.p[p][2];
         const float rv0 = b[0] + xi * f1[0] + eta * f2[0];
