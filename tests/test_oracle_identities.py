@@ -9,6 +9,11 @@ rules only (no discretisation error: the polyhedron is the surface).  The
 sums run over every pair class: regular (1-point to 6-point rules),
 nearly singular (semi-analytic static parts; polar schemes on quads) and
 self terms.
+
+The Laplace hypersingular operator annihilates constants (the double-layer
+potential of a constant density is piecewise constant, so its normal
+derivative vanishes): the collocational HSP rows sum to zero, which checks
+the finite-part self term against the nearly singular and regular schemes.
 """
 import numpy as np
 import pytest
@@ -50,3 +55,10 @@ def test_galerkin_dlp_rows_sum_to_minus_half_area(name):
     m = make()
     D = oracle.assemble_galerkin(m, m, oracle.LAPLACE, oracle.DLP, 0.0, threads=8)
     assert np.abs(D.real.sum(axis=1) / areas(m) + 0.5).max() < tol
+
+
+@pytest.mark.parametrize("name", ["ico2", "ico3"])
+def test_laplace_hsp_rows_sum_to_zero(name):
+    m = MESHES[name][0]()
+    H = oracle.assemble(m, m, oracle.LAPLACE, oracle.HSP, 0.0, threads=8)
+    assert np.abs(H.real.sum(axis=1)).max() < 1e-5 * np.abs(np.diag(H)).max()
